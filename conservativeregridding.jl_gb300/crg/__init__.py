@@ -1,0 +1,34 @@
+"""GB300-native conservative regridding (the build and apply hot paths of
+ConservativeRegridding.jl) over the C ABI of ``libcrg_gb300.so``."""
+from ._lib import ArgumentError, CrgError, DimensionMismatch
+from .grids import (
+    Grid,
+    cubed_sphere,
+    healpix_grid,
+    lonlat_grid,
+    lonlat_jittered,
+    lonlat_regular,
+    polygon_grid,
+    regular_grid,
+    unit_sphere_from_geographic,
+)
+from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
+
+__all__ = [
+    "ArgumentError",
+    "CrgError",
+    "DimensionMismatch",
+    "Grid",
+    "Regridder",
+    "cubed_sphere",
+    "healpix_grid",
+    "lonlat_grid",
+    "lonlat_jittered",
+    "lonlat_regular",
+    "polygon_grid",
+    "regrid",
+    "regrid_",
+    "regrid_adjoint_",
+    "regular_grid",
+    "unit_sphere_from_geographic",
+]

@@ -1,0 +1,134 @@
+"""ctypes binding of ``libcrg_gb300.so`` (declared in include/crg.h).
+
+The library is the only compute path: if it cannot be loaded the import of
+the functions below raises, there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import _build
+
+CRG_OK = 0
+CRG_ERR_INVALID_ARGUMENT = 1
+CRG_ERR_DIMENSION_MISMATCH = 2
+CRG_ERR_CUDA = 3
+CRG_ERR_OUT_OF_MEMORY = 4
+CRG_ERR_NOT_SUPPORTED = 5
+CRG_ERR_GEOMETRY = 6
+CRG_ERR_INTERNAL = 7
+
+CRG_PLANAR = 0
+CRG_SPHERICAL = 1
+CRG_GRID_CURVILINEAR = 0
+CRG_GRID_CELLS = 1
+CRG_F64 = 0
+CRG_F32 = 1
+CRG_BF16 = 2
+
+
+class crg_grid_desc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("manifold", C.c_int32),
+        ("nblocks", C.c_int32),
+        ("max_verts", C.c_int32),
+        ("ncells", C.c_int64),
+        ("block_nx", C.POINTER(C.c_int64)),
+        ("block_ny", C.POINTER(C.c_int64)),
+        ("points", C.c_void_p),
+        ("cell_verts", C.c_void_p),
+        ("cell_nverts", C.c_void_p),
+    ]
+
+
+class crg_build_opts(C.Structure):
+    _fields_ = [("normalize", C.c_int32), ("flags", C.c_int32), ("stream", C.c_void_p)]
+
+
+class crg_info(C.Structure):
+    _fields_ = [
+        ("n_dst", C.c_int64),
+        ("n_src", C.c_int64),
+        ("nnz", C.c_int64),
+        ("n_candidates", C.c_int64),
+        ("manifold", C.c_int32),
+        ("normalized", C.c_int32),
+        ("normalizer", C.c_double),
+        ("t_build_ms", C.c_double),
+        ("t_search_ms", C.c_double),
+        ("t_clip_ms", C.c_double),
+        ("t_assemble_ms", C.c_double),
+        ("clip_overflows", C.c_int64),
+        ("device", C.c_int32),
+        ("pad", C.c_int32),
+    ]
+
+
+# exported symbol -> (restype, argtypes)
+SIGNATURES = {
+    "crg_build": (C.c_int, [C.POINTER(crg_grid_desc), C.POINTER(crg_grid_desc), C.POINTER(crg_build_opts), C.POINTER(C.c_void_p)]),
+    "crg_regridder_retain": (C.c_int, [C.c_void_p]),
+    "crg_regridder_release": (C.c_int, [C.c_void_p]),
+    "crg_regridder_info": (C.c_int, [C.c_void_p, C.POINTER(crg_info)]),
+    "crg_apply": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
+                            C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p]),
+    "crg_apply_adjoint": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
+                                    C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p]),
+    "crg_get_csc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_get_csr": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_get_areas": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_get_row_col_sums": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_last_error": (C.c_char_p, []),
+    "crg_status_string": (C.c_char_p, [C.c_int]),
+    "crg_abi_version": (C.c_int32, []),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load (building first if stale) the CUDA library."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if build_if_missing:
+                _build.build()
+            if not _build.LIB_PATH.exists():
+                raise RuntimeError(f"{_build.LIB_PATH} is missing: the CUDA extension has not been built")
+            lib = C.CDLL(str(_build.LIB_PATH))
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+        return _lib
+
+
+class CrgError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(msg)
+        self.status = status
+
+
+class ArgumentError(ValueError):
+    """Counterpart of Julia's ArgumentError (src/regridder/regrid.jl:242-245)."""
+
+
+class DimensionMismatch(ValueError):
+    """Counterpart of Julia's DimensionMismatch (src/regridder/regrid.jl:289-296)."""
+
+
+def check(status: int) -> None:
+    if status == CRG_OK:
+        return
+    lib = load()
+    msg = lib.crg_last_error().decode(errors="replace")
+    what = lib.crg_status_string(status).decode()
+    if status == CRG_ERR_INVALID_ARGUMENT:
+        raise ArgumentError(msg)
+    if status == CRG_ERR_DIMENSION_MISMATCH:
+        raise DimensionMismatch(msg)
+    raise CrgError(status, f"{what}: {msg}")

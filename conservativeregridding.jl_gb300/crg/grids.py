@@ -1,0 +1,340 @@
+"""Grid descriptions handed to the regridder.
+
+ConservativeRegridding.jl turns its inputs into trees with ``Trees.treeify``
+(src/trees/interfaces.jl:94-129): vertex matrices become a
+``CellBasedGrid`` under a ``TopDownQuadtreeCursor`` (src/trees/grids.jl:57-85),
+lon-lat ocean grids are wrapped in ``KnownFullSphereExtentWrapper``
+(ext/ConservativeRegriddingOceananigansExt.jl:242-264), cubed spheres become a
+``CubedSphereToplevelTree`` of six index-offset quadtrees
+(ext/ConservativeRegriddingClimaCoreExt.jl:43-94) and HEALPix maps a 12-face
+nested tree whose cells are the pixel corner quadrilaterals
+(ext/ConservativeRegriddingHealpixExt.jl:76-90, :159-167).
+
+Here a :class:`Grid` carries the same information as plain arrays:
+
+* ``kind='curvilinear'``: one or more blocks of ``(nx+1) x (ny+1)`` points
+  (stored as arrays of shape ``(ny+1, nx+1, dim)``, so point ``(i, j)`` is
+  ``block[j, i]``); cell ``(i, j)`` of block ``b`` has the 0-based index
+  ``offset_b + i + j*nx`` and the ring ``p(i,j), p(i+1,j), p(i+1,j+1), p(i,j+1)``.
+* ``kind='cells'``: a ``(ncells, maxv, dim)`` table of ring vertices with an
+  optional vertex count per cell (HEALPix pixels, explicit polygons).
+
+The builders below generate the synthetic grids used by the tests and the
+benchmark: regular and shifted lon-lat grids, jittered lon-lat grids, the
+equiangular gnomonic cubed sphere and HEALPix.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Optional, Sequence
+
+import numpy as np
+
+SPHERICAL = "spherical"
+PLANAR = "planar"
+
+
+# ----------------------------------------------------------------- coordinates
+
+def sincosd(x):
+    """sin and cos of angles in degrees, exact at multiples of 90 degrees.
+
+    The reference converts geographic points with GeometryOps'
+    ``UnitSphereFromGeographic`` (src/trees/grids.jl:195,246); degree-exact
+    trigonometry makes the pole vertices of lon-lat grids coincide exactly.
+    """
+    x = np.asarray(x, dtype=np.float64)
+    r = np.remainder(x, 360.0)
+    q = np.round(r / 90.0)
+    d = np.deg2rad(r - 90.0 * q)
+    s, c = np.sin(d), np.cos(d)
+    q = q.astype(np.int64) % 4
+    sin = np.select([q == 0, q == 1, q == 2, q == 3], [s, c, -s, -c])
+    cos = np.select([q == 0, q == 1, q == 2, q == 3], [c, -s, -c, s])
+    return sin, cos
+
+
+def unit_sphere_from_geographic(lon, lat):
+    """(lon, lat) in degrees -> unit vectors of shape (..., 3)."""
+    slon, clon = sincosd(lon)
+    slat, clat = sincosd(lat)
+    return np.stack([clat * clon, clat * slon, slat], axis=-1)
+
+
+# ----------------------------------------------------------------- grid type
+
+@dataclasses.dataclass
+class Grid:
+    kind: str                       # 'curvilinear' | 'cells'
+    manifold: str                   # 'spherical' | 'planar'
+    blocks: Optional[list] = None   # curvilinear: list of (ny+1, nx+1, dim) arrays
+    cells: Optional[np.ndarray] = None   # cells: (ncells, maxv, dim)
+    nverts: Optional[np.ndarray] = None  # cells: (ncells,) int32 or None
+    full_sphere: bool = False       # root extent is the whole sphere (KnownFullSphereExtentWrapper)
+    healpix: Optional[tuple] = None  # (nside, nested) for HEALPix grids
+    name: str = ""
+
+    def __post_init__(self):
+        if self.kind == "curvilinear":
+            self.blocks = [np.ascontiguousarray(b, dtype=np.float64) for b in self.blocks]
+        else:
+            self.cells = np.ascontiguousarray(self.cells, dtype=np.float64)
+            if self.nverts is not None:
+                self.nverts = np.ascontiguousarray(self.nverts, dtype=np.int32)
+
+    @property
+    def dim(self) -> int:
+        return 3 if self.manifold == SPHERICAL else 2
+
+    @property
+    def ncells(self) -> int:
+        if self.kind == "curvilinear":
+            return int(sum((b.shape[0] - 1) * (b.shape[1] - 1) for b in self.blocks))
+        return int(self.cells.shape[0])
+
+    @property
+    def block_shapes(self):
+        """[(nx, ny)] per block."""
+        return [(b.shape[1] - 1, b.shape[0] - 1) for b in self.blocks]
+
+    def points_flat(self) -> np.ndarray:
+        """All block points back to back, i fastest inside a block."""
+        return np.concatenate([b.reshape(-1, self.dim) for b in self.blocks], axis=0)
+
+    def cell_table(self) -> tuple[np.ndarray, np.ndarray]:
+        """(ncells, maxv, dim) ring vertices and (ncells,) vertex counts."""
+        if self.kind == "cells":
+            nv = self.nverts if self.nverts is not None else np.full(self.ncells, self.cells.shape[1], np.int32)
+            return self.cells, nv
+        out = []
+        for b in self.blocks:
+            p00 = b[:-1, :-1]
+            p10 = b[:-1, 1:]
+            p11 = b[1:, 1:]
+            p01 = b[1:, :-1]
+            quad = np.stack([p00, p10, p11, p01], axis=2)  # (ny, nx, 4, dim)
+            out.append(quad.reshape(-1, 4, self.dim))
+        t = np.concatenate(out, axis=0)
+        return t, np.full(t.shape[0], 4, np.int32)
+
+    def to_spherical(self) -> "Grid":
+        """Planar (lon, lat) degrees -> unit sphere (the manifold promotion of
+        Regridder(dst, src), src/regridder/regridder.jl:109-117)."""
+        if self.manifold == SPHERICAL:
+            return self
+        if self.kind == "curvilinear":
+            blocks = [unit_sphere_from_geographic(b[..., 0], b[..., 1]) for b in self.blocks]
+            return Grid("curvilinear", SPHERICAL, blocks=blocks, full_sphere=self.full_sphere, name=self.name)
+        cells = unit_sphere_from_geographic(self.cells[..., 0], self.cells[..., 1])
+        return Grid("cells", SPHERICAL, cells=cells, nverts=self.nverts, name=self.name)
+
+
+# ----------------------------------------------------------------- lon-lat
+
+def lonlat_grid(lon_edges: Sequence[float], lat_edges: Sequence[float], full_sphere: Optional[bool] = None,
+                name: str = "") -> Grid:
+    """Lon-lat grid with great-circle cell edges between the corner points
+    (the Oceananigans lon-lat convention: a vertex matrix turned into a
+    CellBasedGrid, ext/ConservativeRegriddingOceananigansExt.jl:246-263)."""
+    lon = np.asarray(lon_edges, np.float64)
+    lat = np.asarray(lat_edges, np.float64)
+    LON, LAT = np.meshgrid(lon, lat)  # (ny+1, nx+1)
+    pts = unit_sphere_from_geographic(LON, LAT)
+    if full_sphere is None:
+        full_sphere = bool(abs((lon[-1] - lon[0]) - 360.0) < 1e-9 and lat[0] <= -90.0 and lat[-1] >= 90.0)
+    return Grid("curvilinear", SPHERICAL, blocks=[pts], full_sphere=full_sphere, name=name)
+
+
+def lonlat_regular(dlon: float, dlat: float, lon0: float = 0.0, lat0: float = -90.0, name: str = "") -> Grid:
+    """Global lon-lat grid with spacing (dlon, dlat) starting at (lon0, lat0);
+    latitude edges are clamped to [-90, 90]."""
+    nx = int(round(360.0 / dlon))
+    ny = int(round(180.0 / dlat))
+    lon = lon0 + dlon * np.arange(nx + 1)
+    lat = np.clip(lat0 + dlat * np.arange(ny + 1), -90.0, 90.0)
+    return lonlat_grid(lon, lat, full_sphere=True, name=name or f"lonlat_{nx}x{ny}")
+
+
+def lonlat_jittered(nx: int, ny: int, jitter: float, seed: int, name: str = "") -> Grid:
+    """Global nx x ny lon-lat grid whose interior vertices move by
+    U(-jitter, jitter) cell widths in lon and lat.  Pole rows stay on the
+    poles and the 360-degree column repeats the jitter of column 0."""
+    rng = np.random.default_rng(seed)
+    dlon, dlat = 360.0 / nx, 180.0 / ny
+    lon = dlon * np.arange(nx + 1)[None, :].repeat(ny + 1, 0)
+    lat = (-90.0 + dlat * np.arange(ny + 1))[:, None].repeat(nx + 1, 1)
+    jl = rng.uniform(-jitter, jitter, size=(ny + 1, nx)) * dlon
+    jt = rng.uniform(-jitter, jitter, size=(ny + 1, nx)) * dlat
+    jl = np.concatenate([jl, jl[:, :1]], axis=1)
+    jt = np.concatenate([jt, jt[:, :1]], axis=1)
+    jl[0, :] = 0.0
+    jl[-1, :] = 0.0
+    jt[0, :] = 0.0
+    jt[-1, :] = 0.0
+    pts = unit_sphere_from_geographic(lon + jl, lat + jt)
+    return Grid("curvilinear", SPHERICAL, blocks=[pts], full_sphere=True, name=name or f"lonlat_jit_{nx}x{ny}")
+
+
+# ----------------------------------------------------------------- cubed sphere
+
+def _cube_face(f: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    one = np.ones_like(a)
+    if f == 0:
+        v = (one, a, b)
+    elif f == 1:
+        v = (-a, one, b)
+    elif f == 2:
+        v = (-one, -a, b)
+    elif f == 3:
+        v = (a, -one, b)
+    elif f == 4:
+        v = (-b, a, one)
+    else:
+        v = (b, a, -one)
+    p = np.stack(v, axis=-1)
+    return p / np.linalg.norm(p, axis=-1, keepdims=True)
+
+
+def cubed_sphere(ne: int, jitter: float = 0.0, seed: int = 0, name: str = "") -> Grid:
+    """Equiangular gnomonic cubed sphere (Ronchi, Iacono & Paolucci 1996)
+    with ne x ne cells per face; face f has cell offset f*ne^2 like the
+    reference's ClimaCore adapter (ext/ConservativeRegriddingClimaCoreExt.jl:56-61).
+    Cells are counter-clockwise seen from outside.  With ``jitter`` > 0 the
+    face-interior vertices move by U(-jitter, jitter) cell widths in both
+    face angles (shared face-edge vertices stay put)."""
+    rng = np.random.default_rng(seed)
+    t = np.linspace(-1.0, 1.0, ne + 1) * (np.pi / 4)
+    blocks = []
+    for f in range(6):
+        A, B = np.meshgrid(t, t)  # (ne+1, ne+1): [j, i] -> alpha_i, beta_j
+        if jitter > 0:
+            h = (np.pi / 2) / ne
+            ja = rng.uniform(-jitter, jitter, size=A.shape) * h
+            jb = rng.uniform(-jitter, jitter, size=A.shape) * h
+            ja[[0, -1], :] = 0.0
+            ja[:, [0, -1]] = 0.0
+            jb[[0, -1], :] = 0.0
+            jb[:, [0, -1]] = 0.0
+            A = A + ja
+            B = B + jb
+        blocks.append(_cube_face(f, np.tan(A), np.tan(B)))
+    return Grid("curvilinear", SPHERICAL, blocks=blocks, full_sphere=True, name=name or f"cs_C{ne}")
+
+
+# ----------------------------------------------------------------- HEALPix
+
+_JRLL = np.array([2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4], np.int64)
+_JPLL = np.array([1, 3, 5, 7, 0, 2, 4, 6, 1, 3, 5, 7], np.int64)
+
+
+def _compact_bits(v: np.ndarray) -> np.ndarray:
+    r = np.zeros_like(v)
+    for b in range(31):
+        r |= ((v >> (2 * b)) & 1) << b
+    return r
+
+
+def healpix_nest2xyf(nside: int, pix: np.ndarray):
+    npface = nside * nside
+    face = pix // npface
+    ipf = pix % npface
+    return _compact_bits(ipf), _compact_bits(ipf >> 1), face
+
+
+def _hp_loc2vec(x: np.ndarray, y: np.ndarray, face: np.ndarray) -> np.ndarray:
+    """Face coordinates (x, y) in [0, 1]^2 -> unit vectors (Gorski et al. 2005)."""
+    jr = _JRLL[face] - x - y
+    north = jr < 1.0
+    south = jr > 3.0
+    nr = np.where(north, jr, np.where(south, 4.0 - jr, 1.0))
+    tmp = nr * nr / 3.0
+    z = np.where(north, 1.0 - tmp, np.where(south, tmp - 1.0, (2.0 - jr) * 2.0 / 3.0))
+    sth = np.where(north | south, np.sqrt(np.maximum(tmp * (2.0 - tmp), 0.0)),
+                   np.sqrt(np.maximum((1.0 - z) * (1.0 + z), 0.0)))
+    t = _JPLL[face] * nr + x - y
+    t = np.where(t < 0, t + 8, t)
+    t = np.where(t >= 8, t - 8, t)
+    phi = np.where(nr < 1e-15, 0.0, (np.pi / 4) * t / np.where(nr < 1e-15, 1.0, nr))
+    return np.stack([sth * np.cos(phi), sth * np.sin(phi), z], axis=-1)
+
+
+def healpix_corners_nested(nside: int, pix: np.ndarray) -> np.ndarray:
+    """Corners (N, W, S, E) of nested pixels ``pix``: shape (len(pix), 4, 3)."""
+    pix = np.asarray(pix, np.int64)
+    ix, iy, face = healpix_nest2xyf(nside, pix)
+    ns = float(nside)
+    c = [
+        _hp_loc2vec((ix + 1) / ns, (iy + 1) / ns, face),
+        _hp_loc2vec(ix / ns, (iy + 1) / ns, face),
+        _hp_loc2vec(ix / ns, iy / ns, face),
+        _hp_loc2vec((ix + 1) / ns, iy / ns, face),
+    ]
+    return np.stack(c, axis=1)
+
+
+def healpix_nest2ring(nside: int, pix: np.ndarray) -> np.ndarray:
+    pix = np.asarray(pix, np.int64)
+    ix, iy, face = healpix_nest2xyf(nside, pix)
+    nl4 = 4 * nside
+    npix = 12 * nside * nside
+    ncap = 2 * nside * (nside - 1)
+    jr = _JRLL[face] * nside - ix - iy - 1
+    north = jr < nside
+    south = jr > 3 * nside
+    nr = np.where(north, jr, np.where(south, nl4 - jr, nside))
+    nbefore = np.where(north, 2 * nr * (nr - 1), np.where(south, npix - 2 * (nr + 1) * nr, ncap + (jr - nside) * nl4))
+    kshift = np.where(north | south, 0, (jr - nside) & 1)
+    jp = (_JPLL[face] * nr + ix - iy + 1 + kshift) // 2
+    jp = np.where(jp > nl4, jp - nl4, jp)
+    jp = np.where(jp < 1, jp + nl4, jp)
+    return nbefore + jp - 1
+
+
+def healpix_grid(nside: int, order: str = "nested", name: str = "") -> Grid:
+    """HEALPix pixels as great-circle quadrilaterals through their 4 corners
+    (N, W, S, E), indexed in nested or ring order like HealpixRootNode{O}
+    (ext/ConservativeRegriddingHealpixExt.jl:154-169)."""
+    if nside < 1 or (nside & (nside - 1)) != 0:
+        raise ValueError("nside must be a power of two")
+    npix = 12 * nside * nside
+    nested = np.arange(npix, dtype=np.int64)
+    corners = healpix_corners_nested(nside, nested)
+    if order == "ring":
+        ring = healpix_nest2ring(nside, nested)
+        out = np.empty_like(corners)
+        out[ring] = corners
+        corners = out
+    elif order != "nested":
+        raise ValueError("order must be 'nested' or 'ring'")
+    return Grid("cells", SPHERICAL, cells=corners, full_sphere=True, healpix=(nside, order == "nested"),
+                name=name or f"healpix_{nside}_{order}")
+
+
+# ----------------------------------------------------------------- polygons
+
+def polygon_grid(polys, manifold: str = PLANAR, name: str = "") -> Grid:
+    """Explicit convex polygons (FlatNoTree of the reference).  Each polygon
+    is a sequence of vertices; a closing repeat of the first vertex is dropped."""
+    dim = 3 if manifold == SPHERICAL else 2
+    rings = []
+    for p in polys:
+        a = np.asarray(p, np.float64).reshape(-1, dim)
+        if len(a) > 1 and np.array_equal(a[0], a[-1]):
+            a = a[:-1]
+        rings.append(a)
+    maxv = max(len(r) for r in rings)
+    if maxv > 8:
+        raise ValueError("polygons with more than 8 vertices are not supported")
+    cells = np.zeros((len(rings), maxv, dim))
+    nv = np.zeros(len(rings), np.int32)
+    for k, r in enumerate(rings):
+        cells[k, : len(r)] = r
+        cells[k, len(r):] = r[-1]
+        nv[k] = len(r)
+    return Grid("cells", manifold, cells=cells, nverts=nv, name=name)
+
+
+def regular_grid(x: Sequence[float], y: Sequence[float], name: str = "") -> Grid:
+    """Planar RegularGrid (src/trees/grids.jl:96-115) as a vertex matrix."""
+    X, Y = np.meshgrid(np.asarray(x, np.float64), np.asarray(y, np.float64))
+    return Grid("curvilinear", PLANAR, blocks=[np.stack([X, Y], axis=-1)], name=name)

@@ -1,0 +1,312 @@
+// crg_apply.cu -- applying the regridder: d = (A s) ./ a_d and its transpose.
+//
+// Replaces regrid! (src/regridder/regrid.jl:63-118): the stdlib CSC mul!
+// (single-threaded column scatter, :95-98) followed by the division by the
+// destination areas (:104-118), the one-mul!-per-slice N-D loop
+// (NDSliceLoop, :225-318), and regrid!(dst, transpose(R), src)
+// (src/regridder/regridder.jl:49-50).  A is stored twice (CSR rows = dst and
+// rows = src), so every direction is a row gather with no atomics.
+//
+// Kernels:
+//   k_spmv_f64      FP64, one thread per (row, field), summation in ascending
+//                   column order from 0.0 -- the same sequence as the
+//                   reference's column-scatter mul! for each row -- then the
+//                   optional division by the row area.
+//   k_spmm_rows     FP32/BF16 fields stored cell-major (the fields of one cell
+//                   side by side): G lanes per row, each lane owns 4
+//                   consecutive fields (128-bit FP32 / 64-bit BF16 loads),
+//                   FP32 accumulation, weights read once per row.
+//   k_spmm_tile     FP32/BF16 fields stored field-major (dims = 1): a block
+//                   owns 128 consecutive rows, stages their (column, weight)
+//                   entries in shared memory once, then sweeps all fields.
+//   k_spmm_generic  any strides, one thread per (row, field).
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "crg_internal.cuh"
+
+namespace crg {
+
+namespace {
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ------------------------------------------------------------------ element IO
+
+template <class T> __device__ __forceinline__ float ld1(const T* p);
+template <> __device__ __forceinline__ float ld1<float>(const float* p) { return __ldg(p); }
+template <> __device__ __forceinline__ float ld1<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(__ldg(p)); }
+
+template <class T> __device__ __forceinline__ void st1(T* p, float v);
+template <> __device__ __forceinline__ void st1<float>(float* p, float v) { *p = v; }
+template <> __device__ __forceinline__ void st1<__nv_bfloat16>(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+
+// 4 consecutive elements (16 B FP32 / 8 B BF16, aligned)
+template <class T> __device__ __forceinline__ float4 ld4(const T* p);
+template <> __device__ __forceinline__ float4 ld4<float>(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+template <> __device__ __forceinline__ float4 ld4<__nv_bfloat16>(const __nv_bfloat16* p) {
+  uint2 u = __ldg(reinterpret_cast<const uint2*>(p));
+  __nv_bfloat162 a = *reinterpret_cast<__nv_bfloat162*>(&u.x);
+  __nv_bfloat162 b = *reinterpret_cast<__nv_bfloat162*>(&u.y);
+  float2 fa = __bfloat1622float2(a), fb = __bfloat1622float2(b);
+  return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+
+template <class T> __device__ __forceinline__ void st4(T* p, float4 v);
+template <> __device__ __forceinline__ void st4<float>(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+template <> __device__ __forceinline__ void st4<__nv_bfloat16>(__nv_bfloat16* p, float4 v) {
+  __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y), b = __floats2bfloat162_rn(v.z, v.w);
+  uint2 u;
+  u.x = *reinterpret_cast<uint32_t*>(&a);
+  u.y = *reinterpret_cast<uint32_t*>(&b);
+  *reinterpret_cast<uint2*>(p) = u;
+}
+
+// ------------------------------------------------------------------ FP64
+
+__global__ void k_spmv_f64(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                           const double* __restrict__ val, int64_t nrows, const double* __restrict__ x, int64_t xsc,
+                           int64_t xsf, double* __restrict__ y, int64_t ysc, int64_t ysf, int64_t f0,
+                           const double* __restrict__ row_div, const double* __restrict__ col_div) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int64_t f = f0 + blockIdx.y;
+  const double* xf = x + f * xsf;
+  double acc = 0.0;
+  for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) {
+    int32_t j = idx[k];
+    double xv = xf[(int64_t)j * xsc];
+    if (col_div) xv = xv / col_div[j];
+    acc = acc + val[k] * xv;
+  }
+  if (row_div) acc = acc / row_div[r];
+  y[r * ysc + f * ysf] = acc;
+}
+
+// ------------------------------------------------------------------ cell-major fields
+
+template <class T, int G, bool kVec>
+__global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                   const float* __restrict__ w, int64_t nrows, const T* __restrict__ x,
+                                                   int64_t xsc, T* __restrict__ y, int64_t ysc, int64_t nf) {
+  const int g = threadIdx.x % G;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  if (r >= nrows) return;
+  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
+  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool full = kVec && f + 4 <= nf;
+    for (int32_t k = k0; k < k1; ++k) {
+      const int64_t j = idx[k];
+      const float ww = __ldg(w + k);
+      const T* xp = x + j * xsc + f;
+      float4 v;
+      if (full) {
+        v = ld4<T>(xp);
+      } else {
+        v.x = ld1<T>(xp);
+        v.y = f + 1 < nf ? ld1<T>(xp + 1) : 0.f;
+        v.z = f + 2 < nf ? ld1<T>(xp + 2) : 0.f;
+        v.w = f + 3 < nf ? ld1<T>(xp + 3) : 0.f;
+      }
+      acc.x = fmaf(ww, v.x, acc.x);
+      acc.y = fmaf(ww, v.y, acc.y);
+      acc.z = fmaf(ww, v.z, acc.z);
+      acc.w = fmaf(ww, v.w, acc.w);
+    }
+    T* yp = y + r * ysc + f;
+    if (full) {
+      st4<T>(yp, acc);
+    } else {
+      st1<T>(yp, acc.x);
+      if (f + 1 < nf) st1<T>(yp + 1, acc.y);
+      if (f + 2 < nf) st1<T>(yp + 2, acc.z);
+      if (f + 3 < nf) st1<T>(yp + 3, acc.w);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ field-major fields
+
+constexpr int kTileRows = 128;
+constexpr int kTileEntries = 4096;  // shared-memory capacity (32 KB)
+constexpr int kTileF = 8;           // fields per sweep step
+
+template <class T>
+__global__ void __launch_bounds__(kTileRows) k_spmm_tile(const int32_t* __restrict__ ptr,
+                                                          const int32_t* __restrict__ idx,
+                                                          const float* __restrict__ w, int64_t nrows,
+                                                          const T* __restrict__ x, int64_t xsf, T* __restrict__ y,
+                                                          int64_t ysf, int64_t nf) {
+  __shared__ int32_t s_idx[kTileEntries];
+  __shared__ float s_w[kTileEntries];
+  const int64_t r0 = (int64_t)blockIdx.x * kTileRows;
+  const int64_t r = r0 + threadIdx.x;
+  const int64_t rend = min(nrows, r0 + kTileRows);
+  const int32_t e0 = ptr[r0], e1 = ptr[rend];
+  const bool staged = (e1 - e0) <= kTileEntries;
+  if (staged) {
+    for (int32_t e = e0 + threadIdx.x; e < e1; e += kTileRows) {
+      s_idx[e - e0] = idx[e];
+      s_w[e - e0] = w[e];
+    }
+  }
+  __syncthreads();
+  if (r >= nrows) return;
+  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
+  for (int64_t f0 = 0; f0 < nf; f0 += kTileF) {
+    float acc[kTileF];
+#pragma unroll
+    for (int q = 0; q < kTileF; ++q) acc[q] = 0.f;
+    const int nq = (int)(nf - f0 < kTileF ? nf - f0 : kTileF);
+    for (int32_t k = k0; k < k1; ++k) {
+      const int64_t j = staged ? s_idx[k - e0] : idx[k];
+      const float ww = staged ? s_w[k - e0] : w[k];
+      const T* xp = x + f0 * xsf + j;
+#pragma unroll
+      for (int q = 0; q < kTileF; ++q)
+        if (q < nq) acc[q] = fmaf(ww, ld1<T>(xp + q * xsf), acc[q]);
+    }
+    T* yp = y + f0 * ysf + r;
+#pragma unroll
+    for (int q = 0; q < kTileF; ++q)
+      if (q < nq) st1<T>(yp + q * ysf, acc[q]);
+  }
+}
+
+// ------------------------------------------------------------------ generic strides
+
+template <class T>
+__global__ void k_spmm_generic(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                               const float* __restrict__ w, int64_t nrows, const T* __restrict__ x, int64_t xsc,
+                               int64_t xsf, T* __restrict__ y, int64_t ysc, int64_t ysf, int64_t f0) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int64_t f = f0 + blockIdx.y;
+  float acc = 0.f;
+  for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) acc = fmaf(w[k], ld1<T>(x + (int64_t)idx[k] * xsc + f * xsf), acc);
+  st1<T>(y + r * ysc + f * ysf, acc);
+}
+
+template <class T>
+void launch_f32(const DevCsr& c, const float* w, const T* x, int64_t xsc, int64_t xsf, T* y, int64_t ysc, int64_t ysf,
+                int64_t nf, cudaStream_t st) {
+  const int64_t n = c.nrows;
+  if (n == 0 || nf == 0) return;
+  const bool cell_major = (xsf == 1 && ysf == 1) && nf > 1;
+  const bool field_major = (xsc == 1 && ysc == 1);
+  if (cell_major) {
+    const bool vec = (xsc % 4 == 0) && (ysc % 4 == 0) && (nf % 4 == 0) &&
+                     ((uintptr_t)x % (4 * sizeof(T)) == 0) && ((uintptr_t)y % (4 * sizeof(T)) == 0);
+    int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
+    int G = 1;
+    while (G < lanes) G <<= 1;
+    const unsigned blocks = nblk(n * G, 256);
+#define CRG_ROWS_CASE(GG)                                                                                  \
+  case GG:                                                                                                 \
+    if (vec) k_spmm_rows<T, GG, true><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, x, xsc, y, ysc, nf);     \
+    else k_spmm_rows<T, GG, false><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, x, xsc, y, ysc, nf);        \
+    break;
+    switch (G) {
+      CRG_ROWS_CASE(1)
+      CRG_ROWS_CASE(2)
+      CRG_ROWS_CASE(4)
+      CRG_ROWS_CASE(8)
+      CRG_ROWS_CASE(16)
+      CRG_ROWS_CASE(32)
+    }
+#undef CRG_ROWS_CASE
+  } else if (field_major) {
+    k_spmm_tile<T><<<nblk(n, kTileRows), kTileRows, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
+  } else {
+    for (int64_t f0 = 0; f0 < nf; f0 += 65535) {
+      dim3 grid(nblk(n, 256), (unsigned)std::min<int64_t>(65535, nf - f0));
+      k_spmm_generic<T><<<grid, 256, 0, st>>>(c.ptr, c.idx, w, n, x, xsc, xsf, y, ysc, ysf, f0);
+    }
+  }
+  CRG_CHECK_CUDA(cudaGetLastError());
+}
+
+size_t elem_size(int dtype) { return dtype == CRG_F64 ? 8 : (dtype == CRG_F32 ? 4 : 2); }
+
+}  // namespace
+
+void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint, const void* src, int64_t ssc,
+                int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st) {
+  crg_regridder* r = const_cast<crg_regridder*>(rc);
+  CRG_REQUIRE(r != nullptr, CRG_ERR_INVALID_ARGUMENT, "regridder is NULL");
+  CRG_REQUIRE(dtype == CRG_F64 || dtype == CRG_F32 || dtype == CRG_BF16, CRG_ERR_INVALID_ARGUMENT, "unknown dtype %d",
+              dtype);
+  CRG_REQUIRE(nf >= 0, CRG_ERR_INVALID_ARGUMENT, "nfields must be >= 0");
+  CRG_REQUIRE(ssc >= 0 && ssf >= 0 && dsc >= 0 && dsf >= 0, CRG_ERR_INVALID_ARGUMENT, "strides must be >= 0");
+  const bool t = transpose != 0;
+  // direction: which copy of A is read, and which area vector divides
+  const DevCsr& c = adjoint ? (t ? r->fwd : r->rev) : (t ? r->rev : r->fwd);
+  const double* div = normalize ? (t ? r->src_area : r->dst_area) : nullptr;
+  const int64_t nin = c.ncols, nout = c.nrows;
+  if (nf == 0 || nout == 0) return;
+  CRG_REQUIRE(dst != nullptr && (src != nullptr || nin == 0), CRG_ERR_INVALID_ARGUMENT, "field pointer is NULL");
+  CRG_REQUIRE(nin == 0 || (ssc > 0 || nin == 1), CRG_ERR_INVALID_ARGUMENT, "source cell stride must be > 0");
+  CRG_REQUIRE(dsc > 0 || nout == 1, CRG_ERR_INVALID_ARGUMENT, "destination cell stride must be > 0");
+  CRG_REQUIRE(nf == 1 || (ssf > 0 && dsf > 0), CRG_ERR_INVALID_ARGUMENT, "field stride must be > 0");
+  int dev = 0;
+  CRG_CHECK_CUDA(cudaGetDevice(&dev));
+  CRG_REQUIRE(dev == r->device, CRG_ERR_INVALID_ARGUMENT, "regridder lives on device %d but device %d is current",
+              r->device, dev);
+
+  const size_t es = elem_size(dtype);
+  const int64_t in_span = nin > 0 ? (nin - 1) * ssc + (nf - 1) * ssf + 1 : 0;
+  const int64_t out_span = (nout - 1) * dsc + (nf - 1) * dsf + 1;
+  const bool src_host = nin > 0 && !is_device_pointer(src);
+  const bool dst_host = !is_device_pointer(dst);
+
+  std::unique_lock<std::mutex> lock(r->stage_mu, std::defer_lock);
+  const void* xs = src;
+  void* ys = dst;
+  if (src_host || dst_host) {
+    lock.lock();
+    size_t need = (src_host ? (size_t)in_span * es : 0) + (dst_host ? (size_t)out_span * es : 0) + 256;
+    if (r->stage_bytes < need) {
+      if (r->stage) CRG_CHECK_CUDA(cudaFree(r->stage));
+      r->stage = nullptr;
+      r->stage_bytes = 0;
+      CRG_CHECK_CUDA(cudaMalloc(&r->stage, need));
+      r->stage_bytes = need;
+    }
+    char* base = (char*)r->stage;
+    if (src_host) {
+      CRG_CHECK_CUDA(cudaMemcpyAsync(base, src, (size_t)in_span * es, cudaMemcpyHostToDevice, st));
+      xs = base;
+      base += ((size_t)in_span * es + 255) / 256 * 256;
+    }
+    if (dst_host) {
+      // a strided destination keeps the elements between ours: bring them along
+      if (out_span != nout * nf)
+        CRG_CHECK_CUDA(cudaMemcpyAsync(base, dst, (size_t)out_span * es, cudaMemcpyHostToDevice, st));
+      ys = base;
+    }
+  }
+
+  if (dtype == CRG_F64) {
+    const double* cdiv = adjoint ? div : nullptr;
+    const double* rdiv = adjoint ? nullptr : div;
+    for (int64_t f0 = 0; f0 < nf; f0 += 65535) {
+      dim3 grid(nblk(nout, 128), (unsigned)std::min<int64_t>(65535, nf - f0));
+      k_spmv_f64<<<grid, 128, 0, st>>>(c.ptr, c.idx, c.val, nout, (const double*)xs, ssc, ssf, (double*)ys, dsc, dsf,
+                                       f0, rdiv, cdiv);
+    }
+    CRG_CHECK_CUDA(cudaGetLastError());
+  } else {
+    const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
+    if (dtype == CRG_F32)
+      launch_f32<float>(c, w, (const float*)xs, ssc, ssf, (float*)ys, dsc, dsf, nf, st);
+    else
+      launch_f32<__nv_bfloat16>(c, w, (const __nv_bfloat16*)xs, ssc, ssf, (__nv_bfloat16*)ys, dsc, dsf, nf, st);
+  }
+
+  if (dst_host) CRG_CHECK_CUDA(cudaMemcpyAsync(dst, ys, (size_t)out_span * es, cudaMemcpyDeviceToHost, st));
+  if (src_host || dst_host) CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace crg

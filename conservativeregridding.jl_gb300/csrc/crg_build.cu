@@ -1,0 +1,1020 @@
+// crg_build.cu -- device build of the regridder.
+//
+// Replaces Regridder(dst, src; normalize) of ConservativeRegridding.jl
+// (src/regridder/regridder.jl:105-163):
+//   K1 per-cell geometry: vertex tables, bounding balls, exact cell areas
+//      (areas: regridder.jl:165-178; caps: src/trees/grids.jl:245-287)
+//   K2 spatial order (cube-face Morton key, counting sort) and an implicit
+//      binary hierarchy of axis-aligned boxes over leaves of 8 cells
+//   K3 level-synchronous dual traversal of the two hierarchies with
+//      warp-aggregated compaction of node pairs, then leaf-cell pair tests
+//      (replaces the multithreaded dual DFS of
+//      src/utils/MultithreadedDualDepthFirstSearch.jl:12-65 and
+//      src/regridder/intersection_areas.jl:48-65)
+//   K4 FP64 clip + area of every candidate pair (intersection_areas.jl:4-32)
+//   K5 counting-sort assembly into CSR (rows = dst) and CSR of A^T, sorted
+//      inside rows -- the pattern of SparseArrays.sparse(i_dst, i_src, area)
+//      (intersection_areas.jl:115-121) -- plus normalize! and the derived
+//      FP32 weights used by the apply kernels.
+#include <stdarg.h>
+#include <stdio.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "crg_geom.cuh"
+#include "crg_internal.cuh"
+#include "crg_scan.cuh"
+
+namespace crg {
+
+namespace {
+
+constexpr int kLeaf = 8;          // cells per hierarchy leaf
+constexpr int kMaxBlocks = 12;    // curvilinear blocks per grid
+constexpr int kMaxLevels = 40;
+constexpr int kSortShift = 10;    // bins of the counting sort = key >> kSortShift
+
+// ------------------------------------------------------------------ buffers
+
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaStream_t st = nullptr;
+  DBuf() = default;
+  DBuf(size_t n_, cudaStream_t s) { alloc(n_, s); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  void alloc(size_t n_, cudaStream_t s) {
+    release();
+    st = s;
+    n = n_;
+    if (n) CRG_CHECK_CUDA(cudaMallocAsync((void**)&p, n * sizeof(T), s));
+  }
+  void zero() {
+    if (n) CRG_CHECK_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+};
+
+template <class T>
+T* persistent_alloc(size_t n) {
+  T* p = nullptr;
+  if (n == 0) n = 1;
+  CRG_CHECK_CUDA(cudaMalloc((void**)&p, n * sizeof(T)));
+  return p;
+}
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// ------------------------------------------------------------------ K1: cell tables
+
+struct BlockInfo {
+  int nblocks;
+  int dim;
+  int64_t cell_off[kMaxBlocks + 1];
+  int64_t point_off[kMaxBlocks];
+  int64_t nx[kMaxBlocks];
+};
+
+__global__ void k_expand_curvi(const double* __restrict__ pts, BlockInfo bi, int64_t ncells, double* __restrict__ v,
+                               int8_t* __restrict__ nv) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  int b = 0;
+  while (b + 1 < bi.nblocks && c >= bi.cell_off[b + 1]) b++;
+  int64_t loc = c - bi.cell_off[b];
+  int64_t nx = bi.nx[b];
+  int64_t i = loc % nx, j = loc / nx;
+  int64_t p[4] = {i + j * (nx + 1), (i + 1) + j * (nx + 1), (i + 1) + (j + 1) * (nx + 1), i + (j + 1) * (nx + 1)};
+  for (int k = 0; k < 4; ++k) {
+    const double* q = pts + (bi.point_off[b] + p[k]) * bi.dim;
+    double* o = v + (c * 4 + k) * 3;
+    o[0] = q[0];
+    o[1] = q[1];
+    o[2] = bi.dim == 3 ? q[2] : 0.0;
+  }
+  nv[c] = 4;
+}
+
+__global__ void k_expand_cells(const double* __restrict__ cv, const int32_t* __restrict__ cn, int maxv, int dim,
+                               int64_t ncells, double* __restrict__ v, int8_t* __restrict__ nv,
+                               int32_t* __restrict__ bad) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  int n = cn ? cn[c] : maxv;
+  if (n < 3 || n > maxv) {
+    atomicAdd(bad, 1);
+    n = n < 3 ? 0 : maxv;
+  }
+  for (int k = 0; k < maxv; ++k) {
+    const double* q = cv + (c * maxv + k) * dim;
+    double* o = v + (c * maxv + k) * 3;
+    o[0] = q[0];
+    o[1] = q[1];
+    o[2] = dim == 3 ? q[2] : 0.0;
+  }
+  nv[c] = (int8_t)n;
+}
+
+__device__ __forceinline__ uint32_t spread_bits14(uint32_t x) {
+  // interleave: bit k of x -> bit 2k
+  x &= 0x3fffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t spread_bits16(uint32_t x) {
+  x &= 0xffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+__device__ __forceinline__ uint32_t q14(double u) {  // u in [-1, 1]
+  double t = (u + 1.0) * 8191.5;
+  t = t < 0.0 ? 0.0 : (t > 16383.0 ? 16383.0 : t);
+  return (uint32_t)t;
+}
+
+// Cube-face Morton key of a unit vector: face (3 bits) | 2 x 14 bits.
+__device__ __forceinline__ uint32_t sphere_key(double x, double y, double z) {
+  double ax = fabs(x), ay = fabs(y), az = fabs(z);
+  uint32_t face;
+  double u, v, m;
+  if (ax >= ay && ax >= az) { face = x >= 0 ? 0 : 1; m = ax; u = y; v = z; }
+  else if (ay >= az) { face = y >= 0 ? 2 : 3; m = ay; u = x; v = z; }
+  else { face = z >= 0 ? 4 : 5; m = az; u = x; v = y; }
+  if (!(m > 0.0)) return 0;
+  u /= m; v /= m;
+  return (face << 28) | spread_bits14(q14(u)) | (spread_bits14(q14(v)) << 1);
+}
+
+// Per-cell exact area, bounding volume and (spherical) order key.
+// Spherical bounds: a ball in R^3 around the unit centre c = normalize(sum v)
+// with chord radius rho = max |c - v_k|; the cell (great-circle edges) lies in
+// the spherical cap that ball cuts out whenever rho < sqrt(2), and rho = 2 is
+// used otherwise.  Planar bounds: the box of the vertices.  Both are rounded
+// outward to float and inflated so that the float tests are a superset of the
+// exact ones.
+template <bool kSph>
+__global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restrict__ nv, int maxv, int64_t ncells,
+                            double* __restrict__ area, float4* __restrict__ bound, uint32_t* __restrict__ key) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  d3 p[CRG_MAXV];
+  int n = nv[c];
+  for (int k = 0; k < n; ++k) {
+    const double* q = v + (c * maxv + k) * 3;
+    p[k].x = q[0]; p[k].y = q[1]; p[k].z = q[2];
+  }
+  area[c] = n >= 3 ? cell_area<kSph>(p, n) : 0.0;
+  if (kSph) {
+    double sx = 0, sy = 0, sz = 0;
+    for (int k = 0; k < n; ++k) { sx += p[k].x; sy += p[k].y; sz += p[k].z; }
+    double nr = sqrt(sx * sx + sy * sy + sz * sz);
+    double cx = 0, cy = 0, cz = 1;
+    if (nr > 0) { cx = sx / nr; cy = sy / nr; cz = sz / nr; }
+    double rho = 0;
+    for (int k = 0; k < n; ++k) {
+      double dx = p[k].x - cx, dy = p[k].y - cy, dz = p[k].z - cz;
+      rho = fmax(rho, sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    if (!(rho < 1.4) || !(nr > 0)) rho = 2.0;
+    float rf = __double2float_ru(rho * (1.0 + 4e-6) + 4e-6);
+    bound[c] = make_float4((float)cx, (float)cy, (float)cz, rf);
+    key[c] = sphere_key(cx, cy, cz);
+  } else {
+    double x0 = p[0].x, x1 = p[0].x, y0 = p[0].y, y1 = p[0].y;
+    for (int k = 1; k < n; ++k) {
+      x0 = fmin(x0, p[k].x); x1 = fmax(x1, p[k].x);
+      y0 = fmin(y0, p[k].y); y1 = fmax(y1, p[k].y);
+    }
+    bound[c] = make_float4(__double2float_rd(x0), __double2float_rd(y0), __double2float_ru(x1), __double2float_ru(y1));
+  }
+}
+
+// Planar keys after the global box is known (computed on the host from a
+// reduction): 2 x 16-bit Morton of the box centre.
+__global__ void k_planar_keys(const float4* __restrict__ bound, int64_t ncells, float4 gbox, uint32_t* __restrict__ key) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  float4 b = bound[c];
+  float cx = 0.5f * (b.x + b.z), cy = 0.5f * (b.y + b.w);
+  float wx = gbox.z - gbox.x, wy = gbox.w - gbox.y;
+  float ux = wx > 0 ? (cx - gbox.x) / wx : 0.f, uy = wy > 0 ? (cy - gbox.y) / wy : 0.f;
+  ux = fminf(fmaxf(ux, 0.f), 1.f);
+  uy = fminf(fmaxf(uy, 0.f), 1.f);
+  uint32_t qx = (uint32_t)(ux * 65535.f), qy = (uint32_t)(uy * 65535.f);
+  key[c] = spread_bits16(qx) | (spread_bits16(qy) << 1);
+}
+
+// Block-wise min/max of planar boxes -> per-block partials.
+__global__ void k_box_partials(const float4* __restrict__ bound, int64_t ncells, float4* __restrict__ part) {
+  __shared__ float4 sh[256];
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float4 b = c < ncells ? bound[c] : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
+  sh[threadIdx.x] = b;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) {
+      float4 o = sh[threadIdx.x + s];
+      float4 m = sh[threadIdx.x];
+      m.x = fminf(m.x, o.x); m.y = fminf(m.y, o.y); m.z = fmaxf(m.z, o.z); m.w = fmaxf(m.w, o.w);
+      sh[threadIdx.x] = m;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// ------------------------------------------------------------------ K2: order + hierarchy
+
+__global__ void k_hist(const uint32_t* __restrict__ key, int64_t n, int shift, int32_t* __restrict__ cnt) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) atomicAdd(&cnt[key[c] >> shift], 1);
+}
+
+__global__ void k_bin_scatter(const uint32_t* __restrict__ key, int64_t n, int shift, const int32_t* __restrict__ off,
+                              int32_t* __restrict__ fill, int32_t* __restrict__ perm) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  uint32_t b = key[c] >> shift;
+  int32_t slot = off[b] + atomicAdd(&fill[b], 1);
+  perm[slot] = (int32_t)c;
+}
+
+// Sort each bin by (key, cell index): bins are tiny, insertion sort per thread.
+__global__ void k_bin_sort(const uint32_t* __restrict__ key, const int32_t* __restrict__ off, int64_t nbins,
+                           int32_t* __restrict__ perm) {
+  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nbins) return;
+  int32_t lo = off[b], hi = off[b + 1];
+  for (int32_t i = lo + 1; i < hi; ++i) {
+    int32_t x = perm[i];
+    uint32_t kx = key[x];
+    int32_t j = i - 1;
+    while (j >= lo) {
+      int32_t y = perm[j];
+      uint32_t ky = key[y];
+      if (ky < kx || (ky == kx && y < x)) break;
+      perm[j + 1] = y;
+      --j;
+    }
+    perm[j + 1] = x;
+  }
+}
+
+// Leaf boxes (level 0) and the per-cell bounds in sorted order.
+template <bool kSph>
+__global__ void k_leaves(const float4* __restrict__ bound, const int32_t* __restrict__ perm, int64_t ncells,
+                         int64_t nleaves, float4* __restrict__ lo, float4* __restrict__ hi,
+                         float4* __restrict__ sbound) {
+  int64_t l = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nleaves) return;
+  float4 a = make_float4(INFINITY, INFINITY, INFINITY, 0.f), b = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.f);
+  int64_t e = min(ncells, (l + 1) * kLeaf);
+  for (int64_t s = l * kLeaf; s < e; ++s) {
+    float4 q = bound[perm[s]];
+    sbound[s] = q;
+    float x0, y0, z0, x1, y1, z1;
+    if (kSph) {
+      x0 = __fsub_rd(q.x, q.w); x1 = __fadd_ru(q.x, q.w);
+      y0 = __fsub_rd(q.y, q.w); y1 = __fadd_ru(q.y, q.w);
+      z0 = __fsub_rd(q.z, q.w); z1 = __fadd_ru(q.z, q.w);
+    } else {
+      x0 = q.x; y0 = q.y; x1 = q.z; y1 = q.w; z0 = 0.f; z1 = 0.f;
+    }
+    a.x = fminf(a.x, x0); a.y = fminf(a.y, y0); a.z = fminf(a.z, z0);
+    b.x = fmaxf(b.x, x1); b.y = fmaxf(b.y, y1); b.z = fmaxf(b.z, z1);
+  }
+  lo[l] = a;
+  hi[l] = b;
+}
+
+__global__ void k_level_up(const float4* __restrict__ clo, const float4* __restrict__ chi, int64_t nchild,
+                           float4* __restrict__ plo, float4* __restrict__ phi, int64_t nparent) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nparent) return;
+  float4 a = clo[2 * i], b = chi[2 * i];
+  if (2 * i + 1 < nchild) {
+    float4 c = clo[2 * i + 1], d = chi[2 * i + 1];
+    a.x = fminf(a.x, c.x); a.y = fminf(a.y, c.y); a.z = fminf(a.z, c.z);
+    b.x = fmaxf(b.x, d.x); b.y = fmaxf(b.y, d.y); b.z = fmaxf(b.z, d.z);
+  }
+  plo[i] = a;
+  phi[i] = b;
+}
+
+struct Tree {
+  int nlev = 0;                 // number of levels, leaves are level 0, root is nlev-1
+  int64_t off[kMaxLevels] = {}; // node offset of each level in lo/hi
+  int64_t cnt[kMaxLevels] = {}; // nodes per level
+  int64_t ncells = 0;
+  const float4* lo = nullptr;
+  const float4* hi = nullptr;
+  const float4* sbound = nullptr;  // per-cell bounds in sorted order
+  const int32_t* perm = nullptr;   // sorted position -> cell index
+};
+
+// ------------------------------------------------------------------ K3: dual traversal
+
+__device__ __forceinline__ uint32_t pack_node(int lev, int64_t idx) { return ((uint32_t)lev << 27) | (uint32_t)idx; }
+__device__ __forceinline__ int node_lev(uint32_t p) { return (int)(p >> 27); }
+__device__ __forceinline__ int64_t node_idx(uint32_t p) { return (int64_t)(p & 0x07ffffffu); }
+
+__device__ __forceinline__ bool box_overlap(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+  return alo.x <= bhi.x && blo.x <= ahi.x && alo.y <= bhi.y && blo.y <= ahi.y && alo.z <= bhi.z && blo.z <= ahi.z;
+}
+
+struct TreeView {
+  int64_t off[kMaxLevels];
+  int64_t cnt[kMaxLevels];
+  const float4* lo;
+  const float4* hi;
+};
+
+// Warp-aggregated append of `k` items (k per lane may differ); returns the
+// first output slot of this lane.
+__device__ __forceinline__ int64_t warp_append(int k, unsigned long long* counter) {
+  const int lane = threadIdx.x & 31;
+  int incl = k;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  int total = __shfl_sync(0xffffffffu, incl, 31);
+  unsigned long long base = 0;
+  if (lane == 31 && total > 0) base = atomicAdd(counter, (unsigned long long)total);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  return (int64_t)base + incl - k;
+}
+
+// One level of the dual traversal.  Each frontier pair (dst node, src node)
+// expands the non-leaf side(s); child pairs whose boxes overlap go to the next
+// frontier, or to the leaf-pair list when both children are leaves.
+__global__ void k_traverse(const uint2* __restrict__ in, int64_t nin, TreeView td, TreeView ts,
+                           uint2* __restrict__ next, unsigned long long* __restrict__ nnext,
+                           uint2* __restrict__ leaves, unsigned long long* __restrict__ nleaves) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nloop = (nin + 31) / 32 * 32;
+  for (int64_t it = tid; it < ((nloop + stride - 1) / stride) * stride; it += stride) {
+    uint2 outs[4];
+    int nout = 0;
+    if (it < nin) {
+      uint2 pr = in[it];
+      int la = node_lev(pr.x), lb = node_lev(pr.y);
+      int64_t ia = node_idx(pr.x), ib = node_idx(pr.y);
+      uint32_t ca[2], cb[2];
+      int na = 0, nb = 0;
+      if (la > 0) {
+        ca[na++] = pack_node(la - 1, 2 * ia);
+        if (2 * ia + 1 < td.cnt[la - 1]) ca[na++] = pack_node(la - 1, 2 * ia + 1);
+      } else {
+        ca[na++] = pr.x;
+      }
+      if (lb > 0) {
+        cb[nb++] = pack_node(lb - 1, 2 * ib);
+        if (2 * ib + 1 < ts.cnt[lb - 1]) cb[nb++] = pack_node(lb - 1, 2 * ib + 1);
+      } else {
+        cb[nb++] = pr.y;
+      }
+      for (int a = 0; a < na; ++a) {
+        int64_t ga = td.off[node_lev(ca[a])] + node_idx(ca[a]);
+        float4 alo = td.lo[ga], ahi = td.hi[ga];
+        for (int b = 0; b < nb; ++b) {
+          int64_t gb = ts.off[node_lev(cb[b])] + node_idx(cb[b]);
+          if (box_overlap(alo, ahi, ts.lo[gb], ts.hi[gb])) outs[nout++] = make_uint2(ca[a], cb[b]);
+        }
+      }
+    }
+    // split into leaf pairs and internal pairs
+    int nl = 0, ni = 0;
+    for (int k = 0; k < nout; ++k) {
+      if (node_lev(outs[k].x) == 0 && node_lev(outs[k].y) == 0) nl++;
+      else ni++;
+    }
+    int64_t pi = warp_append(ni, nnext);
+    int64_t pl = warp_append(nl, nleaves);
+    for (int k = 0; k < nout; ++k) {
+      if (node_lev(outs[k].x) == 0 && node_lev(outs[k].y) == 0) leaves[pl++] = outs[k];
+      else next[pi++] = outs[k];
+    }
+  }
+}
+
+template <bool kSph>
+__device__ __forceinline__ bool cell_test(float4 a, float4 b) {
+  if (kSph) {
+    float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float r = a.w + b.w;
+    return d2 <= r * r * 1.000002f;
+  }
+  return a.x <= b.z && b.x <= a.z && a.y <= b.w && b.y <= a.w;
+}
+
+// Leaf pair -> number of cell pairs whose bounds intersect.
+template <bool kSph>
+__global__ void k_leaf_count(const uint2* __restrict__ lp, int64_t nlp, const float4* __restrict__ dsb, int64_t nd,
+                             const float4* __restrict__ ssb, int64_t ns, int32_t* __restrict__ cnt) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nlp) return;
+  uint2 p = lp[t];
+  int64_t d0 = node_idx(p.x) * kLeaf, s0 = node_idx(p.y) * kLeaf;
+  int64_t d1 = min(nd, d0 + kLeaf), s1 = min(ns, s0 + kLeaf);
+  float4 db[kLeaf];
+  int ndc = (int)(d1 - d0);
+  for (int k = 0; k < ndc; ++k) db[k] = dsb[d0 + k];
+  int c = 0;
+  for (int64_t s = s0; s < s1; ++s) {
+    float4 sb = ssb[s];
+    for (int k = 0; k < ndc; ++k) c += cell_test<kSph>(db[k], sb) ? 1 : 0;
+  }
+  cnt[t] = c;
+}
+
+template <bool kSph>
+__global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const float4* __restrict__ dsb,
+                            const int32_t* __restrict__ dperm, int64_t nd, const float4* __restrict__ ssb,
+                            const int32_t* __restrict__ sperm, int64_t ns, const int32_t* __restrict__ off,
+                            int2* __restrict__ cand) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nlp) return;
+  uint2 p = lp[t];
+  int64_t d0 = node_idx(p.x) * kLeaf, s0 = node_idx(p.y) * kLeaf;
+  int64_t d1 = min(nd, d0 + kLeaf), s1 = min(ns, s0 + kLeaf);
+  float4 db[kLeaf];
+  int ndc = (int)(d1 - d0);
+  for (int k = 0; k < ndc; ++k) db[k] = dsb[d0 + k];
+  int32_t o = off[t];
+  for (int64_t s = s0; s < s1; ++s) {
+    float4 sb = ssb[s];
+    int32_t sc = sperm[s];
+    for (int k = 0; k < ndc; ++k)
+      if (cell_test<kSph>(db[k], sb)) cand[o++] = make_int2(dperm[d0 + k], sc);
+  }
+}
+
+// ------------------------------------------------------------------ K4: clip + area
+
+template <bool kSph>
+__global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
+                                              const int8_t* __restrict__ dnv, int dmaxv, const double* __restrict__ sv,
+                                              const int8_t* __restrict__ snv, int smaxv, double* __restrict__ area,
+                                              int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt,
+                                              unsigned long long* __restrict__ overflow) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc) return;
+  int2 pr = cand[t];
+  d3 clip[CRG_MAXV];
+  d3 bufA[CRG_MAXC], bufB[CRG_MAXC];
+  int nd = dnv[pr.x], ns = snv[pr.y];
+  const double* q = dv + (int64_t)pr.x * dmaxv * 3;
+  for (int k = 0; k < nd; ++k) { clip[k].x = q[3 * k]; clip[k].y = q[3 * k + 1]; clip[k].z = q[3 * k + 2]; }
+  q = sv + (int64_t)pr.y * smaxv * 3;
+  for (int k = 0; k < ns; ++k) { bufA[k].x = q[3 * k]; bufA[k].y = q[3 * k + 1]; bufA[k].z = q[3 * k + 2]; }
+  double sig = kSph ? orient_sph(bufA, ns) : orient_pl(bufA, ns);
+  double a = 0.0;
+  if (nd >= 3 && ns >= 3) {
+    d3* res;
+    int m = clip_polygon<kSph>(bufA, bufB, ns, clip, nd, &res);
+    if (m < 0) {
+      atomicAdd(overflow, 1ull);
+    } else {
+      a = (kSph ? area_sph_signed(res, m) : area_pl_signed(res, m)) * sig;
+    }
+  }
+  area[t] = a;
+  if (a > 0.0) {
+    atomicAdd(&rowcnt[pr.x], 1);
+    atomicAdd(&colcnt[pr.y], 1);
+  }
+}
+
+// ------------------------------------------------------------------ K5: assembly
+
+__global__ void k_scatter_pairs(const int2* __restrict__ cand, const double* __restrict__ area, int64_t nc,
+                                const int32_t* __restrict__ rowptr, int32_t* __restrict__ rowfill,
+                                const int32_t* __restrict__ colptr, int32_t* __restrict__ colfill,
+                                int32_t* __restrict__ fidx, double* __restrict__ fval, int32_t* __restrict__ ridx,
+                                double* __restrict__ rval) {
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc) return;
+  double a = area[t];
+  if (!(a > 0.0)) return;
+  int2 pr = cand[t];
+  int32_t p = rowptr[pr.x] + atomicAdd(&rowfill[pr.x], 1);
+  fidx[p] = pr.y;
+  fval[p] = a;
+  int32_t q = colptr[pr.y] + atomicAdd(&colfill[pr.y], 1);
+  ridx[q] = pr.x;
+  rval[q] = a;
+}
+
+// Sort each row segment by column (insertion sort; rows are short).
+__global__ void k_row_sort(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ idx,
+                           double* __restrict__ val) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  int32_t lo = ptr[r], hi = ptr[r + 1];
+  for (int32_t i = lo + 1; i < hi; ++i) {
+    int32_t x = idx[i];
+    double v = val[i];
+    int32_t j = i - 1;
+    while (j >= lo && idx[j] > x) {
+      idx[j + 1] = idx[j];
+      val[j + 1] = val[j];
+      --j;
+    }
+    idx[j + 1] = x;
+    val[j + 1] = v;
+  }
+}
+
+__global__ void k_max_val(const double* __restrict__ v, int64_t n, unsigned long long* __restrict__ mx) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = 0.0;  // maximum(A) of a SparseMatrixCSC includes its implicit zeros; values are > 0 here
+  for (; i < n; i += (int64_t)gridDim.x * blockDim.x) m = fmax(m, v[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, (unsigned long long)__double_as_longlong(m));
+}
+
+__global__ void k_div_by(double* __restrict__ v, int64_t n, const unsigned long long* __restrict__ mx) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = v[i] / __longlong_as_double((long long)*mx);
+}
+
+// FP32 weights: val32 = A, wn32 = A / area_row, adj32 = A / area_col, plus the
+// Kahan row sums of A.
+__global__ void k_derive(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                         const double* __restrict__ val, int64_t nrows, const double* __restrict__ area_row,
+                         const double* __restrict__ area_col, float* __restrict__ val32, float* __restrict__ wn32,
+                         float* __restrict__ adj32, double* __restrict__ rowsum) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  double ar = area_row[r];
+  double s = 0.0, comp = 0.0;
+  for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) {
+    double a = val[k];
+    val32[k] = (float)a;
+    wn32[k] = (float)(a / ar);
+    adj32[k] = (float)(a / area_col[idx[k]]);
+    double y = a - comp;
+    double t = s + y;
+    comp = (t - s) - y;
+    s = t;
+  }
+  rowsum[r] = s;
+}
+
+// ------------------------------------------------------------------ host helpers
+
+struct DevGrid {
+  CellTable tab;
+  DBuf<double> v;
+  DBuf<int8_t> nv;
+  int64_t ncells = 0;
+};
+
+void upload_grid(const crg_grid_desc* g, DevGrid& out, cudaStream_t st) {
+  CRG_REQUIRE(g != nullptr, CRG_ERR_INVALID_ARGUMENT, "grid descriptor is NULL");
+  CRG_REQUIRE(g->manifold == CRG_PLANAR || g->manifold == CRG_SPHERICAL, CRG_ERR_INVALID_ARGUMENT,
+              "unknown manifold %d", g->manifold);
+  CRG_REQUIRE(g->ncells >= 0 && g->ncells < (int64_t)1 << 31, CRG_ERR_NOT_SUPPORTED,
+              "ncells = %lld is outside [0, 2^31)", (long long)g->ncells);
+  const int dim = g->manifold == CRG_SPHERICAL ? 3 : 2;
+  out.ncells = g->ncells;
+  if (g->kind == CRG_GRID_CURVILINEAR) {
+    CRG_REQUIRE(g->nblocks >= 1 && g->nblocks <= kMaxBlocks, CRG_ERR_INVALID_ARGUMENT,
+                "nblocks = %d must be in 1..%d", g->nblocks, kMaxBlocks);
+    CRG_REQUIRE(g->block_nx && g->block_ny && g->points, CRG_ERR_INVALID_ARGUMENT, "curvilinear grid arrays are NULL");
+    BlockInfo bi{};
+    bi.nblocks = g->nblocks;
+    bi.dim = dim;
+    int64_t cells = 0, pts = 0;
+    for (int b = 0; b < g->nblocks; ++b) {
+      CRG_REQUIRE(g->block_nx[b] >= 1 && g->block_ny[b] >= 1, CRG_ERR_INVALID_ARGUMENT,
+                  "block %d has %lld x %lld cells", b, (long long)g->block_nx[b], (long long)g->block_ny[b]);
+      bi.cell_off[b] = cells;
+      bi.point_off[b] = pts;
+      bi.nx[b] = g->block_nx[b];
+      cells += g->block_nx[b] * g->block_ny[b];
+      pts += (g->block_nx[b] + 1) * (g->block_ny[b] + 1);
+    }
+    bi.cell_off[g->nblocks] = cells;
+    CRG_REQUIRE(cells == g->ncells, CRG_ERR_DIMENSION_MISMATCH,
+                "ncells = %lld but the blocks hold %lld cells", (long long)g->ncells, (long long)cells);
+    const double* dpts = g->points;
+    DBuf<double> staged;
+    if (!is_device_pointer(g->points)) {
+      staged.alloc((size_t)pts * dim, st);
+      CRG_CHECK_CUDA(cudaMemcpyAsync(staged.p, g->points, sizeof(double) * pts * dim, cudaMemcpyHostToDevice, st));
+      dpts = staged.p;
+    }
+    out.tab.n = cells;
+    out.tab.maxv = 4;
+    out.v.alloc((size_t)cells * 4 * 3, st);
+    out.nv.alloc((size_t)cells, st);
+    if (cells) {
+      k_expand_curvi<<<nblk(cells, 256), 256, 0, st>>>(dpts, bi, cells, out.v.p, out.nv.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+  } else if (g->kind == CRG_GRID_CELLS) {
+    CRG_REQUIRE(g->max_verts >= 3 && g->max_verts <= CRG_MAXV, CRG_ERR_INVALID_ARGUMENT,
+                "max_verts = %d must be in 3..%d", g->max_verts, CRG_MAXV);
+    CRG_REQUIRE(g->cell_verts || g->ncells == 0, CRG_ERR_INVALID_ARGUMENT, "cell_verts is NULL");
+    const int64_t n = g->ncells, mv = g->max_verts;
+    const double* dcv = g->cell_verts;
+    const int32_t* dcn = g->cell_nverts;
+    DBuf<double> s1;
+    DBuf<int32_t> s2;
+    if (n && !is_device_pointer(g->cell_verts)) {
+      s1.alloc((size_t)n * mv * dim, st);
+      CRG_CHECK_CUDA(cudaMemcpyAsync(s1.p, g->cell_verts, sizeof(double) * n * mv * dim, cudaMemcpyHostToDevice, st));
+      dcv = s1.p;
+    }
+    if (n && dcn && !is_device_pointer(dcn)) {
+      s2.alloc((size_t)n, st);
+      CRG_CHECK_CUDA(cudaMemcpyAsync(s2.p, dcn, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+      dcn = s2.p;
+    }
+    out.tab.n = n;
+    out.tab.maxv = (int)mv;
+    out.v.alloc((size_t)n * mv * 3, st);
+    out.nv.alloc((size_t)n, st);
+    DBuf<int32_t> bad(1, st);
+    bad.zero();
+    if (n) {
+      k_expand_cells<<<nblk(n, 256), 256, 0, st>>>(dcv, dcn, (int)mv, dim, n, out.v.p, out.nv.p, bad.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    int32_t hbad = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    CRG_REQUIRE(hbad == 0, CRG_ERR_INVALID_ARGUMENT, "%d cells have a vertex count outside 3..max_verts", hbad);
+  } else {
+    CRG_REQUIRE(false, CRG_ERR_INVALID_ARGUMENT, "unknown grid kind %d", g->kind);
+  }
+  out.tab.v = out.v.p;
+  out.tab.nv = out.nv.p;
+}
+
+struct HostTree {
+  Tree t;
+  DBuf<float4> bound, sbound, lo, hi;
+  DBuf<uint32_t> key;
+  DBuf<int32_t> perm;
+};
+
+// K1 + K2 for one grid.  `area_out` receives the exact cell areas.
+void build_tree(const DevGrid& g, bool sph, double* area_out, HostTree& h, cudaStream_t st) {
+  const int64_t n = g.ncells;
+  h.t.ncells = n;
+  h.bound.alloc((size_t)n, st);
+  h.key.alloc((size_t)n, st);
+  if (n == 0) return;
+  if (sph) {
+    k_cell_geom<true><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  } else {
+    k_cell_geom<false><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    int64_t nb = nblk(n, 256);
+    DBuf<float4> part((size_t)nb, st);
+    k_box_partials<<<(unsigned)nb, 256, 0, st>>>(h.bound.p, n, part.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    std::vector<float4> hp((size_t)nb);
+    CRG_CHECK_CUDA(cudaMemcpyAsync(hp.data(), part.p, sizeof(float4) * nb, cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    float4 gb = make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
+    for (auto& b : hp) {
+      gb.x = std::min(gb.x, b.x); gb.y = std::min(gb.y, b.y);
+      gb.z = std::max(gb.z, b.z); gb.w = std::max(gb.w, b.w);
+    }
+    k_planar_keys<<<nblk(n, 256), 256, 0, st>>>(h.bound.p, n, gb, h.key.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  // counting sort by the top key bits, then sort inside bins
+  const int64_t nbins = ((int64_t)1 << (32 - kSortShift));
+  DBuf<int32_t> cnt((size_t)nbins + 1, st), fill((size_t)nbins, st);
+  cnt.zero();
+  fill.zero();
+  k_hist<<<nblk(n, 256), 256, 0, st>>>(h.key.p, n, kSortShift, cnt.p);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  exclusive_scan_i32(cnt.p, cnt.p, nbins, st);
+  h.perm.alloc((size_t)n, st);
+  k_bin_scatter<<<nblk(n, 256), 256, 0, st>>>(h.key.p, n, kSortShift, cnt.p, fill.p, h.perm.p);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  k_bin_sort<<<nblk(nbins, 256), 256, 0, st>>>(h.key.p, cnt.p, nbins, h.perm.p);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  // hierarchy
+  int64_t nleaves = (n + kLeaf - 1) / kLeaf;
+  int64_t total = 0;
+  int nlev = 0;
+  for (int64_t c = nleaves;; c = (c + 1) / 2) {
+    CRG_REQUIRE(nlev < kMaxLevels, CRG_ERR_INTERNAL, "hierarchy too deep");
+    h.t.off[nlev] = total;
+    h.t.cnt[nlev] = c;
+    total += c;
+    nlev++;
+    if (c == 1) break;
+  }
+  h.t.nlev = nlev;
+  CRG_REQUIRE(nleaves < ((int64_t)1 << 27), CRG_ERR_NOT_SUPPORTED, "too many cells for the hierarchy");
+  h.lo.alloc((size_t)total, st);
+  h.hi.alloc((size_t)total, st);
+  h.sbound.alloc((size_t)n, st);
+  if (sph)
+    k_leaves<true><<<nblk(nleaves, 128), 128, 0, st>>>(h.bound.p, h.perm.p, n, nleaves, h.lo.p, h.hi.p, h.sbound.p);
+  else
+    k_leaves<false><<<nblk(nleaves, 128), 128, 0, st>>>(h.bound.p, h.perm.p, n, nleaves, h.lo.p, h.hi.p, h.sbound.p);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  for (int l = 1; l < nlev; ++l) {
+    k_level_up<<<nblk(h.t.cnt[l], 256), 256, 0, st>>>(h.lo.p + h.t.off[l - 1], h.hi.p + h.t.off[l - 1], h.t.cnt[l - 1],
+                                                    h.lo.p + h.t.off[l], h.hi.p + h.t.off[l], h.t.cnt[l]);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  h.t.lo = h.lo.p;
+  h.t.hi = h.hi.p;
+  h.t.sbound = h.sbound.p;
+  h.t.perm = h.perm.p;
+}
+
+TreeView view_of(const Tree& t) {
+  TreeView v{};
+  for (int l = 0; l < kMaxLevels; ++l) { v.off[l] = t.off[l]; v.cnt[l] = t.cnt[l]; }
+  v.lo = t.lo;
+  v.hi = t.hi;
+  return v;
+}
+
+// K3 host loop.  Returns the candidate list (dst cell, src cell).
+void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& cand, int64_t& ncand, cudaStream_t st) {
+  ncand = 0;
+  if (D.t.ncells == 0 || S.t.ncells == 0) return;
+  TreeView tv_d = view_of(D.t), tv_s = view_of(S.t);
+  DBuf<unsigned long long> counters(2, st);
+  DBuf<uint2> front, next, leafp;
+  size_t front_cap = 1024, leaf_cap = 1 << 16;
+  front.alloc(front_cap, st);
+  next.alloc(front_cap * 4, st);
+  leafp.alloc(leaf_cap, st);
+  int64_t nleaf = 0;
+  uint2 root = make_uint2(((uint32_t)(D.t.nlev - 1) << 27), ((uint32_t)(S.t.nlev - 1) << 27));
+  int64_t nfront = 1;
+  if (D.t.nlev == 1 && S.t.nlev == 1) {
+    CRG_CHECK_CUDA(cudaMemcpyAsync(leafp.p, &root, sizeof(uint2), cudaMemcpyHostToDevice, st));
+    nleaf = 1;
+    nfront = 0;
+  } else {
+    CRG_CHECK_CUDA(cudaMemcpyAsync(front.p, &root, sizeof(uint2), cudaMemcpyHostToDevice, st));
+  }
+  while (nfront > 0) {
+    if (next.n < (size_t)nfront * 4) next.alloc((size_t)nfront * 8, st);
+    if (leafp.n < (size_t)(nleaf + nfront * 4)) {
+      DBuf<uint2> bigger((size_t)(nleaf + nfront * 4) * 2, st);
+      if (nleaf) CRG_CHECK_CUDA(cudaMemcpyAsync(bigger.p, leafp.p, sizeof(uint2) * nleaf, cudaMemcpyDeviceToDevice, st));
+      std::swap(bigger.p, leafp.p);
+      std::swap(bigger.n, leafp.n);
+    }
+    unsigned long long hc[2] = {0ull, (unsigned long long)nleaf};
+    CRG_CHECK_CUDA(cudaMemcpyAsync(counters.p, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
+    int64_t blocks = std::min<int64_t>(nblk(nfront, 256), 152 * 16);
+    k_traverse<<<(unsigned)blocks, 256, 0, st>>>(front.p, nfront, tv_d, tv_s, next.p, counters.p, leafp.p, counters.p + 1);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    CRG_CHECK_CUDA(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    nfront = (int64_t)hc[0];
+    nleaf = (int64_t)hc[1];
+    std::swap(front.p, next.p);
+    std::swap(front.n, next.n);
+  }
+  if (nleaf == 0) return;
+  DBuf<int32_t> cnt((size_t)nleaf + 1, st);
+  if (sph)
+    k_leaf_count<true><<<nblk(nleaf, 128), 128, 0, st>>>(leafp.p, nleaf, D.t.sbound, D.t.ncells, S.t.sbound, S.t.ncells, cnt.p);
+  else
+    k_leaf_count<false><<<nblk(nleaf, 128), 128, 0, st>>>(leafp.p, nleaf, D.t.sbound, D.t.ncells, S.t.sbound, S.t.ncells, cnt.p);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  exclusive_scan_i32(cnt.p, cnt.p, nleaf, st);
+  int32_t tot = 0;
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&tot, cnt.p + nleaf, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  CRG_REQUIRE(tot >= 0, CRG_ERR_NOT_SUPPORTED, "candidate count overflows int32");
+  ncand = tot;
+  cand.alloc((size_t)(tot > 0 ? tot : 1), st);
+  if (tot == 0) return;
+  if (sph)
+    k_leaf_emit<true><<<nblk(nleaf, 128), 128, 0, st>>>(leafp.p, nleaf, D.t.sbound, D.t.perm, D.t.ncells, S.t.sbound,
+                                                       S.t.perm, S.t.ncells, cnt.p, cand.p);
+  else
+    k_leaf_emit<false><<<nblk(nleaf, 128), 128, 0, st>>>(leafp.p, nleaf, D.t.sbound, D.t.perm, D.t.ncells, S.t.sbound,
+                                                        S.t.perm, S.t.ncells, cnt.p, cand.p);
+  CRG_CHECK_CUDA(cudaGetLastError());
+}
+
+struct Events {
+  cudaEvent_t e[5] = {};
+  Events() {
+    for (auto& x : e) CRG_CHECK_CUDA(cudaEventCreate(&x));
+  }
+  ~Events() {
+    for (auto& x : e) if (x) cudaEventDestroy(x);
+  }
+};
+
+}  // namespace
+
+bool is_device_pointer(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+void free_csr(DevCsr& c) {
+  cudaFree(c.ptr); cudaFree(c.idx); cudaFree(c.val); cudaFree(c.val32); cudaFree(c.wn32); cudaFree(c.adj32);
+  c = DevCsr{};
+}
+
+void free_regridder(crg_regridder* r) {
+  if (!r) return;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaSetDevice(r->device);
+  free_csr(r->fwd);
+  free_csr(r->rev);
+  cudaFree(r->dst_area);
+  cudaFree(r->src_area);
+  cudaFree(r->row_sum);
+  cudaFree(r->col_sum);
+  if (r->stage) cudaFree(r->stage);
+  cudaSetDevice(dev);
+  delete r;
+}
+
+crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts) {
+  CRG_REQUIRE(dst && src, CRG_ERR_INVALID_ARGUMENT, "dst and src grids must not be NULL");
+  CRG_REQUIRE(dst->manifold == src->manifold, CRG_ERR_INVALID_ARGUMENT,
+              "Destination and source manifolds must be the same (got %d and %d); promote planar lon/lat to the sphere first",
+              dst->manifold, src->manifold);
+  CRG_REQUIRE(!opts || opts->flags == 0, CRG_ERR_INVALID_ARGUMENT, "crg_build_opts.flags must be 0");
+  const bool sph = dst->manifold == CRG_SPHERICAL;
+  cudaStream_t st = opts ? (cudaStream_t)opts->stream : nullptr;
+  const int normalize = opts ? opts->normalize : 0;
+
+  crg_regridder* R = new crg_regridder();
+  try {
+    CRG_CHECK_CUDA(cudaGetDevice(&R->device));
+    R->manifold = dst->manifold;
+    Events ev;
+    CRG_CHECK_CUDA(cudaEventRecord(ev.e[0], st));
+
+    DevGrid gd, gs;
+    upload_grid(dst, gd, st);
+    upload_grid(src, gs, st);
+    const int64_t nd = gd.ncells, ns = gs.ncells;
+    R->nd = nd;
+    R->ns = ns;
+    R->dst_area = persistent_alloc<double>((size_t)nd);
+    R->src_area = persistent_alloc<double>((size_t)ns);
+
+    HostTree td, ts;
+    build_tree(gd, sph, R->dst_area, td, st);
+    build_tree(gs, sph, R->src_area, ts, st);
+    DBuf<int2> cand;
+    int64_t nc = 0;
+    dual_traverse(td, ts, sph, cand, nc, st);
+    R->ncand = nc;
+    CRG_CHECK_CUDA(cudaEventRecord(ev.e[1], st));
+
+    // K4
+    DBuf<double> area((size_t)(nc > 0 ? nc : 1), st);
+    DBuf<int32_t> rowcnt((size_t)nd + 1, st), colcnt((size_t)ns + 1, st);
+    DBuf<unsigned long long> ovf(1, st);
+    rowcnt.zero();
+    colcnt.zero();
+    ovf.zero();
+    if (nc) {
+      if (sph)
+        k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.maxv, gs.tab.v, gs.tab.nv,
+                                                    gs.tab.maxv, area.p, rowcnt.p, colcnt.p, ovf.p);
+      else
+        k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.maxv, gs.tab.v, gs.tab.nv,
+                                                     gs.tab.maxv, area.p, rowcnt.p, colcnt.p, ovf.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    CRG_CHECK_CUDA(cudaEventRecord(ev.e[2], st));
+
+    // K5
+    R->fwd.nrows = nd; R->fwd.ncols = ns;
+    R->rev.nrows = ns; R->rev.ncols = nd;
+    R->fwd.ptr = persistent_alloc<int32_t>((size_t)nd + 1);
+    R->rev.ptr = persistent_alloc<int32_t>((size_t)ns + 1);
+    exclusive_scan_i32(rowcnt.p, R->fwd.ptr, nd, st);
+    exclusive_scan_i32(colcnt.p, R->rev.ptr, ns, st);
+    int32_t hnnz = 0;
+    unsigned long long hovf = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hnnz, R->fwd.ptr + nd, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hovf, ovf.p, sizeof(hovf), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    CRG_REQUIRE(hovf == 0, CRG_ERR_GEOMETRY,
+                "%llu candidate pairs exceeded the clipped-polygon capacity of %d vertices (non-convex cells?)",
+                (unsigned long long)hovf, CRG_MAXC);
+    const int64_t nnz = hnnz;
+    R->nnz = nnz;
+    R->fwd.nnz = R->rev.nnz = nnz;
+    R->fwd.idx = persistent_alloc<int32_t>((size_t)nnz);
+    R->fwd.val = persistent_alloc<double>((size_t)nnz);
+    R->rev.idx = persistent_alloc<int32_t>((size_t)nnz);
+    R->rev.val = persistent_alloc<double>((size_t)nnz);
+    rowcnt.zero();
+    colcnt.zero();
+    if (nc) {
+      k_scatter_pairs<<<nblk(nc, 256), 256, 0, st>>>(cand.p, area.p, nc, R->fwd.ptr, rowcnt.p, R->rev.ptr, colcnt.p,
+                                                     R->fwd.idx, R->fwd.val, R->rev.idx, R->rev.val);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (nd) k_row_sort<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, nd, R->fwd.idx, R->fwd.val);
+    if (ns) k_row_sort<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, ns, R->rev.idx, R->rev.val);
+    CRG_CHECK_CUDA(cudaGetLastError());
+
+    // normalize! (regridder.jl:54-62)
+    DBuf<unsigned long long> mx(1, st);
+    mx.zero();
+    if (nnz) {
+      k_max_val<<<(unsigned)std::min<int64_t>(nblk(nnz, 256), 152 * 8), 256, 0, st>>>(R->fwd.val, nnz, mx.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    unsigned long long hmx = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hmx, mx.p, sizeof(hmx), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    double maxA;
+    memcpy(&maxA, &hmx, sizeof(double));
+    R->normalizer = normalize ? maxA : 1.0;
+    R->normalized = normalize;
+    if (normalize) {
+      if (nnz) {
+        k_div_by<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.val, nnz, mx.p);
+        k_div_by<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.val, nnz, mx.p);
+      }
+      if (nd) k_div_by<<<nblk(nd, 256), 256, 0, st>>>(R->dst_area, nd, mx.p);
+      if (ns) k_div_by<<<nblk(ns, 256), 256, 0, st>>>(R->src_area, ns, mx.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    // derived FP32 weights + Kahan sums
+    for (DevCsr* c : {&R->fwd, &R->rev}) {
+      c->val32 = persistent_alloc<float>((size_t)nnz);
+      c->wn32 = persistent_alloc<float>((size_t)nnz);
+      c->adj32 = persistent_alloc<float>((size_t)nnz);
+    }
+    R->row_sum = persistent_alloc<double>((size_t)nd);
+    R->col_sum = persistent_alloc<double>((size_t)ns);
+    if (nd)
+      k_derive<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, R->fwd.idx, R->fwd.val, nd, R->dst_area, R->src_area,
+                                              R->fwd.val32, R->fwd.wn32, R->fwd.adj32, R->row_sum);
+    if (ns)
+      k_derive<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, R->rev.idx, R->rev.val, ns, R->src_area, R->dst_area,
+                                              R->rev.val32, R->rev.wn32, R->rev.adj32, R->col_sum);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    CRG_CHECK_CUDA(cudaEventRecord(ev.e[3], st));
+    CRG_CHECK_CUDA(cudaEventSynchronize(ev.e[3]));
+    float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
+    cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);
+    cudaEventElapsedTime(&t12, ev.e[1], ev.e[2]);
+    cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
+    cudaEventElapsedTime(&t03, ev.e[0], ev.e[3]);
+    crg_info& I = R->info;
+    I.n_dst = nd; I.n_src = ns; I.nnz = nnz; I.n_candidates = nc;
+    I.manifold = R->manifold; I.normalized = normalize;
+    I.normalizer = R->normalizer;
+    I.t_build_ms = t03; I.t_search_ms = t01; I.t_clip_ms = t12; I.t_assemble_ms = t23;
+    I.clip_overflows = (int64_t)hovf;
+    I.device = R->device;
+    // temporaries are freed stream-ordered by the DBuf destructors
+  } catch (...) {
+    free_regridder(R);
+    throw;
+  }
+  return R;
+}
+
+}  // namespace crg

@@ -1,0 +1,87 @@
+// crg_internal.cuh -- internal types shared by the build, apply and ABI units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <atomic>
+#include <mutex>
+#include <string>
+
+#include "crg.h"
+
+namespace crg {
+
+// Sets the thread-local message returned by crg_last_error().
+void set_error(const char* fmt, ...);
+
+struct Fail {
+  crg_status st;
+};
+
+#define CRG_CHECK_CUDA(expr)                                                              \
+  do {                                                                                    \
+    cudaError_t e_ = (expr);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      ::crg::set_error("CUDA error %s (%s) at %s:%d", cudaGetErrorName(e_),               \
+                       cudaGetErrorString(e_), __FILE__, __LINE__);                       \
+      throw ::crg::Fail{e_ == cudaErrorMemoryAllocation ? CRG_ERR_OUT_OF_MEMORY : CRG_ERR_CUDA}; \
+    }                                                                                     \
+  } while (0)
+
+#define CRG_REQUIRE(cond, status, ...)        \
+  do {                                        \
+    if (!(cond)) {                            \
+      ::crg::set_error(__VA_ARGS__);          \
+      throw ::crg::Fail{status};              \
+    }                                         \
+  } while (0)
+
+// Device CSR of one direction.  rows = dst cells for the forward copy,
+// src cells for the reverse copy (A^T).
+struct DevCsr {
+  int64_t nrows = 0, ncols = 0, nnz = 0;
+  int32_t* ptr = nullptr;    // [nrows + 1]
+  int32_t* idx = nullptr;    // [nnz] column indices, ascending in each row
+  double* val = nullptr;     // [nnz] A entries (FP64)
+  float* val32 = nullptr;    // [nnz] A entries (FP32)
+  float* wn32 = nullptr;     // [nnz] A_rc / area_row (FP32): normalised weights of this direction
+  float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
+};
+
+// Per-cell vertex table on the device: [n][maxv] unit vectors (z = 0 planar).
+struct CellTable {
+  int64_t n = 0;
+  int maxv = 0;
+  double* v = nullptr;   // [n * maxv * 3]
+  int8_t* nv = nullptr;  // [n]
+};
+
+}  // namespace crg
+
+struct crg_regridder {
+  std::atomic<int> refs{1};
+  int device = 0;
+  int manifold = CRG_SPHERICAL;
+  int normalized = 0;
+  int64_t nd = 0, ns = 0, nnz = 0, ncand = 0;
+  double normalizer = 1.0;
+  crg::DevCsr fwd;  // CSR of A (rows = dst)
+  crg::DevCsr rev;  // CSR of A^T (rows = src)
+  double* dst_area = nullptr;   // [nd]
+  double* src_area = nullptr;   // [ns]
+  double* row_sum = nullptr;    // [nd] Kahan row sums of A
+  double* col_sum = nullptr;    // [ns] Kahan column sums of A
+  crg_info info{};
+  // staging for host-memory fields in crg_apply
+  std::mutex stage_mu;
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+};
+
+namespace crg {
+// crg_build_impl lives in crg_build.cu; apply entry points in crg_apply.cu.
+crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts);
+void free_regridder(crg_regridder* r);
+void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, const void* src, int64_t ssc,
+                int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int normalize, cudaStream_t st);
+bool is_device_pointer(const void* p);
+}  // namespace crg

@@ -1,0 +1,164 @@
+/*
+ * crg.h -- C ABI of the GB300-native conservative-regridding library.
+ *
+ * This is the drop-in boundary for ConservativeRegridding.jl v0.2.5's two hot
+ * paths.  Each entry point names the reference interface it replaces
+ * (paths relative to the ConservativeRegridding.jl repository).  Plain
+ * pointers and sizes only; no exceptions cross it; every call returns a
+ * crg_status and crg_last_error() gives the message of the last failure on
+ * the calling thread.
+ *
+ * Index conventions.  Cells are numbered from 0.  A curvilinear block with
+ * nx x ny cells has (nx+1) x (ny+1) points stored i-fastest; cell (i, j) has
+ * index block_offset + i + j*nx and the ring p(i,j), p(i+1,j), p(i+1,j+1),
+ * p(i,j+1) -- the reference's CellBasedGrid (src/trees/grids.jl:71-85) and
+ * cartesian_to_linear_idx (src/trees/interfaces.jl:241-243) shifted to
+ * 0-based, with blocks laid out like the cubed-sphere face offsets
+ * (ext/ConservativeRegriddingClimaCoreExt.jl:56-61).
+ *
+ * Field layout.  A field array holds nfields fields of n cells; element
+ * (cell c, field f) is at base[c*stride_cell + f*stride_field] (in elements).
+ * stride_cell = 1 is the reference's dims=1 N-D layout; stride_field = 1
+ * puts the fields of one cell side by side (dims = last).
+ */
+#ifndef CRG_H
+#define CRG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CRG_ABI_VERSION 1
+
+typedef enum {
+    CRG_OK = 0,
+    CRG_ERR_INVALID_ARGUMENT = 1,   /* reference: ArgumentError (src/regridder/regrid.jl:242-245) */
+    CRG_ERR_DIMENSION_MISMATCH = 2, /* reference: DimensionMismatch (src/regridder/regrid.jl:289-296) */
+    CRG_ERR_CUDA = 3,
+    CRG_ERR_OUT_OF_MEMORY = 4,
+    CRG_ERR_NOT_SUPPORTED = 5,
+    CRG_ERR_GEOMETRY = 6,           /* a clipped polygon exceeded its vertex capacity (non-convex input) */
+    CRG_ERR_INTERNAL = 7
+} crg_status;
+
+typedef enum { CRG_PLANAR = 0, CRG_SPHERICAL = 1 } crg_manifold;
+typedef enum { CRG_GRID_CURVILINEAR = 0, CRG_GRID_CELLS = 1 } crg_grid_kind;
+typedef enum { CRG_F64 = 0, CRG_F32 = 1, CRG_BF16 = 2 } crg_dtype;
+
+/* A grid of convex cells.  Pointers may be host or device memory (detected).
+ * Spherical coordinates are unit vectors (x, y, z); planar ones are (x, y).
+ * Replaces the grids the reference turns into trees with Trees.treeify
+ * (src/trees/interfaces.jl:94-129): vertex matrices (CellBasedGrid,
+ * TopDownQuadtreeCursor), cubed-sphere faces (CubedSphereToplevelTree,
+ * src/trees/wrappers.jl:140-159) and per-cell polygons (HEALPix pixels,
+ * ext/ConservativeRegriddingHealpixExt.jl:159-167; FlatNoTree polygon lists). */
+typedef struct crg_grid_desc {
+    int32_t kind;               /* crg_grid_kind */
+    int32_t manifold;           /* crg_manifold */
+    int32_t nblocks;            /* CURVILINEAR: number of blocks, 1..12 */
+    int32_t max_verts;          /* CELLS: vertex slots per cell, 3..8 */
+    int64_t ncells;             /* total number of cells */
+    const int64_t* block_nx;    /* CURVILINEAR: [nblocks] cells along i (host memory) */
+    const int64_t* block_ny;    /* CURVILINEAR: [nblocks] cells along j (host memory) */
+    const double* points;       /* CURVILINEAR: blocks back to back, (nx+1)*(ny+1) points each, i fastest */
+    const double* cell_verts;   /* CELLS: [ncells][max_verts][dim] in ring order (not closed) */
+    const int32_t* cell_nverts; /* CELLS: [ncells] vertex counts, or NULL when all are max_verts */
+} crg_grid_desc;
+
+typedef struct crg_build_opts {
+    int32_t normalize;  /* divide A and both area vectors by maximum(A): normalize!(::Regridder),
+                           src/regridder/regridder.jl:54-62 (the reference's keyword default is false) */
+    int32_t flags;      /* reserved, must be 0 */
+    void* stream;       /* cudaStream_t for the build; NULL = legacy default stream */
+} crg_build_opts;
+
+typedef struct crg_regridder crg_regridder;
+
+typedef struct crg_info {
+    int64_t n_dst, n_src, nnz, n_candidates;
+    int32_t manifold, normalized;
+    double normalizer;       /* maximum(A) before normalisation (1.0 when not normalised) */
+    double t_build_ms;       /* wall time of crg_build on the stream (CUDA events) */
+    double t_search_ms;      /* caps, ordering, hierarchy and dual traversal */
+    double t_clip_ms;        /* per-pair clip + area */
+    double t_assemble_ms;    /* CSR/CSC assembly, areas, normalisation, weight derivation */
+    int64_t clip_overflows;  /* pairs whose clip exceeded the vertex capacity */
+    int32_t device;
+    int32_t pad;
+} crg_info;
+
+/* Build the regridder from `src` to `dst`.
+ * Replaces Regridder(dst, src; normalize) (src/regridder/regridder.jl:105-163):
+ * candidate search (src/regridder/intersection_areas.jl:48-65, :67-122), the
+ * per-pair DefaultIntersectionOperator (src/regridder/regridder.jl:96-103),
+ * SparseArrays.sparse assembly (src/regridder/intersection_areas.jl:115-121),
+ * per-cell areas (src/regridder/regridder.jl:165-178) and normalize!.
+ * Mixed planar/spherical inputs are rejected: promote on the host, as the
+ * reference's Regridder(dst, src) does (src/regridder/regridder.jl:109-117). */
+crg_status crg_build(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
+                     crg_regridder** out);
+
+/* Reference counting: transpose(R) (src/regridder/regridder.jl:49-50) shares
+ * the same arrays; a host wrapper that hands out a transposed view retains the
+ * handle and releases it when the view dies.  The last release frees it. */
+crg_status crg_regridder_retain(crg_regridder* r);
+crg_status crg_regridder_release(crg_regridder* r);
+
+crg_status crg_regridder_info(const crg_regridder* r, crg_info* out);
+
+/* dst = (A src) ./ a_d  (transpose = 0)   or   dst = (A^T src) ./ a_s  (transpose = 1);
+ * without the division when normalize = 0.
+ * Replaces regrid!(dst, R, src; dims) with its pipeline extract/initialize/
+ * perform_regridding!/finalize_regridding! (src/regridder/regrid.jl:63-118),
+ * the N-D NDSliceLoop one-mul!-per-slice loop (src/regridder/regrid.jl:225-318)
+ * by a single SpMM over all fields, and regrid!(dst, transpose(R), src).
+ * dtype CRG_F64 accumulates in FP64 in the reference's summation order;
+ * CRG_F32 / CRG_BF16 read FP32 weights and accumulate in FP32.
+ * src and dst may be host or device pointers; host buffers are staged through
+ * device memory on `stream`, which the call synchronises before returning. */
+crg_status crg_apply(const crg_regridder* r, int32_t transpose, int32_t dtype,
+                     const void* src, int64_t src_stride_cell, int64_t src_stride_field,
+                     void* dst, int64_t dst_stride_cell, int64_t dst_stride_field,
+                     int64_t nfields, int32_t normalize, void* stream);
+
+/* Adjoint of crg_apply with the same arguments: given gdst = dL/d(dst), write
+ * gsrc = dL/d(src) = A^T (gdst ./ a_d) (transpose = 0), or A (gdst ./ a_s)
+ * (transpose = 1); without the division when normalize = 0.  It reads the
+ * opposite-direction copy of A, so no atomics are needed.  The reference has
+ * no derivative rules (Project.toml has no ChainRulesCore); this is the
+ * backward of regrid! for an rrule. */
+crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t dtype,
+                             const void* gdst, int64_t gdst_stride_cell, int64_t gdst_stride_field,
+                             void* gsrc, int64_t gsrc_stride_cell, int64_t gsrc_stride_field,
+                             int64_t nfields, int32_t normalize, void* stream);
+
+/* Copy A out as CSC (rows = dst cells, columns = src cells), i.e. the
+ * reference's R.intersections::SparseMatrixCSC (src/regridder/regridder.jl:25-36)
+ * with rows ascending inside each column.  index_base 1 gives Julia's 1-based
+ * colptr/rowval.  Host or device destination pointers; colptr has n_src+1
+ * entries, rowval and nzval have nnz. */
+crg_status crg_get_csc(const crg_regridder* r, int32_t index_base, int64_t* colptr, int64_t* rowval, double* nzval);
+
+/* The same matrix as CSR (rows = dst cells, columns ascending in each row). */
+crg_status crg_get_csr(const crg_regridder* r, int32_t index_base, int64_t* rowptr, int64_t* colval, double* nzval);
+
+/* Per-cell areas R.dst_areas and R.src_areas (src/regridder/regridder.jl:149-150),
+ * divided by the normaliser when the regridder was built with normalize. */
+crg_status crg_get_areas(const crg_regridder* r, double* dst_areas, double* src_areas);
+
+/* Kahan-summed row sums (length n_dst) and column sums (length n_src) of A:
+ * the quantities the reference's area-agreement test compares with the cell
+ * areas (lib/ConservativeRegriddingTestHelpers/src/ConservativeRegriddingTestHelpers.jl:70-73). */
+crg_status crg_get_row_col_sums(const crg_regridder* r, double* row_sums, double* col_sums);
+
+const char* crg_last_error(void);
+const char* crg_status_string(crg_status s);
+int32_t crg_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CRG_H */

@@ -1,0 +1,1155 @@
+/*
+ * crg_oracle.c -- CPU oracle for the conservative-regridding hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: tests/, the smoke
+ * check in __graft_entry__.py and the cpu_baseline / reference legs of
+ * bench.py load it; the product library never links, includes or calls it.
+ *
+ * It restates, in plain C, what ConservativeRegridding.jl v0.2.5 does when it
+ * builds and applies a regridder on the sphere (or the plane):
+ *
+ *   Regridder(dst, src; normalize)            src/regridder/regridder.jl:105-163
+ *     treeify -> TopDownQuadtreeCursor /      src/trees/interfaces.jl:94-129
+ *                Healpix tree / cubed sphere  ext/ConservativeRegriddingHealpixExt.jl:18-175,
+ *                                             src/trees/wrappers.jl:140-159
+ *     candidate search (threaded dual DFS)    src/utils/MultithreadedDualDepthFirstSearch.jl:12-65
+ *       + GeometryOps STI.dual_depth_first_search (third party, restated below)
+ *     bounding caps                           src/trees/grids.jl:245-287
+ *     per-pair clip + area, keep area > 0     src/regridder/intersection_areas.jl:4-32,
+ *                                             src/regridder/regridder.jl:96-103
+ *     SparseArrays.sparse(i_dst,i_src,a)      src/regridder/intersection_areas.jl:115-121
+ *     per-cell areas, normalize! by max(A)    src/regridder/regridder.jl:54-62,165-178
+ *   regrid!(dst, R, src) = (A*s) ./ a_d       src/regridder/regrid.jl:63-118
+ *   transpose(R)                              src/regridder/regridder.jl:49-50
+ *
+ * The polygon arithmetic itself lives in GeometryOps.jl (compat 0.1.33, not
+ * vendored with the reference).  It is restated here from published methods:
+ *   - Sutherland & Hodgman (1974) re-entrant convex polygon clipping, with
+ *     great-circle half-spaces s(x) = n.(x - a), n = a x (b - a) = a x b, on
+ *     the sphere (differences first, so short edges keep full precision);
+ *   - the arc/plane crossing point x = |s_a| b + |s_b| a (both weights >= 0);
+ *   - polygon solid angle as the sum over a vertex fan of the triangle solid
+ *     angles of Van Oosterom & Strackee (1983), tan(W/2) = N / D with
+ *     N = a.((b-a) x (c-a)), accumulated as the argument of the product of
+ *     the complex numbers D + iN; orientation = sign of the fan sum of N;
+ *   - arctangent by octant/pi-8 range reduction and the Maclaurin series
+ *     atan t = sum (-1)^k t^(2k+1)/(2k+1) (Abramowitz & Stegun 4.4.42);
+ *   - HEALPix pixel corners from the face/ring geometry of Gorski et al. (2005),
+ *     ApJ 622:759.
+ * The clip/area arithmetic follows a fixed operation order with explicit fma()
+ * and is compiled with -ffp-contract=off, so an independent coding of the same
+ * sequence (the CUDA kernels) reproduces it bit for bit.
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define OG_MAXV 8   /* max vertices of an input cell */
+#define OG_MAXC 24  /* capacity of a clipped polygon */
+
+typedef struct { double x, y, z; } v3;
+
+/* ------------------------------------------------------------------------ */
+/* Exact-order arithmetic (shared spec with the device code).               */
+/* ------------------------------------------------------------------------ */
+
+static inline double og_dot(v3 a, v3 b) { return fma(a.x, b.x, fma(a.y, b.y, a.z * b.z)); }
+
+/* Plain products (no fma): a x a and a x 0 are exactly zero. */
+static inline v3 og_cross(v3 a, v3 b) {
+    v3 r;
+    r.x = a.y * b.z - a.z * b.y;
+    r.y = a.z * b.x - a.x * b.z;
+    r.z = a.x * b.y - a.y * b.x;
+    return r;
+}
+
+/* ---- exact signs (error-free transformations, Shewchuk 1997) ---- */
+
+static inline void og_two_prod(double a, double b, double* p, double* e) { *p = a * b; *e = fma(a, b, -*p); }
+static inline void og_two_sum(double a, double b, double* s, double* e) {
+    double x = a + b, bv = x - a, av = x - bv;
+    *e = (a - av) + (b - bv);
+    *s = x;
+}
+
+/* Exact sign of t[0] + ... + t[n-1]: grow a non-overlapping expansion with
+ * zero elimination; its largest component carries the sign. */
+static int og_exact_sign(const double* t, int n) {
+    double e[32];
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+        double q = t[i];
+        int k = 0;
+        for (int j = 0; j < m; ++j) {
+            double sm, h;
+            og_two_sum(q, e[j], &sm, &h);
+            if (h != 0.0) e[k++] = h;
+            q = sm;
+        }
+        if (q != 0.0) e[k++] = q;
+        m = k;
+    }
+    return m == 0 ? 0 : (e[m - 1] > 0.0 ? 1 : -1);
+}
+
+/* exact p*q*r as four doubles */
+static inline void og_prod3(double p, double q, double r, double sg, double* t) {
+    double s1, e1;
+    og_two_prod(p, q, &s1, &e1);
+    og_two_prod(s1, r, &t[0], &t[1]);
+    og_two_prod(e1, r, &t[2], &t[3]);
+    for (int k = 0; k < 4; ++k) t[k] *= sg;
+}
+
+/* sign of det[a; b; c] = a.(b x c), exactly */
+static int og_det3_sign(v3 a, v3 b, v3 c) {
+    double t[24];
+    og_prod3(a.x, b.y, c.z, 1.0, t + 0);
+    og_prod3(a.x, b.z, c.y, -1.0, t + 4);
+    og_prod3(a.y, b.z, c.x, 1.0, t + 8);
+    og_prod3(a.y, b.x, c.z, -1.0, t + 12);
+    og_prod3(a.z, b.x, c.y, 1.0, t + 16);
+    og_prod3(a.z, b.y, c.x, -1.0, t + 20);
+    return og_exact_sign(t, 24);
+}
+
+/* sign of (bx-ax)(vy-ay) - (by-ay)(vx-ax), exactly */
+static int og_orient2_sign(double ax, double ay, double bx, double by, double vx, double vy) {
+    double d[4][2];
+    og_two_sum(bx, -ax, &d[0][0], &d[0][1]);
+    og_two_sum(vy, -ay, &d[1][0], &d[1][1]);
+    og_two_sum(by, -ay, &d[2][0], &d[2][1]);
+    og_two_sum(vx, -ax, &d[3][0], &d[3][1]);
+    double t[16];
+    int n = 0;
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            og_two_prod(d[0][i], d[1][j], &t[n], &t[n + 1]);
+            n += 2;
+        }
+    for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) {
+            og_two_prod(d[2][i], d[3][j], &t[n], &t[n + 1]);
+            t[n] = -t[n];
+            t[n + 1] = -t[n + 1];
+            n += 2;
+        }
+    return og_exact_sign(t, 16);
+}
+
+#define OG_U32 3.552713678800501e-15  /* 32 * 2^-53 */
+#define OG_U8 8.881784197001252e-16   /* 8 * 2^-53 */
+#define OG_TINY 1e-290
+
+/* Decide the side value: keep the FP64 estimate s when it clears the error
+ * bound, otherwise take the exact sign (0 -> exactly on the line). */
+static inline double og_settle(double s, double bound, int exact_sign) {
+    if (fabs(s) > bound) return s;
+    if (exact_sign == 0) return 0.0;
+    double m = fmax(fabs(s), 2.2250738585072014e-308);
+    return exact_sign > 0 ? m : -m;
+}
+
+static const double OG_ATAN_C[20] = {
+    1.0, 0.3333333333333333, 0.2, 0.14285714285714285, 0.1111111111111111,
+    0.09090909090909091, 0.07692307692307693, 0.06666666666666667, 0.058823529411764705,
+    0.05263157894736842, 0.047619047619047616, 0.043478260869565216, 0.04,
+    0.037037037037037035, 0.034482758620689655, 0.03225806451612903, 0.030303030303030304,
+    0.02857142857142857, 0.02702702702702703, 0.02564102564102564};
+/* OG_ATAN_TH[n]: largest t^2 for which the terms k = 0..n reach 2^-56 relative. */
+static const double OG_ATAN_TH[20] = {
+    4.163336342344337e-17, 8.33000234328132e-09, 4.596981552458248e-06, 0.0001057159916729051,
+    0.0006866613224549, 0.0023770807360687612, 0.005751393360079481, 0.011132588223807069,
+    0.018578395538006495, 0.02795464321653044, 0.039019086539122956, 0.051485905388814555,
+    0.06506692879763946, 0.07949448812181649, 0.09453198900334307, 0.10997706781109234,
+    0.12566065265206888, 0.1414440078610017, 0.15721498531213599, 0.17288416032961332};
+
+#define OG_TAN_PI_8 0.41421356237309503
+#define OG_PI_4 0.7853981633974483
+#define OG_PI_2 1.5707963267948966
+#define OG_PI 3.141592653589793
+
+/* atan(t) for |t| <= tan(pi/8): Maclaurin series, Horner in z = t^2. */
+static double og_atan_series(double t) {
+    double z = t * t;
+    int n = 0;
+    while (n < 19 && z > OG_ATAN_TH[n]) n++;
+    double p = OG_ATAN_C[n];
+    for (int k = n - 1; k >= 0; --k) p = fma(p, -z, OG_ATAN_C[k]);
+    return t * p;
+}
+
+/* atan2 by octant reduction: |y|<=|x| swap, then t>tan(pi/8) -> (t-1)/(t+1) + pi/4. */
+double og_atan2(double y, double x) {
+    double ay = fabs(y), ax = fabs(x);
+    int swap = ay > ax;
+    double num = swap ? ax : ay, den = swap ? ay : ax;
+    if (den == 0.0) return 0.0;
+    double t = num / den;
+    double r;
+    if (t > OG_TAN_PI_8) {
+        double u = (t - 1.0) / (t + 1.0);
+        r = OG_PI_4 + og_atan_series(u);
+    } else {
+        r = og_atan_series(t);
+    }
+    if (swap) r = OG_PI_2 - r;
+    if (x < 0.0) r = OG_PI - r;
+    if (y < 0.0) r = -r;
+    return r;
+}
+
+/* ---- spherical clip + area ---- */
+
+static inline v3 og_sub(v3 a, v3 b) { v3 r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+
+/* Triple product a.((b-a) x (c-a)) = a.(b x c), evaluated in the frame of a so
+ * that tiny triangles keep full relative precision. */
+static inline double og_triple(v3 a, v3 b, v3 c) { return og_dot(a, og_cross(og_sub(b, a), og_sub(c, a))); }
+
+/* Orientation: sign of the fan sum of triple products (+1 counter-clockwise
+ * seen from outside the sphere). */
+static double og_orient_sph(const v3* c, int n) {
+    double s = 0.0;
+    for (int k = 1; k + 1 < n; ++k) s = s + og_triple(c[0], c[k], c[k + 1]);
+    return s >= 0.0 ? 1.0 : -1.0;
+}
+
+static inline v3 og_isect_sph(v3 a, double sa, v3 b, double sb) {
+    if (sa == 0.0) return a;
+    if (sb == 0.0) return b;
+    double wa = fabs(sb), wb = fabs(sa);
+    v3 x;
+    x.x = fma(wb, b.x, wa * a.x);
+    x.y = fma(wb, b.y, wa * a.y);
+    x.z = fma(wb, b.z, wa * a.z);
+    double r = sqrt(og_dot(x, x));
+    x.x = x.x / r; x.y = x.y / r; x.z = x.z / r;
+    return x;
+}
+
+/* Side of v w.r.t. the great circle through ca, cb: FP64 value of
+ * n.(v - ca) (n = ca x (cb - ca), pre-signed by the clip orientation) with an
+ * exact sign whenever |value| <= eb * |v - ca|_1. */
+static inline double og_side_sph(v3 nrm, v3 ca, v3 cb, double eb, int isig, v3 v) {
+    v3 w = og_sub(v, ca);
+    double s = og_dot(nrm, w);
+    double bound = eb * (fabs(w.x) + fabs(w.y) + fabs(w.z)) + OG_TINY;
+    if (fabs(s) > bound) return s;
+    return og_settle(s, bound, isig * og_det3_sign(ca, cb, v));
+}
+
+/* Clip convex `subj` by convex `clip` (Sutherland-Hodgman); returns vertex
+ * count, or -1 on capacity overflow. */
+static int og_clip_sph(const v3* subj, int ns, const v3* clip, int nc, v3* res) {
+    v3 ba[OG_MAXC], bb[OG_MAXC];
+    v3* in = ba; v3* out = bb;
+    for (int i = 0; i < ns; ++i) in[i] = subj[i];
+    int n = ns;
+    double sig = og_orient_sph(clip, nc);
+    for (int k = 0; k < nc && n > 0; ++k) {
+        /* half-space of edge c_k -> c_k+1: n = c_k x (c_k+1 - c_k), s(v) = n.(v - c_k) */
+        v3 ck = clip[k], ck1 = clip[(k + 1) % nc];
+        v3 d1 = og_sub(ck1, ck);
+        v3 nrm = og_cross(ck, d1);
+        if (sig < 0.0) { nrm.x = -nrm.x; nrm.y = -nrm.y; nrm.z = -nrm.z; }
+        int isig = sig < 0.0 ? -1 : 1;
+        double eb = OG_U32 * (fabs(ck.x) + fabs(ck.y) + fabs(ck.z)) * (fabs(d1.x) + fabs(d1.y) + fabs(d1.z));
+        int m = 0;
+        v3 prev = in[n - 1];
+        double sp = og_side_sph(nrm, ck, ck1, eb, isig, prev);
+        for (int i = 0; i < n; ++i) {
+            v3 cur = in[i];
+            double sc = og_side_sph(nrm, ck, ck1, eb, isig, cur);
+            if (sc >= 0.0) {
+                if (sp < 0.0) { if (m >= OG_MAXC) return -1; out[m++] = og_isect_sph(prev, sp, cur, sc); }
+                if (m >= OG_MAXC) return -1;
+                out[m++] = cur;
+            } else if (sp >= 0.0) {
+                if (m >= OG_MAXC) return -1;
+                out[m++] = og_isect_sph(prev, sp, cur, sc);
+            }
+            prev = cur; sp = sc;
+        }
+        v3* t = in; in = out; out = t;
+        n = m;
+    }
+    for (int i = 0; i < n; ++i) res[i] = in[i];
+    return n;
+}
+
+/* Signed solid angle of a polygon (fan from vertex 0). */
+static double og_area_sph_signed(const v3* v, int m) {
+    if (m < 3) return 0.0;
+    double re = 1.0, im = 0.0;
+    v3 a = v[0];
+    for (int k = 1; k + 1 < m; ++k) {
+        v3 b = v[k], c = v[k + 1];
+        double N = og_triple(a, b, c);
+        double D = ((1.0 + og_dot(a, b)) + og_dot(b, c)) + og_dot(c, a);
+        double re2 = fma(re, D, -(im * N));
+        double im2 = fma(re, N, im * D);
+        re = re2; im = im2;
+    }
+    return 2.0 * og_atan2(im, re);
+}
+
+/* ---- planar clip + area (z ignored) ---- */
+
+static inline double og_cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
+
+static double og_area_pl_signed(const v3* v, int m);
+static double og_orient_pl(const v3* c, int n) { return og_area_pl_signed(c, n) >= 0.0 ? 1.0 : -1.0; }
+
+static inline v3 og_isect_pl(v3 a, double sa, v3 b, double sb) {
+    if (sa == 0.0) return a;
+    if (sb == 0.0) return b;
+    double wa = fabs(sb), wb = fabs(sa);
+    double w = wa + wb;
+    v3 x;
+    x.x = fma(wb, b.x, wa * a.x) / w;
+    x.y = fma(wb, b.y, wa * a.y) / w;
+    x.z = 0.0;
+    return x;
+}
+
+/* Side of v w.r.t. the directed line a -> b, signed by the clip orientation,
+ * with an exact sign when the FP64 value is within its error bound. */
+static inline double og_side_pl(v3 a, v3 b, double ex, double ey, int isig, v3 v) {
+    double wx = v.x - a.x, wy = v.y - a.y;
+    double s = og_cross2(ex, ey, wx, wy);
+    if (isig < 0) s = -s;
+    double bound = OG_U8 * (fabs(ex) * fabs(wy) + fabs(ey) * fabs(wx)) + OG_TINY;
+    if (fabs(s) > bound) return s;
+    return og_settle(s, bound, isig * og_orient2_sign(a.x, a.y, b.x, b.y, v.x, v.y));
+}
+
+static int og_clip_pl(const v3* subj, int ns, const v3* clip, int nc, v3* res) {
+    v3 ba[OG_MAXC], bb[OG_MAXC];
+    v3* in = ba; v3* out = bb;
+    for (int i = 0; i < ns; ++i) in[i] = subj[i];
+    int n = ns;
+    double sig = og_orient_pl(clip, nc);
+    for (int k = 0; k < nc && n > 0; ++k) {
+        v3 a = clip[k], b = clip[(k + 1) % nc];
+        double ex = b.x - a.x, ey = b.y - a.y;
+        int isig = sig < 0.0 ? -1 : 1;
+        int m = 0;
+        v3 prev = in[n - 1];
+        double sp = og_side_pl(a, b, ex, ey, isig, prev);
+        for (int i = 0; i < n; ++i) {
+            v3 cur = in[i];
+            double sc = og_side_pl(a, b, ex, ey, isig, cur);
+            if (sc >= 0.0) {
+                if (sp < 0.0) { if (m >= OG_MAXC) return -1; out[m++] = og_isect_pl(prev, sp, cur, sc); }
+                if (m >= OG_MAXC) return -1;
+                out[m++] = cur;
+            } else if (sp >= 0.0) {
+                if (m >= OG_MAXC) return -1;
+                out[m++] = og_isect_pl(prev, sp, cur, sc);
+            }
+            prev = cur; sp = sc;
+        }
+        v3* t = in; in = out; out = t;
+        n = m;
+    }
+    for (int i = 0; i < n; ++i) res[i] = in[i];
+    return n;
+}
+
+/* shoelace formula relative to v[0] */
+static double og_area_pl_signed(const v3* v, int m) {
+    if (m < 3) return 0.0;
+    double s = 0.0;
+    for (int k = 1; k + 1 < m; ++k)
+        s = s + og_cross2(v[k].x - v[0].x, v[k].y - v[0].y, v[k + 1].x - v[0].x, v[k + 1].y - v[0].y);
+    return 0.5 * s;
+}
+
+/* Intersection area of src cell (subject) with dst cell (clip); the reference's
+ * DefaultIntersectionOperator (regridder.jl:96-103) passes (p_src, p_dst).
+ * Returns the area signed by the subject's orientation, so a correct overlap
+ * is positive; *ovf is set on clip capacity overflow. */
+static double og_pair_area(int spherical, const v3* s, int ns, const v3* d, int nd, int* ovf) {
+    v3 res[OG_MAXC];
+    if (spherical) {
+        int m = og_clip_sph(s, ns, d, nd, res);
+        if (m < 0) { *ovf = 1; return 0.0; }
+        return og_area_sph_signed(res, m) * og_orient_sph(s, ns);
+    } else {
+        int m = og_clip_pl(s, ns, d, nd, res);
+        if (m < 0) { *ovf = 1; return 0.0; }
+        return og_area_pl_signed(res, m) * og_orient_pl(s, ns);
+    }
+}
+
+static double og_cell_area(int spherical, const v3* v, int n) {
+    if (spherical) return og_area_sph_signed(v, n) * og_orient_sph(v, n);
+    return og_area_pl_signed(v, n) * og_orient_pl(v, n);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Extents: spherical caps (grids.jl:245-287) and planar boxes.             */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { v3 c; double r; double xmin, xmax, ymin, ymax; } og_ext;
+
+static v3 og_normalize_libm(v3 a) {
+    double n = sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+    v3 r = {a.x / n, a.y / n, a.z / n};
+    return r;
+}
+
+/* GeometryOps spherical_distance: angle between unit vectors. */
+static double og_sdist(v3 a, v3 b) {
+    v3 c = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+    double s = sqrt(c.x * c.x + c.y * c.y + c.z * c.z);
+    double d = a.x * b.x + a.y * b.y + a.z * b.z;
+    return atan2(s, d);
+}
+
+/* GeometryOps UnitSpherical.slerp(a, b, 0.5) in its sin(t W)/sin(W) form:
+ * (sin(W/2)/sin W)(a + b) with W the angle between a and b.  Coincident points
+ * (W = 0, e.g. the repeated pole vertex of a lon-lat pole row) give `a`;
+ * antipodal points give the (near) zero vector, whose spherical_distance to
+ * any centre is atan2(0, 0) = 0. */
+static v3 og_mid(v3 a, v3 b) {
+    double w = og_sdist(a, b);
+    if (w == 0.0) return a;
+    double k = sin(0.5 * w) / sin(w);
+    v3 s = {k * (a.x + b.x), k * (a.y + b.y), k * (a.z + b.z)};
+    return s;
+}
+
+static og_ext og_full_sphere(void) {
+    og_ext e;
+    e.c.x = 0; e.c.y = 0; e.c.z = 1;
+    e.r = nextafter(OG_PI, INFINITY);
+    e.xmin = -INFINITY; e.xmax = INFINITY; e.ymin = -INFINITY; e.ymax = INFINITY;
+    return e;
+}
+
+/* _spherical_cap(p1..p4, perimeter) grids.jl:256-273: centre = normalize(mean
+ * of 4 corners); radius = 1.0001 * max distance to corners, edge midpoints and
+ * perimeter points. */
+typedef struct {
+    double d;
+    v3 c;
+} og_capacc;
+
+static og_capacc og_cap_begin(v3 p1, v3 p2, v3 p3, v3 p4) {
+    og_capacc a;
+    v3 m = {(p1.x + p2.x + p3.x + p4.x) / 4, (p1.y + p2.y + p3.y + p4.y) / 4, (p1.z + p2.z + p3.z + p4.z) / 4};
+    a.c = og_normalize_libm(m);
+    v3 pts[8] = {p1, p2, p3, p4, og_mid(p1, p2), og_mid(p2, p3), og_mid(p3, p4), og_mid(p4, p1)};
+    double d = 0.0;
+    for (int k = 0; k < 8; ++k) { double t = og_sdist(a.c, pts[k]); d = (t > d || t != t) ? t : d; }
+    a.d = d;
+    return a;
+}
+static inline void og_cap_add(og_capacc* a, v3 p) {
+    double t = og_sdist(a->c, p);
+    if (t > a->d || t != t) a->d = t;
+}
+static og_ext og_cap_end(og_capacc a) {
+    og_ext e;
+    e.c = a.c; e.r = a.d * 1.0001;
+    e.xmin = e.xmax = e.ymin = e.ymax = 0;
+    return e;
+}
+
+/* GeometryOps UnitSpherical._intersects(cap, cap): centre distance <= r1 + r2. */
+static inline int og_pred(int spherical, const og_ext* a, const og_ext* b) {
+    if (spherical) return og_sdist(a->c, b->c) <= a->r + b->r;
+    return a->xmin <= b->xmax && b->xmin <= a->xmax && a->ymin <= b->ymax && b->ymin <= a->ymax;
+}
+
+/* ------------------------------------------------------------------------ */
+/* HEALPix geometry (Gorski et al. 2005): nested pixel -> 4 corners N,W,S,E. */
+/* ------------------------------------------------------------------------ */
+
+static const int OG_JRLL[12] = {2, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4};
+static const int OG_JPLL[12] = {1, 3, 5, 7, 0, 2, 4, 6, 1, 3, 5, 7};
+
+static int64_t og_compact_bits(int64_t v) {
+    int64_t r = 0;
+    for (int b = 0; b < 31; ++b) r |= ((v >> (2 * b)) & 1) << b;
+    return r;
+}
+
+static void og_nest2xyf(int64_t nside, int64_t pix, int64_t* ix, int64_t* iy, int* face) {
+    int64_t npface = nside * nside;
+    *face = (int)(pix / npface);
+    int64_t ipf = pix % npface;
+    *ix = og_compact_bits(ipf);
+    *iy = og_compact_bits(ipf >> 1);
+}
+
+/* face-normalised (x, y) in [0,1]^2 -> unit vector */
+static v3 og_hp_loc2vec(double x, double y, int face) {
+    double jr = OG_JRLL[face] - x - y;
+    double nr, z, sth;
+    if (jr < 1.0) {
+        nr = jr;
+        double tmp = nr * nr / 3.0;
+        z = 1.0 - tmp;
+        sth = sqrt(tmp * (2.0 - tmp));
+    } else if (jr > 3.0) {
+        nr = 4.0 - jr;
+        double tmp = nr * nr / 3.0;
+        z = tmp - 1.0;
+        sth = sqrt(tmp * (2.0 - tmp));
+    } else {
+        nr = 1.0;
+        z = (2.0 - jr) * 2.0 / 3.0;
+        sth = sqrt((1.0 - z) * (1.0 + z));
+    }
+    double tmp = OG_JPLL[face] * nr + x - y;
+    if (tmp < 0) tmp += 8;
+    if (tmp >= 8) tmp -= 8;
+    double phi = (nr < 1e-15) ? 0.0 : (OG_PI_4 * tmp) / nr;
+    v3 v = {sth * cos(phi), sth * sin(phi), z};
+    return v;
+}
+
+void og_healpix_corners(int64_t nside, int64_t pix_nested, double* out12) {
+    int64_t ix, iy; int face;
+    og_nest2xyf(nside, pix_nested, &ix, &iy, &face);
+    double ns = (double)nside;
+    v3 c[4];
+    c[0] = og_hp_loc2vec((ix + 1) / ns, (iy + 1) / ns, face); /* N */
+    c[1] = og_hp_loc2vec((ix) / ns, (iy + 1) / ns, face);     /* W */
+    c[2] = og_hp_loc2vec((ix) / ns, (iy) / ns, face);         /* S */
+    c[3] = og_hp_loc2vec((ix + 1) / ns, (iy) / ns, face);     /* E */
+    for (int k = 0; k < 4; ++k) { out12[3 * k] = c[k].x; out12[3 * k + 1] = c[k].y; out12[3 * k + 2] = c[k].z; }
+}
+
+int64_t og_healpix_nest2ring(int64_t nside, int64_t pix_nested) {
+    int64_t ix, iy; int face;
+    og_nest2xyf(nside, pix_nested, &ix, &iy, &face);
+    int64_t nl4 = 4 * nside, npix = 12 * nside * nside, ncap = 2 * nside * (nside - 1);
+    int64_t jr = (int64_t)OG_JRLL[face] * nside - ix - iy - 1;
+    int64_t nr, nbefore, kshift;
+    if (jr < nside) { nr = jr; nbefore = 2 * nr * (nr - 1); kshift = 0; }
+    else if (jr > 3 * nside) { nr = nl4 - jr; nbefore = npix - 2 * (nr + 1) * nr; kshift = 0; }
+    else { nr = nside; nbefore = ncap + (jr - nside) * nl4; kshift = (jr - nside) & 1; }
+    int64_t jp = ((int64_t)OG_JPLL[face] * nr + ix - iy + 1 + kshift) / 2;
+    if (jp > nl4) jp -= nl4;
+    if (jp < 1) jp += nl4;
+    return nbefore + jp - 1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Grids and trees.                                                         */
+/* ------------------------------------------------------------------------ */
+
+enum { OG_CURVI = 0, OG_HEALPIX = 1, OG_POLYS = 2 };
+
+/* Grid description (host pointers).  Curvilinear blocks: point (i,j) of block
+ * b at points[(block_point_off[b] + i + j*(nx+1)) * dim]; cell (i,j) has global
+ * index block_cell_off[b] + i + j*nx and ring p(i,j),p(i+1,j),p(i+1,j+1),p(i,j+1)
+ * (grids.jl:77-83, interfaces.jl:241-243, ClimaCoreExt.jl:56-61).  HEALPix and
+ * polygon grids: poly_verts[(cell*maxv + k)*dim], nverts[cell] (NULL -> maxv). */
+typedef struct {
+    int32_t kind, manifold, nblocks, nested;
+    int32_t maxv, full_sphere_root, dim, pad;
+    int64_t ncells, nside;
+    const int64_t* block_nx;
+    const int64_t* block_ny;
+    const int64_t* block_point_off;
+    const int64_t* block_cell_off;
+    const double* points;
+    const int32_t* nverts;
+    const double* poly_verts;
+} og_grid;
+
+typedef struct {
+    int8_t type;  /* 0 toplevel multi-block, 1 quad range, 2 hp root, 3 hp node, 4 flat */
+    int8_t full;  /* node_extent overridden by the full sphere (KnownFullSphereExtentWrapper) */
+    int32_t block;
+    int32_t level;
+    int64_t i0, i1, j0, j1;
+    int64_t pixel;
+} og_node;
+
+typedef struct {
+    const og_grid* g;
+    int spherical;
+    int hp_L;              /* leaf level of the HEALPix tree */
+    int64_t par_threshold_den; /* nthreads * 32 */
+    og_ext* cell_ext;      /* cached leaf extents per global cell index */
+    int64_t* hp_ring_of_nested; /* nested leaf pixel -> output index */
+} og_tree;
+
+static v3 og_gpoint(const og_grid* g, int b, int64_t i, int64_t j) {
+    int64_t nx = g->block_nx[b];
+    const double* p = g->points + (g->block_point_off[b] + i + j * (nx + 1)) * g->dim;
+    v3 v = {p[0], p[1], g->dim == 3 ? p[2] : 0.0};
+    return v;
+}
+
+/* Vertices of global cell `idx` in ring order; returns count. */
+static int og_cell_verts(const og_grid* g, int64_t idx, v3* out) {
+    if (g->kind == OG_CURVI) {
+        int b = 0;
+        while (b + 1 < g->nblocks && idx >= g->block_cell_off[b + 1]) b++;
+        int64_t loc = idx - g->block_cell_off[b];
+        int64_t nx = g->block_nx[b];
+        int64_t i = loc % nx, j = loc / nx;
+        out[0] = og_gpoint(g, b, i, j);
+        out[1] = og_gpoint(g, b, i + 1, j);
+        out[2] = og_gpoint(g, b, i + 1, j + 1);
+        out[3] = og_gpoint(g, b, i, j + 1);
+        return 4;
+    }
+    int n = g->nverts ? g->nverts[idx] : g->maxv;
+    for (int k = 0; k < n; ++k) {
+        const double* p = g->poly_verts + (idx * g->maxv + k) * g->dim;
+        out[k].x = p[0]; out[k].y = p[1]; out[k].z = g->dim == 3 ? p[2] : 0.0;
+    }
+    return n;
+}
+
+/* cell_range_extent (grids.jl:279-287 spherical, :148-152 planar) over cells
+ * [i0..i1] x [j0..j1] of block b. */
+static og_ext og_range_extent(const og_tree* t, int b, int64_t i0, int64_t i1, int64_t j0, int64_t j1) {
+    const og_grid* g = t->g;
+    int64_t imin = i0, imax = i1 + 1, jmin = j0, jmax = j1 + 1;
+    if (!t->spherical) {
+        og_ext e;
+        e.xmin = INFINITY; e.xmax = -INFINITY; e.ymin = INFINITY; e.ymax = -INFINITY;
+        for (int64_t j = jmin; j <= jmax; ++j)
+            for (int64_t i = imin; i <= imax; ++i) {
+                v3 p = og_gpoint(g, b, i, j);
+                if (p.x < e.xmin) e.xmin = p.x;
+                if (p.x > e.xmax) e.xmax = p.x;
+                if (p.y < e.ymin) e.ymin = p.y;
+                if (p.y > e.ymax) e.ymax = p.y;
+            }
+        e.c.x = e.c.y = e.c.z = 0; e.r = 0;
+        return e;
+    }
+    og_capacc a = og_cap_begin(og_gpoint(g, b, imin, jmin), og_gpoint(g, b, imax, jmin),
+                               og_gpoint(g, b, imax, jmax), og_gpoint(g, b, imin, jmax));
+    /* CurvilinearGridPerimeterPoints (grids.jl:205-232): west and east columns,
+     * then the interiors of the south and north rows. */
+    for (int64_t j = jmin; j <= jmax; ++j) { og_cap_add(&a, og_gpoint(g, b, imin, j)); og_cap_add(&a, og_gpoint(g, b, imax, j)); }
+    for (int64_t i = imin + 1; i < imax; ++i) { og_cap_add(&a, og_gpoint(g, b, i, jmin)); og_cap_add(&a, og_gpoint(g, b, i, jmax)); }
+    return og_cap_end(a);
+}
+
+/* circle_from_four_corners(corners, ()) with corners in (N,W,S,E) order as
+ * returned for a HEALPix pixel; reordered raw[1],raw[3],raw[4],raw[2]
+ * (grids.jl:245-251). */
+static og_ext og_cap_from_hp_corners(const v3* c) {
+    og_capacc a = og_cap_begin(c[0], c[2], c[3], c[1]);
+    return og_cap_end(a);
+}
+
+static og_ext og_poly_extent(const og_tree* t, int64_t idx) {
+    v3 v[OG_MAXV];
+    int n = og_cell_verts(t->g, idx, v);
+    og_ext e;
+    if (!t->spherical) {
+        e.xmin = INFINITY; e.xmax = -INFINITY; e.ymin = INFINITY; e.ymax = -INFINITY;
+        for (int k = 0; k < n; ++k) {
+            if (v[k].x < e.xmin) e.xmin = v[k].x;
+            if (v[k].x > e.xmax) e.xmax = v[k].x;
+            if (v[k].y < e.ymin) e.ymin = v[k].y;
+            if (v[k].y > e.ymax) e.ymax = v[k].y;
+        }
+        e.c.x = e.c.y = e.c.z = 0; e.r = 0;
+        return e;
+    }
+    /* ExplicitPolygonGrid{Spherical} cell_range_extent (grids.jl:133-146) over
+     * the closed ring (first vertex repeated). */
+    v3 s = {0, 0, 0};
+    for (int k = 0; k <= n; ++k) { v3 p = v[k % n]; s.x += p.x; s.y += p.y; s.z += p.z; }
+    s.x /= (n + 1); s.y /= (n + 1); s.z /= (n + 1);
+    e.c = og_normalize_libm(s);
+    double d = 0;
+    for (int k = 0; k < n; ++k) { double q = og_sdist(e.c, v[k]); if (q > d || q != q) d = q; }
+    e.r = d * 1.0001;
+    e.xmin = e.xmax = e.ymin = e.ymax = 0;
+    return e;
+}
+
+static int og_isleaf(const og_tree* t, const og_node* n) {
+    switch (n->type) {
+        case 1: return (n->i1 - n->i0 + 1) <= 2 && (n->j1 - n->j0 + 1) <= 2;
+        case 3: return n->level == t->hp_L;
+        case 4: return 1;
+        default: return 0;
+    }
+}
+
+static int og_children(const og_tree* t, const og_node* n, og_node* ch) {
+    const og_grid* g = t->g;
+    if (n->type == 0) {
+        for (int b = 0; b < g->nblocks; ++b) {
+            og_node c = {1, 0, b, 0, 0, g->block_nx[b] - 1, 0, g->block_ny[b] - 1, 0};
+            ch[b] = c;
+        }
+        return g->nblocks;
+    }
+    if (n->type == 2) {
+        for (int k = 0; k < 12; ++k) { og_node c = {3, 0, 0, 0, 0, 0, 0, 0, k}; ch[k] = c; }
+        return 12;
+    }
+    if (n->type == 3) {
+        for (int k = 0; k < 4; ++k) { og_node c = {3, 0, 0, n->level + 1, 0, 0, 0, 0, 4 * n->pixel + k}; ch[k] = c; }
+        return 4;
+    }
+    /* type 1: TopDownQuadtreeCursor getchild (quadtree_cursors.jl:258-287) */
+    int64_t li = n->i1 - n->i0 + 1, lj = n->j1 - n->j0 + 1;
+    og_node base = *n; base.full = 0;
+    if (li == 1) {
+        int64_t s = lj / 2;
+        ch[0] = base; ch[0].j1 = n->j0 + s - 1;
+        ch[1] = base; ch[1].j0 = n->j0 + s;
+        return 2;
+    }
+    if (lj == 1) {
+        int64_t s = li / 2;
+        ch[0] = base; ch[0].i1 = n->i0 + s - 1;
+        ch[1] = base; ch[1].i0 = n->i0 + s;
+        return 2;
+    }
+    int64_t si = li / 2, sj = lj / 2;
+    for (int k = 0; k < 4; ++k) ch[k] = base;
+    ch[0].i1 = n->i0 + si - 1; ch[0].j1 = n->j0 + sj - 1;
+    ch[1].i1 = n->i0 + si - 1; ch[1].j0 = n->j0 + sj;
+    ch[2].i0 = n->i0 + si;     ch[2].j1 = n->j0 + sj - 1;
+    ch[3].i0 = n->i0 + si;     ch[3].j0 = n->j0 + sj;
+    return 4;
+}
+
+static og_ext og_node_extent(const og_tree* t, const og_node* n) {
+    if (n->full || n->type == 0 || n->type == 2) return og_full_sphere();
+    if (n->type == 1) return og_range_extent(t, n->block, n->i0, n->i1, n->j0, n->j1);
+    if (n->type == 3) {
+        if (n->level == t->hp_L) return t->cell_ext[t->hp_ring_of_nested[n->pixel]];
+        double c12[12];
+        og_healpix_corners((int64_t)1 << n->level, n->pixel, c12);
+        v3 c[4];
+        for (int k = 0; k < 4; ++k) { c[k].x = c12[3 * k]; c[k].y = c12[3 * k + 1]; c[k].z = c12[3 * k + 2]; }
+        return og_cap_from_hp_corners(c);
+    }
+    /* flat: union of all polygon extents */
+    og_ext e;
+    if (!t->spherical) {
+        e.xmin = INFINITY; e.xmax = -INFINITY; e.ymin = INFINITY; e.ymax = -INFINITY;
+        for (int64_t i = 0; i < t->g->ncells; ++i) {
+            og_ext c = t->cell_ext[i];
+            if (c.xmin < e.xmin) e.xmin = c.xmin;
+            if (c.xmax > e.xmax) e.xmax = c.xmax;
+            if (c.ymin < e.ymin) e.ymin = c.ymin;
+            if (c.ymax > e.ymax) e.ymax = c.ymax;
+        }
+        e.c.x = e.c.y = e.c.z = 0; e.r = 0;
+        return e;
+    }
+    return og_full_sphere();
+}
+
+/* leaf cells of a leaf node */
+static int og_leaf_cells(const og_tree* t, const og_node* n, int64_t* idx, int cap) {
+    const og_grid* g = t->g;
+    if (n->type == 1) {
+        int c = 0;
+        int64_t nx = g->block_nx[n->block];
+        for (int64_t j = n->j0; j <= n->j1; ++j)
+            for (int64_t i = n->i0; i <= n->i1; ++i) idx[c++] = g->block_cell_off[n->block] + i + j * nx;
+        return c;
+    }
+    if (n->type == 3) { idx[0] = t->hp_ring_of_nested[n->pixel]; return 1; }
+    (void)cap;
+    return -1; /* flat: all cells, handled by caller */
+}
+
+typedef struct { int64_t* a; int64_t n, cap; } og_vec;
+static void og_push2(og_vec* v, int64_t x, int64_t y) {
+    if (v->n + 2 > v->cap) {
+        v->cap = v->cap ? 2 * v->cap : 1024;
+        v->a = (int64_t*)realloc(v->a, sizeof(int64_t) * v->cap);
+    }
+    v->a[v->n++] = x; v->a[v->n++] = y;
+}
+
+static void og_leaf_pairs(const og_tree* t1, const og_node* n1, const og_tree* t2, const og_node* n2, og_vec* out) {
+    int64_t c1[4], c2[4];
+    int k1 = og_leaf_cells(t1, n1, c1, 4), k2 = og_leaf_cells(t2, n2, c2, 4);
+    int64_t m1 = k1 < 0 ? t1->g->ncells : k1, m2 = k2 < 0 ? t2->g->ncells : k2;
+    for (int64_t a = 0; a < m1; ++a) {
+        int64_t i1 = k1 < 0 ? a : c1[a];
+        for (int64_t b = 0; b < m2; ++b) {
+            int64_t i2 = k2 < 0 ? b : c2[b];
+            if (og_pred(t1->spherical, &t1->cell_ext[i1], &t2->cell_ext[i2])) og_push2(out, i1, i2);
+        }
+    }
+}
+
+/* GeometryOps STI.dual_depth_first_search restated: descend both trees while
+ * the child extents intersect; emit leaf-cell pairs whose extents intersect. */
+static void og_dual_dfs(const og_tree* t1, og_node n1, const og_tree* t2, og_node n2, og_vec* out) {
+    int l1 = og_isleaf(t1, &n1), l2 = og_isleaf(t2, &n2);
+    og_node ch1[12], ch2[12];
+    if (l1 && l2) { og_leaf_pairs(t1, &n1, t2, &n2, out); return; }
+    if (l1) {
+        og_ext e1 = og_node_extent(t1, &n1);
+        int k2 = og_children(t2, &n2, ch2);
+        for (int b = 0; b < k2; ++b) {
+            og_ext e2 = og_node_extent(t2, &ch2[b]);
+            if (og_pred(t1->spherical, &e1, &e2)) og_dual_dfs(t1, n1, t2, ch2[b], out);
+        }
+        return;
+    }
+    if (l2) {
+        og_ext e2 = og_node_extent(t2, &n2);
+        int k1 = og_children(t1, &n1, ch1);
+        for (int a = 0; a < k1; ++a) {
+            og_ext e1 = og_node_extent(t1, &ch1[a]);
+            if (og_pred(t1->spherical, &e1, &e2)) og_dual_dfs(t1, ch1[a], t2, n2, out);
+        }
+        return;
+    }
+    int k1 = og_children(t1, &n1, ch1), k2 = og_children(t2, &n2, ch2);
+    og_ext e2s[12];
+    for (int b = 0; b < k2; ++b) e2s[b] = og_node_extent(t2, &ch2[b]);
+    for (int a = 0; a < k1; ++a) {
+        og_ext e1 = og_node_extent(t1, &ch1[a]);
+        for (int b = 0; b < k2; ++b)
+            if (og_pred(t1->spherical, &e1, &e2s[b])) og_dual_dfs(t1, ch1[a], t2, ch2[b], out);
+    }
+}
+
+/* should_parallelize (quadtree_cursors.jl:17-25, interfaces.jl:80-81) */
+static int og_should_par(const og_tree* t, const og_node* n, const og_ext* e) {
+    if (n->type == 1) {
+        int64_t total = t->g->block_nx[n->block] * t->g->block_ny[n->block];
+        int64_t th = total / t->par_threshold_den;
+        if (th < 1) th = 1;
+        return (n->i1 - n->i0 + 1) * (n->j1 - n->j0 + 1) <= th;
+    }
+    if (!t->spherical) return 0;
+    return (2 * OG_PI * (1 - cos(e->r))) < OG_PI;
+}
+
+typedef struct { og_node a, b; } og_task;
+typedef struct { og_task* t; int64_t n, cap; } og_tasks;
+
+/* multithreaded_dual_depth_first_search (MultithreadedDualDepthFirstSearch.jl:12-42) */
+static void og_mt_dfs(const og_tree* t1, og_node n1, og_ext e1, const og_tree* t2, og_node n2, og_ext e2, og_tasks* ts) {
+    int push = og_isleaf(t1, &n1) || og_isleaf(t2, &n2) ||
+               (og_should_par(t1, &n1, &e1) && og_should_par(t2, &n2, &e2));
+    if (push) {
+        if (ts->n == ts->cap) { ts->cap = ts->cap ? 2 * ts->cap : 256; ts->t = (og_task*)realloc(ts->t, sizeof(og_task) * ts->cap); }
+        ts->t[ts->n].a = n1; ts->t[ts->n].b = n2; ts->n++;
+        return;
+    }
+    og_node ch1[12], ch2[12];
+    int k1 = og_children(t1, &n1, ch1), k2 = og_children(t2, &n2, ch2);
+    og_ext e2s[12];
+    for (int b = 0; b < k2; ++b) e2s[b] = og_node_extent(t2, &ch2[b]);
+    for (int a = 0; a < k1; ++a) {
+        og_ext ce1 = og_node_extent(t1, &ch1[a]);
+        for (int b = 0; b < k2; ++b)
+            if (og_pred(t1->spherical, &ce1, &e2s[b])) og_mt_dfs(t1, ch1[a], ce1, t2, ch2[b], e2s[b], ts);
+    }
+}
+
+static og_node og_root(const og_grid* g) {
+    og_node r;
+    memset(&r, 0, sizeof(r));
+    if (g->kind == OG_CURVI) {
+        if (g->nblocks > 1) { r.type = 0; r.full = 1; }
+        else { r.type = 1; r.block = 0; r.i1 = g->block_nx[0] - 1; r.j1 = g->block_ny[0] - 1; r.full = (int8_t)g->full_sphere_root; }
+    } else if (g->kind == OG_HEALPIX) {
+        r.type = 2; r.full = 1;
+    } else {
+        r.type = 4;
+    }
+    return r;
+}
+
+static void og_tree_init(og_tree* t, const og_grid* g, int nthreads) {
+    memset(t, 0, sizeof(*t));
+    t->g = g;
+    t->spherical = g->manifold == 1;
+    t->par_threshold_den = (int64_t)nthreads * 32;
+    t->cell_ext = (og_ext*)malloc(sizeof(og_ext) * (g->ncells > 0 ? g->ncells : 1));
+    if (g->kind == OG_HEALPIX) {
+        int L = 0;
+        while (((int64_t)1 << L) < g->nside) L++;
+        t->hp_L = L;
+        t->hp_ring_of_nested = (int64_t*)malloc(sizeof(int64_t) * g->ncells);
+        for (int64_t p = 0; p < g->ncells; ++p)
+            t->hp_ring_of_nested[p] = g->nested ? p : og_healpix_nest2ring(g->nside, p);
+    }
+    /* cache leaf extents: identical to recomputing them on every visit */
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < g->ncells; ++i) {
+        if (g->kind == OG_CURVI) {
+            int b = 0;
+            while (b + 1 < g->nblocks && i >= g->block_cell_off[b + 1]) b++;
+            int64_t loc = i - g->block_cell_off[b], nx = g->block_nx[b];
+            t->cell_ext[i] = og_range_extent(t, b, loc % nx, loc % nx, loc / nx, loc / nx);
+        } else if (g->kind == OG_HEALPIX) {
+            v3 c[OG_MAXV];
+            og_cell_verts(g, i, c);
+            t->cell_ext[i] = og_cap_from_hp_corners(c);
+        } else {
+            t->cell_ext[i] = og_poly_extent(t, i);
+        }
+    }
+}
+
+static void og_tree_free(og_tree* t) {
+    free(t->cell_ext);
+    free(t->hp_ring_of_nested);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Regridder build (regridder.jl:125-163).                                  */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    int64_t nd, ns, nnz, ncand;
+    int64_t* colptr;  /* CSC of A (nd x ns): column = src cell, rows sorted */
+    int64_t* rowval;
+    double* nzval;
+    double* dst_areas;
+    double* src_areas;
+    int64_t clip_overflows;
+} og_regridder;
+
+/* Candidate search only: returns pairs (src, dst) in *out (2 per pair).
+ * use_tree = 0 replaces the dual DFS by the exhaustive leaf test (for tests). */
+int64_t og_candidates(const og_grid* dst, const og_grid* src, int use_tree, int nthreads, int64_t** out) {
+    og_tree ts, td;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    int nth = omp_get_max_threads();
+#else
+    int nth = 1;
+#endif
+    og_tree_init(&ts, src, nth);
+    og_tree_init(&td, dst, nth);
+    og_vec all = {0, 0, 0};
+    if (use_tree) {
+        og_node rs = og_root(src), rd = og_root(dst);
+        og_tasks tasks = {0, 0, 0};
+        og_mt_dfs(&ts, rs, og_node_extent(&ts, &rs), &td, rd, og_node_extent(&td, &rd), &tasks);
+        og_vec* per = (og_vec*)calloc(tasks.n > 0 ? tasks.n : 1, sizeof(og_vec));
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int64_t k = 0; k < tasks.n; ++k) og_dual_dfs(&ts, tasks.t[k].a, &td, tasks.t[k].b, &per[k]);
+        int64_t tot = 0;
+        for (int64_t k = 0; k < tasks.n; ++k) tot += per[k].n;
+        all.a = (int64_t*)malloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
+        for (int64_t k = 0; k < tasks.n; ++k) {
+            if (per[k].n) memcpy(all.a + all.n, per[k].a, sizeof(int64_t) * per[k].n);
+            all.n += per[k].n;
+            free(per[k].a);
+        }
+        free(per);
+        free(tasks.t);
+    } else {
+        int64_t nsrc = src->ncells;
+        og_vec* per = (og_vec*)calloc(nsrc > 0 ? nsrc : 1, sizeof(og_vec));
+#pragma omp parallel for schedule(dynamic, 64)
+        for (int64_t i = 0; i < nsrc; ++i)
+            for (int64_t j = 0; j < dst->ncells; ++j)
+                if (og_pred(ts.spherical, &ts.cell_ext[i], &td.cell_ext[j])) og_push2(&per[i], i, j);
+        int64_t tot = 0;
+        for (int64_t k = 0; k < nsrc; ++k) tot += per[k].n;
+        all.a = (int64_t*)malloc(sizeof(int64_t) * (tot > 0 ? tot : 1));
+        for (int64_t k = 0; k < nsrc; ++k) {
+            if (per[k].n) memcpy(all.a + all.n, per[k].a, sizeof(int64_t) * per[k].n);
+            all.n += per[k].n;
+            free(per[k].a);
+        }
+        free(per);
+    }
+    og_tree_free(&ts);
+    og_tree_free(&td);
+    *out = all.a;
+    return all.n / 2;
+}
+
+void og_free_buffer(void* p) { free(p); }
+
+/* SparseArrays.sparse(I=dst, J=src, V, nd, ns): CSC by counting sort on the
+ * column, rows ascending within a column, duplicates combined with +. */
+static void og_sparse(og_regridder* R, const int64_t* i_dst, const int64_t* i_src, const double* v, int64_t n) {
+    int64_t nd = R->nd, ns = R->ns;
+    int64_t* cnt = (int64_t*)calloc(ns + 1, sizeof(int64_t));
+    for (int64_t k = 0; k < n; ++k) cnt[i_src[k] + 1]++;
+    for (int64_t j = 0; j < ns; ++j) cnt[j + 1] += cnt[j];
+    int64_t* pos = (int64_t*)malloc(sizeof(int64_t) * (ns + 1));
+    memcpy(pos, cnt, sizeof(int64_t) * (ns + 1));
+    int64_t* rows = (int64_t*)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+    double* vals = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
+    for (int64_t k = 0; k < n; ++k) { int64_t p = pos[i_src[k]]++; rows[p] = i_dst[k]; vals[p] = v[k]; }
+    /* sort rows within each column (insertion sort: columns are short) and combine duplicates */
+    R->colptr = (int64_t*)malloc(sizeof(int64_t) * (ns + 1));
+    R->rowval = (int64_t*)malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+    R->nzval = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
+    int64_t out = 0;
+    R->colptr[0] = 0;
+    for (int64_t j = 0; j < ns; ++j) {
+        int64_t a = cnt[j], b = cnt[j + 1];
+        for (int64_t p = a + 1; p < b; ++p) {
+            int64_t r = rows[p]; double x = vals[p]; int64_t q = p - 1;
+            while (q >= a && rows[q] > r) { rows[q + 1] = rows[q]; vals[q + 1] = vals[q]; q--; }
+            rows[q + 1] = r; vals[q + 1] = x;
+        }
+        for (int64_t p = a; p < b; ++p) {
+            if (out > R->colptr[j] && R->rowval[out - 1] == rows[p]) R->nzval[out - 1] += vals[p];
+            else { R->rowval[out] = rows[p]; R->nzval[out] = vals[p]; out++; }
+        }
+        R->colptr[j + 1] = out;
+    }
+    R->nnz = out;
+    (void)nd;
+    free(cnt); free(pos); free(rows); free(vals);
+}
+
+og_regridder* og_build(const og_grid* dst, const og_grid* src, int normalize, int use_tree, int nthreads) {
+    og_regridder* R = (og_regridder*)calloc(1, sizeof(og_regridder));
+    R->nd = dst->ncells; R->ns = src->ncells;
+    int spherical = (dst->manifold == 1) || (src->manifold == 1);
+    int64_t* cand = NULL;
+    int64_t nc = og_candidates(dst, src, use_tree, nthreads, &cand);
+    R->ncand = nc;
+    double* area = (double*)malloc(sizeof(double) * (nc > 0 ? nc : 1));
+    int64_t ovf_total = 0;
+    /* chunked per-pair clip + area (intersection_areas.jl:4-32, :86-113) */
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : ovf_total)
+    for (int64_t k = 0; k < nc; ++k) {
+        v3 s[OG_MAXV], d[OG_MAXV];
+        int ns_ = og_cell_verts(src, cand[2 * k], s);
+        int nd_ = og_cell_verts(dst, cand[2 * k + 1], d);
+        int ovf = 0;
+        area[k] = og_pair_area(spherical, s, ns_, d, nd_, &ovf);
+        ovf_total += ovf;
+    }
+    R->clip_overflows = ovf_total;
+    /* keep area > 0, concatenated in candidate order */
+    int64_t m = 0;
+    int64_t* id = (int64_t*)malloc(sizeof(int64_t) * (nc > 0 ? nc : 1));
+    int64_t* is = (int64_t*)malloc(sizeof(int64_t) * (nc > 0 ? nc : 1));
+    for (int64_t k = 0; k < nc; ++k)
+        if (area[k] > 0) { is[m] = cand[2 * k]; id[m] = cand[2 * k + 1]; area[m] = area[k]; m++; }
+    og_sparse(R, id, is, area, m);
+    free(id); free(is); free(area); free(cand);
+    /* per-cell areas (regridder.jl:165-178) */
+    R->dst_areas = (double*)malloc(sizeof(double) * (R->nd > 0 ? R->nd : 1));
+    R->src_areas = (double*)malloc(sizeof(double) * (R->ns > 0 ? R->ns : 1));
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < R->nd; ++i) { v3 v[OG_MAXV]; int n = og_cell_verts(dst, i, v); R->dst_areas[i] = og_cell_area(spherical, v, n); }
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < R->ns; ++i) { v3 v[OG_MAXV]; int n = og_cell_verts(src, i, v); R->src_areas[i] = og_cell_area(spherical, v, n); }
+    if (normalize) {
+        /* normalize!(::Regridder) regridder.jl:54-62: maximum(A) includes implicit zeros */
+        double mx = (R->nnz < R->nd * R->ns) ? 0.0 : -INFINITY;
+        for (int64_t k = 0; k < R->nnz; ++k) if (R->nzval[k] > mx) mx = R->nzval[k];
+        for (int64_t k = 0; k < R->nnz; ++k) R->nzval[k] /= mx;
+        for (int64_t i = 0; i < R->nd; ++i) R->dst_areas[i] /= mx;
+        for (int64_t i = 0; i < R->ns; ++i) R->src_areas[i] /= mx;
+    }
+    return R;
+}
+
+int64_t og_nnz(const og_regridder* R) { return R->nnz; }
+int64_t og_ncand(const og_regridder* R) { return R->ncand; }
+int64_t og_overflows(const og_regridder* R) { return R->clip_overflows; }
+
+void og_get_csc(const og_regridder* R, int64_t* colptr, int64_t* rowval, double* nzval) {
+    memcpy(colptr, R->colptr, sizeof(int64_t) * (R->ns + 1));
+    if (R->nnz) {
+        memcpy(rowval, R->rowval, sizeof(int64_t) * R->nnz);
+        memcpy(nzval, R->nzval, sizeof(double) * R->nnz);
+    }
+}
+
+void og_get_areas(const og_regridder* R, double* dst_areas, double* src_areas) {
+    memcpy(dst_areas, R->dst_areas, sizeof(double) * R->nd);
+    memcpy(src_areas, R->src_areas, sizeof(double) * R->ns);
+}
+
+void og_free(og_regridder* R) {
+    if (!R) return;
+    free(R->colptr); free(R->rowval); free(R->nzval); free(R->dst_areas); free(R->src_areas);
+    free(R);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Apply (regrid.jl:63-118, regridder.jl:49-50).                            */
+/* Fields: element (cell c, field f) at base[c*stride_cell + f*stride_field]. */
+/* ------------------------------------------------------------------------ */
+
+/* forward: mul!(y, A, x) as the stdlib CSC kernel (column scatter), then ./ a_d */
+static void og_apply_fwd1(const og_regridder* R, const double* x, int64_t sx, double* y, int64_t sy, int normalize) {
+    for (int64_t i = 0; i < R->nd; ++i) y[i * sy] = 0.0;
+    for (int64_t j = 0; j < R->ns; ++j) {
+        double xj = x[j * sx];
+        for (int64_t k = R->colptr[j]; k < R->colptr[j + 1]; ++k) y[R->rowval[k] * sy] += R->nzval[k] * xj;
+    }
+    if (normalize) for (int64_t i = 0; i < R->nd; ++i) y[i * sy] = y[i * sy] / R->dst_areas[i];
+}
+
+/* transpose: mul!(y, transpose(A), x) column gather, then ./ a_s */
+static void og_apply_rev1(const og_regridder* R, const double* x, int64_t sx, double* y, int64_t sy, int normalize) {
+    for (int64_t j = 0; j < R->ns; ++j) {
+        double acc = 0.0;
+        for (int64_t k = R->colptr[j]; k < R->colptr[j + 1]; ++k) acc += R->nzval[k] * x[R->rowval[k] * sx];
+        y[j * sy] = normalize ? acc / R->src_areas[j] : acc;
+    }
+}
+
+/* One 1-D pass per field, as NDSliceLoop does (regrid.jl:303-318); fields are
+ * spread over threads. */
+void og_apply(const og_regridder* R, int transpose, const double* src, int64_t src_stride_cell, int64_t src_stride_field,
+              double* dst, int64_t dst_stride_cell, int64_t dst_stride_field, int64_t nfields, int normalize, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t f = 0; f < nfields; ++f) {
+        if (!transpose) og_apply_fwd1(R, src + f * src_stride_field, src_stride_cell, dst + f * dst_stride_field, dst_stride_cell, normalize);
+        else og_apply_rev1(R, src + f * src_stride_field, src_stride_cell, dst + f * dst_stride_field, dst_stride_cell, normalize);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Test hooks for single geometric operations.                              */
+/* ------------------------------------------------------------------------ */
+
+double og_pair_area_hook(int spherical, const double* s, int ns, const double* d, int nd, int* ovf) {
+    v3 sv[OG_MAXV], dv[OG_MAXV];
+    int dim = spherical ? 3 : 2;
+    for (int k = 0; k < ns; ++k) { sv[k].x = s[k * dim]; sv[k].y = s[k * dim + 1]; sv[k].z = spherical ? s[k * dim + 2] : 0; }
+    for (int k = 0; k < nd; ++k) { dv[k].x = d[k * dim]; dv[k].y = d[k * dim + 1]; dv[k].z = spherical ? d[k * dim + 2] : 0; }
+    *ovf = 0;
+    return og_pair_area(spherical, sv, ns, dv, nd, ovf);
+}
+
+double og_cell_area_hook(int spherical, const double* v, int n) {
+    v3 p[OG_MAXV];
+    int dim = spherical ? 3 : 2;
+    for (int k = 0; k < n; ++k) { p[k].x = v[k * dim]; p[k].y = v[k * dim + 1]; p[k].z = spherical ? v[k * dim + 2] : 0; }
+    return og_cell_area(spherical, p, n);
+}
+
+int og_num_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

@@ -1,0 +1,274 @@
+"""GPU parity: the CUDA build and apply against the CPU oracle, through the
+C ABI.  Nonzero patterns must be bit-exact; the FP64 clip/area arithmetic is a
+fixed operation sequence, so areas are expected bit-identical and are held to
+1e-12 relative at worst; FP64 apply follows the reference's summation order.
+"""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, c1_grids
+from crg import Regridder, grids, regrid, regrid_, regrid_adjoint_
+from crg.regridder import ArgumentError, DimensionMismatch
+
+pytestmark = pytest.mark.gpu
+
+AREA_RTOL = 1e-12
+
+
+def assert_parity(R, O, exact=True):
+    colptr, rowval, nzval = R.csc_arrays()
+    assert R.nnz == O.nnz
+    assert np.array_equal(colptr, O.colptr), "column pointers differ"
+    assert np.array_equal(rowval, O.rowval), "row indices differ"
+    scale = np.maximum(np.abs(O.nzval), 1e-300)
+    assert np.max(np.abs(nzval - O.nzval) / scale, initial=0) <= AREA_RTOL
+    assert np.allclose(R.dst_areas, O.dst_areas, rtol=AREA_RTOL, atol=0)
+    assert np.allclose(R.src_areas, O.src_areas, rtol=AREA_RTOL, atol=0)
+    if exact:
+        assert np.array_equal(nzval, O.nzval), "areas are not bit-identical"
+        assert np.array_equal(R.dst_areas, O.dst_areas) and np.array_equal(R.src_areas, O.src_areas)
+
+
+def test_readme_known_answer_gpu(cuda):
+    g = json.loads((GOLDEN / "readme_planar.json").read_text())["readme"]
+    R = Regridder(grids.polygon_grid(g["dst"]), grids.polygon_grid(g["src"]), normalize=False)
+    assert np.array_equal(R.intersections.toarray(), np.array(g["matrix"]))
+    assert np.array_equal(R.src_areas, g["src_areas"]) and np.array_equal(R.dst_areas, g["dst_areas"])
+
+
+def test_simple_jl_exact_conservation_gpu(cuda):
+    g = json.loads((GOLDEN / "readme_planar.json").read_text())["simple_jl"]
+    R = Regridder(grids.polygon_grid(g["dst"]), grids.polygon_grid(g["src"]), normalize=False)
+    A = R.intersections
+    assert np.array_equal(np.asarray(A.sum(axis=1)).ravel(), R.dst_areas)
+    assert np.array_equal(np.asarray(A.sum(axis=0)).ravel(), R.src_areas)
+    v2 = np.array(g["values_on_src"], float)
+    v1 = np.zeros(4)
+    regrid_(v1, R, v2)
+    assert np.sum(v1 * R.dst_areas) == np.sum(v2 * R.src_areas)
+    back = np.zeros(5)
+    regrid_(back, R.transpose(), v1)
+    assert np.sum(back * R.src_areas) == np.sum(v2 * R.src_areas)
+
+
+CASES = {
+    "C1_lonlat2_to_lonlat3_shifted": c1_grids,
+    "lonlat4_to_healpix16": lambda: (grids.healpix_grid(16), grids.lonlat_regular(4.0, 4.0)),
+    "healpix16_to_lonlat4": lambda: (grids.lonlat_regular(4.0, 4.0), grids.healpix_grid(16)),
+    "lonlat4_to_healpix8_ring": lambda: (grids.healpix_grid(8, "ring"), grids.lonlat_regular(4.0, 4.0)),
+    "lonlat4_to_cs12": lambda: (grids.cubed_sphere(12), grids.lonlat_regular(4.0, 4.0)),
+    "cs8_to_lonlat5": lambda: (grids.lonlat_regular(5.0, 5.0), grids.cubed_sphere(8)),
+    "jittered_lonlat": lambda: (grids.lonlat_jittered(60, 30, 0.2, 3), grids.lonlat_jittered(90, 45, 0.2, 4)),
+    "jittered_cs_to_lonlat2": lambda: (grids.cubed_sphere(16, jitter=0.15, seed=5), grids.lonlat_regular(2.0, 2.0)),
+    "coincident_lonlat4_lonlat2": lambda: (grids.lonlat_regular(4.0, 4.0), grids.lonlat_regular(2.0, 2.0)),
+    "identical_healpix8": lambda: (grids.healpix_grid(8), grids.healpix_grid(8)),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("normalize", [False, True])
+def test_build_parity(cuda, name, normalize):
+    dst, src = CASES[name]()
+    R = Regridder(dst, src, normalize=normalize)
+    O = oracle.OracleRegridder(dst, src, normalize=normalize)
+    assert R.info["clip_overflows"] == 0
+    assert_parity(R, O)
+
+
+def test_planar_regular_grids(cuda):
+    """Planar RegularGrid on both sides (test/regridding.jl:131-211 style)."""
+    dst = grids.regular_grid(np.linspace(0, 1, 9), np.linspace(0, 1, 9))
+    src = grids.regular_grid(np.linspace(0, 1, 5), np.linspace(0, 1, 5))
+    R = Regridder(dst, src)
+    O = oracle.OracleRegridder(dst, src)
+    assert_parity(R, O)
+    s = np.arange(1.0, 17.0)
+    d = np.zeros(64)
+    regrid_(d, R, s)
+    assert np.array_equal(d, O.apply(s))
+
+
+def test_empty_and_tiny(cuda):
+    # no overlap at all: empty matrix, zero output
+    a = grids.polygon_grid([[(0, 0), (1, 0), (1, 1), (0, 1)]])
+    b = grids.polygon_grid([[(5, 5), (6, 5), (6, 6), (5, 6)], [(2, 2), (3, 2), (3, 3)]])
+    R = Regridder(a, b)
+    assert R.nnz == 0 and R.intersections.shape == (1, 2)
+    d = np.full(1, 7.0)
+    regrid_(d, R, np.array([1.0, 2.0]), normalize=False)
+    assert d[0] == 0.0
+    # one spherical cell on each side
+    one = grids.lonlat_grid([0.0, 10.0], [0.0, 10.0])
+    R1 = Regridder(one, one)
+    O1 = oracle.OracleRegridder(one, one)
+    assert_parity(R1, O1)
+
+
+# ----------------------------------------------------------------- apply
+
+@pytest.fixture(scope="module")
+def c1(cuda):
+    dst, src = c1_grids()
+    return Regridder(dst, src, normalize=True), oracle.OracleRegridder(dst, src, normalize=True)
+
+
+def test_apply_f64_bit_exact(c1):
+    """regrid! in FP64: the reference's column-scatter mul! then ./ a_d; the
+    row gather accumulates in the same order, so results are bit-identical."""
+    R, O = c1
+    rng = np.random.default_rng(11)
+    s = rng.random(R.shape[1])
+    d = np.zeros(R.shape[0])
+    regrid_(d, R, s)
+    assert np.array_equal(d, O.apply(s))
+    # transpose(R) shares the matrices
+    g = rng.random(R.shape[0])
+    back = np.zeros(R.shape[1])
+    regrid_(back, R.transpose(), g)
+    assert np.array_equal(back, O.apply(g, transpose=True))
+    # without normalisation
+    regrid_(d, R, s, normalize=False)
+    assert np.array_equal(d, O.apply(s, normalize=False))
+
+
+def test_apply_f64_many_fields_layouts(c1):
+    import torch
+
+    R, O = c1
+    rng = np.random.default_rng(12)
+    K = 7
+    S = rng.random((K, R.shape[1]))
+    ref = O.apply(S)
+    # field-major (dims=2 over a (K, N) array) on the device
+    st = torch.from_numpy(S).cuda()
+    dt = torch.zeros((K, R.shape[0]), dtype=torch.float64, device="cuda")
+    regrid_(dt, R, st, dims=2)
+    assert np.array_equal(dt.cpu().numpy(), ref)
+    # cell-major (dims=1 over an (N, K) array) on the host
+    Sc = np.ascontiguousarray(S.T)
+    Dc = np.zeros((R.shape[0], K))
+    regrid_(Dc, R, Sc, dims=1)
+    assert np.array_equal(Dc.T, ref)
+
+
+@pytest.mark.parametrize("dtype,tol", [("float32", 1e-5), ("bfloat16", 2e-2)])
+@pytest.mark.parametrize("layout", ["cell_major", "field_major"])
+def test_apply_low_precision(c1, dtype, tol, layout):
+    """FP32 weights, FP32/BF16 fields, FP32 accumulation against the FP64 oracle:
+    max abs error relative to max|d| and the relative error of the conserved
+    area-weighted mean."""
+    import torch
+
+    R, O = c1
+    K = 64
+    rng = np.random.default_rng(13)
+    S = rng.random((K, R.shape[1]))
+    ref = O.apply(S)
+    tdt = getattr(torch, dtype)
+    if layout == "field_major":
+        st = torch.from_numpy(S).to("cuda", tdt)
+        dt = torch.zeros((K, R.shape[0]), dtype=tdt, device="cuda")
+        regrid_(dt, R, st, dims=2)
+        got = dt.double().cpu().numpy()
+    else:
+        st = torch.from_numpy(np.ascontiguousarray(S.T)).to("cuda", tdt)
+        dt = torch.zeros((R.shape[0], K), dtype=tdt, device="cuda")
+        regrid_(dt, R, st, dims=1)
+        got = dt.double().cpu().numpy().T
+    err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
+    assert err <= tol
+    if dtype == "float32":
+        cons_ref = ref @ R.dst_areas
+        cons = got @ R.dst_areas
+        assert np.max(np.abs(cons - cons_ref) / np.abs(cons_ref)) <= 1e-6
+
+
+def test_apply_device_equals_host(c1):
+    import torch
+
+    R, O = c1
+    rng = np.random.default_rng(14)
+    S = rng.standard_normal((3, R.shape[1])).astype(np.float32)
+    host = np.zeros((3, R.shape[0]), np.float32)
+    regrid_(host, R, S, dims=2)
+    dev = torch.zeros((3, R.shape[0]), dtype=torch.float32, device="cuda")
+    regrid_(dev, R, torch.from_numpy(S).cuda(), dims=2)
+    assert np.array_equal(host, dev.cpu().numpy())
+
+
+def test_constant_field_preserved(cuda):
+    """test/usecases/constant_field.jl:41-77 and fullclenshaw.jl:19-31: ones stay
+    ones on covered cells, forward and via transpose."""
+    for dst, src in [(grids.healpix_grid(16), grids.lonlat_regular(4.0, 4.0)),
+                     (grids.cubed_sphere(12), grids.lonlat_jittered(90, 45, 0.2, 9))]:
+        R = Regridder(dst, src, normalize=True)
+        d = regrid(R, np.ones(R.shape[1]))
+        assert np.max(np.abs(d - 1)) < 1e-10
+        s = regrid(R.transpose(), np.ones(R.shape[0]))
+        assert np.max(np.abs(s - 1)) < 1e-10
+
+
+def test_nd_dims_semantics(c1):
+    """N-D regrid! (test/regridding.jl:127-203): every slice along the other
+    axes equals the 1-D result; dims selects the spatial axis."""
+    R, O = c1
+    ns, nd = R.shape[1], R.shape[0]
+    rng = np.random.default_rng(15)
+    s3 = rng.random((3, ns, 2))
+    d3 = np.zeros((3, nd, 2))
+    regrid_(d3, R, s3, dims=2)
+    for a in range(3):
+        for b in range(2):
+            assert np.array_equal(d3[a, :, b], O.apply(s3[a, :, b]))
+    with pytest.raises(ArgumentError):
+        regrid_(d3, R, s3, dims=4)
+    with pytest.raises(DimensionMismatch):
+        regrid_(np.zeros((3, nd, 3)), R, s3, dims=2)
+
+
+def test_strided_vector_routes(c1):
+    """test/regridding.jl:131-211: dense and strided vectors give the same
+    result (==), strided ones through the regridder's temporaries."""
+    R, O = c1
+    ns, nd = R.shape[1], R.shape[0]
+    s = np.random.default_rng(16).random(ns)
+    ref = np.zeros(nd)
+    regrid_(ref, R, s)
+    big_s = np.zeros(2 * ns)
+    big_s[::2] = s
+    big_d = np.zeros(2 * nd)
+    R.src_temp[:] = np.nan
+    R.dst_temp[:] = np.nan
+    regrid_(big_d[::2], R, big_s[::2])
+    assert np.array_equal(big_d[::2], ref)
+    assert not np.isnan(R.src_temp).any() and not np.isnan(R.dst_temp).any()
+
+
+def test_adjoint_dot_product(c1):
+    """<W s, g> == <s, W^T g> for the normalised forward map and for transpose(R)."""
+    R, O = c1
+    rng = np.random.default_rng(17)
+    for RR in (R, R.transpose()):
+        s = rng.standard_normal(RR.shape[1])
+        g = rng.standard_normal(RR.shape[0])
+        d = regrid(RR, s)
+        gs = np.zeros(RR.shape[1])
+        regrid_adjoint_(gs, RR, g)
+        lhs, rhs = d @ g, s @ gs
+        assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
+
+
+def test_transpose_shares_handle(c1):
+    R, _ = c1
+    T = R.transpose()
+    assert T.src_areas is R.dst_areas and T.dst_areas is R.src_areas
+    assert T.src_temp is R.dst_temp and T.dst_temp is R.src_temp
+    assert T.shape == (R.shape[1], R.shape[0])
+    assert (T.intersections != R.intersections.T).nnz == 0
+    del R  # the view keeps the handle alive
+    assert T.transpose().nnz == T.nnz

@@ -1,0 +1,91 @@
+"""Host-side logic of the Python mirror (CPU only): grid builders, manifold
+promotion, N-D stride flattening and the argument errors regrid! raises before
+any device work (src/regridder/regrid.jl:242-245, :289-296)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from crg import grids
+from crg.regridder import (ArgumentError, DimensionMismatch, Regridder, _flat_field_stride, as_grid, promote,
+                           regrid_)
+
+
+def test_lonlat_ring_and_index_order():
+    g = grids.lonlat_regular(90.0, 90.0)
+    t, nv = g.cell_table()
+    assert t.shape == (8, 4, 3) and (nv == 4).all()
+    # cell (i, j) = i + j*nx, ring p(i,j), p(i+1,j), p(i+1,j+1), p(i,j+1)
+    p = g.blocks[0]
+    assert np.array_equal(t[1 + 1 * 4], [p[1, 1], p[1, 2], p[2, 2], p[2, 1]])
+    # degree-exact poles coincide
+    assert np.array_equal(p[-1, 0], [0.0, 0.0, 1.0]) and np.array_equal(p[-1, 3], p[-1, 0])
+
+
+def test_cubed_sphere_faces_ccw_and_offsets():
+    g = grids.cubed_sphere(4)
+    assert g.ncells == 6 * 16 and len(g.blocks) == 6
+    t, _ = g.cell_table()
+    # counter-clockwise seen from outside: (b-a) x (c-a) points outward
+    a, b, c = t[:, 0], t[:, 1], t[:, 2]
+    assert (np.einsum("ij,ij->i", np.cross(b - a, c - a), a) > 0).all()
+
+
+def test_jittered_seam_and_poles():
+    g = grids.lonlat_jittered(36, 18, 0.2, 7)
+    p = g.blocks[0]
+    assert np.allclose(p[:, 0], p[:, -1], atol=1e-15)
+    assert np.allclose(p[0, :, 2], -1.0) and np.allclose(p[-1, :, 2], 1.0)
+
+
+def test_polygon_grid_and_promotion():
+    sq = [[(0, 0), (1, 0), (1, 1), (0, 1), (0, 0)]]
+    tri = [[(0, 0), (1, 0), (0, 1)]]
+    g = as_grid(sq + tri)
+    assert g.kind == "cells" and list(g.nverts) == [4, 3]
+    s = grids.lonlat_regular(30.0, 30.0)
+    d, s2 = promote(g, s)
+    assert d.manifold == "spherical" and s2 is s
+    assert np.allclose(d.cells[0, 1], grids.unit_sphere_from_geographic(1.0, 0.0))
+
+
+def test_flat_field_stride():
+    a = np.zeros((5, 3, 4))  # C order strides (12, 4, 1)
+    assert _flat_field_stride(a.shape, (12, 4, 1), 0) == 1
+    assert _flat_field_stride(a.shape, (12, 4, 1), 2) == 4
+    assert _flat_field_stride(a.shape, (12, 4, 1), 1) is None
+    assert _flat_field_stride((7,), (1,), 0) == 0
+
+
+def _fake_regridder(nd, ns):
+    return Regridder(None, None, _view=dict(_h=None, _transposed=False, info={"n_dst": nd, "n_src": ns, "nnz": 0},
+                                            dst_areas=np.ones(nd), src_areas=np.ones(ns), dst_temp=np.zeros(nd),
+                                            src_temp=np.zeros(ns), _csc=[None]))
+
+
+def test_regrid_argument_errors():
+    R = _fake_regridder(9, 4)
+    with pytest.raises(ArgumentError, match="dims=3 is out of range"):
+        regrid_(np.zeros((9, 3)), R, np.zeros((4, 3)), dims=3)
+    with pytest.raises(DimensionMismatch, match="ranks must match"):
+        regrid_(np.zeros((9, 3, 2)), R, np.zeros((4, 3)))
+    with pytest.raises(DimensionMismatch, match="non-spatial axes must match"):
+        regrid_(np.zeros((9, 3)), R, np.zeros((4, 2)))
+    with pytest.raises(DimensionMismatch):
+        regrid_(np.zeros(8), R, np.zeros(4))
+    with pytest.raises(ArgumentError, match="same element type"):
+        regrid_(np.zeros(9, np.float32), R, np.zeros(4))
+
+
+def test_transpose_view_swaps_areas_and_temps():
+    R = _fake_regridder(9, 4)
+    R._h = type("H", (), {"ptr": 0})()
+    # transpose() retains through the library; emulate the view bookkeeping only
+    view = dict(R.__dict__)
+    view["_transposed"] = True
+    view["dst_areas"], view["src_areas"] = R.src_areas, R.dst_areas
+    view["dst_temp"], view["src_temp"] = R.src_temp, R.dst_temp
+    T = Regridder(None, None, _view=view)
+    assert T.shape == (4, 9)
+    assert T.src_areas is R.dst_areas and T.dst_areas is R.src_areas
+    assert T.src_temp is R.dst_temp and T.dst_temp is R.src_temp

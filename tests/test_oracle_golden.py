@@ -1,0 +1,160 @@
+"""The oracle against the reference's known answers and independent
+high-precision values (CPU only).  This pins the checker before it is used to
+judge the CUDA kernels."""
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import GOLDEN, c1_grids
+from crg import grids
+
+
+def _load(name):
+    return json.loads((GOLDEN / name).read_text())
+
+
+def test_readme_known_answer():
+    """README.md:52-80: every intersection of the 2x2 squares with the diamond and
+    triangles is exactly 0.5; areas [0.5,0.5,2,0.5,0.5] and [1,1,1,1]."""
+    g = _load("readme_planar.json")["readme"]
+    R = oracle.OracleRegridder(grids.polygon_grid(g["dst"]), grids.polygon_grid(g["src"]), normalize=False)
+    assert np.array_equal(R.intersections.toarray(), np.array(g["matrix"]))
+    assert np.array_equal(R.src_areas, g["src_areas"])
+    assert np.array_equal(R.dst_areas, g["dst_areas"])
+
+
+def test_simple_jl_exact_conservation():
+    """test/usecases/simple.jl:30-51: row/col sums == cell areas and the mean is
+    conserved exactly, forward and back."""
+    g = _load("readme_planar.json")["simple_jl"]
+    R = oracle.OracleRegridder(grids.polygon_grid(g["dst"]), grids.polygon_grid(g["src"]), normalize=False)
+    A = R.intersections
+    area1 = np.asarray(A.sum(axis=1)).ravel()
+    area2 = np.asarray(A.sum(axis=0)).ravel()
+    assert np.array_equal(area1, g["dst_areas"]) and np.array_equal(area1, R.dst_areas)
+    assert np.array_equal(area2, g["src_areas"]) and np.array_equal(area2, R.src_areas)
+    v2 = np.array(g["values_on_src"], float)
+    v1 = A @ v2 / area1
+    assert np.sum(v1 * area1) == np.sum(v2 * area2)
+    back = A.T @ v1 / area2
+    assert np.sum(back * area2) == np.sum(v2 * area2)
+
+
+def test_sphere_areas_vs_mpmath():
+    g = _load("sphere_areas.json")
+    for name, c in g["polygons"].items():
+        a = oracle.cell_area(np.array(c["verts"]))
+        ref = float(c["area"])
+        assert abs(a - ref) <= 1e-14 * ref, name
+    for name, c in g["pairs"].items():
+        a = oracle.pair_area(np.array(c["src"]), np.array(c["dst"]))
+        ref = float(c["area"])
+        assert abs(a - ref) <= 1e-14 * max(ref, 1e-300) or (ref == 0 and a <= 0), name
+
+
+def test_atan2_accuracy():
+    rng = np.random.default_rng(1)
+    y = np.concatenate([rng.normal(size=2000), 10.0 ** rng.uniform(-20, 3, 2000) * rng.choice([-1, 1], 2000)])
+    x = np.concatenate([rng.normal(size=2000), 10.0 ** rng.uniform(-20, 3, 2000) * rng.choice([-1, 1], 2000)])
+    for a, b in zip(y, x):
+        r = oracle.atan2(a, b)
+        ref = np.arctan2(a, b)
+        assert abs(r - ref) <= 4 * np.spacing(abs(ref)) + 1e-300
+
+
+def test_healpix_geometry():
+    """HEALPix tree shape and indices (test/extensions/healpix.jl:16-107): 12
+    nside^2 pixels, a permutation for ring order, 4 corners per pixel."""
+    for nside in (1, 2, 4, 16):
+        pix = np.arange(12 * nside * nside)
+        ring = grids.healpix_nest2ring(nside, pix)
+        assert np.array_equal(np.sort(ring), pix)
+        c_np = grids.healpix_corners_nested(nside, pix)
+        for p in pix[:: max(1, len(pix) // 97)]:
+            assert np.array_equal(c_np[p], oracle.healpix_corners(nside, p))
+            assert ring[p] == oracle.healpix_nest2ring(nside, p)
+        assert np.allclose(np.linalg.norm(c_np, axis=-1), 1.0, atol=1e-15)
+    g = grids.healpix_grid(8)
+    R = oracle.OracleRegridder(g, g)
+    assert abs(R.dst_areas.sum() - 4 * np.pi) < 1e-12
+
+
+CASES = {
+    "C1_lonlat2_to_lonlat3_shifted": c1_grids,
+    "lonlat4_to_healpix16": lambda: (grids.healpix_grid(16), grids.lonlat_regular(4.0, 4.0)),
+    "lonlat4_to_healpix8_ring": lambda: (grids.healpix_grid(8, "ring"), grids.lonlat_regular(4.0, 4.0)),
+    "lonlat4_to_cs12": lambda: (grids.cubed_sphere(12), grids.lonlat_regular(4.0, 4.0)),
+    "cs8_to_lonlat5": lambda: (grids.lonlat_regular(5.0, 5.0), grids.cubed_sphere(8)),
+    "jittered": lambda: (grids.lonlat_jittered(60, 30, 0.2, 3), grids.lonlat_jittered(90, 45, 0.2, 4)),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_tree_search_is_complete(name):
+    """The restated dual DFS over the reference's trees finds every pair with
+    positive area that an exhaustive cap test finds (quadtree_cursors.jl:55-80
+    style completeness)."""
+    dst, src = CASES[name]()
+    Rt = oracle.OracleRegridder(dst, src, use_tree=True)
+    Re = oracle.OracleRegridder(dst, src, use_tree=False)
+    assert Rt.nnz > 0 and Rt.overflows == 0
+    assert np.array_equal(Rt.colptr, Re.colptr)
+    assert np.array_equal(Rt.rowval, Re.rowval)
+    assert np.array_equal(Rt.nzval, Re.nzval)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_area_agreement(name):
+    """Row sums of A equal the destination cell areas and column sums the source
+    cell areas where the other grid covers the cell (ConservativeRegriddingTestHelpers
+    test_intersection_areas_agree, rtol = sqrt(eps))."""
+    dst, src = CASES[name]()
+    R = oracle.OracleRegridder(dst, src)
+    A = R.intersections
+    rs = np.asarray(A.sum(axis=1)).ravel()
+    cs = np.asarray(A.sum(axis=0)).ravel()
+    if dst.full_sphere and src.full_sphere:
+        assert np.allclose(rs, R.dst_areas, rtol=np.sqrt(np.finfo(float).eps), atol=0)
+        assert np.allclose(cs, R.src_areas, rtol=np.sqrt(np.finfo(float).eps), atol=0)
+        assert abs(R.dst_areas.sum() - 4 * np.pi) < 1e-11
+    else:
+        assert np.allclose(rs, R.dst_areas, rtol=np.sqrt(np.finfo(float).eps), atol=0)
+        assert np.all(cs <= R.src_areas * (1 + 1e-12))
+
+
+def test_constant_field_and_conservation():
+    """Constant fields stay constant (test/usecases/fullclenshaw.jl:19-31,
+    atol 1e-10) and the area-weighted total is conserved (rtol 1e-10), forward
+    and through the transpose."""
+    dst, src = grids.healpix_grid(16), grids.lonlat_regular(4.0, 4.0)
+    R = oracle.OracleRegridder(dst, src, normalize=True)
+    d = R.apply(np.ones(R.ns))
+    assert np.max(np.abs(d - 1)) < 1e-10
+    s = R.apply(np.ones(R.nd), transpose=True)
+    assert np.max(np.abs(s - 1)) < 1e-10
+    rng = np.random.default_rng(0)
+    f = rng.random(R.ns)
+    d = R.apply(f)
+    assert abs(np.sum(d * R.dst_areas) - np.sum(f * R.src_areas)) <= 1e-10 * abs(np.sum(f * R.src_areas))
+
+
+def test_normalize_divides_by_max():
+    dst, src = c1_grids()
+    R0 = oracle.OracleRegridder(dst, src, normalize=False)
+    R1 = oracle.OracleRegridder(dst, src, normalize=True)
+    m = R0.nzval.max()
+    assert np.array_equal(R1.nzval, R0.nzval / m)
+    assert np.array_equal(R1.dst_areas, R0.dst_areas / m)
+    assert R1.nzval.max() == 1.0
+
+
+def test_disjoint_grids_have_empty_matrix():
+    a = grids.polygon_grid([[(0, 0), (1, 0), (1, 1), (0, 1)]])
+    b = grids.polygon_grid([[(5, 5), (6, 5), (6, 6), (5, 6)], [(2, 2), (3, 2), (3, 3)]])
+    R = oracle.OracleRegridder(a, b)
+    assert R.nnz == 0
+    assert np.array_equal(R.colptr, [0, 0, 0])
