@@ -1,0 +1,428 @@
+"""Benchmark: batched conservative regridding on one GB300.
+
+Workload (the largest single-GPU configuration): HEALPix nside=256 (786,432
+pixels, 4 great-circle corners each, nested order) <-> 0.25-degree lon-lat
+(1440 x 720 = 1,036,800 cells).  R = Regridder(dst=HEALPix, src=lon-lat) is
+built in FP64 on the GPU; one step applies 128 FP32 fields (8 variables x 16
+levels of smooth degree-64 spherical harmonics + N(0, 0.1) noise) forward with
+R and back with transpose(R).  Inputs (0.9 GB per direction) exceed the
+129 MB L2, so no flush is needed between steps.
+
+value  = algorithmic bytes of one step / device time of one step (GB/s), with
+         bytes per direction = nnz*(4 col + 4 weight) + 4*(rows+1)
+                               + 4*K*(cols + rows)   (each field element once).
+e2e    = the same metric through the public API with pinned host buffers:
+         host->device copy, SpMM, device->host copy inside the timed region.
+Also reported: build pairs/s (GPU build of R), plain FP64 one-field-per-launch
+apply, the FP32 error against the FP64 apply, the ncu-free roofline of the
+SpMM kernel, and the CPU oracle on the host cores.
+
+--impl reference times the CPU restatement of the reference's apply (one CSC
+mul! per field, fields spread over all host threads) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "conservativeregridding.jl_gb300"))
+
+METRIC = "batched-apply GB/s (build pairs/s, fields/s, vs plain FP64 apply)"
+WORKLOAD = "healpix256_nested <-> lonlat_0.25deg, 128 fp32 fields, R then transpose(R)"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--fields", type=int, default=128)
+    p.add_argument("--layout", default="field_major", choices=["field_major", "cell_major"])
+    p.add_argument("--nside", type=int, default=256)
+    p.add_argument("--dlon", type=float, default=0.25)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return p.parse_args()
+
+
+def grids_c5(nside, dlon):
+    from crg import grids
+
+    return grids.healpix_grid(nside, "nested"), grids.lonlat_regular(dlon, dlon)
+
+
+def step_bytes(nnz, nd, ns, K, elem=4, idx=4, wbytes=4):
+    """Algorithmic bytes of forward + transpose."""
+    fwd = nnz * (idx + wbytes) + 4 * (nd + 1) + elem * K * (ns + nd)
+    rev = nnz * (idx + wbytes) + 4 * (ns + 1) + elem * K * (ns + nd)
+    return fwd, rev
+
+
+# ----------------------------------------------------------------- synthetic fields
+
+def cell_centres(g):
+    t, nv = g.cell_table()
+    c = t[:, :4].sum(axis=1)
+    return c / np.linalg.norm(c, axis=1, keepdims=True)
+
+
+def sh_fields(centres, K, lmax, seed, noise, device):
+    """K fields sum_{l<=lmax, m} c_lm Ybar_lm + N(0, noise) at unit vectors
+    `centres` (fully normalised real harmonics by the standard three-term
+    recurrence), evaluated on the GPU with torch; returns (K, n) float32."""
+    import torch
+
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    x = torch.as_tensor(centres, dtype=torch.float64, device=device)
+    z = x[:, 2].clamp(-1, 1)
+    s = torch.sqrt((1 - z) * (1 + z))
+    lon = torch.atan2(x[:, 1], x[:, 0])
+    n = x.shape[0]
+    out = torch.zeros((n, K), dtype=torch.float64, device=device)
+    scale = 1.0 / np.sqrt((lmax + 1) ** 2)
+    pmm = torch.ones(n, dtype=torch.float64, device=device)
+    for m in range(lmax + 1):
+        if m > 0:
+            pmm = pmm * s * np.sqrt((2 * m + 1) / (2 * m))
+        L = lmax - m + 1
+        P = torch.empty((n, L), dtype=torch.float64, device=device)
+        P[:, 0] = pmm
+        if L > 1:
+            P[:, 1] = np.sqrt(2 * m + 3) * z * pmm
+        for l in range(m + 2, lmax + 1):
+            a = np.sqrt((4 * l * l - 1) / (l * l - m * m))
+            b = np.sqrt(((l - 1) ** 2 - m * m) / (4 * (l - 1) ** 2 - 1))
+            P[:, l - m] = a * (z * P[:, l - m - 1] - b * P[:, l - m - 2])
+        ca = torch.randn((L, K), generator=gen, dtype=torch.float64).to(device) * scale
+        out += (P @ ca) * torch.cos(m * lon)[:, None]
+        if m > 0:
+            cb = torch.randn((L, K), generator=gen, dtype=torch.float64).to(device) * scale
+            out += (P @ cb) * torch.sin(m * lon)[:, None]
+    out += noise * torch.randn((n, K), generator=gen, dtype=torch.float64).to(device)
+    return out.T.contiguous().float()
+
+
+# ----------------------------------------------------------------- clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- our arm
+
+def run_ours(a, rank, world):
+    import torch
+
+    from crg import Regridder, regrid_
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream(dev)
+    hp, ll = grids_c5(a.nside, a.dlon)
+
+    # --- build: warm once, then time (host grid arrays -> device CSR/CSC)
+    R = Regridder(hp, ll, normalize=True)
+    builds = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Rb = Regridder(hp, ll, normalize=True)
+        torch.cuda.synchronize()
+        builds.append(time.perf_counter() - t0)
+        info = Rb.info
+        del Rb
+    build_s = statistics.median(builds)
+    nnz, nd, ns = R.nnz, R.shape[0], R.shape[1]
+    T = R.transpose()
+    K = a.fields
+
+    # --- fields
+    src = sh_fields(cell_centres(ll), K, 64, 1, 0.1, dev)  # (K, ns)
+    dsrc = sh_fields(cell_centres(hp), K, 64, 2, 0.1, dev)  # (K, nd) input of the transpose
+    if a.layout == "cell_major":
+        src, dsrc = src.T.contiguous(), dsrc.T.contiguous()
+        dims = 1
+        out_f = torch.empty((nd, K), dtype=torch.float32, device=dev)
+        out_r = torch.empty((ns, K), dtype=torch.float32, device=dev)
+    else:
+        dims = 2
+        out_f = torch.empty((K, nd), dtype=torch.float32, device=dev)
+        out_r = torch.empty((K, ns), dtype=torch.float32, device=dev)
+
+    def step():
+        regrid_(out_f, R, src, dims=dims)
+        regrid_(out_r, T, dsrc, dims=dims)
+
+    for _ in range(max(a.warmup, 3)):
+        step()
+    # per-kernel events for the roofline (launches are on `stream`)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    kf, kr = [], []
+    for _ in range(5):
+        ev[0].record(stream)
+        regrid_(out_f, R, src, dims=dims)
+        ev[1].record(stream)
+        regrid_(out_r, T, dsrc, dims=dims)
+        ev[2].record(stream)
+        ev[2].synchronize()
+        kf.append(ev[0].elapsed_time(ev[1]))
+        kr.append(ev[1].elapsed_time(ev[2]))
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        start.record(stream)
+        for _ in range(a.steps):
+            step()
+        stop.record(stream)
+        stop.synchronize()
+    torch.cuda.synchronize()
+    ms = start.elapsed_time(stop) / a.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    bf, br = step_bytes(nnz, nd, ns, K)
+    value = world * (bf + br) / (ms * 1e-3) / 1e9
+
+    # --- accuracy against the FP64 apply (bit-exact with the oracle, see tests)
+    src64 = src.double()
+    out64 = torch.empty(out_f.shape, dtype=torch.float64, device=dev)
+    regrid_(out64, R, src64, dims=dims)
+    f32 = out_f.double()
+    max_abs = float((f32 - out64).abs().max() / out64.abs().max())
+    ad = torch.as_tensor(R.dst_areas, device=dev)
+    as_ = torch.as_tensor(R.src_areas, device=dev)
+    fa = (0 if dims == 1 else 1)
+    tot_ref = (out64 * (ad[:, None] if dims == 1 else ad[None, :])).sum(dim=fa)
+    tot = (f32 * (ad[:, None] if dims == 1 else ad[None, :])).sum(dim=fa)
+    tot_src = (src64 * (as_[:, None] if dims == 1 else as_[None, :])).sum(dim=fa)
+    cons_err = float(((tot - tot_ref).abs() / tot_ref.abs()).max())
+    cons_err_src = float(((tot - tot_src).abs() / tot_src.abs()).max())
+
+    # --- plain FP64, one field per launch
+    s1 = src64[0] if dims == 2 else src64[:, 0].contiguous()
+    d1 = torch.empty(nd, dtype=torch.float64, device=dev)
+    r1 = dsrc.double()[0] if dims == 2 else dsrc.double()[:, 0].contiguous()
+    o1 = torch.empty(ns, dtype=torch.float64, device=dev)
+    for _ in range(3):
+        regrid_(d1, R, s1)
+        regrid_(o1, T, r1)
+    start.record(stream)
+    n64 = 20
+    for _ in range(n64):
+        regrid_(d1, R, s1)
+        regrid_(o1, T, r1)
+    stop.record(stream)
+    stop.synchronize()
+    ms64 = start.elapsed_time(stop) / n64
+    b64f = nnz * 12 + 4 * (nd + 1) + 8 * (ns + nd) + 8 * nd
+    b64r = nnz * 12 + 4 * (ns + 1) + 8 * (ns + nd) + 8 * ns
+    fp64_gbs = (b64f + b64r) / (ms64 * 1e-3) / 1e9
+
+    # --- e2e through the public API with pinned host buffers
+    hs = src.cpu().pin_memory()
+    hd = dsrc.cpu().pin_memory()
+    ho_f = torch.empty(tuple(out_f.shape), dtype=torch.float32).pin_memory()
+    ho_r = torch.empty(tuple(out_r.shape), dtype=torch.float32).pin_memory()
+
+    def step_host():
+        regrid_(ho_f, R, hs, dims=dims)
+        regrid_(ho_r, T, hd, dims=dims)
+
+    step_host()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ne = max(3, a.steps // 4)
+    for _ in range(ne):
+        step_host()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / ne
+    h2d = 4 * K * (ns + nd)
+    d2h = 4 * K * (nd + ns)
+    assert torch.equal(ho_f, out_f.cpu()), "host-buffer apply differs from the device apply"
+
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    kms = statistics.median(kf + kr)
+    achieved = ((bf + br) / 2) / (kms * 1e-3) / 1e9
+    line = {
+        "metric": METRIC,
+        "value": round(value, 2),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": round(ms, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 fields, fp32 weights, fp32 accumulate (fp64 build)",
+        "data": "synthetic: degree-64 spherical harmonics + N(0,0.1) noise",
+        "config": {"workload": WORKLOAD, "n_dst": nd, "n_src": ns, "nnz": nnz, "fields": K, "layout": a.layout,
+                   "l2": "inputs 0.9 GB per direction > 129 MB L2, no flush", "parallelism": f"replicas x{world}"},
+        "fields_per_s": round(world * 2 * K / (ms * 1e-3), 1),
+        "build": {"ms": round(build_s * 1e3, 3), "pairs_per_s": round(nnz / build_s, 1),
+                  "candidates": info["n_candidates"], "search_ms": round(info["t_search_ms"], 3),
+                  "clip_ms": round(info["t_clip_ms"], 3), "assemble_ms": round(info["t_assemble_ms"], 3)},
+        "fp64_one_field_per_launch": {"ms_per_field_both_directions": round(ms64, 4), "GB/s": round(fp64_gbs, 2),
+                                      "fields_per_s": round(2 / (ms64 * 1e-3), 1)},
+        "accuracy_vs_fp64": {"max_abs_err_rel_to_max": max_abs, "mean_conservation_rel_err": cons_err,
+                             "mean_conservation_rel_err_vs_src_total": cons_err_src},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "kernel": "k_spmm_tile" if a.layout == "field_major" else "k_spmm_rows",
+                     "launch_ms": {"forward": round(statistics.median(kf), 4), "transpose": round(statistics.median(kr), 4)},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)"},
+        "e2e": {"value": round(world * (bf + br) / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * a.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(hp, ll, K, sample_fields=8)
+    return line
+
+
+# ----------------------------------------------------------------- CPU legs (oracle)
+
+def cpu_baseline(hp, ll, K, sample_fields):
+    """The oracle's apply (reference algorithm: one CSC mul! per field then ./
+    areas; fields over all host threads) on a bounded sample of the workload."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    t0 = time.perf_counter()
+    O = oracle.OracleRegridder(hp, ll, normalize=True)
+    tb = time.perf_counter() - t0
+    rng = np.random.default_rng(3)
+    S = rng.standard_normal((sample_fields, O.ns))
+    D = rng.standard_normal((sample_fields, O.nd))
+    O.apply(S[:1])
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        O.apply(S)
+        O.apply(D, transpose=True)
+    t = (time.perf_counter() - t0) / reps
+    bf, br = step_bytes(O.nnz, O.nd, O.ns, sample_fields, elem=8, idx=8, wbytes=8)
+    cores = oracle.load().og_num_threads()
+    return {"value": round((bf + br) / t / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+            "sample": f"{sample_fields} of {K} fields, forward + transpose, fp64 (reference precision); "
+                      f"oracle build {tb:.2f}s = {O.nnz / tb:.3g} pairs/s on {cores} threads"}
+
+
+def run_reference(a):
+    """The reference arm: CPU restatement of regrid! with R and transpose(R)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    hp, ll = grids_c5(a.nside, a.dlon)
+    O = oracle.OracleRegridder(hp, ll, normalize=True)
+    K = 16  # bounded sample per step (of the 128 fields)
+    rng = np.random.default_rng(3)
+    S = rng.standard_normal((K, O.ns))
+    D = rng.standard_normal((K, O.nd))
+    for _ in range(a.warmup):
+        O.apply(S)
+        O.apply(D, transpose=True)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        O.apply(S)
+        O.apply(D, transpose=True)
+    ms = (time.perf_counter() - t0) * 1e3 / a.steps
+    bf, br = step_bytes(O.nnz, O.nd, O.ns, K, elem=8, idx=8, wbytes=8)
+    value = (bf + br) / (ms * 1e-3) / 1e9
+    cores = oracle.load().og_num_threads()
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "GB/s", "n_gpus": 0,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_dst": O.nd, "n_src": O.ns, "nnz": O.nnz, "fields": a.fields},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": f"{K} of {a.fields} fields per step, forward + transpose (C restatement of the "
+                                   "reference apply; Julia is not installed)"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    a = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if a.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(a)))
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group("nccl")
+    line = run_ours(a, rank, world)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

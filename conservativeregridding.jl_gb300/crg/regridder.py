@@ -259,6 +259,14 @@ def _flat_field_stride(shape, strides, dim):
     return axes[-1][1]
 
 
+def _moveaxis(x, src, dst):
+    if _is_torch(x):
+        import torch
+
+        return torch.movedim(x, src, dst)
+    return np.moveaxis(x, src, dst)
+
+
 def _contiguous_like(x):
     if _is_torch(x):
         return x.contiguous()
@@ -328,22 +336,24 @@ def _regrid(dst_field, R: Regridder, src_field, dims: int, normalize: bool, adjo
 
     ssf = _flat_field_stride(src.shape, src.strides, d)
     dsf = _flat_field_stride(dst.shape, dst.strides, d)
-    s_obj, d_obj = src_field, dst_field
-    if ssf is None:
-        s_obj = _contiguous_like(src_field)
-        src = _Field(s_obj)
-        ssf = _flat_field_stride(src.shape, src.strides, d)
+    ssc, dsc = src.strides[d], dst.strides[d]
     staged_dst = None
+    if ssf is None:
+        # the other axes do not collapse to one stride: stage a copy with the
+        # spatial axis last (fields one after another)
+        s_obj = _contiguous_like(_moveaxis(src_field, d, -1))
+        src = _Field(s_obj)
+        ssc, ssf = 1, n_in
     if dsf is None:
-        staged_dst = _contiguous_like(dst_field)
+        staged_dst = _contiguous_like(_moveaxis(dst_field, d, -1))
         dst = _Field(staged_dst)
-        dsf = _flat_field_stride(dst.shape, dst.strides, d)
+        dsc, dsf = 1, n_out
     if nf == 1:
         ssf = ssf or 1
         dsf = dsf or 1
-    _call(R, adjoint, src, src.strides[d], ssf, dst, dst.strides[d], dsf, nf, normalize, stream)
+    _call(R, adjoint, src, ssc, ssf, dst, dsc, dsf, nf, normalize, stream)
     if staged_dst is not None:
-        dst_field[...] = staged_dst
+        _moveaxis(dst_field, d, -1)[...] = staged_dst
     return dst_field
 
 
