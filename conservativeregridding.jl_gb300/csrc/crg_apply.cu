@@ -189,13 +189,213 @@ __global__ void k_spmm_generic(const int32_t* __restrict__ ptr, const int32_t* _
   st1<T>(y + r * ysc + f * ysf, acc);
 }
 
+// ------------------------------------------------------------------ staged tiles
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+template <class T> __device__ __forceinline__ float4 lds4(const T* p);
+template <> __device__ __forceinline__ float4 lds4<float>(const float* p) { return *reinterpret_cast<const float4*>(p); }
+template <> __device__ __forceinline__ float4 lds4<__nv_bfloat16>(const __nv_bfloat16* p) {
+  uint2 u = *reinterpret_cast<const uint2*>(p);
+  float2 a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&u.x));
+  float2 b = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&u.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+template <class T, int KC>
+__host__ __device__ constexpr int stage_stride() { return KC + 16 / (int)sizeof(T); }
+
+template <class T, bool kFM, int KC>
+constexpr size_t tiled_smem() {
+  return (size_t)kTileUMax * stage_stride<T, KC>() * sizeof(T) + (kFM ? (size_t)kTileRows * (KC + 1) * sizeof(float) : 0);
+}
+
+// One CTA per staged tile.  For each chunk of KC fields: copy the tile's
+// distinct source columns into shared memory (cp.async; 16-byte pieces of a
+// cell's contiguous fields when cell-major, 4-byte gathers when field-major),
+// then G = KC/4 lanes per row accumulate 4 fields each from shared memory in
+// FP32 and write the row (cell-major) or stage it and write field by field
+// (field-major, so the stores are runs of consecutive cells).
+template <class T, bool kFM, int KC>
+__global__ void __launch_bounds__(256, 2) k_spmm_tiled(const int2* __restrict__ tiles, const int32_t* __restrict__ uoff,
+                                                       const int32_t* __restrict__ ucol,
+                                                       const int32_t* __restrict__ rows,
+                                                       const int32_t* __restrict__ lptr,
+                                                       const uint16_t* __restrict__ lcol,
+                                                       const float* __restrict__ lw, const T* __restrict__ x,
+                                                       int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
+  constexpr int SP = stage_stride<T, KC>();
+  constexpr int G = KC / 4;
+  constexpr int RPW = 32 / G;
+  constexpr int OS = KC + 1;
+  extern __shared__ __align__(16) unsigned char smem[];
+  T* stage = reinterpret_cast<T*>(smem);
+  float* outs = reinterpret_cast<float*>(smem + (size_t)kTileUMax * SP * sizeof(T));
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane % G, sub = lane / G;
+  const int2 tr = tiles[blockIdx.x];
+  const int p0 = tr.x, nr = tr.y - tr.x;
+  const int u0 = uoff[blockIdx.x], u = uoff[blockIdx.x + 1] - u0;
+  for (int64_t f0 = 0; f0 < nf; f0 += KC) {
+    const int kc = (int)(nf - f0 < KC ? nf - f0 : KC);
+    if (!kFM) {
+      const int cpc = kc * (int)sizeof(T) / 16;
+      for (int i = tid; i < u * cpc; i += 256) {
+        const int c = i / cpc, q = i - c * cpc;
+        cp_async16(stage + c * SP + q * (16 / (int)sizeof(T)), x + (int64_t)__ldg(ucol + u0 + c) * xs + f0 + q * (16 / (int)sizeof(T)));
+      }
+    } else {
+      for (int i = tid; i < u * kc; i += 256) {
+        const int f = i / u, c = i - f * u;
+        const T* src = x + (f0 + f) * xs + __ldg(ucol + u0 + c);
+        if (sizeof(T) == 4) cp_async4(stage + c * SP + f, src);
+        else stage[c * SP + f] = *src;
+      }
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    for (int rb = warp * RPW + sub; rb < nr; rb += 8 * RPW) {
+      const int p = p0 + rb;
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (g * 4 < kc) {
+        const int k1 = lptr[p + 1];
+        for (int k = lptr[p]; k < k1; ++k) {
+          const int lc = lcol[k];
+          const float w = lw[k];
+          const float4 v = lds4<T>(stage + lc * SP + g * 4);
+          acc.x = fmaf(w, v.x, acc.x);
+          acc.y = fmaf(w, v.y, acc.y);
+          acc.z = fmaf(w, v.z, acc.z);
+          acc.w = fmaf(w, v.w, acc.w);
+        }
+        if (!kFM) {
+          st4<T>(y + (int64_t)rows[p] * ys + f0 + g * 4, acc);
+        } else {
+          float* o = outs + rb * OS + g * 4;
+          o[0] = acc.x; o[1] = acc.y; o[2] = acc.z; o[3] = acc.w;
+        }
+      }
+    }
+    if (kFM) {
+      __syncthreads();
+      for (int i = tid; i < kc * nr; i += 256) {
+        const int f = i / nr, r = i - f * nr;
+        st1<T>(y + (f0 + f) * ys + rows[p0 + r], outs[r * OS + f]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Rows left out of the tiles (too many distinct columns), cell-major fields:
+// one warp per row, 4 fields per lane.
 template <class T>
-void launch_f32(const DevCsr& c, const float* w, const T* x, int64_t xsc, int64_t xsf, T* y, int64_t ysc, int64_t ysf,
-                int64_t nf, cudaStream_t st) {
+__global__ void __launch_bounds__(256) k_direct_cm(const int32_t* __restrict__ pos, int64_t npos,
+                                                   const int32_t* __restrict__ rows, const int32_t* __restrict__ ptr,
+                                                   const int32_t* __restrict__ idx, const float* __restrict__ w,
+                                                   const T* __restrict__ x, int64_t xs, T* __restrict__ y, int64_t ys,
+                                                   int64_t nf) {
+  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wi >= npos) return;
+  const int32_t r = rows[pos[wi]];
+  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
+  for (int64_t f = (int64_t)lane * 4; f < nf; f += 128) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int32_t k = k0; k < k1; ++k) {
+      const float4 v = ld4<T>(x + (int64_t)idx[k] * xs + f);
+      const float ww = w[k];
+      acc.x = fmaf(ww, v.x, acc.x);
+      acc.y = fmaf(ww, v.y, acc.y);
+      acc.z = fmaf(ww, v.z, acc.z);
+      acc.w = fmaf(ww, v.w, acc.w);
+    }
+    st4<T>(y + (int64_t)r * ys + f, acc);
+  }
+}
+
+// Rows left out of the tiles, field-major fields: one warp per row, lanes
+// split the row's entries, warp reduction per field.
+template <class T>
+__global__ void __launch_bounds__(256) k_direct_fm(const int32_t* __restrict__ pos, int64_t npos,
+                                                   const int32_t* __restrict__ rows, const int32_t* __restrict__ ptr,
+                                                   const int32_t* __restrict__ idx, const float* __restrict__ w,
+                                                   const T* __restrict__ x, int64_t xs, T* __restrict__ y, int64_t ys,
+                                                   int64_t nf) {
+  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wi >= npos) return;
+  const int32_t r = rows[pos[wi]];
+  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
+  for (int64_t f = 0; f < nf; ++f) {
+    float acc = 0.f;
+    for (int32_t k = k0 + lane; k < k1; k += 32) acc = fmaf(w[k], ld1<T>(x + f * xs + idx[k]), acc);
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) st1<T>(y + f * ys + r, acc);
+  }
+}
+
+template <class T, bool kFM, int KC>
+void launch_tiled_kc(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xs, T* y, int64_t ys,
+                     int64_t nf, cudaStream_t st) {
+  const DevTiles& tl = c.tiles;
+  const float* lw = normalize ? (adjoint ? tl.lw_adj : tl.lw_wn) : tl.lw_val;
+  const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
+  constexpr size_t smem = tiled_smem<T, kFM, KC>();
+  static bool configured = false;  // per template instance
+  if (!configured) {
+    CRG_CHECK_CUDA(cudaFuncSetAttribute(k_spmm_tiled<T, kFM, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    configured = true;
+  }
+  if (tl.ngood) {
+    k_spmm_tiled<T, kFM, KC><<<(unsigned)tl.ngood, 256, smem, st>>>(tl.tiles, tl.uoff, tl.ucol, tl.rows, tl.lptr, tl.lcol,
+                                                                     lw, x, xs, y, ys, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  if (tl.ndirect) {
+    const unsigned blocks = nblk(tl.ndirect * 32, 256);
+    if (kFM) k_direct_fm<T><<<blocks, 256, 0, st>>>(tl.direct, tl.ndirect, tl.rows, c.ptr, c.idx, w, x, xs, y, ys, nf);
+    else k_direct_cm<T><<<blocks, 256, 0, st>>>(tl.direct, tl.ndirect, tl.rows, c.ptr, c.idx, w, x, xs, y, ys, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+}
+
+template <class T, bool kFM>
+void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                  cudaStream_t st) {
+  if (nf >= 128) launch_tiled_kc<T, kFM, 128>(c, normalize, adjoint, x, xs, y, ys, nf, st);
+  else if (nf >= 64) launch_tiled_kc<T, kFM, 64>(c, normalize, adjoint, x, xs, y, ys, nf, st);
+  else launch_tiled_kc<T, kFM, 32>(c, normalize, adjoint, x, xs, y, ys, nf, st);
+}
+
+template <class T>
+void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xsc, int64_t xsf, T* y,
+                int64_t ysc, int64_t ysf, int64_t nf, cudaStream_t st) {
   const int64_t n = c.nrows;
   if (n == 0 || nf == 0) return;
+  const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
   const bool cell_major = (xsf == 1 && ysf == 1) && nf > 1;
-  const bool field_major = (xsc == 1 && ysc == 1);
+  const bool field_major = (xsc == 1 && ysc == 1) && nf > 1;
+  const int es = (int)sizeof(T);
+  const int vecf = 16 / es;  // fields per 16 bytes
+  // staged tiles for batches of >= 16 fields
+  if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 &&
+      (uintptr_t)x % 16 == 0 && (uintptr_t)y % (4 * es) == 0) {
+    launch_tiled<T, false>(c, normalize, adjoint, x, xsc, y, ysc, nf, st);
+    return;
+  }
+  if (field_major && nf >= 16) {
+    launch_tiled<T, true>(c, normalize, adjoint, x, xsf, y, ysf, nf, st);
+    return;
+  }
   if (cell_major) {
     const bool vec = (xsc % 4 == 0) && (ysc % 4 == 0) && (nf % 4 == 0) &&
                      ((uintptr_t)x % (4 * sizeof(T)) == 0) && ((uintptr_t)y % (4 * sizeof(T)) == 0);
@@ -298,11 +498,11 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
     }
     CRG_CHECK_CUDA(cudaGetLastError());
   } else {
-    const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
     if (dtype == CRG_F32)
-      launch_f32<float>(c, w, (const float*)xs, ssc, ssf, (float*)ys, dsc, dsf, nf, st);
+      launch_f32<float>(c, normalize, adjoint, (const float*)xs, ssc, ssf, (float*)ys, dsc, dsf, nf, st);
     else
-      launch_f32<__nv_bfloat16>(c, w, (const __nv_bfloat16*)xs, ssc, ssf, (__nv_bfloat16*)ys, dsc, dsf, nf, st);
+      launch_f32<__nv_bfloat16>(c, normalize, adjoint, (const __nv_bfloat16*)xs, ssc, ssf, (__nv_bfloat16*)ys, dsc,
+                                dsf, nf, st);
   }
 
   if (dst_host) CRG_CHECK_CUDA(cudaMemcpyAsync(dst, ys, (size_t)out_span * es, cudaMemcpyDeviceToHost, st));

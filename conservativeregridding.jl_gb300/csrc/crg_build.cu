@@ -851,6 +851,7 @@ bool is_device_pointer(const void* p) {
 }
 
 void free_csr(DevCsr& c) {
+  free_tiles(c.tiles);
   cudaFree(c.ptr); cudaFree(c.idx); cudaFree(c.val); cudaFree(c.val32); cudaFree(c.wn32); cudaFree(c.adj32);
   c = DevCsr{};
 }
@@ -995,6 +996,9 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
       k_derive<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, R->rev.idx, R->rev.val, ns, R->src_area, R->dst_area,
                                               R->rev.val32, R->rev.wn32, R->rev.adj32, R->col_sum);
     CRG_CHECK_CUDA(cudaGetLastError());
+    // staged-tile layouts, rows in the spatial order of their cells
+    build_tiles(R->fwd, td.perm.p, st);
+    build_tiles(R->rev, ts.perm.p, st);
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[3], st));
     CRG_CHECK_CUDA(cudaEventSynchronize(ev.e[3]));
     float t01 = 0, t12 = 0, t23 = 0, t03 = 0;

@@ -35,6 +35,25 @@ struct Fail {
     }                                         \
   } while (0)
 
+// Row tiles of one direction (see crg_tiles.cu).
+constexpr int kTileRows = 64;    // rows of a full tile
+constexpr int kTileUMax = 128;   // distinct source columns a tile may stage
+constexpr int kTileEMax = 2048;  // entries a tile may hold
+
+struct DevTiles {
+  int64_t ngood = 0, ndirect = 0, nucol = 0;
+  int32_t* rows = nullptr;     // [nrows] processing order: position -> row
+  int32_t* lptr = nullptr;     // [nrows+1] entry offsets in processing order
+  uint16_t* lcol = nullptr;    // [nnz] column index inside the tile's distinct set
+  float* lw_val = nullptr;     // [nnz] val32 in processing order
+  float* lw_wn = nullptr;      // [nnz] wn32 in processing order
+  float* lw_adj = nullptr;     // [nnz] adj32 in processing order
+  int2* tiles = nullptr;       // [ngood] position ranges [x, y) of staged tiles
+  int32_t* uoff = nullptr;     // [ngood+1] offsets into ucol
+  int32_t* ucol = nullptr;     // [nucol] distinct source columns per tile, ascending
+  int32_t* direct = nullptr;   // [ndirect] positions of rows applied by direct gathers
+};
+
 // Device CSR of one direction.  rows = dst cells for the forward copy,
 // src cells for the reverse copy (A^T).
 struct DevCsr {
@@ -45,6 +64,7 @@ struct DevCsr {
   float* val32 = nullptr;    // [nnz] A entries (FP32)
   float* wn32 = nullptr;     // [nnz] A_rc / area_row (FP32): normalised weights of this direction
   float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
+  DevTiles tiles;            // staged-tile layout for the batched FP32/BF16 apply
 };
 
 // Per-cell vertex table on the device: [n][maxv] unit vectors (z = 0 planar).
@@ -84,4 +104,6 @@ void free_regridder(crg_regridder* r);
 void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, const void* src, int64_t ssc,
                 int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int normalize, cudaStream_t st);
 bool is_device_pointer(const void* p);
+void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st);
+void free_tiles(DevTiles& t);
 }  // namespace crg
