@@ -295,7 +295,8 @@ def test_apply_tiled_paths(cuda, case, K, layout, dtype):
     dst, src = TILED_CASES[case]()
     R = Regridder(dst, src, normalize=True)
     O = oracle.OracleRegridder(dst, src, normalize=True)
-    tol = 2e-6 if dtype == "float32" else 2e-2
+    # FP32 accumulation over rows of up to ~1600 entries (20-degree cells over 0.5 degrees)
+    tol = 1e-5 if dtype == "float32" else 2e-2
     tdt = getattr(torch, dtype)
     rng = np.random.default_rng(21)
     for transpose in (False, True):
