@@ -51,7 +51,50 @@ def parse():
     p.add_argument("--nside", type=int, default=256)
     p.add_argument("--dlon", type=float, default=0.25)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--profile", action="store_true",
+                   help="only build and run `steps` forward+transpose SpMM rounds (for an ncu capture)")
     return p.parse_args()
+
+
+def run_profile(a):
+    """Build R, make the fields, run a.steps rounds of forward + transpose
+    SpMM and print per-launch times and the tile layout statistics."""
+    import torch
+
+    from crg import Regridder, regrid_
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    hp, ll = grids_c5(a.nside, a.dlon)
+    R = Regridder(hp, ll, normalize=True)
+    T = R.transpose()
+    K, nd, ns = a.fields, R.shape[0], R.shape[1]
+    gen = torch.Generator(device=dev).manual_seed(0)
+    if a.layout == "cell_major":
+        src = torch.randn((ns, K), generator=gen, device=dev)
+        dsrc = torch.randn((nd, K), generator=gen, device=dev)
+        out_f = torch.empty((nd, K), device=dev)
+        out_r = torch.empty((ns, K), device=dev)
+        dims = 1
+    else:
+        src = torch.randn((K, ns), generator=gen, device=dev)
+        dsrc = torch.randn((K, nd), generator=gen, device=dev)
+        out_f = torch.empty((K, nd), device=dev)
+        out_r = torch.empty((K, ns), device=dev)
+        dims = 2
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    for i in range(a.steps):
+        ev[0].record()
+        regrid_(out_f, R, src, dims=dims)
+        ev[1].record()
+        regrid_(out_r, T, dsrc, dims=dims)
+        ev[2].record()
+        ev[2].synchronize()
+        bf, br = step_bytes(R.nnz, nd, ns, K)
+        print(json.dumps({"round": i, "fwd_ms": ev[0].elapsed_time(ev[1]), "rev_ms": ev[1].elapsed_time(ev[2]),
+                          "fwd_GBs": bf / ev[0].elapsed_time(ev[1]) / 1e6, "rev_GBs": br / ev[1].elapsed_time(ev[2]) / 1e6}))
+    info = {k: R.info[k] for k in ("nnz", "tiles", "tile_columns", "direct_rows", "n_dst", "n_src")}
+    print(json.dumps(info))
 
 
 def grids_c5(nside, dlon):
@@ -405,6 +448,9 @@ def main():
     a = parse()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if a.profile:
+        run_profile(a)
+        return
     if a.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(a)))

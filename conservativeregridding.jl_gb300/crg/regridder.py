@@ -112,7 +112,8 @@ class Regridder:
         self._transposed = False
         info = _lib.crg_info()
         check(lib.crg_regridder_info(C.c_void_p(h.value), C.byref(info)))
-        self.info = {k: getattr(info, k) for k, _ in _lib.crg_info._fields_ if k != "pad"}
+        self.info = {k: (list(getattr(info, k)) if k in ("tiles", "tile_columns", "direct_rows") else getattr(info, k))
+                     for k, _ in _lib.crg_info._fields_ if k != "pad"}
         nd, ns = info.n_dst, info.n_src
         self.dst_areas = np.empty(nd)
         self.src_areas = np.empty(ns)

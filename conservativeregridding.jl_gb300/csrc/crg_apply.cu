@@ -21,6 +21,8 @@
 //                   entries in shared memory once, then sweeps all fields.
 //   k_spmm_generic  any strides, one thread per (row, field).
 #include <cuda_bf16.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include <algorithm>
 
@@ -129,25 +131,25 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
 
 // ------------------------------------------------------------------ field-major fields
 
-constexpr int kTileRows = 128;
-constexpr int kTileEntries = 4096;  // shared-memory capacity (32 KB)
-constexpr int kTileF = 8;           // fields per sweep step
+constexpr int kFmRows = 128;
+constexpr int kFmEntries = 4096;  // shared-memory capacity (32 KB)
+constexpr int kFmF = 8;           // fields per sweep step
 
 template <class T>
-__global__ void __launch_bounds__(kTileRows) k_spmm_tile(const int32_t* __restrict__ ptr,
+__global__ void __launch_bounds__(kFmRows) k_spmm_tile(const int32_t* __restrict__ ptr,
                                                           const int32_t* __restrict__ idx,
                                                           const float* __restrict__ w, int64_t nrows,
                                                           const T* __restrict__ x, int64_t xsf, T* __restrict__ y,
                                                           int64_t ysf, int64_t nf) {
-  __shared__ int32_t s_idx[kTileEntries];
-  __shared__ float s_w[kTileEntries];
-  const int64_t r0 = (int64_t)blockIdx.x * kTileRows;
+  __shared__ int32_t s_idx[kFmEntries];
+  __shared__ float s_w[kFmEntries];
+  const int64_t r0 = (int64_t)blockIdx.x * kFmRows;
   const int64_t r = r0 + threadIdx.x;
-  const int64_t rend = min(nrows, r0 + kTileRows);
+  const int64_t rend = min(nrows, r0 + kFmRows);
   const int32_t e0 = ptr[r0], e1 = ptr[rend];
-  const bool staged = (e1 - e0) <= kTileEntries;
+  const bool staged = (e1 - e0) <= kFmEntries;
   if (staged) {
-    for (int32_t e = e0 + threadIdx.x; e < e1; e += kTileRows) {
+    for (int32_t e = e0 + threadIdx.x; e < e1; e += kFmRows) {
       s_idx[e - e0] = idx[e];
       s_w[e - e0] = w[e];
     }
@@ -155,22 +157,22 @@ __global__ void __launch_bounds__(kTileRows) k_spmm_tile(const int32_t* __restri
   __syncthreads();
   if (r >= nrows) return;
   const int32_t k0 = ptr[r], k1 = ptr[r + 1];
-  for (int64_t f0 = 0; f0 < nf; f0 += kTileF) {
-    float acc[kTileF];
+  for (int64_t f0 = 0; f0 < nf; f0 += kFmF) {
+    float acc[kFmF];
 #pragma unroll
-    for (int q = 0; q < kTileF; ++q) acc[q] = 0.f;
-    const int nq = (int)(nf - f0 < kTileF ? nf - f0 : kTileF);
+    for (int q = 0; q < kFmF; ++q) acc[q] = 0.f;
+    const int nq = (int)(nf - f0 < kFmF ? nf - f0 : kFmF);
     for (int32_t k = k0; k < k1; ++k) {
       const int64_t j = staged ? s_idx[k - e0] : idx[k];
       const float ww = staged ? s_w[k - e0] : w[k];
       const T* xp = x + f0 * xsf + j;
 #pragma unroll
-      for (int q = 0; q < kTileF; ++q)
+      for (int q = 0; q < kFmF; ++q)
         if (q < nq) acc[q] = fmaf(ww, ld1<T>(xp + q * xsf), acc[q]);
     }
     T* yp = y + f0 * ysf + r;
 #pragma unroll
-    for (int q = 0; q < kTileF; ++q)
+    for (int q = 0; q < kFmF; ++q)
       if (q < nq) st1<T>(yp + q * ysf, acc[q]);
   }
 }
@@ -386,13 +388,19 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
   const bool field_major = (xsc == 1 && ysc == 1) && nf > 1;
   const int es = (int)sizeof(T);
   const int vecf = 16 / es;  // fields per 16 bytes
-  // staged tiles for batches of >= 16 fields
-  if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 &&
+  // CRG_SPMM_PATH=rows forces the direct row-gather kernels (a tuning and
+  // profiling switch; the default picks staged tiles for >= 16 fields).
+  static const bool force_rows = [] {
+    const char* e = getenv("CRG_SPMM_PATH");
+    return e && strcmp(e, "rows") == 0;
+  }();
+  if (force_rows) {
+    // fall through to the direct kernels below
+  } else if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 &&
       (uintptr_t)x % 16 == 0 && (uintptr_t)y % (4 * es) == 0) {
     launch_tiled<T, false>(c, normalize, adjoint, x, xsc, y, ysc, nf, st);
     return;
-  }
-  if (field_major && nf >= 16) {
+  } else if (field_major && nf >= 16) {
     launch_tiled<T, true>(c, normalize, adjoint, x, xsf, y, ysf, nf, st);
     return;
   }
@@ -418,7 +426,7 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
     }
 #undef CRG_ROWS_CASE
   } else if (field_major) {
-    k_spmm_tile<T><<<nblk(n, kTileRows), kTileRows, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
+    k_spmm_tile<T><<<nblk(n, kFmRows), kFmRows, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
   } else {
     for (int64_t f0 = 0; f0 < nf; f0 += 65535) {
       dim3 grid(nblk(n, 256), (unsigned)std::min<int64_t>(65535, nf - f0));

@@ -1013,6 +1013,12 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     I.t_build_ms = t03; I.t_search_ms = t01; I.t_clip_ms = t12; I.t_assemble_ms = t23;
     I.clip_overflows = (int64_t)hovf;
     I.device = R->device;
+    const DevTiles* tl[2] = {&R->fwd.tiles, &R->rev.tiles};
+    for (int d = 0; d < 2; ++d) {
+      I.tiles[d] = tl[d]->ngood;
+      I.tile_columns[d] = tl[d]->nucol;
+      I.direct_rows[d] = tl[d]->ndirect;
+    }
     // temporaries are freed stream-ordered by the DBuf destructors
   } catch (...) {
     free_regridder(R);

@@ -87,6 +87,10 @@ typedef struct crg_info {
     int64_t clip_overflows;  /* pairs whose clip exceeded the vertex capacity */
     int32_t device;
     int32_t pad;
+    /* staged-tile layout of the batched apply, [0] = forward (rows = dst), [1] = transpose */
+    int64_t tiles[2];        /* row tiles whose source columns are staged in shared memory */
+    int64_t tile_columns[2]; /* distinct source columns summed over those tiles */
+    int64_t direct_rows[2];  /* rows applied by direct gathers (too many distinct columns) */
 } crg_info;
 
 /* Build the regridder from `src` to `dst`.
