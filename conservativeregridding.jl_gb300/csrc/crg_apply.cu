@@ -129,6 +129,118 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
   }
 }
 
+// Cell-major fields, G lanes per row (4 fields per lane, G*4 fields per pass).
+// The row's (column, weight) entries are loaded once, G at a time, by the
+// row's lanes with one coalesced load and broadcast by shuffles, so all
+// gathers of a row are in flight together (up to 4 per lane before the FMAs).
+template <class T, int G>
+__global__ void __launch_bounds__(256, 4) k_cm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                 const float* __restrict__ w, int64_t nrows,
+                                                 const int32_t* __restrict__ order, const T* __restrict__ x,
+                                                 int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane % G;
+  const int gbase = lane - g;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+  const int64_t ri = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  if (ri >= nrows) return;
+  const int32_t r = order ? order[ri] : (int32_t)ri;
+  const int32_t k0 = __ldg(ptr + r), k1 = __ldg(ptr + r + 1);
+  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int32_t kb = k0; kb < k1; kb += G) {
+      const int n = min(G, k1 - kb);
+      const int32_t myj = g < n ? __ldg(idx + kb + g) : 0;
+      const float myw = g < n ? __ldg(w + kb + g) : 0.f;
+      int e = 0;
+      for (; e + 4 <= n; e += 4) {
+        const int32_t j0 = __shfl_sync(gmask, myj, gbase + e), j1 = __shfl_sync(gmask, myj, gbase + e + 1);
+        const int32_t j2 = __shfl_sync(gmask, myj, gbase + e + 2), j3 = __shfl_sync(gmask, myj, gbase + e + 3);
+        const float w0 = __shfl_sync(gmask, myw, gbase + e), w1 = __shfl_sync(gmask, myw, gbase + e + 1);
+        const float w2 = __shfl_sync(gmask, myw, gbase + e + 2), w3 = __shfl_sync(gmask, myw, gbase + e + 3);
+        const float4 v0 = ld4<T>(x + (int64_t)j0 * xs + f), v1 = ld4<T>(x + (int64_t)j1 * xs + f);
+        const float4 v2 = ld4<T>(x + (int64_t)j2 * xs + f), v3 = ld4<T>(x + (int64_t)j3 * xs + f);
+        acc.x = fmaf(w0, v0.x, acc.x); acc.y = fmaf(w0, v0.y, acc.y); acc.z = fmaf(w0, v0.z, acc.z); acc.w = fmaf(w0, v0.w, acc.w);
+        acc.x = fmaf(w1, v1.x, acc.x); acc.y = fmaf(w1, v1.y, acc.y); acc.z = fmaf(w1, v1.z, acc.z); acc.w = fmaf(w1, v1.w, acc.w);
+        acc.x = fmaf(w2, v2.x, acc.x); acc.y = fmaf(w2, v2.y, acc.y); acc.z = fmaf(w2, v2.z, acc.z); acc.w = fmaf(w2, v2.w, acc.w);
+        acc.x = fmaf(w3, v3.x, acc.x); acc.y = fmaf(w3, v3.y, acc.y); acc.z = fmaf(w3, v3.z, acc.z); acc.w = fmaf(w3, v3.w, acc.w);
+      }
+      for (; e < n; ++e) {
+        const int32_t j = __shfl_sync(gmask, myj, gbase + e);
+        const float ww = __shfl_sync(gmask, myw, gbase + e);
+        const float4 v = ld4<T>(x + (int64_t)j * xs + f);
+        acc.x = fmaf(ww, v.x, acc.x); acc.y = fmaf(ww, v.y, acc.y); acc.z = fmaf(ww, v.z, acc.z); acc.w = fmaf(ww, v.w, acc.w);
+      }
+    }
+    st4<T>(y + (int64_t)r * ys + f, acc);
+  }
+}
+
+// Field-major fields: one lane per row, so a warp reads and writes 32
+// consecutive cells of each field.  The row's entries stay in registers (up to
+// kFmE at a time) while the lane sweeps the fields 4 at a time, keeping
+// 4 * entries gathers in flight.
+constexpr int kFmE = 8;
+
+template <class T>
+__global__ void __launch_bounds__(256) k_fm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                 const float* __restrict__ w, int64_t nrows, const T* __restrict__ x,
+                                                 int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int32_t k0 = __ldg(ptr + r), k1 = __ldg(ptr + r + 1);
+  if (k1 - k0 <= kFmE) {
+    // common case: all entries in registers for the whole field sweep
+    const int n = k1 - k0;
+    int32_t jj[kFmE];
+    float ww[kFmE];
+#pragma unroll
+    for (int e = 0; e < kFmE; ++e) {
+      jj[e] = e < n ? __ldg(idx + k0 + e) : 0;
+      ww[e] = e < n ? __ldg(w + k0 + e) : 0.f;
+    }
+    int64_t f = 0;
+    for (; f + 4 <= nf; f += 4) {
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+      for (int e = 0; e < kFmE; ++e) {
+        if (e < n) {
+          const T* xp = x + f * xs + jj[e];
+          a0 = fmaf(ww[e], ld1<T>(xp), a0);
+          a1 = fmaf(ww[e], ld1<T>(xp + xs), a1);
+          a2 = fmaf(ww[e], ld1<T>(xp + 2 * xs), a2);
+          a3 = fmaf(ww[e], ld1<T>(xp + 3 * xs), a3);
+        }
+      }
+      T* yp = y + f * ys + r;
+      st1<T>(yp, a0); st1<T>(yp + ys, a1); st1<T>(yp + 2 * ys, a2); st1<T>(yp + 3 * ys, a3);
+    }
+    for (; f < nf; ++f) {
+      float a = 0.f;
+#pragma unroll
+      for (int e = 0; e < kFmE; ++e)
+        if (e < n) a = fmaf(ww[e], ld1<T>(x + f * xs + jj[e]), a);
+      st1<T>(y + f * ys + r, a);
+    }
+    return;
+  }
+  // long rows: entries re-read (from cache) for every group of 4 fields
+  for (int64_t f = 0; f < nf; f += 4) {
+    const int nq = (int)(nf - f < 4 ? nf - f : 4);
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int32_t k = k0; k < k1; ++k) {
+      const int32_t j = __ldg(idx + k);
+      const float wk = __ldg(w + k);
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q < nq) a[q] = fmaf(wk, ld1<T>(x + (f + q) * xs + j), a[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (q < nq) st1<T>(y + (f + q) * ys + r, a[q]);
+  }
+}
+
 // ------------------------------------------------------------------ field-major fields
 
 constexpr int kFmRows = 128;
@@ -378,6 +490,39 @@ void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int
   else launch_tiled_kc<T, kFM, 32>(c, normalize, adjoint, x, xs, y, ys, nf, st);
 }
 
+// Kernel choice for FP32/BF16 fields.  CRG_SPMM_PATH selects an alternative
+// for tuning and profiling: "tiled" (shared-memory staged tiles) or "legacy"
+// (first-generation row kernels); unset = the register-blocked row kernels.
+enum class SpmmPath { kRows, kTiled, kLegacy };
+
+inline SpmmPath spmm_path() {
+  static const SpmmPath p = [] {
+    const char* e = getenv("CRG_SPMM_PATH");
+    if (e && strcmp(e, "tiled") == 0) return SpmmPath::kTiled;
+    if (e && strcmp(e, "legacy") == 0) return SpmmPath::kLegacy;
+    return SpmmPath::kRows;
+  }();
+  return p;
+}
+
+template <class T>
+void launch_cm_rows(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                    cudaStream_t st) {
+  const int64_t n = c.nrows;
+  const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
+  int G = 1;
+  while (G < lanes) G <<= 1;
+  const unsigned blocks = nblk(n * G, 256);
+  switch (G) {
+    case 1: k_cm_rows<T, 1><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+    case 2: k_cm_rows<T, 2><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+    case 4: k_cm_rows<T, 4><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+    case 8: k_cm_rows<T, 8><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+    case 16: k_cm_rows<T, 16><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+    default: k_cm_rows<T, 32><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+  }
+}
+
 template <class T>
 void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xsc, int64_t xsf, T* y,
                 int64_t ysc, int64_t ysf, int64_t nf, cudaStream_t st) {
@@ -385,24 +530,35 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
   if (n == 0 || nf == 0) return;
   const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
   const bool cell_major = (xsf == 1 && ysf == 1) && nf > 1;
-  const bool field_major = (xsc == 1 && ysc == 1) && nf > 1;
+  const bool field_major = (xsc == 1 && ysc == 1);
   const int es = (int)sizeof(T);
   const int vecf = 16 / es;  // fields per 16 bytes
-  // CRG_SPMM_PATH=rows forces the direct row-gather kernels (a tuning and
-  // profiling switch; the default picks staged tiles for >= 16 fields).
-  static const bool force_rows = [] {
-    const char* e = getenv("CRG_SPMM_PATH");
-    return e && strcmp(e, "rows") == 0;
-  }();
-  if (force_rows) {
-    // fall through to the direct kernels below
-  } else if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 &&
-      (uintptr_t)x % 16 == 0 && (uintptr_t)y % (4 * es) == 0) {
-    launch_tiled<T, false>(c, normalize, adjoint, x, xsc, y, ysc, nf, st);
-    return;
-  } else if (field_major && nf >= 16) {
-    launch_tiled<T, true>(c, normalize, adjoint, x, xsf, y, ysf, nf, st);
-    return;
+  // 4-field vectors: 16-byte (FP32) / 8-byte (BF16) aligned loads and stores
+  const bool vec4 = nf % 4 == 0 && xsc % 4 == 0 && ysc % 4 == 0 && (uintptr_t)x % (4 * es) == 0 &&
+                    (uintptr_t)y % (4 * es) == 0;
+  const SpmmPath path = spmm_path();
+  if (path == SpmmPath::kTiled) {
+    if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 && (uintptr_t)x % 16 == 0 &&
+        (uintptr_t)y % (4 * es) == 0) {
+      launch_tiled<T, false>(c, normalize, adjoint, x, xsc, y, ysc, nf, st);
+      return;
+    }
+    if (field_major && nf >= 16) {
+      launch_tiled<T, true>(c, normalize, adjoint, x, xsf, y, ysf, nf, st);
+      return;
+    }
+  }
+  if (path == SpmmPath::kRows) {
+    if (cell_major && vec4) {
+      launch_cm_rows<T>(c, w, x, xsc, y, ysc, nf, st);
+      CRG_CHECK_CUDA(cudaGetLastError());
+      return;
+    }
+    if (field_major) {
+      k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
+      CRG_CHECK_CUDA(cudaGetLastError());
+      return;
+    }
   }
   if (cell_major) {
     const bool vec = (xsc % 4 == 0) && (ysc % 4 == 0) && (nf % 4 == 0) &&
@@ -425,7 +581,7 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       CRG_ROWS_CASE(32)
     }
 #undef CRG_ROWS_CASE
-  } else if (field_major) {
+  } else if (field_major && nf > 1) {
     k_spmm_tile<T><<<nblk(n, kFmRows), kFmRows, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
   } else {
     for (int64_t f0 = 0; f0 < nf; f0 += 65535) {
