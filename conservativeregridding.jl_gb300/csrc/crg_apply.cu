@@ -146,7 +146,12 @@ __global__ void __launch_bounds__(256, 4) k_cm_rows(const int32_t* __restrict__ 
   if (ri >= nrows) return;
   const int32_t r = order ? order[ri] : (int32_t)ri;
   const int32_t k0 = __ldg(ptr + r), k1 = __ldg(ptr + r + 1);
-  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+  // every lane of the group runs every pass (the shuffles need the whole
+  // group); lanes past the last field only skip their loads and stores
+  for (int64_t f0 = 0; f0 < nf; f0 += (int64_t)G * 4) {
+    const int64_t fl = f0 + (int64_t)g * 4;
+    const bool on = fl < nf;
+    const int64_t f = on ? fl : 0;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int32_t kb = k0; kb < k1; kb += G) {
       const int n = min(G, k1 - kb);
@@ -172,7 +177,7 @@ __global__ void __launch_bounds__(256, 4) k_cm_rows(const int32_t* __restrict__ 
         acc.x = fmaf(ww, v.x, acc.x); acc.y = fmaf(ww, v.y, acc.y); acc.z = fmaf(ww, v.z, acc.z); acc.w = fmaf(ww, v.w, acc.w);
       }
     }
-    st4<T>(y + (int64_t)r * ys + f, acc);
+    if (on) st4<T>(y + (int64_t)r * ys + f, acc);
   }
 }
 
