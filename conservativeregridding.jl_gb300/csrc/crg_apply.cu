@@ -129,55 +129,84 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
   }
 }
 
-// Cell-major fields, G lanes per row (4 fields per lane, G*4 fields per pass).
-// The row's (column, weight) entries are loaded once, G at a time, by the
-// row's lanes with one coalesced load and broadcast by shuffles, so all
-// gathers of a row are in flight together (up to 4 per lane before the FMAs).
-template <class T, int G>
+// Cell-major fields, G lanes per row group (4 fields per lane, G*4 fields per
+// pass), RB consecutive rows per group processed together.  The rows'
+// (column, weight) entries are loaded G at a time by the group's lanes with
+// one coalesced load per row and broadcast by shuffles, so the gathers of all
+// RB rows are in flight together before the FMAs.
+template <class T, int G, int RB>
 __global__ void __launch_bounds__(256, 4) k_cm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                                                 const float* __restrict__ w, int64_t nrows,
-                                                 const int32_t* __restrict__ order, const T* __restrict__ x,
-                                                 int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
+                                                    const float* __restrict__ w, int64_t nrows,
+                                                    const int32_t* __restrict__ order, const T* __restrict__ x,
+                                                    int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
   const int lane = threadIdx.x & 31;
   const int g = lane % G;
   const int gbase = lane - g;
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
-  const int64_t ri = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-  if (ri >= nrows) return;
-  const int32_t r = order ? order[ri] : (int32_t)ri;
-  const int32_t k0 = __ldg(ptr + r), k1 = __ldg(ptr + r + 1);
+  const int64_t grp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t r0 = grp * RB;
+  if (r0 >= nrows) return;
+  int32_t rr[RB], k0[RB], nn[RB];
+#pragma unroll
+  for (int q = 0; q < RB; ++q) {
+    const int64_t ri = r0 + q;
+    rr[q] = ri < nrows ? (order ? order[ri] : (int32_t)ri) : -1;
+    k0[q] = rr[q] >= 0 ? __ldg(ptr + rr[q]) : 0;
+    nn[q] = rr[q] >= 0 ? __ldg(ptr + rr[q] + 1) - k0[q] : 0;
+  }
+  int nmax = 0;
+#pragma unroll
+  for (int q = 0; q < RB; ++q) nmax = max(nmax, nn[q]);
   // every lane of the group runs every pass (the shuffles need the whole
-  // group); lanes past the last field only skip their loads and stores
+  // group); lanes past the last field only skip their stores
   for (int64_t f0 = 0; f0 < nf; f0 += (int64_t)G * 4) {
     const int64_t fl = f0 + (int64_t)g * 4;
     const bool on = fl < nf;
     const int64_t f = on ? fl : 0;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int32_t kb = k0; kb < k1; kb += G) {
-      const int n = min(G, k1 - kb);
-      const int32_t myj = g < n ? __ldg(idx + kb + g) : 0;
-      const float myw = g < n ? __ldg(w + kb + g) : 0.f;
-      int e = 0;
-      for (; e + 4 <= n; e += 4) {
-        const int32_t j0 = __shfl_sync(gmask, myj, gbase + e), j1 = __shfl_sync(gmask, myj, gbase + e + 1);
-        const int32_t j2 = __shfl_sync(gmask, myj, gbase + e + 2), j3 = __shfl_sync(gmask, myj, gbase + e + 3);
-        const float w0 = __shfl_sync(gmask, myw, gbase + e), w1 = __shfl_sync(gmask, myw, gbase + e + 1);
-        const float w2 = __shfl_sync(gmask, myw, gbase + e + 2), w3 = __shfl_sync(gmask, myw, gbase + e + 3);
-        const float4 v0 = ld4<T>(x + (int64_t)j0 * xs + f), v1 = ld4<T>(x + (int64_t)j1 * xs + f);
-        const float4 v2 = ld4<T>(x + (int64_t)j2 * xs + f), v3 = ld4<T>(x + (int64_t)j3 * xs + f);
-        acc.x = fmaf(w0, v0.x, acc.x); acc.y = fmaf(w0, v0.y, acc.y); acc.z = fmaf(w0, v0.z, acc.z); acc.w = fmaf(w0, v0.w, acc.w);
-        acc.x = fmaf(w1, v1.x, acc.x); acc.y = fmaf(w1, v1.y, acc.y); acc.z = fmaf(w1, v1.z, acc.z); acc.w = fmaf(w1, v1.w, acc.w);
-        acc.x = fmaf(w2, v2.x, acc.x); acc.y = fmaf(w2, v2.y, acc.y); acc.z = fmaf(w2, v2.z, acc.z); acc.w = fmaf(w2, v2.w, acc.w);
-        acc.x = fmaf(w3, v3.x, acc.x); acc.y = fmaf(w3, v3.y, acc.y); acc.z = fmaf(w3, v3.z, acc.z); acc.w = fmaf(w3, v3.w, acc.w);
+    float4 acc[RB];
+#pragma unroll
+    for (int q = 0; q < RB; ++q) acc[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int kb = 0; kb < nmax; kb += G) {
+      int32_t myj[RB];
+      float myw[RB];
+#pragma unroll
+      for (int q = 0; q < RB; ++q) {
+        const bool in = kb + g < nn[q];
+        myj[q] = in ? __ldg(idx + k0[q] + kb + g) : 0;
+        myw[q] = in ? __ldg(w + k0[q] + kb + g) : 0.f;
       }
-      for (; e < n; ++e) {
-        const int32_t j = __shfl_sync(gmask, myj, gbase + e);
-        const float ww = __shfl_sync(gmask, myw, gbase + e);
-        const float4 v = ld4<T>(x + (int64_t)j * xs + f);
-        acc.x = fmaf(ww, v.x, acc.x); acc.y = fmaf(ww, v.y, acc.y); acc.z = fmaf(ww, v.z, acc.z); acc.w = fmaf(ww, v.w, acc.w);
+      const int ne = min(G, nmax - kb);
+      for (int e = 0; e < ne; e += 2) {
+        float4 v[RB][2];
+        float ww[RB][2];
+#pragma unroll
+        for (int q = 0; q < RB; ++q) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int src = gbase + min(e + h, G - 1);
+            const int32_t j = __shfl_sync(gmask, myj[q], src);
+            ww[q][h] = __shfl_sync(gmask, myw[q], src);
+            const bool live = (kb + e + h) < nn[q];
+            ww[q][h] = live ? ww[q][h] : 0.f;
+            v[q][h] = live ? ld4<T>(x + (int64_t)j * xs + f) : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < RB; ++q)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            acc[q].x = fmaf(ww[q][h], v[q][h].x, acc[q].x);
+            acc[q].y = fmaf(ww[q][h], v[q][h].y, acc[q].y);
+            acc[q].z = fmaf(ww[q][h], v[q][h].z, acc[q].z);
+            acc[q].w = fmaf(ww[q][h], v[q][h].w, acc[q].w);
+          }
       }
     }
-    if (on) st4<T>(y + (int64_t)r * ys + f, acc);
+    if (on) {
+#pragma unroll
+      for (int q = 0; q < RB; ++q)
+        if (rr[q] >= 0) st4<T>(y + (int64_t)rr[q] * ys + f, acc[q]);
+    }
   }
 }
 
@@ -188,11 +217,13 @@ __global__ void __launch_bounds__(256, 4) k_cm_rows(const int32_t* __restrict__ 
 constexpr int kFmE = 8;
 
 template <class T>
-__global__ void __launch_bounds__(256) k_fm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                                                 const float* __restrict__ w, int64_t nrows, const T* __restrict__ x,
-                                                 int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
+__global__ void __launch_bounds__(256, 4) k_fm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                    const float* __restrict__ w, int64_t nrows,
+                                                    const int32_t* __restrict__ order, const T* __restrict__ x,
+                                                    int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
+  const int64_t ri = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (ri >= nrows) return;
+  const int64_t r = order ? order[ri] : ri;
   const int32_t k0 = __ldg(ptr + r), k1 = __ldg(ptr + r + 1);
   if (k1 - k0 <= kFmE) {
     // common case: all entries in registers for the whole field sweep
@@ -517,15 +548,25 @@ void launch_cm_rows(const DevCsr& c, const float* w, const T* x, int64_t xs, T* 
   const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
   int G = 1;
   while (G < lanes) G <<= 1;
-  const unsigned blocks = nblk(n * G, 256);
+  static const int RB = [] {
+    const char* e = getenv("CRG_SPMM_RB");
+    int v = e ? atoi(e) : 2;
+    return (v == 1 || v == 2 || v == 4) ? v : 2;
+  }();
+  const unsigned blocks = nblk((n + RB - 1) / RB * G, 256);
+#define CRG_CM(GG, RR) k_cm_rows<T, GG, RR><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf)
+#define CRG_CM_RB(GG) \
+  if (RB == 1) CRG_CM(GG, 1); else if (RB == 2) CRG_CM(GG, 2); else CRG_CM(GG, 4);
   switch (G) {
-    case 1: k_cm_rows<T, 1><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
-    case 2: k_cm_rows<T, 2><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
-    case 4: k_cm_rows<T, 4><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
-    case 8: k_cm_rows<T, 8><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
-    case 16: k_cm_rows<T, 16><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
-    default: k_cm_rows<T, 32><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf); break;
+    case 1: CRG_CM_RB(1) break;
+    case 2: CRG_CM_RB(2) break;
+    case 4: CRG_CM_RB(4) break;
+    case 8: CRG_CM_RB(8) break;
+    case 16: CRG_CM_RB(16) break;
+    default: CRG_CM_RB(32) break;
   }
+#undef CRG_CM_RB
+#undef CRG_CM
 }
 
 template <class T>
@@ -560,7 +601,12 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       return;
     }
     if (field_major) {
-      k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
+      static const bool by_col = [] {
+        const char* e = getenv("CRG_FM_ORDER");
+        return !(e && strcmp(e, "natural") == 0);
+      }();
+      k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, by_col ? c.order_by_col : nullptr, x, xsf, y,
+                                                ysf, nf);
       CRG_CHECK_CUDA(cudaGetLastError());
       return;
     }

@@ -65,6 +65,7 @@ struct DevCsr {
   float* wn32 = nullptr;     // [nnz] A_rc / area_row (FP32): normalised weights of this direction
   float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
   DevTiles tiles;            // staged-tile layout for the batched FP32/BF16 apply
+  int32_t* order_by_col = nullptr;  // [nrows] rows ordered by their first column (field-major sweep order)
 };
 
 // Per-cell vertex table on the device: [n][maxv] unit vectors (z = 0 planar).

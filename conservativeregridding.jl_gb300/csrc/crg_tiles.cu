@@ -170,6 +170,25 @@ __global__ void __launch_bounds__(kThreads) k_tile_fill(const int32_t* __restric
   }
 }
 
+// Rows keyed by their first (smallest) column; empty rows get key ncols.
+__global__ void k_firstcol_hist(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
+                                int64_t ncols, int32_t* __restrict__ cnt) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t k = ptr[r];
+  atomicAdd(&cnt[k < ptr[r + 1] ? idx[k] : ncols], 1);
+}
+
+__global__ void k_firstcol_scatter(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
+                                   int64_t ncols, const int32_t* __restrict__ off, int32_t* __restrict__ fill,
+                                   int32_t* __restrict__ order) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t k = ptr[r];
+  const int64_t key = k < ptr[r + 1] ? idx[k] : ncols;
+  order[off[key] + atomicAdd(&fill[key], 1)] = (int32_t)r;
+}
+
 __global__ void k_len_perm(const int32_t* __restrict__ ptr, const int32_t* __restrict__ rows, int64_t n,
                            int32_t* __restrict__ len) {
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -204,6 +223,23 @@ void free_tiles(DevTiles& t) {
 void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st) {
   DevTiles& T = c.tiles;
   const int64_t n = c.nrows, nnz = c.nnz;
+  // rows by first column: counting sort over ncols + 1 keys
+  c.order_by_col = palloc<int32_t>((size_t)n);
+  if (n > 0) {
+    const int64_t nk = c.ncols + 1;
+    int32_t *cnt = nullptr, *fill = nullptr;
+    CRG_CHECK_CUDA(cudaMallocAsync((void**)&cnt, sizeof(int32_t) * (nk + 1), st));
+    CRG_CHECK_CUDA(cudaMallocAsync((void**)&fill, sizeof(int32_t) * nk, st));
+    CRG_CHECK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nk + 1), st));
+    CRG_CHECK_CUDA(cudaMemsetAsync(fill, 0, sizeof(int32_t) * nk, st));
+    k_firstcol_hist<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, n, c.ncols, cnt);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    exclusive_scan_i32(cnt, cnt, nk, st);
+    k_firstcol_scatter<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, n, c.ncols, cnt, fill, c.order_by_col);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    CRG_CHECK_CUDA(cudaFreeAsync(cnt, st));
+    CRG_CHECK_CUDA(cudaFreeAsync(fill, st));
+  }
   T.rows = palloc<int32_t>((size_t)n);
   T.lptr = palloc<int32_t>((size_t)n + 1);
   T.lcol = palloc<uint16_t>((size_t)nnz);
