@@ -345,10 +345,15 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
   unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 template <class T> __device__ __forceinline__ float4 lds4(const T* p);
@@ -359,90 +364,190 @@ template <> __device__ __forceinline__ float4 lds4<__nv_bfloat16>(const __nv_bfl
   float2 b = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&u.y));
   return make_float4(a.x, a.y, b.x, b.y);
 }
+template <class T> __device__ __forceinline__ float lds1(const T* p);
+template <> __device__ __forceinline__ float lds1<float>(const float* p) { return *p; }
+template <> __device__ __forceinline__ float lds1<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
 
-template <class T, int KC>
-__host__ __device__ constexpr int stage_stride() { return KC + 16 / (int)sizeof(T); }
+__host__ __device__ constexpr size_t align16(size_t b) { return (b + 15) / 16 * 16; }
 
-template <class T, bool kFM, int KC>
-constexpr size_t tiled_smem() {
-  return (size_t)kTileUMax * stage_stride<T, KC>() * sizeof(T) + (kFM ? (size_t)kTileRows * (KC + 1) * sizeof(float) : 0);
-}
+// Shared-memory layout of the pipelined tile kernel.  Two data buffers
+// (fields of one work item + its row/entry metadata) and three small list
+// buffers (the distinct columns or chunks of an item, needed one step ahead
+// of its field copies).
+template <class T, bool kFM>
+struct Pipe {
+  static constexpr int KC = kFM ? 16 : 64;  // fields per work item
+  static constexpr int PADT = 16 / (int)sizeof(T);
+  // field-major: [KC][4*kTileUMax + pad] (a row per field, 4 cells per chunk);
+  // cell-major: [kTileUMax][KC + pad] (a row per distinct column)
+  static constexpr int SP = kFM ? (4 * kTileUMax + PADT) : (KC + PADT);
+  static constexpr int SROWS = kFM ? KC : kTileUMax;
+  static constexpr size_t kStage = align16((size_t)SROWS * SP * sizeof(T));
+  static constexpr size_t kRows = align16(sizeof(int32_t) * kTileRows);
+  static constexpr size_t kLptr = align16(sizeof(int32_t) * (kTileRows + 1));
+  static constexpr size_t kLw = align16(sizeof(float) * kTileEMax);
+  static constexpr size_t kLidx = align16(sizeof(uint16_t) * (kTileEMax + 2));
+  static constexpr size_t kData = kStage + kRows + kLptr + kLw + kLidx;
+  static constexpr size_t kList = align16(sizeof(int32_t) * kTileUMax);
+  static constexpr size_t kSmem = 2 * kData + 3 * kList;
+};
 
-// One CTA per staged tile.  For each chunk of KC fields: copy the tile's
-// distinct source columns into shared memory (cp.async; 16-byte pieces of a
-// cell's contiguous fields when cell-major, 4-byte gathers when field-major),
-// then G = KC/4 lanes per row accumulate 4 fields each from shared memory in
-// FP32 and write the row (cell-major) or stage it and write field by field
-// (field-major, so the stores are runs of consecutive cells).
-template <class T, bool kFM, int KC>
-__global__ void __launch_bounds__(256, 2) k_spmm_tiled(const int2* __restrict__ tiles, const int32_t* __restrict__ uoff,
-                                                       const int32_t* __restrict__ ucol,
-                                                       const int32_t* __restrict__ rows,
-                                                       const int32_t* __restrict__ lptr,
-                                                       const uint16_t* __restrict__ lcol,
-                                                       const float* __restrict__ lw, const T* __restrict__ x,
-                                                       int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf) {
-  constexpr int SP = stage_stride<T, KC>();
-  constexpr int G = KC / 4;
-  constexpr int RPW = 32 / G;
-  constexpr int OS = KC + 1;
+struct TileArgs {
+  const int32_t* desc;
+  const int32_t* rows;
+  const int32_t* lptr;
+  const uint16_t* lidx;  // lcol (cell-major) or lchk (field-major)
+  const float* lw;
+  const int32_t* list;   // ucol (cell-major) or uchunk (field-major)
+  int64_t nitems, nkc, ngood;
+};
+
+// Persistent CTAs walk a contiguous range of work items (tile, field chunk),
+// field chunk fastest.  cp.async groups are double buffered: while item i is
+// computed from shared memory, the copies of item i+1's fields and metadata
+// and of item i+2's column / chunk list are in flight.
+template <class T, bool kFM>
+__global__ void __launch_bounds__(256, 2) k_tiled(TileArgs ta, const T* __restrict__ x, int64_t xs, T* __restrict__ y,
+                                                  int64_t ys, int64_t nf) {
+  using P = Pipe<T, kFM>;
+  constexpr int KC = P::KC, SP = P::SP;
   extern __shared__ __align__(16) unsigned char smem[];
-  T* stage = reinterpret_cast<T*>(smem);
-  float* outs = reinterpret_cast<float*>(smem + (size_t)kTileUMax * SP * sizeof(T));
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = lane % G, sub = lane / G;
-  const int2 tr = tiles[blockIdx.x];
-  const int p0 = tr.x, nr = tr.y - tr.x;
-  const int u0 = uoff[blockIdx.x], u = uoff[blockIdx.x + 1] - u0;
-  for (int64_t f0 = 0; f0 < nf; f0 += KC) {
+  const int tid = threadIdx.x;
+  const int64_t per = (ta.nitems + gridDim.x - 1) / gridDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * per;
+  const int64_t i1 = min(ta.nitems, i0 + per);
+  if (i0 >= i1) return;
+
+  auto data = [&](int b) { return smem + (size_t)b * P::kData; };
+  auto stage = [&](int b) { return reinterpret_cast<T*>(data(b)); };
+  auto srows = [&](int b) { return reinterpret_cast<int32_t*>(data(b) + P::kStage); };
+  auto slptr = [&](int b) { return reinterpret_cast<int32_t*>(data(b) + P::kStage + P::kRows); };
+  auto slw = [&](int b) { return reinterpret_cast<float*>(data(b) + P::kStage + P::kRows + P::kLptr); };
+  auto slidx = [&](int b) {
+    return reinterpret_cast<uint16_t*>(data(b) + P::kStage + P::kRows + P::kLptr + P::kLw);
+  };
+  auto slist = [&](int b) { return reinterpret_cast<int32_t*>(smem + 2 * P::kData + (size_t)b * P::kList); };
+
+  // copy the column / chunk list of item `it` into list buffer lb
+  auto issue_list = [&](int64_t it, int lb) {
+    const int32_t* d = ta.desc + (it / ta.nkc) * kDescInts;
+    const int l0 = kFM ? __ldg(d + kDescC0) : __ldg(d + kDescU0);
+    const int nl = kFM ? __ldg(d + kDescNc) : __ldg(d + kDescNu);
+    int32_t* dst = slist(lb);
+    for (int i = tid; i < nl; i += 256) cp_async4(dst + i, ta.list + l0 + i);
+  };
+  // copy the fields and metadata of item `it` into data buffer db, using list buffer lb
+  auto issue_data = [&](int64_t it, int db, int lb) {
+    const int64_t t = it / ta.nkc;
+    const int64_t f0 = (it % ta.nkc) * KC;
     const int kc = (int)(nf - f0 < KC ? nf - f0 : KC);
+    const int32_t* d = ta.desc + t * kDescInts;
+    const int p0 = __ldg(d + kDescP0), nr = __ldg(d + kDescNr);
+    const int e0 = __ldg(d + kDescE0), ne = __ldg(d + kDescNe);
+    const int nl = kFM ? __ldg(d + kDescNc) : __ldg(d + kDescNu);
+    const int32_t* lst = slist(lb);
+    T* sg = stage(db);
     if (!kFM) {
-      const int cpc = kc * (int)sizeof(T) / 16;
-      for (int i = tid; i < u * cpc; i += 256) {
-        const int c = i / cpc, q = i - c * cpc;
-        cp_async16(stage + c * SP + q * (16 / (int)sizeof(T)), x + (int64_t)__ldg(ucol + u0 + c) * xs + f0 + q * (16 / (int)sizeof(T)));
+      // one distinct column = the kc contiguous fields of a cell, in 16-byte pieces
+      const int qpc = kc * (int)sizeof(T) / 16;
+      for (int i = tid; i < nl * qpc; i += 256) {
+        const int c = i / qpc, q = i - c * qpc;
+        cp_async16(sg + c * SP + q * P::PADT, x + (int64_t)lst[c] * xs + f0 + q * P::PADT);
       }
     } else {
-      for (int i = tid; i < u * kc; i += 256) {
-        const int f = i / u, c = i - f * u;
-        const T* src = x + (f0 + f) * xs + __ldg(ucol + u0 + c);
-        if (sizeof(T) == 4) cp_async4(stage + c * SP + f, src);
-        else stage[c * SP + f] = *src;
+      // one chunk = 4 consecutive cells of one field (16 B FP32, 8 B BF16)
+      for (int i = tid; i < kc * nl; i += 256) {
+        const int f = i / nl, c = i - f * nl;
+        const T* src = x + (f0 + f) * xs + (int64_t)lst[c] * 4;
+        if (sizeof(T) == 4) cp_async16(sg + f * SP + c * 4, src);
+        else cp_async8(sg + f * SP + c * 4, src);
       }
     }
+    int32_t* rw = srows(db);
+    int32_t* lp = slptr(db);
+    for (int i = tid; i < nr; i += 256) cp_async4(rw + i, ta.rows + p0 + i);
+    for (int i = tid; i <= nr; i += 256) cp_async4(lp + i, ta.lptr + p0 + i);
+    float* lw = slw(db);
+    for (int i = tid; i < ne; i += 256) cp_async4(lw + i, ta.lw + e0 + i);
+    // 16-bit indices as 32-bit words: word w0 = e0 / 2 covers entries from 2*w0
+    uint32_t* li = reinterpret_cast<uint32_t*>(slidx(db));
+    const int w0 = e0 >> 1, nw = ((e0 + ne + 1) >> 1) - w0;
+    const uint32_t* gw = reinterpret_cast<const uint32_t*>(ta.lidx);
+    for (int i = tid; i < nw; i += 256) cp_async4(li + i, gw + w0 + i);
+  };
+  auto compute = [&](int64_t it, int db) {
+    const int64_t t = it / ta.nkc;
+    const int64_t f0 = (it % ta.nkc) * KC;
+    const int kc = (int)(nf - f0 < KC ? nf - f0 : KC);
+    const int32_t* d = ta.desc + t * kDescInts;
+    const int nr = __ldg(d + kDescNr), e0 = __ldg(d + kDescE0);
+    const T* sg = stage(db);
+    const int32_t* rw = srows(db);
+    const int32_t* lp = slptr(db);
+    const float* lw = slw(db);
+    const uint16_t* li = slidx(db) + (e0 & 1);
+    const int eb = lp[0];
+    if (!kFM) {
+      constexpr int G = KC / 4;   // 16 lanes per row, 4 fields each
+      const int lane = tid & 31, warp = tid >> 5, g = lane % G;
+      for (int rb = warp * (32 / G) + lane / G; rb < nr; rb += 8 * (32 / G)) {
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int k1 = lp[rb + 1] - eb;
+        for (int k = lp[rb] - eb; k < k1; ++k) {
+          const float wk = lw[k];
+          const float4 v = lds4<T>(sg + li[k] * SP + g * 4);
+          acc.x = fmaf(wk, v.x, acc.x); acc.y = fmaf(wk, v.y, acc.y);
+          acc.z = fmaf(wk, v.z, acc.z); acc.w = fmaf(wk, v.w, acc.w);
+        }
+        if (g * 4 < kc) st4<T>(y + (int64_t)rw[rb] * ys + f0 + g * 4, acc);
+      }
+    } else {
+      // (row, group of 4 fields) pairs; consecutive threads = consecutive rows
+      const int ng = (kc + 3) >> 2;
+      for (int q = tid; q < nr * ng; q += 256) {
+        const int r = q % nr, fg = q / nr;
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+        const int k1 = lp[r + 1] - eb;
+        const T* s0 = sg + fg * 4 * SP;
+        for (int k = lp[r] - eb; k < k1; ++k) {
+          const float wk = lw[k];
+          const int lc = li[k];
+          a0 = fmaf(wk, lds1<T>(s0 + lc), a0);
+          a1 = fmaf(wk, lds1<T>(s0 + SP + lc), a1);
+          a2 = fmaf(wk, lds1<T>(s0 + 2 * SP + lc), a2);
+          a3 = fmaf(wk, lds1<T>(s0 + 3 * SP + lc), a3);
+        }
+        const int64_t fb = f0 + fg * 4;
+        T* yp = y + fb * ys + rw[r];
+        st1<T>(yp, a0);
+        if (fb + 1 < f0 + kc) st1<T>(yp + ys, a1);
+        if (fb + 2 < f0 + kc) st1<T>(yp + 2 * ys, a2);
+        if (fb + 3 < f0 + kc) st1<T>(yp + 3 * ys, a3);
+      }
+    }
+  };
+
+  // prologue: list(i0) -> L0; then data(i0) with L0 and list(i0+1) -> L1
+  issue_list(i0, 0);
+  cp_async_commit();
+  cp_async_wait_all();
+  __syncthreads();
+  issue_data(i0, 0, 0);
+  if (i0 + 1 < i1) issue_list(i0 + 1, 1);
+  cp_async_commit();
+  for (int64_t it = i0; it < i1; ++it) {
+    const int k = (int)(it - i0);
     cp_async_wait_all();
     __syncthreads();
-    for (int rb = warp * RPW + sub; rb < nr; rb += 8 * RPW) {
-      const int p = p0 + rb;
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (g * 4 < kc) {
-        const int k1 = lptr[p + 1];
-        for (int k = lptr[p]; k < k1; ++k) {
-          const int lc = lcol[k];
-          const float w = lw[k];
-          const float4 v = lds4<T>(stage + lc * SP + g * 4);
-          acc.x = fmaf(w, v.x, acc.x);
-          acc.y = fmaf(w, v.y, acc.y);
-          acc.z = fmaf(w, v.z, acc.z);
-          acc.w = fmaf(w, v.w, acc.w);
-        }
-        if (!kFM) {
-          st4<T>(y + (int64_t)rows[p] * ys + f0 + g * 4, acc);
-        } else {
-          float* o = outs + rb * OS + g * 4;
-          o[0] = acc.x; o[1] = acc.y; o[2] = acc.z; o[3] = acc.w;
-        }
-      }
+    if (it + 1 < i1) {
+      issue_data(it + 1, (k + 1) & 1, (k + 1) % 3);
+      if (it + 2 < i1) issue_list(it + 2, (k + 2) % 3);
     }
-    if (kFM) {
-      __syncthreads();
-      for (int i = tid; i < kc * nr; i += 256) {
-        const int f = i / nr, r = i - f * nr;
-        st1<T>(y + (f0 + f) * ys + rows[p0 + r], outs[r * OS + f]);
-      }
-    }
+    cp_async_commit();
+    compute(it, k & 1);
     __syncthreads();
   }
+  cp_async_wait_all();
 }
 
 // Rows left out of the tiles (too many distinct columns), cell-major fields:
@@ -493,21 +598,40 @@ __global__ void __launch_bounds__(256) k_direct_fm(const int32_t* __restrict__ p
   }
 }
 
-template <class T, bool kFM, int KC>
-void launch_tiled_kc(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xs, T* y, int64_t ys,
-                     int64_t nf, cudaStream_t st) {
+int num_sms() {
+  static int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+template <class T, bool kFM>
+void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                  cudaStream_t st) {
+  using P = Pipe<T, kFM>;
   const DevTiles& tl = c.tiles;
-  const float* lw = normalize ? (adjoint ? tl.lw_adj : tl.lw_wn) : tl.lw_val;
   const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
-  constexpr size_t smem = tiled_smem<T, kFM, KC>();
+  TileArgs ta;
+  ta.desc = tl.desc;
+  ta.rows = tl.rows;
+  ta.lptr = tl.lptr;
+  ta.lidx = kFM ? tl.lchk : tl.lcol;
+  ta.lw = normalize ? (adjoint ? tl.lw_adj : tl.lw_wn) : tl.lw_val;
+  ta.list = kFM ? tl.uchunk : tl.ucol;
+  ta.nkc = (nf + P::KC - 1) / P::KC;
+  ta.ngood = tl.ngood;
+  ta.nitems = tl.ngood * ta.nkc;
   static bool configured = false;  // per template instance
   if (!configured) {
-    CRG_CHECK_CUDA(cudaFuncSetAttribute(k_spmm_tiled<T, kFM, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CRG_CHECK_CUDA(cudaFuncSetAttribute(k_tiled<T, kFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::kSmem));
     configured = true;
   }
-  if (tl.ngood) {
-    k_spmm_tiled<T, kFM, KC><<<(unsigned)tl.ngood, 256, smem, st>>>(tl.tiles, tl.uoff, tl.ucol, tl.rows, tl.lptr, tl.lcol,
-                                                                     lw, x, xs, y, ys, nf);
+  if (ta.nitems) {
+    const int64_t grid = std::min<int64_t>(ta.nitems, (int64_t)num_sms() * 2);
+    k_tiled<T, kFM><<<(unsigned)grid, 256, P::kSmem, st>>>(ta, x, xs, y, ys, nf);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
   if (tl.ndirect) {
@@ -516,14 +640,6 @@ void launch_tiled_kc(const DevCsr& c, bool normalize, bool adjoint, const T* x, 
     else k_direct_cm<T><<<blocks, 256, 0, st>>>(tl.direct, tl.ndirect, tl.rows, c.ptr, c.idx, w, x, xs, y, ys, nf);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
-}
-
-template <class T, bool kFM>
-void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                  cudaStream_t st) {
-  if (nf >= 128) launch_tiled_kc<T, kFM, 128>(c, normalize, adjoint, x, xs, y, ys, nf, st);
-  else if (nf >= 64) launch_tiled_kc<T, kFM, 64>(c, normalize, adjoint, x, xs, y, ys, nf, st);
-  else launch_tiled_kc<T, kFM, 32>(c, normalize, adjoint, x, xs, y, ys, nf, st);
 }
 
 // Kernel choice for FP32/BF16 fields.  CRG_SPMM_PATH selects an alternative
@@ -584,12 +700,14 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
                     (uintptr_t)y % (4 * es) == 0;
   const SpmmPath path = spmm_path();
   if (path == SpmmPath::kTiled) {
+    // cell-major: 16-byte pieces of each cell's field vector
     if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 && (uintptr_t)x % 16 == 0 &&
         (uintptr_t)y % (4 * es) == 0) {
       launch_tiled<T, false>(c, normalize, adjoint, x, xsc, y, ysc, nf, st);
       return;
     }
-    if (field_major && nf >= 16) {
+    // field-major: aligned 4-cell chunks of each field (all chunks inside the field)
+    if (field_major && nf >= 4 && c.ncols % 4 == 0 && xsf % 4 == 0 && (uintptr_t)x % (4 * es) == 0) {
       launch_tiled<T, true>(c, normalize, adjoint, x, xsf, y, ysf, nf, st);
       return;
     }
@@ -601,12 +719,7 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       return;
     }
     if (field_major) {
-      static const bool by_col = [] {
-        const char* e = getenv("CRG_FM_ORDER");
-        return !(e && strcmp(e, "natural") == 0);
-      }();
-      k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, by_col ? c.order_by_col : nullptr, x, xsf, y,
-                                                ysf, nf);
+      k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xsf, y, ysf, nf);
       CRG_CHECK_CUDA(cudaGetLastError());
       return;
     }

@@ -852,7 +852,6 @@ bool is_device_pointer(const void* p) {
 
 void free_csr(DevCsr& c) {
   free_tiles(c.tiles);
-  cudaFree(c.order_by_col);
   cudaFree(c.ptr); cudaFree(c.idx); cudaFree(c.val); cudaFree(c.val32); cudaFree(c.wn32); cudaFree(c.adj32);
   c = DevCsr{};
 }

@@ -40,17 +40,23 @@ constexpr int kTileRows = 64;    // rows of a full tile
 constexpr int kTileUMax = 128;   // distinct source columns a tile may stage
 constexpr int kTileEMax = 2048;  // entries a tile may hold
 
+// Per-tile descriptor (8 x int32): rows [p0, p0+nr) of the processing order,
+// distinct columns ucol[u0, u0+nu), entries [e0, e0+ne) of the permuted
+// entry arrays, distinct 4-cell chunks uchunk[c0, c0+nc).
+enum { kDescP0 = 0, kDescNr, kDescU0, kDescNu, kDescE0, kDescNe, kDescC0, kDescNc, kDescInts };
+
 struct DevTiles {
-  int64_t ngood = 0, ndirect = 0, nucol = 0;
+  int64_t ngood = 0, ndirect = 0, nucol = 0, nuchunk = 0;
   int32_t* rows = nullptr;     // [nrows] processing order: position -> row
   int32_t* lptr = nullptr;     // [nrows+1] entry offsets in processing order
-  uint16_t* lcol = nullptr;    // [nnz] column index inside the tile's distinct set
+  uint16_t* lcol = nullptr;    // [nnz] column index inside the tile's distinct-column set
+  uint16_t* lchk = nullptr;    // [nnz] 4 * (chunk index inside the tile's chunk set) + (column & 3)
   float* lw_val = nullptr;     // [nnz] val32 in processing order
   float* lw_wn = nullptr;      // [nnz] wn32 in processing order
   float* lw_adj = nullptr;     // [nnz] adj32 in processing order
-  int2* tiles = nullptr;       // [ngood] position ranges [x, y) of staged tiles
-  int32_t* uoff = nullptr;     // [ngood+1] offsets into ucol
+  int32_t* desc = nullptr;     // [ngood][kDescInts] tile descriptors, in row order
   int32_t* ucol = nullptr;     // [nucol] distinct source columns per tile, ascending
+  int32_t* uchunk = nullptr;   // [nuchunk] distinct source chunks (column >> 2) per tile, ascending
   int32_t* direct = nullptr;   // [ndirect] positions of rows applied by direct gathers
 };
 
@@ -65,7 +71,6 @@ struct DevCsr {
   float* wn32 = nullptr;     // [nnz] A_rc / area_row (FP32): normalised weights of this direction
   float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
   DevTiles tiles;            // staged-tile layout for the batched FP32/BF16 apply
-  int32_t* order_by_col = nullptr;  // [nrows] rows ordered by their first column (field-major sweep order)
 };
 
 // Per-cell vertex table on the device: [n][maxv] unit vectors (z = 0 planar).

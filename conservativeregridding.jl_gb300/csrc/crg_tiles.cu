@@ -1,16 +1,19 @@
-// crg_tiles.cu -- row tiles with shared-memory column staging for the batched
-// apply (built once per regridder direction).
+// crg_tiles.cu -- row tiles for the staged batched apply (built once per
+// regridder direction).
 //
 // Rows are taken in the spatial (cube-face Morton) order of their cells.  A
-// tile is a run of consecutive rows in that order; for each tile the sorted
-// set of distinct source columns it touches is stored, and every entry gets a
-// 16-bit index into that set.  At apply time a CTA copies the tile's source
-// field columns into shared memory once and then reads them from there, so a
-// source element crosses L2 -> SM about once per tile instead of once per
-// nonzero.  Tiles start at kTileRows rows; a tile that touches more than
-// kTileUMax columns (or holds more than kTileEMax entries) is split into four
-// quarter tiles, down to single rows; single rows that are still too wide
-// (a coarse cell over a fine grid) go to the direct-gather kernels.
+// tile is a run of consecutive rows in that order; per tile the library keeps
+// (a) the sorted distinct source columns it touches, with a 16-bit index into
+// that set for every entry -- the staging unit for fields stored cell-major,
+// where one column is the contiguous vector of a cell's fields -- and (b) the
+// sorted distinct 4-cell chunks (column >> 2) with a 16-bit index
+// 4 * chunk + (column & 3) for every entry -- the staging unit for fields
+// stored field-major, where a chunk is one aligned 16-byte (FP32) piece of a
+// field.  At apply time a CTA copies a tile's pieces into shared memory with
+// asynchronous copies and computes from there.  Tiles start at kTileRows rows;
+// a tile touching more than kTileUMax columns (or holding more than kTileEMax
+// entries) is split into quarters down to single rows; single rows that are
+// still too wide (a coarse cell over a fine grid) go to direct-gather kernels.
 #include <algorithm>
 #include <vector>
 
@@ -26,7 +29,7 @@ inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 constexpr int kThreads = 256;
 
 // Column indices of rows [p0, p0+nr) gathered into s_col[0..E), padded with
-// INT_MAX to a power of two P and sorted; returns E, or -1 if E > kTileEMax.
+// INT_MAX to a power of two and sorted; returns E, or -1 if E > kTileEMax.
 __device__ int load_tile_cols(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                               const int32_t* __restrict__ rows, int64_t p0, int nr, int32_t* s_col, int32_t* s_off,
                               int32_t* s_rowbeg) {
@@ -75,12 +78,23 @@ __device__ int load_tile_cols(const int32_t* __restrict__ ptr, const int32_t* __
   return E;
 }
 
-// Distinct-column count of candidate tiles cand[b] = [id*TR, id*TR+TR); -1 if too large.
+__device__ __forceinline__ int block_count(int c, int* s_red) {
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = c;
+  __syncthreads();
+  int t = 0;
+  for (int w = 0; w < kThreads / 32; ++w) t += s_red[w];
+  __syncthreads();
+  return t;
+}
+
+// Candidate tiles [id*TR, id*TR+TR): distinct columns and distinct chunks
+// (-1 in u_out when the tile has to be split).
 __global__ void __launch_bounds__(kThreads) k_tile_count(const int32_t* __restrict__ ptr,
                                                         const int32_t* __restrict__ idx,
                                                         const int32_t* __restrict__ rows, int64_t nrows,
                                                         const int32_t* __restrict__ cand, int TR,
-                                                        int32_t* __restrict__ u_out) {
+                                                        int32_t* __restrict__ u_out, int32_t* __restrict__ c_out) {
   __shared__ int32_t s_col[kTileEMax];
   __shared__ int32_t s_off[kTileRows + 1];
   __shared__ int32_t s_rowbeg[kTileRows];
@@ -92,44 +106,26 @@ __global__ void __launch_bounds__(kThreads) k_tile_count(const int32_t* __restri
     if (threadIdx.x == 0) u_out[blockIdx.x] = -1;
     return;
   }
-  int c = 0;
-  for (int i = threadIdx.x; i < E; i += kThreads) c += (i == 0 || s_col[i] != s_col[i - 1]) ? 1 : 0;
-  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
-  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = c;
-  __syncthreads();
+  int cu = 0, cc = 0;
+  for (int i = threadIdx.x; i < E; i += kThreads) {
+    cu += (i == 0 || s_col[i] != s_col[i - 1]) ? 1 : 0;
+    cc += (i == 0 || (s_col[i] >> 2) != (s_col[i - 1] >> 2)) ? 1 : 0;
+  }
+  const int u = block_count(cu, s_red);
+  const int nc = block_count(cc, s_red);
   if (threadIdx.x == 0) {
-    int u = 0;
-    for (int w = 0; w < kThreads / 32; ++w) u += s_red[w];
     u_out[blockIdx.x] = u <= kTileUMax ? u : -1;
+    c_out[blockIdx.x] = nc;
   }
 }
 
-// Good tiles: distinct columns, 16-bit local column of every entry, and the
-// three weight arrays permuted into processing order.
-__global__ void __launch_bounds__(kThreads) k_tile_fill(const int32_t* __restrict__ ptr,
-                                                       const int32_t* __restrict__ idx,
-                                                       const float* __restrict__ val32, const float* __restrict__ wn32,
-                                                       const float* __restrict__ adj32,
-                                                       const int32_t* __restrict__ rows,
-                                                       const int2* __restrict__ tiles,
-                                                       const int32_t* __restrict__ uoff,
-                                                       const int32_t* __restrict__ lptr, int32_t* __restrict__ ucol,
-                                                       uint16_t* __restrict__ lcol, float* __restrict__ lw_val,
-                                                       float* __restrict__ lw_wn, float* __restrict__ lw_adj) {
-  __shared__ int32_t s_col[kTileEMax];
-  __shared__ int32_t s_uniq[kTileUMax];
-  __shared__ int32_t s_off[kTileRows + 1];
-  __shared__ int32_t s_rowbeg[kTileRows];
-  __shared__ int32_t s_wcnt[kThreads / 32 + 1];
-  const int2 tr = tiles[blockIdx.x];
-  const int64_t p0 = tr.x;
-  const int nr = tr.y - tr.x;
-  const int E = load_tile_cols(ptr, idx, rows, p0, nr, s_col, s_off, s_rowbeg);
+// Order-preserving compaction of the flagged keys of s_col[0..E) into out.
+__device__ int compact_sorted(const int32_t* s_col, int E, int shift, int32_t* out, int32_t* s_wcnt) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   int base = 0;
   for (int c0 = 0; c0 < E; c0 += kThreads) {
     int i = c0 + tid;
-    int flag = (i < E && (i == 0 || s_col[i] != s_col[i - 1])) ? 1 : 0;
+    int flag = (i < E && (i == 0 || (s_col[i] >> shift) != (s_col[i - 1] >> shift))) ? 1 : 0;
     unsigned m = __ballot_sync(0xffffffffu, flag);
     int pre = __popc(m & ((1u << lane) - 1));
     if (lane == 0) s_wcnt[warp] = __popc(m);
@@ -140,13 +136,50 @@ __global__ void __launch_bounds__(kThreads) k_tile_fill(const int32_t* __restric
       s_wcnt[kThreads / 32] = run;
     }
     __syncthreads();
-    if (flag) s_uniq[base + s_wcnt[warp] + pre] = s_col[i];
+    if (flag) out[base + s_wcnt[warp] + pre] = s_col[i] >> shift;
     base += s_wcnt[kThreads / 32];
     __syncthreads();
   }
-  const int u = base;
-  const int32_t u0 = uoff[blockIdx.x];
-  for (int i = tid; i < u; i += kThreads) ucol[u0 + i] = s_uniq[i];
+  return base;
+}
+
+__device__ __forceinline__ int lower_bound(const int32_t* a, int n, int32_t key) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Good tiles: distinct columns and chunks, the two 16-bit local indices of
+// every entry, and the three weight arrays permuted into processing order.
+__global__ void __launch_bounds__(kThreads) k_tile_fill(const int32_t* __restrict__ ptr,
+                                                       const int32_t* __restrict__ idx,
+                                                       const float* __restrict__ val32, const float* __restrict__ wn32,
+                                                       const float* __restrict__ adj32,
+                                                       const int32_t* __restrict__ rows,
+                                                       const int32_t* __restrict__ desc,
+                                                       const int32_t* __restrict__ lptr, int32_t* __restrict__ ucol,
+                                                       int32_t* __restrict__ uchunk, uint16_t* __restrict__ lcol,
+                                                       uint16_t* __restrict__ lchk, float* __restrict__ lw_val,
+                                                       float* __restrict__ lw_wn, float* __restrict__ lw_adj) {
+  __shared__ int32_t s_col[kTileEMax];
+  __shared__ int32_t s_uniq[kTileUMax];
+  __shared__ int32_t s_chunk[kTileUMax];
+  __shared__ int32_t s_off[kTileRows + 1];
+  __shared__ int32_t s_rowbeg[kTileRows];
+  __shared__ int32_t s_wcnt[kThreads / 32 + 1];
+  const int32_t* d = desc + (int64_t)blockIdx.x * kDescInts;
+  const int64_t p0 = d[kDescP0];
+  const int nr = d[kDescNr];
+  const int E = load_tile_cols(ptr, idx, rows, p0, nr, s_col, s_off, s_rowbeg);
+  const int u = compact_sorted(s_col, E, 0, s_uniq, s_wcnt);
+  const int nc = compact_sorted(s_col, E, 2, s_chunk, s_wcnt);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < u; i += kThreads) ucol[d[kDescU0] + i] = s_uniq[i];
+  for (int i = tid; i < nc; i += kThreads) uchunk[d[kDescC0] + i] = s_chunk[i];
   for (int e = tid; e < E; e += kThreads) {
     int lo = 0, hi = nr - 1;
     while (lo < hi) {
@@ -156,37 +189,13 @@ __global__ void __launch_bounds__(kThreads) k_tile_fill(const int32_t* __restric
     }
     const int32_t src = s_rowbeg[lo] + (e - s_off[lo]);
     const int32_t col = idx[src];
-    int a = 0, b = u - 1;
-    while (a < b) {
-      int mid = (a + b) >> 1;
-      if (s_uniq[mid] < col) a = mid + 1;
-      else b = mid;
-    }
     const int32_t dk = lptr[p0 + lo] + (e - s_off[lo]);
-    lcol[dk] = (uint16_t)a;
+    lcol[dk] = (uint16_t)lower_bound(s_uniq, u, col);
+    lchk[dk] = (uint16_t)(4 * lower_bound(s_chunk, nc, col >> 2) + (col & 3));
     lw_val[dk] = val32[src];
     lw_wn[dk] = wn32[src];
     lw_adj[dk] = adj32[src];
   }
-}
-
-// Rows keyed by their first (smallest) column; empty rows get key ncols.
-__global__ void k_firstcol_hist(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
-                                int64_t ncols, int32_t* __restrict__ cnt) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  const int32_t k = ptr[r];
-  atomicAdd(&cnt[k < ptr[r + 1] ? idx[k] : ncols], 1);
-}
-
-__global__ void k_firstcol_scatter(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx, int64_t n,
-                                   int64_t ncols, const int32_t* __restrict__ off, int32_t* __restrict__ fill,
-                                   int32_t* __restrict__ order) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  const int32_t k = ptr[r];
-  const int64_t key = k < ptr[r + 1] ? idx[k] : ncols;
-  order[off[key] + atomicAdd(&fill[key], 1)] = (int32_t)r;
 }
 
 __global__ void k_len_perm(const int32_t* __restrict__ ptr, const int32_t* __restrict__ rows, int64_t n,
@@ -206,79 +215,70 @@ T* palloc(size_t n) {
 }
 
 template <class T>
-T* upload(const std::vector<T>& v) {
+T* upload(const std::vector<T>& v, cudaStream_t st) {
   T* p = palloc<T>(v.size());
-  if (!v.empty()) CRG_CHECK_CUDA(cudaMemcpy(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+  if (!v.empty()) {
+    CRG_CHECK_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  }
   return p;
 }
 
 }  // namespace
 
 void free_tiles(DevTiles& t) {
-  cudaFree(t.rows); cudaFree(t.lptr); cudaFree(t.lcol); cudaFree(t.lw_val); cudaFree(t.lw_wn); cudaFree(t.lw_adj);
-  cudaFree(t.tiles); cudaFree(t.uoff); cudaFree(t.ucol); cudaFree(t.direct);
+  cudaFree(t.rows); cudaFree(t.lptr); cudaFree(t.lcol); cudaFree(t.lchk);
+  cudaFree(t.lw_val); cudaFree(t.lw_wn); cudaFree(t.lw_adj);
+  cudaFree(t.desc); cudaFree(t.ucol); cudaFree(t.uchunk); cudaFree(t.direct);
   t = DevTiles{};
 }
 
 void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st) {
   DevTiles& T = c.tiles;
   const int64_t n = c.nrows, nnz = c.nnz;
-  // rows by first column: counting sort over ncols + 1 keys
-  c.order_by_col = palloc<int32_t>((size_t)n);
-  if (n > 0) {
-    const int64_t nk = c.ncols + 1;
-    int32_t *cnt = nullptr, *fill = nullptr;
-    CRG_CHECK_CUDA(cudaMallocAsync((void**)&cnt, sizeof(int32_t) * (nk + 1), st));
-    CRG_CHECK_CUDA(cudaMallocAsync((void**)&fill, sizeof(int32_t) * nk, st));
-    CRG_CHECK_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nk + 1), st));
-    CRG_CHECK_CUDA(cudaMemsetAsync(fill, 0, sizeof(int32_t) * nk, st));
-    k_firstcol_hist<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, n, c.ncols, cnt);
-    CRG_CHECK_CUDA(cudaGetLastError());
-    exclusive_scan_i32(cnt, cnt, nk, st);
-    k_firstcol_scatter<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, n, c.ncols, cnt, fill, c.order_by_col);
-    CRG_CHECK_CUDA(cudaGetLastError());
-    CRG_CHECK_CUDA(cudaFreeAsync(cnt, st));
-    CRG_CHECK_CUDA(cudaFreeAsync(fill, st));
-  }
   T.rows = palloc<int32_t>((size_t)n);
   T.lptr = palloc<int32_t>((size_t)n + 1);
-  T.lcol = palloc<uint16_t>((size_t)nnz);
+  T.lcol = palloc<uint16_t>((size_t)nnz + 2);  // +2: read as 32-bit words
+  T.lchk = palloc<uint16_t>((size_t)nnz + 2);
   T.lw_val = palloc<float>((size_t)nnz);
   T.lw_wn = palloc<float>((size_t)nnz);
   T.lw_adj = palloc<float>((size_t)nnz);
-  std::vector<int2> good;
-  std::vector<int32_t> gu, direct;
+  struct Good { int32_t p0, p1, u, nc; };
+  std::vector<Good> good;
+  std::vector<int32_t> direct;
+  std::vector<int32_t> hlptr((size_t)n + 1, 0);
   if (n > 0) {
     CRG_CHECK_CUDA(cudaMemcpyAsync(T.rows, row_order, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st));
     k_len_perm<<<nblk(n, 256), 256, 0, st>>>(c.ptr, T.rows, n, T.lptr);
     CRG_CHECK_CUDA(cudaGetLastError());
     exclusive_scan_i32(T.lptr, T.lptr, n, st);
+    CRG_CHECK_CUDA(cudaMemcpyAsync(hlptr.data(), T.lptr, sizeof(int32_t) * (n + 1), cudaMemcpyDeviceToHost, st));
     // refinement: tiles of kTileRows, then quarters, down to single rows
     std::vector<int32_t> cand((size_t)((n + kTileRows - 1) / kTileRows));
     for (size_t i = 0; i < cand.size(); ++i) cand[i] = (int32_t)i;
-    int32_t* dcand = nullptr;
-    int32_t* du = nullptr;
+    int32_t *dcand = nullptr, *du = nullptr, *dc = nullptr;
     size_t cap = 0;
     for (int TR = kTileRows; TR >= 1 && !cand.empty(); TR /= 4) {
       if (cand.size() > cap) {
-        if (dcand) { cudaFreeAsync(dcand, st); cudaFreeAsync(du, st); }
+        if (dcand) { cudaFreeAsync(dcand, st); cudaFreeAsync(du, st); cudaFreeAsync(dc, st); }
         cap = cand.size();
         CRG_CHECK_CUDA(cudaMallocAsync((void**)&dcand, sizeof(int32_t) * cap, st));
         CRG_CHECK_CUDA(cudaMallocAsync((void**)&du, sizeof(int32_t) * cap, st));
+        CRG_CHECK_CUDA(cudaMallocAsync((void**)&dc, sizeof(int32_t) * cap, st));
       }
       CRG_CHECK_CUDA(cudaMemcpyAsync(dcand, cand.data(), sizeof(int32_t) * cand.size(), cudaMemcpyHostToDevice, st));
-      k_tile_count<<<(unsigned)cand.size(), kThreads, 0, st>>>(c.ptr, c.idx, T.rows, n, dcand, TR, du);
+      k_tile_count<<<(unsigned)cand.size(), kThreads, 0, st>>>(c.ptr, c.idx, T.rows, n, dcand, TR, du, dc);
       CRG_CHECK_CUDA(cudaGetLastError());
-      std::vector<int32_t> u(cand.size());
+      std::vector<int32_t> u(cand.size()), nc(cand.size());
       CRG_CHECK_CUDA(cudaMemcpyAsync(u.data(), du, sizeof(int32_t) * u.size(), cudaMemcpyDeviceToHost, st));
+      CRG_CHECK_CUDA(cudaMemcpyAsync(nc.data(), dc, sizeof(int32_t) * nc.size(), cudaMemcpyDeviceToHost, st));
       CRG_CHECK_CUDA(cudaStreamSynchronize(st));
       std::vector<int32_t> next;
       const int sub = TR / 4;
       for (size_t i = 0; i < cand.size(); ++i) {
         const int64_t p0 = (int64_t)cand[i] * TR, p1 = std::min<int64_t>(n, p0 + TR);
         if (u[i] >= 0) {
-          good.push_back(make_int2((int)p0, (int)p1));
-          gu.push_back(u[i]);
+          good.push_back(Good{(int32_t)p0, (int32_t)p1, u[i], nc[i]});
         } else if (TR > 1) {
           for (int j = 0; j < 4; ++j) {
             int64_t q = (int64_t)cand[i] * 4 + j;
@@ -291,32 +291,40 @@ void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st) {
       cand.swap(next);
       if (TR == 1) break;
     }
-    if (dcand) { cudaFreeAsync(dcand, st); cudaFreeAsync(du, st); }
+    if (dcand) { cudaFreeAsync(dcand, st); cudaFreeAsync(du, st); cudaFreeAsync(dc, st); }
   } else {
     CRG_CHECK_CUDA(cudaMemsetAsync(T.lptr, 0, sizeof(int32_t), st));
   }
-  // process tiles in row order (neighbouring CTAs share source columns in L2)
-  std::vector<size_t> order(good.size());
-  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
-  std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return good[a].x < good[b].x; });
-  std::vector<int2> gs(good.size());
-  std::vector<int32_t> uoff(good.size() + 1, 0);
-  for (size_t i = 0; i < order.size(); ++i) {
-    gs[i] = good[order[i]];
-    uoff[i + 1] = uoff[i] + gu[order[i]];
+  // descriptors in row order, so neighbouring work shares source columns in L2
+  std::sort(good.begin(), good.end(), [](const Good& a, const Good& b) { return a.p0 < b.p0; });
+  std::vector<int32_t> desc(good.size() * kDescInts);
+  int64_t uacc = 0, cacc = 0;
+  for (size_t i = 0; i < good.size(); ++i) {
+    int32_t* d = &desc[i * kDescInts];
+    d[kDescP0] = good[i].p0;
+    d[kDescNr] = good[i].p1 - good[i].p0;
+    d[kDescU0] = (int32_t)uacc;
+    d[kDescNu] = good[i].u;
+    d[kDescE0] = hlptr[good[i].p0];
+    d[kDescNe] = hlptr[good[i].p1] - hlptr[good[i].p0];
+    d[kDescC0] = (int32_t)cacc;
+    d[kDescNc] = good[i].nc;
+    uacc += good[i].u;
+    cacc += good[i].nc;
   }
   std::sort(direct.begin(), direct.end());
-  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-  T.ngood = (int64_t)gs.size();
+  T.ngood = (int64_t)good.size();
   T.ndirect = (int64_t)direct.size();
-  T.nucol = uoff.back();
-  T.tiles = upload(gs);
-  T.uoff = upload(uoff);
-  T.direct = upload(direct);
-  T.ucol = palloc<int32_t>((size_t)T.nucol);
+  T.nucol = uacc;
+  T.nuchunk = cacc;
+  T.desc = upload(desc, st);
+  T.direct = upload(direct, st);
+  T.ucol = palloc<int32_t>((size_t)uacc);
+  T.uchunk = palloc<int32_t>((size_t)cacc);
   if (T.ngood) {
-    k_tile_fill<<<(unsigned)T.ngood, kThreads, 0, st>>>(c.ptr, c.idx, c.val32, c.wn32, c.adj32, T.rows, T.tiles,
-                                                        T.uoff, T.lptr, T.ucol, T.lcol, T.lw_val, T.lw_wn, T.lw_adj);
+    k_tile_fill<<<(unsigned)T.ngood, kThreads, 0, st>>>(c.ptr, c.idx, c.val32, c.wn32, c.adj32, T.rows, T.desc,
+                                                        T.lptr, T.ucol, T.uchunk, T.lcol, T.lchk, T.lw_val, T.lw_wn,
+                                                        T.lw_adj);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
 }
