@@ -53,6 +53,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--profile", action="store_true",
                    help="only build and run `steps` forward+transpose SpMM rounds (for an ncu capture)")
+    p.add_argument("--pair", default="c5", choices=["c5", "identity"],
+                   help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
+                        "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
     return p.parse_args()
 
 
@@ -66,6 +69,8 @@ def run_profile(a):
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
     hp, ll = grids_c5(a.nside, a.dlon)
+    if a.pair == "identity":
+        hp = ll
     R = Regridder(hp, ll, normalize=True)
     T = R.transpose()
     K, nd, ns = a.fields, R.shape[0], R.shape[1]
