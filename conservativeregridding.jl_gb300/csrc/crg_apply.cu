@@ -642,17 +642,143 @@ void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int
   }
 }
 
+// ------------------------------------------------------------------ merge-path (cell-major)
+
+// Each warp walks tasks of kTaskNnz consecutive entries.  Lanes load 32
+// (column, weight, row) entries with one coalesced load each, then every entry
+// is broadcast and the whole warp gathers that cell's 128 fields (4 per lane,
+// 16-byte loads); 8 gathers are issued before they are consumed.  Rows are
+// accumulated in entry order and written when the row changes; a row that
+// began in an earlier task or continues into a later one is written to the
+// task's carry slot (0 = first row, 1 = last row) for k_cm_fixup.
+template <class T>
+__global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                   const int32_t* __restrict__ erow, const float* __restrict__ w,
+                                                   int64_t nnz, int64_t ntasks, const T* __restrict__ x, int64_t xs,
+                                                   T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf,
+                                                   float* __restrict__ carry) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t f = f0 + (int64_t)lane * 4;
+  const bool on = f < nf;
+  const int64_t fo = on ? f : f0;
+  for (int64_t task = gw; task < ntasks; task += nw) {
+    const int64_t e0 = task * kTaskNnz;
+    const int64_t e1 = min(nnz, e0 + kTaskNnz);
+    const int32_t first = __ldg(erow + e0), last = __ldg(erow + e1 - 1);
+    const bool first_split = __ldg(ptr + first) < e0;
+    const bool last_split = __ldg(ptr + last + 1) > e1;
+    int32_t cur = -1;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    auto flush = [&](int32_t row) {
+      if (!on) return;
+      if (row == first && first_split) {
+        *reinterpret_cast<float4*>(carry + (task * 2 + 0) * 128 + lane * 4) = acc;
+      } else if (row == last && last_split) {
+        *reinterpret_cast<float4*>(carry + (task * 2 + 1) * 128 + lane * 4) = acc;
+      } else {
+        st4<T>(y + (int64_t)row * ys + fo, acc);
+      }
+    };
+    for (int64_t c0 = e0; c0 < e1; c0 += 32) {
+      const int64_t e = c0 + lane;
+      const bool valid = e < e1;
+      const int32_t myj = valid ? __ldg(idx + e) : 0;
+      const float myw = valid ? __ldg(w + e) : 0.f;
+      const int32_t myr = valid ? __ldg(erow + e) : -1;
+      const int n = (int)(e1 - c0 < 32 ? e1 - c0 : 32);
+      for (int k = 0; k < n; k += 8) {
+        float4 v[8];
+        float ww[8];
+        int32_t rr[8];
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          const int32_t j = __shfl_sync(0xffffffffu, myj, k + h);
+          ww[h] = __shfl_sync(0xffffffffu, myw, k + h);
+          rr[h] = __shfl_sync(0xffffffffu, myr, k + h);
+          const bool live = k + h < n;
+          if (!live) rr[h] = -2;
+          v[h] = live ? ld4<T>(x + (int64_t)j * xs + fo) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          if (rr[h] == -2) break;
+          if (rr[h] != cur) {
+            if (cur >= 0) flush(cur);
+            cur = rr[h];
+            acc = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+          acc.x = fmaf(ww[h], v[h].x, acc.x);
+          acc.y = fmaf(ww[h], v[h].y, acc.y);
+          acc.z = fmaf(ww[h], v[h].z, acc.z);
+          acc.w = fmaf(ww[h], v[h].w, acc.w);
+        }
+      }
+    }
+    if (cur >= 0) flush(cur);
+  }
+}
+
+// Rows spanning tasks: sum the carries in task order (deterministic).
+template <class T>
+__global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, const float* __restrict__ carry,
+                           T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf) {
+  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wi >= nsplit) return;
+  const int32_t row = split[3 * wi], t0 = split[3 * wi + 1], t1 = split[3 * wi + 2];
+  const int64_t f = f0 + (int64_t)lane * 4;
+  if (f >= nf) return;
+  float4 s = *reinterpret_cast<const float4*>(carry + ((int64_t)t0 * 2 + 1) * 128 + lane * 4);
+  for (int32_t t = t0 + 1; t <= t1; ++t) {
+    const float4 c = *reinterpret_cast<const float4*>(carry + ((int64_t)t * 2 + 0) * 128 + lane * 4);
+    s.x += c.x; s.y += c.y; s.z += c.z; s.w += c.w;
+  }
+  st4<T>(y + (int64_t)row * ys + f, s);
+}
+
+template <class T>
+void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                   cudaStream_t st) {
+  const int64_t ntasks = (c.nnz + kTaskNnz - 1) / kTaskNnz;
+  float* carry = nullptr;
+  if (ntasks) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * ntasks * 2 * 128, st));
+  const int64_t warps = std::min<int64_t>(ntasks, (int64_t)num_sms() * 24);
+  for (int64_t f0 = 0; f0 < nf; f0 += 128) {
+    if (ntasks) {
+      k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.ptr, c.idx, c.erow, w, c.nnz, ntasks, x, xs, y, ys, f0,
+                                                         nf, carry);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (c.nsplit) {
+      k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+  }
+  if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
+}
+
+// Rows without entries produce zero output (the row gather writes nothing for them).
+template <class T>
+__global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* __restrict__ y, int64_t ys, int64_t nf) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n || ptr[r + 1] > ptr[r]) return;
+  for (int64_t f = 0; f < nf; ++f) st1<T>(y + r * ys + f, 0.f);
+}
+
 // Kernel choice for FP32/BF16 fields.  CRG_SPMM_PATH selects an alternative
 // for tuning and profiling: "tiled" (shared-memory staged tiles) or "legacy"
 // (first-generation row kernels); unset = the register-blocked row kernels.
-enum class SpmmPath { kRows, kTiled, kLegacy };
+enum class SpmmPath { kAuto, kRows, kTiled, kLegacy };
 
 inline SpmmPath spmm_path() {
   static const SpmmPath p = [] {
     const char* e = getenv("CRG_SPMM_PATH");
     if (e && strcmp(e, "tiled") == 0) return SpmmPath::kTiled;
     if (e && strcmp(e, "legacy") == 0) return SpmmPath::kLegacy;
-    return SpmmPath::kRows;
+    if (e && strcmp(e, "rows") == 0) return SpmmPath::kRows;
+    return SpmmPath::kAuto;
   }();
   return p;
 }
@@ -712,7 +838,14 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       return;
     }
   }
-  if (path == SpmmPath::kRows) {
+  if (path == SpmmPath::kAuto && cell_major && vec4 && nf >= 32) {
+    // merge-path over entries; rows with no entries are zeroed separately
+    launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st);
+    k_zero_empty_cm<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, y, ysc, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    return;
+  }
+  if (path == SpmmPath::kRows || path == SpmmPath::kAuto) {
     if (cell_major && vec4) {
       launch_cm_rows<T>(c, w, x, xsc, y, ysc, nf, st);
       CRG_CHECK_CUDA(cudaGetLastError());

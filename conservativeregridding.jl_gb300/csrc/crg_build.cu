@@ -852,6 +852,8 @@ bool is_device_pointer(const void* p) {
 
 void free_csr(DevCsr& c) {
   free_tiles(c.tiles);
+  cudaFree(c.erow);
+  cudaFree(c.split);
   cudaFree(c.ptr); cudaFree(c.idx); cudaFree(c.val); cudaFree(c.val32); cudaFree(c.wn32); cudaFree(c.adj32);
   c = DevCsr{};
 }
@@ -999,6 +1001,8 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     // staged-tile layouts, rows in the spatial order of their cells
     build_tiles(R->fwd, td.perm.p, st);
     build_tiles(R->rev, ts.perm.p, st);
+    build_merge_path(R->fwd, st);
+    build_merge_path(R->rev, st);
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[3], st));
     CRG_CHECK_CUDA(cudaEventSynchronize(ev.e[3]));
     float t01 = 0, t12 = 0, t23 = 0, t03 = 0;

@@ -71,7 +71,13 @@ struct DevCsr {
   float* wn32 = nullptr;     // [nnz] A_rc / area_row (FP32): normalised weights of this direction
   float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
   DevTiles tiles;            // staged-tile layout for the batched FP32/BF16 apply
+  // merge-path layout: fixed runs of kTaskNnz entries per task
+  int32_t* erow = nullptr;   // [nnz] row of each entry
+  int32_t* split = nullptr;  // [nsplit][3] rows spanning tasks: row, first task, last task
+  int64_t nsplit = 0;
 };
+
+constexpr int kTaskNnz = 256;  // entries per merge-path task
 
 // Per-cell vertex table on the device: [n][maxv] unit vectors (z = 0 planar).
 struct CellTable {
@@ -111,5 +117,6 @@ void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, 
                 int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int normalize, cudaStream_t st);
 bool is_device_pointer(const void* p);
 void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st);
+void build_merge_path(DevCsr& c, cudaStream_t st);
 void free_tiles(DevTiles& t);
 }  // namespace crg

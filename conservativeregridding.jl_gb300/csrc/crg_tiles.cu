@@ -330,3 +330,69 @@ void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st) {
 }
 
 }  // namespace crg
+
+// ---------------------------------------------------------------------------
+// Merge-path layout: the entries of a direction are cut into tasks of
+// kTaskNnz consecutive entries (CSR order).  Rows whose entries straddle a task
+// boundary are listed with the first and last task they touch, so the apply
+// can combine their per-task partial sums in task order afterwards.
+
+namespace crg {
+
+namespace {
+
+__global__ void k_expand_rows(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ erow) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) erow[k] = (int32_t)r;
+}
+
+__global__ void k_split_flags(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ flag) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t a = ptr[r], b = ptr[r + 1];
+  flag[r] = (b > a && (a / kTaskNnz) != ((b - 1) / kTaskNnz)) ? 1 : 0;
+}
+
+__global__ void k_split_fill(const int32_t* __restrict__ ptr, int64_t n, const int32_t* __restrict__ pos,
+                             int32_t* __restrict__ split) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t a = ptr[r], b = ptr[r + 1];
+  if (b > a && (a / kTaskNnz) != ((b - 1) / kTaskNnz)) {
+    int32_t* s = split + 3 * (int64_t)pos[r];
+    s[0] = (int32_t)r;
+    s[1] = a / kTaskNnz;
+    s[2] = (b - 1) / kTaskNnz;
+  }
+}
+
+}  // namespace
+
+void build_merge_path(DevCsr& c, cudaStream_t st) {
+  const int64_t n = c.nrows, nnz = c.nnz;
+  CRG_CHECK_CUDA(cudaMalloc((void**)&c.erow, sizeof(int32_t) * (nnz ? nnz : 1)));
+  if (n == 0) {
+    CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3));
+    return;
+  }
+  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  int32_t* pos = nullptr;
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&pos, sizeof(int32_t) * (n + 1), st));
+  k_split_flags<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, pos);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  exclusive_scan_i32(pos, pos, n, st);
+  int32_t ns = 0;
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&ns, pos + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  c.nsplit = ns;
+  CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3 * (ns ? ns : 1)));
+  if (ns) {
+    k_split_fill<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, pos, c.split);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  CRG_CHECK_CUDA(cudaFreeAsync(pos, st));
+}
+
+}  // namespace crg
