@@ -651,6 +651,14 @@ void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int
 // accumulated in entry order and written when the row changes; a row that
 // began in an earlier task or continues into a later one is written to the
 // task's carry slot (0 = first row, 1 = last row) for k_cm_fixup.
+template <class T> __device__ __forceinline__ float4 ldoff4(const char* base, uint32_t off);
+template <> __device__ __forceinline__ float4 ldoff4<float>(const char* base, uint32_t off) {
+  return __ldg(reinterpret_cast<const float4*>(base + off));
+}
+template <> __device__ __forceinline__ float4 ldoff4<__nv_bfloat16>(const char* base, uint32_t off) {
+  return ld4<__nv_bfloat16>(reinterpret_cast<const __nv_bfloat16*>(base + off));
+}
+
 template <class T>
 __global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                                                    const int32_t* __restrict__ erow, const float* __restrict__ w,
@@ -663,13 +671,16 @@ __global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ p
   const int64_t f = f0 + (int64_t)lane * 4;
   const bool on = f < nf;
   const int64_t fo = on ? f : f0;
+  // per-lane base of this lane's 4 fields; cell j adds j * xs elements (32-bit byte offset)
+  const char* xb = reinterpret_cast<const char*>(x + fo);
+  const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(T));
   for (int64_t task = gw; task < ntasks; task += nw) {
     const int64_t e0 = task * kTaskNnz;
     const int64_t e1 = min(nnz, e0 + kTaskNnz);
     const int32_t first = __ldg(erow + e0), last = __ldg(erow + e1 - 1);
     const bool first_split = __ldg(ptr + first) < e0;
     const bool last_split = __ldg(ptr + last + 1) > e1;
-    int32_t cur = -1;
+    int32_t cur = first;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto flush = [&](int32_t row) {
       if (!on) return;
@@ -681,32 +692,33 @@ __global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ p
         st4<T>(y + (int64_t)row * ys + fo, acc);
       }
     };
+    int32_t prev_last = first;  // row of the entry before the current chunk
     for (int64_t c0 = e0; c0 < e1; c0 += 32) {
       const int64_t e = c0 + lane;
       const bool valid = e < e1;
-      const int32_t myj = valid ? __ldg(idx + e) : 0;
+      const int32_t myr = valid ? __ldg(erow + e) : 0x7fffffff;
+      const uint32_t myo = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
       const float myw = valid ? __ldg(w + e) : 0.f;
-      const int32_t myr = valid ? __ldg(erow + e) : -1;
+      int32_t before = __shfl_up_sync(0xffffffffu, myr, 1);
+      if (lane == 0) before = prev_last;
+      const unsigned newrow = __ballot_sync(0xffffffffu, valid && myr != before);  // entry starts a new row
+      prev_last = __shfl_sync(0xffffffffu, myr, 31);
       const int n = (int)(e1 - c0 < 32 ? e1 - c0 : 32);
       for (int k = 0; k < n; k += 8) {
         float4 v[8];
         float ww[8];
-        int32_t rr[8];
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
-          const int32_t j = __shfl_sync(0xffffffffu, myj, k + h);
+          const uint32_t o = __shfl_sync(0xffffffffu, myo, k + h);
           ww[h] = __shfl_sync(0xffffffffu, myw, k + h);
-          rr[h] = __shfl_sync(0xffffffffu, myr, k + h);
-          const bool live = k + h < n;
-          if (!live) rr[h] = -2;
-          v[h] = live ? ld4<T>(x + (int64_t)j * xs + fo) : make_float4(0.f, 0.f, 0.f, 0.f);
+          v[h] = ldoff4<T>(xb, o);  // past-the-end entries load cell 0 with weight 0
         }
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
-          if (rr[h] == -2) break;
-          if (rr[h] != cur) {
-            if (cur >= 0) flush(cur);
-            cur = rr[h];
+          if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
+          if ((newrow >> (k + h)) & 1u) {
+            flush(cur);
+            cur = __shfl_sync(0xffffffffu, myr, k + h);
             acc = make_float4(0.f, 0.f, 0.f, 0.f);
           }
           acc.x = fmaf(ww[h], v[h].x, acc.x);
@@ -716,7 +728,7 @@ __global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ p
         }
       }
     }
-    if (cur >= 0) flush(cur);
+    flush(cur);
   }
 }
 
@@ -838,7 +850,9 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       return;
     }
   }
-  if (path == SpmmPath::kAuto && cell_major && vec4 && nf >= 32) {
+  // the merge-path kernel addresses source cells with 32-bit byte offsets
+  const bool span32 = (double)c.ncols * (double)xsc * es < 4.0e9;
+  if (path == SpmmPath::kAuto && cell_major && vec4 && nf >= 32 && span32) {
     // merge-path over entries; rows with no entries are zeroed separately
     launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st);
     k_zero_empty_cm<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, y, ysc, nf);
