@@ -1,0 +1,163 @@
+"""
+    ConservativeRegriddingGB300
+
+Julia binding of `libcrg_gb300.so` (declared in `include/crg.h`): the GPU build
+and apply of ConservativeRegridding.jl's `Regridder`, `regrid!` and
+`transpose(R)`.  The matrix, the areas and the weights live on the GPU; field
+arrays may be `CuArray`s (device pointers) or host `Array`s (staged by the
+library).
+
+This file is the `ccall` layer a maintainer adds next to ConservativeRegridding.jl;
+it depends only on `Libdl` and `SparseArrays`.
+"""
+module ConservativeRegriddingGB300
+
+using Libdl
+using SparseArrays
+using LinearAlgebra
+
+const libcrg = Ref{String}("")
+
+function __init__()
+    path = get(ENV, "CRG_GB300_LIB", joinpath(@__DIR__, "..", "..", "..", "_build", "libcrg_gb300.so"))
+    libcrg[] = path
+end
+
+# --- C structs (must match include/crg.h) -------------------------------------
+
+struct CrgGridDesc
+    kind::Int32          # 0 curvilinear, 1 cells
+    manifold::Int32      # 0 planar, 1 spherical
+    nblocks::Int32
+    max_verts::Int32
+    ncells::Int64
+    block_nx::Ptr{Int64}
+    block_ny::Ptr{Int64}
+    points::Ptr{Float64}
+    cell_verts::Ptr{Float64}
+    cell_nverts::Ptr{Int32}
+end
+
+struct CrgBuildOpts
+    normalize::Int32
+    flags::Int32
+    stream::Ptr{Cvoid}
+end
+
+struct CrgInfo
+    n_dst::Int64; n_src::Int64; nnz::Int64; n_candidates::Int64
+    manifold::Int32; normalized::Int32
+    normalizer::Float64
+    t_build_ms::Float64; t_search_ms::Float64; t_clip_ms::Float64; t_assemble_ms::Float64
+    clip_overflows::Int64
+    device::Int32; pad::Int32
+    tiles::NTuple{2,Int64}; tile_columns::NTuple{2,Int64}; direct_rows::NTuple{2,Int64}
+end
+
+const CRG_F64, CRG_F32, CRG_BF16 = Int32(0), Int32(1), Int32(2)
+
+function check(status::Cint)
+    status == 0 && return nothing
+    msg = unsafe_string(ccall((:crg_last_error, libcrg[]), Cstring, ()))
+    status == 1 && throw(ArgumentError(msg))       # CRG_ERR_INVALID_ARGUMENT
+    status == 2 && throw(DimensionMismatch(msg))   # CRG_ERR_DIMENSION_MISMATCH
+    error("libcrg_gb300: " * unsafe_string(ccall((:crg_status_string, libcrg[]), Cstring, (Cint,), status)) * ": " * msg)
+end
+
+# --- the handle ---------------------------------------------------------------
+
+mutable struct GB300Sparse
+    ptr::Ptr{Cvoid}
+    info::CrgInfo
+    function GB300Sparse(ptr::Ptr{Cvoid})
+        info = Ref{CrgInfo}()
+        check(ccall((:crg_regridder_info, libcrg[]), Cint, (Ptr{Cvoid}, Ref{CrgInfo}), ptr, info))
+        h = new(ptr, info[])
+        finalizer(h) do x
+            ccall((:crg_regridder_release, libcrg[]), Cint, (Ptr{Cvoid},), x.ptr)
+        end
+        return h
+    end
+end
+
+"A transposed view: shares the handle (retained), swaps the direction."
+struct GB300SparseT
+    parent::GB300Sparse
+end
+
+Base.size(A::GB300Sparse) = (Int(A.info.n_dst), Int(A.info.n_src))
+Base.size(A::GB300SparseT) = reverse(size(A.parent))
+LinearAlgebra.transpose(A::GB300Sparse) = GB300SparseT(A)
+LinearAlgebra.transpose(A::GB300SparseT) = A.parent
+
+"""
+    curvilinear(points::Array{Float64,3})
+
+Describe a grid of `(nx+1) x (ny+1)` vertices given as a `3 x (nx+1) x (ny+1)`
+array of unit vectors (the reference's `CellBasedGrid` vertex matrix).
+"""
+function curvilinear(points::Array{Float64,3})
+    dim, nxp, nyp = size(points)
+    nx = Ref(Int64(nxp - 1)); ny = Ref(Int64(nyp - 1))
+    desc = CrgGridDesc(0, dim == 3 ? 1 : 0, 1, 0, nx[] * ny[],
+                       Base.unsafe_convert(Ptr{Int64}, nx), Base.unsafe_convert(Ptr{Int64}, ny),
+                       pointer(points), C_NULL, C_NULL)
+    return desc, (points, nx, ny)
+end
+
+"""
+    Regridder(dst_points, src_points; normalize = false) -> ConservativeRegridding.Regridder
+
+GPU build of `Regridder(dst, src; normalize)` for vertex-matrix grids.  The
+returned struct has `intersections::GB300Sparse` and host copies of the areas.
+"""
+function build(dst, src; normalize::Bool = false)
+    d, keep_d = dst
+    s, keep_s = src
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    opts = Ref(CrgBuildOpts(normalize, 0, C_NULL))
+    GC.@preserve keep_d keep_s begin
+        check(ccall((:crg_build, libcrg[]), Cint, (Ref{CrgGridDesc}, Ref{CrgGridDesc}, Ref{CrgBuildOpts}, Ref{Ptr{Cvoid}}),
+                    Ref(d), Ref(s), opts, out))
+    end
+    A = GB300Sparse(out[])
+    nd, ns = size(A)
+    dst_areas = Vector{Float64}(undef, nd)
+    src_areas = Vector{Float64}(undef, ns)
+    check(ccall((:crg_get_areas, libcrg[]), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), A.ptr, dst_areas, src_areas))
+    return A, dst_areas, src_areas
+end
+
+"""
+    apply!(y, A, x; transpose = false, normalize = true, dims = 1)
+
+`perform_regridding!` + `finalize_regridding!` for dense arrays: one call for
+all slices along the non-spatial axes (the reference loops `mul!` per slice).
+"""
+function apply!(y::AbstractArray{T}, A::Union{GB300Sparse,GB300SparseT}, x::AbstractArray{T};
+                normalize::Bool = true, dims::Int = 1) where {T<:Union{Float64,Float32}}
+    ndims(x) == ndims(y) || throw(DimensionMismatch("source and destination ranks must match"))
+    1 <= dims <= ndims(x) || throw(ArgumentError("dims=$dims is out of range for a $(ndims(x))-dimensional array"))
+    h, t = A isa GB300SparseT ? (A.parent, Int32(1)) : (A, Int32(0))
+    sx, sy = strides(x), strides(y)
+    nf = length(x) ÷ size(x, dims)
+    fx = nf == 1 ? 1 : sx[dims == 1 ? 2 : 1]   # slices must be uniformly strided (dense arrays)
+    fy = nf == 1 ? 1 : sy[dims == 1 ? 2 : 1]
+    dtype = T === Float64 ? CRG_F64 : CRG_F32
+    check(ccall((:crg_apply, libcrg[]), Cint,
+                (Ptr{Cvoid}, Int32, Int32, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Int64, Int32, Ptr{Cvoid}),
+                h.ptr, t, dtype, pointer(x), sx[dims], fx, pointer(y), sy[dims], fy, nf, normalize, C_NULL))
+    return y
+end
+
+"CSC copy of A with Julia's 1-based indices: the reference's `R.intersections`."
+function SparseArrays.SparseMatrixCSC(A::GB300Sparse)
+    nd, ns = size(A)
+    nnz = Int(A.info.nnz)
+    colptr = Vector{Int64}(undef, ns + 1); rowval = Vector{Int64}(undef, nnz); nzval = Vector{Float64}(undef, nnz)
+    check(ccall((:crg_get_csc, libcrg[]), Cint, (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}),
+                A.ptr, 1, colptr, rowval, nzval))
+    return SparseMatrixCSC(nd, ns, colptr, rowval, nzval)
+end
+
+end # module
