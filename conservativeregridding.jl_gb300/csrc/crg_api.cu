@@ -117,6 +117,14 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
   });
 }
 
+crg_status crg_apply_noalloc(const crg_regridder* r, int32_t transpose, int32_t dtype, const void* src, int64_t ssc,
+                             int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int32_t normalize,
+                             void* stream) {
+  return guarded([&] {
+    apply_noalloc_impl(r, transpose, dtype, src, ssc, ssf, dst, dsc, dsf, nfields, normalize, (cudaStream_t)stream);
+  });
+}
+
 crg_status crg_get_csc(const crg_regridder* r, int32_t index_base, int64_t* colptr, int64_t* rowval, double* nzval) {
   return guarded([&] {
     CRG_REQUIRE(r != nullptr, CRG_ERR_INVALID_ARGUMENT, "regridder is NULL");

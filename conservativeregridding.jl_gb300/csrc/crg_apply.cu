@@ -25,6 +25,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "crg_internal.cuh"
 
@@ -982,6 +983,103 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
 
   if (dst_host) CRG_CHECK_CUDA(cudaMemcpyAsync(dst, ys, (size_t)out_span * es, cudaMemcpyDeviceToHost, st));
   if (src_host || dst_host) CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace crg
+
+// ------------------------------------------------------------------ allocation-free apply
+//
+// crg_apply_noalloc runs the merge-path kernels above with their carry buffer
+// in a statically declared device array instead of memory allocated per call,
+// for callers that must not allocate device memory.  Each carry slot holds
+// 128 FP32 partial sums; a call needs 2 slots per 256-entry task.
+
+static __device__ __align__(256) float g_noalloc_carry[CRG_NOALLOC_SCRATCH_BYTES / sizeof(float)];
+
+namespace crg {
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+float* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_carry on the current device, looked up once per
+// device (the host-side name is only a stand-in, not a device address).
+float* noalloc_scratch(int dev) {
+  CRG_REQUIRE(dev >= 0 && dev < kMaxDevices, CRG_ERR_NOT_SUPPORTED, "device %d is beyond the supported %d", dev,
+              kMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    CRG_CHECK_CUDA(cudaGetSymbolAddress(&p, g_noalloc_carry));
+    CRG_REQUIRE(p != nullptr, CRG_ERR_CUDA, "cudaGetSymbolAddress returned a null scratch address");
+    g_noalloc_ptr[dev] = static_cast<float*>(p);
+  }
+  return g_noalloc_ptr[dev];
+}
+
+template <class T>
+void noalloc_launch(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                    float* carry, cudaStream_t st) {
+  const int64_t ntasks = (c.nnz + kTaskNnz - 1) / kTaskNnz;
+  const int64_t warps = std::min<int64_t>(ntasks, (int64_t)num_sms() * 24);
+  for (int64_t f0 = 0; f0 < nf; f0 += 128) {
+    if (ntasks) {
+      k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.ptr, c.idx, c.erow, w, c.nnz, ntasks, x, xs, y, ys, f0,
+                                                         nf, carry);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (c.nsplit) {
+      k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+  }
+  if (c.nrows) {
+    k_zero_empty_cm<T><<<nblk(c.nrows, 256), 256, 0, st>>>(c.ptr, c.nrows, y, ys, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+}
+
+}  // namespace
+
+void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
+                        void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st) {
+  CRG_REQUIRE(r != nullptr, CRG_ERR_INVALID_ARGUMENT, "regridder is NULL");
+  CRG_REQUIRE(dtype == CRG_F32 || dtype == CRG_BF16, CRG_ERR_NOT_SUPPORTED,
+              "crg_apply_noalloc supports CRG_F32 and CRG_BF16 fields (got dtype %d)", dtype);
+  CRG_REQUIRE(nf > 0 && nf % 4 == 0, CRG_ERR_NOT_SUPPORTED, "nfields must be a positive multiple of 4 (got %lld)",
+              (long long)nf);
+  CRG_REQUIRE(ssf == 1 && dsf == 1, CRG_ERR_NOT_SUPPORTED,
+              "crg_apply_noalloc needs the fields of a cell side by side (field strides 1)");
+  CRG_REQUIRE(ssc >= nf && dsc >= nf && ssc % 4 == 0 && dsc % 4 == 0, CRG_ERR_NOT_SUPPORTED,
+              "cell strides must be >= nfields and multiples of 4");
+  const size_t es = dtype == CRG_F32 ? 4 : 2;
+  CRG_REQUIRE(src && dst && (uintptr_t)src % (4 * es) == 0 && (uintptr_t)dst % (4 * es) == 0, CRG_ERR_NOT_SUPPORTED,
+              "field pointers must be non-NULL and %d-byte aligned", (int)(4 * es));
+  CRG_REQUIRE(is_device_pointer(src) && is_device_pointer(dst), CRG_ERR_NOT_SUPPORTED,
+              "crg_apply_noalloc takes device pointers only (host fields would need staging memory)");
+  int dev = 0;
+  CRG_CHECK_CUDA(cudaGetDevice(&dev));
+  CRG_REQUIRE(dev == r->device, CRG_ERR_INVALID_ARGUMENT, "regridder lives on device %d but device %d is current",
+              r->device, dev);
+  const bool t = transpose != 0;
+  const DevCsr& c = t ? r->rev : r->fwd;
+  const int64_t ntasks = (c.nnz + kTaskNnz - 1) / kTaskNnz;
+  const size_t need = (size_t)ntasks * 2 * 128 * sizeof(float);
+  CRG_REQUIRE(need <= CRG_NOALLOC_SCRATCH_BYTES, CRG_ERR_NOT_SUPPORTED,
+              "this regridder has %lld nonzeros and needs %zu bytes of scratch; the static scratch of "
+              "crg_apply_noalloc holds %u bytes (at most %lld nonzeros)",
+              (long long)c.nnz, need, (unsigned)CRG_NOALLOC_SCRATCH_BYTES,
+              (long long)(CRG_NOALLOC_SCRATCH_BYTES / (2 * 128 * sizeof(float))) * kTaskNnz);
+  CRG_REQUIRE((double)c.ncols * (double)ssc * (double)es < 4.0e9, CRG_ERR_NOT_SUPPORTED,
+              "source fields span 4 GB or more");
+  float* carry = noalloc_scratch(dev);
+  const float* w = normalize ? c.wn32 : c.val32;
+  if (dtype == CRG_F32)
+    noalloc_launch<float>(c, w, (const float*)src, ssc, (float*)dst, dsc, nf, carry, st);
+  else
+    noalloc_launch<__nv_bfloat16>(c, w, (const __nv_bfloat16*)src, ssc, (__nv_bfloat16*)dst, dsc, nf, carry, st);
 }
 
 }  // namespace crg

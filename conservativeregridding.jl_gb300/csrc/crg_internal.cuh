@@ -116,6 +116,8 @@ void free_regridder(crg_regridder* r);
 void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, const void* src, int64_t ssc,
                 int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int normalize, cudaStream_t st);
 bool is_device_pointer(const void* p);
+void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
+                        void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
 void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st);
 void build_merge_path(DevCsr& c, cudaStream_t st);
 void free_tiles(DevTiles& t);

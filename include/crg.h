@@ -138,6 +138,32 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
                              void* gsrc, int64_t gsrc_stride_cell, int64_t gsrc_stride_field,
                              int64_t nfields, int32_t normalize, void* stream);
 
+/* Scratch held by crg_apply_noalloc, in bytes (per GPU that loads the library). */
+#define CRG_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* crg_apply without any device allocation.  It has no counterpart in the
+ * reference; it exists for callers that cannot call cudaMalloc: an
+ * application whose memory pool owns the whole device (a Julia CUDA.jl or
+ * PyTorch caching allocator sized to the GPU, a model that pre-allocates
+ * everything at start-up and forbids allocation while it runs).  Same
+ * arguments as crg_apply, restricted to the batched cell-major path: device
+ * pointers only, dtype CRG_F32 or CRG_BF16, src_stride_field = dst_stride_field
+ * = 1, nfields and both cell strides multiples of 4, 16-byte aligned (FP32) /
+ * 8-byte aligned (BF16) base pointers.  The partial sums of rows that span
+ * several work blocks go to a scratch array the library declares statically
+ * (CRG_NOALLOC_SCRATCH_BYTES per GPU, kept until the process exits), which
+ * limits the regridder to at most 4,194,304 nonzeros; larger ones are refused
+ * with CRG_ERR_NOT_SUPPORTED.  The first call on a device looks up that
+ * array's device address (cudaGetSymbolAddress), so make that first call
+ * before any stream capture.  The scratch is shared by every call on the
+ * device and keeps the previous call's contents (each call writes every slot
+ * it reads before reading it), so calls that may overlap on the GPU -- on
+ * different streams without ordering -- race on it. */
+crg_status crg_apply_noalloc(const crg_regridder* r, int32_t transpose, int32_t dtype,
+                             const void* src, int64_t src_stride_cell, int64_t src_stride_field,
+                             void* dst, int64_t dst_stride_cell, int64_t dst_stride_field,
+                             int64_t nfields, int32_t normalize, void* stream);
+
 /* Copy A out as CSC (rows = dst cells, columns = src cells), i.e. the
  * reference's R.intersections::SparseMatrixCSC (src/regridder/regridder.jl:25-36)
  * with rows ascending inside each column.  index_base 1 gives Julia's 1-based
