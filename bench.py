@@ -43,11 +43,11 @@ WORKLOAD = "healpix256_nested <-> lonlat_0.25deg, 128 fp32 fields, R then transp
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=1000)
+    p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--fields", type=int, default=128)
-    p.add_argument("--layout", default="field_major", choices=["field_major", "cell_major"])
+    p.add_argument("--layout", default="cell_major", choices=["field_major", "cell_major"])
     p.add_argument("--nside", type=int, default=256)
     p.add_argument("--dlon", type=float, default=0.25)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -179,7 +179,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
         return self
@@ -225,14 +225,16 @@ def run_ours(a, rank, world):
     stream = torch.cuda.current_stream(dev)
     hp, ll = grids_c5(a.nside, a.dlon)
 
-    # --- build: warm once, then time (host grid arrays -> device CSR/CSC)
+    # --- build: warm once, then time (host grid arrays -> device CSR/CSC + apply layouts)
     R = Regridder(hp, ll, normalize=True)
     builds = []
-    for _ in range(3):
+    for i in range(3):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        torch.cuda.nvtx.range_push(f"build{i}")  # NVTX ranges select launches for ncu's launch list
         Rb = Regridder(hp, ll, normalize=True)
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
         builds.append(time.perf_counter() - t0)
         info = Rb.info
         del Rb
@@ -241,49 +243,58 @@ def run_ours(a, rank, world):
     T = R.transpose()
     K = a.fields
 
-    # --- fields
-    src = sh_fields(cell_centres(ll), K, 64, 1, 0.1, dev)  # (K, ns)
-    dsrc = sh_fields(cell_centres(hp), K, 64, 2, 0.1, dev)  # (K, nd) input of the transpose
-    if a.layout == "cell_major":
-        src, dsrc = src.T.contiguous(), dsrc.T.contiguous()
-        dims = 1
-        out_f = torch.empty((nd, K), dtype=torch.float32, device=dev)
-        out_r = torch.empty((ns, K), dtype=torch.float32, device=dev)
-    else:
-        dims = 2
-        out_f = torch.empty((K, nd), dtype=torch.float32, device=dev)
-        out_r = torch.empty((K, ns), dtype=torch.float32, device=dev)
+    # --- fields: (cells, fields) cell-major (dims=1) or (fields, cells) field-major (dims=2)
+    src_fm = sh_fields(cell_centres(ll), K, 64, 1, 0.1, dev)   # (K, ns): input of R
+    dsrc_fm = sh_fields(cell_centres(hp), K, 64, 2, 0.1, dev)  # (K, nd): input of transpose(R)
+
+    def layout(fm_src, fm_dsrc, cell_major):
+        if cell_major:
+            return (fm_src.T.contiguous(), fm_dsrc.T.contiguous(), torch.empty((nd, K), device=dev),
+                    torch.empty((ns, K), device=dev), 1)
+        return fm_src, fm_dsrc, torch.empty((K, nd), device=dev), torch.empty((K, ns), device=dev), 2
+
+    cm = a.layout == "cell_major"
+    src, dsrc, out_f, out_r, dims = layout(src_fm, dsrc_fm, cm)
 
     def step():
         regrid_(out_f, R, src, dims=dims)
         regrid_(out_r, T, dsrc, dims=dims)
 
-    for _ in range(max(a.warmup, 3)):
-        step()
-    # per-kernel events for the roofline (launches are on `stream`)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    kf, kr = [], []
-    for _ in range(5):
-        ev[0].record(stream)
-        regrid_(out_f, R, src, dims=dims)
-        ev[1].record(stream)
-        regrid_(out_r, T, dsrc, dims=dims)
-        ev[2].record(stream)
-        ev[2].synchronize()
-        kf.append(ev[0].elapsed_time(ev[1]))
-        kr.append(ev[1].elapsed_time(ev[2]))
-
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(dev.index) as clk:
+        # untimed warm-up: at least `warmup` steps and at least 1.5 s, so that the
+        # clock sampler (100 ms period) has samples under load before timing starts
+        t_w = time.perf_counter()
+        n_w = 0
+        while n_w < max(a.warmup, 3) or time.perf_counter() - t_w < 1.5:
+            step()
+            n_w += 1
+            if n_w % 50 == 0:
+                torch.cuda.synchronize()
+        # per-direction launch times (each direction is one apply: the merge-path
+        # kernel, its carry fixup and the empty-row fill, back to back on `stream`)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        kf, kr = [], []
+        for _ in range(5):
+            ev[0].record(stream)
+            regrid_(out_f, R, src, dims=dims)
+            ev[1].record(stream)
+            regrid_(out_r, T, dsrc, dims=dims)
+            ev[2].record(stream)
+            ev[2].synchronize()
+            kf.append(ev[0].elapsed_time(ev[1]))
+            kr.append(ev[1].elapsed_time(ev[2]))
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push("timed_steps")
         start.record(stream)
         for _ in range(a.steps):
             step()
         stop.record(stream)
         stop.synchronize()
-    torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
     ms = start.elapsed_time(stop) / a.steps
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -291,8 +302,19 @@ def run_ours(a, rank, world):
         ms = float(t.item())
     bf, br = step_bytes(nnz, nd, ns, K)
     value = world * (bf + br) / (ms * 1e-3) / 1e9
+    # one more timed window of back-to-back launches per direction for the roofline
+    reps = 20
+    ev[0].record(stream)
+    for _ in range(reps):
+        regrid_(out_f, R, src, dims=dims)
+    ev[1].record(stream)
+    for _ in range(reps):
+        regrid_(out_r, T, dsrc, dims=dims)
+    ev[2].record(stream)
+    ev[2].synchronize()
+    kfb, krb = ev[0].elapsed_time(ev[1]) / reps, ev[1].elapsed_time(ev[2]) / reps
 
-    # --- accuracy against the FP64 apply (bit-exact with the oracle, see tests)
+    # --- accuracy against the FP64 apply (the FP64 path is bit-exact with the oracle, see tests)
     src64 = src.double()
     out64 = torch.empty(out_f.shape, dtype=torch.float64, device=dev)
     regrid_(out64, R, src64, dims=dims)
@@ -300,23 +322,62 @@ def run_ours(a, rank, world):
     max_abs = float((f32 - out64).abs().max() / out64.abs().max())
     ad = torch.as_tensor(R.dst_areas, device=dev)
     as_ = torch.as_tensor(R.src_areas, device=dev)
-    fa = (0 if dims == 1 else 1)
-    tot_ref = (out64 * (ad[:, None] if dims == 1 else ad[None, :])).sum(dim=fa)
-    tot = (f32 * (ad[:, None] if dims == 1 else ad[None, :])).sum(dim=fa)
-    tot_src = (src64 * (as_[:, None] if dims == 1 else as_[None, :])).sum(dim=fa)
+    fa = 0 if dims == 1 else 1
+    wshape_d = ad[:, None] if dims == 1 else ad[None, :]
+    wshape_s = as_[:, None] if dims == 1 else as_[None, :]
+    tot_ref = (out64 * wshape_d).sum(dim=fa)
+    tot = (f32 * wshape_d).sum(dim=fa)
+    tot_src = (src64 * wshape_s).sum(dim=fa)
     cons_err = float(((tot - tot_ref).abs() / tot_ref.abs()).max())
     cons_err_src = float(((tot - tot_src).abs() / tot_src.abs()).max())
+    del src64, out64
+
+    # --- bf16 fields (FP32 accumulation) on the same layout
+    sb, db = src.bfloat16(), dsrc.bfloat16()
+    ob_f = torch.empty(out_f.shape, dtype=torch.bfloat16, device=dev)
+    ob_r = torch.empty(out_r.shape, dtype=torch.bfloat16, device=dev)
+    for _ in range(3):
+        regrid_(ob_f, R, sb, dims=dims)
+    ev[0].record(stream)
+    for _ in range(reps):
+        regrid_(ob_f, R, sb, dims=dims)
+        regrid_(ob_r, T, db, dims=dims)
+    ev[1].record(stream)
+    ev[1].synchronize()
+    ms_bf16 = ev[0].elapsed_time(ev[1]) / reps
+    bbf, bbr = step_bytes(nnz, nd, ns, K, elem=2)
+    bf16_err = float((ob_f.double() - out_f.double()).abs().max() / out_f.double().abs().max())
+    del sb, db, ob_f, ob_r
+
+    # --- the other layout, same fields
+    src2, dsrc2, of2, or2, dims2 = layout(src_fm, dsrc_fm, not cm)
+    for _ in range(3):
+        regrid_(of2, R, src2, dims=dims2)
+        regrid_(or2, T, dsrc2, dims=dims2)
+    ev[0].record(stream)
+    for _ in range(reps):
+        regrid_(of2, R, src2, dims=dims2)
+    ev[1].record(stream)
+    for _ in range(reps):
+        regrid_(or2, T, dsrc2, dims=dims2)
+    ev[2].record(stream)
+    ev[2].synchronize()
+    other = {"layout": "field_major" if cm else "cell_major",
+             "ms_forward": round(ev[0].elapsed_time(ev[1]) / reps, 4),
+             "ms_transpose": round(ev[1].elapsed_time(ev[2]) / reps, 4)}
+    other["GB/s"] = round((bf + br) / ((other["ms_forward"] + other["ms_transpose"]) * 1e-3) / 1e9, 1)
+    del src2, dsrc2, of2, or2
 
     # --- plain FP64, one field per launch
-    s1 = src64[0] if dims == 2 else src64[:, 0].contiguous()
+    s1 = src.double()[:, 0].contiguous() if dims == 1 else src.double()[0]
+    r1 = dsrc.double()[:, 0].contiguous() if dims == 1 else dsrc.double()[0]
     d1 = torch.empty(nd, dtype=torch.float64, device=dev)
-    r1 = dsrc.double()[0] if dims == 2 else dsrc.double()[:, 0].contiguous()
     o1 = torch.empty(ns, dtype=torch.float64, device=dev)
     for _ in range(3):
         regrid_(d1, R, s1)
         regrid_(o1, T, r1)
-    start.record(stream)
     n64 = 20
+    start.record(stream)
     for _ in range(n64):
         regrid_(d1, R, s1)
         regrid_(o1, T, r1)
@@ -327,7 +388,7 @@ def run_ours(a, rank, world):
     b64r = nnz * 12 + 4 * (ns + 1) + 8 * (ns + nd) + 8 * ns
     fp64_gbs = (b64f + b64r) / (ms64 * 1e-3) / 1e9
 
-    # --- e2e through the public API with pinned host buffers
+    # --- e2e through the public API with pinned host buffers (copies inside the timed region)
     hs = src.cpu().pin_memory()
     hd = dsrc.cpu().pin_memory()
     ho_f = torch.empty(tuple(out_f.shape), dtype=torch.float32).pin_memory()
@@ -340,7 +401,7 @@ def run_ours(a, rank, world):
     step_host()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    ne = max(3, a.steps // 4)
+    ne = max(3, min(a.steps, 20))
     for _ in range(ne):
         step_host()
     torch.cuda.synchronize()
@@ -348,11 +409,21 @@ def run_ours(a, rank, world):
     h2d = 4 * K * (ns + nd)
     d2h = 4 * K * (nd + ns)
     assert torch.equal(ho_f, out_f.cpu()), "host-buffer apply differs from the device apply"
+    # link ceiling: plain pinned copies of the same bytes
+    gb = torch.empty(hs.shape, device=dev)
+    ev[0].record(stream)
+    gb.copy_(hs, non_blocking=True)
+    ev[1].record(stream)
+    hs.copy_(gb, non_blocking=True)
+    ev[2].record(stream)
+    ev[2].synchronize()
+    link = {"h2d_GBs": round(hs.numel() * 4 / ev[0].elapsed_time(ev[1]) / 1e6, 1),
+            "d2h_GBs": round(hs.numel() * 4 / ev[1].elapsed_time(ev[2]) / 1e6, 1)}
 
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = peaks.get("hbm_gbs", 6800.0)
-    kms = statistics.median(kf + kr)
-    achieved = ((bf + br) / 2) / (kms * 1e-3) / 1e9
+    launch_ms = (kfb + krb) / 2
+    achieved = ((bf + br) / 2) / (launch_ms * 1e-3) / 1e9
     line = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -364,26 +435,33 @@ def run_ours(a, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "fp32 fields, fp32 weights, fp32 accumulate (fp64 build)",
+        "dtype": "fp32",
         "data": "synthetic: degree-64 spherical harmonics + N(0,0.1) noise",
         "config": {"workload": WORKLOAD, "n_dst": nd, "n_src": ns, "nnz": nnz, "fields": K, "layout": a.layout,
-                   "l2": "inputs 0.9 GB per direction > 129 MB L2, no flush", "parallelism": f"replicas x{world}"},
+                   "l2": "inputs 0.9 GB per direction > 129 MB L2, no flush", "parallelism": f"replicas x{world}",
+                   "weights": "fp32, FP64-built", "accumulate": "fp32"},
         "fields_per_s": round(world * 2 * K / (ms * 1e-3), 1),
         "build": {"ms": round(build_s * 1e3, 3), "pairs_per_s": round(nnz / build_s, 1),
                   "candidates": info["n_candidates"], "search_ms": round(info["t_search_ms"], 3),
                   "clip_ms": round(info["t_clip_ms"], 3), "assemble_ms": round(info["t_assemble_ms"], 3)},
         "fp64_one_field_per_launch": {"ms_per_field_both_directions": round(ms64, 4), "GB/s": round(fp64_gbs, 2),
                                       "fields_per_s": round(2 / (ms64 * 1e-3), 1)},
+        "bf16": {"ms_per_step": round(ms_bf16, 4), "GB/s": round((bbf + bbr) / (ms_bf16 * 1e-3) / 1e9, 1),
+                 "fields_per_s": round(2 * K / (ms_bf16 * 1e-3), 1), "max_abs_err_vs_fp32_rel_to_max": bf16_err},
+        "other_layout": other,
         "accuracy_vs_fp64": {"max_abs_err_rel_to_max": max_abs, "mean_conservation_rel_err": cons_err,
                              "mean_conservation_rel_err_vs_src_total": cons_err_src},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "k_spmm_tile" if a.layout == "field_major" else "k_spmm_rows",
-                     "launch_ms": {"forward": round(statistics.median(kf), 4), "transpose": round(statistics.median(kr), 4)},
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)"},
+                     "kernel": "k_cm_nnz (+ k_cm_fixup, k_zero_empty_cm in the same timed launch group)"
+                     if a.layout == "cell_major" else "k_fm_rows",
+                     "launch_ms": {"forward": round(kfb, 4), "transpose": round(krb, 4)},
+                     "algorithmic_bytes_per_launch": {"forward": bf, "transpose": br},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "e2e": {"value": round(world * (bf + br) / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
-                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 2 * a.steps,
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "link_probe": link},
+        "gpu_launches": 6 * a.steps if a.layout == "cell_major" else 2 * a.steps,
         "clocks": clk.summary(),
     }
     if rank == 0 and not a.no_cpu:
