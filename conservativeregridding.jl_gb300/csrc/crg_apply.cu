@@ -660,12 +660,12 @@ template <> __device__ __forceinline__ float4 ldoff4<__nv_bfloat16>(const char* 
   return ld4<__nv_bfloat16>(reinterpret_cast<const __nv_bfloat16*>(base + off));
 }
 
-template <class T>
-__global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                                                   const int32_t* __restrict__ erow, const float* __restrict__ w,
-                                                   int64_t nnz, int64_t ntasks, const T* __restrict__ x, int64_t xs,
-                                                   T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf,
-                                                   float* __restrict__ carry) {
+template <class T, int B = 8>
+__global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
+    k_cm_nnz(const int4* __restrict__ tasks, const int32_t* __restrict__ idx, const int32_t* __restrict__ erow,
+             const float* __restrict__ w, int64_t ntasks, const T* __restrict__ x, int64_t xs, T* __restrict__ y,
+             int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
+  static_assert(B == 8 || B == 16, "gathers in flight per warp");
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -676,46 +676,61 @@ __global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ p
   const char* xb = reinterpret_cast<const char*>(x + fo);
   const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(T));
   for (int64_t task = gw; task < ntasks; task += nw) {
-    const int64_t e0 = task * kTaskNnz;
-    const int64_t e1 = min(nnz, e0 + kTaskNnz);
-    const int32_t first = __ldg(erow + e0), last = __ldg(erow + e1 - 1);
-    const bool first_split = __ldg(ptr + first) < e0;
-    const bool last_split = __ldg(ptr + last + 1) > e1;
+    const int4 tr = __ldg(tasks + task);
+    const int32_t e0 = tr.x, e1 = tr.y;
+    if (e0 >= e1) continue;  // warp-uniform
+    const int32_t first = tr.z & 0x7fffffff;
+    // rows written to the carry slots: the first row if it began in an earlier
+    // task, the last row if it continues into a later one (-1: no such row)
+    const int32_t carry_first = tr.z < 0 ? first : -1;
+    const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
     int32_t cur = first;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto flush = [&](int32_t row) {
       if (!on) return;
-      if (row == first && first_split) {
+      if (row == carry_first) {
         *reinterpret_cast<float4*>(carry + (task * 2 + 0) * 128 + lane * 4) = acc;
-      } else if (row == last && last_split) {
+      } else if (row == carry_last) {
         *reinterpret_cast<float4*>(carry + (task * 2 + 1) * 128 + lane * 4) = acc;
       } else {
         st4<T>(y + (int64_t)row * ys + fo, acc);
       }
     };
-    int32_t prev_last = first;  // row of the entry before the current chunk
-    for (int64_t c0 = e0; c0 < e1; c0 += 32) {
-      const int64_t e = c0 + lane;
+    // lane's entry of the chunk at c0: row, byte offset of its source cell, weight
+    auto load = [&](int32_t c0, int32_t& r, uint32_t& o, float& wt) {
+      const int32_t e = c0 + lane;
       const bool valid = e < e1;
-      const int32_t myr = valid ? __ldg(erow + e) : 0x7fffffff;
-      const uint32_t myo = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
-      const float myw = valid ? __ldg(w + e) : 0.f;
+      r = valid ? __ldg(erow + e) : 0x7fffffff;
+      o = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
+      wt = valid ? __ldg(w + e) : 0.f;
+    };
+    int32_t myr;
+    uint32_t myo;
+    float myw;
+    load(e0, myr, myo, myw);
+    int32_t prev_last = first;  // row of the entry before the current chunk
+    for (int32_t c0 = e0; c0 < e1; c0 += 32) {
+      // the next chunk's entries load while this one is gathered
+      int32_t nr = 0x7fffffff;
+      uint32_t no = 0u;
+      float nwt = 0.f;
+      if (c0 + 32 < e1) load(c0 + 32, nr, no, nwt);
       int32_t before = __shfl_up_sync(0xffffffffu, myr, 1);
       if (lane == 0) before = prev_last;
-      const unsigned newrow = __ballot_sync(0xffffffffu, valid && myr != before);  // entry starts a new row
+      const unsigned newrow = __ballot_sync(0xffffffffu, myr != 0x7fffffff && myr != before);  // starts a row
       prev_last = __shfl_sync(0xffffffffu, myr, 31);
-      const int n = (int)(e1 - c0 < 32 ? e1 - c0 : 32);
-      for (int k = 0; k < n; k += 8) {
-        float4 v[8];
-        float ww[8];
+      const int n = e1 - c0 < 32 ? e1 - c0 : 32;
+      for (int k = 0; k < n; k += B) {
+        float4 v[B];
+        float ww[B];
 #pragma unroll
-        for (int h = 0; h < 8; ++h) {
-          const uint32_t o = __shfl_sync(0xffffffffu, myo, k + h);
-          ww[h] = __shfl_sync(0xffffffffu, myw, k + h);
+        for (int h = 0; h < B; ++h) {
+          const uint32_t o = __shfl_sync(0xffffffffu, myo, (k + h) & 31);
+          ww[h] = __shfl_sync(0xffffffffu, myw, (k + h) & 31);
           v[h] = ldoff4<T>(xb, o);  // past-the-end entries load cell 0 with weight 0
         }
 #pragma unroll
-        for (int h = 0; h < 8; ++h) {
+        for (int h = 0; h < B; ++h) {
           if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
           if ((newrow >> (k + h)) & 1u) {
             flush(cur);
@@ -728,6 +743,9 @@ __global__ void __launch_bounds__(256, 3) k_cm_nnz(const int32_t* __restrict__ p
           acc.w = fmaf(ww[h], v[h].w, acc.w);
         }
       }
+      myr = nr;
+      myo = no;
+      myw = nwt;
     }
     flush(cur);
   }
@@ -751,24 +769,19 @@ __global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, co
   st4<T>(y + (int64_t)row * ys + f, s);
 }
 
+// The merge-path kernel over all 128-field passes, the fixup of rows cut
+// between tasks, and zeros for rows without entries.  `carry` holds
+// ntasks * 2 * 128 floats when the layout has rows cut between tasks.
+template <class T>
+void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                   float* carry, cudaStream_t st);
+
 template <class T>
 void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
                    cudaStream_t st) {
-  const int64_t ntasks = (c.nnz + kTaskNnz - 1) / kTaskNnz;
   float* carry = nullptr;
-  if (ntasks) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * ntasks * 2 * 128, st));
-  const int64_t warps = std::min<int64_t>(ntasks, (int64_t)num_sms() * 24);
-  for (int64_t f0 = 0; f0 < nf; f0 += 128) {
-    if (ntasks) {
-      k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.ptr, c.idx, c.erow, w, c.nnz, ntasks, x, xs, y, ys, f0,
-                                                         nf, carry);
-      CRG_CHECK_CUDA(cudaGetLastError());
-    }
-    if (c.nsplit) {
-      k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
-      CRG_CHECK_CUDA(cudaGetLastError());
-    }
-  }
+  if (c.nsplit) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * c.ntasks * 2 * 128, st));
+  cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st);
   if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
 }
 
@@ -780,14 +793,46 @@ __global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* _
   for (int64_t f = 0; f < nf; ++f) st1<T>(y + r * ys + f, 0.f);
 }
 
+template <class T>
+void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                   float* carry, cudaStream_t st) {
+  // gathers in flight per warp: CRG_NNZ_DEPTH=16 selects 16 (two blocks of 256 per SM) for tuning
+  static const int depth = [] {
+    const char* e = getenv("CRG_NNZ_DEPTH");
+    return (e && atoi(e) == 16) ? 16 : 8;
+  }();
+  const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * (depth == 16 ? 16 : 24));
+  for (int64_t f0 = 0; f0 < nf; f0 += 128) {
+    if (c.ntasks) {
+      if (depth == 16)
+        k_cm_nnz<T, 16><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.idx, c.erow, w, c.ntasks, x, xs, y, ys, f0,
+                                                               nf, carry);
+      else
+        k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.idx, c.erow, w, c.ntasks, x, xs, y, ys, f0, nf,
+                                                           carry);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (c.nsplit) {
+      k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+  }
+  if (c.nempty) {
+    k_zero_empty_cm<T><<<nblk(c.nrows, 256), 256, 0, st>>>(c.ptr, c.nrows, y, ys, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+}
+
 // Kernel choice for FP32/BF16 fields.  CRG_SPMM_PATH selects an alternative
-// for tuning and profiling: "tiled" (shared-memory staged tiles) or "legacy"
-// (first-generation row kernels); unset = the register-blocked row kernels.
-enum class SpmmPath { kAuto, kRows, kTiled, kLegacy };
+// for tuning and profiling: "nnz" (merge-path with register gathers),
+// "rows" (register-blocked row kernels), "tiled" (shared-memory staged
+// tiles) or "legacy" (first-generation row kernels); unset = automatic.
+enum class SpmmPath { kAuto, kRows, kTiled, kLegacy, kNnz };
 
 inline SpmmPath spmm_path() {
   static const SpmmPath p = [] {
     const char* e = getenv("CRG_SPMM_PATH");
+    if (e && strcmp(e, "nnz") == 0) return SpmmPath::kNnz;
     if (e && strcmp(e, "tiled") == 0) return SpmmPath::kTiled;
     if (e && strcmp(e, "legacy") == 0) return SpmmPath::kLegacy;
     if (e && strcmp(e, "rows") == 0) return SpmmPath::kRows;
@@ -853,11 +898,9 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
   }
   // the merge-path kernel addresses source cells with 32-bit byte offsets
   const bool span32 = (double)c.ncols * (double)xsc * es < 4.0e9;
-  if (path == SpmmPath::kAuto && cell_major && vec4 && nf >= 32 && span32) {
+  if ((path == SpmmPath::kAuto || path == SpmmPath::kNnz) && cell_major && vec4 && nf >= 32 && span32) {
     // merge-path over entries; rows with no entries are zeroed separately
     launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st);
-    k_zero_empty_cm<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, y, ysc, nf);
-    CRG_CHECK_CUDA(cudaGetLastError());
     return;
   }
   if (path == SpmmPath::kRows || path == SpmmPath::kAuto) {
@@ -1019,28 +1062,6 @@ float* noalloc_scratch(int dev) {
   return g_noalloc_ptr[dev];
 }
 
-template <class T>
-void noalloc_launch(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                    float* carry, cudaStream_t st) {
-  const int64_t ntasks = (c.nnz + kTaskNnz - 1) / kTaskNnz;
-  const int64_t warps = std::min<int64_t>(ntasks, (int64_t)num_sms() * 24);
-  for (int64_t f0 = 0; f0 < nf; f0 += 128) {
-    if (ntasks) {
-      k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.ptr, c.idx, c.erow, w, c.nnz, ntasks, x, xs, y, ys, f0,
-                                                         nf, carry);
-      CRG_CHECK_CUDA(cudaGetLastError());
-    }
-    if (c.nsplit) {
-      k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
-      CRG_CHECK_CUDA(cudaGetLastError());
-    }
-  }
-  if (c.nrows) {
-    k_zero_empty_cm<T><<<nblk(c.nrows, 256), 256, 0, st>>>(c.ptr, c.nrows, y, ys, nf);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-}
-
 }  // namespace
 
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
@@ -1065,8 +1086,7 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
               r->device, dev);
   const bool t = transpose != 0;
   const DevCsr& c = t ? r->rev : r->fwd;
-  const int64_t ntasks = (c.nnz + kTaskNnz - 1) / kTaskNnz;
-  const size_t need = (size_t)ntasks * 2 * 128 * sizeof(float);
+  const size_t need = (size_t)c.ntasks * 2 * 128 * sizeof(float);
   CRG_REQUIRE(need <= CRG_NOALLOC_SCRATCH_BYTES, CRG_ERR_NOT_SUPPORTED,
               "this regridder has %lld nonzeros and needs %zu bytes of scratch; the static scratch of "
               "crg_apply_noalloc holds %u bytes (at most %lld nonzeros)",
@@ -1077,9 +1097,9 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
   float* carry = noalloc_scratch(dev);
   const float* w = normalize ? c.wn32 : c.val32;
   if (dtype == CRG_F32)
-    noalloc_launch<float>(c, w, (const float*)src, ssc, (float*)dst, dsc, nf, carry, st);
+    cm_nnz_passes<float>(c, w, (const float*)src, ssc, (float*)dst, dsc, nf, carry, st);
   else
-    noalloc_launch<__nv_bfloat16>(c, w, (const __nv_bfloat16*)src, ssc, (__nv_bfloat16*)dst, dsc, nf, carry, st);
+    cm_nnz_passes<__nv_bfloat16>(c, w, (const __nv_bfloat16*)src, ssc, (__nv_bfloat16*)dst, dsc, nf, carry, st);
 }
 
 }  // namespace crg

@@ -63,11 +63,12 @@ struct DBuf {
   ~DBuf() { release(); }
 };
 
+// Four spare elements: a 16-byte bulk copy of an array's last entries stays
+// inside the allocation.
 template <class T>
 T* persistent_alloc(size_t n) {
   T* p = nullptr;
-  if (n == 0) n = 1;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&p, n * sizeof(T)));
+  CRG_CHECK_CUDA(cudaMalloc((void**)&p, (n + 4) * sizeof(T)));
   return p;
 }
 
@@ -854,6 +855,7 @@ void free_csr(DevCsr& c) {
   free_tiles(c.tiles);
   cudaFree(c.erow);
   cudaFree(c.split);
+  cudaFree(c.tasks);
   cudaFree(c.ptr); cudaFree(c.idx); cudaFree(c.val); cudaFree(c.val32); cudaFree(c.wn32); cudaFree(c.adj32);
   c = DevCsr{};
 }

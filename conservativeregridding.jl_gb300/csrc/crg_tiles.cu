@@ -17,6 +17,9 @@
 #include <algorithm>
 #include <vector>
 
+#include <stdlib.h>
+#include <string.h>
+
 #include "crg_internal.cuh"
 #include "crg_scan.cuh"
 
@@ -341,58 +344,115 @@ namespace crg {
 
 namespace {
 
-__global__ void k_expand_rows(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ erow) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) erow[k] = (int32_t)r;
-}
-
-__global__ void k_split_flags(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ flag) {
+__global__ void k_expand_rows(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ erow,
+                              int* __restrict__ nempty) {
   int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const int32_t a = ptr[r], b = ptr[r + 1];
-  flag[r] = (b > a && (a / kTaskNnz) != ((b - 1) / kTaskNnz)) ? 1 : 0;
+  for (int32_t k = a; k < b; ++k) erow[k] = (int32_t)r;
+  if (a == b) atomicAdd(nempty, 1);
 }
 
-__global__ void k_split_fill(const int32_t* __restrict__ ptr, int64_t n, const int32_t* __restrict__ pos,
-                             int32_t* __restrict__ split) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  const int32_t a = ptr[r], b = ptr[r + 1];
-  if (b > a && (a / kTaskNnz) != ((b - 1) / kTaskNnz)) {
-    int32_t* s = split + 3 * (int64_t)pos[r];
-    s[0] = (int32_t)r;
-    s[1] = a / kTaskNnz;
-    s[2] = (b - 1) / kTaskNnz;
+// Start of task k: entry k * kTaskNnz moved up to the next row start, unless
+// it falls inside a row longer than kLongRow (that row is then cut and its
+// pieces summed by k_cm_fixup).  bound[ntasks] = nnz.
+__global__ void k_task_bounds(const int32_t* __restrict__ ptr, const int32_t* __restrict__ erow, int64_t nnz,
+                              int64_t ntasks, int long_row, int32_t* __restrict__ bound) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > ntasks) return;
+  if (k == ntasks) {
+    bound[k] = (int32_t)nnz;
+    return;
   }
+  const int64_t e = k * kTaskNnz;
+  const int32_t r = erow[e], a = ptr[r], b = ptr[r + 1];
+  bound[k] = (a == e || b - a > long_row) ? (int32_t)e : b;
+}
+
+// last task whose start is <= e
+__device__ int64_t task_of_entry(const int32_t* __restrict__ bound, int64_t ntasks, int64_t e) {
+  int64_t lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (bound[mid] <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Task records, and a flag on every task that ends a row begun in an earlier task.
+__global__ void k_task_records(const int32_t* __restrict__ ptr, const int32_t* __restrict__ erow,
+                               const int32_t* __restrict__ bound, int64_t ntasks, int4* __restrict__ tasks,
+                               int32_t* __restrict__ ends) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntasks) return;
+  const int32_t e0 = bound[t], e1 = bound[t + 1];
+  if (e0 >= e1) {  // only the last task can be empty
+    tasks[t] = make_int4(e0, e0, 0, 0);
+    ends[t] = 0;
+    return;
+  }
+  const int32_t first = erow[e0], last = erow[e1 - 1];
+  const uint32_t fs = ptr[first] < e0 ? 1u : 0u, ls = ptr[last + 1] > e1 ? 1u : 0u;
+  tasks[t] = make_int4(e0, e1, (int32_t)((uint32_t)first | (fs << 31)), (int32_t)((uint32_t)last | (ls << 31)));
+  ends[t] = (fs && !(first == last && ls)) ? 1 : 0;
+}
+
+__global__ void k_split_fill(const int32_t* __restrict__ ptr, const int32_t* __restrict__ bound, int64_t ntasks,
+                             const int4* __restrict__ tasks, const int32_t* __restrict__ pos,
+                             int32_t* __restrict__ split) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntasks || pos[t + 1] == pos[t]) return;
+  const int32_t row = tasks[t].z & 0x7fffffff;
+  int32_t* s = split + 3 * (int64_t)pos[t];
+  s[0] = row;
+  s[1] = (int32_t)task_of_entry(bound, ntasks, ptr[row]);
+  s[2] = (int32_t)t;
 }
 
 }  // namespace
 
 void build_merge_path(DevCsr& c, cudaStream_t st) {
   const int64_t n = c.nrows, nnz = c.nnz;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&c.erow, sizeof(int32_t) * (nnz ? nnz : 1)));
-  if (n == 0) {
-    CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3));
-    return;
-  }
-  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow);
+  CRG_CHECK_CUDA(cudaMalloc((void**)&c.erow, sizeof(int32_t) * (nnz + 4)));  // 4 spare: whole 16-byte loads
+  c.ntasks = (nnz + kTaskNnz - 1) / kTaskNnz;
+  CRG_CHECK_CUDA(cudaMalloc((void**)&c.tasks, sizeof(int4) * (c.ntasks ? c.ntasks : 1)));
+  CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3));
+  c.nsplit = 0;
+  c.nempty = n;
+  if (n == 0 || nnz == 0) return;
+  int32_t* work = nullptr;  // [1] empty rows | [ntasks + 1] bounds | [ntasks + 1] split positions
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&work, sizeof(int32_t) * (2 * c.ntasks + 3), st));
+  int32_t* nempty = work;
+  int32_t* bound = work + 1;
+  int32_t* pos = bound + c.ntasks + 1;
+  CRG_CHECK_CUDA(cudaMemsetAsync(nempty, 0, sizeof(int32_t), st));
+  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow, nempty);
   CRG_CHECK_CUDA(cudaGetLastError());
-  int32_t* pos = nullptr;
-  CRG_CHECK_CUDA(cudaMallocAsync((void**)&pos, sizeof(int32_t) * (n + 1), st));
-  k_split_flags<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, pos);
+  // CRG_TASK_CUT=fixed cuts every task at exactly kTaskNnz entries (rows spanning tasks everywhere), for tuning
+  static const int long_row = [] {
+    const char* e = getenv("CRG_TASK_CUT");
+    return (e && strcmp(e, "fixed") == 0) ? -1 : kLongRow;
+  }();
+  k_task_bounds<<<nblk(c.ntasks + 1, 256), 256, 0, st>>>(c.ptr, c.erow, nnz, c.ntasks, long_row, bound);
   CRG_CHECK_CUDA(cudaGetLastError());
-  exclusive_scan_i32(pos, pos, n, st);
-  int32_t ns = 0;
-  CRG_CHECK_CUDA(cudaMemcpyAsync(&ns, pos + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  k_task_records<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, c.erow, bound, c.ntasks, c.tasks, pos);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  exclusive_scan_i32(pos, pos, c.ntasks, st);
+  int32_t counts[2] = {0, 0};
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&counts[0], pos + c.ntasks, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&counts[1], nempty, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-  c.nsplit = ns;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3 * (ns ? ns : 1)));
-  if (ns) {
-    k_split_fill<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, pos, c.split);
+  c.nsplit = counts[0];
+  c.nempty = counts[1];
+  if (c.nsplit) {
+    CRG_CHECK_CUDA(cudaFree(c.split));
+    c.split = nullptr;
+    CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3 * c.nsplit));
+    k_split_fill<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, bound, c.ntasks, c.tasks, pos, c.split);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
-  CRG_CHECK_CUDA(cudaFreeAsync(pos, st));
+  CRG_CHECK_CUDA(cudaFreeAsync(work, st));
 }
 
 }  // namespace crg

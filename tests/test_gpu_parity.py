@@ -280,6 +280,9 @@ TILED_CASES = {
     # coarse destination over a fine source: wide rows go to the direct kernels
     "lonlat20_from_lonlat0.5": lambda: (grids.lonlat_regular(20.0, 20.0), grids.lonlat_regular(0.5, 0.5)),
     "cs6_from_healpix64": lambda: (grids.cubed_sphere(6), grids.healpix_grid(64)),
+    # global destination over a regional source: destination rows without entries
+    "lonlat5_from_regional1": lambda: (grids.lonlat_regular(5.0, 5.0),
+                                       grids.lonlat_grid(np.arange(10.5, 51.0, 1.0), np.arange(-20.5, 31.0, 1.0))),
 }
 
 
@@ -305,14 +308,15 @@ def test_apply_tiled_paths(cuda, case, K, layout, dtype):
         S = rng.standard_normal((K, nin))
         Sq = torch.from_numpy(S).to(tdt)  # the values the GPU sees
         ref = O.apply(Sq.double().numpy(), transpose=transpose)
+        # NaN-filled outputs: every row, with entries or without, must be written
         if layout == "field_major":
             x = Sq.cuda()
-            y = torch.zeros((K, nout), dtype=tdt, device="cuda")
+            y = torch.full((K, nout), float("nan"), dtype=tdt, device="cuda")
             regrid_(y, RR, x, dims=2)
             got = y.double().cpu().numpy()
         else:
             x = Sq.T.contiguous().cuda()
-            y = torch.zeros((nout, K), dtype=tdt, device="cuda")
+            y = torch.full((nout, K), float("nan"), dtype=tdt, device="cuda")
             regrid_(y, RR, x, dims=1)
             got = y.double().cpu().numpy().T
         err = np.max(np.abs(got - ref)) / np.max(np.abs(ref))
