@@ -66,6 +66,10 @@ class crg_info(C.Structure):
         ("tiles", C.c_int64 * 2),
         ("tile_columns", C.c_int64 * 2),
         ("direct_rows", C.c_int64 * 2),
+        ("merge_tasks", C.c_int64 * 2),
+        ("cut_rows", C.c_int64 * 2),
+        ("carry_slots", C.c_int64 * 2),
+        ("empty_rows", C.c_int64 * 2),
     ]
 
 

@@ -21,6 +21,9 @@ from . import _lib
 from ._lib import ArgumentError, DimensionMismatch, check
 from .grids import PLANAR, SPHERICAL, Grid, polygon_grid
 
+# crg_info fields holding [forward, transpose] pairs
+_PAIR_FIELDS = ("tiles", "tile_columns", "direct_rows", "merge_tasks", "cut_rows", "carry_slots", "empty_rows")
+
 
 # ----------------------------------------------------------------- grid -> descriptor
 
@@ -112,7 +115,7 @@ class Regridder:
         self._transposed = False
         info = _lib.crg_info()
         check(lib.crg_regridder_info(C.c_void_p(h.value), C.byref(info)))
-        self.info = {k: (list(getattr(info, k)) if k in ("tiles", "tile_columns", "direct_rows") else getattr(info, k))
+        self.info = {k: (list(getattr(info, k)) if k in _PAIR_FIELDS else getattr(info, k))
                      for k, _ in _lib.crg_info._fields_ if k != "pad"}
         nd, ns = info.n_dst, info.n_src
         self.dst_areas = np.empty(nd)

@@ -645,7 +645,7 @@ void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int
 
 // ------------------------------------------------------------------ merge-path (cell-major)
 
-// Each warp walks tasks of kTaskNnz consecutive entries.  Lanes load 32
+// Each warp walks tasks of about kTaskNnz consecutive entries.  Lanes load 32
 // (column, weight, row) entries with one coalesced load each, then every entry
 // is broadcast and the whole warp gathers that cell's 128 fields (4 per lane,
 // 16-byte loads); 8 gathers are issued before they are consumed.  Rows are
@@ -662,9 +662,9 @@ template <> __device__ __forceinline__ float4 ldoff4<__nv_bfloat16>(const char* 
 
 template <class T, int B = 8>
 __global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
-    k_cm_nnz(const int4* __restrict__ tasks, const int32_t* __restrict__ idx, const int32_t* __restrict__ erow,
-             const float* __restrict__ w, int64_t ntasks, const T* __restrict__ x, int64_t xs, T* __restrict__ y,
-             int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
+    k_cm_nnz(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
+             const int32_t* __restrict__ erow, const float* __restrict__ w, int64_t ntasks, const T* __restrict__ x,
+             int64_t xs, T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
   static_assert(B == 8 || B == 16, "gathers in flight per warp");
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -684,14 +684,15 @@ __global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
     // task, the last row if it continues into a later one (-1: no such row)
     const int32_t carry_first = tr.z < 0 ? first : -1;
     const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
+    const int2 slot = (tr.z | tr.w) < 0 ? __ldg(tslot + task) : make_int2(-1, -1);
     int32_t cur = first;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     auto flush = [&](int32_t row) {
       if (!on) return;
       if (row == carry_first) {
-        *reinterpret_cast<float4*>(carry + (task * 2 + 0) * 128 + lane * 4) = acc;
+        *reinterpret_cast<float4*>(carry + (int64_t)slot.x * 128 + lane * 4) = acc;
       } else if (row == carry_last) {
-        *reinterpret_cast<float4*>(carry + (task * 2 + 1) * 128 + lane * 4) = acc;
+        *reinterpret_cast<float4*>(carry + (int64_t)slot.y * 128 + lane * 4) = acc;
       } else {
         st4<T>(y + (int64_t)row * ys + fo, acc);
       }
@@ -751,19 +752,19 @@ __global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
   }
 }
 
-// Rows spanning tasks: sum the carries in task order (deterministic).
+// Rows cut between tasks: sum their pieces in task order (deterministic).
 template <class T>
 __global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, const float* __restrict__ carry,
                            T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf) {
   const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (wi >= nsplit) return;
-  const int32_t row = split[3 * wi], t0 = split[3 * wi + 1], t1 = split[3 * wi + 2];
+  const int32_t row = split[3 * wi], s0 = split[3 * wi + 1], pieces = split[3 * wi + 2];
   const int64_t f = f0 + (int64_t)lane * 4;
   if (f >= nf) return;
-  float4 s = *reinterpret_cast<const float4*>(carry + ((int64_t)t0 * 2 + 1) * 128 + lane * 4);
-  for (int32_t t = t0 + 1; t <= t1; ++t) {
-    const float4 c = *reinterpret_cast<const float4*>(carry + ((int64_t)t * 2 + 0) * 128 + lane * 4);
+  float4 s = *reinterpret_cast<const float4*>(carry + (int64_t)s0 * 128 + lane * 4);
+  for (int32_t k = 1; k < pieces; ++k) {
+    const float4 c = *reinterpret_cast<const float4*>(carry + (int64_t)(s0 + k) * 128 + lane * 4);
     s.x += c.x; s.y += c.y; s.z += c.z; s.w += c.w;
   }
   st4<T>(y + (int64_t)row * ys + f, s);
@@ -771,7 +772,7 @@ __global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, co
 
 // The merge-path kernel over all 128-field passes, the fixup of rows cut
 // between tasks, and zeros for rows without entries.  `carry` holds
-// ntasks * 2 * 128 floats when the layout has rows cut between tasks.
+// nslots * 128 floats when the layout has rows cut between tasks.
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
                    float* carry, cudaStream_t st);
@@ -780,7 +781,7 @@ template <class T>
 void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
                    cudaStream_t st) {
   float* carry = nullptr;
-  if (c.nsplit) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * c.ntasks * 2 * 128, st));
+  if (c.nslots) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * c.nslots * 128, st));
   cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st);
   if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
 }
@@ -805,11 +806,11 @@ void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y
   for (int64_t f0 = 0; f0 < nf; f0 += 128) {
     if (c.ntasks) {
       if (depth == 16)
-        k_cm_nnz<T, 16><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.idx, c.erow, w, c.ntasks, x, xs, y, ys, f0,
-                                                               nf, carry);
+        k_cm_nnz<T, 16><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.erow, w, c.ntasks, x, xs,
+                                                               y, ys, f0, nf, carry);
       else
-        k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.idx, c.erow, w, c.ntasks, x, xs, y, ys, f0, nf,
-                                                           carry);
+        k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.erow, w, c.ntasks, x, xs, y,
+                                                           ys, f0, nf, carry);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (c.nsplit) {
@@ -1035,7 +1036,7 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
 // crg_apply_noalloc runs the merge-path kernels above with their carry buffer
 // in a statically declared device array instead of memory allocated per call,
 // for callers that must not allocate device memory.  Each carry slot holds
-// 128 FP32 partial sums; a call needs 2 slots per 256-entry task.
+// 128 FP32 partial sums of one piece of a row cut between tasks.
 
 static __device__ __align__(256) float g_noalloc_carry[CRG_NOALLOC_SCRATCH_BYTES / sizeof(float)];
 
@@ -1086,12 +1087,12 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
               r->device, dev);
   const bool t = transpose != 0;
   const DevCsr& c = t ? r->rev : r->fwd;
-  const size_t need = (size_t)c.ntasks * 2 * 128 * sizeof(float);
+  const size_t need = (size_t)c.nslots * 128 * sizeof(float);
   CRG_REQUIRE(need <= CRG_NOALLOC_SCRATCH_BYTES, CRG_ERR_NOT_SUPPORTED,
-              "this regridder has %lld nonzeros and needs %zu bytes of scratch; the static scratch of "
-              "crg_apply_noalloc holds %u bytes (at most %lld nonzeros)",
-              (long long)c.nnz, need, (unsigned)CRG_NOALLOC_SCRATCH_BYTES,
-              (long long)(CRG_NOALLOC_SCRATCH_BYTES / (2 * 128 * sizeof(float))) * kTaskNnz);
+              "this regridder cuts %lld long rows into %lld pieces and needs %zu bytes of scratch; the static "
+              "scratch of crg_apply_noalloc holds %u bytes (%lld pieces)",
+              (long long)c.nsplit, (long long)c.nslots, need, (unsigned)CRG_NOALLOC_SCRATCH_BYTES,
+              (long long)(CRG_NOALLOC_SCRATCH_BYTES / (128 * sizeof(float))));
   CRG_REQUIRE((double)c.ncols * (double)ssc * (double)es < 4.0e9, CRG_ERR_NOT_SUPPORTED,
               "source fields span 4 GB or more");
   float* carry = noalloc_scratch(dev);

@@ -526,24 +526,133 @@ __global__ void k_scatter_pairs(const int2* __restrict__ cand, const double* __r
   rval[q] = a;
 }
 
-// Sort each row segment by column (insertion sort; rows are short).
-__global__ void k_row_sort(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ idx,
-                           double* __restrict__ val) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
-  int32_t lo = ptr[r], hi = ptr[r + 1];
-  for (int32_t i = lo + 1; i < hi; ++i) {
-    int32_t x = idx[i];
-    double v = val[i];
-    int32_t j = i - 1;
-    while (j >= lo && idx[j] > x) {
-      idx[j + 1] = idx[j];
-      val[j + 1] = val[j];
-      --j;
+// Sorting each row segment by column (columns are distinct within a row, so
+// any correct sort gives the same result).  Rows of up to 32 entries: one warp
+// each, a bitonic network across the lanes.  Longer rows: one block each, a
+// bitonic network over the row padded to a power of two, in shared memory up
+// to kRowSortSmem entries and in a global scratch beyond.
+constexpr int kRowSortSmem = 4096;
+constexpr int kRowSortThreads = 256;
+
+__global__ void k_row_sort_warp(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ idx,
+                                double* __restrict__ val) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= nrows) return;  // warp-uniform
+  const int32_t lo = ptr[r], len = ptr[r + 1] - lo;
+  if (len < 2 || len > 32) return;  // warp-uniform
+  int32_t key = lane < len ? idx[lo + lane] : INT32_MAX;
+  double v = lane < len ? val[lo + lane] : 0.0;
+  for (int k = 2; k <= 32; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int32_t pk = __shfl_xor_sync(0xffffffffu, key, j);
+      const double pv = __shfl_xor_sync(0xffffffffu, v, j);
+      const bool up = (lane & k) == 0, lower = (lane & j) == 0;
+      if (lower == up ? pk < key : pk > key) {
+        key = pk;
+        v = pv;
+      }
     }
-    idx[j + 1] = x;
-    val[j + 1] = v;
   }
+  if (lane < len) {
+    idx[lo + lane] = key;
+    val[lo + lane] = v;
+  }
+}
+
+// rows longer than 32 entries, split by whether they fit in shared memory
+__global__ void k_row_classes(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ mid,
+                              int32_t* __restrict__ longr, int32_t* __restrict__ counts) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  const int32_t len = ptr[r + 1] - ptr[r];
+  if (len <= 32) return;
+  if (len <= kRowSortSmem) mid[atomicAdd(&counts[0], 1)] = (int32_t)r;
+  else longr[atomicAdd(&counts[1], 1)] = (int32_t)r;
+}
+
+// bitonic network over n2 (a power of two) keys/values in k[], v[] (shared or global)
+__device__ void bitonic_block(int32_t* k, double* v, int n2) {
+  for (int sz = 2; sz <= n2; sz <<= 1) {
+    for (int j = sz >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int p = i ^ j;
+        if (p > i) {
+          const bool up = (i & sz) == 0;
+          const int32_t a = k[i], b = k[p];
+          if (up ? a > b : a < b) {
+            k[i] = b;
+            k[p] = a;
+            const double t = v[i];
+            v[i] = v[p];
+            v[p] = t;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRowSortThreads) k_row_sort_block(const int32_t* __restrict__ ptr,
+                                                                    const int32_t* __restrict__ rows,
+                                                                    int32_t* __restrict__ idx,
+                                                                    double* __restrict__ val) {
+  __shared__ int32_t sk[kRowSortSmem];
+  __shared__ double sv[kRowSortSmem];
+  const int32_t r = rows[blockIdx.x];
+  const int32_t lo = ptr[r], len = ptr[r + 1] - lo;
+  int n2 = 64;
+  while (n2 < len) n2 <<= 1;
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+    sk[i] = i < len ? idx[lo + i] : INT32_MAX;
+    sv[i] = i < len ? val[lo + i] : 0.0;
+  }
+  __syncthreads();
+  bitonic_block(sk, sv, n2);
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    idx[lo + i] = sk[i];
+    val[lo + i] = sv[i];
+  }
+}
+
+// long rows: each block owns the scratch window [off[b], off[b] + n2) of k/v
+__global__ void __launch_bounds__(1024) k_row_sort_long(const int32_t* __restrict__ ptr,
+                                                        const int32_t* __restrict__ rows,
+                                                        const int64_t* __restrict__ off, int32_t* __restrict__ idx,
+                                                        double* __restrict__ val, int32_t* __restrict__ gk,
+                                                        double* __restrict__ gv) {
+  const int32_t r = rows[blockIdx.x];
+  const int32_t lo = ptr[r], len = ptr[r + 1] - lo;
+  int n2 = kRowSortSmem;
+  while (n2 < len) n2 <<= 1;
+  int32_t* k = gk + off[blockIdx.x];
+  double* v = gv + off[blockIdx.x];
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+    k[i] = i < len ? idx[lo + i] : INT32_MAX;
+    v[i] = i < len ? val[lo + i] : 0.0;
+  }
+  __syncthreads();
+  bitonic_block(k, v, n2);
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    idx[lo + i] = k[i];
+    val[lo + i] = v[i];
+  }
+}
+
+__global__ void k_long_windows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ rows, int64_t n,
+                               int64_t* __restrict__ off) {
+  // sequential prefix over the (few) long rows
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  int64_t o = 0;
+  for (int64_t b = 0; b < n; ++b) {
+    off[b] = o;
+    const int32_t len = ptr[rows[b] + 1] - ptr[rows[b]];
+    int64_t n2 = kRowSortSmem;
+    while (n2 < len) n2 <<= 1;
+    o += n2;
+  }
+  off[n] = o;
 }
 
 __global__ void k_max_val(const double* __restrict__ v, int64_t n, unsigned long long* __restrict__ mx) {
@@ -851,11 +960,43 @@ bool is_device_pointer(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+// Sorts the columns (and values) of every row of a CSR ascending.
+void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cudaStream_t st) {
+  if (nrows == 0) return;
+  k_row_sort_warp<<<nblk(nrows * 32, 256), 256, 0, st>>>(ptr, nrows, idx, val);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  DBuf<int32_t> lists(2 * nrows + 2, st);  // [nrows] mid rows | [nrows] long rows | [2] counts
+  int32_t* counts = lists.p + 2 * nrows;
+  CRG_CHECK_CUDA(cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), st));
+  k_row_classes<<<nblk(nrows, 256), 256, 0, st>>>(ptr, nrows, lists.p, lists.p + nrows, counts);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  int32_t h[2] = {0, 0};
+  CRG_CHECK_CUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (h[0]) {
+    k_row_sort_block<<<(unsigned)h[0], kRowSortThreads, 0, st>>>(ptr, lists.p, idx, val);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  if (h[1]) {
+    DBuf<int64_t> off(h[1] + 1, st);
+    k_long_windows<<<1, 1, 0, st>>>(ptr, lists.p + nrows, h[1], off.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    int64_t total = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&total, off.p + h[1], sizeof(total), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    DBuf<int32_t> gk(total, st);
+    DBuf<double> gv(total, st);
+    k_row_sort_long<<<(unsigned)h[1], 1024, 0, st>>>(ptr, lists.p + nrows, off.p, idx, val, gk.p, gv.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+}
+
 void free_csr(DevCsr& c) {
   free_tiles(c.tiles);
   cudaFree(c.erow);
   cudaFree(c.split);
   cudaFree(c.tasks);
+  cudaFree(c.tslot);
   cudaFree(c.ptr); cudaFree(c.idx); cudaFree(c.val); cudaFree(c.val32); cudaFree(c.wn32); cudaFree(c.adj32);
   c = DevCsr{};
 }
@@ -958,9 +1099,8 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
                                                      R->fwd.idx, R->fwd.val, R->rev.idx, R->rev.val);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
-    if (nd) k_row_sort<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, nd, R->fwd.idx, R->fwd.val);
-    if (ns) k_row_sort<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, ns, R->rev.idx, R->rev.val);
-    CRG_CHECK_CUDA(cudaGetLastError());
+    sort_rows(R->fwd.ptr, nd, R->fwd.idx, R->fwd.val, st);
+    sort_rows(R->rev.ptr, ns, R->rev.idx, R->rev.val, st);
 
     // normalize! (regridder.jl:54-62)
     DBuf<unsigned long long> mx(1, st);
@@ -1024,6 +1164,13 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
       I.tiles[d] = tl[d]->ngood;
       I.tile_columns[d] = tl[d]->nucol;
       I.direct_rows[d] = tl[d]->ndirect;
+    }
+    const DevCsr* cs[2] = {&R->fwd, &R->rev};
+    for (int d = 0; d < 2; ++d) {
+      I.merge_tasks[d] = cs[d]->ntasks;
+      I.cut_rows[d] = cs[d]->nsplit;
+      I.carry_slots[d] = cs[d]->nslots;
+      I.empty_rows[d] = cs[d]->nempty;
     }
     // temporaries are freed stream-ordered by the DBuf destructors
   } catch (...) {

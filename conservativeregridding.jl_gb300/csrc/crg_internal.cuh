@@ -72,19 +72,20 @@ struct DevCsr {
   float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
   DevTiles tiles;            // staged-tile layout for the batched FP32/BF16 apply
   // merge-path layout: runs of about kTaskNnz entries per task, cut at row
-  // starts except inside rows longer than kLongRow
+  // starts except inside rows longer than kTaskNnz / 4
   int32_t* erow = nullptr;   // [nnz] row of each entry
   int64_t ntasks = 0;
   int4* tasks = nullptr;     // [ntasks] x = first entry, y = end entry,
                              //   z = first row | (row began in an earlier task) << 31,
                              //   w = last row | (row continues into a later task) << 31
-  int32_t* split = nullptr;  // [nsplit][3] rows spanning tasks: row, first task, last task
+  int2* tslot = nullptr;     // [ntasks] carry slots of the first / last row when they are cut (-1: none)
+  int32_t* split = nullptr;  // [nsplit][3] rows cut between tasks: row, first carry slot, number of slots
   int64_t nsplit = 0;
+  int64_t nslots = 0;        // carry slots (128 floats each) of all cut rows
   int64_t nempty = 0;        // rows without entries
 };
 
-constexpr int kTaskNnz = 256;  // nominal entries per merge-path task
-constexpr int kLongRow = 64;   // rows longer than this may be cut between tasks
+constexpr int kTaskNnz = 64;  // nominal entries per merge-path task
 
 // Per-cell vertex table on the device: [n][maxv] unit vectors (z = 0 planar).
 struct CellTable {

@@ -91,6 +91,11 @@ typedef struct crg_info {
     int64_t tiles[2];        /* row tiles whose source columns are staged in shared memory */
     int64_t tile_columns[2]; /* distinct source columns summed over those tiles */
     int64_t direct_rows[2];  /* rows applied by direct gathers (too many distinct columns) */
+    /* merge-path layout of the batched cell-major apply, [0] = forward, [1] = transpose */
+    int64_t merge_tasks[2];  /* tasks of about 64 entries, cut at row starts */
+    int64_t cut_rows[2];     /* rows longer than 16 entries cut between tasks */
+    int64_t carry_slots[2];  /* pieces of the cut rows (512-byte partial sums each) */
+    int64_t empty_rows[2];   /* rows without entries (written as zeros) */
 } crg_info;
 
 /* Build the regridder from `src` to `dst`.
@@ -149,11 +154,13 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
  * arguments as crg_apply, restricted to the batched cell-major path: device
  * pointers only, dtype CRG_F32 or CRG_BF16, src_stride_field = dst_stride_field
  * = 1, nfields and both cell strides multiples of 4, 16-byte aligned (FP32) /
- * 8-byte aligned (BF16) base pointers.  The partial sums of rows that span
- * several work blocks go to a scratch array the library declares statically
- * (CRG_NOALLOC_SCRATCH_BYTES per GPU, kept until the process exits), which
- * limits the regridder to at most 4,194,304 nonzeros; larger ones are refused
- * with CRG_ERR_NOT_SUPPORTED.  The first call on a device looks up that
+ * 8-byte aligned (BF16) base pointers.  The partial sums of rows cut between
+ * work blocks (crg_info.carry_slots, 512 bytes each) go to a scratch array the
+ * library declares statically (CRG_NOALLOC_SCRATCH_BYTES per GPU, kept until
+ * the process exits): at most 32,768 pieces.  Every regridder with at most
+ * 1,048,576 nonzeros fits; a larger one fits unless many of its rows are
+ * longer than 16 entries, and one that does not fit is refused with
+ * CRG_ERR_NOT_SUPPORTED.  The first call on a device looks up that
  * array's device address (cudaGetSymbolAddress), so make that first call
  * before any stream capture.  The scratch is shared by every call on the
  * device and keeps the previous call's contents (each call writes every slot

@@ -67,6 +67,9 @@ CASES = {
     "jittered_cs_to_lonlat2": lambda: (grids.cubed_sphere(16, jitter=0.15, seed=5), grids.lonlat_regular(2.0, 2.0)),
     "coincident_lonlat4_lonlat2": lambda: (grids.lonlat_regular(4.0, 4.0), grids.lonlat_regular(2.0, 2.0)),
     "identical_healpix8": lambda: (grids.healpix_grid(8), grids.healpix_grid(8)),
+    # rows of ~400 and ~8,100 entries: the shared-memory and global-memory row sorts
+    "lonlat10_from_lonlat0.5": lambda: (grids.lonlat_regular(10.0, 10.0), grids.lonlat_regular(0.5, 0.5)),
+    "lonlat45_from_lonlat0.5": lambda: (grids.lonlat_regular(45.0, 45.0), grids.lonlat_regular(0.5, 0.5)),
 }
 
 

@@ -32,7 +32,10 @@ def test_noalloc_matches_apply_on_consecutive_calls(cuda):
     import torch
 
     lib = _lib.load()
-    R = Regridder(grids.healpix_grid(32), grids.lonlat_regular(2.0, 2.0), normalize=True)
+    # 10-degree cells over HEALPix 32: forward rows of ~30 entries are cut between
+    # work blocks, so the static scratch carries partial sums
+    R = Regridder(grids.lonlat_regular(10.0, 10.0), grids.healpix_grid(32), normalize=True)
+    assert R.info["carry_slots"][0] > 0
     nd, ns = R.shape
     K = 64
     gen = torch.Generator(device="cuda").manual_seed(5)
@@ -62,9 +65,10 @@ def test_noalloc_refusals(cuda):
     yh = torch.zeros((nd, K))
     assert _call(lib.crg_apply_noalloc, R, 0, xh, K, yh) == _lib.CRG_ERR_NOT_SUPPORTED
     assert b"device pointers" in lib.crg_last_error()
-    # a regridder whose merge-path carries exceed the static scratch (> 4,194,304 nonzeros)
-    big = Regridder(grids.healpix_grid(256), grids.lonlat_regular(0.25, 0.25), normalize=True)
-    assert big.nnz > 4194304
+    # a regridder whose cut rows need more than the static scratch's 32,768 pieces:
+    # 30-degree cells over a 0.15-degree source, about 40,000 entries per row
+    big = Regridder(grids.lonlat_regular(30.0, 30.0), grids.lonlat_regular(0.15, 0.15), normalize=True)
+    assert big.info["carry_slots"][0] > 32768
     x = torch.zeros((big.shape[1], K), device="cuda")
     y = torch.zeros((big.shape[0], K), device="cuda")
     assert _call(lib.crg_apply_noalloc, big, 0, x, K, y) == _lib.CRG_ERR_NOT_SUPPORTED
