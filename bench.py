@@ -452,8 +452,8 @@ def run_ours(a, rank, world):
         "accuracy_vs_fp64": {"max_abs_err_rel_to_max": max_abs, "mean_conservation_rel_err": cons_err,
                              "mean_conservation_rel_err_vs_src_total": cons_err_src},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
-                     "kernel": "k_cm_nnz (+ k_cm_fixup, k_zero_empty_cm in the same timed launch group)"
+                     "frac": round(achieved / peak, 4), "traffic": profiled_traffic(a),
+                     "kernel": "k_cm_nnz (launch_ms: each direction's launches, incl. k_cm_fixup for cut rows)"
                      if a.layout == "cell_major" else "k_fm_rows",
                      "launch_ms": {"forward": round(kfb, 4), "transpose": round(krb, 4)},
                      "algorithmic_bytes_per_launch": {"forward": bf, "transpose": br},
@@ -461,12 +461,38 @@ def run_ours(a, rank, world):
         "e2e": {"value": round(world * (bf + br) / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
                 "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "link_probe": link},
-        "gpu_launches": 6 * a.steps if a.layout == "cell_major" else 2 * a.steps,
+        "gpu_launches": a.steps * launches_per_step(R.info, K, a.layout),
         "clocks": clk.summary(),
     }
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(hp, ll, K, sample_fields=8)
     return line
+
+
+def launches_per_step(info, K, layout):
+    """Kernels one forward + transpose step launches: per 128-field pass the
+    merge-path kernel and, when the direction has rows cut between tasks, their
+    fixup; one zero fill per direction with empty rows (field-major: one row
+    kernel per direction)."""
+    if layout != "cell_major":
+        return 2
+    passes = (K + 127) // 128
+    n = 0
+    for d in range(2):
+        n += passes * (1 + (info["cut_rows"][d] > 0)) + (info["empty_rows"][d] > 0)
+    return n
+
+
+def profiled_traffic(a):
+    """DRAM bytes (read + write) of one k_cm_nnz launch on this workload, from
+    the ncu summary kept beside the code; None when there is none for it."""
+    f = ROOT / "profiles" / "k_cm_nnz_healpix256_lonlat025_k128.md"
+    if a.layout != "cell_major" or a.fields != 128 or a.nside != 256 or a.dlon != 0.25 or not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch:"):
+            return int(line.split(":")[1].strip())
+    return None
 
 
 # ----------------------------------------------------------------- CPU legs (oracle)
@@ -492,9 +518,17 @@ def cpu_baseline(hp, ll, K, sample_fields):
     t = (time.perf_counter() - t0) / reps
     bf, br = step_bytes(O.nnz, O.nd, O.ns, sample_fields, elem=8, idx=8, wbytes=8)
     cores = oracle.load().og_num_threads()
+    # the reference's apply is one single-threaded mul! per field: one thread, one field
+    t0 = time.perf_counter()
+    O.apply(S[:1], nthreads=1)
+    O.apply(D[:1], transpose=True, nthreads=1)
+    t1 = time.perf_counter() - t0
+    b1f, b1r = step_bytes(O.nnz, O.nd, O.ns, 1, elem=8, idx=8, wbytes=8)
     return {"value": round((bf + br) / t / 1e9, 3), "unit": "GB/s", "cores": cores, "kind": "port",
             "sample": f"{sample_fields} of {K} fields, forward + transpose, fp64 (reference precision); "
-                      f"oracle build {tb:.2f}s = {O.nnz / tb:.3g} pairs/s on {cores} threads"}
+                      f"oracle build {tb:.2f}s = {O.nnz / tb:.3g} pairs/s on {cores} threads",
+            "single_thread": {"value": round((b1f + b1r) / t1 / 1e9, 3), "unit": "GB/s",
+                              "sample": "1 field, forward + transpose, 1 thread"}}
 
 
 def run_reference(a):
