@@ -13,6 +13,7 @@ from .grids import (
     unit_sphere_from_geographic,
 )
 from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
+from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
 
 __all__ = [
     "ArgumentError",
@@ -20,15 +21,19 @@ __all__ = [
     "DimensionMismatch",
     "Grid",
     "Regridder",
+    "area_grad",
     "cubed_sphere",
     "healpix_grid",
     "lonlat_grid",
     "lonlat_jittered",
     "lonlat_regular",
+    "lonlat_tangents",
     "polygon_grid",
     "regrid",
     "regrid_",
     "regrid_adjoint_",
+    "regrid_pullback",
     "regular_grid",
+    "split_points",
     "unit_sphere_from_geographic",
 ]

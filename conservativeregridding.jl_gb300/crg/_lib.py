@@ -85,6 +85,8 @@ SIGNATURES = {
                                     C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p]),
     "crg_apply_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
                                     C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p]),
+    "crg_area_grad": (C.c_int, [C.c_void_p, C.POINTER(crg_grid_desc), C.POINTER(crg_grid_desc), C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_csc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_csr": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_areas": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -117,6 +117,14 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
   });
 }
 
+crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src,
+                         const double* row_weight, const double* src_field, const double* area_weight, double* grad,
+                         void* stream) {
+  return guarded([&] {
+    area_grad_impl(r, dst, src, row_weight, src_field, area_weight, grad, (cudaStream_t)stream);
+  });
+}
+
 crg_status crg_apply_noalloc(const crg_regridder* r, int32_t transpose, int32_t dtype, const void* src, int64_t ssc,
                              int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int32_t normalize,
                              void* stream) {

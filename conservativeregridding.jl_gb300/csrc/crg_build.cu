@@ -31,7 +31,7 @@ namespace crg {
 namespace {
 
 constexpr int kLeaf = 8;          // cells per hierarchy leaf
-constexpr int kMaxBlocks = 12;    // curvilinear blocks per grid
+constexpr int kMaxBlocks = kMaxGridBlocks;
 constexpr int kMaxLevels = 40;
 constexpr int kSortShift = 10;    // bins of the counting sort = key >> kSortShift
 

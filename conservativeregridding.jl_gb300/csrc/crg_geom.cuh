@@ -61,7 +61,7 @@ __device__ __forceinline__ void two_sum(double a, double b, double& s, double& e
   s = x;
 }
 
-__device__ __noinline__ int exact_sign(const double* t, int n) {
+static __device__ __noinline__ int exact_sign(const double* t, int n) {
   double e[32];
   int m = 0;
   for (int i = 0; i < n; ++i) {
@@ -88,7 +88,7 @@ __device__ __forceinline__ void prod3(double p, double q, double r, double sg, d
 }
 
 // sign of det[a; b; c] = a.(b x c), exactly
-__device__ __noinline__ int det3_sign(d3 a, d3 b, d3 c) {
+static __device__ __noinline__ int det3_sign(d3 a, d3 b, d3 c) {
   double t[24];
   prod3(a.x, b.y, c.z, 1.0, t + 0);
   prod3(a.x, b.z, c.y, -1.0, t + 4);
@@ -100,7 +100,7 @@ __device__ __noinline__ int det3_sign(d3 a, d3 b, d3 c) {
 }
 
 // sign of (bx-ax)(vy-ay) - (by-ay)(vx-ax), exactly
-__device__ __noinline__ int orient2_sign(double ax, double ay, double bx, double by, double vx, double vy) {
+static __device__ __noinline__ int orient2_sign(double ax, double ay, double bx, double by, double vx, double vy) {
   double d[4][2];
   two_sum(bx, -ax, d[0][0], d[0][1]);
   two_sum(vy, -ay, d[1][0], d[1][1]);
@@ -134,14 +134,14 @@ __device__ __forceinline__ double settle(double s, double bound, int sg) {
   return sg > 0 ? m : -m;
 }
 
-__constant__ double kAtanC[20] = {
+static __constant__ double kAtanC[20] = {
     1.0, 0.3333333333333333, 0.2, 0.14285714285714285, 0.1111111111111111,
     0.09090909090909091, 0.07692307692307693, 0.06666666666666667, 0.058823529411764705,
     0.05263157894736842, 0.047619047619047616, 0.043478260869565216, 0.04,
     0.037037037037037035, 0.034482758620689655, 0.03225806451612903, 0.030303030303030304,
     0.02857142857142857, 0.02702702702702703, 0.02564102564102564};
 // kAtanTh[n]: the largest t^2 for which terms k = 0..n reach 2^-56 relative accuracy.
-__constant__ double kAtanTh[20] = {
+static __constant__ double kAtanTh[20] = {
     4.163336342344337e-17, 8.33000234328132e-09, 4.596981552458248e-06, 0.0001057159916729051,
     0.0006866613224549, 0.0023770807360687612, 0.005751393360079481, 0.011132588223807069,
     0.018578395538006495, 0.02795464321653044, 0.039019086539122956, 0.051485905388814555,

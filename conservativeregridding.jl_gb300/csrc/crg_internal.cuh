@@ -35,6 +35,8 @@ struct Fail {
     }                                         \
   } while (0)
 
+constexpr int kMaxGridBlocks = 12;  // curvilinear blocks per grid (cube faces and more)
+
 // Row tiles of one direction (see crg_tiles.cu).
 constexpr int kTileRows = 64;    // rows of a full tile
 constexpr int kTileUMax = 128;   // distinct source columns a tile may stage
@@ -129,4 +131,6 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
 void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st);
 void build_merge_path(DevCsr& c, cudaStream_t st);
 void free_tiles(DevTiles& t);
+void area_grad_impl(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src, const double* u,
+                    const double* s, const double* c, double* grad, cudaStream_t st);
 }  // namespace crg

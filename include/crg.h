@@ -143,6 +143,26 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
                              void* gsrc, int64_t gsrc_stride_cell, int64_t gsrc_stride_field,
                              int64_t nfields, int32_t normalize, void* stream);
 
+/* Derivatives of the areas with respect to the destination grid's vertices.
+ * No counterpart in the reference (it has no derivatives, Project.toml:10-23);
+ * with crg_apply_adjoint it gives the pullback of regrid! for a ChainRulesCore
+ * rrule.  Computes, into grad (zeroed first),
+ *     G = sum_ij row_weight[i] * src_field[j] * dA_ij/dV + sum_i area_weight[i] * da_i/dV,
+ * where A_ij is the unnormalised intersection area of destination cell i and
+ * source cell j (the nonzeros of r), a_i the unnormalised area of destination
+ * cell i, and V the destination vertex coordinates exactly as `dst` lays them
+ * out: [points][dim] for CRG_GRID_CURVILINEAR (shared corners accumulate),
+ * [ncells][max_verts][dim] for CRG_GRID_CELLS; dim is 3 (x, y, z of the unit
+ * vectors; project onto longitude/latitude tangents for angle derivatives) or
+ * 2 on the plane.  dst and src must be the grids r was built from.
+ * row_weight and src_field may both be NULL (area term only); area_weight
+ * may be NULL.  For d = (A s) ./ a and an output cotangent g:
+ * row_weight = g ./ a, area_weight = -g .* d ./ a.  Host or device pointers;
+ * returns after the result is in grad. */
+crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src,
+                         const double* row_weight, const double* src_field, const double* area_weight, double* grad,
+                         void* stream);
+
 /* Scratch held by crg_apply_noalloc, in bytes (per GPU that loads the library). */
 #define CRG_NOALLOC_SCRATCH_BYTES (16u << 20)
 
