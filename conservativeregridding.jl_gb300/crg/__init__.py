@@ -14,14 +14,17 @@ from .grids import (
 )
 from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
 from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
+from .batch import ApplyPlan, build_batch
 
 __all__ = [
+    "ApplyPlan",
     "ArgumentError",
     "CrgError",
     "DimensionMismatch",
     "Grid",
     "Regridder",
     "area_grad",
+    "build_batch",
     "cubed_sphere",
     "healpix_grid",
     "lonlat_grid",

@@ -47,6 +47,23 @@ class crg_build_opts(C.Structure):
     _fields_ = [("normalize", C.c_int32), ("flags", C.c_int32), ("stream", C.c_void_p)]
 
 
+class crg_apply_item(C.Structure):
+    _fields_ = [
+        ("regridder", C.c_void_p),
+        ("transpose", C.c_int32),
+        ("dtype", C.c_int32),
+        ("src", C.c_void_p),
+        ("src_stride_cell", C.c_int64),
+        ("src_stride_field", C.c_int64),
+        ("dst", C.c_void_p),
+        ("dst_stride_cell", C.c_int64),
+        ("dst_stride_field", C.c_int64),
+        ("nfields", C.c_int64),
+        ("normalize", C.c_int32),
+        ("adjoint", C.c_int32),
+    ]
+
+
 class crg_info(C.Structure):
     _fields_ = [
         ("n_dst", C.c_int64),
@@ -87,6 +104,11 @@ SIGNATURES = {
                                     C.c_int64, C.c_int64, C.c_int64, C.c_int32, C.c_void_p]),
     "crg_area_grad": (C.c_int, [C.c_void_p, C.POINTER(crg_grid_desc), C.POINTER(crg_grid_desc), C.c_void_p,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_build_batch": (C.c_int, [C.c_int64, C.POINTER(crg_grid_desc), C.POINTER(crg_grid_desc),
+                                  C.POINTER(crg_build_opts), C.c_int32, C.POINTER(C.c_void_p)]),
+    "crg_apply_plan_create": (C.c_int, [C.c_int64, C.POINTER(crg_apply_item), C.POINTER(C.c_void_p)]),
+    "crg_apply_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "crg_apply_plan_destroy": (C.c_int, [C.c_void_p]),
     "crg_get_csc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_csr": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_areas": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

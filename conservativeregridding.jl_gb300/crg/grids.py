@@ -175,6 +175,32 @@ def lonlat_jittered(nx: int, ny: int, jitter: float, seed: int, name: str = "") 
     return Grid("curvilinear", SPHERICAL, blocks=[pts], full_sphere=True, name=name or f"lonlat_jit_{nx}x{ny}")
 
 
+def convex_cells(g: Grid) -> np.ndarray:
+    """True for every cell whose corners all turn the same way (convex, in
+    either orientation; repeated vertices such as a lon-lat cell's two pole
+    corners do not count as turns).  The spherical clip needs convex
+    destination cells."""
+    t, nv = g.cell_table()
+    n, m = t.shape[0], t.shape[1]
+    nv = np.asarray(nv, np.int64)
+    rows = np.arange(n)
+    pos = np.zeros(n, bool)
+    neg = np.zeros(n, bool)
+    for k in range(m):
+        valid = k < nv
+        kk = np.minimum(k, nv - 1)
+        a = t[rows, (kk - 1) % nv]
+        b = t[rows, kk]
+        c = t[rows, (kk + 1) % nv]
+        if g.manifold == SPHERICAL:
+            turn = np.einsum("ij,ij->i", b, np.cross(b - a, c - b))
+        else:
+            turn = (b[:, 0] - a[:, 0]) * (c[:, 1] - b[:, 1]) - (b[:, 1] - a[:, 1]) * (c[:, 0] - b[:, 0])
+        pos |= valid & (turn > 0)
+        neg |= valid & (turn < 0)
+    return ~(pos & neg)
+
+
 # ----------------------------------------------------------------- cubed sphere
 
 def _cube_face(f: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:

@@ -111,20 +111,31 @@ class Regridder:
         opts = _lib.crg_build_opts(int(bool(normalize)), 0, _stream_ptr(stream))
         h = C.c_void_p()
         check(lib.crg_build(C.byref(dd), C.byref(ds), C.byref(opts), C.byref(h)))
-        self._h = _Handle(h.value)
+        del keep_d, keep_s
+        self._adopt_handle(h.value)
+
+    @classmethod
+    def _adopt(cls, ptr: int) -> "Regridder":
+        """Wrap a crg_regridder* whose one reference passes to the wrapper."""
+        self = cls.__new__(cls)
+        self._adopt_handle(ptr)
+        return self
+
+    def _adopt_handle(self, ptr: int):
+        lib = _lib.load()
+        self._h = _Handle(ptr)
         self._transposed = False
         info = _lib.crg_info()
-        check(lib.crg_regridder_info(C.c_void_p(h.value), C.byref(info)))
+        check(lib.crg_regridder_info(C.c_void_p(ptr), C.byref(info)))
         self.info = {k: (list(getattr(info, k)) if k in _PAIR_FIELDS else getattr(info, k))
                      for k, _ in _lib.crg_info._fields_ if k != "pad"}
         nd, ns = info.n_dst, info.n_src
         self.dst_areas = np.empty(nd)
         self.src_areas = np.empty(ns)
-        check(lib.crg_get_areas(C.c_void_p(h.value), self.dst_areas.ctypes.data, self.src_areas.ctypes.data))
+        check(lib.crg_get_areas(C.c_void_p(ptr), self.dst_areas.ctypes.data, self.src_areas.ctypes.data))
         self.dst_temp = np.zeros(nd)
         self.src_temp = np.zeros(ns)
         self._csc = [None]  # shared cache with transposed views
-        del keep_d, keep_s
 
     # -- shape ---------------------------------------------------------
     @property

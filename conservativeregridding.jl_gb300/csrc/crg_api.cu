@@ -117,6 +117,27 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
   });
 }
 
+crg_status crg_build_batch(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
+                           int32_t nthreads, crg_regridder** out) {
+  return guarded([&] { build_batch_impl(n, dst, src, opts, nthreads, out); });
+}
+
+crg_status crg_apply_plan_create(int64_t n, const crg_apply_item* items, crg_apply_plan** out) {
+  return guarded([&] {
+    CRG_REQUIRE(out != nullptr, CRG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    *out = apply_plan_impl(n, items);
+  });
+}
+
+crg_status crg_apply_plan_launch(crg_apply_plan* plan, void* stream) {
+  return guarded([&] { apply_plan_launch_impl(plan, (cudaStream_t)stream); });
+}
+
+crg_status crg_apply_plan_destroy(crg_apply_plan* plan) {
+  return guarded([&] { apply_plan_destroy_impl(plan); });
+}
+
 crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src,
                          const double* row_weight, const double* src_field, const double* area_weight, double* grad,
                          void* stream) {

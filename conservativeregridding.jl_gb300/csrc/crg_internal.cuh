@@ -133,4 +133,9 @@ void build_merge_path(DevCsr& c, cudaStream_t st);
 void free_tiles(DevTiles& t);
 void area_grad_impl(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src, const double* u,
                     const double* s, const double* c, double* grad, cudaStream_t st);
+void build_batch_impl(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
+                      int nthreads, crg_regridder** out);
+crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items);
+void apply_plan_launch_impl(crg_apply_plan* p, cudaStream_t st);
+void apply_plan_destroy_impl(crg_apply_plan* p);
 }  // namespace crg

@@ -143,6 +143,41 @@ crg_status crg_apply_adjoint(const crg_regridder* r, int32_t transpose, int32_t 
                              void* gsrc, int64_t gsrc_stride_cell, int64_t gsrc_stride_field,
                              int64_t nfields, int32_t normalize, void* stream);
 
+/* Builds n regridders at once, out[k] from src[k] to dst[k] (k < n), with the
+ * options in *opts (opts->stream is ignored).  No counterpart in the
+ * reference, which builds one Regridder at a time
+ * (src/regridder/regridder.jl:105-163); for many small grid pairs, whose
+ * builds are short kernels separated by host synchronisations, nthreads host
+ * threads (0: up to 8) build concurrently, each on its own stream.  On a
+ * failure every regridder of the call is released, out[] is all NULL and the
+ * lowest failing k's status is returned (its message names k). */
+crg_status crg_build_batch(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
+                           int32_t nthreads, crg_regridder** out);
+
+/* One apply of a batch: the arguments of crg_apply (adjoint = 1 for
+ * crg_apply_adjoint), device pointers only. */
+typedef struct crg_apply_item {
+    const crg_regridder* regridder;
+    int32_t transpose, dtype;
+    const void* src;
+    int64_t src_stride_cell, src_stride_field;
+    void* dst;
+    int64_t dst_stride_cell, dst_stride_field;
+    int64_t nfields;
+    int32_t normalize, adjoint;
+} crg_apply_item;
+
+/* A CUDA graph of the applies of n items (in order), captured once and
+ * replayed by crg_apply_plan_launch with one launch: the batched form of
+ * regrid! over many regridders (no counterpart in the reference).  The
+ * plan retains the regridders and keeps the field pointers: launch it again
+ * after writing new values into the same buffers.  Its temporaries are graph
+ * allocations; launches of one plan must not overlap. */
+typedef struct crg_apply_plan crg_apply_plan;
+crg_status crg_apply_plan_create(int64_t n, const crg_apply_item* items, crg_apply_plan** out);
+crg_status crg_apply_plan_launch(crg_apply_plan* plan, void* stream);
+crg_status crg_apply_plan_destroy(crg_apply_plan* plan);
+
 /* Derivatives of the areas with respect to the destination grid's vertices.
  * No counterpart in the reference (it has no derivatives, Project.toml:10-23);
  * with crg_apply_adjoint it gives the pullback of regrid! for a ChainRulesCore

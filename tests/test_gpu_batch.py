@@ -1,0 +1,96 @@
+"""Batches of regridders: crg_build_batch (concurrent builds) must give the
+same matrices as one-at-a-time builds, and an ApplyPlan (one CUDA graph for
+the applies of a whole batch) the same fields as one-at-a-time applies --
+bit for bit, since both run the same kernels.  The pairs follow the batched
+workload: jittered global lon-lat grids of uneven resolutions (cells moved by
+U(-0.2, 0.2) widths, convex), plus a HEALPix and a cubed-sphere pair."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from crg import ApplyPlan, ArgumentError, Regridder, build_batch, grids, regrid_
+
+pytestmark = pytest.mark.gpu
+
+
+def _jittered(rng, res):
+    nx, ny = int(round(360.0 / res)), int(round(180.0 / res))
+    while True:
+        g = grids.lonlat_jittered(nx, ny, 0.2, int(rng.integers(1 << 31)))
+        if grids.convex_cells(g).all():
+            return g
+
+
+@pytest.fixture(scope="module")
+def pairs(cuda):
+    rng = np.random.default_rng(33)
+    out = []
+    for _ in range(6):
+        r = np.exp(rng.uniform(np.log(2.0), np.log(8.0), size=2))
+        out.append((_jittered(rng, r[0]), _jittered(rng, r[1])))
+    out.append((grids.healpix_grid(16), grids.lonlat_regular(3.0, 3.0)))
+    out.append((grids.lonlat_regular(5.0, 5.0), grids.cubed_sphere(12, jitter=0.1, seed=2)))
+    return out
+
+
+def test_build_batch_equals_single_builds(pairs):
+    batch = build_batch(pairs, normalize=True, nthreads=4)
+    assert len(batch) == len(pairs)
+    for (dst, src), Rb in zip(pairs, batch):
+        Rs = Regridder(dst, src, normalize=True)
+        for a, b in zip(Rb.csc_arrays(), Rs.csc_arrays()):
+            assert np.array_equal(a, b)
+        assert np.array_equal(Rb.dst_areas, Rs.dst_areas) and np.array_equal(Rb.src_areas, Rs.src_areas)
+        assert Rb.info["normalizer"] == Rs.info["normalizer"]
+
+
+def test_build_batch_failure_releases_everything(pairs):
+    # a 9-gon: more vertices than the library's cells take (max_verts 3..8)
+    t = np.linspace(0.0, 2.0 * np.pi, 10)[:-1]
+    bad = grids.Grid("cells", grids.PLANAR, cells=np.stack([np.cos(t), np.sin(t)], axis=1)[None])
+    with pytest.raises(ArgumentError, match="pair 1"):
+        build_batch([pairs[0], (bad, bad), pairs[1]], nthreads=2)
+
+
+def test_apply_plan_equals_single_applies(pairs):
+    import torch
+
+    Rs = build_batch(pairs, normalize=True)
+    gen = torch.Generator(device="cuda").manual_seed(8)
+    specs = [(1, torch.float64, 1), (40, torch.float32, 1), (7, torch.float32, 2), (64, torch.bfloat16, 1),
+             (128, torch.float32, 1), (3, torch.float64, 2), (33, torch.float32, 1), (256, torch.float32, 1)]
+    items, refs = [], []
+    for k, ((K, dt, dims), R) in enumerate(zip(specs, Rs)):
+        RR = R.transpose() if k % 3 == 2 else R
+        n_out, n_in = RR.shape
+        if K == 1:
+            shape_in, shape_out = (n_in,), (n_out,)
+        elif dims == 1:
+            shape_in, shape_out = (n_in, K), (n_out, K)
+        else:
+            shape_in, shape_out = (K, n_in), (K, n_out)
+        x = torch.randn(shape_in, generator=gen, device="cuda").to(dt)
+        y = torch.full(shape_out, float("nan"), device="cuda").to(dt)
+        items.append((y, RR, x, dims))
+        refs.append((RR, x, dims))
+    plan = ApplyPlan(items)
+    for round_ in range(2):
+        if round_:  # new values in the same buffers: the replay reads them
+            for _, _, x, _ in items:
+                x.copy_(torch.randn(x.shape, generator=gen, device="cuda").to(x.dtype))
+        plan.launch()
+        torch.cuda.synchronize()
+        for (y, _, _, _), (RR, x, dims) in zip(items, refs):
+            expect = torch.empty_like(y)
+            regrid_(expect, RR, x, dims=dims)
+            torch.cuda.synchronize()
+            assert torch.equal(y, expect)
+
+
+def test_apply_plan_rejects_host_fields(pairs):
+    import torch
+
+    R = Regridder(*pairs[-1])
+    with pytest.raises(ArgumentError):
+        ApplyPlan([(torch.zeros(R.shape[0]), R, torch.zeros(R.shape[1]))])
