@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--pair", default="c5", choices=["c5", "identity"],
                    help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
                         "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
+    p.add_argument("--workload", default="c5", choices=["c5", "c3"],
+                   help="c5: the headline (HEALPix 256 <-> 0.25 degree, 128 fields); c3: 32 jittered lon-lat "
+                        "pairs of uneven resolution built as one batch and applied as one CUDA graph")
     return p.parse_args()
 
 
@@ -495,6 +498,101 @@ def profiled_traffic(a):
     return None
 
 
+# ----------------------------------------------------------------- batched workload
+
+def c3_pairs(seed=20250):
+    """32 (dst, src) pairs: each side a global lon-lat grid of resolution
+    r = exp(U[ln 0.4, ln 4]) degrees with its vertices jittered by U(-0.2, 0.2)
+    cell widths (re-seeded until every cell is convex), and K =
+    round(exp(U[0, ln 512])) FP32 fields per pair."""
+    from crg import grids
+
+    rng = np.random.default_rng(seed)
+    pairs, ks = [], []
+    for _ in range(32):
+        sides = []
+        for r in np.exp(rng.uniform(np.log(0.4), np.log(4.0), size=2)):
+            nx, ny = int(round(360.0 / r)), int(round(180.0 / r))
+            while True:
+                g = grids.lonlat_jittered(nx, ny, 0.2, int(rng.integers(1 << 31)))
+                if grids.convex_cells(g).all():
+                    break
+            sides.append(g)
+        pairs.append((sides[0], sides[1]))
+        ks.append(int(round(np.exp(rng.uniform(0.0, np.log(512.0))))))
+    return pairs, ks
+
+
+def run_c3(a):
+    """Build the 32 pairs one at a time and as one batch; apply every pair's
+    fields one call at a time and as one captured graph (forward direction,
+    cell-major FP32 fields, inputs resident on the device)."""
+    import torch
+
+    from crg import ApplyPlan, Regridder, build_batch, regrid_
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    pairs, ks = c3_pairs()
+    build_batch(pairs[:2])  # warm the library and the allocator
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    single = [Regridder(d, s, normalize=True) for d, s in pairs]
+    torch.cuda.synchronize()
+    t_single = time.perf_counter() - t0
+    del single
+    t0 = time.perf_counter()
+    Rs = build_batch(pairs, normalize=True, nthreads=8)
+    torch.cuda.synchronize()
+    t_batch = time.perf_counter() - t0
+    nnz = sum(R.nnz for R in Rs)
+    gen = torch.Generator(device=dev).manual_seed(5)
+    items, nbytes = [], 0
+    for R, K in zip(Rs, ks):
+        nd, ns = R.shape
+        shp_in, shp_out = ((ns,), (nd,)) if K == 1 else ((ns, K), (nd, K))
+        x = torch.randn(shp_in, generator=gen, device=dev)
+        y = torch.empty(shp_out, device=dev)
+        items.append((y, R, x, 1))
+        nbytes += step_bytes(R.nnz, nd, ns, K)[0]
+    plan = ApplyPlan(items)
+
+    def loop():
+        for y, R, x, dims in items:
+            regrid_(y, R, x, dims=dims)
+
+    stream = torch.cuda.current_stream(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    for _ in range(max(a.warmup, 3)):
+        loop()
+        plan.launch()
+    reps = max(5, min(a.steps, 50))
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for _ in range(reps):
+        loop()
+    ev[1].record(stream)
+    for _ in range(reps):
+        plan.launch()
+    ev[2].record(stream)
+    ev[2].synchronize()
+    ms_loop = ev[0].elapsed_time(ev[1]) / reps
+    ms_plan = ev[1].elapsed_time(ev[2]) / reps
+    cells = [(R.shape[0], R.shape[1]) for R in Rs]
+    return {
+        "metric": "batched build pairs/s (summed) and batched apply GB/s",
+        "workload": "32 jittered global lon-lat pairs, resolution exp(U[ln 0.4, ln 4]) deg per side, "
+                    "K = round(exp(U[0, ln 512])) fp32 fields, forward applies",
+        "pairs": 32, "nnz_total": nnz, "fields_total": int(sum(ks)),
+        "cells_min_max": [int(min(min(c) for c in cells)), int(max(max(c) for c in cells))],
+        "build": {"single_ms": round(t_single * 1e3, 2), "batch_ms": round(t_batch * 1e3, 2),
+                  "pairs_per_s_batch": round(nnz / t_batch, 1), "pairs_per_s_single": round(nnz / t_single, 1)},
+        "apply": {"loop_ms": round(ms_loop, 4), "graph_ms": round(ms_plan, 4),
+                  "GB/s_graph": round(nbytes / (ms_plan * 1e-3) / 1e9, 1),
+                  "GB/s_loop": round(nbytes / (ms_loop * 1e-3) / 1e9, 1), "bytes_per_batch": nbytes},
+    }
+
+
 # ----------------------------------------------------------------- CPU legs (oracle)
 
 def cpu_baseline(hp, ll, K, sample_fields):
@@ -571,6 +669,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", 1))
     if a.profile:
         run_profile(a)
+        return
+    if a.workload == "c3":
+        if rank == 0:
+            print(json.dumps(run_c3(a)))
         return
     if a.impl == "reference":
         if rank == 0:

@@ -47,8 +47,9 @@ class ApplyPlan:
     Items are ``(dst, R, src)`` or ``(dst, R, src, dims)`` with CUDA torch
     tensors: 1-D fields, or 2-D with the spatial axis ``dims`` (1: (cells,
     fields), the cell-major layout; 2: (fields, cells)).  ``R`` may be a
-    transposed view.  The plan keeps the tensors alive and reads/writes them
-    in place on every launch."""
+    transposed view.  Items run as parallel branches of the graph, so their
+    outputs must not overlap.  The plan keeps the tensors alive and
+    reads/writes them in place on every launch."""
 
     def __init__(self, items, normalize: bool = True):
         arr = (_lib.crg_apply_item * len(items))()

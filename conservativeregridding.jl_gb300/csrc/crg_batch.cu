@@ -86,32 +86,49 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
     CRG_REQUIRE(it.dst && is_device_pointer(it.dst) && (!it.src || is_device_pointer(it.src)), CRG_ERR_NOT_SUPPORTED,
                 "item %lld: a plan replays on the GPU alone, so fields must be device pointers", (long long)k);
   }
-  cudaStream_t cap = nullptr;
-  CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  // Capture: the origin stream forks one branch per item (their outputs are
+  // distinct), so the graph runs small items side by side.
+  std::vector<cudaStream_t> sts(n + 1, nullptr);
+  std::vector<cudaEvent_t> evs(n + 1, nullptr);
+  auto cleanup = [&]() {
+    for (auto e : evs)
+      if (e) cudaEventDestroy(e);
+    for (auto s : sts)
+      if (s) cudaStreamDestroy(s);
+  };
   cudaGraph_t graph = nullptr;
-  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
-  if (e != cudaSuccess) {
-    cudaStreamDestroy(cap);
-    CRG_CHECK_CUDA(e);
-  }
   try {
-    for (int64_t k = 0; k < n; ++k) {
-      const crg_apply_item& it = items[k];
-      apply_impl(it.regridder, it.transpose, it.dtype, it.adjoint != 0, it.src, it.src_stride_cell,
-                 it.src_stride_field, it.dst, it.dst_stride_cell, it.dst_stride_field, it.nfields, it.normalize, cap);
+    for (int64_t k = 0; k <= n; ++k) {
+      CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&sts[k], cudaStreamNonBlocking));
+      CRG_CHECK_CUDA(cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming));
     }
+    cudaStream_t origin = sts[n];
+    CRG_CHECK_CUDA(cudaStreamBeginCapture(origin, cudaStreamCaptureModeThreadLocal));
+    try {
+      CRG_CHECK_CUDA(cudaEventRecord(evs[n], origin));
+      for (int64_t k = 0; k < n; ++k) {
+        const crg_apply_item& it = items[k];
+        CRG_CHECK_CUDA(cudaStreamWaitEvent(sts[k], evs[n], 0));
+        apply_impl(it.regridder, it.transpose, it.dtype, it.adjoint != 0, it.src, it.src_stride_cell,
+                   it.src_stride_field, it.dst, it.dst_stride_cell, it.dst_stride_field, it.nfields, it.normalize,
+                   sts[k]);
+        CRG_CHECK_CUDA(cudaEventRecord(evs[k], sts[k]));
+        CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[k], 0));
+      }
+    } catch (...) {
+      cudaStreamEndCapture(origin, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    CRG_CHECK_CUDA(cudaStreamEndCapture(origin, &graph));
   } catch (...) {
-    cudaStreamEndCapture(cap, &graph);
-    if (graph) cudaGraphDestroy(graph);
-    cudaStreamDestroy(cap);
+    cleanup();
     throw;
   }
-  e = cudaStreamEndCapture(cap, &graph);
-  cudaStreamDestroy(cap);
-  CRG_CHECK_CUDA(e);
+  cleanup();
   crg_apply_plan* p = new crg_apply_plan;
   p->device = dev;
-  e = cudaGraphInstantiate(&p->exec, graph, 0);
+  const cudaError_t e = cudaGraphInstantiate(&p->exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
     delete p;

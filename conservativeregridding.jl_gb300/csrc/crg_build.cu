@@ -63,14 +63,6 @@ struct DBuf {
   ~DBuf() { release(); }
 };
 
-// Four spare elements: a 16-byte bulk copy of an array's last entries stays
-// inside the allocation.
-template <class T>
-T* persistent_alloc(size_t n) {
-  T* p = nullptr;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&p, (n + 4) * sizeof(T)));
-  return p;
-}
 
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
@@ -1040,8 +1032,8 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     const int64_t nd = gd.ncells, ns = gs.ncells;
     R->nd = nd;
     R->ns = ns;
-    R->dst_area = persistent_alloc<double>((size_t)nd);
-    R->src_area = persistent_alloc<double>((size_t)ns);
+    R->dst_area = keep_alloc<double>((size_t)nd, st);
+    R->src_area = keep_alloc<double>((size_t)ns, st);
 
     HostTree td, ts;
     build_tree(gd, sph, R->dst_area, td, st);
@@ -1073,8 +1065,8 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     // K5
     R->fwd.nrows = nd; R->fwd.ncols = ns;
     R->rev.nrows = ns; R->rev.ncols = nd;
-    R->fwd.ptr = persistent_alloc<int32_t>((size_t)nd + 1);
-    R->rev.ptr = persistent_alloc<int32_t>((size_t)ns + 1);
+    R->fwd.ptr = keep_alloc<int32_t>((size_t)nd + 1, st);
+    R->rev.ptr = keep_alloc<int32_t>((size_t)ns + 1, st);
     exclusive_scan_i32(rowcnt.p, R->fwd.ptr, nd, st);
     exclusive_scan_i32(colcnt.p, R->rev.ptr, ns, st);
     int32_t hnnz = 0;
@@ -1088,10 +1080,10 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     const int64_t nnz = hnnz;
     R->nnz = nnz;
     R->fwd.nnz = R->rev.nnz = nnz;
-    R->fwd.idx = persistent_alloc<int32_t>((size_t)nnz);
-    R->fwd.val = persistent_alloc<double>((size_t)nnz);
-    R->rev.idx = persistent_alloc<int32_t>((size_t)nnz);
-    R->rev.val = persistent_alloc<double>((size_t)nnz);
+    R->fwd.idx = keep_alloc<int32_t>((size_t)nnz, st);
+    R->fwd.val = keep_alloc<double>((size_t)nnz, st);
+    R->rev.idx = keep_alloc<int32_t>((size_t)nnz, st);
+    R->rev.val = keep_alloc<double>((size_t)nnz, st);
     rowcnt.zero();
     colcnt.zero();
     if (nc) {
@@ -1127,12 +1119,12 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     }
     // derived FP32 weights + Kahan sums
     for (DevCsr* c : {&R->fwd, &R->rev}) {
-      c->val32 = persistent_alloc<float>((size_t)nnz);
-      c->wn32 = persistent_alloc<float>((size_t)nnz);
-      c->adj32 = persistent_alloc<float>((size_t)nnz);
+      c->val32 = keep_alloc<float>((size_t)nnz, st);
+      c->wn32 = keep_alloc<float>((size_t)nnz, st);
+      c->adj32 = keep_alloc<float>((size_t)nnz, st);
     }
-    R->row_sum = persistent_alloc<double>((size_t)nd);
-    R->col_sum = persistent_alloc<double>((size_t)ns);
+    R->row_sum = keep_alloc<double>((size_t)nd, st);
+    R->col_sum = keep_alloc<double>((size_t)ns, st);
     if (nd)
       k_derive<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, R->fwd.idx, R->fwd.val, nd, R->dst_area, R->src_area,
                                               R->fwd.val32, R->fwd.wn32, R->fwd.adj32, R->row_sum);

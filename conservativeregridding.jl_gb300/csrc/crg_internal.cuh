@@ -97,6 +97,17 @@ struct CellTable {
   int8_t* nv = nullptr;  // [n]
 };
 
+// Device memory a regridder keeps, allocated in stream order (no device-wide
+// synchronisation, so builds on different streams overlap) with four spare
+// elements (a 16-byte load or copy of an array's last entries stays inside);
+// freed with cudaFree when the regridder is released.
+template <class T>
+T* keep_alloc(size_t n, cudaStream_t st) {
+  T* p = nullptr;
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&p, (n + 4) * sizeof(T), st));
+  return p;
+}
+
 }  // namespace crg
 
 struct crg_regridder {

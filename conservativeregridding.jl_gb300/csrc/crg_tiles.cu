@@ -210,16 +210,10 @@ __global__ void k_len_perm(const int32_t* __restrict__ ptr, const int32_t* __res
   }
 }
 
-template <class T>
-T* palloc(size_t n) {
-  T* p = nullptr;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&p, (n ? n : 1) * sizeof(T)));
-  return p;
-}
 
 template <class T>
 T* upload(const std::vector<T>& v, cudaStream_t st) {
-  T* p = palloc<T>(v.size());
+  T* p = keep_alloc<T>(v.size(), st);
   if (!v.empty()) {
     CRG_CHECK_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, st));
     CRG_CHECK_CUDA(cudaStreamSynchronize(st));
@@ -239,13 +233,13 @@ void free_tiles(DevTiles& t) {
 void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st) {
   DevTiles& T = c.tiles;
   const int64_t n = c.nrows, nnz = c.nnz;
-  T.rows = palloc<int32_t>((size_t)n);
-  T.lptr = palloc<int32_t>((size_t)n + 1);
-  T.lcol = palloc<uint16_t>((size_t)nnz + 2);  // +2: read as 32-bit words
-  T.lchk = palloc<uint16_t>((size_t)nnz + 2);
-  T.lw_val = palloc<float>((size_t)nnz);
-  T.lw_wn = palloc<float>((size_t)nnz);
-  T.lw_adj = palloc<float>((size_t)nnz);
+  T.rows = keep_alloc<int32_t>((size_t)n, st);
+  T.lptr = keep_alloc<int32_t>((size_t)n + 1, st);
+  T.lcol = keep_alloc<uint16_t>((size_t)nnz + 2, st);  // +2: read as 32-bit words
+  T.lchk = keep_alloc<uint16_t>((size_t)nnz + 2, st);
+  T.lw_val = keep_alloc<float>((size_t)nnz, st);
+  T.lw_wn = keep_alloc<float>((size_t)nnz, st);
+  T.lw_adj = keep_alloc<float>((size_t)nnz, st);
   struct Good { int32_t p0, p1, u, nc; };
   std::vector<Good> good;
   std::vector<int32_t> direct;
@@ -322,8 +316,8 @@ void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st) {
   T.nuchunk = cacc;
   T.desc = upload(desc, st);
   T.direct = upload(direct, st);
-  T.ucol = palloc<int32_t>((size_t)uacc);
-  T.uchunk = palloc<int32_t>((size_t)cacc);
+  T.ucol = keep_alloc<int32_t>((size_t)uacc, st);
+  T.uchunk = keep_alloc<int32_t>((size_t)cacc, st);
   if (T.ngood) {
     k_tile_fill<<<(unsigned)T.ngood, kThreads, 0, st>>>(c.ptr, c.idx, c.val32, c.wn32, c.adj32, T.rows, T.desc,
                                                         T.lptr, T.ucol, T.uchunk, T.lcol, T.lchk, T.lw_val, T.lw_wn,
@@ -430,7 +424,7 @@ __global__ void k_slot_fill(int32_t* __restrict__ split, int64_t nsplit, const i
 
 void build_merge_path(DevCsr& c, cudaStream_t st) {
   const int64_t n = c.nrows, nnz = c.nnz;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&c.erow, sizeof(int32_t) * (nnz + 4)));  // 4 spare: whole 16-byte loads
+  c.erow = keep_alloc<int32_t>((size_t)nnz, st);
   // CRG_TASK_NNZ (32..1024) sets the nominal task length for tuning; CRG_TASK_CUT=fixed
   // cuts every task at exactly that length (rows spanning tasks everywhere)
   static const int task_nnz = [] {
@@ -443,9 +437,8 @@ void build_merge_path(DevCsr& c, cudaStream_t st) {
     return (e && strcmp(e, "fixed") == 0) ? -1 : task_nnz / 4;
   }();
   c.ntasks = (nnz + task_nnz - 1) / task_nnz;
-  CRG_CHECK_CUDA(cudaMalloc((void**)&c.tasks, sizeof(int4) * (c.ntasks ? c.ntasks : 1)));
-  CRG_CHECK_CUDA(cudaMalloc((void**)&c.tslot, sizeof(int2) * (c.ntasks ? c.ntasks : 1)));
-  CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3));
+  c.tasks = keep_alloc<int4>((size_t)c.ntasks, st);
+  c.tslot = keep_alloc<int2>((size_t)c.ntasks, st);
   c.nsplit = 0;
   c.nslots = 0;
   c.nempty = n;
@@ -470,10 +463,8 @@ void build_merge_path(DevCsr& c, cudaStream_t st) {
   c.nsplit = counts[0];
   c.nempty = counts[1];
   CRG_CHECK_CUDA(cudaMemsetAsync(c.tslot, 0xff, sizeof(int2) * c.ntasks, st));  // -1: row not cut
+  c.split = keep_alloc<int32_t>((size_t)3 * c.nsplit, st);
   if (c.nsplit) {
-    CRG_CHECK_CUDA(cudaFree(c.split));
-    c.split = nullptr;
-    CRG_CHECK_CUDA(cudaMalloc((void**)&c.split, sizeof(int32_t) * 3 * c.nsplit));
     int32_t* span = nullptr;  // [nsplit + 1] pieces per cut row, scanned to first slots
     CRG_CHECK_CUDA(cudaMallocAsync((void**)&span, sizeof(int32_t) * (c.nsplit + 1), st));
     k_split_fill<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, bound, c.ntasks, c.tasks, pos, c.split, span);

@@ -167,12 +167,13 @@ typedef struct crg_apply_item {
     int32_t normalize, adjoint;
 } crg_apply_item;
 
-/* A CUDA graph of the applies of n items (in order), captured once and
- * replayed by crg_apply_plan_launch with one launch: the batched form of
- * regrid! over many regridders (no counterpart in the reference).  The
- * plan retains the regridders and keeps the field pointers: launch it again
- * after writing new values into the same buffers.  Its temporaries are graph
- * allocations; launches of one plan must not overlap. */
+/* A CUDA graph of the applies of n items, captured once and replayed by
+ * crg_apply_plan_launch with one launch: the batched form of regrid! over
+ * many regridders (no counterpart in the reference).  The items are parallel
+ * branches of the graph, so their outputs must not overlap (inputs may be
+ * shared).  The plan retains the regridders and keeps the field pointers:
+ * launch it again after writing new values into the same buffers.  Its
+ * temporaries are graph allocations; launches of one plan must not overlap. */
 typedef struct crg_apply_plan crg_apply_plan;
 crg_status crg_apply_plan_create(int64_t n, const crg_apply_item* items, crg_apply_plan** out);
 crg_status crg_apply_plan_launch(crg_apply_plan* plan, void* stream);
