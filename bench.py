@@ -298,13 +298,9 @@ def run_ours(a, rank, world):
         stop.synchronize()
         torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
-    ms = start.elapsed_time(stop) / a.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(stop) / a.steps, world, dev)
     bf, br = step_bytes(nnz, nd, ns, K)
-    value = world * (bf + br) / (ms * 1e-3) / 1e9
+    value = job_rate(world, bf + br, ms)
     # one more timed window of back-to-back launches per direction for the roofline
     reps = 20
     ev[0].record(stream)
@@ -470,6 +466,24 @@ def run_ours(a, rank, world):
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(hp, ll, K, sample_fields=8)
     return line
+
+
+def max_over_ranks(ms, world, device):
+    """The slowest replica's time per step (every rank gets it)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, bytes_per_step, ms):
+    """Whole-job GB/s: every replica moves bytes_per_step per step, the job
+    takes the slowest replica's time."""
+    return world * bytes_per_step / (ms * 1e-3) / 1e9
 
 
 def launches_per_step(info, K, layout):
