@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "crg_internal.cuh"
 
@@ -981,12 +982,32 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   const bool src_host = nin > 0 && !is_device_pointer(src);
   const bool dst_host = !is_device_pointer(dst);
 
-  std::unique_lock<std::mutex> lock(r->stage_mu, std::defer_lock);
-  const void* xs = src;
-  void* ys = dst;
-  if (src_host || dst_host) {
-    lock.lock();
-    size_t need = (src_host ? (size_t)in_span * es : 0) + (dst_host ? (size_t)out_span * es : 0) + 256;
+  // the apply on device buffers
+  auto compute = [&](const void* x, int64_t xsc, int64_t xsf, void* y, int64_t ysc, int64_t ysf, int64_t n,
+                     cudaStream_t s) {
+    if (dtype == CRG_F64) {
+      const double* cdiv = adjoint ? div : nullptr;
+      const double* rdiv = adjoint ? nullptr : div;
+      for (int64_t f0 = 0; f0 < n; f0 += 65535) {
+        dim3 grid(nblk(nout, 128), (unsigned)std::min<int64_t>(65535, n - f0));
+        k_spmv_f64<<<grid, 128, 0, s>>>(c.ptr, c.idx, c.val, nout, (const double*)x, xsc, xsf, (double*)y, ysc, ysf,
+                                        f0, rdiv, cdiv);
+      }
+      CRG_CHECK_CUDA(cudaGetLastError());
+    } else if (dtype == CRG_F32) {
+      launch_f32<float>(c, normalize, adjoint, (const float*)x, xsc, xsf, (float*)y, ysc, ysf, n, s);
+    } else {
+      launch_f32<__nv_bfloat16>(c, normalize, adjoint, (const __nv_bfloat16*)x, xsc, xsf, (__nv_bfloat16*)y, ysc, ysf,
+                                n, s);
+    }
+  };
+  if (!src_host && !dst_host) {
+    compute(src, ssc, ssf, dst, dsc, dsf, nf, st);
+    return;
+  }
+
+  std::lock_guard<std::mutex> lock(r->stage_mu);
+  auto stage = [&](size_t need) {
     if (r->stage_bytes < need) {
       if (r->stage) CRG_CHECK_CUDA(cudaFree(r->stage));
       r->stage = nullptr;
@@ -994,39 +1015,91 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
       CRG_CHECK_CUDA(cudaMalloc(&r->stage, need));
       r->stage_bytes = need;
     }
-    char* base = (char*)r->stage;
-    if (src_host) {
-      CRG_CHECK_CUDA(cudaMemcpyAsync(base, src, (size_t)in_span * es, cudaMemcpyHostToDevice, st));
-      xs = base;
-      base += ((size_t)in_span * es + 255) / 256 * 256;
+    return (char*)r->stage;
+  };
+
+  // Host fields in both directions, fields side by side (cell-major) or
+  // whole fields contiguous (field-major): a pipeline over chunks of fields.
+  // Chunk k+1 moves to the device while chunk k is applied and chunk k-1
+  // moves back, on two copy streams, so the two directions of the host link
+  // run at once.  Cell-major chunks are 2-D copies of 256-byte rows (full link
+  // speed); each chunk is applied as a contiguous (cells, fields) block.
+  const bool cm = ssf == 1 && dsf == 1 && nf > 1;
+  const bool fm = ssc == 1 && dsc == 1 && nf > 1 && !cm;
+  // CRG_HOST_CHUNK_BYTES (64..4096, default 256) sets the cell-major row width for tuning
+  static const int64_t row_bytes = [] {
+    const char* e = getenv("CRG_HOST_CHUNK_BYTES");
+    const int64_t v = e ? atoll(e) : 256;
+    return (v >= 64 && v <= 4096) ? v : 256;
+  }();
+  const int64_t chunk = cm ? std::max<int64_t>(4, row_bytes / (int64_t)es / 4 * 4) : (nf + 3) / 4;
+  if (src_host && dst_host && nin > 0 && (cm || fm) && nf >= 2 * chunk) {
+    const int64_t nchunks = (nf + chunk - 1) / chunk;
+    const size_t in_bytes = ((size_t)nin * nf * es + 255) / 256 * 256;
+    char* din = stage(in_bytes + (size_t)nout * nf * es + 256);
+    char* dout = din + in_bytes;
+    if (!r->copy_in) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&r->copy_in, cudaStreamNonBlocking));
+    if (!r->copy_out) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&r->copy_out, cudaStreamNonBlocking));
+    std::vector<cudaEvent_t> ev(2 * nchunks + 1, nullptr);
+    struct Events {
+      std::vector<cudaEvent_t>& v;
+      ~Events() {
+        for (auto e : v)
+          if (e) cudaEventDestroy(e);
+      }
+    } guard{ev};
+    for (auto& e : ev) CRG_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    // the copies start after the work the caller queued on its stream
+    CRG_CHECK_CUDA(cudaEventRecord(ev[2 * nchunks], st));
+    CRG_CHECK_CUDA(cudaStreamWaitEvent(r->copy_in, ev[2 * nchunks], 0));
+    const char* hs = (const char*)src;
+    char* hd = (char*)dst;
+    for (int64_t k = 0; k < nchunks; ++k) {
+      const int64_t f0 = k * chunk, fc = std::min(chunk, nf - f0);
+      char* xk = din + (size_t)f0 * nin * es;
+      char* yk = dout + (size_t)f0 * nout * es;
+      if (cm)
+        CRG_CHECK_CUDA(cudaMemcpy2DAsync(xk, fc * es, hs + f0 * es, ssc * es, fc * es, nin, cudaMemcpyHostToDevice,
+                                         r->copy_in));
+      else
+        CRG_CHECK_CUDA(cudaMemcpy2DAsync(xk, nin * es, hs + f0 * ssf * es, ssf * es, nin * es, fc,
+                                         cudaMemcpyHostToDevice, r->copy_in));
+      CRG_CHECK_CUDA(cudaEventRecord(ev[2 * k], r->copy_in));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(st, ev[2 * k], 0));
+      if (cm) compute(xk, fc, 1, yk, fc, 1, fc, st);
+      else compute(xk, 1, nin, yk, 1, nout, fc, st);
+      CRG_CHECK_CUDA(cudaEventRecord(ev[2 * k + 1], st));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(r->copy_out, ev[2 * k + 1], 0));
+      if (cm)
+        CRG_CHECK_CUDA(cudaMemcpy2DAsync(hd + f0 * es, dsc * es, yk, fc * es, fc * es, nout, cudaMemcpyDeviceToHost,
+                                         r->copy_out));
+      else
+        CRG_CHECK_CUDA(cudaMemcpy2DAsync(hd + f0 * dsf * es, dsf * es, yk, nout * es, nout * es, fc,
+                                         cudaMemcpyDeviceToHost, r->copy_out));
     }
-    if (dst_host) {
-      // a strided destination keeps the elements between ours: bring them along
-      if (out_span != nout * nf)
-        CRG_CHECK_CUDA(cudaMemcpyAsync(base, dst, (size_t)out_span * es, cudaMemcpyHostToDevice, st));
-      ys = base;
-    }
+    CRG_CHECK_CUDA(cudaStreamSynchronize(r->copy_out));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    return;
   }
 
-  if (dtype == CRG_F64) {
-    const double* cdiv = adjoint ? div : nullptr;
-    const double* rdiv = adjoint ? nullptr : div;
-    for (int64_t f0 = 0; f0 < nf; f0 += 65535) {
-      dim3 grid(nblk(nout, 128), (unsigned)std::min<int64_t>(65535, nf - f0));
-      k_spmv_f64<<<grid, 128, 0, st>>>(c.ptr, c.idx, c.val, nout, (const double*)xs, ssc, ssf, (double*)ys, dsc, dsf,
-                                       f0, rdiv, cdiv);
-    }
-    CRG_CHECK_CUDA(cudaGetLastError());
-  } else {
-    if (dtype == CRG_F32)
-      launch_f32<float>(c, normalize, adjoint, (const float*)xs, ssc, ssf, (float*)ys, dsc, dsf, nf, st);
-    else
-      launch_f32<__nv_bfloat16>(c, normalize, adjoint, (const __nv_bfloat16*)xs, ssc, ssf, (__nv_bfloat16*)ys, dsc,
-                                dsf, nf, st);
+  // Otherwise: one copy in, the apply, one copy out.
+  char* base = stage((src_host ? (size_t)in_span * es : 0) + (dst_host ? (size_t)out_span * es : 0) + 256);
+  const void* xs = src;
+  void* ys = dst;
+  if (src_host) {
+    CRG_CHECK_CUDA(cudaMemcpyAsync(base, src, (size_t)in_span * es, cudaMemcpyHostToDevice, st));
+    xs = base;
+    base += ((size_t)in_span * es + 255) / 256 * 256;
   }
-
+  if (dst_host) {
+    // a strided destination keeps the elements between ours: bring them along
+    if (out_span != nout * nf)
+      CRG_CHECK_CUDA(cudaMemcpyAsync(base, dst, (size_t)out_span * es, cudaMemcpyHostToDevice, st));
+    ys = base;
+  }
+  compute(xs, ssc, ssf, ys, dsc, dsf, nf, st);
   if (dst_host) CRG_CHECK_CUDA(cudaMemcpyAsync(dst, ys, (size_t)out_span * es, cudaMemcpyDeviceToHost, st));
-  if (src_host || dst_host) CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace crg

@@ -1005,6 +1005,8 @@ void free_regridder(crg_regridder* r) {
   cudaFree(r->row_sum);
   cudaFree(r->col_sum);
   if (r->stage) cudaFree(r->stage);
+  if (r->copy_in) cudaStreamDestroy(r->copy_in);
+  if (r->copy_out) cudaStreamDestroy(r->copy_out);
   cudaSetDevice(dev);
   delete r;
 }

@@ -128,6 +128,8 @@ struct crg_regridder {
   std::mutex stage_mu;
   void* stage = nullptr;
   size_t stage_bytes = 0;
+  cudaStream_t copy_in = nullptr;   // host -> device copies of the chunked host-field pipeline
+  cudaStream_t copy_out = nullptr;  // device -> host copies of it
 };
 
 namespace crg {
