@@ -25,6 +25,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -871,9 +872,60 @@ void launch_cm_rows(const DevCsr& c, const float* w, const T* x, int64_t xs, T* 
 #undef CRG_CM
 }
 
+// out[j * ldo + i] = in[i * ldi + j] for i < rows, j < cols: 32 x 32 tiles
+// through shared memory, coalesced on both sides.
+template <class T>
+__global__ void k_transpose(const T* __restrict__ in, int64_t ldi, T* __restrict__ out, int64_t ldo, int64_t rows,
+                            int64_t cols) {
+  __shared__ T tile[32][33];
+  const int64_t bi = (int64_t)blockIdx.y * 32, bj = (int64_t)blockIdx.x * 32;
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int64_t i = bi + k, j = bj + threadIdx.x;
+    if (i < rows && j < cols) tile[k][threadIdx.x] = in[i * ldi + j];
+  }
+  __syncthreads();
+  for (int k = threadIdx.y; k < 32; k += 8) {
+    const int64_t j = bj + k, i = bi + threadIdx.x;
+    if (i < rows && j < cols) out[j * ldo + i] = tile[threadIdx.x][k];
+  }
+}
+
+template <class T>
+void launch_transpose(const T* in, int64_t ldi, T* out, int64_t ldo, int64_t rows, int64_t cols, cudaStream_t st) {
+  for (int64_t r0 = 0; r0 < rows; r0 += 32 * 65535) {
+    const int64_t rr = std::min<int64_t>(rows - r0, 32 * 65535);
+    dim3 grid(nblk(cols, 32), nblk(rr, 32));
+    k_transpose<T><<<grid, dim3(32, 8), 0, st>>>(in + r0 * ldi, ldi, out + r0, ldo, rr, cols);
+  }
+  CRG_CHECK_CUDA(cudaGetLastError());
+}
+
 template <class T>
 void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xsc, int64_t xsf, T* y,
-                int64_t ysc, int64_t ysf, int64_t nf, cudaStream_t st) {
+                int64_t ysc, int64_t ysf, int64_t nf, cudaStream_t st, std::atomic<int>* fm_choice = nullptr);
+
+// Field-major fields through the cell-major kernels: transpose the input to
+// (cells, fields), apply, transpose the output back.  Fields are padded to a
+// multiple of 4 (zeros) so the cell-major path takes its vector kernels.
+template <class T>
+void field_major_via_cells(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xsf, T* y, int64_t ysf,
+                           int64_t nf, cudaStream_t st) {
+  const int64_t nin = c.ncols, nout = c.nrows, nfp = (nf + 3) / 4 * 4;
+  T* xt = nullptr;
+  T* yt = nullptr;
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&xt, sizeof(T) * (nin * nfp + 4), st));
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&yt, sizeof(T) * (nout * nfp + 4), st));
+  if (nfp != nf) CRG_CHECK_CUDA(cudaMemsetAsync(xt, 0, sizeof(T) * nin * nfp, st));
+  launch_transpose<T>(x, xsf, xt, nfp, nf, nin, st);
+  launch_f32<T>(c, normalize, adjoint, xt, nfp, 1, yt, nfp, 1, nfp, st);
+  launch_transpose<T>(yt, nfp, y, ysf, nout, nf, st);
+  CRG_CHECK_CUDA(cudaFreeAsync(xt, st));
+  CRG_CHECK_CUDA(cudaFreeAsync(yt, st));
+}
+
+template <class T>
+void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xsc, int64_t xsf, T* y,
+                int64_t ysc, int64_t ysf, int64_t nf, cudaStream_t st, std::atomic<int>* fm_choice) {
   const int64_t n = c.nrows;
   if (n == 0 || nf == 0) return;
   const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
@@ -912,8 +964,44 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       return;
     }
     if (field_major) {
-      k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xsf, y, ysf, nf);
-      CRG_CHECK_CUDA(cudaGetLastError());
+      auto rows = [&]() {
+        k_fm_rows<T><<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xsf, y, ysf, nf);
+        CRG_CHECK_CUDA(cudaGetLastError());
+      };
+      auto cells = [&]() { field_major_via_cells<T>(c, normalize, adjoint, x, xsf, y, ysf, nf, st); };
+      // With 32 fields or more the field-major gathers may touch many cache
+      // lines per warp (rows whose columns are far apart in the source
+      // numbering); then two transposes around the cell-major kernel win.
+      // The first such apply of a direction times both (twice, after their
+      // first launches) and keeps the faster; during stream capture, or
+      // without a place to keep the choice, the row kernel runs.
+      int choice = (path == SpmmPath::kAuto && nf >= 32 && fm_choice) ? fm_choice->load() : 1;
+      if (choice == 0) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        CRG_CHECK_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone) {
+          choice = 1;
+        } else {
+          cudaEvent_t e[5];
+          for (auto& ev : e) CRG_CHECK_CUDA(cudaEventCreate(&ev));
+          rows();
+          cells();
+          CRG_CHECK_CUDA(cudaEventRecord(e[0], st));
+          rows();
+          CRG_CHECK_CUDA(cudaEventRecord(e[1], st));
+          cells();
+          CRG_CHECK_CUDA(cudaEventRecord(e[2], st));
+          CRG_CHECK_CUDA(cudaEventSynchronize(e[2]));
+          float t_rows = 0.f, t_cells = 0.f;
+          CRG_CHECK_CUDA(cudaEventElapsedTime(&t_rows, e[0], e[1]));
+          CRG_CHECK_CUDA(cudaEventElapsedTime(&t_cells, e[1], e[2]));
+          for (auto& ev : e) cudaEventDestroy(ev);
+          fm_choice->store(t_cells < t_rows ? 2 : 1);
+          return;  // y holds the result of the last variant
+        }
+      }
+      if (choice == 2) cells();
+      else rows();
       return;
     }
   }
@@ -982,6 +1070,8 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   const bool src_host = nin > 0 && !is_device_pointer(src);
   const bool dst_host = !is_device_pointer(dst);
 
+  // the field-major kernel choice of this matrix copy and dtype
+  std::atomic<int>* choice = &r->fm_choice[&c == &r->rev ? 1 : 0][dtype == CRG_BF16 ? 1 : 0];
   // the apply on device buffers
   auto compute = [&](const void* x, int64_t xsc, int64_t xsf, void* y, int64_t ysc, int64_t ysf, int64_t n,
                      cudaStream_t s) {
@@ -995,10 +1085,10 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
       }
       CRG_CHECK_CUDA(cudaGetLastError());
     } else if (dtype == CRG_F32) {
-      launch_f32<float>(c, normalize, adjoint, (const float*)x, xsc, xsf, (float*)y, ysc, ysf, n, s);
+      launch_f32<float>(c, normalize, adjoint, (const float*)x, xsc, xsf, (float*)y, ysc, ysf, n, s, choice);
     } else {
       launch_f32<__nv_bfloat16>(c, normalize, adjoint, (const __nv_bfloat16*)x, xsc, xsf, (__nv_bfloat16*)y, ysc, ysf,
-                                n, s);
+                                n, s, choice);
     }
   };
   if (!src_host && !dst_host) {

@@ -130,6 +130,9 @@ struct crg_regridder {
   size_t stage_bytes = 0;
   cudaStream_t copy_in = nullptr;   // host -> device copies of the chunked host-field pipeline
   cudaStream_t copy_out = nullptr;  // device -> host copies of it
+  // field-major apply per matrix copy (fwd, rev) and dtype (FP32, BF16):
+  // 0 not yet timed, 1 row kernel, 2 transposes around the cell-major kernel
+  std::atomic<int> fm_choice[2][2] = {};
 };
 
 namespace crg {

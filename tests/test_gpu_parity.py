@@ -377,3 +377,28 @@ def test_host_pipeline_matches_device(cuda, K, layout):
         assert np.array_equal(got, ref)
     else:
         assert np.max(np.abs(got - ref)) <= 1e-6 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("dtype,tol", [("float32", 1e-5), ("bfloat16", 2e-2)])
+def test_field_major_both_kernels(cuda, dtype, tol):
+    """Field-major fields with >= 32 fields: the first apply of a direction
+    times the row kernel and the transposes around the cell-major kernel and
+    keeps the faster; every apply (the timed first one and the later ones)
+    matches the FP64 oracle."""
+    import torch
+
+    dst, src = grids.healpix_grid(64), grids.lonlat_regular(1.0, 1.0)
+    R = Regridder(dst, src, normalize=True)
+    O = oracle.OracleRegridder(dst, src, normalize=True)
+    tdt = getattr(torch, dtype)
+    rng = np.random.default_rng(64)
+    for transpose in (False, True):
+        RR = R.transpose() if transpose else R
+        K = 45  # not a multiple of 4: the transposed copy pads to 48
+        Sq = torch.from_numpy(rng.standard_normal((K, RR.shape[1]))).to(tdt)
+        ref = O.apply(Sq.double().numpy(), transpose=transpose)
+        for _ in range(3):
+            y = torch.full((K, RR.shape[0]), float("nan"), dtype=tdt, device="cuda")
+            regrid_(y, RR, Sq.cuda(), dims=2)
+            err = np.max(np.abs(y.double().cpu().numpy() - ref)) / np.max(np.abs(ref))
+            assert err <= tol, (transpose, err)
