@@ -15,6 +15,7 @@ from .grids import (
 from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
 from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
 from .batch import ApplyPlan, build_batch
+from .esmf import esmf_weights, load_esmf_weights, save_esmf_weights
 
 __all__ = [
     "ApplyPlan",
@@ -26,10 +27,12 @@ __all__ = [
     "area_grad",
     "build_batch",
     "cubed_sphere",
+    "esmf_weights",
     "healpix_grid",
     "lonlat_grid",
     "lonlat_jittered",
     "lonlat_regular",
+    "load_esmf_weights",
     "lonlat_tangents",
     "polygon_grid",
     "regrid",
@@ -37,6 +40,7 @@ __all__ = [
     "regrid_adjoint_",
     "regrid_pullback",
     "regular_grid",
+    "save_esmf_weights",
     "split_points",
     "unit_sphere_from_geographic",
 ]

@@ -64,6 +64,59 @@ void export_csr(const DevCsr& c, int32_t base, int64_t* ptr, int64_t* idx, doubl
   CRG_CHECK_CUDA(e);
 }
 
+// ESMF offline weights from the CSC of A (rows of the transposed copy):
+// entry k of source column j gives row = its destination cell, col = j,
+// S = A_ij / a_i (ESMF "destarea" normalisation).
+__global__ void k_esmf_entries(const int32_t* __restrict__ cptr, const int32_t* __restrict__ rows,
+                               const double* __restrict__ val, int64_t ncols, const double* __restrict__ dst_area,
+                               int64_t base, int64_t* __restrict__ row, int64_t* __restrict__ col,
+                               double* __restrict__ S) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= ncols) return;
+  for (int32_t k = cptr[j]; k < cptr[j + 1]; ++k) {
+    const int32_t i = rows[k];
+    row[k] = i + base;
+    col[k] = j + base;
+    S[k] = val[k] / dst_area[i];
+  }
+}
+
+__global__ void k_ratio(const double* __restrict__ a, const double* __restrict__ b, int64_t n, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] / b[i];
+}
+
+void export_esmf(const crg_regridder* r, int32_t base, int64_t* row, int64_t* col, double* S, double* frac_a,
+                 double* frac_b, double* area_a, double* area_b) {
+  CRG_REQUIRE(r != nullptr, CRG_ERR_INVALID_ARGUMENT, "regridder is NULL");
+  CRG_REQUIRE(base == 0 || base == 1, CRG_ERR_INVALID_ARGUMENT, "index_base must be 0 or 1");
+  const int64_t nnz = r->nnz, na = r->ns, nb = r->nd;
+  CRG_REQUIRE(nnz == 0 || (row && col && S), CRG_ERR_INVALID_ARGUMENT, "row, col and S must not be NULL");
+  // device scratch: [nnz] row | [nnz] col | [nnz] S | [na] frac_a | [nb] frac_b
+  char* buf = nullptr;
+  const size_t bytes = sizeof(int64_t) * 2 * nnz + sizeof(double) * (nnz + na + nb) + 64;
+  CRG_CHECK_CUDA(cudaMalloc(&buf, bytes));
+  int64_t* drow = reinterpret_cast<int64_t*>(buf);
+  int64_t* dcol = drow + nnz;
+  double* dS = reinterpret_cast<double*>(dcol + nnz);
+  double* dfa = dS + nnz;
+  double* dfb = dfa + na;
+  if (na) k_esmf_entries<<<(unsigned)((na + 255) / 256), 256>>>(r->rev.ptr, r->rev.idx, r->rev.val, na, r->dst_area,
+                                                                base, drow, dcol, dS);
+  if (na) k_ratio<<<(unsigned)((na + 255) / 256), 256>>>(r->col_sum, r->src_area, na, dfa);
+  if (nb) k_ratio<<<(unsigned)((nb + 255) / 256), 256>>>(r->row_sum, r->dst_area, nb, dfb);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && nnz) e = cudaMemcpy(row, drow, sizeof(int64_t) * nnz, cudaMemcpyDefault);
+  if (e == cudaSuccess && nnz) e = cudaMemcpy(col, dcol, sizeof(int64_t) * nnz, cudaMemcpyDefault);
+  if (e == cudaSuccess && nnz) e = cudaMemcpy(S, dS, sizeof(double) * nnz, cudaMemcpyDefault);
+  if (e == cudaSuccess && frac_a && na) e = cudaMemcpy(frac_a, dfa, sizeof(double) * na, cudaMemcpyDefault);
+  if (e == cudaSuccess && frac_b && nb) e = cudaMemcpy(frac_b, dfb, sizeof(double) * nb, cudaMemcpyDefault);
+  if (e == cudaSuccess && area_a && na) e = cudaMemcpy(area_a, r->src_area, sizeof(double) * na, cudaMemcpyDefault);
+  if (e == cudaSuccess && area_b && nb) e = cudaMemcpy(area_b, r->dst_area, sizeof(double) * nb, cudaMemcpyDefault);
+  cudaFree(buf);
+  CRG_CHECK_CUDA(e);
+}
+
 }  // namespace
 }  // namespace crg
 
@@ -182,6 +235,11 @@ crg_status crg_get_row_col_sums(const crg_regridder* r, double* row_sums, double
     if (row_sums && r->nd) CRG_CHECK_CUDA(cudaMemcpy(row_sums, r->row_sum, sizeof(double) * r->nd, cudaMemcpyDefault));
     if (col_sums && r->ns) CRG_CHECK_CUDA(cudaMemcpy(col_sums, r->col_sum, sizeof(double) * r->ns, cudaMemcpyDefault));
   });
+}
+
+crg_status crg_get_esmf_weights(const crg_regridder* r, int32_t index_base, int64_t* row, int64_t* col, double* S,
+                                double* frac_a, double* frac_b, double* area_a, double* area_b) {
+  return guarded([&] { export_esmf(r, index_base, row, col, S, frac_a, frac_b, area_a, area_b); });
 }
 
 const char* crg_last_error(void) { return g_err; }

@@ -151,6 +151,116 @@ function apply!(y::AbstractArray{T}, A::Union{GB300Sparse,GB300SparseT}, x::Abst
     return y
 end
 
+"""
+    adjoint!(gs, A, gd; normalize = true, dims = 1)
+
+Pullback of `apply!` with respect to the source field: `gs = A' (gd ./ a_d)`
+(or `A gd ./ ...` for a transposed view), through the other stored copy of A.
+"""
+function adjoint!(gs::AbstractArray{T}, A::Union{GB300Sparse,GB300SparseT}, gd::AbstractArray{T};
+                  normalize::Bool = true, dims::Int = 1) where {T<:Union{Float64,Float32}}
+    h, t = A isa GB300SparseT ? (A.parent, Int32(1)) : (A, Int32(0))
+    sx, sy = strides(gd), strides(gs)
+    nf = length(gd) ÷ size(gd, dims)
+    fx = nf == 1 ? 1 : sx[dims == 1 ? 2 : 1]
+    fy = nf == 1 ? 1 : sy[dims == 1 ? 2 : 1]
+    dtype = T === Float64 ? CRG_F64 : CRG_F32
+    check(ccall((:crg_apply_adjoint, libcrg[]), Cint,
+                (Ptr{Cvoid}, Int32, Int32, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Int64, Int32, Ptr{Cvoid}),
+                h.ptr, t, dtype, pointer(gd), sx[dims], fx, pointer(gs), sy[dims], fy, nf, normalize, C_NULL))
+    return gs
+end
+
+"""
+    area_grad(A, dst, src; row_weight, src_field, area_weight) -> Array{Float64}
+
+Cotangent of the destination vertices for `sum_ij u_i s_j dA_ij/dV + sum_i c_i da_i/dV`
+(`crg_area_grad`), laid out like `dst`'s vertex array.  For the rrule of
+`d = regrid(R, s)` with output cotangent `g`: `u = g ./ a`, `c = -g .* d ./ a`
+(unnormalised areas `a`).
+"""
+function area_grad(A::GB300Sparse, dst, src; row_weight = nothing, src_field = nothing, area_weight = nothing)
+    d, keep_d = dst
+    s, keep_s = src
+    g = zeros(Float64, d.kind == 0 ? size(keep_d[1]) : (Int(d.ncells) * Int(d.max_verts) * 3,))
+    ptr(v) = v === nothing ? Ptr{Float64}(C_NULL) : pointer(v)
+    GC.@preserve keep_d keep_s row_weight src_field area_weight begin
+        check(ccall((:crg_area_grad, libcrg[]), Cint,
+                    (Ptr{Cvoid}, Ref{CrgGridDesc}, Ref{CrgGridDesc}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                     Ptr{Float64}, Ptr{Cvoid}),
+                    A.ptr, Ref(d), Ref(s), ptr(row_weight), ptr(src_field), ptr(area_weight), g, C_NULL))
+    end
+    return g
+end
+
+"""
+    build_batch(pairs; normalize = false, nthreads = 0) -> Vector{GB300Sparse}
+
+`crg_build_batch`: many `(dst, src)` descriptor pairs built concurrently.
+"""
+function build_batch(pairs; normalize::Bool = false, nthreads::Integer = 0)
+    n = length(pairs)
+    dd = [p[1][1] for p in pairs]; ds = [p[2][1] for p in pairs]
+    keep = [(p[1][2], p[2][2]) for p in pairs]
+    out = Vector{Ptr{Cvoid}}(undef, n)
+    opts = Ref(CrgBuildOpts(normalize, 0, C_NULL))
+    GC.@preserve keep begin
+        check(ccall((:crg_build_batch, libcrg[]), Cint,
+                    (Int64, Ptr{CrgGridDesc}, Ptr{CrgGridDesc}, Ref{CrgBuildOpts}, Int32, Ptr{Ptr{Cvoid}}),
+                    n, dd, ds, opts, Int32(nthreads), out))
+    end
+    return [GB300Sparse(p) for p in out]
+end
+
+struct CrgApplyItem
+    regridder::Ptr{Cvoid}
+    transpose::Int32; dtype::Int32
+    src::Ptr{Cvoid}; src_stride_cell::Int64; src_stride_field::Int64
+    dst::Ptr{Cvoid}; dst_stride_cell::Int64; dst_stride_field::Int64
+    nfields::Int64
+    normalize::Int32; adjoint::Int32
+end
+
+"""
+    ApplyPlan(items) / launch(plan) / destroy(plan)
+
+`crg_apply_plan_*`: the applies of many regridders (items built from device
+arrays, e.g. `CuArray` pointers) captured as one CUDA graph.
+"""
+mutable struct ApplyPlan
+    ptr::Ptr{Cvoid}
+    function ApplyPlan(items::Vector{CrgApplyItem})
+        out = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:crg_apply_plan_create, libcrg[]), Cint, (Int64, Ptr{CrgApplyItem}, Ref{Ptr{Cvoid}}),
+                    length(items), items, out))
+        p = new(out[])
+        finalizer(p) do x
+            ccall((:crg_apply_plan_destroy, libcrg[]), Cint, (Ptr{Cvoid},), x.ptr)
+        end
+        return p
+    end
+end
+launch(p::ApplyPlan; stream::Ptr{Cvoid} = C_NULL) =
+    check(ccall((:crg_apply_plan_launch, libcrg[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.ptr, stream))
+
+"""
+    esmf_weights(A) -> NamedTuple
+
+`crg_get_esmf_weights`: the arrays `save_esmf_weights` writes (S, row, col,
+frac_a, frac_b, area_a, area_b; 1-based, CSC order), for the reference's
+NCDatasets extension to write.
+"""
+function esmf_weights(A::GB300Sparse)
+    nd, ns = size(A); nnz = Int(A.info.nnz)
+    row = Vector{Int64}(undef, nnz); col = Vector{Int64}(undef, nnz); S = Vector{Float64}(undef, nnz)
+    frac_a = Vector{Float64}(undef, ns); frac_b = Vector{Float64}(undef, nd)
+    area_a = Vector{Float64}(undef, ns); area_b = Vector{Float64}(undef, nd)
+    check(ccall((:crg_get_esmf_weights, libcrg[]), Cint,
+                (Ptr{Cvoid}, Int32, Ptr{Int64}, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                 Ptr{Float64}), A.ptr, 1, row, col, S, frac_a, frac_b, area_a, area_b))
+    return (; S, row, col, frac_a, frac_b, area_a, area_b)
+end
+
 "CSC copy of A with Julia's 1-based indices: the reference's `R.intersections`."
 function SparseArrays.SparseMatrixCSC(A::GB300Sparse)
     nd, ns = size(A)

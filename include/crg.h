@@ -237,6 +237,19 @@ crg_status crg_get_csc(const crg_regridder* r, int32_t index_base, int64_t* colp
 /* The same matrix as CSR (rows = dst cells, columns ascending in each row). */
 crg_status crg_get_csr(const crg_regridder* r, int32_t index_base, int64_t* rowptr, int64_t* colval, double* nzval);
 
+/* The ESMF offline-weights arrays of save_esmf_weights
+ * (ext/ConservativeRegriddingNCDatasetsExt.jl:18-60): entries in CSC order
+ * (source column ascending, destination row ascending inside it, as findnz
+ * returns them), row = destination cell, col = source cell (index_base 1
+ * for ESMF files), S = A_ij / a_i ("destarea" normalisation); frac_a =
+ * column sums of A / source areas, frac_b = row sums / destination areas
+ * (Kahan sums); area_a, area_b = the cell areas.  frac_*, area_* may be NULL.
+ * Host or device pointers.  Like the reference, the weights follow ESMF
+ * conventions for a regridder built without normalize (S and frac_* are the
+ * same either way; the areas are divided by the normaliser). */
+crg_status crg_get_esmf_weights(const crg_regridder* r, int32_t index_base, int64_t* row, int64_t* col, double* S,
+                                double* frac_a, double* frac_b, double* area_a, double* area_b);
+
 /* Per-cell areas R.dst_areas and R.src_areas (src/regridder/regridder.jl:149-150),
  * divided by the normaliser when the regridder was built with normalize. */
 crg_status crg_get_areas(const crg_regridder* r, double* dst_areas, double* src_areas);

@@ -402,3 +402,44 @@ def test_field_major_both_kernels(cuda, dtype, tol):
             regrid_(y, RR, Sq.cuda(), dims=2)
             err = np.max(np.abs(y.double().cpu().numpy() - ref)) / np.max(np.abs(ref))
             assert err <= tol, (transpose, err)
+
+
+def test_concurrent_applies_on_two_streams(cuda):
+    """One handle applied at the same time from two host threads on two
+    streams (read-only matrices, per-call temporaries) gives each thread the
+    result of a lone apply."""
+    import threading
+
+    import torch
+
+    R = Regridder(grids.healpix_grid(64), grids.lonlat_regular(1.0, 1.0), normalize=True)
+    nd, ns = R.shape
+    gen = torch.Generator(device="cuda").manual_seed(4)
+    xs = [torch.randn((ns, 64), generator=gen, device="cuda") for _ in range(2)]
+    refs = []
+    for x in xs:
+        y = torch.empty((nd, 64), device="cuda")
+        regrid_(y, R, x)
+        refs.append(y)
+    torch.cuda.synchronize()
+    outs = [torch.empty((nd, 64), device="cuda") for _ in range(2)]
+    errors = []
+
+    def work(k):
+        try:
+            s = torch.cuda.Stream()
+            with torch.cuda.stream(s):
+                for _ in range(20):
+                    regrid_(outs[k], R, xs[k], stream=s)
+            s.synchronize()
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    for y, ref in zip(outs, refs):
+        assert torch.equal(y, ref)

@@ -89,3 +89,23 @@ def test_transpose_view_swaps_areas_and_temps():
     assert T.shape == (4, 9)
     assert T.src_areas is R.dst_areas and T.dst_areas is R.src_areas
     assert T.src_temp is R.dst_temp and T.dst_temp is R.src_temp
+
+
+def test_esmf_file_round_trip(tmp_path):
+    """ESMF weight-file layout of save_esmf_weights (the reference's NCDatasets
+    extension): dimensions, variables, 1-based indices, global attributes."""
+    from scipy.io import netcdf_file
+
+    from crg.esmf import load_esmf_weights, write_esmf_file
+
+    w = {"S": np.array([0.5, 0.5, 1.0]), "row": np.array([1, 2, 2]), "col": np.array([1, 1, 2]),
+         "frac_a": np.ones(2), "frac_b": np.ones(2), "area_a": np.array([2.0, 1.0]), "area_b": np.array([1.0, 2.0])}
+    path = write_esmf_file(tmp_path / "w.nc", w, "src", "dst", src_shape=(2, 1), dst_shape=(1, 2))
+    f = load_esmf_weights(path)
+    assert np.array_equal(f["matrix"].toarray(), [[0.5, 0.0], [0.5, 1.0]])
+    for k in w:
+        assert np.array_equal(f[k], w[k])
+    with netcdf_file(path, "r", mmap=False) as ds:
+        assert set(ds.dimensions) == {"n_s", "n_a", "n_b"}
+        assert ds.normalization == b"destarea" and ds.source_grid == b"src"
+        assert list(ds.destination_grid_shape) == [1, 2]
