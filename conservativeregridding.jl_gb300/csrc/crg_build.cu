@@ -163,7 +163,8 @@ __device__ __forceinline__ uint32_t sphere_key(double x, double y, double z) {
 // exact ones.
 template <bool kSph>
 __global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restrict__ nv, int maxv, int64_t ncells,
-                            double* __restrict__ area, float4* __restrict__ bound, uint32_t* __restrict__ key) {
+                            double* __restrict__ area, float4* __restrict__ bound, uint32_t* __restrict__ key,
+                            int8_t* __restrict__ ori) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   d3 p[CRG_MAXV];
@@ -173,6 +174,8 @@ __global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restri
     p[k].x = q[0]; p[k].y = q[1]; p[k].z = q[2];
   }
   area[c] = n >= 3 ? cell_area<kSph>(p, n) : 0.0;
+  // the orientation every clip of this cell uses, computed once
+  ori[c] = (int8_t)((n >= 3 ? (kSph ? orient_sph(p, n) : orient_pl(p, n)) : 1.0) > 0.0 ? 1 : -1);
   if (kSph) {
     double sx = 0, sy = 0, sz = 0;
     for (int k = 0; k < n; ++k) { sx += p[k].x; sy += p[k].y; sz += p[k].z; }
@@ -466,8 +469,10 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 
 template <bool kSph>
 __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
-                                              const int8_t* __restrict__ dnv, int dmaxv, const double* __restrict__ sv,
-                                              const int8_t* __restrict__ snv, int smaxv, double* __restrict__ area,
+                                              const int8_t* __restrict__ dnv, const int8_t* __restrict__ dori,
+                                              int dmaxv, const double* __restrict__ sv,
+                                              const int8_t* __restrict__ snv, const int8_t* __restrict__ sori,
+                                              int smaxv, double* __restrict__ area,
                                               int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt,
                                               unsigned long long* __restrict__ overflow) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -480,11 +485,11 @@ __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int
   for (int k = 0; k < nd; ++k) { clip[k].x = q[3 * k]; clip[k].y = q[3 * k + 1]; clip[k].z = q[3 * k + 2]; }
   q = sv + (int64_t)pr.y * smaxv * 3;
   for (int k = 0; k < ns; ++k) { bufA[k].x = q[3 * k]; bufA[k].y = q[3 * k + 1]; bufA[k].z = q[3 * k + 2]; }
-  double sig = kSph ? orient_sph(bufA, ns) : orient_pl(bufA, ns);
+  const double sig = sori[pr.y];  // the subject's orientation (k_cell_geom)
   double a = 0.0;
   if (nd >= 3 && ns >= 3) {
     d3* res;
-    int m = clip_polygon<kSph>(bufA, bufB, ns, clip, nd, &res);
+    int m = clip_polygon_oriented<kSph>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res);
     if (m < 0) {
       atomicAdd(overflow, 1ull);
     } else {
@@ -689,6 +694,7 @@ struct DevGrid {
   CellTable tab;
   DBuf<double> v;
   DBuf<int8_t> nv;
+  DBuf<int8_t> ori;
   int64_t ncells = 0;
 };
 
@@ -773,6 +779,8 @@ void upload_grid(const crg_grid_desc* g, DevGrid& out, cudaStream_t st) {
   }
   out.tab.v = out.v.p;
   out.tab.nv = out.nv.p;
+  out.ori.alloc((size_t)out.tab.n, st);  // filled with the cell geometry
+  out.tab.ori = out.ori.p;
 }
 
 struct HostTree {
@@ -790,10 +798,12 @@ void build_tree(const DevGrid& g, bool sph, double* area_out, HostTree& h, cudaS
   h.key.alloc((size_t)n, st);
   if (n == 0) return;
   if (sph) {
-    k_cell_geom<true><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p);
+    k_cell_geom<true><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p,
+                                                     g.tab.ori);
     CRG_CHECK_CUDA(cudaGetLastError());
   } else {
-    k_cell_geom<false><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p);
+    k_cell_geom<false><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p,
+                                                      g.tab.ori);
     CRG_CHECK_CUDA(cudaGetLastError());
     int64_t nb = nblk(n, 256);
     DBuf<float4> part((size_t)nb, st);
@@ -1055,11 +1065,13 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     ovf.zero();
     if (nc) {
       if (sph)
-        k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.maxv, gs.tab.v, gs.tab.nv,
-                                                    gs.tab.maxv, area.p, rowcnt.p, colcnt.p, ovf.p);
+        k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv, gs.tab.v,
+                                                    gs.tab.nv, gs.tab.ori, gs.tab.maxv, area.p, rowcnt.p, colcnt.p,
+                                                    ovf.p);
       else
-        k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.maxv, gs.tab.v, gs.tab.nv,
-                                                     gs.tab.maxv, area.p, rowcnt.p, colcnt.p, ovf.p);
+        k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv,
+                                                     gs.tab.v, gs.tab.nv, gs.tab.ori, gs.tab.maxv, area.p, rowcnt.p,
+                                                     colcnt.p, ovf.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[2], st));

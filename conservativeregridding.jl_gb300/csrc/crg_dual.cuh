@@ -127,8 +127,8 @@ __device__ __forceinline__ D3n<N> isect_sph_n(const D3n<N>& a, const Dn<N>& sa, 
   if (sb.v == 0.0) return b;
   const Dn<N> wa = dn_abs(sb), wb = dn_abs(sa);
   D3n<N> x{dn_fma(wb, b.x, dn_mul(wa, a.x)), dn_fma(wb, b.y, dn_mul(wa, a.y)), dn_fma(wb, b.z, dn_mul(wa, a.z))};
-  const Dn<N> r = dn_sqrt(d3n_dot(x, x));
-  return D3n<N>{dn_div(x.x, r), dn_div(x.y, r), dn_div(x.z, r)};
+  const Dn<N> ir = dn_div(dn_const<N>(1.0), dn_sqrt(d3n_dot(x, x)));
+  return D3n<N>{dn_mul(x.x, ir), dn_mul(x.y, ir), dn_mul(x.z, ir)};
 }
 
 // 2 arg(prod (D + iN)); d atan2(y, x) = (x dy - y dx) / (x^2 + y^2)

@@ -13,7 +13,8 @@
 //    differences are taken first so that short edges keep full relative
 //    precision.
 //  * crossing of segment a->b with the clip plane: x = |s_a| b + |s_b| a
-//    (both weights non-negative, so x lies on the minor arc), then normalised.
+//    (both weights non-negative, so x lies on the minor arc), then normalised
+//    by one reciprocal square root taken as 1 / sqrt and three products.
 //  * polygon solid angle: fan from vertex 0; each triangle contributes the
 //    complex factor D + iN of Van Oosterom & Strackee (1983),
 //    N = a.((b-a) x (c-a)) = a.(b x c), D = 1 + a.b + b.c + c.a; the area is
@@ -215,8 +216,9 @@ __device__ __forceinline__ d3 isect_sph(d3 a, double sa, d3 b, double sb) {
   x.x = fma(wb, b.x, wa * a.x);
   x.y = fma(wb, b.y, wa * a.y);
   x.z = fma(wb, b.z, wa * a.z);
-  double r = sqrt(ddot(x, x));
-  x.x = x.x / r; x.y = x.y / r; x.z = x.z / r;
+  // one reciprocal and three products: FP64 division is a long instruction sequence
+  const double ir = 1.0 / sqrt(ddot(x, x));
+  x.x = x.x * ir; x.y = x.y * ir; x.z = x.z * ir;
   return x;
 }
 
@@ -275,15 +277,15 @@ __device__ __forceinline__ d3 isect_pl(d3 a, double sa, d3 b, double sb) {
 // ---------------------------------------------------------------- clip
 
 // Sutherland-Hodgman clip of `subj` (ns vertices, copied into buf A) by the
-// convex polygon `clip` (nc vertices).  Ping-pongs between bufA and bufB;
+// convex polygon `clip` (nc vertices) of orientation `sig` (+1 / -1).  Ping-pongs between bufA and bufB;
 // returns the vertex count and sets *res to the buffer holding the result, or
 // returns -1 if a stage would exceed CRG_MAXC vertices.
 template <bool kSpherical>
-__device__ __forceinline__ int clip_polygon(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, d3** res) {
+__device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, double sig,
+                                                     d3** res) {
   d3* in = bufA;
   d3* out = bufB;
   int n = ns;
-  double sig = kSpherical ? orient_sph(clip, nc) : orient_pl(clip, nc);
   for (int k = 0; k < nc && n > 0; ++k) {
     d3 ca = clip[k], cb = clip[k + 1 == nc ? 0 : k + 1];
     const int isig = sig < 0.0 ? -1 : 1;
@@ -322,6 +324,13 @@ __device__ __forceinline__ int clip_polygon(d3* bufA, d3* bufB, int ns, const d3
   }
   *res = in;
   return n;
+}
+
+// clip_polygon_oriented with the clip polygon's orientation computed here
+template <bool kSpherical>
+__device__ __forceinline__ int clip_polygon(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, d3** res) {
+  const double sig = kSpherical ? orient_sph(clip, nc) : orient_pl(clip, nc);
+  return clip_polygon_oriented<kSpherical>(bufA, bufB, ns, clip, nc, sig, res);
 }
 
 template <bool kSpherical>

@@ -95,6 +95,7 @@ struct CellTable {
   int maxv = 0;
   double* v = nullptr;   // [n * maxv * 3]
   int8_t* nv = nullptr;  // [n]
+  int8_t* ori = nullptr;  // [n] +1 counter-clockwise seen from outside (or from +z), -1 clockwise
 };
 
 // Device memory a regridder keeps, allocated in stream order (no device-wide

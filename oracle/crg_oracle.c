@@ -228,8 +228,10 @@ static inline v3 og_isect_sph(v3 a, double sa, v3 b, double sb) {
     x.x = fma(wb, b.x, wa * a.x);
     x.y = fma(wb, b.y, wa * a.y);
     x.z = fma(wb, b.z, wa * a.z);
-    double r = sqrt(og_dot(x, x));
-    x.x = x.x / r; x.y = x.y / r; x.z = x.z / r;
+    /* normalised with one reciprocal and three products (one rounding more
+       than three quotients, and the same sequence as the GPU coding) */
+    double ir = 1.0 / sqrt(og_dot(x, x));
+    x.x = x.x * ir; x.y = x.y * ir; x.z = x.z * ir;
     return x;
 }
 
