@@ -16,6 +16,7 @@ from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
 from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
 from .batch import ApplyPlan, build_batch
 from .esmf import esmf_weights, load_esmf_weights, save_esmf_weights
+from .fold import mirror_fold_
 
 __all__ = [
     "ApplyPlan",
@@ -34,6 +35,7 @@ __all__ = [
     "lonlat_regular",
     "load_esmf_weights",
     "lonlat_tangents",
+    "mirror_fold_",
     "polygon_grid",
     "regrid",
     "regrid_",

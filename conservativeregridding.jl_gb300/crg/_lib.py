@@ -110,6 +110,8 @@ SIGNATURES = {
     "crg_apply_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "crg_apply_plan_destroy": (C.c_int, [C.c_void_p]),
     "crg_get_csc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_mirror_fold": (C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                  C.c_void_p]),
     "crg_get_esmf_weights": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_csr": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),

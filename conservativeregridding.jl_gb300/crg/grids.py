@@ -201,6 +201,52 @@ def convex_cells(g: Grid) -> np.ndarray:
     return ~(pos & neg)
 
 
+# ----------------------------------------------------------------- folded (tripolar) grids
+
+def folded_lonlat(nx: int, ny: int, fold_lat: float, name: str = "") -> Grid:
+    """A RightCenterFolded global grid with the geometry of a tripolar ocean
+    grid's fold: ny-1 lon-lat rows from the south pole up to latitude
+    ``fold_lat``, then a fold row whose top vertex row is its bottom row
+    reversed, so that fold cells i and nx+1-i (1-based) are the same
+    quadrilateral (a strip of the cap above ``fold_lat`` between two chords).
+    Every physical cell of the fold row has two slots, as in the reference's
+    folded Oceananigans grids (ext/ConservativeRegriddingOceananigansExt.jl:117-175)."""
+    if nx % 4:
+        raise ValueError("nx must be a multiple of 4")
+    lon = np.linspace(0.0, 360.0, nx + 1)
+    lat = np.linspace(-90.0, fold_lat, ny)
+    LON, LAT = np.meshgrid(lon, lat)
+    pts = unit_sphere_from_geographic(LON, LAT)           # (ny, nx+1, 3)
+    top = pts[-1][::-1][None]                             # the fold: top row = bottom row reversed
+    return Grid("curvilinear", SPHERICAL, blocks=[np.concatenate([pts, top], axis=0)], full_sphere=True,
+                name=name or f"folded_{nx}x{ny}")
+
+
+def fold_primaries(nx: int) -> np.ndarray:
+    """1-based fold-row slots that keep the cells: 1..nx/4 and nx/2+1..nx/2+nx/4;
+    slot r's partner is nx+1-r."""
+    nq, nh = nx // 4, nx // 2
+    return np.concatenate([np.arange(1, nq + 1), np.arange(nh + 1, nh + nq + 1)])
+
+
+def fold_ghosts(g: Grid) -> Grid:
+    """The per-cell polygons of a one-block RightCenterFolded grid with the
+    fold-row partner slots made ghosts (0 vertices: no area, never a
+    candidate), numbered like the grid (i + j*nx)."""
+    if g.kind != "curvilinear" or len(g.blocks) != 1:
+        raise ValueError("fold_ghosts takes a one-block curvilinear grid")
+    t, _ = g.cell_table()
+    ny1, nx1 = g.blocks[0].shape[:2]
+    nx, ny = nx1 - 1, ny1 - 1
+    if nx % 4:
+        raise ValueError("nx must be a multiple of 4")
+    nv = np.full(t.shape[0], t.shape[1], np.int32)
+    keep = np.zeros(nx, bool)
+    keep[fold_primaries(nx) - 1] = True
+    nv[(ny - 1) * nx + np.flatnonzero(~keep)] = 0
+    return Grid("cells", g.manifold, cells=t.copy(), nverts=nv, full_sphere=g.full_sphere, name=g.name + "_ghosts")
+
+
 # ----------------------------------------------------------------- cubed sphere
 
 def _cube_face(f: int, a: np.ndarray, b: np.ndarray) -> np.ndarray:

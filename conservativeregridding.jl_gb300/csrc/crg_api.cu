@@ -237,6 +237,11 @@ crg_status crg_get_row_col_sums(const crg_regridder* r, double* row_sums, double
   });
 }
 
+crg_status crg_mirror_fold(int32_t dtype, void* field, int64_t stride_cell, int64_t stride_field, int64_t nfields,
+                           int64_t nx, int64_t ny, void* stream) {
+  return guarded([&] { mirror_fold_impl(dtype, field, stride_cell, stride_field, nfields, nx, ny, (cudaStream_t)stream); });
+}
+
 crg_status crg_get_esmf_weights(const crg_regridder* r, int32_t index_base, int64_t* row, int64_t* col, double* S,
                                 double* frac_a, double* frac_b, double* area_a, double* area_b) {
   return guarded([&] { export_esmf(r, index_base, row, col, S, frac_a, frac_b, area_a, area_b); });

@@ -1192,6 +1192,63 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   CRG_CHECK_CUDA(cudaStreamSynchronize(st));
 }
 
+// ------------------------------------------------------------------ folded grids
+
+namespace {
+
+// Fold row of a RightCenterFolded (tripolar) grid, cells numbered i + j * nx:
+// the primary slots r = 1..nq and nh+1..nh+nq (1-based) hold the values, their
+// partners nx+1-r are ghost slots of the same physical cells and get a copy.
+template <class T>
+__global__ void k_mirror_fold(T* __restrict__ f, int64_t sc, int64_t sf, int64_t nfields, int64_t nx, int64_t nq,
+                              int64_t nh, int64_t off) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t k = blockIdx.y;
+  if (q >= 2 * nq || k >= nfields) return;
+  const int64_t r = q < nq ? q + 1 : q - nq + nh + 1;
+  f[(off + nx - r) * sc + k * sf] = f[(off + r - 1) * sc + k * sf];
+}
+
+template <class T>
+void mirror_host(T* f, int64_t sc, int64_t sf, int64_t nfields, int64_t nx, int64_t nq, int64_t nh, int64_t off) {
+  for (int64_t k = 0; k < nfields; ++k)
+    for (int64_t q = 0; q < 2 * nq; ++q) {
+      const int64_t r = q < nq ? q + 1 : q - nq + nh + 1;
+      f[(off + nx - r) * sc + k * sf] = f[(off + r - 1) * sc + k * sf];
+    }
+}
+
+}  // namespace
+
+void mirror_fold_impl(int dtype, void* field, int64_t sc, int64_t sf, int64_t nfields, int64_t nx, int64_t ny,
+                      cudaStream_t st) {
+  CRG_REQUIRE(dtype == CRG_F64 || dtype == CRG_F32 || dtype == CRG_BF16, CRG_ERR_INVALID_ARGUMENT, "unknown dtype %d",
+              dtype);
+  CRG_REQUIRE(nx > 0 && ny > 0 && nx % 4 == 0, CRG_ERR_INVALID_ARGUMENT,
+              "a folded grid needs nx a positive multiple of 4 (got nx = %lld, ny = %lld)", (long long)nx,
+              (long long)ny);
+  CRG_REQUIRE(field != nullptr && sc > 0 && nfields >= 1 && (nfields == 1 || sf > 0), CRG_ERR_INVALID_ARGUMENT,
+              "field pointer, strides or field count invalid");
+  CRG_REQUIRE(nfields <= 65535 || !is_device_pointer(field), CRG_ERR_NOT_SUPPORTED, "at most 65535 fields per call");
+  const int64_t nq = nx / 4, nh = nx / 2, off = (ny - 1) * nx;
+  if (!is_device_pointer(field)) {
+    // the caller's queued work on this field comes first (nothing can be queued without a device)
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) cudaGetLastError();
+    else CRG_CHECK_CUDA(e);
+    if (dtype == CRG_F64) mirror_host((double*)field, sc, sf, nfields, nx, nq, nh, off);
+    else if (dtype == CRG_F32) mirror_host((float*)field, sc, sf, nfields, nx, nq, nh, off);
+    else mirror_host((__nv_bfloat16*)field, sc, sf, nfields, nx, nq, nh, off);
+    return;
+  }
+  dim3 grid(nblk(2 * nq, 128), (unsigned)nfields);
+  if (dtype == CRG_F64) k_mirror_fold<double><<<grid, 128, 0, st>>>((double*)field, sc, sf, nfields, nx, nq, nh, off);
+  else if (dtype == CRG_F32) k_mirror_fold<float><<<grid, 128, 0, st>>>((float*)field, sc, sf, nfields, nx, nq, nh, off);
+  else
+    k_mirror_fold<__nv_bfloat16><<<grid, 128, 0, st>>>((__nv_bfloat16*)field, sc, sf, nfields, nx, nq, nh, off);
+  CRG_CHECK_CUDA(cudaGetLastError());
+}
+
 }  // namespace crg
 
 // ------------------------------------------------------------------ allocation-free apply

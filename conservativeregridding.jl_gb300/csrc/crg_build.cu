@@ -102,7 +102,8 @@ __global__ void k_expand_cells(const double* __restrict__ cv, const int32_t* __r
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   int n = cn ? cn[c] : maxv;
-  if (n < 3 || n > maxv) {
+  // 0 vertices: a ghost slot (no geometry, no area, never a candidate)
+  if ((n != 0 && n < 3) || n > maxv) {
     atomicAdd(bad, 1);
     n = n < 3 ? 0 : maxv;
   }
@@ -176,6 +177,11 @@ __global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restri
   area[c] = n >= 3 ? cell_area<kSph>(p, n) : 0.0;
   // the orientation every clip of this cell uses, computed once
   ori[c] = (int8_t)((n >= 3 ? (kSph ? orient_sph(p, n) : orient_pl(p, n)) : 1.0) > 0.0 ? 1 : -1);
+  if (n == 0) {  // a ghost slot: a bound that overlaps nothing (negative radius / inverted box)
+    bound[c] = kSph ? make_float4(0.f, 0.f, 1.f, -4.f) : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
+    if (kSph) key[c] = sphere_key(0.0, 0.0, 1.0);
+    return;
+  }
   if (kSph) {
     double sx = 0, sy = 0, sz = 0;
     for (int k = 0; k < n; ++k) { sx += p[k].x; sy += p[k].y; sz += p[k].z; }
@@ -418,7 +424,7 @@ __device__ __forceinline__ bool cell_test(float4 a, float4 b) {
     float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
     float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     float r = a.w + b.w;
-    return d2 <= r * r * 1.000002f;
+    return r >= 0.f && d2 <= r * r * 1.000002f;  // a ghost slot's negative radius meets nothing
   }
   return a.x <= b.z && b.x <= a.z && a.y <= b.w && b.y <= a.w;
 }
@@ -773,7 +779,8 @@ void upload_grid(const crg_grid_desc* g, DevGrid& out, cudaStream_t st) {
     int32_t hbad = 0;
     CRG_CHECK_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-    CRG_REQUIRE(hbad == 0, CRG_ERR_INVALID_ARGUMENT, "%d cells have a vertex count outside 3..max_verts", hbad);
+    CRG_REQUIRE(hbad == 0, CRG_ERR_INVALID_ARGUMENT, "%d cells have a vertex count outside 3..max_verts (or 0)",
+                hbad);
   } else {
     CRG_REQUIRE(false, CRG_ERR_INVALID_ARGUMENT, "unknown grid kind %d", g->kind);
   }

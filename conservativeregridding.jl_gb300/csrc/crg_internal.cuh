@@ -150,6 +150,8 @@ void build_merge_path(DevCsr& c, cudaStream_t st);
 void free_tiles(DevTiles& t);
 void area_grad_impl(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src, const double* u,
                     const double* s, const double* c, double* grad, cudaStream_t st);
+void mirror_fold_impl(int dtype, void* field, int64_t sc, int64_t sf, int64_t nfields, int64_t nx, int64_t ny,
+                      cudaStream_t st);
 void build_batch_impl(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
                       int nthreads, crg_regridder** out);
 crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items);

@@ -237,6 +237,21 @@ crg_status crg_get_csc(const crg_regridder* r, int32_t index_base, int64_t* colp
 /* The same matrix as CSR (rows = dst cells, columns ascending in each row). */
 crg_status crg_get_csr(const crg_regridder* r, int32_t index_base, int64_t* rowptr, int64_t* colval, double* nzval);
 
+/* Folded (tripolar) grids, RightCenterFolded: in the top cell row (j = ny,
+ * 1-based) cell i and cell nx+1-i are the same physical quadrilateral.  As in
+ * the reference (ext/ConservativeRegriddingOceananigansExt.jl:117-175), the
+ * grid handed to crg_build keeps one slot of each pair as a real cell (slots
+ * 1..nx/4 and nx/2+1..nx/2+nx/4) and makes the partner a ghost: a
+ * CRG_GRID_CELLS cell with 0 vertices, which has no area and is never a
+ * candidate.  After an apply to such a destination, crg_mirror_fold copies
+ * each primary's value into its partner (the reference's
+ * mirror_fold_partners!, :205-240), for every field: cells are numbered
+ * i + j * nx, the field is (cells, fields) with the given strides, nx is a
+ * multiple of 4.  Device pointers run a kernel on `stream`; host pointers are
+ * copied on the host after the stream's work. */
+crg_status crg_mirror_fold(int32_t dtype, void* field, int64_t stride_cell, int64_t stride_field, int64_t nfields,
+                           int64_t nx, int64_t ny, void* stream);
+
 /* The ESMF offline-weights arrays of save_esmf_weights
  * (ext/ConservativeRegriddingNCDatasetsExt.jl:18-60): entries in CSC order
  * (source column ascending, destination row ascending inside it, as findnz

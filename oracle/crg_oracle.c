@@ -657,6 +657,13 @@ static og_ext og_poly_extent(const og_tree* t, int64_t idx) {
     v3 v[OG_MAXV];
     int n = og_cell_verts(t->g, idx, v);
     og_ext e;
+    if (n == 0) {
+        /* a cell without vertices (a ghost slot, like the padding cells of the
+           reference's folded grids) is in no extent: no pair ever tests true */
+        e.c.x = e.c.y = 0; e.c.z = 1; e.r = -INFINITY;
+        e.xmin = e.ymin = INFINITY; e.xmax = e.ymax = -INFINITY;
+        return e;
+    }
     if (!t->spherical) {
         e.xmin = INFINITY; e.xmax = -INFINITY; e.ymin = INFINITY; e.ymax = -INFINITY;
         for (int k = 0; k < n; ++k) {
