@@ -4,12 +4,16 @@ from ._lib import ArgumentError, CrgError, DimensionMismatch
 from .grids import (
     Grid,
     cubed_sphere,
+    full_clenshaw_grid,
+    full_gaussian_grid,
+    full_ring_grid,
     healpix_grid,
     lonlat_grid,
     lonlat_jittered,
     lonlat_regular,
     polygon_grid,
     regular_grid,
+    reorder_cells,
     unit_sphere_from_geographic,
 )
 from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
@@ -28,6 +32,9 @@ __all__ = [
     "area_grad",
     "build_batch",
     "cubed_sphere",
+    "full_clenshaw_grid",
+    "full_gaussian_grid",
+    "full_ring_grid",
     "esmf_weights",
     "healpix_grid",
     "lonlat_grid",
@@ -42,6 +49,7 @@ __all__ = [
     "regrid_adjoint_",
     "regrid_pullback",
     "regular_grid",
+    "reorder_cells",
     "save_esmf_weights",
     "split_points",
     "unit_sphere_from_geographic",

@@ -201,6 +201,60 @@ def convex_cells(g: Grid) -> np.ndarray:
     return ~(pos & neg)
 
 
+# ----------------------------------------------------------------- reordered and ring grids
+
+def reorder_cells(g: Grid, order, name: str = "") -> Grid:
+    """Cell k of the result is cell ``order[k]`` of ``g`` (same vertex ring):
+    any numbering of a grid's cells, as the reference's reordered quadtree
+    cursors give (src/trees/specialized_quadtree_cursors.jl:152-270), as
+    per-cell polygons."""
+    t, nv = g.cell_table()
+    order = np.asarray(order, np.int64)
+    if order.ndim != 1 or len(order) != len(t) or not np.array_equal(np.sort(order), np.arange(len(t))):
+        raise ValueError("order must be a permutation of the cell indices")
+    return Grid("cells", g.manifold, cells=t[order].copy(), nverts=np.asarray(nv)[order].copy(),
+                full_sphere=g.full_sphere, name=name or g.name + "_reordered")
+
+
+def full_ring_grid(latd, lond, name: str = "") -> Grid:
+    """A RingGrids full grid (rings of equal longitude spacing) from its ring
+    latitudes ``latd`` (north to south) and longitudes ``lond``, as the
+    reference's RingGrids extension builds it (ext/ConservativeRegriddingRingGridsExt.jl:21-48):
+    latitude edges halfway between rings and pinned to the poles, longitude
+    edges half a cell either side of ``lond``, cells numbered ring by ring from
+    the north (east within a ring)."""
+    latd = np.asarray(latd, np.float64)
+    lond = np.asarray(lond, np.float64)
+    nlat, nlon = len(latd), len(lond)
+    lat_edges = np.empty(nlat + 1)
+    lat_edges[0], lat_edges[-1] = 90.0, -90.0
+    lat_edges[1:-1] = 0.5 * (latd[:-1] + latd[1:])
+    dlon = 360.0 / nlon
+    lon_edges = lond[0] - dlon / 2 + dlon * np.arange(nlon + 1)
+    g = lonlat_grid(lon_edges, lat_edges[::-1], full_sphere=True)   # south to north: counter-clockwise cells
+    ring = np.arange(nlat)[:, None]                                  # 0 = northernmost
+    order = ((nlat - 1 - ring) * nlon + np.arange(nlon)[None, :]).ravel()
+    return reorder_cells(g, order, name=name or f"ring_{nlon}x{nlat}")
+
+
+def full_clenshaw_grid(nlat_half: int) -> Grid:
+    """Full Clenshaw-Curtis grid: 2*nlat_half - 1 rings at equally spaced
+    colatitudes j*180/(2*nlat_half) (j = 1..2*nlat_half-1, the equator
+    included, no pole rings), 4*nlat_half points per ring from longitude 0."""
+    nlat, nlon = 2 * nlat_half - 1, 4 * nlat_half
+    latd = 90.0 - np.arange(1, nlat + 1) * 180.0 / (nlat + 1)
+    return full_ring_grid(latd, np.arange(nlon) * 360.0 / nlon, name=f"full_clenshaw_{nlat_half}")
+
+
+def full_gaussian_grid(nlat_half: int) -> Grid:
+    """Full Gaussian grid: 2*nlat_half rings at the Gauss-Legendre latitudes,
+    4*nlat_half points per ring from longitude 0."""
+    nlat, nlon = 2 * nlat_half, 4 * nlat_half
+    x, _ = np.polynomial.legendre.leggauss(nlat)
+    latd = np.degrees(np.arcsin(x))[::-1]                             # north to south
+    return full_ring_grid(latd, np.arange(nlon) * 360.0 / nlon, name=f"full_gaussian_{nlat_half}")
+
+
 # ----------------------------------------------------------------- folded (tripolar) grids
 
 def folded_lonlat(nx: int, ny: int, fold_lat: float, name: str = "") -> Grid:

@@ -67,6 +67,10 @@ CASES = {
     "jittered_cs_to_lonlat2": lambda: (grids.cubed_sphere(16, jitter=0.15, seed=5), grids.lonlat_regular(2.0, 2.0)),
     "coincident_lonlat4_lonlat2": lambda: (grids.lonlat_regular(4.0, 4.0), grids.lonlat_regular(2.0, 2.0)),
     "identical_healpix8": lambda: (grids.healpix_grid(8), grids.healpix_grid(8)),
+    # RingGrids full grids (cells numbered ring by ring from the north) and a permuted numbering
+    "full_clenshaw12_to_full_gaussian16": lambda: (grids.full_gaussian_grid(16), grids.full_clenshaw_grid(12)),
+    "reordered_lonlat5_to_healpix8": lambda: (grids.healpix_grid(8), grids.reorder_cells(
+        grids.lonlat_regular(5.0, 5.0), np.random.default_rng(5).permutation(72 * 36))),
     # rows of ~400 and ~8,100 entries: the shared-memory and global-memory row sorts
     "lonlat10_from_lonlat0.5": lambda: (grids.lonlat_regular(10.0, 10.0), grids.lonlat_regular(0.5, 0.5)),
     "lonlat45_from_lonlat0.5": lambda: (grids.lonlat_regular(45.0, 45.0), grids.lonlat_regular(0.5, 0.5)),
