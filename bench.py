@@ -56,9 +56,10 @@ def parse():
     p.add_argument("--pair", default="c5", choices=["c5", "identity"],
                    help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
                         "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
-    p.add_argument("--workload", default="c5", choices=["c5", "c3"],
+    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1"],
                    help="c5: the headline (HEALPix 256 <-> 0.25 degree, 128 fields); c3: 32 jittered lon-lat "
-                        "pairs of uneven resolution built as one batch and applied as one CUDA graph")
+                        "pairs of uneven resolution built as one batch and applied as one CUDA graph; c1: the "
+                        "small FP64 case (2 degree -> shifted 3 degree lon-lat), build and plain FP64 apply")
     return p.parse_args()
 
 
@@ -607,6 +608,53 @@ def run_c3(a):
     }
 
 
+# ----------------------------------------------------------------- small FP64 workload
+
+def run_c1(a):
+    """2-degree lon-lat source, 3-degree destination shifted by (+0.7, +0.4)
+    degrees with latitude edges clamped to the poles; normalize = true; one
+    FP64 field U[0, 1).  Build pairs/s and candidates/s (median of 20 builds),
+    FP64 apply GB/s (bytes 12 nnz + 4 (rows + 1) + 8 (cols + rows) + 8 rows)."""
+    import torch
+
+    from crg import Regridder, grids, regrid_
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    src = grids.lonlat_regular(2.0, 2.0)
+    dst = grids.lonlat_grid(0.7 + 3 * np.arange(121), np.clip(-89.6 + 3 * np.arange(61), -90, 90))
+    Regridder(dst, src, normalize=True)
+    times = []
+    for _ in range(20):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        R = Regridder(dst, src, normalize=True)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    tb = statistics.median(times)
+    nd, ns = R.shape
+    s = torch.rand(ns, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(1))
+    d = torch.empty(nd, dtype=torch.float64, device=dev)
+    for _ in range(max(a.warmup, 3)):
+        regrid_(d, R, s)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 200
+    e0.record(stream)
+    for _ in range(reps):
+        regrid_(d, R, s)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = 12 * R.nnz + 4 * (nd + 1) + 8 * (ns + nd) + 8 * nd
+    return {"metric": "small FP64 build pairs/s and apply GB/s", "workload": "lonlat 2deg -> lonlat 3deg shifted, fp64",
+            "n_dst": nd, "n_src": ns, "nnz": R.nnz, "candidates": R.info["n_candidates"],
+            "build": {"ms_median": round(tb * 1e3, 3), "pairs_per_s": round(R.nnz / tb, 1),
+                      "candidates_per_s": round(R.info["n_candidates"] / tb, 1)},
+            "apply_fp64": {"ms": round(ms, 4), "GB/s": round(nbytes / (ms * 1e-3) / 1e9, 2),
+                           "note": "one launch of ~16 K rows: launch-latency bound"}}
+
+
 # ----------------------------------------------------------------- CPU legs (oracle)
 
 def cpu_baseline(hp, ll, K, sample_fields):
@@ -684,9 +732,9 @@ def main():
     if a.profile:
         run_profile(a)
         return
-    if a.workload == "c3":
+    if a.workload in ("c3", "c1"):
         if rank == 0:
-            print(json.dumps(run_c3(a)))
+            print(json.dumps(run_c3(a) if a.workload == "c3" else run_c1(a)))
         return
     if a.impl == "reference":
         if rank == 0:

@@ -473,6 +473,23 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 
 // ------------------------------------------------------------------ K4: clip + area
 
+// Every destination edge's half-space, once per cell (the clip of each pair reads it).
+__global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __restrict__ nv,
+                              const int8_t* __restrict__ ori, int maxv, int64_t ncells, double4* __restrict__ planes) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  const int n = nv[c];
+  const double* q = v + c * maxv * 3;
+  for (int k = 0; k < n; ++k) {
+    const int k1 = k + 1 == n ? 0 : k + 1;
+    d3 nrm;
+    double eb;
+    edge_plane(d3{q[3 * k], q[3 * k + 1], q[3 * k + 2]}, d3{q[3 * k1], q[3 * k1 + 1], q[3 * k1 + 2]}, (double)ori[c],
+               nrm, eb);
+    planes[c * maxv + k] = make_double4(nrm.x, nrm.y, nrm.z, eb);
+  }
+}
+
 template <bool kSph>
 __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
                                               const int8_t* __restrict__ dnv, const int8_t* __restrict__ dori,
@@ -480,7 +497,8 @@ __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int
                                               const int8_t* __restrict__ snv, const int8_t* __restrict__ sori,
                                               int smaxv, double* __restrict__ area,
                                               int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt,
-                                              unsigned long long* __restrict__ overflow) {
+                                              unsigned long long* __restrict__ overflow,
+                                              const double4* __restrict__ dplanes) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
   int2 pr = cand[t];
@@ -495,7 +513,8 @@ __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int
   double a = 0.0;
   if (nd >= 3 && ns >= 3) {
     d3* res;
-    int m = clip_polygon_oriented<kSph>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res);
+    int m = clip_polygon_oriented<kSph>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res,
+                                        kSph ? dplanes + (int64_t)pr.x * dmaxv : nullptr);
     if (m < 0) {
       atomicAdd(overflow, 1ull);
     } else {
@@ -1071,14 +1090,19 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     colcnt.zero();
     ovf.zero();
     if (nc) {
-      if (sph)
+      if (sph) {
+        DBuf<double4> planes((size_t)nd * gd.tab.maxv, st);
+        if (nd) {
+          k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv, nd, planes.p);
+          CRG_CHECK_CUDA(cudaGetLastError());
+        }
         k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv, gs.tab.v,
                                                     gs.tab.nv, gs.tab.ori, gs.tab.maxv, area.p, rowcnt.p, colcnt.p,
-                                                    ovf.p);
-      else
+                                                    ovf.p, planes.p);
+      } else
         k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv,
                                                      gs.tab.v, gs.tab.nv, gs.tab.ori, gs.tab.maxv, area.p, rowcnt.p,
-                                                     colcnt.p, ovf.p);
+                                                     colcnt.p, ovf.p, nullptr);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[2], st));

@@ -280,9 +280,21 @@ __device__ __forceinline__ d3 isect_pl(d3 a, double sa, d3 b, double sb) {
 // convex polygon `clip` (nc vertices) of orientation `sig` (+1 / -1).  Ping-pongs between bufA and bufB;
 // returns the vertex count and sets *res to the buffer holding the result, or
 // returns -1 if a stage would exceed CRG_MAXC vertices.
+// Great-circle half-space of the clip edge ca -> cb of a polygon of
+// orientation sig: n = ca x (cb - ca) (negated when clockwise) and the error
+// bound factor of n.(v - ca).
+__device__ __forceinline__ void edge_plane(d3 ca, d3 cb, double sig, d3& nrm, double& eb) {
+  d3 d1 = dsub(cb, ca);
+  nrm = dcross(ca, d1);
+  if (sig < 0.0) { nrm.x = -nrm.x; nrm.y = -nrm.y; nrm.z = -nrm.z; }
+  eb = kU32 * (fabs(ca.x) + fabs(ca.y) + fabs(ca.z)) * (fabs(d1.x) + fabs(d1.y) + fabs(d1.z));
+}
+
+// `planes`, when given (spherical only), holds edge_plane of every clip edge
+// (x, y, z = n, w = eb), computed once per clip polygon.
 template <bool kSpherical>
 __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, double sig,
-                                                     d3** res) {
+                                                     d3** res, const double4* planes = nullptr) {
   d3* in = bufA;
   d3* out = bufB;
   int n = ns;
@@ -293,10 +305,13 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
     double ex = 0.0, ey = 0.0, eb = 0.0;
     if (kSpherical) {
       // half-space of edge ca -> cb: n = ca x (cb - ca), s(v) = n.(v - ca)
-      d3 d1 = dsub(cb, ca);
-      nrm = dcross(ca, d1);
-      if (sig < 0.0) { nrm.x = -nrm.x; nrm.y = -nrm.y; nrm.z = -nrm.z; }
-      eb = kU32 * (fabs(ca.x) + fabs(ca.y) + fabs(ca.z)) * (fabs(d1.x) + fabs(d1.y) + fabs(d1.z));
+      if (planes) {
+        const double4 p = planes[k];
+        nrm = d3{p.x, p.y, p.z};
+        eb = p.w;
+      } else {
+        edge_plane(ca, cb, sig, nrm, eb);
+      }
     } else {
       ex = cb.x - ca.x; ey = cb.y - ca.y;
     }
