@@ -258,24 +258,74 @@ __global__ void k_bin_scatter(const uint32_t* __restrict__ key, int64_t n, int s
 }
 
 // Sort each bin by (key, cell index): bins are tiny, insertion sort per thread.
-__global__ void k_bin_sort(const uint32_t* __restrict__ key, const int32_t* __restrict__ off, int64_t nbins,
-                           int32_t* __restrict__ perm) {
-  int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Inside the bins of the counting sort, cells go in (key, index) order: the
+// pair is packed as key << 32 | index and sorted in place.  Bins of up to
+// kBinSmall cells: one thread, insertion sort on the contiguous words; larger
+// bins are listed for k_bin_sort_large (bitonic, shared memory up to
+// kBinLarge words, which covers any realistic grid; larger bins fail loudly).
+constexpr int kBinSmall = 32;
+constexpr int kBinLarge = 4096;
+
+__global__ void k_bin_pack(const uint32_t* __restrict__ key, const int32_t* __restrict__ perm, int64_t n,
+                           uint64_t* __restrict__ w) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) w[i] = ((uint64_t)key[perm[i]] << 32) | (uint32_t)perm[i];
+}
+
+__global__ void k_bin_sort(uint64_t* __restrict__ w, const int32_t* __restrict__ off, int64_t nbins,
+                           int32_t* __restrict__ large, int32_t* __restrict__ nlarge) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= nbins) return;
-  int32_t lo = off[b], hi = off[b + 1];
+  const int32_t lo = off[b], hi = off[b + 1];
+  if (hi - lo > kBinSmall) {
+    large[atomicAdd(nlarge, 1)] = (int32_t)b;
+    return;
+  }
   for (int32_t i = lo + 1; i < hi; ++i) {
-    int32_t x = perm[i];
-    uint32_t kx = key[x];
+    const uint64_t x = w[i];
     int32_t j = i - 1;
-    while (j >= lo) {
-      int32_t y = perm[j];
-      uint32_t ky = key[y];
-      if (ky < kx || (ky == kx && y < x)) break;
-      perm[j + 1] = y;
+    while (j >= lo && w[j] > x) {
+      w[j + 1] = w[j];
       --j;
     }
-    perm[j + 1] = x;
+    w[j + 1] = x;
   }
+}
+
+__global__ void __launch_bounds__(256) k_bin_sort_large(uint64_t* __restrict__ w, const int32_t* __restrict__ off,
+                                                        const int32_t* __restrict__ large,
+                                                        unsigned long long* __restrict__ too_big) {
+  __shared__ uint64_t sk[kBinLarge];
+  const int32_t b = large[blockIdx.x];
+  const int32_t lo = off[b], len = off[b + 1] - lo;
+  if (len > kBinLarge) {  // block-uniform
+    if (threadIdx.x == 0) atomicAdd(too_big, 1ull);
+    return;
+  }
+  int n2 = 64;
+  while (n2 < len) n2 <<= 1;
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) sk[i] = i < len ? w[lo + i] : ~0ull;
+  __syncthreads();
+  for (int sz = 2; sz <= n2; sz <<= 1)
+    for (int j = sz >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int p = i ^ j;
+        if (p > i) {
+          const uint64_t a = sk[i], c = sk[p];
+          if (((i & sz) == 0) ? a > c : a < c) {
+            sk[i] = c;
+            sk[p] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = threadIdx.x; i < len; i += blockDim.x) w[lo + i] = sk[i];
+}
+
+__global__ void k_bin_unpack(const uint64_t* __restrict__ w, int64_t n, int32_t* __restrict__ perm) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) perm[i] = (int32_t)(uint32_t)(w[i] & 0xffffffffu);
 }
 
 // Leaf boxes (level 0) and the per-cell bounds in sorted order.
@@ -475,7 +525,7 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 
 // Every destination edge's half-space, once per cell (the clip of each pair reads it).
 __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __restrict__ nv,
-                              const int8_t* __restrict__ ori, int maxv, int64_t ncells, double4* __restrict__ planes) {
+                              const int8_t* __restrict__ ori, int maxv, int64_t ncells, double4_32a* __restrict__ planes) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   const int n = nv[c];
@@ -486,7 +536,7 @@ __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __rest
     double eb;
     edge_plane(d3{q[3 * k], q[3 * k + 1], q[3 * k + 2]}, d3{q[3 * k1], q[3 * k1 + 1], q[3 * k1 + 2]}, (double)ori[c],
                nrm, eb);
-    planes[c * maxv + k] = make_double4(nrm.x, nrm.y, nrm.z, eb);
+    planes[c * maxv + k] = make_double4_32a(nrm.x, nrm.y, nrm.z, eb);
   }
 }
 
@@ -498,7 +548,7 @@ __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int
                                               int smaxv, double* __restrict__ area,
                                               int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt,
                                               unsigned long long* __restrict__ overflow,
-                                              const double4* __restrict__ dplanes) {
+                                              const double4_32a* __restrict__ dplanes) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
   int2 pr = cand[t];
@@ -857,8 +907,29 @@ void build_tree(const DevGrid& g, bool sph, double* area_out, HostTree& h, cudaS
   h.perm.alloc((size_t)n, st);
   k_bin_scatter<<<nblk(n, 256), 256, 0, st>>>(h.key.p, n, kSortShift, cnt.p, fill.p, h.perm.p);
   CRG_CHECK_CUDA(cudaGetLastError());
-  k_bin_sort<<<nblk(nbins, 256), 256, 0, st>>>(h.key.p, cnt.p, nbins, h.perm.p);
-  CRG_CHECK_CUDA(cudaGetLastError());
+  {
+    DBuf<uint64_t> w((size_t)n, st);
+    DBuf<int32_t> large((size_t)nbins + 1, st);  // [nbins] large bins | [1] their count
+    DBuf<unsigned long long> too_big(1, st);
+    CRG_CHECK_CUDA(cudaMemsetAsync(large.p + nbins, 0, sizeof(int32_t), st));
+    too_big.zero();
+    if (n) k_bin_pack<<<nblk(n, 256), 256, 0, st>>>(h.key.p, h.perm.p, n, w.p);
+    k_bin_sort<<<nblk(nbins, 256), 256, 0, st>>>(w.p, cnt.p, nbins, large.p, large.p + nbins);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    int32_t hl = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hl, large.p + nbins, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    if (hl) {
+      k_bin_sort_large<<<(unsigned)hl, 256, 0, st>>>(w.p, cnt.p, large.p, too_big.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+      unsigned long long hb = 0;
+      CRG_CHECK_CUDA(cudaMemcpyAsync(&hb, too_big.p, sizeof(hb), cudaMemcpyDeviceToHost, st));
+      CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+      CRG_REQUIRE(hb == 0, CRG_ERR_NOT_SUPPORTED, "%llu Morton bins hold more than %d cells", hb, kBinLarge);
+    }
+    if (n) k_bin_unpack<<<nblk(n, 256), 256, 0, st>>>(w.p, n, h.perm.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
   // hierarchy
   int64_t nleaves = (n + kLeaf - 1) / kLeaf;
   int64_t total = 0;
@@ -1091,7 +1162,7 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     ovf.zero();
     if (nc) {
       if (sph) {
-        DBuf<double4> planes((size_t)nd * gd.tab.maxv, st);
+        DBuf<double4_32a> planes((size_t)nd * gd.tab.maxv, st);
         if (nd) {
           k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv, nd, planes.p);
           CRG_CHECK_CUDA(cudaGetLastError());

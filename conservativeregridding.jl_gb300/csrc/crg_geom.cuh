@@ -294,7 +294,7 @@ __device__ __forceinline__ void edge_plane(d3 ca, d3 cb, double sig, d3& nrm, do
 // (x, y, z = n, w = eb), computed once per clip polygon.
 template <bool kSpherical>
 __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, double sig,
-                                                     d3** res, const double4* planes = nullptr) {
+                                                     d3** res, const double4_32a* planes = nullptr) {
   d3* in = bufA;
   d3* out = bufB;
   int n = ns;
@@ -306,7 +306,7 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
     if (kSpherical) {
       // half-space of edge ca -> cb: n = ca x (cb - ca), s(v) = n.(v - ca)
       if (planes) {
-        const double4 p = planes[k];
+        const double4_32a p = planes[k];
         nrm = d3{p.x, p.y, p.z};
         eb = p.w;
       } else {
