@@ -106,7 +106,7 @@ def run_profile(a):
         ev[2].synchronize()
         tf, tr = ev[0].elapsed_time(ev[1]) / reps, ev[1].elapsed_time(ev[2]) / reps
         print(json.dumps({"round": i, "fwd_ms": tf, "rev_ms": tr, "fwd_GBs": bf / tf / 1e6, "rev_GBs": br / tr / 1e6}))
-    info = {k: R.info[k] for k in ("nnz", "tiles", "tile_columns", "direct_rows", "n_dst", "n_src")}
+    info = {k: R.info[k] for k in ("nnz", "merge_tasks", "cut_rows", "carry_slots", "n_dst", "n_src")}
     print(json.dumps(info))
 
 

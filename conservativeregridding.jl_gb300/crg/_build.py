@@ -21,7 +21,7 @@ INCLUDE = REPO_ROOT / "include"
 BUILD_DIR = PKG_ROOT / "_build"
 LIB_PATH = BUILD_DIR / "libcrg_gb300.so"
 
-SOURCES = ["crg_scan.cu", "crg_build.cu", "crg_tiles.cu", "crg_apply.cu", "crg_grad.cu", "crg_batch.cu", "crg_api.cu"]
+SOURCES = ["crg_scan.cu", "crg_build.cu", "crg_layout.cu", "crg_apply.cu", "crg_grad.cu", "crg_batch.cu", "crg_api.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: only explicit fma() fuses, so the FP64 geometry follows the
 # exact operation order that the CPU oracle restates.

@@ -80,9 +80,6 @@ class crg_info(C.Structure):
         ("clip_overflows", C.c_int64),
         ("device", C.c_int32),
         ("pad", C.c_int32),
-        ("tiles", C.c_int64 * 2),
-        ("tile_columns", C.c_int64 * 2),
-        ("direct_rows", C.c_int64 * 2),
         ("merge_tasks", C.c_int64 * 2),
         ("cut_rows", C.c_int64 * 2),
         ("carry_slots", C.c_int64 * 2),

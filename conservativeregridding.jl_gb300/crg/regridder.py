@@ -22,7 +22,7 @@ from ._lib import ArgumentError, DimensionMismatch, check
 from .grids import PLANAR, SPHERICAL, Grid, polygon_grid
 
 # crg_info fields holding [forward, transpose] pairs
-_PAIR_FIELDS = ("tiles", "tile_columns", "direct_rows", "merge_tasks", "cut_rows", "carry_slots", "empty_rows")
+_PAIR_FIELDS = ("merge_tasks", "cut_rows", "carry_slots", "empty_rows")
 
 
 # ----------------------------------------------------------------- grid -> descriptor

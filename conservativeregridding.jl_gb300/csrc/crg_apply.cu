@@ -12,13 +12,17 @@
 //                   column order from 0.0 -- the same sequence as the
 //                   reference's column-scatter mul! for each row -- then the
 //                   optional division by the row area.
-//   k_spmm_rows     FP32/BF16 fields stored cell-major (the fields of one cell
-//                   side by side): G lanes per row, each lane owns 4
-//                   consecutive fields (128-bit FP32 / 64-bit BF16 loads),
-//                   FP32 accumulation, weights read once per row.
-//   k_spmm_tile     FP32/BF16 fields stored field-major (dims = 1): a block
-//                   owns 128 consecutive rows, stages their (column, weight)
-//                   entries in shared memory once, then sweeps all fields.
+//   k_cm_nnz        FP32/BF16 fields stored cell-major (the fields of one cell
+//                   side by side), >= 32 of them: merge-path over ~64-entry
+//                   tasks, a warp per task, 4 fields per lane, 8 gathers of a
+//                   source cell's field vector in flight (+ k_cm_fixup for
+//                   rows cut between tasks, k_zero_empty_cm for empty rows).
+//   k_cm_rows       cell-major, fewer fields: G lanes per row, RB rows per
+//                   lane group, 4 fields per lane.
+//   k_fm_rows       field-major (spatial index contiguous per field): a row
+//                   per lane; with >= 32 fields the first apply of a direction
+//                   may choose k_transpose + the cell-major path instead.
+//   k_spmm_rows     cell-major without 16-byte alignment or a multiple of 4 fields.
 //   k_spmm_generic  any strides, one thread per (row, field).
 #include <cuda_bf16.h>
 #include <stdlib.h>
@@ -280,54 +284,6 @@ __global__ void __launch_bounds__(256, 4) k_fm_rows(const int32_t* __restrict__ 
   }
 }
 
-// ------------------------------------------------------------------ field-major fields
-
-constexpr int kFmRows = 128;
-constexpr int kFmEntries = 4096;  // shared-memory capacity (32 KB)
-constexpr int kFmF = 8;           // fields per sweep step
-
-template <class T>
-__global__ void __launch_bounds__(kFmRows) k_spmm_tile(const int32_t* __restrict__ ptr,
-                                                          const int32_t* __restrict__ idx,
-                                                          const float* __restrict__ w, int64_t nrows,
-                                                          const T* __restrict__ x, int64_t xsf, T* __restrict__ y,
-                                                          int64_t ysf, int64_t nf) {
-  __shared__ int32_t s_idx[kFmEntries];
-  __shared__ float s_w[kFmEntries];
-  const int64_t r0 = (int64_t)blockIdx.x * kFmRows;
-  const int64_t r = r0 + threadIdx.x;
-  const int64_t rend = min(nrows, r0 + kFmRows);
-  const int32_t e0 = ptr[r0], e1 = ptr[rend];
-  const bool staged = (e1 - e0) <= kFmEntries;
-  if (staged) {
-    for (int32_t e = e0 + threadIdx.x; e < e1; e += kFmRows) {
-      s_idx[e - e0] = idx[e];
-      s_w[e - e0] = w[e];
-    }
-  }
-  __syncthreads();
-  if (r >= nrows) return;
-  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
-  for (int64_t f0 = 0; f0 < nf; f0 += kFmF) {
-    float acc[kFmF];
-#pragma unroll
-    for (int q = 0; q < kFmF; ++q) acc[q] = 0.f;
-    const int nq = (int)(nf - f0 < kFmF ? nf - f0 : kFmF);
-    for (int32_t k = k0; k < k1; ++k) {
-      const int64_t j = staged ? s_idx[k - e0] : idx[k];
-      const float ww = staged ? s_w[k - e0] : w[k];
-      const T* xp = x + f0 * xsf + j;
-#pragma unroll
-      for (int q = 0; q < kFmF; ++q)
-        if (q < nq) acc[q] = fmaf(ww, ld1<T>(xp + q * xsf), acc[q]);
-    }
-    T* yp = y + f0 * ysf + r;
-#pragma unroll
-    for (int q = 0; q < kFmF; ++q)
-      if (q < nq) st1<T>(yp + q * ysf, acc[q]);
-  }
-}
-
 // ------------------------------------------------------------------ generic strides
 
 template <class T>
@@ -342,265 +298,6 @@ __global__ void k_spmm_generic(const int32_t* __restrict__ ptr, const int32_t* _
   st1<T>(y + r * ysc + f * ysf, acc);
 }
 
-// ------------------------------------------------------------------ staged tiles
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
-
-template <class T> __device__ __forceinline__ float4 lds4(const T* p);
-template <> __device__ __forceinline__ float4 lds4<float>(const float* p) { return *reinterpret_cast<const float4*>(p); }
-template <> __device__ __forceinline__ float4 lds4<__nv_bfloat16>(const __nv_bfloat16* p) {
-  uint2 u = *reinterpret_cast<const uint2*>(p);
-  float2 a = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&u.x));
-  float2 b = __bfloat1622float2(*reinterpret_cast<__nv_bfloat162*>(&u.y));
-  return make_float4(a.x, a.y, b.x, b.y);
-}
-template <class T> __device__ __forceinline__ float lds1(const T* p);
-template <> __device__ __forceinline__ float lds1<float>(const float* p) { return *p; }
-template <> __device__ __forceinline__ float lds1<__nv_bfloat16>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
-
-__host__ __device__ constexpr size_t align16(size_t b) { return (b + 15) / 16 * 16; }
-
-// Shared-memory layout of the pipelined tile kernel.  Two data buffers
-// (fields of one work item + its row/entry metadata) and three small list
-// buffers (the distinct columns or chunks of an item, needed one step ahead
-// of its field copies).
-template <class T, bool kFM>
-struct Pipe {
-  static constexpr int KC = kFM ? 16 : 64;  // fields per work item
-  static constexpr int PADT = 16 / (int)sizeof(T);
-  // field-major: [KC][4*kTileUMax + pad] (a row per field, 4 cells per chunk);
-  // cell-major: [kTileUMax][KC + pad] (a row per distinct column)
-  static constexpr int SP = kFM ? (4 * kTileUMax + PADT) : (KC + PADT);
-  static constexpr int SROWS = kFM ? KC : kTileUMax;
-  static constexpr size_t kStage = align16((size_t)SROWS * SP * sizeof(T));
-  static constexpr size_t kRows = align16(sizeof(int32_t) * kTileRows);
-  static constexpr size_t kLptr = align16(sizeof(int32_t) * (kTileRows + 1));
-  static constexpr size_t kLw = align16(sizeof(float) * kTileEMax);
-  static constexpr size_t kLidx = align16(sizeof(uint16_t) * (kTileEMax + 2));
-  static constexpr size_t kData = kStage + kRows + kLptr + kLw + kLidx;
-  static constexpr size_t kList = align16(sizeof(int32_t) * kTileUMax);
-  static constexpr size_t kSmem = 2 * kData + 3 * kList;
-};
-
-struct TileArgs {
-  const int32_t* desc;
-  const int32_t* rows;
-  const int32_t* lptr;
-  const uint16_t* lidx;  // lcol (cell-major) or lchk (field-major)
-  const float* lw;
-  const int32_t* list;   // ucol (cell-major) or uchunk (field-major)
-  int64_t nitems, nkc, ngood;
-};
-
-// Persistent CTAs walk a contiguous range of work items (tile, field chunk),
-// field chunk fastest.  cp.async groups are double buffered: while item i is
-// computed from shared memory, the copies of item i+1's fields and metadata
-// and of item i+2's column / chunk list are in flight.
-template <class T, bool kFM>
-__global__ void __launch_bounds__(256, 2) k_tiled(TileArgs ta, const T* __restrict__ x, int64_t xs, T* __restrict__ y,
-                                                  int64_t ys, int64_t nf) {
-  using P = Pipe<T, kFM>;
-  constexpr int KC = P::KC, SP = P::SP;
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int tid = threadIdx.x;
-  const int64_t per = (ta.nitems + gridDim.x - 1) / gridDim.x;
-  const int64_t i0 = (int64_t)blockIdx.x * per;
-  const int64_t i1 = min(ta.nitems, i0 + per);
-  if (i0 >= i1) return;
-
-  auto data = [&](int b) { return smem + (size_t)b * P::kData; };
-  auto stage = [&](int b) { return reinterpret_cast<T*>(data(b)); };
-  auto srows = [&](int b) { return reinterpret_cast<int32_t*>(data(b) + P::kStage); };
-  auto slptr = [&](int b) { return reinterpret_cast<int32_t*>(data(b) + P::kStage + P::kRows); };
-  auto slw = [&](int b) { return reinterpret_cast<float*>(data(b) + P::kStage + P::kRows + P::kLptr); };
-  auto slidx = [&](int b) {
-    return reinterpret_cast<uint16_t*>(data(b) + P::kStage + P::kRows + P::kLptr + P::kLw);
-  };
-  auto slist = [&](int b) { return reinterpret_cast<int32_t*>(smem + 2 * P::kData + (size_t)b * P::kList); };
-
-  // copy the column / chunk list of item `it` into list buffer lb
-  auto issue_list = [&](int64_t it, int lb) {
-    const int32_t* d = ta.desc + (it / ta.nkc) * kDescInts;
-    const int l0 = kFM ? __ldg(d + kDescC0) : __ldg(d + kDescU0);
-    const int nl = kFM ? __ldg(d + kDescNc) : __ldg(d + kDescNu);
-    int32_t* dst = slist(lb);
-    for (int i = tid; i < nl; i += 256) cp_async4(dst + i, ta.list + l0 + i);
-  };
-  // copy the fields and metadata of item `it` into data buffer db, using list buffer lb
-  auto issue_data = [&](int64_t it, int db, int lb) {
-    const int64_t t = it / ta.nkc;
-    const int64_t f0 = (it % ta.nkc) * KC;
-    const int kc = (int)(nf - f0 < KC ? nf - f0 : KC);
-    const int32_t* d = ta.desc + t * kDescInts;
-    const int p0 = __ldg(d + kDescP0), nr = __ldg(d + kDescNr);
-    const int e0 = __ldg(d + kDescE0), ne = __ldg(d + kDescNe);
-    const int nl = kFM ? __ldg(d + kDescNc) : __ldg(d + kDescNu);
-    const int32_t* lst = slist(lb);
-    T* sg = stage(db);
-    if (!kFM) {
-      // one distinct column = the kc contiguous fields of a cell, in 16-byte pieces
-      const int qpc = kc * (int)sizeof(T) / 16;
-      for (int i = tid; i < nl * qpc; i += 256) {
-        const int c = i / qpc, q = i - c * qpc;
-        cp_async16(sg + c * SP + q * P::PADT, x + (int64_t)lst[c] * xs + f0 + q * P::PADT);
-      }
-    } else {
-      // one chunk = 4 consecutive cells of one field (16 B FP32, 8 B BF16)
-      for (int i = tid; i < kc * nl; i += 256) {
-        const int f = i / nl, c = i - f * nl;
-        const T* src = x + (f0 + f) * xs + (int64_t)lst[c] * 4;
-        if (sizeof(T) == 4) cp_async16(sg + f * SP + c * 4, src);
-        else cp_async8(sg + f * SP + c * 4, src);
-      }
-    }
-    int32_t* rw = srows(db);
-    int32_t* lp = slptr(db);
-    for (int i = tid; i < nr; i += 256) cp_async4(rw + i, ta.rows + p0 + i);
-    for (int i = tid; i <= nr; i += 256) cp_async4(lp + i, ta.lptr + p0 + i);
-    float* lw = slw(db);
-    for (int i = tid; i < ne; i += 256) cp_async4(lw + i, ta.lw + e0 + i);
-    // 16-bit indices as 32-bit words: word w0 = e0 / 2 covers entries from 2*w0
-    uint32_t* li = reinterpret_cast<uint32_t*>(slidx(db));
-    const int w0 = e0 >> 1, nw = ((e0 + ne + 1) >> 1) - w0;
-    const uint32_t* gw = reinterpret_cast<const uint32_t*>(ta.lidx);
-    for (int i = tid; i < nw; i += 256) cp_async4(li + i, gw + w0 + i);
-  };
-  auto compute = [&](int64_t it, int db) {
-    const int64_t t = it / ta.nkc;
-    const int64_t f0 = (it % ta.nkc) * KC;
-    const int kc = (int)(nf - f0 < KC ? nf - f0 : KC);
-    const int32_t* d = ta.desc + t * kDescInts;
-    const int nr = __ldg(d + kDescNr), e0 = __ldg(d + kDescE0);
-    const T* sg = stage(db);
-    const int32_t* rw = srows(db);
-    const int32_t* lp = slptr(db);
-    const float* lw = slw(db);
-    const uint16_t* li = slidx(db) + (e0 & 1);
-    const int eb = lp[0];
-    if (!kFM) {
-      constexpr int G = KC / 4;   // 16 lanes per row, 4 fields each
-      const int lane = tid & 31, warp = tid >> 5, g = lane % G;
-      for (int rb = warp * (32 / G) + lane / G; rb < nr; rb += 8 * (32 / G)) {
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        const int k1 = lp[rb + 1] - eb;
-        for (int k = lp[rb] - eb; k < k1; ++k) {
-          const float wk = lw[k];
-          const float4 v = lds4<T>(sg + li[k] * SP + g * 4);
-          acc.x = fmaf(wk, v.x, acc.x); acc.y = fmaf(wk, v.y, acc.y);
-          acc.z = fmaf(wk, v.z, acc.z); acc.w = fmaf(wk, v.w, acc.w);
-        }
-        if (g * 4 < kc) st4<T>(y + (int64_t)rw[rb] * ys + f0 + g * 4, acc);
-      }
-    } else {
-      // (row, group of 4 fields) pairs; consecutive threads = consecutive rows
-      const int ng = (kc + 3) >> 2;
-      for (int q = tid; q < nr * ng; q += 256) {
-        const int r = q % nr, fg = q / nr;
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-        const int k1 = lp[r + 1] - eb;
-        const T* s0 = sg + fg * 4 * SP;
-        for (int k = lp[r] - eb; k < k1; ++k) {
-          const float wk = lw[k];
-          const int lc = li[k];
-          a0 = fmaf(wk, lds1<T>(s0 + lc), a0);
-          a1 = fmaf(wk, lds1<T>(s0 + SP + lc), a1);
-          a2 = fmaf(wk, lds1<T>(s0 + 2 * SP + lc), a2);
-          a3 = fmaf(wk, lds1<T>(s0 + 3 * SP + lc), a3);
-        }
-        const int64_t fb = f0 + fg * 4;
-        T* yp = y + fb * ys + rw[r];
-        st1<T>(yp, a0);
-        if (fb + 1 < f0 + kc) st1<T>(yp + ys, a1);
-        if (fb + 2 < f0 + kc) st1<T>(yp + 2 * ys, a2);
-        if (fb + 3 < f0 + kc) st1<T>(yp + 3 * ys, a3);
-      }
-    }
-  };
-
-  // prologue: list(i0) -> L0; then data(i0) with L0 and list(i0+1) -> L1
-  issue_list(i0, 0);
-  cp_async_commit();
-  cp_async_wait_all();
-  __syncthreads();
-  issue_data(i0, 0, 0);
-  if (i0 + 1 < i1) issue_list(i0 + 1, 1);
-  cp_async_commit();
-  for (int64_t it = i0; it < i1; ++it) {
-    const int k = (int)(it - i0);
-    cp_async_wait_all();
-    __syncthreads();
-    if (it + 1 < i1) {
-      issue_data(it + 1, (k + 1) & 1, (k + 1) % 3);
-      if (it + 2 < i1) issue_list(it + 2, (k + 2) % 3);
-    }
-    cp_async_commit();
-    compute(it, k & 1);
-    __syncthreads();
-  }
-  cp_async_wait_all();
-}
-
-// Rows left out of the tiles (too many distinct columns), cell-major fields:
-// one warp per row, 4 fields per lane.
-template <class T>
-__global__ void __launch_bounds__(256) k_direct_cm(const int32_t* __restrict__ pos, int64_t npos,
-                                                   const int32_t* __restrict__ rows, const int32_t* __restrict__ ptr,
-                                                   const int32_t* __restrict__ idx, const float* __restrict__ w,
-                                                   const T* __restrict__ x, int64_t xs, T* __restrict__ y, int64_t ys,
-                                                   int64_t nf) {
-  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (wi >= npos) return;
-  const int32_t r = rows[pos[wi]];
-  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
-  for (int64_t f = (int64_t)lane * 4; f < nf; f += 128) {
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int32_t k = k0; k < k1; ++k) {
-      const float4 v = ld4<T>(x + (int64_t)idx[k] * xs + f);
-      const float ww = w[k];
-      acc.x = fmaf(ww, v.x, acc.x);
-      acc.y = fmaf(ww, v.y, acc.y);
-      acc.z = fmaf(ww, v.z, acc.z);
-      acc.w = fmaf(ww, v.w, acc.w);
-    }
-    st4<T>(y + (int64_t)r * ys + f, acc);
-  }
-}
-
-// Rows left out of the tiles, field-major fields: one warp per row, lanes
-// split the row's entries, warp reduction per field.
-template <class T>
-__global__ void __launch_bounds__(256) k_direct_fm(const int32_t* __restrict__ pos, int64_t npos,
-                                                   const int32_t* __restrict__ rows, const int32_t* __restrict__ ptr,
-                                                   const int32_t* __restrict__ idx, const float* __restrict__ w,
-                                                   const T* __restrict__ x, int64_t xs, T* __restrict__ y, int64_t ys,
-                                                   int64_t nf) {
-  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (wi >= npos) return;
-  const int32_t r = rows[pos[wi]];
-  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
-  for (int64_t f = 0; f < nf; ++f) {
-    float acc = 0.f;
-    for (int32_t k = k0 + lane; k < k1; k += 32) acc = fmaf(w[k], ld1<T>(x + f * xs + idx[k]), acc);
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) st1<T>(y + f * ys + r, acc);
-  }
-}
-
 int num_sms() {
   static int n = [] {
     int dev = 0, v = 0;
@@ -609,40 +306,6 @@ int num_sms() {
     return v > 0 ? v : 1;
   }();
   return n;
-}
-
-template <class T, bool kFM>
-void launch_tiled(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                  cudaStream_t st) {
-  using P = Pipe<T, kFM>;
-  const DevTiles& tl = c.tiles;
-  const float* w = normalize ? (adjoint ? c.adj32 : c.wn32) : c.val32;
-  TileArgs ta;
-  ta.desc = tl.desc;
-  ta.rows = tl.rows;
-  ta.lptr = tl.lptr;
-  ta.lidx = kFM ? tl.lchk : tl.lcol;
-  ta.lw = normalize ? (adjoint ? tl.lw_adj : tl.lw_wn) : tl.lw_val;
-  ta.list = kFM ? tl.uchunk : tl.ucol;
-  ta.nkc = (nf + P::KC - 1) / P::KC;
-  ta.ngood = tl.ngood;
-  ta.nitems = tl.ngood * ta.nkc;
-  static bool configured = false;  // per template instance
-  if (!configured) {
-    CRG_CHECK_CUDA(cudaFuncSetAttribute(k_tiled<T, kFM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::kSmem));
-    configured = true;
-  }
-  if (ta.nitems) {
-    const int64_t grid = std::min<int64_t>(ta.nitems, (int64_t)num_sms() * 2);
-    k_tiled<T, kFM><<<(unsigned)grid, 256, P::kSmem, st>>>(ta, x, xs, y, ys, nf);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-  if (tl.ndirect) {
-    const unsigned blocks = nblk(tl.ndirect * 32, 256);
-    if (kFM) k_direct_fm<T><<<blocks, 256, 0, st>>>(tl.direct, tl.ndirect, tl.rows, c.ptr, c.idx, w, x, xs, y, ys, nf);
-    else k_direct_cm<T><<<blocks, 256, 0, st>>>(tl.direct, tl.ndirect, tl.rows, c.ptr, c.idx, w, x, xs, y, ys, nf);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
 }
 
 // ------------------------------------------------------------------ merge-path (cell-major)
@@ -827,19 +490,14 @@ void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y
 }
 
 // Kernel choice for FP32/BF16 fields.  CRG_SPMM_PATH selects an alternative
-// for tuning and profiling: "nnz" (merge-path with register gathers),
-// "rows" (register-blocked row kernels), "tiled" (shared-memory staged
-// tiles) or "legacy" (first-generation row kernels); unset = automatic.
-enum class SpmmPath { kAuto, kRows, kTiled, kLegacy, kNnz };
+// for tuning and profiling: "rows" (the row kernels for every layout, no
+// merge-path, no transposes); unset = automatic.
+enum class SpmmPath { kAuto, kRows };
 
 inline SpmmPath spmm_path() {
   static const SpmmPath p = [] {
     const char* e = getenv("CRG_SPMM_PATH");
-    if (e && strcmp(e, "nnz") == 0) return SpmmPath::kNnz;
-    if (e && strcmp(e, "tiled") == 0) return SpmmPath::kTiled;
-    if (e && strcmp(e, "legacy") == 0) return SpmmPath::kLegacy;
-    if (e && strcmp(e, "rows") == 0) return SpmmPath::kRows;
-    return SpmmPath::kAuto;
+    return (e && strcmp(e, "rows") == 0) ? SpmmPath::kRows : SpmmPath::kAuto;
   }();
   return p;
 }
@@ -932,32 +590,18 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
   const bool cell_major = (xsf == 1 && ysf == 1) && nf > 1;
   const bool field_major = (xsc == 1 && ysc == 1);
   const int es = (int)sizeof(T);
-  const int vecf = 16 / es;  // fields per 16 bytes
   // 4-field vectors: 16-byte (FP32) / 8-byte (BF16) aligned loads and stores
   const bool vec4 = nf % 4 == 0 && xsc % 4 == 0 && ysc % 4 == 0 && (uintptr_t)x % (4 * es) == 0 &&
                     (uintptr_t)y % (4 * es) == 0;
   const SpmmPath path = spmm_path();
-  if (path == SpmmPath::kTiled) {
-    // cell-major: 16-byte pieces of each cell's field vector
-    if (cell_major && nf >= 16 && nf % vecf == 0 && xsc % vecf == 0 && ysc % 4 == 0 && (uintptr_t)x % 16 == 0 &&
-        (uintptr_t)y % (4 * es) == 0) {
-      launch_tiled<T, false>(c, normalize, adjoint, x, xsc, y, ysc, nf, st);
-      return;
-    }
-    // field-major: aligned 4-cell chunks of each field (all chunks inside the field)
-    if (field_major && nf >= 4 && c.ncols % 4 == 0 && xsf % 4 == 0 && (uintptr_t)x % (4 * es) == 0) {
-      launch_tiled<T, true>(c, normalize, adjoint, x, xsf, y, ysf, nf, st);
-      return;
-    }
-  }
   // the merge-path kernel addresses source cells with 32-bit byte offsets
   const bool span32 = (double)c.ncols * (double)xsc * es < 4.0e9;
-  if ((path == SpmmPath::kAuto || path == SpmmPath::kNnz) && cell_major && vec4 && nf >= 32 && span32) {
+  if (path == SpmmPath::kAuto && cell_major && vec4 && nf >= 32 && span32) {
     // merge-path over entries; rows with no entries are zeroed separately
     launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st);
     return;
   }
-  if (path == SpmmPath::kRows || path == SpmmPath::kAuto) {
+  {
     if (cell_major && vec4) {
       launch_cm_rows<T>(c, w, x, xsc, y, ysc, nf, st);
       CRG_CHECK_CUDA(cudaGetLastError());
@@ -1026,8 +670,6 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
       CRG_ROWS_CASE(32)
     }
 #undef CRG_ROWS_CASE
-  } else if (field_major && nf > 1) {
-    k_spmm_tile<T><<<nblk(n, kFmRows), kFmRows, 0, st>>>(c.ptr, c.idx, w, n, x, xsf, y, ysf, nf);
   } else {
     for (int64_t f0 = 0; f0 < nf; f0 += 65535) {
       dim3 grid(nblk(n, 256), (unsigned)std::min<int64_t>(65535, nf - f0));

@@ -1091,7 +1091,6 @@ void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cud
 }
 
 void free_csr(DevCsr& c) {
-  free_tiles(c.tiles);
   cudaFree(c.erow);
   cudaFree(c.split);
   cudaFree(c.tasks);
@@ -1248,9 +1247,6 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
       k_derive<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, R->rev.idx, R->rev.val, ns, R->src_area, R->dst_area,
                                               R->rev.val32, R->rev.wn32, R->rev.adj32, R->col_sum);
     CRG_CHECK_CUDA(cudaGetLastError());
-    // staged-tile layouts, rows in the spatial order of their cells
-    build_tiles(R->fwd, td.perm.p, st);
-    build_tiles(R->rev, ts.perm.p, st);
     build_merge_path(R->fwd, st);
     build_merge_path(R->rev, st);
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[3], st));
@@ -1267,12 +1263,6 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     I.t_build_ms = t03; I.t_search_ms = t01; I.t_clip_ms = t12; I.t_assemble_ms = t23;
     I.clip_overflows = (int64_t)hovf;
     I.device = R->device;
-    const DevTiles* tl[2] = {&R->fwd.tiles, &R->rev.tiles};
-    for (int d = 0; d < 2; ++d) {
-      I.tiles[d] = tl[d]->ngood;
-      I.tile_columns[d] = tl[d]->nucol;
-      I.direct_rows[d] = tl[d]->ndirect;
-    }
     const DevCsr* cs[2] = {&R->fwd, &R->rev};
     for (int d = 0; d < 2; ++d) {
       I.merge_tasks[d] = cs[d]->ntasks;

@@ -37,31 +37,6 @@ struct Fail {
 
 constexpr int kMaxGridBlocks = 12;  // curvilinear blocks per grid (cube faces and more)
 
-// Row tiles of one direction (see crg_tiles.cu).
-constexpr int kTileRows = 64;    // rows of a full tile
-constexpr int kTileUMax = 128;   // distinct source columns a tile may stage
-constexpr int kTileEMax = 2048;  // entries a tile may hold
-
-// Per-tile descriptor (8 x int32): rows [p0, p0+nr) of the processing order,
-// distinct columns ucol[u0, u0+nu), entries [e0, e0+ne) of the permuted
-// entry arrays, distinct 4-cell chunks uchunk[c0, c0+nc).
-enum { kDescP0 = 0, kDescNr, kDescU0, kDescNu, kDescE0, kDescNe, kDescC0, kDescNc, kDescInts };
-
-struct DevTiles {
-  int64_t ngood = 0, ndirect = 0, nucol = 0, nuchunk = 0;
-  int32_t* rows = nullptr;     // [nrows] processing order: position -> row
-  int32_t* lptr = nullptr;     // [nrows+1] entry offsets in processing order
-  uint16_t* lcol = nullptr;    // [nnz] column index inside the tile's distinct-column set
-  uint16_t* lchk = nullptr;    // [nnz] 4 * (chunk index inside the tile's chunk set) + (column & 3)
-  float* lw_val = nullptr;     // [nnz] val32 in processing order
-  float* lw_wn = nullptr;      // [nnz] wn32 in processing order
-  float* lw_adj = nullptr;     // [nnz] adj32 in processing order
-  int32_t* desc = nullptr;     // [ngood][kDescInts] tile descriptors, in row order
-  int32_t* ucol = nullptr;     // [nucol] distinct source columns per tile, ascending
-  int32_t* uchunk = nullptr;   // [nuchunk] distinct source chunks (column >> 2) per tile, ascending
-  int32_t* direct = nullptr;   // [ndirect] positions of rows applied by direct gathers
-};
-
 // Device CSR of one direction.  rows = dst cells for the forward copy,
 // src cells for the reverse copy (A^T).
 struct DevCsr {
@@ -72,7 +47,6 @@ struct DevCsr {
   float* val32 = nullptr;    // [nnz] A entries (FP32)
   float* wn32 = nullptr;     // [nnz] A_rc / area_row (FP32): normalised weights of this direction
   float* adj32 = nullptr;    // [nnz] A_rc / area_col (FP32): adjoint weights of the other direction
-  DevTiles tiles;            // staged-tile layout for the batched FP32/BF16 apply
   // merge-path layout: runs of about kTaskNnz entries per task, cut at row
   // starts except inside rows longer than kTaskNnz / 4
   int32_t* erow = nullptr;   // [nnz] row of each entry
@@ -145,9 +119,7 @@ void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, 
 bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
-void build_tiles(DevCsr& c, const int32_t* row_order, cudaStream_t st);
 void build_merge_path(DevCsr& c, cudaStream_t st);
-void free_tiles(DevTiles& t);
 void area_grad_impl(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src, const double* u,
                     const double* s, const double* c, double* grad, cudaStream_t st);
 void mirror_fold_impl(int dtype, void* field, int64_t sc, int64_t sf, int64_t nfields, int64_t nx, int64_t ny,

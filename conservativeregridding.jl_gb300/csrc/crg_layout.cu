@@ -1,0 +1,164 @@
+// crg_layout.cu -- the merge-path layout of each direction of a regridder
+// (built once per direction, read by every batched cell-major apply).
+#include <stdlib.h>
+#include <string.h>
+
+#include "crg_internal.cuh"
+#include "crg_scan.cuh"
+
+// ---------------------------------------------------------------------------
+// Merge-path layout: the entries of a direction are cut into tasks of
+// kTaskNnz consecutive entries (CSR order).  Rows whose entries straddle a task
+// boundary are listed with the first and last task they touch, so the apply
+// can combine their per-task partial sums in task order afterwards.
+
+namespace crg {
+
+namespace {
+
+inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
+
+__global__ void k_expand_rows(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ erow,
+                              int* __restrict__ nempty) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t a = ptr[r], b = ptr[r + 1];
+  for (int32_t k = a; k < b; ++k) erow[k] = (int32_t)r;
+  if (a == b) atomicAdd(nempty, 1);
+}
+
+// Start of task k: entry k * task_nnz moved up to the next row start, unless
+// it falls inside a row longer than long_row (that row is then cut and its
+// pieces summed by k_cm_fixup).  bound[ntasks] = nnz.
+__global__ void k_task_bounds(const int32_t* __restrict__ ptr, const int32_t* __restrict__ erow, int64_t nnz,
+                              int64_t ntasks, int task_nnz, int long_row, int32_t* __restrict__ bound) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k > ntasks) return;
+  if (k == ntasks) {
+    bound[k] = (int32_t)nnz;
+    return;
+  }
+  const int64_t e = k * task_nnz;
+  const int32_t r = erow[e], a = ptr[r], b = ptr[r + 1];
+  bound[k] = (a == e || b - a > long_row) ? (int32_t)e : b;
+}
+
+// last task whose start is <= e
+__device__ int64_t task_of_entry(const int32_t* __restrict__ bound, int64_t ntasks, int64_t e) {
+  int64_t lo = 0, hi = ntasks - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (bound[mid] <= e) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Task records, and a flag on every task that ends a row begun in an earlier task.
+__global__ void k_task_records(const int32_t* __restrict__ ptr, const int32_t* __restrict__ erow,
+                               const int32_t* __restrict__ bound, int64_t ntasks, int4* __restrict__ tasks,
+                               int32_t* __restrict__ ends) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntasks) return;
+  const int32_t e0 = bound[t], e1 = bound[t + 1];
+  if (e0 >= e1) {  // only the last task can be empty
+    tasks[t] = make_int4(e0, e0, 0, 0);
+    ends[t] = 0;
+    return;
+  }
+  const int32_t first = erow[e0], last = erow[e1 - 1];
+  const uint32_t fs = ptr[first] < e0 ? 1u : 0u, ls = ptr[last + 1] > e1 ? 1u : 0u;
+  tasks[t] = make_int4(e0, e1, (int32_t)((uint32_t)first | (fs << 31)), (int32_t)((uint32_t)last | (ls << 31)));
+  ends[t] = (fs && !(first == last && ls)) ? 1 : 0;
+}
+
+// Cut row number pos[t] ends in task t: its row, first task and number of
+// pieces (one carry slot per piece).
+__global__ void k_split_fill(const int32_t* __restrict__ ptr, const int32_t* __restrict__ bound, int64_t ntasks,
+                             const int4* __restrict__ tasks, const int32_t* __restrict__ pos,
+                             int32_t* __restrict__ split, int32_t* __restrict__ span) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntasks || pos[t + 1] == pos[t]) return;
+  const int32_t row = tasks[t].z & 0x7fffffff;
+  const int64_t t0 = task_of_entry(bound, ntasks, ptr[row]);
+  int32_t* s = split + 3 * (int64_t)pos[t];
+  s[0] = row;
+  s[1] = (int32_t)t0;  // replaced by the first slot in k_slot_fill
+  s[2] = (int32_t)(t - t0 + 1);
+  span[pos[t]] = (int32_t)(t - t0 + 1);
+}
+
+// Slots of cut row s are base[s] .. base[s] + pieces - 1 in task order: the
+// row's first task writes its last-row slot, the later tasks their first-row slot.
+__global__ void k_slot_fill(int32_t* __restrict__ split, int64_t nsplit, const int32_t* __restrict__ base,
+                            int2* __restrict__ tslot) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nsplit) return;
+  const int32_t t0 = split[3 * s + 1], pieces = split[3 * s + 2], b = base[s];
+  tslot[t0].y = b;
+  for (int32_t k = 1; k < pieces; ++k) tslot[t0 + k].x = b + k;
+  split[3 * s + 1] = b;
+}
+
+}  // namespace
+
+void build_merge_path(DevCsr& c, cudaStream_t st) {
+  const int64_t n = c.nrows, nnz = c.nnz;
+  c.erow = keep_alloc<int32_t>((size_t)nnz, st);
+  // CRG_TASK_NNZ (32..1024) sets the nominal task length for tuning; CRG_TASK_CUT=fixed
+  // cuts every task at exactly that length (rows spanning tasks everywhere)
+  static const int task_nnz = [] {
+    const char* e = getenv("CRG_TASK_NNZ");
+    const int v = e ? atoi(e) : kTaskNnz;
+    return (v >= 32 && v <= 1024) ? v : kTaskNnz;
+  }();
+  static const int long_row = [] {
+    const char* e = getenv("CRG_TASK_CUT");
+    return (e && strcmp(e, "fixed") == 0) ? -1 : task_nnz / 4;
+  }();
+  c.ntasks = (nnz + task_nnz - 1) / task_nnz;
+  c.tasks = keep_alloc<int4>((size_t)c.ntasks, st);
+  c.tslot = keep_alloc<int2>((size_t)c.ntasks, st);
+  c.nsplit = 0;
+  c.nslots = 0;
+  c.nempty = n;
+  if (n == 0 || nnz == 0) return;
+  int32_t* work = nullptr;  // [1] empty rows | [ntasks + 1] bounds | [ntasks + 1] split positions
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&work, sizeof(int32_t) * (2 * c.ntasks + 3), st));
+  int32_t* nempty = work;
+  int32_t* bound = work + 1;
+  int32_t* pos = bound + c.ntasks + 1;
+  CRG_CHECK_CUDA(cudaMemsetAsync(nempty, 0, sizeof(int32_t), st));
+  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow, nempty);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  k_task_bounds<<<nblk(c.ntasks + 1, 256), 256, 0, st>>>(c.ptr, c.erow, nnz, c.ntasks, task_nnz, long_row, bound);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  k_task_records<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, c.erow, bound, c.ntasks, c.tasks, pos);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  exclusive_scan_i32(pos, pos, c.ntasks, st);
+  int32_t counts[2] = {0, 0};
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&counts[0], pos + c.ntasks, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&counts[1], nempty, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  c.nsplit = counts[0];
+  c.nempty = counts[1];
+  CRG_CHECK_CUDA(cudaMemsetAsync(c.tslot, 0xff, sizeof(int2) * c.ntasks, st));  // -1: row not cut
+  c.split = keep_alloc<int32_t>((size_t)3 * c.nsplit, st);
+  if (c.nsplit) {
+    int32_t* span = nullptr;  // [nsplit + 1] pieces per cut row, scanned to first slots
+    CRG_CHECK_CUDA(cudaMallocAsync((void**)&span, sizeof(int32_t) * (c.nsplit + 1), st));
+    k_split_fill<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, bound, c.ntasks, c.tasks, pos, c.split, span);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    exclusive_scan_i32(span, span, c.nsplit, st);
+    k_slot_fill<<<nblk(c.nsplit, 256), 256, 0, st>>>(c.split, c.nsplit, span, c.tslot);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    int32_t nslots = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&nslots, span + c.nsplit, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaFreeAsync(span, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    c.nslots = nslots;
+  }
+  CRG_CHECK_CUDA(cudaFreeAsync(work, st));
+}
+
+}  // namespace crg

@@ -51,7 +51,6 @@ struct CrgInfo
     t_build_ms::Float64; t_search_ms::Float64; t_clip_ms::Float64; t_assemble_ms::Float64
     clip_overflows::Int64
     device::Int32; pad::Int32
-    tiles::NTuple{2,Int64}; tile_columns::NTuple{2,Int64}; direct_rows::NTuple{2,Int64}
     merge_tasks::NTuple{2,Int64}; cut_rows::NTuple{2,Int64}; carry_slots::NTuple{2,Int64}; empty_rows::NTuple{2,Int64}
 end
 

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define CRG_ABI_VERSION 1
+#define CRG_ABI_VERSION 2
 
 typedef enum {
     CRG_OK = 0,
@@ -87,10 +87,6 @@ typedef struct crg_info {
     int64_t clip_overflows;  /* pairs whose clip exceeded the vertex capacity */
     int32_t device;
     int32_t pad;
-    /* staged-tile layout of the batched apply, [0] = forward (rows = dst), [1] = transpose */
-    int64_t tiles[2];        /* row tiles whose source columns are staged in shared memory */
-    int64_t tile_columns[2]; /* distinct source columns summed over those tiles */
-    int64_t direct_rows[2];  /* rows applied by direct gathers (too many distinct columns) */
     /* merge-path layout of the batched cell-major apply, [0] = forward, [1] = transpose */
     int64_t merge_tasks[2];  /* tasks of about 64 entries, cut at row starts */
     int64_t cut_rows[2];     /* rows longer than 16 entries cut between tasks */

@@ -30,7 +30,7 @@ def test_binding_covers_only_declared_symbols():
 
 def test_cpu_safe_entry_points():
     lib = _lib.load()
-    assert lib.crg_abi_version() == 1
+    assert lib.crg_abi_version() == 2
     assert lib.crg_status_string(0) == b"ok"
     assert lib.crg_status_string(2) == b"dimension mismatch"
     # argument validation happens before any device work

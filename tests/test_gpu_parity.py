@@ -281,10 +281,10 @@ def test_transpose_shares_handle(c1):
     assert T.transpose().nnz == T.nnz
 
 
-TILED_CASES = {
-    # fine destination over coarse source: every row fits a staged tile
+BATCHED_CASES = {
+    # fine destination over coarse source: short rows, none cut
     "healpix32_from_lonlat3": lambda: (grids.healpix_grid(32), grids.lonlat_regular(3.0, 3.0)),
-    # coarse destination over a fine source: wide rows go to the direct kernels
+    # coarse destination over a fine source: long rows cut across tasks
     "lonlat20_from_lonlat0.5": lambda: (grids.lonlat_regular(20.0, 20.0), grids.lonlat_regular(0.5, 0.5)),
     "cs6_from_healpix64": lambda: (grids.cubed_sphere(6), grids.healpix_grid(64)),
     # global destination over a regional source: destination rows without entries
@@ -293,16 +293,16 @@ TILED_CASES = {
 }
 
 
-@pytest.mark.parametrize("case", list(TILED_CASES))
+@pytest.mark.parametrize("case", list(BATCHED_CASES))
 @pytest.mark.parametrize("K,layout,dtype", [(128, "cell_major", "float32"), (200, "cell_major", "float32"),
                                             (40, "cell_major", "bfloat16"), (128, "field_major", "float32"),
                                             (37, "field_major", "bfloat16"), (16, "field_major", "float32")])
-def test_apply_tiled_paths(cuda, case, K, layout, dtype):
-    """Staged-tile SpMM (and its direct-row fallback) against the FP64 oracle,
-    forward, transpose and adjoint."""
+def test_apply_batched_paths(cuda, case, K, layout, dtype):
+    """Batched FP32/BF16 SpMM (merge-path cell-major, row kernels, field-major
+    through transposes) against the FP64 oracle, forward, transpose and adjoint."""
     import torch
 
-    dst, src = TILED_CASES[case]()
+    dst, src = BATCHED_CASES[case]()
     R = Regridder(dst, src, normalize=True)
     O = oracle.OracleRegridder(dst, src, normalize=True)
     # FP32 accumulation over rows of up to ~1600 entries (20-degree cells over 0.5 degrees)
