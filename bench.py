@@ -65,7 +65,7 @@ def parse():
 
 def run_profile(a):
     """Build R, make the fields, run a.steps rounds of forward + transpose
-    SpMM and print per-launch times and the tile layout statistics."""
+    SpMM and print per-launch times and the merge-path layout statistics."""
     import torch
 
     from crg import Regridder, regrid_

@@ -311,12 +311,15 @@ int num_sms() {
 // ------------------------------------------------------------------ merge-path (cell-major)
 
 // Each warp walks tasks of about kTaskNnz consecutive entries.  Lanes load 32
-// (column, weight, row) entries with one coalesced load each, then every entry
-// is broadcast and the whole warp gathers that cell's 128 fields (4 per lane,
-// 16-byte loads); 8 gathers are issued before they are consumed.  Rows are
-// accumulated in entry order and written when the row changes; a row that
-// began in an earlier task or continues into a later one is written to the
-// task's carry slot (0 = first row, 1 = last row) for k_cm_fixup.
+// (column, weight) entries with one coalesced load each, and the warp reads
+// which of them start a row from the row-start bitmap (one bit per entry);
+// then every entry is broadcast and the whole warp gathers that cell's 128
+// fields (4 per lane, 16-byte loads); 8 gathers are issued before they are
+// consumed.  Rows are accumulated in entry order and written when the row
+// changes (to the next row, or to nextrow[row] when some rows have no
+// entries); a row that began in an earlier task or continues into a later one
+// is written to the task's carry slot (0 = first row, 1 = last row) for
+// k_cm_fixup.
 template <class T> __device__ __forceinline__ float4 ldoff4(const char* base, uint32_t off);
 template <> __device__ __forceinline__ float4 ldoff4<float>(const char* base, uint32_t off) {
   return __ldg(reinterpret_cast<const float4*>(base + off));
@@ -325,12 +328,13 @@ template <> __device__ __forceinline__ float4 ldoff4<__nv_bfloat16>(const char* 
   return ld4<__nv_bfloat16>(reinterpret_cast<const __nv_bfloat16*>(base + off));
 }
 
-template <class T, int B = 8>
-__global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
+template <class T, bool kGaps>
+__global__ void __launch_bounds__(256, 3)
     k_cm_nnz(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
-             const int32_t* __restrict__ erow, const float* __restrict__ w, int64_t ntasks, const T* __restrict__ x,
+             const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow, const float* __restrict__ w,
+             int64_t ntasks, const T* __restrict__ x,
              int64_t xs, T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
-  static_assert(B == 8 || B == 16, "gathers in flight per warp");
+  constexpr int B = 8;  // gathers in flight per warp
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -362,29 +366,27 @@ __global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
         st4<T>(y + (int64_t)row * ys + fo, acc);
       }
     };
-    // lane's entry of the chunk at c0: row, byte offset of its source cell, weight
-    auto load = [&](int32_t c0, int32_t& r, uint32_t& o, float& wt) {
+    // the chunk at c0: lane's byte offset of its source cell and weight, and
+    // the row starts among the chunk's entries (bit k: entry c0 + k)
+    auto load = [&](int32_t c0, uint32_t& starts, uint32_t& o, float& wt) {
       const int32_t e = c0 + lane;
       const bool valid = e < e1;
-      r = valid ? __ldg(erow + e) : 0x7fffffff;
       o = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
       wt = valid ? __ldg(w + e) : 0.f;
+      starts = __funnelshift_r(__ldg(rbits + (c0 >> 5)), __ldg(rbits + (c0 >> 5) + 1), (uint32_t)c0 & 31u);
+      if (e1 - c0 < 32) starts &= (1u << (e1 - c0)) - 1u;
     };
-    int32_t myr;
+    uint32_t starts;
     uint32_t myo;
     float myw;
-    load(e0, myr, myo, myw);
-    int32_t prev_last = first;  // row of the entry before the current chunk
+    load(e0, starts, myo, myw);
+    starts &= ~1u;  // entry e0 belongs to row `first` (already current)
     for (int32_t c0 = e0; c0 < e1; c0 += 32) {
       // the next chunk's entries load while this one is gathered
-      int32_t nr = 0x7fffffff;
-      uint32_t no = 0u;
+      uint32_t nstarts = 0u, no = 0u;
       float nwt = 0.f;
-      if (c0 + 32 < e1) load(c0 + 32, nr, no, nwt);
-      int32_t before = __shfl_up_sync(0xffffffffu, myr, 1);
-      if (lane == 0) before = prev_last;
-      const unsigned newrow = __ballot_sync(0xffffffffu, myr != 0x7fffffff && myr != before);  // starts a row
-      prev_last = __shfl_sync(0xffffffffu, myr, 31);
+      if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
+      const unsigned newrow = starts;
       const int n = e1 - c0 < 32 ? e1 - c0 : 32;
       for (int k = 0; k < n; k += B) {
         float4 v[B];
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
           if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
           if ((newrow >> (k + h)) & 1u) {
             flush(cur);
-            cur = __shfl_sync(0xffffffffu, myr, k + h);
+            cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
             acc = make_float4(0.f, 0.f, 0.f, 0.f);
           }
           acc.x = fmaf(ww[h], v[h].x, acc.x);
@@ -409,7 +411,7 @@ __global__ void __launch_bounds__(256, B == 8 ? 3 : 2)
           acc.w = fmaf(ww[h], v[h].w, acc.w);
         }
       }
-      myr = nr;
+      starts = nstarts;
       myo = no;
       myw = nwt;
     }
@@ -462,20 +464,16 @@ __global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* _
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
                    float* carry, cudaStream_t st) {
-  // gathers in flight per warp: CRG_NNZ_DEPTH=16 selects 16 (two blocks of 256 per SM) for tuning
-  static const int depth = [] {
-    const char* e = getenv("CRG_NNZ_DEPTH");
-    return (e && atoi(e) == 16) ? 16 : 8;
-  }();
-  const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * (depth == 16 ? 16 : 24));
+  // three blocks of 8 warps per SM
+  const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 24);
   for (int64_t f0 = 0; f0 < nf; f0 += 128) {
     if (c.ntasks) {
-      if (depth == 16)
-        k_cm_nnz<T, 16><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.erow, w, c.ntasks, x, xs,
-                                                               y, ys, f0, nf, carry);
+      if (c.nextrow)
+        k_cm_nnz<T, true><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, c.nextrow, w,
+                                                                 c.ntasks, x, xs, y, ys, f0, nf, carry);
       else
-        k_cm_nnz<T><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.erow, w, c.ntasks, x, xs, y,
-                                                           ys, f0, nf, carry);
+        k_cm_nnz<T, false><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, nullptr, w,
+                                                                  c.ntasks, x, xs, y, ys, f0, nf, carry);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (c.nsplit) {

@@ -1092,6 +1092,8 @@ void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cud
 
 void free_csr(DevCsr& c) {
   cudaFree(c.erow);
+  cudaFree(c.rbits);
+  cudaFree(c.nextrow);
   cudaFree(c.split);
   cudaFree(c.tasks);
   cudaFree(c.tslot);

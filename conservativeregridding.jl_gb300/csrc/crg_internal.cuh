@@ -50,6 +50,8 @@ struct DevCsr {
   // merge-path layout: runs of about kTaskNnz entries per task, cut at row
   // starts except inside rows longer than kTaskNnz / 4
   int32_t* erow = nullptr;   // [nnz] row of each entry
+  uint32_t* rbits = nullptr; // [nnz / 32 + 2] bit e set when entry e starts its row
+  int32_t* nextrow = nullptr;  // [nrows] next row with entries (only when some rows have none)
   int64_t ntasks = 0;
   int4* tasks = nullptr;     // [ntasks] x = first entry, y = end entry,
                              //   z = first row | (row began in an earlier task) << 31,

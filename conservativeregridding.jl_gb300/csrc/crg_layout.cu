@@ -19,12 +19,24 @@ namespace {
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 __global__ void k_expand_rows(const int32_t* __restrict__ ptr, int64_t n, int32_t* __restrict__ erow,
-                              int* __restrict__ nempty) {
+                              uint32_t* __restrict__ rbits, int* __restrict__ nempty) {
   int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   const int32_t a = ptr[r], b = ptr[r + 1];
   for (int32_t k = a; k < b; ++k) erow[k] = (int32_t)r;
-  if (a == b) atomicAdd(nempty, 1);
+  if (a == b)
+    atomicAdd(nempty, 1);
+  else
+    atomicOr(rbits + (a >> 5), 1u << (a & 31));
+}
+
+// Row that follows r in entry order (nrows after the last row with entries).
+__global__ void k_next_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ erow, int64_t n,
+                            int64_t nnz, int32_t* __restrict__ nextrow) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int32_t b = ptr[r + 1];
+  nextrow[r] = b < nnz ? erow[b] : (int32_t)n;
 }
 
 // Start of task k: entry k * task_nnz moved up to the next row start, unless
@@ -105,6 +117,9 @@ __global__ void k_slot_fill(int32_t* __restrict__ split, int64_t nsplit, const i
 void build_merge_path(DevCsr& c, cudaStream_t st) {
   const int64_t n = c.nrows, nnz = c.nnz;
   c.erow = keep_alloc<int32_t>((size_t)nnz, st);
+  const size_t nwords = (size_t)(nnz >> 5) + 2;
+  c.rbits = keep_alloc<uint32_t>(nwords, st);
+  CRG_CHECK_CUDA(cudaMemsetAsync(c.rbits, 0, sizeof(uint32_t) * nwords, st));
   // CRG_TASK_NNZ (32..1024) sets the nominal task length for tuning; CRG_TASK_CUT=fixed
   // cuts every task at exactly that length (rows spanning tasks everywhere)
   static const int task_nnz = [] {
@@ -129,7 +144,7 @@ void build_merge_path(DevCsr& c, cudaStream_t st) {
   int32_t* bound = work + 1;
   int32_t* pos = bound + c.ntasks + 1;
   CRG_CHECK_CUDA(cudaMemsetAsync(nempty, 0, sizeof(int32_t), st));
-  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow, nempty);
+  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow, c.rbits, nempty);
   CRG_CHECK_CUDA(cudaGetLastError());
   k_task_bounds<<<nblk(c.ntasks + 1, 256), 256, 0, st>>>(c.ptr, c.erow, nnz, c.ntasks, task_nnz, long_row, bound);
   CRG_CHECK_CUDA(cudaGetLastError());
@@ -142,6 +157,11 @@ void build_merge_path(DevCsr& c, cudaStream_t st) {
   CRG_CHECK_CUDA(cudaStreamSynchronize(st));
   c.nsplit = counts[0];
   c.nempty = counts[1];
+  if (c.nempty) {
+    c.nextrow = keep_alloc<int32_t>((size_t)n, st);
+    k_next_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.erow, n, nnz, c.nextrow);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
   CRG_CHECK_CUDA(cudaMemsetAsync(c.tslot, 0xff, sizeof(int2) * c.ntasks, st));  // -1: row not cut
   c.split = keep_alloc<int32_t>((size_t)3 * c.nsplit, st);
   if (c.nsplit) {
