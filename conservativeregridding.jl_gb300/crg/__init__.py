@@ -21,6 +21,7 @@ from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
 from .batch import ApplyPlan, build_batch
 from .esmf import esmf_weights, load_esmf_weights, save_esmf_weights
 from .fold import mirror_fold_
+from .se import SpectralElementSpace, regrid_field_
 
 __all__ = [
     "ApplyPlan",
@@ -29,6 +30,7 @@ __all__ = [
     "DimensionMismatch",
     "Grid",
     "Regridder",
+    "SpectralElementSpace",
     "area_grad",
     "build_batch",
     "cubed_sphere",
@@ -47,6 +49,7 @@ __all__ = [
     "regrid",
     "regrid_",
     "regrid_adjoint_",
+    "regrid_field_",
     "regrid_pullback",
     "regular_grid",
     "reorder_cells",

@@ -21,11 +21,12 @@ INCLUDE = REPO_ROOT / "include"
 BUILD_DIR = PKG_ROOT / "_build"
 LIB_PATH = BUILD_DIR / "libcrg_gb300.so"
 
-SOURCES = ["crg_scan.cu", "crg_build.cu", "crg_layout.cu", "crg_apply.cu", "crg_grad.cu", "crg_batch.cu", "crg_api.cu"]
+SOURCES = ["crg_scan.cu", "crg_build.cu", "crg_layout.cu", "crg_apply.cu", "crg_grad.cu", "crg_batch.cu", "crg_se.cu", "crg_api.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: only explicit fma() fuses, so the FP64 geometry follows the
 # exact operation order that the CPU oracle restates.
-NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "-Xcompiler", "-ffp-contract=off"]
 
 
 def _nvcc() -> str:

@@ -47,6 +47,15 @@ class crg_build_opts(C.Structure):
     _fields_ = [("normalize", C.c_int32), ("flags", C.c_int32), ("stream", C.c_void_p)]
 
 
+class crg_se_space(C.Structure):
+    _fields_ = [("elements", crg_grid_desc), ("nq", C.c_int32), ("pad", C.c_int32), ("node_weights", C.c_void_p)]
+
+
+class crg_se_opts(C.Structure):
+    _fields_ = [("triangle_quad_degree", C.c_int32), ("flags", C.c_int32), ("radius", C.c_double),
+                ("stream", C.c_void_p)]
+
+
 class crg_apply_item(C.Structure):
     _fields_ = [
         ("regridder", C.c_void_p),
@@ -114,6 +123,13 @@ SIGNATURES = {
     "crg_get_csr": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_areas": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_row_col_sums": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "crg_build_se_to_fv": (C.c_int, [C.POINTER(crg_grid_desc), C.POINTER(crg_se_space), C.POINTER(crg_se_opts),
+                                     C.POINTER(C.c_void_p)]),
+    "crg_build_fv_to_se": (C.c_int, [C.POINTER(crg_se_space), C.POINTER(crg_grid_desc), C.POINTER(crg_se_opts),
+                                     C.POINTER(C.c_void_p)]),
+    "crg_se_nodes": (C.c_int, [C.POINTER(crg_se_space), C.POINTER(crg_se_opts), C.c_void_p, C.c_void_p]),
+    "crg_se_dss": (C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p,
+                             C.c_void_p, C.c_int64, C.c_void_p]),
     "crg_last_error": (C.c_char_p, []),
     "crg_status_string": (C.c_char_p, [C.c_int]),
     "crg_abi_version": (C.c_int32, []),

@@ -100,9 +100,17 @@ class Regridder:
     on first access), ``dst_areas``, ``src_areas``, ``dst_temp``, ``src_temp``.
     """
 
-    def __init__(self, dst, src, normalize: bool = False, stream=None, *, _view=None):
+    def __init__(self, dst, src, normalize: bool = False, stream=None, *, triangle_quad_degree=None, _view=None):
         if _view is not None:
             self.__dict__.update(_view)
+            return
+        from .se import SpectralElementSpace, build_se_regridder
+
+        if isinstance(dst, SpectralElementSpace) or isinstance(src, SpectralElementSpace):
+            # the ClimaCore methods take no normalize (ext/ConservativeRegriddingClimaCoreExt.jl:416-506)
+            self._adopt_handle(build_se_regridder(dst, src, triangle_quad_degree, stream))
+            self.dst_space = dst if isinstance(dst, SpectralElementSpace) else None
+            self.src_space = src if isinstance(src, SpectralElementSpace) else None
             return
         lib = _lib.load()
         dst_g, src_g = promote(as_grid(dst), as_grid(src))
@@ -124,6 +132,7 @@ class Regridder:
     def _adopt_handle(self, ptr: int):
         lib = _lib.load()
         self._h = _Handle(ptr)
+        self.dst_space = self.src_space = None
         self._transposed = False
         info = _lib.crg_info()
         check(lib.crg_regridder_info(C.c_void_p(ptr), C.byref(info)))
@@ -161,6 +170,7 @@ class Regridder:
         view["_transposed"] = not self._transposed
         view["dst_areas"], view["src_areas"] = self.src_areas, self.dst_areas
         view["dst_temp"], view["src_temp"] = self.src_temp, self.dst_temp
+        view["dst_space"], view["src_space"] = self.src_space, self.dst_space
         return Regridder(None, None, _view=view)
 
     @property

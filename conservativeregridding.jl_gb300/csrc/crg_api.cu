@@ -247,6 +247,37 @@ crg_status crg_get_esmf_weights(const crg_regridder* r, int32_t index_base, int6
   return guarded([&] { export_esmf(r, index_base, row, col, S, frac_a, frac_b, area_a, area_b); });
 }
 
+crg_status crg_build_se_to_fv(const crg_grid_desc* dst, const crg_se_space* src, const crg_se_opts* opts,
+                              crg_regridder** out) {
+  return guarded([&] {
+    CRG_REQUIRE(out != nullptr, CRG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    *out = build_se_impl(dst, src, opts, false);
+  });
+}
+
+crg_status crg_build_fv_to_se(const crg_se_space* dst, const crg_grid_desc* src, const crg_se_opts* opts,
+                              crg_regridder** out) {
+  return guarded([&] {
+    CRG_REQUIRE(out != nullptr, CRG_ERR_INVALID_ARGUMENT, "out is NULL");
+    *out = nullptr;
+    *out = build_se_impl(src, dst, opts, true);
+  });
+}
+
+crg_status crg_se_nodes(const crg_se_space* space, const crg_se_opts* opts, double* points, double* weights) {
+  return guarded([&] { se_nodes_impl(space, opts, points, weights); });
+}
+
+crg_status crg_se_dss(int32_t dtype, void* field, int64_t stride_node, int64_t stride_field, int64_t nfields,
+                      const int32_t* group_ptr, const int32_t* group_nodes, const double* weights, int64_t ngroups,
+                      void* stream) {
+  return guarded([&] {
+    se_dss_impl(dtype, field, stride_node, stride_field, nfields, group_ptr, group_nodes, weights, ngroups,
+                (cudaStream_t)stream);
+  });
+}
+
 const char* crg_last_error(void) { return g_err; }
 
 const char* crg_status_string(crg_status s) {

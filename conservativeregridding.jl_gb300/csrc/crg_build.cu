@@ -37,33 +37,6 @@ constexpr int kSortShift = 10;    // bins of the counting sort = key >> kSortShi
 
 // ------------------------------------------------------------------ buffers
 
-template <class T>
-struct DBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  cudaStream_t st = nullptr;
-  DBuf() = default;
-  DBuf(size_t n_, cudaStream_t s) { alloc(n_, s); }
-  DBuf(const DBuf&) = delete;
-  DBuf& operator=(const DBuf&) = delete;
-  void alloc(size_t n_, cudaStream_t s) {
-    release();
-    st = s;
-    n = n_;
-    if (n) CRG_CHECK_CUDA(cudaMallocAsync((void**)&p, n * sizeof(T), s));
-  }
-  void zero() {
-    if (n) CRG_CHECK_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st));
-  }
-  void release() {
-    if (p) cudaFreeAsync(p, st);
-    p = nullptr;
-    n = 0;
-  }
-  ~DBuf() { release(); }
-};
-
-
 inline unsigned nblk(int64_t n, int t) { return (unsigned)((n + t - 1) / t); }
 
 // ------------------------------------------------------------------ K1: cell tables
@@ -1119,6 +1092,139 @@ void free_regridder(crg_regridder* r) {
   delete r;
 }
 
+// ------------------------------------------------------------------ shared build stages
+
+struct PairSearch::Impl {
+  DevGrid gd, gs;
+  HostTree td, ts;
+  DBuf<int2> cand;
+  DBuf<double4_32a> planes;
+};
+
+PairSearch::PairSearch() : impl(new Impl) {}
+PairSearch::~PairSearch() { delete impl; }
+
+void PairSearch::upload(const crg_grid_desc* dst, const crg_grid_desc* src, cudaStream_t st) {
+  CRG_REQUIRE(dst && src, CRG_ERR_INVALID_ARGUMENT, "dst and src grids must not be NULL");
+  CRG_REQUIRE(dst->manifold == src->manifold, CRG_ERR_INVALID_ARGUMENT,
+              "Destination and source manifolds must be the same (got %d and %d); promote planar lon/lat to the sphere first",
+              dst->manifold, src->manifold);
+  sph = dst->manifold == CRG_SPHERICAL;
+  upload_grid(dst, impl->gd, st);
+  upload_grid(src, impl->gs, st);
+  nd = impl->gd.ncells;
+  ns = impl->gs.ncells;
+  dtab = impl->gd.tab;
+  stab = impl->gs.tab;
+}
+
+void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
+  build_tree(impl->gd, sph, dst_area, impl->td, st);
+  build_tree(impl->gs, sph, src_area, impl->ts, st);
+  dual_traverse(impl->td, impl->ts, sph, impl->cand, nc, st);
+  cand = impl->cand.p;
+  if (sph && nc && nd) {
+    impl->planes.alloc((size_t)nd * dtab.maxv, st);
+    k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(dtab.v, dtab.nv, dtab.ori, dtab.maxv, nd, impl->planes.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    dplanes = impl->planes.p;
+  }
+}
+
+namespace {
+
+__global__ void k_coo_count(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t m,
+                            int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  atomicAdd(&rowcnt[rows[t]], 1);
+  atomicAdd(&colcnt[cols[t]], 1);
+}
+
+// Entries land in an arbitrary order inside each row; sort_rows then orders
+// them by column (columns are distinct within a row, so the result is unique).
+__global__ void k_coo_scatter(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols,
+                              const double* __restrict__ vals, int64_t m, const int32_t* __restrict__ rowptr,
+                              int32_t* __restrict__ rowfill, const int32_t* __restrict__ colptr,
+                              int32_t* __restrict__ colfill, int32_t* __restrict__ fidx, double* __restrict__ fval,
+                              int32_t* __restrict__ ridx, double* __restrict__ rval) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const int32_t r = rows[t], c = cols[t];
+  const double v = vals[t];
+  const int32_t p = rowptr[r] + atomicAdd(&rowfill[r], 1);
+  fidx[p] = c;
+  fval[p] = v;
+  const int32_t q = colptr[c] + atomicAdd(&colfill[c], 1);
+  ridx[q] = r;
+  rval[q] = v;
+}
+
+}  // namespace
+
+void assemble_coo(crg_regridder* R, int64_t m, const int32_t* rows, const int32_t* cols, const double* vals,
+                  cudaStream_t st) {
+  CRG_REQUIRE(m < ((int64_t)1 << 31), CRG_ERR_NOT_SUPPORTED, "%lld nonzeros exceed the 32-bit entry range",
+              (long long)m);
+  const int64_t nd = R->nd, ns = R->ns;
+  DBuf<int32_t> rowcnt((size_t)nd + 1, st), colcnt((size_t)ns + 1, st);
+  rowcnt.zero();
+  colcnt.zero();
+  if (m) {
+    k_coo_count<<<nblk(m, 256), 256, 0, st>>>(rows, cols, m, rowcnt.p, colcnt.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  R->fwd.nrows = nd; R->fwd.ncols = ns;
+  R->rev.nrows = ns; R->rev.ncols = nd;
+  R->fwd.ptr = keep_alloc<int32_t>((size_t)nd + 1, st);
+  R->rev.ptr = keep_alloc<int32_t>((size_t)ns + 1, st);
+  exclusive_scan_i32(rowcnt.p, R->fwd.ptr, nd, st);
+  exclusive_scan_i32(colcnt.p, R->rev.ptr, ns, st);
+  R->nnz = m;
+  R->fwd.nnz = R->rev.nnz = m;
+  R->fwd.idx = keep_alloc<int32_t>((size_t)m, st);
+  R->fwd.val = keep_alloc<double>((size_t)m, st);
+  R->rev.idx = keep_alloc<int32_t>((size_t)m, st);
+  R->rev.val = keep_alloc<double>((size_t)m, st);
+  rowcnt.zero();
+  colcnt.zero();
+  if (m) {
+    k_coo_scatter<<<nblk(m, 256), 256, 0, st>>>(rows, cols, vals, m, R->fwd.ptr, rowcnt.p, R->rev.ptr, colcnt.p,
+                                                R->fwd.idx, R->fwd.val, R->rev.idx, R->rev.val);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  sort_rows(R->fwd.ptr, nd, R->fwd.idx, R->fwd.val, st);
+  sort_rows(R->rev.ptr, ns, R->rev.idx, R->rev.val, st);
+}
+
+void finish_build(crg_regridder* R, cudaStream_t st) {
+  const int64_t nd = R->nd, ns = R->ns, nnz = R->nnz;
+  for (DevCsr* c : {&R->fwd, &R->rev}) {
+    c->val32 = keep_alloc<float>((size_t)nnz, st);
+    c->wn32 = keep_alloc<float>((size_t)nnz, st);
+    c->adj32 = keep_alloc<float>((size_t)nnz, st);
+  }
+  R->row_sum = keep_alloc<double>((size_t)nd, st);
+  R->col_sum = keep_alloc<double>((size_t)ns, st);
+  if (nd)
+    k_derive<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, R->fwd.idx, R->fwd.val, nd, R->dst_area, R->src_area,
+                                            R->fwd.val32, R->fwd.wn32, R->fwd.adj32, R->row_sum);
+  if (ns)
+    k_derive<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, R->rev.idx, R->rev.val, ns, R->src_area, R->dst_area,
+                                            R->rev.val32, R->rev.wn32, R->rev.adj32, R->col_sum);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  build_merge_path(R->fwd, st);
+  build_merge_path(R->rev, st);
+  crg_info& I = R->info;
+  const DevCsr* cs[2] = {&R->fwd, &R->rev};
+  for (int d = 0; d < 2; ++d) {
+    I.merge_tasks[d] = cs[d]->ntasks;
+    I.cut_rows[d] = cs[d]->nsplit;
+    I.carry_slots[d] = cs[d]->nslots;
+    I.empty_rows[d] = cs[d]->nempty;
+  }
+}
+
 crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts) {
   CRG_REQUIRE(dst && src, CRG_ERR_INVALID_ARGUMENT, "dst and src grids must not be NULL");
   CRG_REQUIRE(dst->manifold == src->manifold, CRG_ERR_INVALID_ARGUMENT,
@@ -1136,21 +1242,15 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     Events ev;
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[0], st));
 
-    DevGrid gd, gs;
-    upload_grid(dst, gd, st);
-    upload_grid(src, gs, st);
-    const int64_t nd = gd.ncells, ns = gs.ncells;
+    PairSearch ps;
+    ps.upload(dst, src, st);
+    const int64_t nd = ps.nd, ns = ps.ns;
     R->nd = nd;
     R->ns = ns;
     R->dst_area = keep_alloc<double>((size_t)nd, st);
     R->src_area = keep_alloc<double>((size_t)ns, st);
-
-    HostTree td, ts;
-    build_tree(gd, sph, R->dst_area, td, st);
-    build_tree(gs, sph, R->src_area, ts, st);
-    DBuf<int2> cand;
-    int64_t nc = 0;
-    dual_traverse(td, ts, sph, cand, nc, st);
+    ps.search(R->dst_area, R->src_area, st);
+    const int64_t nc = ps.nc;
     R->ncand = nc;
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[1], st));
 
@@ -1162,19 +1262,13 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     colcnt.zero();
     ovf.zero();
     if (nc) {
-      if (sph) {
-        DBuf<double4_32a> planes((size_t)nd * gd.tab.maxv, st);
-        if (nd) {
-          k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv, nd, planes.p);
-          CRG_CHECK_CUDA(cudaGetLastError());
-        }
-        k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv, gs.tab.v,
-                                                    gs.tab.nv, gs.tab.ori, gs.tab.maxv, area.p, rowcnt.p, colcnt.p,
-                                                    ovf.p, planes.p);
-      } else
-        k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(cand.p, nc, gd.tab.v, gd.tab.nv, gd.tab.ori, gd.tab.maxv,
-                                                     gs.tab.v, gs.tab.nv, gs.tab.ori, gs.tab.maxv, area.p, rowcnt.p,
-                                                     colcnt.p, ovf.p, nullptr);
+      const CellTable &D = ps.dtab, &S = ps.stab;
+      if (sph)
+        k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(ps.cand, nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori, S.maxv,
+                                                    area.p, rowcnt.p, colcnt.p, ovf.p, ps.dplanes);
+      else
+        k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(ps.cand, nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori, S.maxv,
+                                                     area.p, rowcnt.p, colcnt.p, ovf.p, nullptr);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[2], st));
@@ -1204,7 +1298,7 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     rowcnt.zero();
     colcnt.zero();
     if (nc) {
-      k_scatter_pairs<<<nblk(nc, 256), 256, 0, st>>>(cand.p, area.p, nc, R->fwd.ptr, rowcnt.p, R->rev.ptr, colcnt.p,
+      k_scatter_pairs<<<nblk(nc, 256), 256, 0, st>>>(ps.cand, area.p, nc, R->fwd.ptr, rowcnt.p, R->rev.ptr, colcnt.p,
                                                      R->fwd.idx, R->fwd.val, R->rev.idx, R->rev.val);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
@@ -1234,23 +1328,7 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
       if (ns) k_div_by<<<nblk(ns, 256), 256, 0, st>>>(R->src_area, ns, mx.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
-    // derived FP32 weights + Kahan sums
-    for (DevCsr* c : {&R->fwd, &R->rev}) {
-      c->val32 = keep_alloc<float>((size_t)nnz, st);
-      c->wn32 = keep_alloc<float>((size_t)nnz, st);
-      c->adj32 = keep_alloc<float>((size_t)nnz, st);
-    }
-    R->row_sum = keep_alloc<double>((size_t)nd, st);
-    R->col_sum = keep_alloc<double>((size_t)ns, st);
-    if (nd)
-      k_derive<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, R->fwd.idx, R->fwd.val, nd, R->dst_area, R->src_area,
-                                              R->fwd.val32, R->fwd.wn32, R->fwd.adj32, R->row_sum);
-    if (ns)
-      k_derive<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, R->rev.idx, R->rev.val, ns, R->src_area, R->dst_area,
-                                              R->rev.val32, R->rev.wn32, R->rev.adj32, R->col_sum);
-    CRG_CHECK_CUDA(cudaGetLastError());
-    build_merge_path(R->fwd, st);
-    build_merge_path(R->rev, st);
+    finish_build(R, st);
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[3], st));
     CRG_CHECK_CUDA(cudaEventSynchronize(ev.e[3]));
     float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
@@ -1265,13 +1343,6 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     I.t_build_ms = t03; I.t_search_ms = t01; I.t_clip_ms = t12; I.t_assemble_ms = t23;
     I.clip_overflows = (int64_t)hovf;
     I.device = R->device;
-    const DevCsr* cs[2] = {&R->fwd, &R->rev};
-    for (int d = 0; d < 2; ++d) {
-      I.merge_tasks[d] = cs[d]->ntasks;
-      I.cut_rows[d] = cs[d]->nsplit;
-      I.carry_slots[d] = cs[d]->nslots;
-      I.empty_rows[d] = cs[d]->nempty;
-    }
     // temporaries are freed stream-ordered by the DBuf destructors
   } catch (...) {
     free_regridder(R);

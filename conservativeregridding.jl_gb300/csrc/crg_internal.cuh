@@ -85,6 +85,33 @@ T* keep_alloc(size_t n, cudaStream_t st) {
   return p;
 }
 
+// Stream-ordered temporary device buffer, freed (in stream order) when it goes out of scope.
+template <class T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  cudaStream_t st = nullptr;
+  DBuf() = default;
+  DBuf(size_t n_, cudaStream_t s) { alloc(n_, s); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  void alloc(size_t n_, cudaStream_t s) {
+    release();
+    st = s;
+    n = n_;
+    if (n) CRG_CHECK_CUDA(cudaMallocAsync((void**)&p, n * sizeof(T), s));
+  }
+  void zero() {
+    if (n) CRG_CHECK_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), st));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+    n = 0;
+  }
+  ~DBuf() { release(); }
+};
+
 }  // namespace crg
 
 struct crg_regridder {
@@ -122,6 +149,42 @@ bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
 void build_merge_path(DevCsr& c, cudaStream_t st);
+void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cudaStream_t st);
+
+// The search stage every build shares: both grids' cell tables on the device,
+// their exact cell areas, the candidate (dst cell, src cell) pairs of the dual
+// traversal and the edge half-spaces of the destination cells (spherical).
+// upload() first (cell counts become known), then search().
+struct PairSearch {
+  struct Impl;
+  Impl* impl = nullptr;
+  bool sph = true;
+  int64_t nd = 0, ns = 0, nc = 0;
+  CellTable dtab, stab;
+  const int2* cand = nullptr;              // [nc]
+  const double4_32a* dplanes = nullptr;    // spherical: [nd * dtab.maxv]
+  PairSearch();
+  ~PairSearch();
+  PairSearch(const PairSearch&) = delete;
+  PairSearch& operator=(const PairSearch&) = delete;
+  void upload(const crg_grid_desc* dst, const crg_grid_desc* src, cudaStream_t st);
+  // cell areas into dst_area [nd] and src_area [ns] (device memory)
+  void search(double* dst_area, double* src_area, cudaStream_t st);
+};
+
+// Fills both CSR copies of R (an R->nd x R->ns matrix, columns ascending in
+// every row) from m distinct (row, col, val) entries in device memory.
+void assemble_coo(crg_regridder* R, int64_t m, const int32_t* rows, const int32_t* cols, const double* vals,
+                  cudaStream_t st);
+// FP32 weights, Kahan row / column sums and the merge-path layouts of both
+// directions of R (after its matrix and areas are final).
+void finish_build(crg_regridder* R, cudaStream_t st);
+// crg_build_se_to_fv / crg_build_fv_to_se (crg_se.cu)
+crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, const crg_se_opts* opts,
+                             bool se_is_dst);
+void se_nodes_impl(const crg_se_space* se, const crg_se_opts* opts, double* points, double* weights);
+void se_dss_impl(int dtype, void* field, int64_t sn, int64_t sf, int64_t nfields, const int32_t* group_ptr,
+                 const int32_t* group_nodes, const double* weights, int64_t ngroups, cudaStream_t st);
 void area_grad_impl(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src, const double* u,
                     const double* s, const double* c, double* grad, cudaStream_t st);
 void mirror_fold_impl(int dtype, void* field, int64_t sc, int64_t sf, int64_t nfields, int64_t nx, int64_t ny,

@@ -270,6 +270,76 @@ crg_status crg_get_areas(const crg_regridder* r, double* dst_areas, double* src_
  * areas (lib/ConservativeRegriddingTestHelpers/src/ConservativeRegriddingTestHelpers.jl:70-73). */
 crg_status crg_get_row_col_sums(const crg_regridder* r, double* row_sums, double* col_sums);
 
+/* ------------------------------------------------------------------------
+ * Spectral-element (SE) <-> finite-volume (FV) regridders on the sphere, the
+ * ClimaCore extension of the reference (ext/ConservativeRegriddingClimaCoreExt.jl).
+ *
+ * An SE space is a set of quadrilateral elements with nq x nq Gauss-Lobatto-
+ * Legendre (GLL) nodes each.  Element e maps the reference square (xi, eta) in
+ * [-1, 1]^2 onto the sphere by the normalised bilinear map of its corners
+ * (vertex k of the element at reference corner k: (-1,-1), (1,-1), (1,1),
+ * (-1,1)); its edges are great-circle arcs.  Node (e, i, j) -- xi = x_i,
+ * eta = x_j, i fastest -- is entry e * nq^2 + i + j * nq of an SE field
+ * (ClimaCore's flattened nodal order, se_field_to_vec :368-370).
+ * ------------------------------------------------------------------------ */
+typedef struct crg_se_space {
+    crg_grid_desc elements;      /* spherical quadrilaterals (curvilinear blocks or 4-vertex cells) */
+    int32_t nq;                  /* GLL nodes per direction (ClimaCore n_quad_points), 2..8 */
+    int32_t pad;
+    const double* node_weights;  /* [nelem * nq * nq] weighted Jacobian W = J w_i w_j of every node
+                                    (Spaces.weighted_jacobian, se_node_weights :153-156), host or device;
+                                    NULL = computed from the element map on a sphere of opts->radius */
+} crg_se_space;
+
+typedef struct crg_se_opts {
+    int32_t triangle_quad_degree;  /* degree of the Dunavant triangle rule for the overlap integrals,
+                                      1..8; 0 = 2 (nq - 1), the reference's default (:434, :583) */
+    int32_t flags;                 /* reserved, must be 0 */
+    double radius;                 /* sphere radius: areas and computed node weights scale by radius^2;
+                                      0 = 1 (the unit sphere) */
+    void* stream;                  /* cudaStream_t of the build; NULL = legacy default stream */
+} crg_se_opts;
+
+/* SE source -> FV destination, the "principled" weights (se_to_fv_principled,
+ * :416-486, accumulate_principled_b :260-305): A[k, (e,i,j)] = integral over cell k ∩ element e of phi_i(xi) phi_j(eta),
+ * by fan triangulation of each overlap from its normalised vertex mean and a
+ * Dunavant rule on every triangle, (xi, eta) from the inverse element map.
+ * dst_areas = the FV cell areas, src_areas = the node weights; not normalised.
+ * regrid! then gives d = (A s) ./ a_d; constants are preserved exactly up to
+ * rounding.  Errors: CRG_ERR_INVALID_ARGUMENT for a non-spherical grid, an
+ * element without 4 vertices, nq outside 2..8 or a rule degree above 8. */
+crg_status crg_build_se_to_fv(const crg_grid_desc* dst, const crg_se_space* src, const crg_se_opts* opts,
+                              crg_regridder** out);
+
+/* FV source -> SE destination, the per-element L2 projection
+ * (fv_to_se_l2_projection :573-689, compute_local_mass_matrix :522-560): the same overlap integrals b(e, k) per
+ * element and cell, then per element the local mass matrix M^e (GLL rule of
+ * ceil((3 nq - 2) / 2) + 1 points, Jacobian interpolated from the node
+ * weights) restricted to the nodes with nonzero total b, each of its rows
+ * scaled to that total, inverted (Gauss-Jordan, partial pivoting) and applied
+ * to every cell's b.  dst_areas = ones, src_areas = the FV cell areas.  Like
+ * the reference's regrid! into a ClimaCore field, follow the apply by
+ * crg_se_dss to make shared nodes agree.  CRG_ERR_GEOMETRY if a local mass
+ * matrix is singular. */
+crg_status crg_build_fv_to_se(const crg_se_space* dst, const crg_grid_desc* src, const crg_se_opts* opts,
+                              crg_regridder** out);
+
+/* Positions (unit vectors, [nnodes][3]) and weighted Jacobians ([nnodes]) of
+ * all nodes of an SE space (se_node_positions / se_node_weights, :139-156);
+ * either output may be NULL; host or device pointers. */
+crg_status crg_se_nodes(const crg_se_space* space, const crg_se_opts* opts, double* points, double* weights);
+
+/* Weighted direct stiffness summation (ClimaCore Spaces.weighted_dss!, the
+ * finalize step of regrid! into an SE field, :709-715): every group of node
+ * copies that are the same point gets the weighted mean
+ * sum(w_n f_n) / sum(w_n) of its copies, for every field.  Groups are
+ * group_nodes[group_ptr[g] .. group_ptr[g+1]) (device memory, ascending node
+ * numbers), w = the node weights (device memory); the field is
+ * (nodes, fields) with the given strides, on `stream`. */
+crg_status crg_se_dss(int32_t dtype, void* field, int64_t stride_node, int64_t stride_field, int64_t nfields,
+                      const int32_t* group_ptr, const int32_t* group_nodes, const double* weights, int64_t ngroups,
+                      void* stream);
+
 const char* crg_last_error(void);
 const char* crg_status_string(crg_status s);
 int32_t crg_abi_version(void);

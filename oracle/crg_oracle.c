@@ -1162,3 +1162,494 @@ int og_num_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------ */
+/* Spectral-element <-> FV regridders: the ClimaCore extension              */
+/* (ext/ConservativeRegriddingClimaCoreExt.jl).                             */
+/*   SE -> FV principled weights   se_to_fv_principled :416-486,            */
+/*                                 accumulate_principled_b :260-305         */
+/*   FV -> SE L2 projection        fv_to_se_l2_projection :573-689,         */
+/*                                 compute_local_mass_matrix :522-560,      */
+/*                                 element_jacobian_at :221-237             */
+/*   triangle rules                src/regridder/triangle_quadrature.jl     */
+/* ClimaCore itself (GLL nodes, the element map, its inverse, the weighted  */
+/* Jacobian) is not vendored; restated from published methods:             */
+/*   - GLL nodes: Newton on f = x P_N - P_(N-1), f' = (N+1) P_N, from the   */
+/*     Chebyshev-Gauss-Lobatto points; weights 2 / (N (N+1) P_N^2);         */
+/*   - the normalised bilinear element map X / |X|, X = a + b xi + c eta +  */
+/*     d xi eta, inverted exactly: X || x <=> X.(x x c) = X.(x x b) = 0, a   */
+/*     quadratic in eta solved in the cancellation-free form;               */
+/*   - area element J = |X.(X_xi x X_eta)| / |X|^3;                          */
+/*   - Dunavant (1985) symmetric triangle rules, degrees 1..8;              */
+/*   - Gauss-Jordan inversion with partial pivoting.                        */
+/* Same operation order as the CUDA coding (crg_se.cu), so the matrices     */
+/* agree bit for bit.                                                       */
+/* ------------------------------------------------------------------------ */
+
+#define OG_SE_MAXNQ 8
+#define OG_SE_MAXTRI 16
+#define OG_SE_MAXMASS 12
+
+typedef struct {
+    int nq, ntri;
+    double x[OG_SE_MAXNQ], w[OG_SE_MAXNQ], c[OG_SE_MAXNQ];
+    double tl[OG_SE_MAXTRI][3], tw[OG_SE_MAXTRI];
+} og_se_rule;
+
+static void og_legendre2(int N, double t, double* pn, double* pn1) {
+    double p0 = 1.0, p1 = t;
+    for (int k = 2; k <= N; ++k) {
+        double p2 = ((double)(2 * k - 1) * t * p1 - (double)(k - 1) * p0) / (double)k;
+        p0 = p1; p1 = p2;
+    }
+    *pn = p1; *pn1 = p0;
+}
+
+void og_se_gll(int n, double* x, double* w) {
+    int N = n - 1;
+    for (int i = 0; i <= N; ++i) x[i] = -cos(3.14159265358979323846 * (double)i / (double)N);
+    for (int it = 0; it < 100; ++it) {
+        double dmax = 0.0;
+        for (int i = 0; i <= N; ++i) {
+            double pn, pn1;
+            og_legendre2(N, x[i], &pn, &pn1);
+            double dx = (x[i] * pn - pn1) / ((double)n * pn);
+            x[i] = x[i] - dx;
+            if (fabs(dx) > dmax) dmax = fabs(dx);
+        }
+        if (dmax <= 1e-15) break;
+    }
+    x[0] = -1.0; x[N] = 1.0;
+    for (int i = 0; i < n / 2; ++i) x[N - i] = -x[i];
+    if (n % 2) x[N / 2] = 0.0;
+    for (int i = 0; i <= N; ++i) {
+        double pn, pn1;
+        og_legendre2(N, x[i], &pn, &pn1);
+        w[i] = 2.0 / ((double)(N * n) * (pn * pn));
+    }
+}
+
+/* Lagrange basis on the nodes x, product form phi_j = c_j prod_(m != j) (t - x_m) */
+static void og_se_lagrange(int nq, const double* x, const double* c, double t, double* phi) {
+    double d[OG_SE_MAXNQ], suf[OG_SE_MAXNQ];
+    for (int m = 0; m < nq; ++m) d[m] = t - x[m];
+    suf[nq - 1] = 1.0;
+    for (int j = nq - 1; j > 0; --j) suf[j - 1] = suf[j] * d[j];
+    double pre = 1.0;
+    for (int j = 0; j < nq; ++j) { phi[j] = (pre * suf[j]) * c[j]; pre = pre * d[j]; }
+}
+
+/* Dunavant (1985) orbits, weights summing to 1: kind 0 centroid, kind 1
+ * permutations of (a, b, b), kind 2 permutations of (a, b, c). */
+typedef struct { int degree, kind; double w, a, b, c; } og_orbit;
+
+static int og_se_orbits(og_orbit* o) {
+    double s15 = sqrt(15.0);
+    double bp = (6.0 + s15) / 21.0, bm = (6.0 - s15) / 21.0;
+    og_orbit t[] = {
+        {1, 0, 1.0, 0, 0, 0},
+        {2, 1, 1.0 / 3.0, 2.0 / 3.0, 1.0 / 6.0, 0},
+        {3, 0, -27.0 / 48.0, 0, 0, 0},
+        {3, 1, 25.0 / 48.0, 0.6, 0.2, 0},
+        {4, 1, 0.223381589678011, 0.108103018168070, 0.445948490915965, 0},
+        {4, 1, 0.109951743655322, 0.816847572980459, 0.091576213509771, 0},
+        {5, 0, 0.225, 0, 0, 0},
+        {5, 1, (155.0 + s15) / 1200.0, 1.0 - 2.0 * bp, bp, 0},
+        {5, 1, (155.0 - s15) / 1200.0, 1.0 - 2.0 * bm, bm, 0},
+        {6, 1, 0.116786275726379, 0.501426509658179, 0.249286745170910, 0},
+        {6, 1, 0.050844906370207, 0.873821971016996, 0.063089014491502, 0},
+        {6, 2, 0.082851075618374, 0.053145049844817, 0.310352451033784, 0.636502499121399},
+        {7, 0, -0.149570044467682, 0, 0, 0},
+        {7, 1, 0.175615257433208, 0.479308067841920, 0.260345966079040, 0},
+        {7, 1, 0.053347235608838, 0.869739794195568, 0.065130102902216, 0},
+        {7, 2, 0.077113760890257, 0.048690315425316, 0.312865496004874, 0.638444188569810},
+        {8, 0, 0.144315607677787, 0, 0, 0},
+        {8, 1, 0.095091634267285, 0.081414823414554, 0.459292588292723, 0},
+        {8, 1, 0.103217370534718, 0.658861384496480, 0.170569307751760, 0},
+        {8, 1, 0.032458497623198, 0.898905543365938, 0.050547228317031, 0},
+        {8, 2, 0.027230314174435, 0.008394777409958, 0.263112829634638, 0.728492392955404},
+    };
+    int n = (int)(sizeof(t) / sizeof(t[0]));
+    memcpy(o, t, sizeof(t));
+    return n;
+}
+
+/* reference_rule(degree) (triangle_quadrature.jl): points and weights (sum 1);
+ * degrees below 1 take rule 1; returns -1 above 8. */
+int og_se_tri_rule(int degree, double* tl, double* tw) {
+    int d = degree < 1 ? 1 : degree;
+    if (d > 8) return -1;
+    og_orbit o[32];
+    int no = og_se_orbits(o), n = 0;
+    double third = 1.0 / 3.0;
+#define OG_PUT(W, A, B, C) do { tl[3 * n] = (A); tl[3 * n + 1] = (B); tl[3 * n + 2] = (C); tw[n] = (W); n++; } while (0)
+    for (int k = 0; k < no; ++k) {
+        if (o[k].degree != d) continue;
+        if (o[k].kind == 0) {
+            OG_PUT(o[k].w, third, third, third);
+        } else if (o[k].kind == 1) {
+            OG_PUT(o[k].w, o[k].a, o[k].b, o[k].b); OG_PUT(o[k].w, o[k].b, o[k].a, o[k].b);
+            OG_PUT(o[k].w, o[k].b, o[k].b, o[k].a);
+        } else {
+            OG_PUT(o[k].w, o[k].a, o[k].b, o[k].c); OG_PUT(o[k].w, o[k].a, o[k].c, o[k].b);
+            OG_PUT(o[k].w, o[k].b, o[k].a, o[k].c); OG_PUT(o[k].w, o[k].b, o[k].c, o[k].a);
+            OG_PUT(o[k].w, o[k].c, o[k].a, o[k].b); OG_PUT(o[k].w, o[k].c, o[k].b, o[k].a);
+        }
+    }
+#undef OG_PUT
+    return n;
+}
+
+static int og_se_rule_make(int nq, int degree, og_se_rule* r) {
+    r->nq = nq;
+    og_se_gll(nq, r->x, r->w);
+    for (int j = 0; j < nq; ++j) {
+        double prod = 1.0;
+        for (int m = 0; m < nq; ++m) if (m != j) prod = prod * (r->x[j] - r->x[m]);
+        r->c[j] = 1.0 / prod;
+    }
+    r->ntri = og_se_tri_rule(degree, &r->tl[0][0], r->tw);
+    return r->ntri > 0 ? 0 : -1;
+}
+
+/* a, b, c, d of the bilinear map and c x a, c x b, c x d, b x a, b x d */
+static void og_se_coeffs(const v3* q, double* g) {
+    v3 c1 = q[0], c2 = q[1], c3 = q[2], c4 = q[3], a, b, c, d;
+    a.x = 0.25 * ((c1.x + c2.x) + (c3.x + c4.x)); a.y = 0.25 * ((c1.y + c2.y) + (c3.y + c4.y));
+    a.z = 0.25 * ((c1.z + c2.z) + (c3.z + c4.z));
+    b.x = 0.25 * ((c2.x - c1.x) + (c3.x - c4.x)); b.y = 0.25 * ((c2.y - c1.y) + (c3.y - c4.y));
+    b.z = 0.25 * ((c2.z - c1.z) + (c3.z - c4.z));
+    c.x = 0.25 * ((c3.x - c2.x) + (c4.x - c1.x)); c.y = 0.25 * ((c3.y - c2.y) + (c4.y - c1.y));
+    c.z = 0.25 * ((c3.z - c2.z) + (c4.z - c1.z));
+    d.x = 0.25 * ((c1.x - c2.x) + (c3.x - c4.x)); d.y = 0.25 * ((c1.y - c2.y) + (c3.y - c4.y));
+    d.z = 0.25 * ((c1.z - c2.z) + (c3.z - c4.z));
+    v3 out[9] = {a, b, c, d, og_cross(c, a), og_cross(c, b), og_cross(c, d), og_cross(b, a), og_cross(b, d)};
+    for (int k = 0; k < 9; ++k) { g[3 * k] = out[k].x; g[3 * k + 1] = out[k].y; g[3 * k + 2] = out[k].z; }
+}
+
+static inline v3 og_v3at(const double* p) { v3 r = {p[0], p[1], p[2]}; return r; }
+
+void og_se_inverse(const double* g, v3 x, double* xi, double* eta) {
+    double A1 = og_dot(x, og_v3at(g + 12)), B1 = og_dot(x, og_v3at(g + 15)), D1 = og_dot(x, og_v3at(g + 18));
+    double A2 = og_dot(x, og_v3at(g + 21)), D2 = og_dot(x, og_v3at(g + 24));
+    double C2 = -B1;
+    double a0 = C2 * D1;
+    double b0 = (A2 * D1 + C2 * B1) - D2 * A1;
+    double c0 = A2 * B1;
+    double disc = b0 * b0 - (4.0 * a0) * c0;
+    if (disc < 0.0) disc = 0.0;
+    double q = b0 + copysign(sqrt(disc), b0);
+    *eta = q != 0.0 ? (-2.0 * c0) / q : 0.0;
+    double den = B1 + D1 * *eta;
+    *xi = den != 0.0 ? -A1 / den : 0.0;
+}
+
+/* B[i + j nq] += integral over the overlap polygon res[0..m) of phi_i(xi) phi_j(eta) */
+static void og_se_poly_b(const og_se_rule* r, const double* g, const v3* res, int m, double sig, double r2,
+                         double* B) {
+    int nq = r->nq;
+    if (m < 3) return;
+    v3 cs = res[0];
+    for (int k = 1; k < m; ++k) { cs.x = cs.x + res[k].x; cs.y = cs.y + res[k].y; cs.z = cs.z + res[k].z; }
+    double ic = 1.0 / sqrt(og_dot(cs, cs));
+    v3 cen = {cs.x * ic, cs.y * ic, cs.z * ic};
+    for (int k = 0; k < m; ++k) {
+        v3 v1 = res[k], v2 = res[k + 1 == m ? 0 : k + 1];
+        double N = og_triple(cen, v1, v2);
+        double D = ((1.0 + og_dot(cen, v1)) + og_dot(v1, v2)) + og_dot(v2, cen);
+        double At = ((2.0 * og_atan2(N, D)) * sig) * r2;
+        if (!(At > 0.0)) continue;
+        for (int gq = 0; gq < r->ntri; ++gq) {
+            double l0 = r->tl[gq][0], l1 = r->tl[gq][1], l2 = r->tl[gq][2];
+            v3 p;
+            p.x = (l0 * cen.x + l1 * v1.x) + l2 * v2.x;
+            p.y = (l0 * cen.y + l1 * v1.y) + l2 * v2.y;
+            p.z = (l0 * cen.z + l1 * v1.z) + l2 * v2.z;
+            double ip = 1.0 / sqrt(og_dot(p, p));
+            v3 x = {p.x * ip, p.y * ip, p.z * ip};
+            double xi, eta, fx[OG_SE_MAXNQ], fy[OG_SE_MAXNQ];
+            og_se_inverse(g, x, &xi, &eta);
+            og_se_lagrange(nq, r->x, r->c, xi, fx);
+            og_se_lagrange(nq, r->x, r->c, eta, fy);
+            double wA = r->tw[gq] * At;
+            for (int i = 0; i < nq; ++i) fx[i] = wA * fx[i];
+            for (int j = 0; j < nq; ++j)
+                for (int i = 0; i < nq; ++i) B[i + j * nq] = B[i + j * nq] + fx[i] * fy[j];
+        }
+    }
+}
+
+/* Node positions and weighted Jacobians of one element (W = J w_i w_j r2). */
+static void og_se_elem_nodes(const double* g, const og_se_rule* r, double r2, double* pts, double* wj) {
+    int nq = r->nq;
+    v3 a = og_v3at(g), b = og_v3at(g + 3), c = og_v3at(g + 6), d = og_v3at(g + 9);
+    for (int j = 0; j < nq; ++j)
+        for (int i = 0; i < nq; ++i) {
+            double xi = r->x[i], eta = r->x[j], xe = xi * eta;
+            v3 X;
+            X.x = ((a.x + b.x * xi) + c.x * eta) + d.x * xe;
+            X.y = ((a.y + b.y * xi) + c.y * eta) + d.y * xe;
+            X.z = ((a.z + b.z * xi) + c.z * eta) + d.z * xe;
+            double n2 = og_dot(X, X);
+            int k = i + j * nq;
+            if (pts) {
+                double ir = 1.0 / sqrt(n2);
+                pts[3 * k] = X.x * ir; pts[3 * k + 1] = X.y * ir; pts[3 * k + 2] = X.z * ir;
+            }
+            if (wj) {
+                v3 Xxi = {b.x + d.x * eta, b.y + d.y * eta, b.z + d.z * eta};
+                v3 Xeta = {c.x + d.x * xi, c.y + d.y * xi, c.z + d.z * xi};
+                double J = fabs(og_dot(X, og_cross(Xxi, Xeta))) / (n2 * sqrt(n2));
+                wj[k] = ((J * r->w[i]) * r->w[j]) * r2;
+            }
+        }
+}
+
+/* Per-element L2 projection (fv_to_se_l2_projection :634-679): M^e from the
+ * GLL rule of ceil((3 nq - 2) / 2) + 1 points and the interpolated Jacobian,
+ * restricted to the nodes of nonzero total b, rows scaled to that total,
+ * inverted; out[p][cov[rc]] = sum_cc Inv[rc][cc] b_p[cov[cc]].  Returns -1 if
+ * singular. */
+static int og_se_project(const og_se_rule* r, const double* wj_e, const double* const* b, int np, double** out) {
+    int nq = r->nq, nq2 = nq * nq;
+    int nm = (3 * nq - 2 + 1) / 2 + 1;
+    double xm[OG_SE_MAXMASS], wm[OG_SE_MAXMASS], L[OG_SE_MAXMASS][OG_SE_MAXNQ];
+    og_se_gll(nm, xm, wm);
+    for (int p = 0; p < nm; ++p) og_se_lagrange(nq, r->x, r->c, xm[p], L[p]);
+    double Jn[OG_SE_MAXNQ * OG_SE_MAXNQ], Jq[OG_SE_MAXMASS * OG_SE_MAXMASS];
+    for (int k = 0; k < nq2; ++k) Jn[k] = wj_e[k] / (r->w[k % nq] * r->w[k / nq]);
+    for (int k = 0; k < nm * nm; ++k) {
+        int pp = k % nm, qq = k / nm;
+        double s = 0.0;
+        for (int qn = 0; qn < nq; ++qn)
+            for (int pn = 0; pn < nq; ++pn) s = s + (Jn[pn + qn * nq] * L[pp][pn]) * L[qq][qn];
+        Jq[k] = s;
+    }
+    double* M = (double*)malloc(sizeof(double) * nq2 * nq2);
+    double* Inv = (double*)malloc(sizeof(double) * nq2 * nq2);
+    for (int k = 0; k < nq2 * nq2; ++k) {
+        int row = k / nq2, col = k % nq2;
+        int a = row % nq, bb = row / nq, i = col % nq, j = col / nq;
+        double s = 0.0;
+        for (int qq = 0; qq < nm; ++qq)
+            for (int pp = 0; pp < nm; ++pp) {
+                double wJ = (wm[pp] * wm[qq]) * Jq[pp + qq * nm];
+                s = s + ((((wJ * L[pp][a]) * L[pp][i]) * L[qq][bb]) * L[qq][j]);
+            }
+        M[k] = s;
+    }
+    double bfull[OG_SE_MAXNQ * OG_SE_MAXNQ];
+    int cov[OG_SE_MAXNQ * OG_SE_MAXNQ], m = 0;
+    for (int k = 0; k < nq2; ++k) {
+        double s = 0.0;
+        for (int p = 0; p < np; ++p) s = s + b[p][k];
+        bfull[k] = s;
+    }
+    for (int k = 0; k < nq2; ++k) if (bfull[k] != 0.0) cov[m++] = k;
+    for (int x = 0; x < m * m; ++x) Inv[(x / m) * nq2 + x % m] = M[cov[x / m] * nq2 + cov[x % m]];
+    for (int x = 0; x < m * m; ++x) M[(x / m) * nq2 + x % m] = Inv[(x / m) * nq2 + x % m];
+    for (int rc = 0; rc < m; ++rc) {
+        double rs = 0.0;
+        for (int cc = 0; cc < m; ++cc) rs = rs + M[rc * nq2 + cc];
+        if (rs != 0.0) {
+            double scale = bfull[cov[rc]] / rs;
+            for (int cc = 0; cc < m; ++cc) M[rc * nq2 + cc] = M[rc * nq2 + cc] * scale;
+        }
+    }
+    for (int x = 0; x < m * m; ++x) Inv[(x / m) * nq2 + x % m] = (x / m == x % m) ? 1.0 : 0.0;
+    for (int k = 0; k < m; ++k) {
+        int p = k;
+        double best = fabs(M[k * nq2 + k]);
+        for (int rr = k + 1; rr < m; ++rr)
+            if (fabs(M[rr * nq2 + k]) > best) { best = fabs(M[rr * nq2 + k]); p = rr; }
+        if (best == 0.0) { free(M); free(Inv); return -1; }
+        if (p != k)
+            for (int cc = 0; cc < m; ++cc) {
+                double t = M[k * nq2 + cc]; M[k * nq2 + cc] = M[p * nq2 + cc]; M[p * nq2 + cc] = t;
+                t = Inv[k * nq2 + cc]; Inv[k * nq2 + cc] = Inv[p * nq2 + cc]; Inv[p * nq2 + cc] = t;
+            }
+        double pk = M[k * nq2 + k];
+        for (int cc = 0; cc < m; ++cc) {
+            if (cc > k) M[k * nq2 + cc] = M[k * nq2 + cc] / pk;
+            Inv[k * nq2 + cc] = Inv[k * nq2 + cc] / pk;
+        }
+        M[k * nq2 + k] = 1.0;
+        double f[OG_SE_MAXNQ * OG_SE_MAXNQ];
+        for (int rr = 0; rr < m; ++rr) f[rr] = M[rr * nq2 + k];
+        for (int rr = 0; rr < m; ++rr) {
+            if (rr == k) continue;
+            for (int cc = 0; cc < m; ++cc) {
+                if (cc > k) M[rr * nq2 + cc] = M[rr * nq2 + cc] - f[rr] * M[k * nq2 + cc];
+                if (cc == k) M[rr * nq2 + cc] = 0.0;
+                Inv[rr * nq2 + cc] = Inv[rr * nq2 + cc] - f[rr] * Inv[k * nq2 + cc];
+            }
+        }
+    }
+    for (int p = 0; p < np; ++p) {
+        for (int k = 0; k < nq2; ++k) out[p][k] = 0.0;
+        for (int rc = 0; rc < m; ++rc) {
+            double s = 0.0;
+            for (int cc = 0; cc < m; ++cc) s = s + Inv[rc * nq2 + cc] * b[p][cov[cc]];
+            out[p][cov[rc]] = s;
+        }
+    }
+    free(M); free(Inv);
+    return 0;
+}
+
+/* SE <-> FV build.  se_is_dst = 0: SE -> FV (rows = FV cells, columns = nodes),
+ * 1: FV -> SE (rows = nodes, columns = FV cells).  node_weights may be NULL.
+ * Returns NULL with *err set: 1 bad argument (rule degree, element without 4
+ * vertices), 2 clip overflow, 3 singular mass matrix. */
+og_regridder* og_build_se(const og_grid* fv, const og_grid* elems, int nq, int degree, double radius,
+                          const double* node_weights, int se_is_dst, int use_tree, int nthreads, int* err) {
+    *err = 0;
+    og_se_rule rule;
+    if (nq < 2 || nq > OG_SE_MAXNQ || og_se_rule_make(nq, degree ? degree : 2 * (nq - 1), &rule) != 0) { *err = 1; return NULL; }
+    double r2 = (radius > 0.0 ? radius : 1.0);
+    r2 = r2 * r2;
+    int nq2 = nq * nq;
+    int64_t nelem = elems->ncells, nfv = fv->ncells, nn = nelem * nq2;
+    double* coef = (double*)malloc(sizeof(double) * 27 * (nelem > 0 ? nelem : 1));
+    for (int64_t e = 0; e < nelem; ++e) {
+        v3 v[OG_MAXV];
+        if (og_cell_verts(elems, e, v) != 4) { free(coef); *err = 1; return NULL; }
+        og_se_coeffs(v, coef + 27 * e);
+    }
+    double* wj = (double*)malloc(sizeof(double) * (nn > 0 ? nn : 1));
+    if (node_weights) memcpy(wj, node_weights, sizeof(double) * nn);
+    else for (int64_t e = 0; e < nelem; ++e) og_se_elem_nodes(coef + 27 * e, &rule, r2, NULL, wj + e * nq2);
+    const og_grid* dst = se_is_dst ? elems : fv;
+    const og_grid* src = se_is_dst ? fv : elems;
+    int64_t* cand = NULL;
+    int64_t nc = og_candidates(dst, src, use_tree, nthreads, &cand);
+    double* bv = (double*)calloc((size_t)(nc > 0 ? nc : 1) * nq2, sizeof(double));
+    int64_t ovf_total = 0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : ovf_total)
+    for (int64_t k = 0; k < nc; ++k) {
+        v3 s[OG_MAXV], d[OG_MAXV], res[OG_MAXC];
+        int ns_ = og_cell_verts(src, cand[2 * k], s);
+        int nd_ = og_cell_verts(dst, cand[2 * k + 1], d);
+        if (ns_ < 3 || nd_ < 3) continue;
+        int m = og_clip_sph(s, ns_, d, nd_, res);
+        if (m < 0) { ovf_total += 1; continue; }
+        int64_t e = se_is_dst ? cand[2 * k + 1] : cand[2 * k];
+        og_se_poly_b(&rule, coef + 27 * e, res, m, og_orient_sph(s, ns_), r2, bv + k * nq2);
+    }
+    if (ovf_total) { free(coef); free(wj); free(cand); free(bv); *err = 2; return NULL; }
+    double* vals = bv;
+    double* pv = NULL;
+    if (se_is_dst) {
+        /* pairs with a nonzero b, grouped by element, cells ascending */
+        int64_t* ecnt = (int64_t*)calloc(nelem + 1, sizeof(int64_t));
+        char* has = (char*)calloc(nc > 0 ? nc : 1, 1);
+        for (int64_t k = 0; k < nc; ++k) {
+            for (int q = 0; q < nq2; ++q) if (bv[k * nq2 + q] != 0.0) { has[k] = 1; break; }
+            if (has[k]) ecnt[cand[2 * k + 1] + 1]++;
+        }
+        for (int64_t e = 0; e < nelem; ++e) ecnt[e + 1] += ecnt[e];
+        int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (nelem + 1));
+        memcpy(fill, ecnt, sizeof(int64_t) * (nelem + 1));
+        int64_t* plist = (int64_t*)malloc(sizeof(int64_t) * (ecnt[nelem] > 0 ? ecnt[nelem] : 1));
+        for (int64_t k = 0; k < nc; ++k) if (has[k]) plist[fill[cand[2 * k + 1]]++] = k;
+        for (int64_t e = 0; e < nelem; ++e) {  /* insertion sort by cell */
+            for (int64_t p = ecnt[e] + 1; p < ecnt[e + 1]; ++p) {
+                int64_t t = plist[p], q = p - 1;
+                while (q >= ecnt[e] && cand[2 * plist[q]] > cand[2 * t]) { plist[q + 1] = plist[q]; q--; }
+                plist[q + 1] = t;
+            }
+        }
+        pv = (double*)calloc((size_t)(nc > 0 ? nc : 1) * nq2, sizeof(double));
+        int bad = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : bad)
+        for (int64_t e = 0; e < nelem; ++e) {
+            int64_t np = ecnt[e + 1] - ecnt[e];
+            if (np == 0) continue;
+            const double** bp = (const double**)malloc(sizeof(double*) * np);
+            double** op = (double**)malloc(sizeof(double*) * np);
+            for (int64_t p = 0; p < np; ++p) {
+                bp[p] = bv + plist[ecnt[e] + p] * nq2;
+                op[p] = pv + plist[ecnt[e] + p] * nq2;
+            }
+            if (og_se_project(&rule, wj + e * nq2, bp, (int)np, op) != 0) bad += 1;
+            free(bp); free(op);
+        }
+        free(ecnt); free(has); free(fill); free(plist);
+        if (bad) { free(coef); free(wj); free(cand); free(bv); free(pv); *err = 3; return NULL; }
+        vals = pv;
+    }
+    /* COO in pair order -> sparse() */
+    int64_t m = 0;
+    for (int64_t k = 0; k < nc * nq2; ++k) m += vals[k] != 0.0;
+    int64_t* ir = (int64_t*)malloc(sizeof(int64_t) * (m > 0 ? m : 1));
+    int64_t* ic = (int64_t*)malloc(sizeof(int64_t) * (m > 0 ? m : 1));
+    double* iv = (double*)malloc(sizeof(double) * (m > 0 ? m : 1));
+    int64_t o = 0;
+    for (int64_t k = 0; k < nc; ++k) {
+        int64_t e = se_is_dst ? cand[2 * k + 1] : cand[2 * k];
+        int64_t cell = se_is_dst ? cand[2 * k] : cand[2 * k + 1];
+        for (int q = 0; q < nq2; ++q) {
+            double v = vals[k * nq2 + q];
+            if (v == 0.0) continue;
+            int64_t node = e * nq2 + q;
+            ir[o] = se_is_dst ? node : cell;
+            ic[o] = se_is_dst ? cell : node;
+            iv[o] = v;
+            o++;
+        }
+    }
+    og_regridder* R = (og_regridder*)calloc(1, sizeof(og_regridder));
+    R->nd = se_is_dst ? nn : nfv;
+    R->ns = se_is_dst ? nfv : nn;
+    R->ncand = nc;
+    og_sparse(R, ir, ic, iv, m);
+    R->dst_areas = (double*)malloc(sizeof(double) * (R->nd > 0 ? R->nd : 1));
+    R->src_areas = (double*)malloc(sizeof(double) * (R->ns > 0 ? R->ns : 1));
+    double* fva = se_is_dst ? R->src_areas : R->dst_areas;
+    for (int64_t i = 0; i < nfv; ++i) { v3 v[OG_MAXV]; int n = og_cell_verts(fv, i, v); fva[i] = og_cell_area(1, v, n) * r2; }
+    if (se_is_dst) for (int64_t i = 0; i < nn; ++i) R->dst_areas[i] = 1.0;
+    else memcpy(R->src_areas, wj, sizeof(double) * nn);
+    free(ir); free(ic); free(iv); free(coef); free(wj); free(cand); free(bv); free(pv);
+    return R;
+}
+
+/* Hooks for the SE known-answer tests. */
+void og_se_lagrange_hook(int nq, double t, double* phi) {
+    og_se_rule r;
+    og_se_rule_make(nq, 1, &r);
+    og_se_lagrange(nq, r.x, r.c, t, phi);
+}
+
+void og_se_inverse_hook(const double* corners12, const double* x3, double* out2) {
+    v3 q[4];
+    for (int k = 0; k < 4; ++k) q[k] = og_v3at(corners12 + 3 * k);
+    double g[27];
+    og_se_coeffs(q, g);
+    og_se_inverse(g, og_v3at(x3), &out2[0], &out2[1]);
+}
+
+void og_se_nodes_hook(const double* corners12, int nq, double radius, double* pts, double* wj) {
+    v3 q[4];
+    for (int k = 0; k < 4; ++k) q[k] = og_v3at(corners12 + 3 * k);
+    double g[27];
+    og_se_coeffs(q, g);
+    og_se_rule r;
+    og_se_rule_make(nq, 1, &r);
+    double r2 = (radius > 0.0 ? radius : 1.0);
+    og_se_elem_nodes(g, &r, r2 * r2, pts, wj);
+}
+
+/* b of one element over a given polygon (counter-clockwise unit vectors). */
+int og_se_poly_b_hook(const double* corners12, const double* poly, int m, int nq, int degree, double* B) {
+    v3 q[4], p[OG_MAXC];
+    if (m > OG_MAXC) return -1;
+    for (int k = 0; k < 4; ++k) q[k] = og_v3at(corners12 + 3 * k);
+    for (int k = 0; k < m; ++k) p[k] = og_v3at(poly + 3 * k);
+    double g[27];
+    og_se_coeffs(q, g);
+    og_se_rule r;
+    if (og_se_rule_make(nq, degree ? degree : 2 * (nq - 1), &r) != 0) return -1;
+    for (int k = 0; k < nq * nq; ++k) B[k] = 0.0;
+    og_se_poly_b(&r, g, p, m, og_orient_sph(p, m), 1.0, B);
+    return 0;
+}

@@ -81,6 +81,14 @@ def load() -> C.CDLL:
                 "og_healpix_corners": (None, [i64, i64, vp]),
                 "og_healpix_nest2ring": (i64, [i64, i64]),
                 "og_num_threads": (C.c_int, []),
+                "og_build_se": (vp, [C.POINTER(og_grid), C.POINTER(og_grid), C.c_int, C.c_int, dbl, vp, C.c_int,
+                                     C.c_int, C.c_int, C.POINTER(C.c_int)]),
+                "og_se_gll": (None, [C.c_int, vp, vp]),
+                "og_se_tri_rule": (C.c_int, [C.c_int, vp, vp]),
+                "og_se_lagrange_hook": (None, [C.c_int, dbl, vp]),
+                "og_se_inverse_hook": (None, [vp, vp, vp]),
+                "og_se_nodes_hook": (None, [vp, C.c_int, dbl, vp, vp]),
+                "og_se_poly_b_hook": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, vp]),
             }
             for n, (r, a) in sig.items():
                 f = getattr(lib, n)
@@ -215,3 +223,89 @@ def healpix_corners(nside, pix) -> np.ndarray:
 
 def healpix_nest2ring(nside, pix) -> int:
     return load().og_healpix_nest2ring(int(nside), int(pix))
+
+
+# ----------------------------------------------------------------- spectral elements
+
+class OracleSERegridder(OracleRegridder):
+    """CPU restatement of the ClimaCore extension's regridders: SE -> FV
+    (se_is_dst False: ``fv`` is the destination) or FV -> SE (se_is_dst True),
+    on the element grid ``elements`` with nq GLL nodes per direction."""
+
+    def __init__(self, fv, elements, nq, se_is_dst, degree=0, radius=1.0, node_weights=None, use_tree=True,
+                 nthreads=0):
+        lib = load()
+        df, k1 = _desc(fv)
+        de, k2 = _desc(elements)
+        w = None if node_weights is None else np.ascontiguousarray(node_weights, np.float64)
+        err = C.c_int(0)
+        self._h = lib.og_build_se(C.byref(df), C.byref(de), int(nq), int(degree), float(radius),
+                                  None if w is None else w.ctypes.data, int(bool(se_is_dst)), int(bool(use_tree)),
+                                  int(nthreads), C.byref(err))
+        if not self._h:
+            raise RuntimeError({1: "bad argument", 2: "clip capacity overflow", 3: "singular mass matrix"}
+                               .get(err.value, "error"))
+        nn = elements.ncells * nq * nq
+        self.nd, self.ns = (nn, fv.ncells) if se_is_dst else (fv.ncells, nn)
+        self.nnz = lib.og_nnz(self._h)
+        self.ncand = lib.og_ncand(self._h)
+        self.overflows = 0
+        self.colptr = np.empty(self.ns + 1, np.int64)
+        self.rowval = np.empty(max(self.nnz, 1), np.int64)
+        self.nzval = np.empty(max(self.nnz, 1), np.float64)
+        lib.og_get_csc(self._h, self.colptr.ctypes.data, self.rowval.ctypes.data, self.nzval.ctypes.data)
+        self.rowval = self.rowval[: self.nnz]
+        self.nzval = self.nzval[: self.nnz]
+        self.dst_areas = np.empty(self.nd)
+        self.src_areas = np.empty(self.ns)
+        lib.og_get_areas(self._h, self.dst_areas.ctypes.data, self.src_areas.ctypes.data)
+        del k1, k2
+
+
+def se_gll(n):
+    """GLL nodes and weights on [-1, 1] (n points)."""
+    x, w = np.empty(n), np.empty(n)
+    load().og_se_gll(int(n), x.ctypes.data, w.ctypes.data)
+    return x, w
+
+
+def se_tri_rule(degree):
+    """Barycentric points (n, 3) and weights (summing to 1) of the triangle rule."""
+    tl, tw = np.empty((16, 3)), np.empty(16)
+    n = load().og_se_tri_rule(int(degree), tl.ctypes.data, tw.ctypes.data)
+    if n < 0:
+        raise ValueError(f"no triangle rule of degree {degree}")
+    return tl[:n].copy(), tw[:n].copy()
+
+
+def se_lagrange(nq, t):
+    phi = np.empty(nq)
+    load().og_se_lagrange_hook(int(nq), float(t), phi.ctypes.data)
+    return phi
+
+
+def se_inverse(corners, x):
+    """(xi, eta) of the unit vector x in the element with corners (4, 3)."""
+    c = np.ascontiguousarray(corners, np.float64)
+    xv = np.ascontiguousarray(x, np.float64)
+    out = np.empty(2)
+    load().og_se_inverse_hook(c.ctypes.data, xv.ctypes.data, out.ctypes.data)
+    return out[0], out[1]
+
+
+def se_nodes(corners, nq, radius=1.0):
+    """Node positions (nq^2, 3) and weighted Jacobians (nq^2) of one element."""
+    c = np.ascontiguousarray(corners, np.float64)
+    pts, wj = np.empty((nq * nq, 3)), np.empty(nq * nq)
+    load().og_se_nodes_hook(c.ctypes.data, int(nq), float(radius), pts.ctypes.data, wj.ctypes.data)
+    return pts, wj
+
+
+def se_poly_b(corners, poly, nq, degree=0):
+    """b[i + j nq] = integral over the polygon of phi_i(xi) phi_j(eta) (unit sphere)."""
+    c = np.ascontiguousarray(corners, np.float64)
+    p = np.ascontiguousarray(poly, np.float64)
+    B = np.empty(nq * nq)
+    if load().og_se_poly_b_hook(c.ctypes.data, p.ctypes.data, len(p), int(nq), int(degree), B.ctypes.data) != 0:
+        raise ValueError("bad polygon or rule")
+    return B
