@@ -56,10 +56,11 @@ def parse():
     p.add_argument("--pair", default="c5", choices=["c5", "identity"],
                    help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
                         "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
-    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1"],
+    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1", "se"],
                    help="c5: the headline (HEALPix 256 <-> 0.25 degree, 128 fields); c3: 32 jittered lon-lat "
                         "pairs of uneven resolution built as one batch and applied as one CUDA graph; c1: the "
-                        "small FP64 case (2 degree -> shifted 3 degree lon-lat), build and plain FP64 apply")
+                        "small FP64 case (2 degree -> shifted 3 degree lon-lat), build and plain FP64 apply; se: "
+                        "spectral-element C48 (nq 4) <-> 0.5 degree lon-lat, both builds, the oracle's beside them")
     return p.parse_args()
 
 
@@ -655,6 +656,60 @@ def run_c1(a):
                            "note": "one launch of ~16 K rows: launch-latency bound"}}
 
 
+def run_se(a):
+    """Spectral-element C48 space with 4 x 4 GLL nodes per element (ClimaCore
+    CubedSphereSpace(h_elem = 48, n_quad_points = 4)) and the 0.5-degree
+    lon-lat grid: SE -> FV principled and FV -> SE L2-projection builds
+    (median of 5 each, pairs = nonzeros), the FP64 apply of one field each way,
+    and the oracle's builds (all host threads) of the same pair."""
+    import torch
+
+    from crg import Regridder, SpectralElementSpace, grids, regrid_
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    space, fv = SpectralElementSpace.cubed_sphere(48, 4), grids.lonlat_regular(0.5, 0.5)
+    out = {"metric": "SE <-> FV build pairs/s", "workload": "cubed sphere C48, nq 4 (36,864 nodes) <-> lonlat 0.5deg",
+           "n_nodes": space.nnodes, "n_fv": fv.ncells}
+    for name, make in (("se_to_fv", lambda: Regridder(fv, space)), ("fv_to_se", lambda: Regridder(space, fv))):
+        make()
+        times = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            R = make()
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        tb = statistics.median(times)
+        nd, ns = R.shape
+        s = torch.rand(ns, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(1))
+        d = torch.empty(nd, dtype=torch.float64, device=dev)
+        for _ in range(max(a.warmup, 3)):
+            regrid_(d, R, s)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stream = torch.cuda.current_stream(dev)
+        e0.record(stream)
+        for _ in range(50):
+            regrid_(d, R, s)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / 50
+        out[name] = {"build_ms_median": round(tb * 1e3, 3), "nnz": R.nnz, "candidates": R.info["n_candidates"],
+                     "pairs_per_s": round(R.nnz / tb, 1), "overlap_integrals_ms": round(R.info["t_clip_ms"], 3),
+                     "apply_fp64_ms": round(ms, 4)}
+    if not a.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import oracle
+
+        for name, se_dst in (("se_to_fv", False), ("fv_to_se", True)):
+            t0 = time.perf_counter()
+            O = oracle.OracleSERegridder(fv, space.elements, 4, se_dst)
+            out[name]["oracle_build_s"] = round(time.perf_counter() - t0, 3)
+            out[name]["oracle_threads"] = oracle.load().og_num_threads()
+            out[name]["same_nnz_as_oracle"] = O.nnz == out[name]["nnz"]
+    return out
+
+
 # ----------------------------------------------------------------- CPU legs (oracle)
 
 def cpu_baseline(hp, ll, K, sample_fields):
@@ -732,9 +787,9 @@ def main():
     if a.profile:
         run_profile(a)
         return
-    if a.workload in ("c3", "c1"):
+    if a.workload in ("c3", "c1", "se"):
         if rank == 0:
-            print(json.dumps(run_c3(a) if a.workload == "c3" else run_c1(a)))
+            print(json.dumps({"c3": run_c3, "c1": run_c1, "se": run_se}[a.workload](a)))
         return
     if a.impl == "reference":
         if rank == 0:

@@ -17,7 +17,7 @@
 //   c = (-c1 - c2 + c3 + c4) / 4, d = (c1 - c2 + c3 - c4) / 4
 // (the normalised bilinear element map; its edges are great-circle arcs, so
 // the element is the quadrilateral the candidate search and the clip see).
-// Inverse map: X(xi, eta) is parallel to the unit vector x exactly when
+// Inverse map: X(xi, eta) is parallel to the vector x exactly when
 // X.(x x c) = 0 and X.(x x b) = 0, i.e.
 //   A1 + B1 xi + D1 xi eta = 0,   A2 - B1 eta + D2 xi eta = 0
 // with A1 = x.(c x a), B1 = x.(c x b), D1 = x.(c x d), A2 = x.(b x a),
@@ -262,13 +262,13 @@ __device__ __forceinline__ void se_inverse(const InvMap& m, d3 x, double& xi, do
   const double A1 = ddot(x, m.P), B1 = ddot(x, m.Q), D1 = ddot(x, m.R), A2 = ddot(x, m.S), D2 = ddot(x, m.U);
   const double C2 = -B1;
   const double a0 = C2 * D1;
-  const double b0 = (A2 * D1 + C2 * B1) - D2 * A1;
+  const double b0 = fma(-D2, A1, fma(A2, D1, C2 * B1));
   const double c0 = A2 * B1;
-  double disc = b0 * b0 - (4.0 * a0) * c0;
+  double disc = fma(b0, b0, -(4.0 * a0) * c0);
   if (disc < 0.0) disc = 0.0;
   const double q = b0 + copysign(sqrt(disc), b0);
   eta = q != 0.0 ? (-2.0 * c0) / q : 0.0;
-  const double den = B1 + D1 * eta;
+  const double den = fma(D1, eta, B1);
   xi = den != 0.0 ? -A1 / den : 0.0;
 }
 
@@ -382,12 +382,12 @@ __global__ void __launch_bounds__(128)
       if (!(At > 0.0)) continue;
       for (int g = 0; g < r.ntri; ++g) {
         const double l0 = r.tl[g][0], l1 = r.tl[g][1], l2 = r.tl[g][2];
-        d3 p;
-        p.x = (l0 * cen.x + l1 * v1.x) + l2 * v2.x;
-        p.y = (l0 * cen.y + l1 * v1.y) + l2 * v2.y;
-        p.z = (l0 * cen.z + l1 * v1.z) + l2 * v2.z;
-        const double ip = 1.0 / sqrt(ddot(p, p));
-        const d3 x{p.x * ip, p.y * ip, p.z * ip};
+        // the rule point l0 cen + l1 v1 + l2 v2; the inverse map is invariant
+        // under scaling of x, so its projection onto the sphere is not needed
+        d3 x;
+        x.x = fma(l2, v2.x, fma(l1, v1.x, l0 * cen.x));
+        x.y = fma(l2, v2.y, fma(l1, v1.y, l0 * cen.y));
+        x.z = fma(l2, v2.z, fma(l1, v1.z, l0 * cen.z));
         double xi, eta;
         se_inverse(im, x, xi, eta);
         double fx[M], fy[M];
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(128)
         for (int j = 0; j < M; ++j)
 #pragma unroll
           for (int i = 0; i < M; ++i)
-            if (i < nq && j < nq) B[i + j * nq] = B[i + j * nq] + fx[i] * fy[j];
+            if (i < nq && j < nq) B[i + j * nq] = fma(fx[i], fy[j], B[i + j * nq]);
       }
     }
   }

@@ -260,6 +260,74 @@ function esmf_weights(A::GB300Sparse)
     return (; S, row, col, frac_a, frac_b, area_a, area_b)
 end
 
+# ---------------------------------------------------------------- spectral elements
+
+struct CrgSeSpace
+    elements::CrgGridDesc
+    nq::Int32
+    pad::Int32
+    node_weights::Ptr{Float64}
+end
+
+struct CrgSeOpts
+    triangle_quad_degree::Int32
+    flags::Int32
+    radius::Float64
+    stream::Ptr{Cvoid}
+end
+
+"""
+    build_se(fv, elements, nq; se_is_dst, node_weights = nothing, triangle_quad_degree = 0, radius = 1.0)
+
+GPU build of the ClimaCore extension's regridders: SE -> FV principled weights
+(`se_is_dst = false`, `crg_build_se_to_fv`, the method `Regridder(manifold, dst, src::SESpaceOrField)`)
+or the FV -> SE L2 projection (`se_is_dst = true`, `crg_build_fv_to_se`).  `elements` is the
+element grid (e.g. `curvilinear` of each cube face's corner matrix), `node_weights` ClimaCore's
+`Spaces.weighted_jacobian` flattened like `se_node_weights`.
+"""
+function build_se(fv, elements, nq::Integer; se_is_dst::Bool, node_weights = nothing,
+                  triangle_quad_degree::Integer = 0, radius::Real = 1.0)
+    f, keep_f = fv
+    e, keep_e = elements
+    w = node_weights === nothing ? Ptr{Float64}(C_NULL) : pointer(node_weights)
+    space = Ref(CrgSeSpace(e, Int32(nq), 0, w))
+    opts = Ref(CrgSeOpts(Int32(triangle_quad_degree), 0, Float64(radius), C_NULL))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    GC.@preserve keep_f keep_e node_weights begin
+        if se_is_dst
+            check(ccall((:crg_build_fv_to_se, libcrg[]), Cint,
+                        (Ref{CrgSeSpace}, Ref{CrgGridDesc}, Ref{CrgSeOpts}, Ref{Ptr{Cvoid}}), space, Ref(f), opts, out))
+        else
+            check(ccall((:crg_build_se_to_fv, libcrg[]), Cint,
+                        (Ref{CrgGridDesc}, Ref{CrgSeSpace}, Ref{CrgSeOpts}, Ref{Ptr{Cvoid}}), Ref(f), space, opts, out))
+        end
+    end
+    A = GB300Sparse(out[])
+    nd, ns = size(A)
+    dst_areas = Vector{Float64}(undef, nd)
+    src_areas = Vector{Float64}(undef, ns)
+    check(ccall((:crg_get_areas, libcrg[]), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), A.ptr, dst_areas, src_areas))
+    return A, dst_areas, src_areas
+end
+
+"""
+    se_dss!(field::CuArray, group_ptr, group_nodes, weights; nfields = 1)
+
+`crg_se_dss`: the weighted DSS of `Spaces.weighted_dss!` on a flat nodal field
+(device arrays; groups of coincident nodes as CSR).
+"""
+function se_dss!(field, group_ptr, group_nodes, weights; stream::Ptr{Cvoid} = C_NULL)
+    T = eltype(field)
+    dt = T == Float64 ? CRG_F64 : T == Float32 ? CRG_F32 : throw(ArgumentError("unsupported eltype $T"))
+    n = size(field, 1)
+    nf = length(field) ÷ n
+    check(ccall((:crg_se_dss, libcrg[]), Cint,
+                (Int32, Ptr{Cvoid}, Int64, Int64, Int64, Ptr{Int32}, Ptr{Int32}, Ptr{Float64}, Int64, Ptr{Cvoid}),
+                dt, pointer(field), 1, n, nf, pointer(group_ptr), pointer(group_nodes), pointer(weights),
+                length(group_ptr) - 1, stream))
+    return field
+end
+
 "CSC copy of A with Julia's 1-based indices: the reference's `R.intersections`."
 function SparseArrays.SparseMatrixCSC(A::GB300Sparse)
     nd, ns = size(A)

@@ -1334,13 +1334,13 @@ void og_se_inverse(const double* g, v3 x, double* xi, double* eta) {
     double A2 = og_dot(x, og_v3at(g + 21)), D2 = og_dot(x, og_v3at(g + 24));
     double C2 = -B1;
     double a0 = C2 * D1;
-    double b0 = (A2 * D1 + C2 * B1) - D2 * A1;
+    double b0 = fma(-D2, A1, fma(A2, D1, C2 * B1));
     double c0 = A2 * B1;
-    double disc = b0 * b0 - (4.0 * a0) * c0;
+    double disc = fma(b0, b0, -(4.0 * a0) * c0);
     if (disc < 0.0) disc = 0.0;
     double q = b0 + copysign(sqrt(disc), b0);
     *eta = q != 0.0 ? (-2.0 * c0) / q : 0.0;
-    double den = B1 + D1 * *eta;
+    double den = fma(D1, *eta, B1);
     *xi = den != 0.0 ? -A1 / den : 0.0;
 }
 
@@ -1361,12 +1361,11 @@ static void og_se_poly_b(const og_se_rule* r, const double* g, const v3* res, in
         if (!(At > 0.0)) continue;
         for (int gq = 0; gq < r->ntri; ++gq) {
             double l0 = r->tl[gq][0], l1 = r->tl[gq][1], l2 = r->tl[gq][2];
-            v3 p;
-            p.x = (l0 * cen.x + l1 * v1.x) + l2 * v2.x;
-            p.y = (l0 * cen.y + l1 * v1.y) + l2 * v2.y;
-            p.z = (l0 * cen.z + l1 * v1.z) + l2 * v2.z;
-            double ip = 1.0 / sqrt(og_dot(p, p));
-            v3 x = {p.x * ip, p.y * ip, p.z * ip};
+            /* the rule point; the inverse map does not depend on its length */
+            v3 x;
+            x.x = fma(l2, v2.x, fma(l1, v1.x, l0 * cen.x));
+            x.y = fma(l2, v2.y, fma(l1, v1.y, l0 * cen.y));
+            x.z = fma(l2, v2.z, fma(l1, v1.z, l0 * cen.z));
             double xi, eta, fx[OG_SE_MAXNQ], fy[OG_SE_MAXNQ];
             og_se_inverse(g, x, &xi, &eta);
             og_se_lagrange(nq, r->x, r->c, xi, fx);
@@ -1374,7 +1373,7 @@ static void og_se_poly_b(const og_se_rule* r, const double* g, const v3* res, in
             double wA = r->tw[gq] * At;
             for (int i = 0; i < nq; ++i) fx[i] = wA * fx[i];
             for (int j = 0; j < nq; ++j)
-                for (int i = 0; i < nq; ++i) B[i + j * nq] = B[i + j * nq] + fx[i] * fy[j];
+                for (int i = 0; i < nq; ++i) B[i + j * nq] = fma(fx[i], fy[j], B[i + j * nq]);
         }
     }
 }
