@@ -443,7 +443,8 @@ def run_ours(a, rank, world):
                    "weights": "fp32, FP64-built", "accumulate": "fp32"},
         "fields_per_s": round(world * 2 * K / (ms * 1e-3), 1),
         "build": {"ms": round(build_s * 1e3, 3), "pairs_per_s": round(nnz / build_s, 1),
-                  "candidates": info["n_candidates"], "search_ms": round(info["t_search_ms"], 3),
+                  "candidates": info["n_candidates"], "clipped": info["n_clipped"],
+                  "search_ms": round(info["t_search_ms"], 3),
                   "clip_ms": round(info["t_clip_ms"], 3), "assemble_ms": round(info["t_assemble_ms"], 3)},
         "fp64_one_field_per_launch": {"ms_per_field_both_directions": round(ms64, 4), "GB/s": round(fp64_gbs, 2),
                                       "fields_per_s": round(2 / (ms64 * 1e-3), 1)},

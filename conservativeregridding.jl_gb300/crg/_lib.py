@@ -93,6 +93,7 @@ class crg_info(C.Structure):
         ("cut_rows", C.c_int64 * 2),
         ("carry_slots", C.c_int64 * 2),
         ("empty_rows", C.c_int64 * 2),
+        ("n_clipped", C.c_int64),
     ]
 
 

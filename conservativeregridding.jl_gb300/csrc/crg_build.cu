@@ -497,6 +497,55 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 // ------------------------------------------------------------------ K4: clip + area
 
 // Every destination edge's half-space, once per cell (the clip of each pair reads it).
+// Separation filter of the candidate pairs (spherical).  A pair whose source
+// cell lies strictly outside one destination edge half-space has no overlap:
+// the FP64 clip would empty the polygon at that edge, so the pair is dropped
+// before it.  Decided in FP32: with n32 the plane normal rounded from FP64 and
+// w32 = v32 - ca32 from rounded unit vectors, |s32 - n.(v - ca)| stays below
+// 2^-21 |n32|_1 (1 + |w32|_inf) (inputs 2^-24 relative, the dot product 3
+// roundings, the FP64 normal's own error far smaller), so s32 < -B with
+// B = 2^-18 |n32|_1 (1 + |w32|_1) is outside by an 8x margin.
+__global__ void __launch_bounds__(256)
+    k_separated(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
+                const int8_t* __restrict__ dnv, int dmaxv, const double* __restrict__ sv,
+                const int8_t* __restrict__ snv, int smaxv, const double4_32a* __restrict__ planes,
+                int32_t* __restrict__ keep) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc) return;
+  const int2 pr = cand[t];
+  const int nd = dnv[pr.x], ns = snv[pr.y];
+  if (nd < 3 || ns < 3) {  // no polygon: never an entry
+    keep[t] = 0;
+    return;
+  }
+  float3 v[CRG_MAXV];
+  const double* q = sv + (int64_t)pr.y * smaxv * 3;
+  for (int i = 0; i < ns; ++i) v[i] = make_float3((float)q[3 * i], (float)q[3 * i + 1], (float)q[3 * i + 2]);
+  const double* c = dv + (int64_t)pr.x * dmaxv * 3;
+  int sep = 0;
+  for (int k = 0; k < nd && !sep; ++k) {
+    const double4_32a p = planes[(int64_t)pr.x * dmaxv + k];
+    const float nx = (float)p.x, ny = (float)p.y, nz = (float)p.z;
+    const float ax = (float)c[3 * k], ay = (float)c[3 * k + 1], az = (float)c[3 * k + 2];
+    const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+    int out = 1;
+    for (int i = 0; i < ns && out; ++i) {
+      const float wx = v[i].x - ax, wy = v[i].y - ay, wz = v[i].z - az;
+      const float s = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
+      const float B = 3.814697265625e-06f * n1 * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
+      out = s < -B;
+    }
+    sep = out;
+  }
+  keep[t] = !sep;
+}
+
+__global__ void k_compact_pairs(const int2* __restrict__ cand, int64_t nc, const int32_t* __restrict__ keep,
+                                const int32_t* __restrict__ pos, int2* __restrict__ out) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nc && keep[t]) out[pos[t]] = cand[t];
+}
+
 __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __restrict__ nv,
                               const int8_t* __restrict__ ori, int maxv, int64_t ncells, double4_32a* __restrict__ planes) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1097,7 +1146,7 @@ void free_regridder(crg_regridder* r) {
 struct PairSearch::Impl {
   DevGrid gd, gs;
   HostTree td, ts;
-  DBuf<int2> cand;
+  DBuf<int2> cand, kept;
   DBuf<double4_32a> planes;
 };
 
@@ -1122,12 +1171,27 @@ void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
   build_tree(impl->gd, sph, dst_area, impl->td, st);
   build_tree(impl->gs, sph, src_area, impl->ts, st);
   dual_traverse(impl->td, impl->ts, sph, impl->cand, nc, st);
+  nc_search = nc;
   cand = impl->cand.p;
   if (sph && nc && nd) {
     impl->planes.alloc((size_t)nd * dtab.maxv, st);
     k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(dtab.v, dtab.nv, dtab.ori, dtab.maxv, nd, impl->planes.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     dplanes = impl->planes.p;
+    // drop the pairs separated by a destination edge (order kept)
+    DBuf<int32_t> keep((size_t)nc + 1, st), pos((size_t)nc + 1, st);
+    k_separated<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, dtab.v, dtab.nv, dtab.maxv, stab.v, stab.nv, stab.maxv,
+                                               dplanes, keep.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    exclusive_scan_i32(keep.p, pos.p, nc, st);
+    int32_t nk = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&nk, pos.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    impl->kept.alloc((size_t)nk + 1, st);
+    k_compact_pairs<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, keep.p, pos.p, impl->kept.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    nc = nk;
+    cand = impl->kept.p;
   }
 }
 
@@ -1251,7 +1315,7 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     R->src_area = keep_alloc<double>((size_t)ns, st);
     ps.search(R->dst_area, R->src_area, st);
     const int64_t nc = ps.nc;
-    R->ncand = nc;
+    R->ncand = ps.nc_search;
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[1], st));
 
     // K4
@@ -1337,7 +1401,7 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
     cudaEventElapsedTime(&t03, ev.e[0], ev.e[3]);
     crg_info& I = R->info;
-    I.n_dst = nd; I.n_src = ns; I.nnz = nnz; I.n_candidates = nc;
+    I.n_dst = nd; I.n_src = ns; I.nnz = nnz; I.n_candidates = ps.nc_search; I.n_clipped = ps.nc;
     I.manifold = R->manifold; I.normalized = normalize;
     I.normalizer = R->normalizer;
     I.t_build_ms = t03; I.t_search_ms = t01; I.t_clip_ms = t12; I.t_assemble_ms = t23;

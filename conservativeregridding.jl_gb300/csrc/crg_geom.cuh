@@ -315,24 +315,57 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
     } else {
       ex = cb.x - ca.x; ey = cb.y - ca.y;
     }
-    int m = 0;
-    d3 prev = in[n - 1];
-    double sp = kSpherical ? side_sph(nrm, ca, cb, eb, isig, prev) : side_pl(ca, cb, ex, ey, isig, prev);
+    // The stage in three passes that emit exactly the vertex sequence of the
+    // one-pass loop (edge i runs from vertex i-1 to vertex i): the sides of
+    // all vertices, then the crossing points -- two for a convex polygon,
+    // computed in fixed slots so the lanes of a warp run them together --
+    // then the output sequence.
+    double sv[CRG_MAXC];
+    int nin = 0;
     for (int i = 0; i < n; ++i) {
-      d3 cur = in[i];
-      double sc = kSpherical ? side_sph(nrm, ca, cb, eb, isig, cur) : side_pl(ca, cb, ex, ey, isig, cur);
-      if (sc >= 0.0) {
-        if (sp < 0.0) {
-          if (m >= CRG_MAXC) return -1;
-          out[m++] = kSpherical ? isect_sph(prev, sp, cur, sc) : isect_pl(prev, sp, cur, sc);
-        }
-        if (m >= CRG_MAXC) return -1;
-        out[m++] = cur;
-      } else if (sp >= 0.0) {
-        if (m >= CRG_MAXC) return -1;
-        out[m++] = kSpherical ? isect_sph(prev, sp, cur, sc) : isect_pl(prev, sp, cur, sc);
+      sv[i] = kSpherical ? side_sph(nrm, ca, cb, eb, isig, in[i]) : side_pl(ca, cb, ex, ey, isig, in[i]);
+      nin += sv[i] >= 0.0;
+    }
+    if (nin == n) continue;  // all inside: the stage returns the polygon unchanged
+    if (nin == 0) {
+      n = 0;
+      break;
+    }
+    int e0 = -1, e1 = -1, ncross = 0;
+    for (int i = 0; i < n; ++i) {
+      const int p = i == 0 ? n - 1 : i - 1;
+      if ((sv[i] >= 0.0) != (sv[p] >= 0.0)) {
+        if (ncross == 0) e0 = i;
+        else e1 = i;
+        ++ncross;
       }
-      prev = cur; sp = sc;
+    }
+    d3 x0{0.0, 0.0, 0.0}, x1{0.0, 0.0, 0.0};
+    if (ncross == 2) {
+      const int p0 = e0 == 0 ? n - 1 : e0 - 1, p1 = e1 == 0 ? n - 1 : e1 - 1;
+      x0 = kSpherical ? isect_sph(in[p0], sv[p0], in[e0], sv[e0]) : isect_pl(in[p0], sv[p0], in[e0], sv[e0]);
+      x1 = kSpherical ? isect_sph(in[p1], sv[p1], in[e1], sv[e1]) : isect_pl(in[p1], sv[p1], in[e1], sv[e1]);
+    }
+    int m = 0;
+    for (int i = 0; i < n; ++i) {
+      const int p = i == 0 ? n - 1 : i - 1;
+      const bool ci = sv[i] >= 0.0, pi = sv[p] >= 0.0;
+      if (ci == pi) {
+        if (ci) {
+          if (m >= CRG_MAXC) return -1;
+          out[m++] = in[i];
+        }
+        continue;
+      }
+      // a crossing edge (more than two only for non-convex input: computed here)
+      const d3 x = ncross == 2 ? (i == e0 ? x0 : x1)
+                              : (kSpherical ? isect_sph(in[p], sv[p], in[i], sv[i]) : isect_pl(in[p], sv[p], in[i], sv[i]));
+      if (m >= CRG_MAXC) return -1;
+      out[m++] = x;
+      if (ci) {
+        if (m >= CRG_MAXC) return -1;
+        out[m++] = in[i];
+      }
     }
     d3* t = in; in = out; out = t;
     n = m;

@@ -160,8 +160,9 @@ struct PairSearch {
   Impl* impl = nullptr;
   bool sph = true;
   int64_t nd = 0, ns = 0, nc = 0;
+  int64_t nc_search = 0;                   // pairs of the traversal, before the separation filter
   CellTable dtab, stab;
-  const int2* cand = nullptr;              // [nc]
+  const int2* cand = nullptr;              // [nc] pairs that may overlap
   const double4_32a* dplanes = nullptr;    // spherical: [nd * dtab.maxv]
   PairSearch();
   ~PairSearch();

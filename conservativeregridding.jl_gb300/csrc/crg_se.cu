@@ -751,7 +751,7 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
     else
       ps.search(fv_area, elem_area.p, st);
     const int64_t nc = ps.nc;
-    R->ncand = nc;
+    R->ncand = ps.nc_search;
     DBuf<double> coef;
     element_coeffs(se_is_dst ? ps.dtab : ps.stab, coef, st);
     DBuf<double> wj((size_t)nn + 1, st);
@@ -855,7 +855,7 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
     cudaEventElapsedTime(&t23, ev.e[2], ev.e[3]);
     cudaEventElapsedTime(&t03, ev.e[0], ev.e[3]);
     crg_info& I = R->info;
-    I.n_dst = R->nd; I.n_src = R->ns; I.nnz = R->nnz; I.n_candidates = nc;
+    I.n_dst = R->nd; I.n_src = R->ns; I.nnz = R->nnz; I.n_candidates = ps.nc_search; I.n_clipped = ps.nc;
     I.manifold = CRG_SPHERICAL; I.normalized = 0; I.normalizer = 1.0;
     I.t_build_ms = t03; I.t_search_ms = t01; I.t_clip_ms = t12; I.t_assemble_ms = t23;
     I.clip_overflows = 0;

@@ -52,6 +52,7 @@ struct CrgInfo
     clip_overflows::Int64
     device::Int32; pad::Int32
     merge_tasks::NTuple{2,Int64}; cut_rows::NTuple{2,Int64}; carry_slots::NTuple{2,Int64}; empty_rows::NTuple{2,Int64}
+    n_clipped::Int64
 end
 
 const CRG_F64, CRG_F32, CRG_BF16 = Int32(0), Int32(1), Int32(2)

@@ -92,6 +92,7 @@ typedef struct crg_info {
     int64_t cut_rows[2];     /* rows longer than 16 entries cut between tasks */
     int64_t carry_slots[2];  /* pieces of the cut rows (512-byte partial sums each) */
     int64_t empty_rows[2];   /* rows without entries (written as zeros) */
+    int64_t n_clipped;       /* candidate pairs left for the clip after the FP32 separation filter */
 } crg_info;
 
 /* Build the regridder from `src` to `dst`.

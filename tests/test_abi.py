@@ -39,6 +39,30 @@ def test_cpu_safe_entry_points():
     assert lib.crg_regridder_release(None) == 0
 
 
+def test_se_entry_points_validate_before_device_work():
+    """The SE builds check the space, the FV grid and the rule degree on the
+    host (the reference's errors: reference_rule's "not available", :416-506)."""
+    lib = _lib.load()
+    out = C.c_void_p()
+    assert lib.crg_build_se_to_fv(None, None, None, C.byref(out)) == _lib.CRG_ERR_INVALID_ARGUMENT
+    fv = _lib.crg_grid_desc()
+    fv.manifold = _lib.CRG_SPHERICAL
+    space = _lib.crg_se_space()
+    space.elements.manifold = _lib.CRG_SPHERICAL
+    space.nq = 9
+    assert lib.crg_build_se_to_fv(C.byref(fv), C.byref(space), None, C.byref(out)) == _lib.CRG_ERR_INVALID_ARGUMENT
+    assert b"nq = 9" in lib.crg_last_error()
+    space.nq = 4
+    opts = _lib.crg_se_opts(9, 0, 0.0, None)
+    assert lib.crg_build_fv_to_se(C.byref(space), C.byref(fv), C.byref(opts), C.byref(out)) == \
+        _lib.CRG_ERR_INVALID_ARGUMENT
+    assert b"degree 9 not available" in lib.crg_last_error()
+    space.elements.manifold = _lib.CRG_PLANAR
+    assert lib.crg_build_se_to_fv(C.byref(fv), C.byref(space), None, C.byref(out)) == _lib.CRG_ERR_INVALID_ARGUMENT
+    assert b"spherical" in lib.crg_last_error()
+    assert out.value is None
+
+
 def test_build_is_sm103a_and_in_tree():
     assert any("sm_103a" in f for f in _build.ARCH_FLAGS)
     assert "--fmad=false" in _build.NVCC_FLAGS
