@@ -505,45 +505,77 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 // 2^-21 |n32|_1 (1 + |w32|_inf) (inputs 2^-24 relative, the dot product 3
 // roundings, the FP64 normal's own error far smaller), so s32 < -B with
 // B = 2^-18 |n32|_1 (1 + |w32|_1) is outside by an 8x margin.
+//
+// The same tests give each kept pair its class: the mask of destination edges
+// that may cut the source cell (neither all vertices clearly inside nor all
+// outside).  Clipping the pairs grouped by class lets the lanes of a warp
+// meet their crossing points at the same stages.
+constexpr int kClasses = 256;  // cut masks of up to 8 edges; class kClasses = dropped
+
 __global__ void __launch_bounds__(256)
     k_separated(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
                 const int8_t* __restrict__ dnv, int dmaxv, const double* __restrict__ sv,
                 const int8_t* __restrict__ snv, int smaxv, const double4_32a* __restrict__ planes,
-                int32_t* __restrict__ keep) {
+                uint16_t* __restrict__ cls) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
   const int2 pr = cand[t];
   const int nd = dnv[pr.x], ns = snv[pr.y];
   if (nd < 3 || ns < 3) {  // no polygon: never an entry
-    keep[t] = 0;
+    cls[t] = kClasses;
     return;
   }
   float3 v[CRG_MAXV];
   const double* q = sv + (int64_t)pr.y * smaxv * 3;
   for (int i = 0; i < ns; ++i) v[i] = make_float3((float)q[3 * i], (float)q[3 * i + 1], (float)q[3 * i + 2]);
   const double* c = dv + (int64_t)pr.x * dmaxv * 3;
-  int sep = 0;
+  int sep = 0, mask = 0;
   for (int k = 0; k < nd && !sep; ++k) {
     const double4_32a p = planes[(int64_t)pr.x * dmaxv + k];
     const float nx = (float)p.x, ny = (float)p.y, nz = (float)p.z;
     const float ax = (float)c[3 * k], ay = (float)c[3 * k + 1], az = (float)c[3 * k + 2];
     const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
-    int out = 1;
-    for (int i = 0; i < ns && out; ++i) {
+    int out = 1, in = 1;
+    for (int i = 0; i < ns; ++i) {
       const float wx = v[i].x - ax, wy = v[i].y - ay, wz = v[i].z - az;
       const float s = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
       const float B = 3.814697265625e-06f * n1 * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
-      out = s < -B;
+      out &= s < -B;
+      in &= s > B;
     }
     sep = out;
+    if (!in) mask |= 1 << k;
   }
-  keep[t] = !sep;
+  cls[t] = sep ? kClasses : (uint16_t)(mask & (kClasses - 1));
 }
 
-__global__ void k_compact_pairs(const int2* __restrict__ cand, int64_t nc, const int32_t* __restrict__ keep,
-                                const int32_t* __restrict__ pos, int2* __restrict__ out) {
+__global__ void __launch_bounds__(256)
+    k_class_count(const uint16_t* __restrict__ cls, int64_t nc, int32_t* __restrict__ cnt) {
+  __shared__ int32_t h[kClasses + 1];
+  for (int i = threadIdx.x; i <= kClasses; i += blockDim.x) h[i] = 0;
+  __syncthreads();
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < nc && keep[t]) out[pos[t]] = cand[t];
+  if (t < nc) atomicAdd(&h[cls[t]], 1);
+  __syncthreads();
+  for (int i = threadIdx.x; i < kClasses; i += blockDim.x)
+    if (h[i]) atomicAdd(&cnt[i], h[i]);
+}
+
+// Kept pairs grouped by class: each block reserves its range of every class
+// (any order inside a class: the clip results do not depend on it).
+__global__ void __launch_bounds__(256)
+    k_class_scatter(const int2* __restrict__ cand, const uint16_t* __restrict__ cls, int64_t nc,
+                    const int32_t* __restrict__ off, int32_t* __restrict__ fill, int2* __restrict__ out) {
+  __shared__ int32_t h[kClasses + 1], base[kClasses + 1];
+  for (int i = threadIdx.x; i <= kClasses; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = t < nc ? cls[t] : kClasses;
+  const int r = b < kClasses ? atomicAdd(&h[b], 1) : 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < kClasses; i += blockDim.x) base[i] = h[i] ? atomicAdd(&fill[i], h[i]) : 0;
+  __syncthreads();
+  if (b < kClasses) out[off[b] + base[b] + r] = cand[t];
 }
 
 __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __restrict__ nv,
@@ -1178,17 +1210,22 @@ void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
     k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(dtab.v, dtab.nv, dtab.ori, dtab.maxv, nd, impl->planes.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     dplanes = impl->planes.p;
-    // drop the pairs separated by a destination edge (order kept)
-    DBuf<int32_t> keep((size_t)nc + 1, st), pos((size_t)nc + 1, st);
+    // drop the pairs separated by a destination edge, group the rest by class
+    DBuf<int32_t> cnt(kClasses + 1, st), off(kClasses + 1, st), fill(kClasses + 1, st);
+    DBuf<uint16_t> cls((size_t)nc + 1, st);
+    cnt.zero();
+    fill.zero();
     k_separated<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, dtab.v, dtab.nv, dtab.maxv, stab.v, stab.nv, stab.maxv,
-                                               dplanes, keep.p);
+                                               dplanes, cls.p);
     CRG_CHECK_CUDA(cudaGetLastError());
-    exclusive_scan_i32(keep.p, pos.p, nc, st);
+    k_class_count<<<nblk(nc, 256), 256, 0, st>>>(cls.p, nc, cnt.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    exclusive_scan_i32(cnt.p, off.p, kClasses, st);
     int32_t nk = 0;
-    CRG_CHECK_CUDA(cudaMemcpyAsync(&nk, pos.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&nk, off.p + kClasses, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     CRG_CHECK_CUDA(cudaStreamSynchronize(st));
     impl->kept.alloc((size_t)nk + 1, st);
-    k_compact_pairs<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, keep.p, pos.p, impl->kept.p);
+    k_class_scatter<<<nblk(nc, 256), 256, 0, st>>>(cand, cls.p, nc, off.p, fill.p, impl->kept.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     nc = nk;
     cand = impl->kept.p;
