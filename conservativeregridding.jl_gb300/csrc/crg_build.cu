@@ -660,13 +660,45 @@ __global__ void k_scatter_pairs(const int2* __restrict__ cand, const double* __r
 constexpr int kRowSortSmem = 4096;
 constexpr int kRowSortThreads = 256;
 
-__global__ void k_row_sort_warp(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ idx,
-                                double* __restrict__ val) {
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (r >= nrows) return;  // warp-uniform
+// Rows of up to 8 entries: one thread each, an odd-even transposition network
+// of 8 elements in registers (missing entries are +inf keys).
+__global__ void k_row_sort_small(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ idx,
+                                 double* __restrict__ val) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
   const int32_t lo = ptr[r], len = ptr[r + 1] - lo;
-  if (len < 2 || len > 32) return;  // warp-uniform
+  if (len < 2 || len > 8) return;
+  int32_t k[8];
+  double v[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    k[i] = i < len ? idx[lo + i] : INT32_MAX;
+    v[i] = i < len ? val[lo + i] : 0.0;
+  }
+#pragma unroll
+  for (int round = 0; round < 8; ++round)
+#pragma unroll
+    for (int i = round & 1; i + 1 < 8; i += 2)
+      if (k[i + 1] < k[i]) {
+        const int32_t tk = k[i]; k[i] = k[i + 1]; k[i + 1] = tk;
+        const double tv = v[i]; v[i] = v[i + 1]; v[i + 1] = tv;
+      }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    if (i < len) {
+      idx[lo + i] = k[i];
+      val[lo + i] = v[i];
+    }
+}
+
+// Rows of 9..32 entries (listed): one warp each, a bitonic network across the lanes.
+__global__ void k_row_sort_warp(const int32_t* __restrict__ ptr, const int32_t* __restrict__ rows, int64_t nlist,
+                                int32_t* __restrict__ idx, double* __restrict__ val) {
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= nlist) return;  // warp-uniform
+  const int32_t r = rows[w];
+  const int32_t lo = ptr[r], len = ptr[r + 1] - lo;
   int32_t key = lane < len ? idx[lo + lane] : INT32_MAX;
   double v = lane < len ? val[lo + lane] : 0.0;
   for (int k = 2; k <= 32; k <<= 1) {
@@ -686,14 +718,16 @@ __global__ void k_row_sort_warp(const int32_t* __restrict__ ptr, int64_t nrows, 
   }
 }
 
-// rows longer than 32 entries, split by whether they fit in shared memory
-__global__ void k_row_classes(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ mid,
-                              int32_t* __restrict__ longr, int32_t* __restrict__ counts) {
+// rows longer than 8 entries: 9..32 (a warp each), up to shared-memory size
+// (a block each) and longer (global memory)
+__global__ void k_row_classes(const int32_t* __restrict__ ptr, int64_t nrows, int32_t* __restrict__ warp,
+                              int32_t* __restrict__ mid, int32_t* __restrict__ longr, int32_t* __restrict__ counts) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
   const int32_t len = ptr[r + 1] - ptr[r];
-  if (len <= 32) return;
-  if (len <= kRowSortSmem) mid[atomicAdd(&counts[0], 1)] = (int32_t)r;
+  if (len <= 8) return;
+  if (len <= 32) warp[atomicAdd(&counts[2], 1)] = (int32_t)r;
+  else if (len <= kRowSortSmem) mid[atomicAdd(&counts[0], 1)] = (int32_t)r;
   else longr[atomicAdd(&counts[1], 1)] = (int32_t)r;
 }
 
@@ -796,21 +830,29 @@ __global__ void k_div_by(double* __restrict__ v, int64_t n, const unsigned long 
 
 // FP32 weights: val32 = A, wn32 = A / area_row, adj32 = A / area_col, plus the
 // Kahan row sums of A.
-__global__ void k_derive(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                         const double* __restrict__ val, int64_t nrows, const double* __restrict__ area_row,
+// FP32 copies of the entries and of the normalised / adjoint weights, one
+// thread per entry (erow: the row of each entry).
+__global__ void k_derive(const int32_t* __restrict__ erow, const int32_t* __restrict__ idx,
+                         const double* __restrict__ val, int64_t nnz, const double* __restrict__ area_row,
                          const double* __restrict__ area_col, float* __restrict__ val32, float* __restrict__ wn32,
-                         float* __restrict__ adj32, double* __restrict__ rowsum) {
-  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                         float* __restrict__ adj32) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnz) return;
+  const double a = val[k];
+  val32[k] = (float)a;
+  wn32[k] = (float)(a / area_row[erow[k]]);
+  adj32[k] = (float)(a / area_col[idx[k]]);
+}
+
+// Kahan-summed rows of A, entries in column order.
+__global__ void k_row_sums(const int32_t* __restrict__ ptr, const double* __restrict__ val, int64_t nrows,
+                           double* __restrict__ rowsum) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
-  double ar = area_row[r];
   double s = 0.0, comp = 0.0;
   for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) {
-    double a = val[k];
-    val32[k] = (float)a;
-    wn32[k] = (float)(a / ar);
-    adj32[k] = (float)(a / area_col[idx[k]]);
-    double y = a - comp;
-    double t = s + y;
+    const double y = val[k] - comp;
+    const double t = s + y;
     comp = (t - s) - y;
     s = t;
   }
@@ -1116,16 +1158,21 @@ bool is_device_pointer(const void* p) {
 // Sorts the columns (and values) of every row of a CSR ascending.
 void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cudaStream_t st) {
   if (nrows == 0) return;
-  k_row_sort_warp<<<nblk(nrows * 32, 256), 256, 0, st>>>(ptr, nrows, idx, val);
+  k_row_sort_small<<<nblk(nrows, 256), 256, 0, st>>>(ptr, nrows, idx, val);
   CRG_CHECK_CUDA(cudaGetLastError());
-  DBuf<int32_t> lists(2 * nrows + 2, st);  // [nrows] mid rows | [nrows] long rows | [2] counts
-  int32_t* counts = lists.p + 2 * nrows;
-  CRG_CHECK_CUDA(cudaMemsetAsync(counts, 0, 2 * sizeof(int32_t), st));
-  k_row_classes<<<nblk(nrows, 256), 256, 0, st>>>(ptr, nrows, lists.p, lists.p + nrows, counts);
+  // [nrows] mid rows | [nrows] long rows | [nrows] 9..32-entry rows | [3] counts
+  DBuf<int32_t> lists(3 * nrows + 3, st);
+  int32_t* counts = lists.p + 3 * nrows;
+  CRG_CHECK_CUDA(cudaMemsetAsync(counts, 0, 3 * sizeof(int32_t), st));
+  k_row_classes<<<nblk(nrows, 256), 256, 0, st>>>(ptr, nrows, lists.p + 2 * nrows, lists.p, lists.p + nrows, counts);
   CRG_CHECK_CUDA(cudaGetLastError());
-  int32_t h[2] = {0, 0};
+  int32_t h[3] = {0, 0, 0};
   CRG_CHECK_CUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
   CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  if (h[2]) {
+    k_row_sort_warp<<<nblk((int64_t)h[2] * 32, 256), 256, 0, st>>>(ptr, lists.p + 2 * nrows, h[2], idx, val);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
   if (h[0]) {
     k_row_sort_block<<<(unsigned)h[0], kRowSortThreads, 0, st>>>(ptr, lists.p, idx, val);
     CRG_CHECK_CUDA(cudaGetLastError());
@@ -1307,15 +1354,17 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
   }
   R->row_sum = keep_alloc<double>((size_t)nd, st);
   R->col_sum = keep_alloc<double>((size_t)ns, st);
-  if (nd)
-    k_derive<<<nblk(nd, 128), 128, 0, st>>>(R->fwd.ptr, R->fwd.idx, R->fwd.val, nd, R->dst_area, R->src_area,
-                                            R->fwd.val32, R->fwd.wn32, R->fwd.adj32, R->row_sum);
-  if (ns)
-    k_derive<<<nblk(ns, 128), 128, 0, st>>>(R->rev.ptr, R->rev.idx, R->rev.val, ns, R->src_area, R->dst_area,
-                                            R->rev.val32, R->rev.wn32, R->rev.adj32, R->col_sum);
-  CRG_CHECK_CUDA(cudaGetLastError());
-  build_merge_path(R->fwd, st);
+  build_merge_path(R->fwd, st);  // also the row of every entry
   build_merge_path(R->rev, st);
+  if (nnz) {
+    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.erow, R->fwd.idx, R->fwd.val, nnz, R->dst_area, R->src_area,
+                                             R->fwd.val32, R->fwd.wn32, R->fwd.adj32);
+    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.erow, R->rev.idx, R->rev.val, nnz, R->src_area, R->dst_area,
+                                             R->rev.val32, R->rev.wn32, R->rev.adj32);
+  }
+  if (nd) k_row_sums<<<nblk(nd, 256), 256, 0, st>>>(R->fwd.ptr, R->fwd.val, nd, R->row_sum);
+  if (ns) k_row_sums<<<nblk(ns, 256), 256, 0, st>>>(R->rev.ptr, R->rev.val, ns, R->col_sum);
+  CRG_CHECK_CUDA(cudaGetLastError());
   crg_info& I = R->info;
   const DevCsr* cs[2] = {&R->fwd, &R->rev};
   for (int d = 0; d < 2; ++d) {
