@@ -98,8 +98,16 @@ class Grid:
         return [(b.shape[1] - 1, b.shape[0] - 1) for b in self.blocks]
 
     def points_flat(self) -> np.ndarray:
-        """All block points back to back, i fastest inside a block."""
-        return np.concatenate([b.reshape(-1, self.dim) for b in self.blocks], axis=0)
+        """All block points back to back, i fastest inside a block (made once per grid)."""
+        flat = self.__dict__.get("_flat")
+        if flat is None:
+            if len(self.blocks) == 1:
+                flat = np.ascontiguousarray(self.blocks[0].reshape(-1, self.dim), np.float64)
+            else:
+                flat = np.ascontiguousarray(np.concatenate([b.reshape(-1, self.dim) for b in self.blocks], axis=0),
+                                            np.float64)
+            self.__dict__["_flat"] = flat
+        return flat
 
     def cell_table(self) -> tuple[np.ndarray, np.ndarray]:
         """(ncells, maxv, dim) ring vertices and (ncells,) vertex counts."""

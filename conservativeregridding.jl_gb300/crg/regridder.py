@@ -139,12 +139,28 @@ class Regridder:
         self.info = {k: (list(getattr(info, k)) if k in _PAIR_FIELDS else getattr(info, k))
                      for k, _ in _lib.crg_info._fields_ if k != "pad"}
         nd, ns = info.n_dst, info.n_src
-        self.dst_areas = np.empty(nd)
-        self.src_areas = np.empty(ns)
-        check(lib.crg_get_areas(C.c_void_p(ptr), self.dst_areas.ctypes.data, self.src_areas.ctypes.data))
         self.dst_temp = np.zeros(nd)
         self.src_temp = np.zeros(ns)
-        self._csc = [None]  # shared cache with transposed views
+        self._csc = [None]  # shared caches with transposed views
+        self._areas = [None]
+
+    # -- R.dst_areas / R.src_areas (copied from the device on first use) --
+    def _area_pair(self):
+        if self._areas[0] is None:
+            lib = _lib.load()
+            d = np.empty(self.info["n_dst"])
+            s = np.empty(self.info["n_src"])
+            check(lib.crg_get_areas(C.c_void_p(self._h.ptr), d.ctypes.data, s.ctypes.data))
+            self._areas[0] = (d, s)
+        return self._areas[0]
+
+    @property
+    def dst_areas(self) -> np.ndarray:
+        return self._area_pair()[1 if self._transposed else 0]
+
+    @property
+    def src_areas(self) -> np.ndarray:
+        return self._area_pair()[0 if self._transposed else 1]
 
     # -- shape ---------------------------------------------------------
     @property
@@ -168,7 +184,6 @@ class Regridder:
         view = dict(self.__dict__)
         view["_h"] = _Handle(self._h.ptr)
         view["_transposed"] = not self._transposed
-        view["dst_areas"], view["src_areas"] = self.src_areas, self.dst_areas
         view["dst_temp"], view["src_temp"] = self.src_temp, self.dst_temp
         view["dst_space"], view["src_space"] = self.src_space, self.dst_space
         return Regridder(None, None, _view=view)

@@ -147,9 +147,19 @@ __global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restri
     const double* q = v + (c * maxv + k) * 3;
     p[k].x = q[0]; p[k].y = q[1]; p[k].z = q[2];
   }
-  area[c] = n >= 3 ? cell_area<kSph>(p, n) : 0.0;
-  // the orientation every clip of this cell uses, computed once
-  ori[c] = (int8_t)((n >= 3 ? (kSph ? orient_sph(p, n) : orient_pl(p, n)) : 1.0) > 0.0 ? 1 : -1);
+  // the orientation every clip of this cell uses, computed once, and the area
+  // (signed area times orientation: the same values as cell_area)
+  double o = 1.0, a = 0.0;
+  if (n >= 3) {
+    if (kSph) {
+      a = area_orient_sph(p, n, o);
+    } else {
+      a = area_pl_signed(p, n);
+      o = a >= 0.0 ? 1.0 : -1.0;
+    }
+  }
+  area[c] = a * o;
+  ori[c] = (int8_t)(o > 0.0 ? 1 : -1);
   if (n == 0) {  // a ghost slot: a bound that overlaps nothing (negative radius / inverted box)
     bound[c] = kSph ? make_float4(0.f, 0.f, 1.f, -4.f) : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
     if (kSph) key[c] = sphere_key(0.0, 0.0, 1.0);
@@ -160,12 +170,16 @@ __global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restri
     for (int k = 0; k < n; ++k) { sx += p[k].x; sy += p[k].y; sz += p[k].z; }
     double nr = sqrt(sx * sx + sy * sy + sz * sz);
     double cx = 0, cy = 0, cz = 1;
-    if (nr > 0) { cx = sx / nr; cy = sy / nr; cz = sz / nr; }
-    double rho = 0;
+    if (nr > 0) {
+      const double inr = 1.0 / nr;
+      cx = sx * inr; cy = sy * inr; cz = sz * inr;
+    }
+    double rho2 = 0;
     for (int k = 0; k < n; ++k) {
       double dx = p[k].x - cx, dy = p[k].y - cy, dz = p[k].z - cz;
-      rho = fmax(rho, sqrt(dx * dx + dy * dy + dz * dz));
+      rho2 = fmax(rho2, dx * dx + dy * dy + dz * dz);
     }
+    double rho = sqrt(rho2);
     if (!(rho < 1.4) || !(nr > 0)) rho = 2.0;
     float rf = __double2float_ru(rho * (1.0 + 4e-6) + 4e-6);
     bound[c] = make_float4((float)cx, (float)cy, (float)cz, rf);

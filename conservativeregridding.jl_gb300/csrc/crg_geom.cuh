@@ -238,6 +238,24 @@ __device__ __forceinline__ double area_sph_signed(const d3* v, int m) {
   return 2.0 * atan2_crg(im, re);
 }
 
+// area_sph_signed and orient_sph of the same polygon from one pass over the
+// fan (the triple products are shared; the values are the same).
+__device__ __forceinline__ double area_orient_sph(const d3* v, int m, double& ori) {
+  double re = 1.0, im = 0.0, s = 0.0;
+  d3 a = v[0];
+  for (int k = 1; k + 1 < m; ++k) {
+    d3 b = v[k], c = v[k + 1];
+    double N = triple(a, b, c);
+    s = s + N;
+    double D = ((1.0 + ddot(a, b)) + ddot(b, c)) + ddot(c, a);
+    double re2 = fma(re, D, -(im * N));
+    double im2 = fma(re, N, im * D);
+    re = re2; im = im2;
+  }
+  ori = s >= 0.0 ? 1.0 : -1.0;
+  return m < 3 ? 0.0 : 2.0 * atan2_crg(im, re);
+}
+
 // ---------------------------------------------------------------- plane
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
