@@ -325,27 +325,29 @@ __global__ void k_se_nodes(const double* __restrict__ coef, int64_t nelem, const
 // ------------------------------------------------------------------ overlap integrals
 
 // b(e, k)[i + j nq] = integral over cell k ∩ element e of phi_i(xi) phi_j(eta)
-// for one candidate pair (accumulate_principled_b :260-305): clip the
-// subject (src cell) by the clip polygon (dst cell), fan-triangulate the
-// overlap from its normalised vertex sum, Dunavant rule on every triangle of
-// positive area (signed by the subject's orientation), (xi, eta) by the
-// inverse element map at each rule point projected onto the sphere.
-template <int NQ>
+// for one candidate pair (accumulate_principled_b :260-305): clip the subject
+// (src cell) by the clip polygon (dst cell), fan-triangulate the overlap from
+// its normalised vertex sum, Dunavant rule on every triangle of positive area
+// (signed by the subject's orientation), (xi, eta) by the inverse element map
+// at each rule point.  Each triangle's rule points are summed on their own and
+// the triangles added in fan order.  The work is split into triangle items so
+// that the lanes of a warp run the same number of rule points:
+//   k_se_overlap   per pair: the clip, the fan's centroid and triangle areas,
+//                  the polygon kept in the pair's slot
+//   k_se_items     per pair: its triangles of positive area as (pair, triangle) items
+//   k_se_tri_b<nq> per item: the sum over its rule points
+//   k_se_pair_sum  per pair: its items in fan order
+
 __global__ void __launch_bounds__(128)
-    k_se_pair_b(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
-                const int8_t* __restrict__ dnv, const int8_t* __restrict__ dori, int dmaxv,
-                const double* __restrict__ sv, const int8_t* __restrict__ snv, const int8_t* __restrict__ sori,
-                int smaxv, const double4_32a* __restrict__ dplanes, const double* __restrict__ coef, int se_is_dst,
-                const __grid_constant__ SeRule r, double r2, double* __restrict__ bv, int32_t* __restrict__ cnt,
-                unsigned long long* __restrict__ overflow) {
-  constexpr int M = NQ ? NQ : kSeMaxNq;
-  const int nq = NQ ? NQ : r.nq, nq2 = nq * nq;
+    k_se_overlap(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
+                 const int8_t* __restrict__ dnv, const int8_t* __restrict__ dori, int dmaxv,
+                 const double* __restrict__ sv, const int8_t* __restrict__ snv, const int8_t* __restrict__ sori,
+                 int smaxv, const double4_32a* __restrict__ dplanes, double r2, double* __restrict__ poly,
+                 double* __restrict__ cen_out, double* __restrict__ tarea, int32_t* __restrict__ nvert,
+                 int32_t* __restrict__ tcount, unsigned long long* __restrict__ overflow) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
   const int2 pr = cand[t];
-  double B[M * M];
-#pragma unroll
-  for (int k = 0; k < M * M; ++k) B[k] = 0.0;
   d3 clip[CRG_MAXV];
   d3 bufA[CRG_MAXC], bufB[CRG_MAXC];
   const int nd = dnv[pr.x], ns = snv[pr.y];
@@ -364,8 +366,8 @@ __global__ void __launch_bounds__(128)
       m = 0;
     }
   }
+  int n = 0;
   if (m >= 3) {
-    const InvMap im = load_invmap(coef + (int64_t)(se_is_dst ? pr.x : pr.y) * kSeCoef);
     d3 cs = res[0];
     for (int k = 1; k < m; ++k) {
       cs.x = cs.x + res[k].x;
@@ -374,46 +376,98 @@ __global__ void __launch_bounds__(128)
     }
     const double ic = 1.0 / sqrt(ddot(cs, cs));
     const d3 cen{cs.x * ic, cs.y * ic, cs.z * ic};
+    cen_out[3 * t] = cen.x; cen_out[3 * t + 1] = cen.y; cen_out[3 * t + 2] = cen.z;
+    double* pp = poly + t * (3 * CRG_MAXC);
+    double* ta = tarea + t * CRG_MAXC;
     for (int k = 0; k < m; ++k) {
       const d3 v1 = res[k], v2 = res[k + 1 == m ? 0 : k + 1];
+      pp[3 * k] = v1.x; pp[3 * k + 1] = v1.y; pp[3 * k + 2] = v1.z;
       const double N = triple(cen, v1, v2);
       const double D = ((1.0 + ddot(cen, v1)) + ddot(v1, v2)) + ddot(v2, cen);
       const double At = ((2.0 * atan2_crg(N, D)) * sig) * r2;
-      if (!(At > 0.0)) continue;
-      for (int g = 0; g < r.ntri; ++g) {
-        const double l0 = r.tl[g][0], l1 = r.tl[g][1], l2 = r.tl[g][2];
-        // the rule point l0 cen + l1 v1 + l2 v2; the inverse map is invariant
-        // under scaling of x, so its projection onto the sphere is not needed
-        d3 x;
-        x.x = fma(l2, v2.x, fma(l1, v1.x, l0 * cen.x));
-        x.y = fma(l2, v2.y, fma(l1, v1.y, l0 * cen.y));
-        x.z = fma(l2, v2.z, fma(l1, v1.z, l0 * cen.z));
-        double xi, eta;
-        se_inverse(im, x, xi, eta);
-        double fx[M], fy[M];
-        lagrange_dev<NQ>(r, nq, xi, fx);
-        lagrange_dev<NQ>(r, nq, eta, fy);
-        const double wA = r.tw[g] * At;
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-          if (i < nq) fx[i] = wA * fx[i];
-#pragma unroll
-        for (int j = 0; j < M; ++j)
-#pragma unroll
-          for (int i = 0; i < M; ++i)
-            if (i < nq && j < nq) B[i + j * nq] = fma(fx[i], fy[j], B[i + j * nq]);
-      }
+      ta[k] = At;
+      n += At > 0.0;
     }
   }
-  int n = 0;
-  double* o = bv + t * nq2;
+  nvert[t] = m;
+  tcount[t] = n;
+}
+
+__global__ void k_se_items(const int32_t* __restrict__ nvert, const double* __restrict__ tarea,
+                           const int32_t* __restrict__ toff, int64_t nc, int2* __restrict__ items) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc) return;
+  const int m = nvert[t];
+  int32_t o = toff[t];
+  for (int k = 0; k < m; ++k)
+    if (tarea[t * CRG_MAXC + k] > 0.0) items[o++] = make_int2((int32_t)t, k);
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(128)
+    k_se_tri_b(const int2* __restrict__ items, int64_t nitems, const double* __restrict__ poly,
+               const double* __restrict__ cenv, const double* __restrict__ tarea, const int32_t* __restrict__ nvert,
+               const int2* __restrict__ cand, const double* __restrict__ coef, int se_is_dst,
+               const __grid_constant__ SeRule r, double* __restrict__ tb) {
+  constexpr int M = NQ ? NQ : kSeMaxNq;
+  const int nq = NQ ? NQ : r.nq, nq2 = nq * nq;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nitems) return;
+  const int2 item = items[t];
+  const int64_t pair = item.x;
+  const int k = item.y, k1 = k + 1 == nvert[pair] ? 0 : k + 1;
+  const int2 pr = cand[pair];
+  const InvMap im = load_invmap(coef + (int64_t)(se_is_dst ? pr.x : pr.y) * kSeCoef);
+  const double* pp = poly + pair * (3 * CRG_MAXC);
+  const d3 cen = ld3(cenv + 3 * pair), v1 = ld3(pp + 3 * k), v2 = ld3(pp + 3 * k1);
+  const double At = tarea[pair * CRG_MAXC + k];
+  double T[M * M];
+#pragma unroll
+  for (int k = 0; k < M * M; ++k) T[k] = 0.0;
+  for (int g = 0; g < r.ntri; ++g) {
+    const double l0 = r.tl[g][0], l1 = r.tl[g][1], l2 = r.tl[g][2];
+    // the rule point l0 cen + l1 v1 + l2 v2; the inverse map is invariant
+    // under scaling of x, so its projection onto the sphere is not needed
+    d3 x;
+    x.x = fma(l2, v2.x, fma(l1, v1.x, l0 * cen.x));
+    x.y = fma(l2, v2.y, fma(l1, v1.y, l0 * cen.y));
+    x.z = fma(l2, v2.z, fma(l1, v1.z, l0 * cen.z));
+    double xi, eta;
+    se_inverse(im, x, xi, eta);
+    double fx[M], fy[M];
+    lagrange_dev<NQ>(r, nq, xi, fx);
+    lagrange_dev<NQ>(r, nq, eta, fy);
+    const double wA = r.tw[g] * At;
+#pragma unroll
+    for (int i = 0; i < M; ++i)
+      if (i < nq) fx[i] = wA * fx[i];
+#pragma unroll
+    for (int j = 0; j < M; ++j)
+#pragma unroll
+      for (int i = 0; i < M; ++i)
+        if (i < nq && j < nq) T[i + j * nq] = fma(fx[i], fy[j], T[i + j * nq]);
+  }
+  double* o = tb + t * nq2;
 #pragma unroll
   for (int k = 0; k < M * M; ++k)
-    if (k < nq2) {
-      o[k] = B[k];
-      n += B[k] != 0.0;
-    }
-  cnt[t] = n;
+    if (k < nq2) o[k] = T[k];
+}
+
+__global__ void k_se_pair_sum(const int32_t* __restrict__ toff, const int32_t* __restrict__ tcount, int64_t nc,
+                              const double* __restrict__ tb, int nq2, double* __restrict__ bv,
+                              int32_t* __restrict__ cnt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc) return;
+  const int64_t a = toff[t];
+  const int n = tcount[t];
+  int nz = 0;
+  for (int k = 0; k < nq2; ++k) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s = s + tb[(a + j) * nq2 + k];
+    bv[t * nq2 + k] = s;
+    nz += s != 0.0;
+  }
+  cnt[t] = nz;
 }
 
 // ------------------------------------------------------------------ L2 projection (FV -> SE)
@@ -467,20 +521,26 @@ __global__ void __launch_bounds__(128)
     const int pp = k % nm, qq = k / nm;
     double s = 0.0;
     for (int qn = 0; qn < nq; ++qn)
-      for (int pn = 0; pn < nq; ++pn) s = s + (Jn[pn + qn * nq] * ms.L[pp][pn]) * ms.L[qq][qn];
+      for (int pn = 0; pn < nq; ++pn) s = fma(Jn[pn + qn * nq] * ms.L[pp][pn], ms.L[qq][qn], s);
     Jq[k] = s;
   }
   __syncthreads();
-  // M[(a,b),(i,j)] = sum_(q,p) w_p w_q J phi_a(xi_p) phi_i(xi_p) phi_b(eta_q) phi_j(eta_q)
+  // M[(a,b),(i,j)] = sum_(q,p) w_p w_q J phi_a(xi_p) phi_i(xi_p) phi_b(eta_q) phi_j(eta_q),
+  // by sum factorisation: G[q][a][i] = sum_p w_p w_q J phi_a(xi_p) phi_i(xi_p) first
+  double* G = Inv;  // nm * nq2 doubles, free until the inverse is formed
+  for (int k = tid; k < nm * nq2; k += nt) {
+    const int qq = k / nq2, a = (k % nq2) % nq, i = (k % nq2) / nq;
+    double s = 0.0;
+    for (int pp = 0; pp < nm; ++pp)
+      s = fma(((ms.w[pp] * ms.w[qq]) * Jq[pp + qq * nm]) * ms.L[pp][a], ms.L[pp][i], s);
+    G[k] = s;
+  }
+  __syncthreads();
   for (int k = tid; k < nq2 * nq2; k += nt) {
     const int row = k / nq2, col = k % nq2;
     const int a = row % nq, b = row / nq, i = col % nq, j = col / nq;
     double s = 0.0;
-    for (int qq = 0; qq < nm; ++qq)
-      for (int pp = 0; pp < nm; ++pp) {
-        const double wJ = (ms.w[pp] * ms.w[qq]) * Jq[pp + qq * nm];
-        s = s + ((((wJ * ms.L[pp][a]) * ms.L[pp][i]) * ms.L[qq][b]) * ms.L[qq][j]);
-      }
+    for (int qq = 0; qq < nm; ++qq) s = fma(G[qq * nq2 + a + i * nq] * ms.L[qq][b], ms.L[qq][j], s);
     M[k] = s;
   }
   for (int k = tid; k < nq2; k += nt) {
@@ -571,7 +631,7 @@ __global__ void __launch_bounds__(128)
     const int64_t t = (int64_t)epair[p0 + x / m];
     const int rc = x % m;
     double s = 0.0;
-    for (int cc = 0; cc < m; ++cc) s = s + Inv[rc * nq2 + cc] * bv[t * nq2 + cov[cc]];
+    for (int cc = 0; cc < m; ++cc) s = fma(Inv[rc * nq2 + cc], bv[t * nq2 + cov[cc]], s);
     pv[t * nq2 + cov[rc]] = s;
   }
   __syncthreads();
@@ -702,12 +762,18 @@ void node_weights(const crg_se_space* se, const SeRule& r, const DBuf<double>& c
   }
 }
 
+struct Overlaps {
+  const int2* items;
+  int64_t nitems;
+  const double *poly, *cen, *tarea;
+  const int32_t* nvert;
+};
+
 template <int NQ>
-void launch_pair_b(const PairSearch& ps, const double* coef, int se_is_dst, const SeRule& r, double r2, double* bv,
-                   int32_t* cnt, unsigned long long* ovf, cudaStream_t st) {
-  const CellTable &D = ps.dtab, &S = ps.stab;
-  k_se_pair_b<NQ><<<nblk(ps.nc, 128), 128, 0, st>>>(ps.cand, ps.nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori,
-                                                    S.maxv, ps.dplanes, coef, se_is_dst, r, r2, bv, cnt, ovf);
+void launch_tri_b(const Overlaps& o, const PairSearch& ps, const double* coef, int se_is_dst, const SeRule& r,
+                  double* tb, cudaStream_t st) {
+  k_se_tri_b<NQ><<<nblk(o.nitems, 128), 128, 0, st>>>(o.items, o.nitems, o.poly, o.cen, o.tarea, o.nvert, ps.cand,
+                                                      coef, se_is_dst, r, tb);
   CRG_CHECK_CUDA(cudaGetLastError());
 }
 
@@ -763,20 +829,39 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
     DBuf<unsigned long long> ovf(1, st);
     ovf.zero();
     if (nc) {
-      switch (nq) {
-        case 2: launch_pair_b<2>(ps, coef.p, se_is_dst, rule, r2, bv.p, cnt.p, ovf.p, st); break;
-        case 3: launch_pair_b<3>(ps, coef.p, se_is_dst, rule, r2, bv.p, cnt.p, ovf.p, st); break;
-        case 4: launch_pair_b<4>(ps, coef.p, se_is_dst, rule, r2, bv.p, cnt.p, ovf.p, st); break;
-        case 5: launch_pair_b<5>(ps, coef.p, se_is_dst, rule, r2, bv.p, cnt.p, ovf.p, st); break;
-        default: launch_pair_b<0>(ps, coef.p, se_is_dst, rule, r2, bv.p, cnt.p, ovf.p, st); break;
+      const CellTable &D = ps.dtab, &S = ps.stab;
+      DBuf<int32_t> tcount((size_t)nc + 1, st), toff((size_t)nc + 1, st), nvert((size_t)nc + 1, st);
+      // per pair: the clipped polygon (CRG_MAXC vertex slots), its centroid and fan-triangle areas
+      DBuf<double> poly((size_t)nc * 3 * CRG_MAXC, st), cen((size_t)nc * 3, st), tarea((size_t)nc * CRG_MAXC, st);
+      k_se_overlap<<<nblk(nc, 128), 128, 0, st>>>(ps.cand, nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori, S.maxv,
+                                                  ps.dplanes, r2, poly.p, cen.p, tarea.p, nvert.p, tcount.p, ovf.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+      exclusive_scan_i32(tcount.p, toff.p, nc, st);
+      unsigned long long hovf = 0;
+      int32_t nitems = 0;
+      CRG_CHECK_CUDA(cudaMemcpyAsync(&hovf, ovf.p, sizeof(hovf), cudaMemcpyDeviceToHost, st));
+      CRG_CHECK_CUDA(cudaMemcpyAsync(&nitems, toff.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+      CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+      CRG_REQUIRE(hovf == 0, CRG_ERR_GEOMETRY,
+                  "%llu candidate pairs exceeded the clipped-polygon capacity of %d vertices (non-convex cells?)",
+                  (unsigned long long)hovf, CRG_MAXC);
+      DBuf<int2> items((size_t)nitems + 1, st);
+      DBuf<double> tb((size_t)nitems * nq2 + 1, st);
+      k_se_items<<<nblk(nc, 128), 128, 0, st>>>(nvert.p, tarea.p, toff.p, nc, items.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+      if (nitems) {
+        const Overlaps o{items.p, nitems, poly.p, cen.p, tarea.p, nvert.p};
+        switch (nq) {
+          case 2: launch_tri_b<2>(o, ps, coef.p, se_is_dst, rule, tb.p, st); break;
+          case 3: launch_tri_b<3>(o, ps, coef.p, se_is_dst, rule, tb.p, st); break;
+          case 4: launch_tri_b<4>(o, ps, coef.p, se_is_dst, rule, tb.p, st); break;
+          case 5: launch_tri_b<5>(o, ps, coef.p, se_is_dst, rule, tb.p, st); break;
+          default: launch_tri_b<0>(o, ps, coef.p, se_is_dst, rule, tb.p, st); break;
+        }
       }
+      k_se_pair_sum<<<nblk(nc, 128), 128, 0, st>>>(toff.p, tcount.p, nc, tb.p, nq2, bv.p, cnt.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
     }
-    unsigned long long hovf = 0;
-    CRG_CHECK_CUDA(cudaMemcpyAsync(&hovf, ovf.p, sizeof(hovf), cudaMemcpyDeviceToHost, st));
-    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-    CRG_REQUIRE(hovf == 0, CRG_ERR_GEOMETRY,
-                "%llu candidate pairs exceeded the clipped-polygon capacity of %d vertices (non-convex cells?)",
-                (unsigned long long)hovf, CRG_MAXC);
 
     const double* vals = bv.p;
     DBuf<double> pv;

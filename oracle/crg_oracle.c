@@ -1344,7 +1344,9 @@ void og_se_inverse(const double* g, v3 x, double* xi, double* eta) {
     *xi = den != 0.0 ? -A1 / den : 0.0;
 }
 
-/* B[i + j nq] += integral over the overlap polygon res[0..m) of phi_i(xi) phi_j(eta) */
+/* B[i + j nq] += integral over the overlap polygon res[0..m) of phi_i(xi) phi_j(eta):
+ * each fan triangle's rule points summed on their own (T), the triangles
+ * then added in fan order (the GPU coding's triangle items). */
 static void og_se_poly_b(const og_se_rule* r, const double* g, const v3* res, int m, double sig, double r2,
                          double* B) {
     int nq = r->nq;
@@ -1359,6 +1361,8 @@ static void og_se_poly_b(const og_se_rule* r, const double* g, const v3* res, in
         double D = ((1.0 + og_dot(cen, v1)) + og_dot(v1, v2)) + og_dot(v2, cen);
         double At = ((2.0 * og_atan2(N, D)) * sig) * r2;
         if (!(At > 0.0)) continue;
+        double T[OG_SE_MAXNQ * OG_SE_MAXNQ];
+        for (int q = 0; q < nq * nq; ++q) T[q] = 0.0;
         for (int gq = 0; gq < r->ntri; ++gq) {
             double l0 = r->tl[gq][0], l1 = r->tl[gq][1], l2 = r->tl[gq][2];
             /* the rule point; the inverse map does not depend on its length */
@@ -1373,8 +1377,9 @@ static void og_se_poly_b(const og_se_rule* r, const double* g, const v3* res, in
             double wA = r->tw[gq] * At;
             for (int i = 0; i < nq; ++i) fx[i] = wA * fx[i];
             for (int j = 0; j < nq; ++j)
-                for (int i = 0; i < nq; ++i) B[i + j * nq] = fma(fx[i], fy[j], B[i + j * nq]);
+                for (int i = 0; i < nq; ++i) T[i + j * nq] = fma(fx[i], fy[j], T[i + j * nq]);
         }
+        for (int q = 0; q < nq * nq; ++q) B[q] = B[q] + T[q];
     }
 }
 
@@ -1421,22 +1426,27 @@ static int og_se_project(const og_se_rule* r, const double* wj_e, const double* 
         int pp = k % nm, qq = k / nm;
         double s = 0.0;
         for (int qn = 0; qn < nq; ++qn)
-            for (int pn = 0; pn < nq; ++pn) s = s + (Jn[pn + qn * nq] * L[pp][pn]) * L[qq][qn];
+            for (int pn = 0; pn < nq; ++pn) s = fma(Jn[pn + qn * nq] * L[pp][pn], L[qq][qn], s);
         Jq[k] = s;
     }
     double* M = (double*)malloc(sizeof(double) * nq2 * nq2);
     double* Inv = (double*)malloc(sizeof(double) * nq2 * nq2);
+    /* sum factorisation: G[q][a][i] = sum_p w_p w_q J phi_a phi_i, then M */
+    double* G = (double*)malloc(sizeof(double) * nm * nq2);
+    for (int k = 0; k < nm * nq2; ++k) {
+        int qq = k / nq2, a = (k % nq2) % nq, i = (k % nq2) / nq;
+        double s = 0.0;
+        for (int pp = 0; pp < nm; ++pp) s = fma(((wm[pp] * wm[qq]) * Jq[pp + qq * nm]) * L[pp][a], L[pp][i], s);
+        G[k] = s;
+    }
     for (int k = 0; k < nq2 * nq2; ++k) {
         int row = k / nq2, col = k % nq2;
         int a = row % nq, bb = row / nq, i = col % nq, j = col / nq;
         double s = 0.0;
-        for (int qq = 0; qq < nm; ++qq)
-            for (int pp = 0; pp < nm; ++pp) {
-                double wJ = (wm[pp] * wm[qq]) * Jq[pp + qq * nm];
-                s = s + ((((wJ * L[pp][a]) * L[pp][i]) * L[qq][bb]) * L[qq][j]);
-            }
+        for (int qq = 0; qq < nm; ++qq) s = fma(G[qq * nq2 + a + i * nq] * L[qq][bb], L[qq][j], s);
         M[k] = s;
     }
+    free(G);
     double bfull[OG_SE_MAXNQ * OG_SE_MAXNQ];
     int cov[OG_SE_MAXNQ * OG_SE_MAXNQ], m = 0;
     for (int k = 0; k < nq2; ++k) {
@@ -1488,7 +1498,7 @@ static int og_se_project(const og_se_rule* r, const double* wj_e, const double* 
         for (int k = 0; k < nq2; ++k) out[p][k] = 0.0;
         for (int rc = 0; rc < m; ++rc) {
             double s = 0.0;
-            for (int cc = 0; cc < m; ++cc) s = s + Inv[rc * nq2 + cc] * b[p][cov[cc]];
+            for (int cc = 0; cc < m; ++cc) s = fma(Inv[rc * nq2 + cc], b[p][cov[cc]], s);
             out[p][cov[rc]] = s;
         }
     }
