@@ -18,7 +18,7 @@ from .grids import (
 )
 from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
 from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
-from .batch import ApplyPlan, build_batch
+from .batch import ApplyPlan, build_batch, regrid_batch_
 from .esmf import esmf_weights, load_esmf_weights, save_esmf_weights
 from .fold import mirror_fold_
 from .se import SpectralElementSpace, regrid_field_
@@ -49,6 +49,7 @@ __all__ = [
     "regrid",
     "regrid_",
     "regrid_adjoint_",
+    "regrid_batch_",
     "regrid_field_",
     "regrid_pullback",
     "regular_grid",

@@ -113,6 +113,7 @@ SIGNATURES = {
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_build_batch": (C.c_int, [C.c_int64, C.POINTER(crg_grid_desc), C.POINTER(crg_grid_desc),
                                   C.POINTER(crg_build_opts), C.c_int32, C.POINTER(C.c_void_p)]),
+    "crg_apply_batch": (C.c_int, [C.c_int64, C.POINTER(crg_apply_item), C.c_int32, C.c_void_p]),
     "crg_apply_plan_create": (C.c_int, [C.c_int64, C.POINTER(crg_apply_item), C.POINTER(C.c_void_p)]),
     "crg_apply_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "crg_apply_plan_destroy": (C.c_int, [C.c_void_p]),

@@ -1,6 +1,6 @@
-"""Many regridders at once: ``build_batch`` (concurrent builds, crg_build_batch)
-and ``ApplyPlan`` (the applies of a whole batch captured in one CUDA graph,
-crg_apply_plan_*).  The reference builds and applies one Regridder at a time
+"""Many regridders at once: ``build_batch`` (concurrent builds, crg_build_batch),
+``regrid_batch_`` (concurrent applies, crg_apply_batch) and ``ApplyPlan`` (the
+applies of a whole batch captured in one CUDA graph, crg_apply_plan_*).  The reference builds and applies one Regridder at a time
 (src/regridder/regridder.jl:105-163, src/regridder/regrid.jl:63-118)."""
 from __future__ import annotations
 
@@ -33,6 +33,48 @@ def build_batch(pairs, normalize: bool = False, nthreads: int = 0) -> list:
     return [Regridder._adopt(out[k]) for k in range(n)]
 
 
+def _items(items, normalize, what):
+    arr = (_lib.crg_apply_item * len(items))()
+    keep = []
+    for k, it in enumerate(items):
+        dst, R, src = it[0], it[1], it[2]
+        dims = it[3] if len(it) > 3 else 1
+        if not isinstance(R, Regridder):
+            raise ArgumentError(f"item {k}: expected a Regridder")
+        fs, fd = _Field(src), _Field(dst)
+        if what == "plan" and not (fs.torch and fs.cuda and fd.torch and fd.cuda):
+            raise ArgumentError(f"item {k}: plan fields must be CUDA tensors")
+        if fs.dtype != fd.dtype:
+            raise ArgumentError(f"item {k}: source and destination dtypes differ")
+        n_out, n_in = R.shape
+        ssc, ssf, nf_s = _layout(fs, dims, n_in, k, "source")
+        dsc, dsf, nf_d = _layout(fd, dims, n_out, k, "destination")
+        if nf_s != nf_d:
+            raise DimensionMismatch(f"item {k}: {nf_s} source fields but {nf_d} destination fields")
+        arr[k] = _lib.crg_apply_item(R._h.ptr, int(R._transposed), fs.dtype, fs.ptr, ssc, ssf, fd.ptr, dsc, dsf,
+                                     nf_s, int(bool(normalize)), 0)
+        keep += [src, dst, R]
+    return arr, keep
+
+
+def regrid_batch_(items, normalize: bool = True, nthreads: int = 0, stream=None):
+    """``regrid!`` for every item at once (crg_apply_batch): the applies run
+    concurrently from ``nthreads`` host threads (0: 4), each on its own
+    stream.  Items are ``(dst, R, src)`` or ``(dst, R, src, dims)`` with numpy
+    arrays or torch tensors (host or CUDA; 1-D, or 2-D with the spatial axis
+    ``dims``); outputs must not overlap.  With host fields the copies of the
+    items share both directions of the host link; they are complete on return."""
+    from .regridder import _resolve_stream
+
+    if not items:
+        return
+    arr, keep = _items(items, normalize, "batch")
+    fields = [_Field(x) for it in items for x in (it[0], it[2])]
+    st = _resolve_stream(fields, stream)
+    check(_lib.load().crg_apply_batch(len(items), arr, int(nthreads), C.c_void_p(st) if st else None))
+    del keep
+
+
 def _destroy(ptr):
     try:
         _lib.load(build_if_missing=False).crg_apply_plan_destroy(C.c_void_p(ptr))
@@ -52,26 +94,7 @@ class ApplyPlan:
     reads/writes them in place on every launch."""
 
     def __init__(self, items, normalize: bool = True):
-        arr = (_lib.crg_apply_item * len(items))()
-        self._keep = []
-        for k, it in enumerate(items):
-            dst, R, src = it[0], it[1], it[2]
-            dims = it[3] if len(it) > 3 else 1
-            if not isinstance(R, Regridder):
-                raise ArgumentError(f"item {k}: expected a Regridder")
-            fs, fd = _Field(src), _Field(dst)
-            if not (fs.torch and fs.cuda and fd.torch and fd.cuda):
-                raise ArgumentError(f"item {k}: plan fields must be CUDA tensors")
-            if fs.dtype != fd.dtype:
-                raise ArgumentError(f"item {k}: source and destination dtypes differ")
-            n_out, n_in = R.shape
-            ssc, ssf, nf_s = _layout(fs, dims, n_in, k, "source")
-            dsc, dsf, nf_d = _layout(fd, dims, n_out, k, "destination")
-            if nf_s != nf_d:
-                raise DimensionMismatch(f"item {k}: {nf_s} source fields but {nf_d} destination fields")
-            arr[k] = _lib.crg_apply_item(R._h.ptr, int(R._transposed), fs.dtype, fs.ptr, ssc, ssf, fd.ptr, dsc, dsf,
-                                         nf_s, int(bool(normalize)), 0)
-            self._keep += [src, dst, R]
+        arr, self._keep = _items(items, normalize, "plan")
         p = C.c_void_p()
         check(_lib.load().crg_apply_plan_create(len(items), arr, C.byref(p)))
         self._p = p.value

@@ -247,6 +247,10 @@ crg_status crg_get_esmf_weights(const crg_regridder* r, int32_t index_base, int6
   return guarded([&] { export_esmf(r, index_base, row, col, S, frac_a, frac_b, area_a, area_b); });
 }
 
+crg_status crg_apply_batch(int64_t n, const crg_apply_item* items, int32_t nthreads, void* stream) {
+  return guarded([&] { apply_batch_impl(n, items, nthreads, (cudaStream_t)stream); });
+}
+
 crg_status crg_build_se_to_fv(const crg_grid_desc* dst, const crg_se_space* src, const crg_se_opts* opts,
                               crg_regridder** out) {
   return guarded([&] {

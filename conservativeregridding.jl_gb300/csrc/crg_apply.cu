@@ -681,8 +681,45 @@ size_t elem_size(int dtype) { return dtype == CRG_F64 ? 8 : (dtype == CRG_F32 ? 
 
 }  // namespace
 
+// Whether an apply with host fields runs as the chunked pipeline, and its chunk.
+HostChunks host_chunks(size_t es, int64_t nin, int64_t nf, int64_t ssc, int64_t ssf, int64_t dsc, int64_t dsf,
+                       bool src_host, bool dst_host) {
+  HostChunks h;
+  h.cm = ssf == 1 && dsf == 1 && nf > 1;
+  const bool fm = ssc == 1 && dsc == 1 && nf > 1 && !h.cm;
+  // CRG_HOST_CHUNK_BYTES (64..4096, default 256) sets the cell-major row width for tuning
+  static const int64_t row_bytes = [] {
+    const char* e = getenv("CRG_HOST_CHUNK_BYTES");
+    const int64_t v = e ? atoll(e) : 256;
+    return (v >= 64 && v <= 4096) ? v : 256;
+  }();
+  h.chunk = h.cm ? std::max<int64_t>(4, row_bytes / (int64_t)es / 4 * 4) : (nf + 3) / 4;
+  h.ok = src_host && dst_host && nin > 0 && (h.cm || fm) && nf >= 2 * h.chunk;
+  return h;
+}
+
+bool host_pipeline_item(const crg_apply_item& it) {
+  const crg_regridder* r = it.regridder;
+  if (!r || it.nfields < 1 || !(it.dtype == CRG_F64 || it.dtype == CRG_F32 || it.dtype == CRG_BF16)) return false;
+  const bool t = it.transpose != 0;
+  const DevCsr& c = it.adjoint ? (t ? r->fwd : r->rev) : (t ? r->rev : r->fwd);
+  if (c.nrows == 0) return false;
+  const bool src_host = c.ncols > 0 && it.src && !is_device_pointer(it.src);
+  const bool dst_host = it.dst && !is_device_pointer(it.dst);
+  return host_chunks(elem_size(it.dtype), c.ncols, it.nfields, it.src_stride_cell, it.src_stride_field,
+                     it.dst_stride_cell, it.dst_stride_field, src_host, dst_host).ok;
+}
+
+int host_pipeline_dir(const crg_apply_item& it) {
+  const crg_regridder* r = it.regridder;
+  const bool t = it.transpose != 0;
+  const DevCsr& c = it.adjoint ? (t ? r->fwd : r->rev) : (t ? r->rev : r->fwd);
+  return &c == &r->rev ? 1 : 0;
+}
+
 void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint, const void* src, int64_t ssc,
-                int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st) {
+                int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st,
+                HostPipe* pipe) {
   crg_regridder* r = const_cast<crg_regridder*>(rc);
   CRG_REQUIRE(r != nullptr, CRG_ERR_INVALID_ARGUMENT, "regridder is NULL");
   CRG_REQUIRE(dtype == CRG_F64 || dtype == CRG_F32 || dtype == CRG_BF16, CRG_ERR_INVALID_ARGUMENT, "unknown dtype %d",
@@ -736,17 +773,21 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
     return;
   }
 
-  std::lock_guard<std::mutex> lock(r->stage_mu);
+  const int dir = &c == &r->rev ? 1 : 0;
+  std::unique_lock<std::mutex> lock(r->stage_mu[dir], std::defer_lock);
+  if (!pipe) lock.lock();  // a batch pipeline holds the staging locks of its items
   auto stage = [&](size_t need) {
-    if (r->stage_bytes < need) {
-      if (r->stage) CRG_CHECK_CUDA(cudaFree(r->stage));
-      r->stage = nullptr;
-      r->stage_bytes = 0;
-      CRG_CHECK_CUDA(cudaMalloc(&r->stage, need));
-      r->stage_bytes = need;
+    if (r->stage_bytes[dir] < need) {
+      if (r->stage[dir]) CRG_CHECK_CUDA(cudaFree(r->stage[dir]));
+      r->stage[dir] = nullptr;
+      r->stage_bytes[dir] = 0;
+      CRG_CHECK_CUDA(cudaMalloc(&r->stage[dir], need));
+      r->stage_bytes[dir] = need;
     }
-    return (char*)r->stage;
+    return (char*)r->stage[dir];
   };
+  cudaStream_t& copy_in = r->copy_in[dir];
+  cudaStream_t& copy_out = r->copy_out[dir];
 
   // Host fields in both directions, fields side by side (cell-major) or
   // whole fields contiguous (field-major): a pipeline over chunks of fields.
@@ -754,34 +795,42 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   // moves back, on two copy streams, so the two directions of the host link
   // run at once.  Cell-major chunks are 2-D copies of 256-byte rows (full link
   // speed); each chunk is applied as a contiguous (cells, fields) block.
-  const bool cm = ssf == 1 && dsf == 1 && nf > 1;
-  const bool fm = ssc == 1 && dsc == 1 && nf > 1 && !cm;
-  // CRG_HOST_CHUNK_BYTES (64..4096, default 256) sets the cell-major row width for tuning
-  static const int64_t row_bytes = [] {
-    const char* e = getenv("CRG_HOST_CHUNK_BYTES");
-    const int64_t v = e ? atoll(e) : 256;
-    return (v >= 64 && v <= 4096) ? v : 256;
-  }();
-  const int64_t chunk = cm ? std::max<int64_t>(4, row_bytes / (int64_t)es / 4 * 4) : (nf + 3) / 4;
-  if (src_host && dst_host && nin > 0 && (cm || fm) && nf >= 2 * chunk) {
+  const HostChunks hc = host_chunks(es, nin, nf, ssc, ssf, dsc, dsf, src_host, dst_host);
+  const bool cm = hc.cm;
+  const int64_t chunk = hc.chunk;
+  CRG_REQUIRE(!pipe || hc.ok, CRG_ERR_INTERNAL, "a batch pipeline item does not fit the chunked host pipeline");
+  if (hc.ok) {
     const int64_t nchunks = (nf + chunk - 1) / chunk;
     const size_t in_bytes = ((size_t)nin * nf * es + 255) / 256 * 256;
     char* din = stage(in_bytes + (size_t)nout * nf * es + 256);
     char* dout = din + in_bytes;
-    if (!r->copy_in) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&r->copy_in, cudaStreamNonBlocking));
-    if (!r->copy_out) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&r->copy_out, cudaStreamNonBlocking));
-    std::vector<cudaEvent_t> ev(2 * nchunks + 1, nullptr);
+    if (!pipe) {
+      if (!copy_in) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
+      if (!copy_out) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    }
+    // a batch pipeline runs every item's chunks on its own three streams, in order
+    cudaStream_t cin = pipe ? pipe->cin : copy_in, cout = pipe ? pipe->cout : copy_out;
+    if (pipe) st = pipe->cst;
+    std::vector<cudaEvent_t> local;
+    std::vector<cudaEvent_t>& ev = pipe ? pipe->events : local;
+    const size_t e0 = ev.size();
     struct Events {
       std::vector<cudaEvent_t>& v;
+      bool own;
       ~Events() {
-        for (auto e : v)
-          if (e) cudaEventDestroy(e);
+        if (own)
+          for (auto e : v)
+            if (e) cudaEventDestroy(e);
       }
-    } guard{ev};
-    for (auto& e : ev) CRG_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    // the copies start after the work the caller queued on its stream
-    CRG_CHECK_CUDA(cudaEventRecord(ev[2 * nchunks], st));
-    CRG_CHECK_CUDA(cudaStreamWaitEvent(r->copy_in, ev[2 * nchunks], 0));
+    } guard{local, true};
+    ev.resize(e0 + 2 * nchunks + 1, nullptr);
+    for (size_t k = e0; k < ev.size(); ++k) CRG_CHECK_CUDA(cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming));
+    auto E = [&](int64_t k) { return ev[e0 + k]; };
+    if (!pipe) {
+      // the copies start after the work the caller queued on its stream
+      CRG_CHECK_CUDA(cudaEventRecord(E(2 * nchunks), st));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(cin, E(2 * nchunks), 0));
+    }
     const char* hs = (const char*)src;
     char* hd = (char*)dst;
     for (int64_t k = 0; k < nchunks; ++k) {
@@ -790,25 +839,27 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
       char* yk = dout + (size_t)f0 * nout * es;
       if (cm)
         CRG_CHECK_CUDA(cudaMemcpy2DAsync(xk, fc * es, hs + f0 * es, ssc * es, fc * es, nin, cudaMemcpyHostToDevice,
-                                         r->copy_in));
+                                         cin));
       else
         CRG_CHECK_CUDA(cudaMemcpy2DAsync(xk, nin * es, hs + f0 * ssf * es, ssf * es, nin * es, fc,
-                                         cudaMemcpyHostToDevice, r->copy_in));
-      CRG_CHECK_CUDA(cudaEventRecord(ev[2 * k], r->copy_in));
-      CRG_CHECK_CUDA(cudaStreamWaitEvent(st, ev[2 * k], 0));
+                                         cudaMemcpyHostToDevice, cin));
+      CRG_CHECK_CUDA(cudaEventRecord(E(2 * k), cin));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(st, E(2 * k), 0));
       if (cm) compute(xk, fc, 1, yk, fc, 1, fc, st);
       else compute(xk, 1, nin, yk, 1, nout, fc, st);
-      CRG_CHECK_CUDA(cudaEventRecord(ev[2 * k + 1], st));
-      CRG_CHECK_CUDA(cudaStreamWaitEvent(r->copy_out, ev[2 * k + 1], 0));
+      CRG_CHECK_CUDA(cudaEventRecord(E(2 * k + 1), st));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(cout, E(2 * k + 1), 0));
       if (cm)
         CRG_CHECK_CUDA(cudaMemcpy2DAsync(hd + f0 * es, dsc * es, yk, fc * es, fc * es, nout, cudaMemcpyDeviceToHost,
-                                         r->copy_out));
+                                         cout));
       else
         CRG_CHECK_CUDA(cudaMemcpy2DAsync(hd + f0 * dsf * es, dsf * es, yk, nout * es, nout * es, fc,
-                                         cudaMemcpyDeviceToHost, r->copy_out));
+                                         cudaMemcpyDeviceToHost, cout));
     }
-    CRG_CHECK_CUDA(cudaStreamSynchronize(r->copy_out));
-    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    if (!pipe) {
+      CRG_CHECK_CUDA(cudaStreamSynchronize(cout));
+      CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    }
     return;
   }
 

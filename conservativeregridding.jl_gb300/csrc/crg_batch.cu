@@ -1,5 +1,5 @@
-// crg_batch.cu -- many regridders at once: concurrent builds and a
-// graph-captured apply of a whole batch.
+// crg_batch.cu -- many regridders at once: concurrent builds, concurrent
+// applies and a graph-captured apply of a whole batch.
 //
 // The reference builds and applies one Regridder at a time
 // (src/regridder/regridder.jl:105-163, src/regridder/regrid.jl:63-118).  For
@@ -7,7 +7,10 @@
 // of short kernels separated by host synchronisations, so crg_build_batch
 // runs the builds from several host threads, each on its own stream, and
 // crg_apply_plan captures the applies of all pairs into one CUDA graph that
-// replays with a single launch.
+// replays with a single launch.  crg_apply_batch runs independent applies
+// from several host threads: with host fields, the copies of one item
+// overlap those of the others on both directions of the host link.
+#include <algorithm>
 #include <atomic>
 #include <string>
 #include <thread>
@@ -74,6 +77,129 @@ void build_batch_impl(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* 
       throw Fail{status[k]};
     }
   }
+}
+
+void apply_batch_impl(int64_t n, const crg_apply_item* items, int nthreads, cudaStream_t st) {
+  CRG_REQUIRE(n >= 0, CRG_ERR_INVALID_ARGUMENT, "n must be >= 0");
+  CRG_REQUIRE(n == 0 || items, CRG_ERR_INVALID_ARGUMENT, "items must not be NULL");
+  for (int64_t k = 0; k < n; ++k)
+    CRG_REQUIRE(items[k].regridder, CRG_ERR_INVALID_ARGUMENT, "item %lld has no regridder", (long long)k);
+  if (n == 0) return;
+  int dev = 0;
+  CRG_CHECK_CUDA(cudaGetDevice(&dev));
+  // Host fields in every item, each matrix copy once: one chunk pipeline over
+  // all items (the copies in of an item follow those of the one before it on
+  // one stream while that one's results go out on another).
+  bool pipeline = n > 1;
+  std::vector<std::mutex*> mus;
+  for (int64_t k = 0; k < n && pipeline; ++k) {
+    if (!host_pipeline_item(items[k])) pipeline = false;
+    else mus.push_back(&const_cast<crg_regridder*>(items[k].regridder)->stage_mu[host_pipeline_dir(items[k])]);
+  }
+  if (pipeline) {
+    std::sort(mus.begin(), mus.end());
+    if (std::adjacent_find(mus.begin(), mus.end()) != mus.end()) pipeline = false;
+  }
+  if (pipeline) {
+    std::vector<std::unique_lock<std::mutex>> locks;
+    for (auto* m : mus) locks.emplace_back(*m);  // address order: no lock-order cycles
+    HostPipe p;
+    cudaEvent_t start = nullptr;
+    auto cleanup = [&]() {
+      for (cudaStream_t s : {p.cin, p.cst, p.cout})
+        if (s) cudaStreamSynchronize(s);
+      for (cudaStream_t s : {p.cin, p.cst, p.cout})
+        if (s) cudaStreamDestroy(s);
+      for (auto e : p.events)
+        if (e) cudaEventDestroy(e);
+      if (start) cudaEventDestroy(start);
+    };
+    try {
+      for (cudaStream_t* s : {&p.cin, &p.cst, &p.cout}) CRG_CHECK_CUDA(cudaStreamCreateWithFlags(s, cudaStreamNonBlocking));
+      CRG_CHECK_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+      CRG_CHECK_CUDA(cudaEventRecord(start, st));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(p.cin, start, 0));
+      CRG_CHECK_CUDA(cudaStreamWaitEvent(p.cst, start, 0));
+      for (int64_t k = 0; k < n; ++k) {
+        const crg_apply_item& it = items[k];
+        try {
+          apply_impl(it.regridder, it.transpose, it.dtype, it.adjoint != 0, it.src, it.src_stride_cell,
+                     it.src_stride_field, it.dst, it.dst_stride_cell, it.dst_stride_field, it.nfields, it.normalize,
+                     p.cst, &p);
+        } catch (const Fail&) {
+          const std::string m = crg_last_error();
+          set_error("item %lld: %s", (long long)k, m.c_str());
+          throw;
+        }
+      }
+      CRG_CHECK_CUDA(cudaStreamSynchronize(p.cout));
+      CRG_CHECK_CUDA(cudaStreamSynchronize(p.cst));
+    } catch (...) {
+      cleanup();
+      throw;
+    }
+    cleanup();
+    return;
+  }
+  cudaEvent_t start = nullptr;
+  CRG_CHECK_CUDA(cudaEventCreateWithFlags(&start, cudaEventDisableTiming));
+  const cudaError_t er = cudaEventRecord(start, st);
+  if (er != cudaSuccess) {
+    cudaEventDestroy(start);
+    CRG_CHECK_CUDA(er);
+  }
+  const int workers = (int)std::min<int64_t>(n, nthreads > 0 ? nthreads : 4);
+  std::vector<crg_status> status(n, CRG_OK);
+  std::vector<std::string> message(n);
+  std::vector<cudaEvent_t> done(workers, nullptr);
+  std::atomic<int64_t> next{0};
+  auto work = [&](int wi) {
+    cudaStream_t s = nullptr;
+    if (cudaSetDevice(dev) != cudaSuccess || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamWaitEvent(s, start, 0) != cudaSuccess) {
+      for (int64_t k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+        status[k] = CRG_ERR_CUDA;
+        message[k] = "could not set up a stream for an apply worker";
+      }
+      if (s) cudaStreamDestroy(s);
+      return;
+    }
+    for (int64_t k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+      const crg_apply_item& it = items[k];
+      try {
+        apply_impl(it.regridder, it.transpose, it.dtype, it.adjoint != 0, it.src, it.src_stride_cell,
+                   it.src_stride_field, it.dst, it.dst_stride_cell, it.dst_stride_field, it.nfields, it.normalize, s);
+      } catch (const Fail& e) {
+        status[k] = e.st;
+        message[k] = crg_last_error();
+      } catch (...) {
+        status[k] = CRG_ERR_INTERNAL;
+        message[k] = "unexpected internal error";
+      }
+    }
+    // the caller's stream continues after this worker's device work
+    if (cudaEventCreateWithFlags(&done[wi], cudaEventDisableTiming) == cudaSuccess) cudaEventRecord(done[wi], s);
+    cudaStreamDestroy(s);
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < workers; ++t) pool.emplace_back(work, t);
+  work(0);  // the calling thread works too
+  for (auto& th : pool) th.join();
+  cudaEventDestroy(start);
+  cudaError_t werr = cudaSuccess;
+  for (auto e : done) {
+    if (!e) continue;
+    const cudaError_t w = cudaStreamWaitEvent(st, e, 0);
+    if (werr == cudaSuccess) werr = w;
+    cudaEventDestroy(e);
+  }
+  for (int64_t k = 0; k < n; ++k) {
+    if (status[k] != CRG_OK) {
+      set_error("item %lld: %s", (long long)k, message[k].c_str());
+      throw Fail{status[k]};
+    }
+  }
+  CRG_CHECK_CUDA(werr);
 }
 
 crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {

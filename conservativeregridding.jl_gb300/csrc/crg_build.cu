@@ -1227,9 +1227,11 @@ void free_regridder(crg_regridder* r) {
   cudaFree(r->src_area);
   cudaFree(r->row_sum);
   cudaFree(r->col_sum);
-  if (r->stage) cudaFree(r->stage);
-  if (r->copy_in) cudaStreamDestroy(r->copy_in);
-  if (r->copy_out) cudaStreamDestroy(r->copy_out);
+  for (int d = 0; d < 2; ++d) {
+    if (r->stage[d]) cudaFree(r->stage[d]);
+    if (r->copy_in[d]) cudaStreamDestroy(r->copy_in[d]);
+    if (r->copy_out[d]) cudaStreamDestroy(r->copy_out[d]);
+  }
   cudaSetDevice(dev);
   delete r;
 }

@@ -5,6 +5,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "crg.h"
 
@@ -129,11 +130,13 @@ struct crg_regridder {
   double* col_sum = nullptr;    // [ns] Kahan column sums of A
   crg_info info{};
   // staging for host-memory fields in crg_apply
-  std::mutex stage_mu;
-  void* stage = nullptr;
-  size_t stage_bytes = 0;
-  cudaStream_t copy_in = nullptr;   // host -> device copies of the chunked host-field pipeline
-  cudaStream_t copy_out = nullptr;  // device -> host copies of it
+  // per matrix copy ([0] A, [1] A^T), so that an apply of R and one of
+  // transpose(R) with host fields can run at the same time
+  std::mutex stage_mu[2];
+  void* stage[2] = {nullptr, nullptr};
+  size_t stage_bytes[2] = {0, 0};
+  cudaStream_t copy_in[2] = {nullptr, nullptr};   // host -> device copies of the chunked host-field pipeline
+  cudaStream_t copy_out[2] = {nullptr, nullptr};  // device -> host copies of it
   // field-major apply per matrix copy (fwd, rev) and dtype (FP32, BF16):
   // 0 not yet timed, 1 row kernel, 2 transposes around the cell-major kernel
   std::atomic<int> fm_choice[2][2] = {};
@@ -143,8 +146,23 @@ namespace crg {
 // crg_build_impl lives in crg_build.cu; apply entry points in crg_apply.cu.
 crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts);
 void free_regridder(crg_regridder* r);
+// Streams and events shared by the applies of a batch with host fields: the
+// chunks of all items form one pipeline (copies in on cin, applies on cst,
+// copies out on cout, in item order).  Owned by the batch.
+struct HostPipe {
+  cudaStream_t cin = nullptr, cst = nullptr, cout = nullptr;
+  std::vector<cudaEvent_t> events;
+};
+struct HostChunks {
+  bool ok = false, cm = false;
+  int64_t chunk = 0;
+};
 void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, const void* src, int64_t ssc,
-                int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int normalize, cudaStream_t st);
+                int64_t ssf, void* dst, int64_t dsc, int64_t dsf, int64_t nfields, int normalize, cudaStream_t st,
+                HostPipe* pipe = nullptr);
+// whether an item's apply runs as the chunked host pipeline, and which matrix copy it reads
+bool host_pipeline_item(const crg_apply_item& it);
+int host_pipeline_dir(const crg_apply_item& it);
 bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
@@ -193,6 +211,7 @@ void mirror_fold_impl(int dtype, void* field, int64_t sc, int64_t sf, int64_t nf
 void build_batch_impl(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
                       int nthreads, crg_regridder** out);
 crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items);
+void apply_batch_impl(int64_t n, const crg_apply_item* items, int nthreads, cudaStream_t st);
 void apply_plan_launch_impl(crg_apply_plan* p, cudaStream_t st);
 void apply_plan_destroy_impl(crg_apply_plan* p);
 }  // namespace crg

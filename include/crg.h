@@ -171,6 +171,16 @@ typedef struct crg_apply_item {
  * shared).  The plan retains the regridders and keeps the field pointers:
  * launch it again after writing new values into the same buffers.  Its
  * temporaries are graph allocations; launches of one plan must not overlap. */
+/* The applies of n items (the arguments of crg_apply; host or device fields)
+ * run concurrently on up to nthreads host threads (0: 4), each on its own
+ * stream, after the work queued on `stream`; `stream` continues after all of
+ * them, and items with host fields are complete on return.  Independent
+ * applies with host fields thus share both directions of the host link (e.g.
+ * R on one field set and transpose(R) on another).  Outputs must not overlap.
+ * On failure the first failing item is named.  No reference counterpart: the
+ * reference applies one regridder, one slice at a time. */
+crg_status crg_apply_batch(int64_t n, const crg_apply_item* items, int32_t nthreads, void* stream);
+
 typedef struct crg_apply_plan crg_apply_plan;
 crg_status crg_apply_plan_create(int64_t n, const crg_apply_item* items, crg_apply_plan** out);
 crg_status crg_apply_plan_launch(crg_apply_plan* plan, void* stream);

@@ -9,7 +9,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from crg import ApplyPlan, ArgumentError, Regridder, build_batch, grids, regrid_
+from crg import ApplyPlan, ArgumentError, Regridder, build_batch, grids, regrid_, regrid_batch_
 
 pytestmark = pytest.mark.gpu
 
@@ -94,3 +94,43 @@ def test_apply_plan_rejects_host_fields(pairs):
     R = Regridder(*pairs[-1])
     with pytest.raises(ArgumentError):
         ApplyPlan([(torch.zeros(R.shape[0]), R, torch.zeros(R.shape[1]))])
+
+
+def test_regrid_batch_equals_single_applies(pairs):
+    """crg_apply_batch: host (numpy, pinned torch) and CUDA fields, R and
+    transpose(R) of the same handle at once (separate staging per direction),
+    bit for bit the single applies."""
+    import torch
+
+    Rs = build_batch(pairs[:4], normalize=True)
+    rng = np.random.default_rng(5)
+    items, refs = [], []
+    for k, R in enumerate(Rs):
+        for RR in (R, R.transpose()):
+            n_out, n_in = RR.shape
+            K = 1 + 37 * k
+            x = rng.standard_normal((n_in, K)).astype(np.float32)
+            if k % 3 == 0:
+                src, dst = x, np.full((n_out, K), np.nan, np.float32)
+            elif k % 3 == 1:
+                src = torch.from_numpy(x).pin_memory()
+                dst = torch.full((n_out, K), float("nan")).pin_memory()
+            else:
+                src, dst = torch.from_numpy(x).cuda(), torch.full((n_out, K), float("nan"), device="cuda")
+            items.append((dst, RR, src, 1))
+            refs.append((RR, x))
+    regrid_batch_(items, nthreads=3)
+    torch.cuda.synchronize()
+    for (dst, _, _, _), (RR, x) in zip(items, refs):
+        expect = np.empty((RR.shape[0], x.shape[1]), np.float32)
+        regrid_(expect, RR, x)
+        got = dst.cpu().numpy() if hasattr(dst, "cpu") else dst
+        assert np.array_equal(got, expect)
+
+
+def test_regrid_batch_names_the_failing_item(pairs):
+    R = Regridder(*pairs[0])
+    good = (np.zeros(R.shape[0]), R, np.ones(R.shape[1]))
+    bad = (np.zeros(R.shape[0] + 1), R, np.ones(R.shape[1]))
+    with pytest.raises(Exception, match="item 1|cells"):
+        regrid_batch_([good, bad])
