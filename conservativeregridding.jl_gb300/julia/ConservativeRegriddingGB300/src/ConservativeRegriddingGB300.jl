@@ -240,6 +240,16 @@ mutable struct ApplyPlan
         return p
     end
 end
+"""
+    apply_batch!(items::Vector{CrgApplyItem}; nthreads = 0)
+
+`crg_apply_batch`: independent applies at once (host arrays: one chunk
+pipeline over all items, so their copies share both link directions).
+"""
+apply_batch!(items::Vector{CrgApplyItem}; nthreads::Integer = 0, stream::Ptr{Cvoid} = C_NULL) =
+    check(ccall((:crg_apply_batch, libcrg[]), Cint, (Int64, Ptr{CrgApplyItem}, Int32, Ptr{Cvoid}),
+                length(items), items, Int32(nthreads), stream))
+
 launch(p::ApplyPlan; stream::Ptr{Cvoid} = C_NULL) =
     check(ccall((:crg_apply_plan_launch, libcrg[]), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), p.ptr, stream))
 

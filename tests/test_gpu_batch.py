@@ -134,3 +134,29 @@ def test_regrid_batch_names_the_failing_item(pairs):
     bad = (np.zeros(R.shape[0] + 1), R, np.ones(R.shape[1]))
     with pytest.raises(Exception, match="item 1|cells"):
         regrid_batch_([good, bad])
+
+
+@pytest.mark.parametrize("same_copy", [False, True])
+def test_regrid_batch_host_pipeline(pairs, same_copy):
+    """Host fields in every item: one chunk pipeline over the items (distinct
+    matrix copies), or threads when a matrix copy repeats; bit for bit the
+    single applies either way, cell-major and field-major."""
+    import torch
+
+    R1, R2 = build_batch(pairs[6:8], normalize=True)
+    rng = np.random.default_rng(9)
+    specs = [(R1, 1), (R1.transpose(), 2), (R2, 1)] if not same_copy else [(R1, 1), (R1, 2)]
+    items, refs = [], []
+    for RR, dims in specs:
+        n_out, n_in = RR.shape
+        K = 160
+        x = rng.standard_normal((n_in, K) if dims == 1 else (K, n_in)).astype(np.float32)
+        src = torch.from_numpy(x).pin_memory()
+        dst = torch.full((n_out, K) if dims == 1 else (K, n_out), float("nan")).pin_memory()
+        items.append((dst, RR, src, dims))
+        refs.append((RR, x, dims))
+    regrid_batch_(items)
+    for (dst, _, _, _), (RR, x, dims) in zip(items, refs):
+        expect = np.empty(dst.shape, np.float32)
+        regrid_(expect, RR, x, dims=dims)
+        assert np.array_equal(dst.numpy(), expect)
