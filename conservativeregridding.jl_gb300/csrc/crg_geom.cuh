@@ -338,21 +338,58 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
     // all vertices, then the crossing points -- two for a convex polygon,
     // computed in fixed slots so the lanes of a warp run them together --
     // then the output sequence.
+    //
+    // On the sphere a side is first decided in FP32: with n32, w32 = v32 - ca32
+    // rounded from the FP64 plane and unit vectors, |s32 - n.(v - ca)| stays
+    // below 2^-21 |n32|_1 (1 + |w32|_inf), so |s32| > B = 2^-18 |n32|_1
+    // (1 + |w32|_1) gives the exact sign with an 8x margin.  The FP64 side
+    // (with its exact-sign fallback) is taken only where that test is
+    // undecided and for the endpoints of the crossing edges, whose values
+    // weight the crossing points: decisions and values are those of the
+    // one-pass loop.
     double sv[CRG_MAXC];
-    int nin = 0;
-    for (int i = 0; i < n; ++i) {
-      sv[i] = kSpherical ? side_sph(nrm, ca, cb, eb, isig, in[i]) : side_pl(ca, cb, ex, ey, isig, in[i]);
-      nin += sv[i] >= 0.0;
+    uint32_t inside = 0u, known = 0u;  // bit i: vertex i inside; sv[i] computed
+    if (kSpherical) {
+      const float nx = (float)nrm.x, ny = (float)nrm.y, nz = (float)nrm.z;
+      const float ax = (float)ca.x, ay = (float)ca.y, az = (float)ca.z;
+      const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+      for (int i = 0; i < n; ++i) {
+        const float wx = (float)in[i].x - ax, wy = (float)in[i].y - ay, wz = (float)in[i].z - az;
+        const float s32 = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
+        const float B = 3.814697265625e-06f * n1 * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
+        if (s32 > B) {
+          inside |= 1u << i;
+        } else if (!(s32 < -B)) {
+          sv[i] = side_sph(nrm, ca, cb, eb, isig, in[i]);
+          known |= 1u << i;
+          if (sv[i] >= 0.0) inside |= 1u << i;
+        }
+      }
+    } else {
+      for (int i = 0; i < n; ++i) {
+        sv[i] = side_pl(ca, cb, ex, ey, isig, in[i]);
+        known |= 1u << i;
+        if (sv[i] >= 0.0) inside |= 1u << i;
+      }
     }
+    const int nin = __popc(inside);
     if (nin == n) continue;  // all inside: the stage returns the polygon unchanged
     if (nin == 0) {
       n = 0;
       break;
     }
+    auto side = [&](int i) -> double {
+      if (!((known >> i) & 1u)) {
+        sv[i] = kSpherical ? side_sph(nrm, ca, cb, eb, isig, in[i]) : side_pl(ca, cb, ex, ey, isig, in[i]);
+        known |= 1u << i;
+      }
+      return sv[i];
+    };
+    auto isin = [&](int i) { return ((inside >> i) & 1u) != 0u; };
     int e0 = -1, e1 = -1, ncross = 0;
     for (int i = 0; i < n; ++i) {
       const int p = i == 0 ? n - 1 : i - 1;
-      if ((sv[i] >= 0.0) != (sv[p] >= 0.0)) {
+      if (isin(i) != isin(p)) {
         if (ncross == 0) e0 = i;
         else e1 = i;
         ++ncross;
@@ -361,13 +398,14 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
     d3 x0{0.0, 0.0, 0.0}, x1{0.0, 0.0, 0.0};
     if (ncross == 2) {
       const int p0 = e0 == 0 ? n - 1 : e0 - 1, p1 = e1 == 0 ? n - 1 : e1 - 1;
-      x0 = kSpherical ? isect_sph(in[p0], sv[p0], in[e0], sv[e0]) : isect_pl(in[p0], sv[p0], in[e0], sv[e0]);
-      x1 = kSpherical ? isect_sph(in[p1], sv[p1], in[e1], sv[e1]) : isect_pl(in[p1], sv[p1], in[e1], sv[e1]);
+      const double s_p0 = side(p0), s_e0 = side(e0), s_p1 = side(p1), s_e1 = side(e1);
+      x0 = kSpherical ? isect_sph(in[p0], s_p0, in[e0], s_e0) : isect_pl(in[p0], s_p0, in[e0], s_e0);
+      x1 = kSpherical ? isect_sph(in[p1], s_p1, in[e1], s_e1) : isect_pl(in[p1], s_p1, in[e1], s_e1);
     }
     int m = 0;
     for (int i = 0; i < n; ++i) {
       const int p = i == 0 ? n - 1 : i - 1;
-      const bool ci = sv[i] >= 0.0, pi = sv[p] >= 0.0;
+      const bool ci = isin(i), pi = isin(p);
       if (ci == pi) {
         if (ci) {
           if (m >= CRG_MAXC) return -1;
@@ -376,8 +414,13 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
         continue;
       }
       // a crossing edge (more than two only for non-convex input: computed here)
-      const d3 x = ncross == 2 ? (i == e0 ? x0 : x1)
-                              : (kSpherical ? isect_sph(in[p], sv[p], in[i], sv[i]) : isect_pl(in[p], sv[p], in[i], sv[i]));
+      d3 x;
+      if (ncross == 2) {
+        x = i == e0 ? x0 : x1;
+      } else {
+        const double sp = side(p), sc = side(i);
+        x = kSpherical ? isect_sph(in[p], sp, in[i], sc) : isect_pl(in[p], sp, in[i], sc);
+      }
       if (m >= CRG_MAXC) return -1;
       out[m++] = x;
       if (ci) {
