@@ -710,6 +710,21 @@ bool host_pipeline_item(const crg_apply_item& it) {
                      it.dst_stride_cell, it.dst_stride_field, src_host, dst_host).ok;
 }
 
+// Bytes of an item's first chunk in and last chunk out: the parts of the
+// pipeline that overlap nothing when the item comes first or last.
+void host_pipeline_ends(const crg_apply_item& it, size_t& fill, size_t& drain) {
+  const crg_regridder* r = it.regridder;
+  const bool t = it.transpose != 0;
+  const DevCsr& c = it.adjoint ? (t ? r->fwd : r->rev) : (t ? r->rev : r->fwd);
+  const size_t es = elem_size(it.dtype);
+  const HostChunks h = host_chunks(es, c.ncols, it.nfields, it.src_stride_cell, it.src_stride_field,
+                                   it.dst_stride_cell, it.dst_stride_field, true, true);
+  const int64_t chunk = std::max<int64_t>(1, h.chunk);
+  const int64_t last = it.nfields - (it.nfields - 1) / chunk * chunk;
+  fill = (size_t)c.ncols * (size_t)std::min<int64_t>(chunk, it.nfields) * es;
+  drain = (size_t)c.nrows * (size_t)last * es;
+}
+
 int host_pipeline_dir(const crg_apply_item& it) {
   const crg_regridder* r = it.regridder;
   const bool t = it.transpose != 0;

@@ -120,7 +120,23 @@ void apply_batch_impl(int64_t n, const crg_apply_item* items, int nthreads, cuda
       CRG_CHECK_CUDA(cudaEventRecord(start, st));
       CRG_CHECK_CUDA(cudaStreamWaitEvent(p.cin, start, 0));
       CRG_CHECK_CUDA(cudaStreamWaitEvent(p.cst, start, 0));
+      // items are independent: the one with the smallest first chunk in goes
+      // first and, of the others, the one with the smallest last chunk out goes
+      // last (the pipeline's fill and drain overlap nothing)
+      std::vector<int64_t> order(n);
+      std::vector<size_t> fill(n), drain(n);
       for (int64_t k = 0; k < n; ++k) {
+        order[k] = k;
+        host_pipeline_ends(items[k], fill[k], drain[k]);
+      }
+      const int64_t f = std::min_element(fill.begin(), fill.end()) - fill.begin();
+      std::swap(order[0], order[f]);
+      int64_t l = 1;
+      for (int64_t k = 2; k < n; ++k)
+        if (drain[order[k]] < drain[order[l]]) l = k;
+      std::swap(order[l], order[n - 1]);
+      for (int64_t q = 0; q < n; ++q) {
+        const int64_t k = order[q];
         const crg_apply_item& it = items[k];
         try {
           apply_impl(it.regridder, it.transpose, it.dtype, it.adjoint != 0, it.src, it.src_stride_cell,

@@ -163,6 +163,7 @@ void apply_impl(const crg_regridder* r, int transpose, int dtype, bool adjoint, 
 // whether an item's apply runs as the chunked host pipeline, and which matrix copy it reads
 bool host_pipeline_item(const crg_apply_item& it);
 int host_pipeline_dir(const crg_apply_item& it);
+void host_pipeline_ends(const crg_apply_item& it, size_t& fill, size_t& drain);
 bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
