@@ -404,9 +404,14 @@ __device__ __forceinline__ int64_t warp_append(int k, unsigned long long* counte
 // One level of the dual traversal.  Each frontier pair (dst node, src node)
 // expands the non-leaf side(s); child pairs whose boxes overlap go to the next
 // frontier, or to the leaf-pair list when both children are leaves.
-__global__ void k_traverse(const uint2* __restrict__ in, int64_t nin, TreeView td, TreeView ts,
-                           uint2* __restrict__ next, unsigned long long* __restrict__ nnext,
-                           uint2* __restrict__ leaves, unsigned long long* __restrict__ nleaves) {
+// One level of the dual traversal.  nin < 0: the frontier size is *nin_dev
+// (written by the previous level on the device).  Appends past the capacities
+// are dropped and raise *overflow (the host then runs the level loop).
+__global__ void k_traverse(const uint2* __restrict__ in, int64_t nin, const unsigned long long* __restrict__ nin_dev,
+                           TreeView td, TreeView ts, uint2* __restrict__ next, unsigned long long* __restrict__ nnext,
+                           int64_t cap_next, uint2* __restrict__ leaves, unsigned long long* __restrict__ nleaves,
+                           int64_t cap_leaves, int* __restrict__ overflow) {
+  if (nin < 0) nin = (int64_t)*nin_dev;
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t nloop = (nin + 31) / 32 * 32;
@@ -448,6 +453,10 @@ __global__ void k_traverse(const uint2* __restrict__ in, int64_t nin, TreeView t
     }
     int64_t pi = warp_append(ni, nnext);
     int64_t pl = warp_append(nl, nleaves);
+    if (pi + ni > cap_next || pl + nl > cap_leaves) {
+      if (nout) atomicExch(overflow, 1);
+      continue;
+    }
     for (int k = 0; k < nout; ++k) {
       if (node_lev(outs[k].x) == 0 && node_lev(outs[k].y) == 0) leaves[pl++] = outs[k];
       else next[pi++] = outs[k];
@@ -1087,6 +1096,8 @@ void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& c
   if (D.t.ncells == 0 || S.t.ncells == 0) return;
   TreeView tv_d = view_of(D.t), tv_s = view_of(S.t);
   DBuf<unsigned long long> counters(2, st);
+  DBuf<int> counters_ovf(1, st);
+  counters_ovf.zero();
   DBuf<uint2> front, next, leafp;
   size_t front_cap = 1024, leaf_cap = 1 << 16;
   front.alloc(front_cap, st);
@@ -1102,6 +1113,39 @@ void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& c
   } else {
     CRG_CHECK_CUDA(cudaMemcpyAsync(front.p, &root, sizeof(uint2), cudaMemcpyHostToDevice, st));
   }
+  // All levels launched back to back (pairs of a level are all at the same
+  // two tree levels, so there are max(levels) - 1 of them), the frontier sizes
+  // kept on the device: one host round trip instead of one per level.
+  if (nfront > 0) {
+    const int steps = std::max(D.t.nlev, S.t.nlev) - 1;
+    const int64_t cap = std::max<int64_t>(1 << 16, 2 * (D.t.ncells + S.t.ncells));
+    DBuf<uint2> fa((size_t)cap, st), fb((size_t)cap, st), fl((size_t)cap, st);
+    DBuf<unsigned long long> cnt((size_t)steps + 2, st);
+    DBuf<int> ovf(1, st);
+    cnt.zero();
+    ovf.zero();
+    const unsigned long long one = 1ull;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(cnt.p, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+    CRG_CHECK_CUDA(cudaMemcpyAsync(fa.p, &root, sizeof(uint2), cudaMemcpyHostToDevice, st));
+    for (int l = 0; l < steps; ++l) {
+      uint2* in = (l & 1) ? fb.p : fa.p;
+      uint2* out = (l & 1) ? fa.p : fb.p;
+      k_traverse<<<152 * 8, 256, 0, st>>>(in, -1, cnt.p + l, tv_d, tv_s, out, cnt.p + l + 1, cap, fl.p,
+                                          cnt.p + steps + 1, cap, ovf.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    unsigned long long hl[2] = {0ull, 0ull};
+    int hov = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(hl, cnt.p + steps, sizeof(hl), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hov, ovf.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    if (!hov && hl[0] == 0) {  // every pair reached the leaves within the capacities
+      nleaf = (int64_t)hl[1];
+      nfront = 0;
+      std::swap(leafp.p, fl.p);
+      std::swap(leafp.n, fl.n);
+    }
+  }
   while (nfront > 0) {
     if (next.n < (size_t)nfront * 4) next.alloc((size_t)nfront * 8, st);
     if (leafp.n < (size_t)(nleaf + nfront * 4)) {
@@ -1113,7 +1157,9 @@ void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& c
     unsigned long long hc[2] = {0ull, (unsigned long long)nleaf};
     CRG_CHECK_CUDA(cudaMemcpyAsync(counters.p, hc, sizeof(hc), cudaMemcpyHostToDevice, st));
     int64_t blocks = std::min<int64_t>(nblk(nfront, 256), 152 * 16);
-    k_traverse<<<(unsigned)blocks, 256, 0, st>>>(front.p, nfront, tv_d, tv_s, next.p, counters.p, leafp.p, counters.p + 1);
+    k_traverse<<<(unsigned)blocks, 256, 0, st>>>(front.p, nfront, nullptr, tv_d, tv_s, next.p, counters.p,
+                                                 (int64_t)next.n, leafp.p, counters.p + 1, (int64_t)leafp.n,
+                                                 counters_ovf.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     CRG_CHECK_CUDA(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, st));
     CRG_CHECK_CUDA(cudaStreamSynchronize(st));
