@@ -1341,72 +1341,6 @@ void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
   }
 }
 
-namespace {
-
-__global__ void k_coo_count(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols, int64_t m,
-                            int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  atomicAdd(&rowcnt[rows[t]], 1);
-  atomicAdd(&colcnt[cols[t]], 1);
-}
-
-// Entries land in an arbitrary order inside each row; sort_rows then orders
-// them by column (columns are distinct within a row, so the result is unique).
-__global__ void k_coo_scatter(const int32_t* __restrict__ rows, const int32_t* __restrict__ cols,
-                              const double* __restrict__ vals, int64_t m, const int32_t* __restrict__ rowptr,
-                              int32_t* __restrict__ rowfill, const int32_t* __restrict__ colptr,
-                              int32_t* __restrict__ colfill, int32_t* __restrict__ fidx, double* __restrict__ fval,
-                              int32_t* __restrict__ ridx, double* __restrict__ rval) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= m) return;
-  const int32_t r = rows[t], c = cols[t];
-  const double v = vals[t];
-  const int32_t p = rowptr[r] + atomicAdd(&rowfill[r], 1);
-  fidx[p] = c;
-  fval[p] = v;
-  const int32_t q = colptr[c] + atomicAdd(&colfill[c], 1);
-  ridx[q] = r;
-  rval[q] = v;
-}
-
-}  // namespace
-
-void assemble_coo(crg_regridder* R, int64_t m, const int32_t* rows, const int32_t* cols, const double* vals,
-                  cudaStream_t st) {
-  CRG_REQUIRE(m < ((int64_t)1 << 31), CRG_ERR_NOT_SUPPORTED, "%lld nonzeros exceed the 32-bit entry range",
-              (long long)m);
-  const int64_t nd = R->nd, ns = R->ns;
-  DBuf<int32_t> rowcnt((size_t)nd + 1, st), colcnt((size_t)ns + 1, st);
-  rowcnt.zero();
-  colcnt.zero();
-  if (m) {
-    k_coo_count<<<nblk(m, 256), 256, 0, st>>>(rows, cols, m, rowcnt.p, colcnt.p);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-  R->fwd.nrows = nd; R->fwd.ncols = ns;
-  R->rev.nrows = ns; R->rev.ncols = nd;
-  R->fwd.ptr = keep_alloc<int32_t>((size_t)nd + 1, st);
-  R->rev.ptr = keep_alloc<int32_t>((size_t)ns + 1, st);
-  exclusive_scan_i32(rowcnt.p, R->fwd.ptr, nd, st);
-  exclusive_scan_i32(colcnt.p, R->rev.ptr, ns, st);
-  R->nnz = m;
-  R->fwd.nnz = R->rev.nnz = m;
-  R->fwd.idx = keep_alloc<int32_t>((size_t)m, st);
-  R->fwd.val = keep_alloc<double>((size_t)m, st);
-  R->rev.idx = keep_alloc<int32_t>((size_t)m, st);
-  R->rev.val = keep_alloc<double>((size_t)m, st);
-  rowcnt.zero();
-  colcnt.zero();
-  if (m) {
-    k_coo_scatter<<<nblk(m, 256), 256, 0, st>>>(rows, cols, vals, m, R->fwd.ptr, rowcnt.p, R->rev.ptr, colcnt.p,
-                                                R->fwd.idx, R->fwd.val, R->rev.idx, R->rev.val);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-  sort_rows(R->fwd.ptr, nd, R->fwd.idx, R->fwd.val, st);
-  sort_rows(R->rev.ptr, ns, R->rev.idx, R->rev.val, st);
-}
-
 void finish_build(crg_regridder* R, cudaStream_t st) {
   const int64_t nd = R->nd, ns = R->ns, nnz = R->nnz;
   for (DevCsr* c : {&R->fwd, &R->rev}) {

@@ -192,10 +192,6 @@ struct PairSearch {
   void search(double* dst_area, double* src_area, cudaStream_t st);
 };
 
-// Fills both CSR copies of R (an R->nd x R->ns matrix, columns ascending in
-// every row) from m distinct (row, col, val) entries in device memory.
-void assemble_coo(crg_regridder* R, int64_t m, const int32_t* rows, const int32_t* cols, const double* vals,
-                  cudaStream_t st);
 // FP32 weights, Kahan row / column sums and the merge-path layouts of both
 // directions of R (after its matrix and areas are final).
 void finish_build(crg_regridder* R, cudaStream_t st);

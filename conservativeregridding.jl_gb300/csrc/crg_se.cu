@@ -472,24 +472,26 @@ __global__ void k_se_pair_sum(const int32_t* __restrict__ toff, const int32_t* _
 
 // ------------------------------------------------------------------ L2 projection (FV -> SE)
 
-__global__ void k_pairs_per_elem(const int2* __restrict__ cand, const int32_t* __restrict__ cnt, int64_t nc,
-                                 int32_t* __restrict__ ecnt) {
+// Pairs with entries grouped by one of their cells (by_x: the dst cell, else
+// the src cell), keyed by the other; sort_rows then orders each group by that
+// key (the pair index rides along as an exactly representable double).
+__global__ void k_group_count(const int2* __restrict__ cand, const int32_t* __restrict__ cnt, int64_t nc, int by_x,
+                              int32_t* __restrict__ gcnt) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc || cnt[t] == 0) return;
-  atomicAdd(&ecnt[cand[t].x], 1);
+  atomicAdd(&gcnt[by_x ? cand[t].x : cand[t].y], 1);
 }
 
-// Pairs of each element, keyed by cell; sort_rows then orders them by cell
-// (the pair index rides along as an exactly representable double).
-__global__ void k_pairs_fill(const int2* __restrict__ cand, const int32_t* __restrict__ cnt, int64_t nc,
-                             const int32_t* __restrict__ eptr, int32_t* __restrict__ efill, int32_t* __restrict__ ecell,
-                             double* __restrict__ epair) {
+__global__ void k_group_fill(const int2* __restrict__ cand, const int32_t* __restrict__ cnt, int64_t nc, int by_x,
+                             const int32_t* __restrict__ gptr, int32_t* __restrict__ gfill, int32_t* __restrict__ key,
+                             double* __restrict__ gpair) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc || cnt[t] == 0) return;
   const int2 pr = cand[t];
-  const int32_t p = eptr[pr.x] + atomicAdd(&efill[pr.x], 1);
-  ecell[p] = pr.y;
-  epair[p] = (double)t;
+  const int32_t g = by_x ? pr.x : pr.y;
+  const int32_t p = gptr[g] + atomicAdd(&gfill[g], 1);
+  key[p] = by_x ? pr.y : pr.x;
+  gpair[p] = (double)t;
 }
 
 // One block per element (fv_to_se_l2_projection :634-679).  Shared memory:
@@ -643,22 +645,62 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-__global__ void k_se_emit(const int2* __restrict__ cand, int64_t nc, const int32_t* __restrict__ off,
-                          const int32_t* __restrict__ cnt, const double* __restrict__ vals, int nq2, int se_is_dst,
-                          int32_t* __restrict__ rows, int32_t* __restrict__ cols, double* __restrict__ out) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nc || cnt[t] == 0) return;
-  const int2 pr = cand[t];
-  const int64_t e = se_is_dst ? pr.x : pr.y;
-  const int32_t cell = se_is_dst ? pr.y : pr.x;
-  int32_t o = off[t];
+// Rows = FV cells: the cell's pairs in element order, each pair's nonzeros in
+// node order (so every row comes out sorted); o = the pair's first position.
+__global__ void k_pair_counts(const double* __restrict__ gpair, int64_t np, const int32_t* __restrict__ cnt,
+                              int32_t* __restrict__ w) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a < np) w[a] = cnt[(int64_t)gpair[a]];
+}
+
+__global__ void k_cell_ptr(const int32_t* __restrict__ gptr, int64_t ncells, const int32_t* __restrict__ poff,
+                           int32_t* __restrict__ ptr) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c <= ncells) ptr[c] = poff[gptr[c]];
+}
+
+__global__ void k_cell_rows(const double* __restrict__ gpair, const int32_t* __restrict__ gkey, int64_t np,
+                            const int32_t* __restrict__ poff, const double* __restrict__ vals, int nq2,
+                            int32_t* __restrict__ idx, double* __restrict__ val) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= np) return;
+  const int64_t pair = (int64_t)gpair[a];
+  const int64_t e = gkey[a];
+  int32_t o = poff[a];
   for (int k = 0; k < nq2; ++k) {
-    const double v = vals[t * nq2 + k];
+    const double v = vals[pair * nq2 + k];
     if (v == 0.0) continue;
-    const int32_t node = (int32_t)(e * nq2 + k);
-    rows[o] = se_is_dst ? node : cell;
-    cols[o] = se_is_dst ? cell : node;
-    out[o] = v;
+    idx[o] = (int32_t)(e * nq2 + k);
+    val[o] = v;
+    ++o;
+  }
+}
+
+// Rows = nodes (e, k): the element's pairs in cell order, entry k of each.
+__global__ void k_node_counts(const int32_t* __restrict__ eptr, const double* __restrict__ epair, int64_t nelem,
+                              const double* __restrict__ vals, int nq2, int32_t* __restrict__ ncnt) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelem * nq2) return;
+  const int64_t e = t / nq2;
+  const int k = (int)(t - e * nq2);
+  int32_t n = 0;
+  for (int32_t p = eptr[e]; p < eptr[e + 1]; ++p) n += vals[(int64_t)epair[p] * nq2 + k] != 0.0;
+  ncnt[t] = n;
+}
+
+__global__ void k_node_rows(const int32_t* __restrict__ eptr, const int32_t* __restrict__ ecell,
+                            const double* __restrict__ epair, int64_t nelem, const double* __restrict__ vals, int nq2,
+                            const int32_t* __restrict__ nptr, int32_t* __restrict__ idx, double* __restrict__ val) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelem * nq2) return;
+  const int64_t e = t / nq2;
+  const int k = (int)(t - e * nq2);
+  int32_t o = nptr[t];
+  for (int32_t p = eptr[e]; p < eptr[e + 1]; ++p) {
+    const double v = vals[(int64_t)epair[p] * nq2 + k];
+    if (v == 0.0) continue;
+    idx[o] = ecell[p];
+    val[o] = v;
     ++o;
   }
 }
@@ -760,6 +802,38 @@ void node_weights(const crg_se_space* se, const SeRule& r, const DBuf<double>& c
     k_se_nodes<<<nblk(nn, 128), 128, 0, st>>>(coef.p, nelem, r, r2, nullptr, out);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
+}
+
+// Pairs with entries grouped by their element (by_x = the element is the dst
+// cell) or by their FV cell, the other index ascending in each group.
+struct Groups {
+  DBuf<int32_t> ptr, key;
+  DBuf<double> pair;
+  int64_t n = 0;
+};
+
+void group_pairs(const PairSearch& ps, const int32_t* cnt, int64_t ngroups, bool by_x, Groups& g, cudaStream_t st) {
+  const int64_t nc = ps.nc;
+  DBuf<int32_t> gcnt((size_t)ngroups + 1, st), fill((size_t)ngroups + 1, st);
+  g.ptr.alloc((size_t)ngroups + 1, st);
+  gcnt.zero();
+  fill.zero();
+  if (nc) {
+    k_group_count<<<nblk(nc, 256), 256, 0, st>>>(ps.cand, cnt, nc, by_x, gcnt.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  exclusive_scan_i32(gcnt.p, g.ptr.p, ngroups, st);
+  int32_t np = 0;
+  CRG_CHECK_CUDA(cudaMemcpyAsync(&np, g.ptr.p + ngroups, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  g.n = np;
+  g.key.alloc((size_t)np + 1, st);
+  g.pair.alloc((size_t)np + 1, st);
+  if (nc) {
+    k_group_fill<<<nblk(nc, 256), 256, 0, st>>>(ps.cand, cnt, nc, by_x, g.ptr.p, fill.p, g.key.p, g.pair.p);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  sort_rows(g.ptr.p, ngroups, g.key.p, g.pair.p, st);
 }
 
 struct Overlaps {
@@ -866,21 +940,11 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
     const double* vals = bv.p;
     DBuf<double> pv;
     if (se_is_dst && nc) {
-      // group the overlapping pairs by element, cells ascending
-      DBuf<int32_t> ecnt((size_t)nelem + 1, st), eptr((size_t)nelem + 1, st), efill((size_t)nelem + 1, st);
-      ecnt.zero();
-      efill.zero();
-      k_pairs_per_elem<<<nblk(nc, 256), 256, 0, st>>>(ps.cand, cnt.p, nc, ecnt.p);
-      CRG_CHECK_CUDA(cudaGetLastError());
-      exclusive_scan_i32(ecnt.p, eptr.p, nelem, st);
-      int32_t np = 0;
-      CRG_CHECK_CUDA(cudaMemcpyAsync(&np, eptr.p + nelem, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-      CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-      DBuf<int32_t> ecell((size_t)np + 1, st);
-      DBuf<double> epair((size_t)np + 1, st);
-      k_pairs_fill<<<nblk(nc, 256), 256, 0, st>>>(ps.cand, cnt.p, nc, eptr.p, efill.p, ecell.p, epair.p);
-      CRG_CHECK_CUDA(cudaGetLastError());
-      sort_rows(eptr.p, nelem, ecell.p, epair.p, st);
+      // the overlapping pairs grouped by element, cells ascending
+      Groups eg;
+      group_pairs(ps, cnt.p, nelem, true, eg, st);
+      const int32_t* eptr_p = eg.ptr.p;
+      const double* epair_p = eg.pair.p;
       const SeMass mass = make_mass(rule);
       pv.alloc((size_t)nc * nq2 + 1, st);
       CRG_CHECK_CUDA(cudaMemsetAsync(pv.p, 0, sizeof(double) * nc * nq2, st));
@@ -890,7 +954,7 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
       DBuf<int> singular(1, st);
       singular.zero();
       if (nelem) {
-        k_se_project<<<(unsigned)nelem, 128, smem, st>>>(eptr.p, epair.p, wj.p, rule, mass, bv.p, pv.p, cnt.p,
+        k_se_project<<<(unsigned)nelem, 128, smem, st>>>(eptr_p, epair_p, wj.p, rule, mass, bv.p, pv.p, cnt.p,
                                                          singular.p);
         CRG_CHECK_CUDA(cudaGetLastError());
       }
@@ -902,22 +966,50 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
     }
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[2], st));
 
-    // COO entries in pair order, then both CSR copies
-    DBuf<int32_t> off((size_t)nc + 1, st);
-    exclusive_scan_i32(cnt.p, off.p, nc, st);
-    int32_t m = 0;
-    if (nc) {
-      CRG_CHECK_CUDA(cudaMemcpyAsync(&m, off.p + nc, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-      CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-    }
-    DBuf<int32_t> rows((size_t)m + 1, st), cols((size_t)m + 1, st);
-    DBuf<double> ent((size_t)m + 1, st);
-    if (nc) {
-      k_se_emit<<<nblk(nc, 256), 256, 0, st>>>(ps.cand, nc, off.p, cnt.p, vals, nq2, se_is_dst, rows.p, cols.p,
-                                               ent.p);
+    // Both CSR copies written in order: rows = FV cells from the pairs grouped
+    // by cell (elements ascending), rows = nodes from the pairs grouped by
+    // element (cells ascending).
+    Groups cg, eg2;
+    group_pairs(ps, cnt.p, nfv, !se_is_dst, cg, st);
+    group_pairs(ps, cnt.p, nelem, se_is_dst, eg2, st);
+    DBuf<int32_t> w((size_t)cg.n + 1, st), poff((size_t)cg.n + 1, st);
+    if (cg.n) {
+      k_pair_counts<<<nblk(cg.n, 256), 256, 0, st>>>(cg.pair.p, cg.n, cnt.p, w.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
-    assemble_coo(R, m, rows.p, cols.p, ent.p, st);
+    exclusive_scan_i32(w.p, poff.p, cg.n, st);
+    int32_t m = 0;
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&m, poff.p + cg.n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    DevCsr& crows = se_is_dst ? R->rev : R->fwd;  // rows = FV cells
+    DevCsr& nrows = se_is_dst ? R->fwd : R->rev;  // rows = nodes
+    crows.nrows = nfv; crows.ncols = nn;
+    nrows.nrows = nn; nrows.ncols = nfv;
+    R->nnz = m;
+    crows.nnz = nrows.nnz = m;
+    crows.ptr = keep_alloc<int32_t>((size_t)nfv + 1, st);
+    nrows.ptr = keep_alloc<int32_t>((size_t)nn + 1, st);
+    for (DevCsr* c : {&crows, &nrows}) {
+      c->idx = keep_alloc<int32_t>((size_t)m, st);
+      c->val = keep_alloc<double>((size_t)m, st);
+    }
+    k_cell_ptr<<<nblk(nfv + 1, 256), 256, 0, st>>>(cg.ptr.p, nfv, poff.p, crows.ptr);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    if (cg.n) {
+      k_cell_rows<<<nblk(cg.n, 256), 256, 0, st>>>(cg.pair.p, cg.key.p, cg.n, poff.p, vals, nq2, crows.idx, crows.val);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    DBuf<int32_t> ncnt((size_t)nn + 1, st);
+    if (nn) {
+      k_node_counts<<<nblk(nn, 256), 256, 0, st>>>(eg2.ptr.p, eg2.pair.p, nelem, vals, nq2, ncnt.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    exclusive_scan_i32(ncnt.p, nrows.ptr, nn, st);
+    if (nn) {
+      k_node_rows<<<nblk(nn, 256), 256, 0, st>>>(eg2.ptr.p, eg2.key.p, eg2.pair.p, nelem, vals, nq2, nrows.ptr,
+                                                 nrows.idx, nrows.val);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
     // areas: FV cells (scaled to the radius), node weights or ones
     if (r2 != 1.0 && nfv) {
       k_scale<<<nblk(nfv, 256), 256, 0, st>>>(fv_area, nfv, r2);
