@@ -222,18 +222,26 @@ __device__ __forceinline__ d3 isect_sph(d3 a, double sa, d3 b, double sb) {
   return x;
 }
 
-// Signed solid angle of polygon v[0..m) (fan from v[0]).
+// Signed solid angle of polygon v[0..m) (fan from v[0]).  Consecutive fan
+// triangles share c - a and a.c (the next triangle's b - a and a.b): each is
+// computed once, with the values triple() and ddot() give.
 __device__ __forceinline__ double area_sph_signed(const d3* v, int m) {
   if (m < 3) return 0.0;
   double re = 1.0, im = 0.0;
-  d3 a = v[0];
+  const d3 a = v[0];
+  d3 db = dsub(v[1], a);
+  double ab = ddot(a, v[1]);
   for (int k = 1; k + 1 < m; ++k) {
-    d3 b = v[k], c = v[k + 1];
-    double N = triple(a, b, c);
-    double D = ((1.0 + ddot(a, b)) + ddot(b, c)) + ddot(c, a);
-    double re2 = fma(re, D, -(im * N));
-    double im2 = fma(re, N, im * D);
+    const d3 b = v[k], c = v[k + 1];
+    const d3 dc = dsub(c, a);
+    const double N = ddot(a, dcross(db, dc));
+    const double ac = ddot(c, a);
+    const double D = ((1.0 + ab) + ddot(b, c)) + ac;
+    const double re2 = fma(re, D, -(im * N));
+    const double im2 = fma(re, N, im * D);
     re = re2; im = im2;
+    db = dc;
+    ab = ac;  // ddot(a, c) == ddot(c, a): the products commute exactly
   }
   return 2.0 * atan2_crg(im, re);
 }
@@ -242,15 +250,21 @@ __device__ __forceinline__ double area_sph_signed(const d3* v, int m) {
 // fan (the triple products are shared; the values are the same).
 __device__ __forceinline__ double area_orient_sph(const d3* v, int m, double& ori) {
   double re = 1.0, im = 0.0, s = 0.0;
-  d3 a = v[0];
+  const d3 a = v[0];
+  d3 db = m > 1 ? dsub(v[1], a) : d3{0.0, 0.0, 0.0};
+  double ab = m > 1 ? ddot(a, v[1]) : 0.0;
   for (int k = 1; k + 1 < m; ++k) {
-    d3 b = v[k], c = v[k + 1];
-    double N = triple(a, b, c);
+    const d3 b = v[k], c = v[k + 1];
+    const d3 dc = dsub(c, a);
+    const double N = ddot(a, dcross(db, dc));
     s = s + N;
-    double D = ((1.0 + ddot(a, b)) + ddot(b, c)) + ddot(c, a);
-    double re2 = fma(re, D, -(im * N));
-    double im2 = fma(re, N, im * D);
+    const double ac = ddot(c, a);
+    const double D = ((1.0 + ab) + ddot(b, c)) + ac;
+    const double re2 = fma(re, D, -(im * N));
+    const double im2 = fma(re, N, im * D);
     re = re2; im = im2;
+    db = dc;
+    ab = ac;
   }
   ori = s >= 0.0 ? 1.0 : -1.0;
   return m < 3 ? 0.0 : 2.0 * atan2_crg(im, re);
@@ -378,9 +392,13 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
       n = 0;
       break;
     }
+    // FP64 side values where the crossing points need them.  A vertex the FP32
+    // test decided is at least 0.8 B from the plane, far outside the FP64
+    // bound, where side_sph returns the plain value n.(v - ca): that is taken
+    // directly.
     auto side = [&](int i) -> double {
       if (!((known >> i) & 1u)) {
-        sv[i] = kSpherical ? side_sph(nrm, ca, cb, eb, isig, in[i]) : side_pl(ca, cb, ex, ey, isig, in[i]);
+        sv[i] = kSpherical ? ddot(nrm, dsub(in[i], ca)) : side_pl(ca, cb, ex, ey, isig, in[i]);
         known |= 1u << i;
       }
       return sv[i];
