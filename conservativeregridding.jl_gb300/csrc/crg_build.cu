@@ -49,8 +49,17 @@ struct BlockInfo {
   int64_t nx[kMaxBlocks];
 };
 
+// The expand kernels write each cell's vertices in FP64 and, rounded to
+// nearest, in FP32 (the screening tests read those, converting nothing per pair).
+__device__ __forceinline__ void put_vertex(double* o, float4* o4, double x, double y, double z) {
+  o[0] = x;
+  o[1] = y;
+  o[2] = z;
+  *o4 = make_float4((float)x, (float)y, (float)z, 0.f);
+}
+
 __global__ void k_expand_curvi(const double* __restrict__ pts, BlockInfo bi, int64_t ncells, double* __restrict__ v,
-                               int8_t* __restrict__ nv) {
+                               float4* __restrict__ v4, int8_t* __restrict__ nv) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   int b = 0;
@@ -61,17 +70,14 @@ __global__ void k_expand_curvi(const double* __restrict__ pts, BlockInfo bi, int
   int64_t p[4] = {i + j * (nx + 1), (i + 1) + j * (nx + 1), (i + 1) + (j + 1) * (nx + 1), i + (j + 1) * (nx + 1)};
   for (int k = 0; k < 4; ++k) {
     const double* q = pts + (bi.point_off[b] + p[k]) * bi.dim;
-    double* o = v + (c * 4 + k) * 3;
-    o[0] = q[0];
-    o[1] = q[1];
-    o[2] = bi.dim == 3 ? q[2] : 0.0;
+    put_vertex(v + (c * 4 + k) * 3, v4 + c * 4 + k, q[0], q[1], bi.dim == 3 ? q[2] : 0.0);
   }
   nv[c] = 4;
 }
 
 __global__ void k_expand_cells(const double* __restrict__ cv, const int32_t* __restrict__ cn, int maxv, int dim,
-                               int64_t ncells, double* __restrict__ v, int8_t* __restrict__ nv,
-                               int32_t* __restrict__ bad) {
+                               int64_t ncells, double* __restrict__ v, float4* __restrict__ v4,
+                               int8_t* __restrict__ nv, int32_t* __restrict__ bad) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   int n = cn ? cn[c] : maxv;
@@ -82,10 +88,7 @@ __global__ void k_expand_cells(const double* __restrict__ cv, const int32_t* __r
   }
   for (int k = 0; k < maxv; ++k) {
     const double* q = cv + (c * maxv + k) * dim;
-    double* o = v + (c * maxv + k) * 3;
-    o[0] = q[0];
-    o[1] = q[1];
-    o[2] = dim == 3 ? q[2] : 0.0;
+    put_vertex(v + (c * maxv + k) * 3, v4 + c * maxv + k, q[0], q[1], dim == 3 ? q[2] : 0.0);
   }
   nv[c] = (int8_t)n;
 }
@@ -109,34 +112,41 @@ __device__ __forceinline__ uint32_t spread_bits16(uint32_t x) {
   return x;
 }
 
-__device__ __forceinline__ uint32_t q14(double u) {  // u in [-1, 1]
-  double t = (u + 1.0) * 8191.5;
-  t = t < 0.0 ? 0.0 : (t > 16383.0 ? 16383.0 : t);
+__device__ __forceinline__ uint32_t q14(float u) {  // u in [-1, 1]
+  float t = (u + 1.0f) * 8191.5f;
+  t = t < 0.0f ? 0.0f : (t > 16383.0f ? 16383.0f : t);
   return (uint32_t)t;
 }
 
-// Cube-face Morton key of a unit vector: face (3 bits) | 2 x 14 bits.
-__device__ __forceinline__ uint32_t sphere_key(double x, double y, double z) {
-  double ax = fabs(x), ay = fabs(y), az = fabs(z);
+// Cube-face Morton key of a direction: face (3 bits) | 2 x 14 bits.  Any
+// deterministic key serves (it only orders the cells of the hierarchy), so it
+// is computed in FP32.
+__device__ __forceinline__ uint32_t sphere_key(float x, float y, float z) {
+  float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
   uint32_t face;
-  double u, v, m;
+  float u, v, m;
   if (ax >= ay && ax >= az) { face = x >= 0 ? 0 : 1; m = ax; u = y; v = z; }
   else if (ay >= az) { face = y >= 0 ? 2 : 3; m = ay; u = x; v = z; }
   else { face = z >= 0 ? 4 : 5; m = az; u = x; v = y; }
-  if (!(m > 0.0)) return 0;
+  if (!(m > 0.0f)) return 0;
   u /= m; v /= m;
   return (face << 28) | spread_bits14(q14(u)) | (spread_bits14(q14(v)) << 1);
 }
 
 // Per-cell exact area, bounding volume and (spherical) order key.
-// Spherical bounds: a ball in R^3 around the unit centre c = normalize(sum v)
-// with chord radius rho = max |c - v_k|; the cell (great-circle edges) lies in
-// the spherical cap that ball cuts out whenever rho < sqrt(2), and rho = 2 is
-// used otherwise.  Planar bounds: the box of the vertices.  Both are rounded
-// outward to float and inflated so that the float tests are a superset of the
-// exact ones.
+// Spherical bounds: a ball in R^3 around c = normalize(sum v) with chord
+// radius rho = max |c - v_k|; the cell (great-circle edges) lies in the
+// spherical cap that ball cuts out whenever rho < sqrt(2), and rho = 2 is used
+// otherwise.  The ball is computed in FP32 from the FP32-rounded vertices q_k
+// (GB300's FP64 rate is a small fraction of its FP32 rate; only the area needs
+// FP64): c is stored as computed, |v_k - q_k| <= 2^-24, and the FP32 distance
+// |c - q_k| is within 2^-21 of its value relative, so rho (1 + 4e-6) + 4e-6,
+// rounded up, bounds every |c - v_k|.  Planar bounds: the box of the FP64
+// vertices rounded outward.  The float tests on these bounds are therefore a
+// superset of the exact ones.
 template <bool kSph>
-__global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restrict__ nv, int maxv, int64_t ncells,
+__global__ void k_cell_geom(const double* __restrict__ v, const float4* __restrict__ v4,
+                            const int8_t* __restrict__ nv, int maxv, int64_t ncells,
                             double* __restrict__ area, float4* __restrict__ bound, uint32_t* __restrict__ key,
                             int8_t* __restrict__ ori) {
   int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -162,27 +172,28 @@ __global__ void k_cell_geom(const double* __restrict__ v, const int8_t* __restri
   ori[c] = (int8_t)(o > 0.0 ? 1 : -1);
   if (n == 0) {  // a ghost slot: a bound that overlaps nothing (negative radius / inverted box)
     bound[c] = kSph ? make_float4(0.f, 0.f, 1.f, -4.f) : make_float4(INFINITY, INFINITY, -INFINITY, -INFINITY);
-    if (kSph) key[c] = sphere_key(0.0, 0.0, 1.0);
+    if (kSph) key[c] = sphere_key(0.f, 0.f, 1.f);
     return;
   }
   if (kSph) {
-    double sx = 0, sy = 0, sz = 0;
-    for (int k = 0; k < n; ++k) { sx += p[k].x; sy += p[k].y; sz += p[k].z; }
-    double nr = sqrt(sx * sx + sy * sy + sz * sz);
-    double cx = 0, cy = 0, cz = 1;
-    if (nr > 0) {
-      const double inr = 1.0 / nr;
+    const float4* q = v4 + c * maxv;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for (int k = 0; k < n; ++k) { sx += q[k].x; sy += q[k].y; sz += q[k].z; }
+    const float nr = sqrtf(sx * sx + sy * sy + sz * sz);
+    float cx = 0.f, cy = 0.f, cz = 1.f;
+    if (nr > 0.f) {
+      const float inr = 1.0f / nr;
       cx = sx * inr; cy = sy * inr; cz = sz * inr;
     }
-    double rho2 = 0;
+    float rho2 = 0.f;
     for (int k = 0; k < n; ++k) {
-      double dx = p[k].x - cx, dy = p[k].y - cy, dz = p[k].z - cz;
-      rho2 = fmax(rho2, dx * dx + dy * dy + dz * dz);
+      const float dx = q[k].x - cx, dy = q[k].y - cy, dz = q[k].z - cz;
+      rho2 = fmaxf(rho2, dx * dx + dy * dy + dz * dz);
     }
-    double rho = sqrt(rho2);
-    if (!(rho < 1.4) || !(nr > 0)) rho = 2.0;
-    float rf = __double2float_ru(rho * (1.0 + 4e-6) + 4e-6);
-    bound[c] = make_float4((float)cx, (float)cy, (float)cz, rf);
+    float rho = sqrtf(rho2);
+    if (!(rho < 1.4f) || !(nr > 0.f)) rho = 2.f;
+    const float rf = __fadd_ru(__fmul_ru(rho, 1.000004f), 4e-6f);
+    bound[c] = make_float4(cx, cy, cz, rf);
     key[c] = sphere_key(cx, cy, cz);
   } else {
     double x0 = p[0].x, x1 = p[0].x, y0 = p[0].y, y1 = p[0].y;
@@ -536,9 +547,9 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 constexpr int kClasses = 256;  // cut masks of up to 8 edges; class kClasses = dropped
 
 __global__ void __launch_bounds__(256)
-    k_separated(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
-                const int8_t* __restrict__ dnv, int dmaxv, const double* __restrict__ sv,
-                const int8_t* __restrict__ snv, int smaxv, const double4_32a* __restrict__ planes,
+    k_separated(const int2* __restrict__ cand, int64_t nc, const float4* __restrict__ dv4,
+                const int8_t* __restrict__ dnv, int dmaxv, const float4* __restrict__ sv4,
+                const int8_t* __restrict__ snv, int smaxv, const float4* __restrict__ planes32,
                 uint16_t* __restrict__ cls) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
@@ -548,21 +559,19 @@ __global__ void __launch_bounds__(256)
     cls[t] = kClasses;
     return;
   }
-  float3 v[CRG_MAXV];
-  const double* q = sv + (int64_t)pr.y * smaxv * 3;
-  for (int i = 0; i < ns; ++i) v[i] = make_float3((float)q[3 * i], (float)q[3 * i + 1], (float)q[3 * i + 2]);
-  const double* c = dv + (int64_t)pr.x * dmaxv * 3;
+  float4 v[CRG_MAXV];
+  const float4* q = sv4 + (int64_t)pr.y * smaxv;
+  for (int i = 0; i < ns; ++i) v[i] = q[i];
+  const float4* c = dv4 + (int64_t)pr.x * dmaxv;
+  const float4* pl = planes32 + (int64_t)pr.x * dmaxv;
   int sep = 0, mask = 0;
   for (int k = 0; k < nd && !sep; ++k) {
-    const double4_32a p = planes[(int64_t)pr.x * dmaxv + k];
-    const float nx = (float)p.x, ny = (float)p.y, nz = (float)p.z;
-    const float ax = (float)c[3 * k], ay = (float)c[3 * k + 1], az = (float)c[3 * k + 2];
-    const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+    const float4 p = pl[k], a = c[k];  // n32 (w = |n32|_1) and ca32
     int out = 1, in = 1;
     for (int i = 0; i < ns; ++i) {
-      const float wx = v[i].x - ax, wy = v[i].y - ay, wz = v[i].z - az;
-      const float s = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
-      const float B = 3.814697265625e-06f * n1 * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
+      const float wx = v[i].x - a.x, wy = v[i].y - a.y, wz = v[i].z - a.z;
+      const float s = fmaf(p.x, wx, fmaf(p.y, wy, p.z * wz));
+      const float B = 3.814697265625e-06f * p.w * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
       out &= s < -B;
       in &= s > B;
     }
@@ -602,7 +611,8 @@ __global__ void __launch_bounds__(256)
 }
 
 __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __restrict__ nv,
-                              const int8_t* __restrict__ ori, int maxv, int64_t ncells, double4_32a* __restrict__ planes) {
+                              const int8_t* __restrict__ ori, int maxv, int64_t ncells, double4_32a* __restrict__ planes,
+                              float4* __restrict__ planes32) {
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   const int n = nv[c];
@@ -614,6 +624,8 @@ __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __rest
     edge_plane(d3{q[3 * k], q[3 * k + 1], q[3 * k + 2]}, d3{q[3 * k1], q[3 * k1 + 1], q[3 * k1 + 2]}, (double)ori[c],
                nrm, eb);
     planes[c * maxv + k] = make_double4_32a(nrm.x, nrm.y, nrm.z, eb);
+    const float nx = (float)nrm.x, ny = (float)nrm.y, nz = (float)nrm.z;
+    planes32[c * maxv + k] = make_float4(nx, ny, nz, fabsf(nx) + fabsf(ny) + fabsf(nz));
   }
 }
 
@@ -625,7 +637,9 @@ __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int
                                               int smaxv, double* __restrict__ area,
                                               int32_t* __restrict__ rowcnt, int32_t* __restrict__ colcnt,
                                               unsigned long long* __restrict__ overflow,
-                                              const double4_32a* __restrict__ dplanes) {
+                                              const double4_32a* __restrict__ dplanes,
+                                              const float4* __restrict__ dplanes32, const float4* __restrict__ dv4,
+                                              const float4* __restrict__ sv4) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
   int2 pr = cand[t];
@@ -640,8 +654,16 @@ __global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int
   double a = 0.0;
   if (nd >= 3 && ns >= 3) {
     d3* res;
+    float4 fa[kSph ? CRG_MAXC : 1], fb[kSph ? CRG_MAXC : 1];
+    Screen32 s32{nullptr, nullptr, fa, fb};
+    if (kSph) {
+      s32.planes = dplanes32 + (int64_t)pr.x * dmaxv;
+      s32.clip = dv4 + (int64_t)pr.x * dmaxv;
+      const float4* q4 = sv4 + (int64_t)pr.y * smaxv;
+      for (int k = 0; k < ns; ++k) fa[k] = q4[k];
+    }
     int m = clip_polygon_oriented<kSph>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res,
-                                        kSph ? dplanes + (int64_t)pr.x * dmaxv : nullptr);
+                                        kSph ? dplanes + (int64_t)pr.x * dmaxv : nullptr, kSph ? &s32 : nullptr);
     if (m < 0) {
       atomicAdd(overflow, 1ull);
     } else {
@@ -887,6 +909,7 @@ __global__ void k_row_sums(const int32_t* __restrict__ ptr, const double* __rest
 struct DevGrid {
   CellTable tab;
   DBuf<double> v;
+  DBuf<float4> v4;
   DBuf<int8_t> nv;
   DBuf<int8_t> ori;
   int64_t ncells = 0;
@@ -930,9 +953,10 @@ void upload_grid(const crg_grid_desc* g, DevGrid& out, cudaStream_t st) {
     out.tab.n = cells;
     out.tab.maxv = 4;
     out.v.alloc((size_t)cells * 4 * 3, st);
+    out.v4.alloc((size_t)cells * 4, st);
     out.nv.alloc((size_t)cells, st);
     if (cells) {
-      k_expand_curvi<<<nblk(cells, 256), 256, 0, st>>>(dpts, bi, cells, out.v.p, out.nv.p);
+      k_expand_curvi<<<nblk(cells, 256), 256, 0, st>>>(dpts, bi, cells, out.v.p, out.v4.p, out.nv.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
   } else if (g->kind == CRG_GRID_CELLS) {
@@ -957,11 +981,12 @@ void upload_grid(const crg_grid_desc* g, DevGrid& out, cudaStream_t st) {
     out.tab.n = n;
     out.tab.maxv = (int)mv;
     out.v.alloc((size_t)n * mv * 3, st);
+    out.v4.alloc((size_t)n * mv, st);
     out.nv.alloc((size_t)n, st);
     DBuf<int32_t> bad(1, st);
     bad.zero();
     if (n) {
-      k_expand_cells<<<nblk(n, 256), 256, 0, st>>>(dcv, dcn, (int)mv, dim, n, out.v.p, out.nv.p, bad.p);
+      k_expand_cells<<<nblk(n, 256), 256, 0, st>>>(dcv, dcn, (int)mv, dim, n, out.v.p, out.v4.p, out.nv.p, bad.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     int32_t hbad = 0;
@@ -973,6 +998,7 @@ void upload_grid(const crg_grid_desc* g, DevGrid& out, cudaStream_t st) {
     CRG_REQUIRE(false, CRG_ERR_INVALID_ARGUMENT, "unknown grid kind %d", g->kind);
   }
   out.tab.v = out.v.p;
+  out.tab.v4 = out.v4.p;
   out.tab.nv = out.nv.p;
   out.ori.alloc((size_t)out.tab.n, st);  // filled with the cell geometry
   out.tab.ori = out.ori.p;
@@ -993,12 +1019,12 @@ void build_tree(const DevGrid& g, bool sph, double* area_out, HostTree& h, cudaS
   h.key.alloc((size_t)n, st);
   if (n == 0) return;
   if (sph) {
-    k_cell_geom<true><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p,
-                                                     g.tab.ori);
+    k_cell_geom<true><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.v4, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p,
+                                                     h.key.p, g.tab.ori);
     CRG_CHECK_CUDA(cudaGetLastError());
   } else {
-    k_cell_geom<false><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.nv, g.tab.maxv, n, area_out, h.bound.p, h.key.p,
-                                                      g.tab.ori);
+    k_cell_geom<false><<<nblk(n, 128), 128, 0, st>>>(g.tab.v, g.tab.v4, g.tab.nv, g.tab.maxv, n, area_out,
+                                                      h.bound.p, h.key.p, g.tab.ori);
     CRG_CHECK_CUDA(cudaGetLastError());
     int64_t nb = nblk(n, 256);
     DBuf<float4> part((size_t)nb, st);
@@ -1289,6 +1315,7 @@ struct PairSearch::Impl {
   HostTree td, ts;
   DBuf<int2> cand, kept;
   DBuf<double4_32a> planes;
+  DBuf<float4> planes32;
 };
 
 PairSearch::PairSearch() : impl(new Impl) {}
@@ -1316,16 +1343,19 @@ void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
   cand = impl->cand.p;
   if (sph && nc && nd) {
     impl->planes.alloc((size_t)nd * dtab.maxv, st);
-    k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(dtab.v, dtab.nv, dtab.ori, dtab.maxv, nd, impl->planes.p);
+    impl->planes32.alloc((size_t)nd * dtab.maxv, st);
+    k_edge_planes<<<nblk(nd, 128), 128, 0, st>>>(dtab.v, dtab.nv, dtab.ori, dtab.maxv, nd, impl->planes.p,
+                                                 impl->planes32.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     dplanes = impl->planes.p;
+    dplanes32 = impl->planes32.p;
     // drop the pairs separated by a destination edge, group the rest by class
     DBuf<int32_t> cnt(kClasses + 1, st), off(kClasses + 1, st), fill(kClasses + 1, st);
     DBuf<uint16_t> cls((size_t)nc + 1, st);
     cnt.zero();
     fill.zero();
-    k_separated<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, dtab.v, dtab.nv, dtab.maxv, stab.v, stab.nv, stab.maxv,
-                                               dplanes, cls.p);
+    k_separated<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, dtab.v4, dtab.nv, dtab.maxv, stab.v4, stab.nv, stab.maxv,
+                                               dplanes32, cls.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     k_class_count<<<nblk(nc, 256), 256, 0, st>>>(cls.p, nc, cnt.p);
     CRG_CHECK_CUDA(cudaGetLastError());
@@ -1411,10 +1441,12 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
       const CellTable &D = ps.dtab, &S = ps.stab;
       if (sph)
         k_clip<true><<<nblk(nc, 128), 128, 0, st>>>(ps.cand, nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori, S.maxv,
-                                                    area.p, rowcnt.p, colcnt.p, ovf.p, ps.dplanes);
+                                                    area.p, rowcnt.p, colcnt.p, ovf.p, ps.dplanes, ps.dplanes32,
+                                                    D.v4, S.v4);
       else
         k_clip<false><<<nblk(nc, 128), 128, 0, st>>>(ps.cand, nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori, S.maxv,
-                                                     area.p, rowcnt.p, colcnt.p, ovf.p, nullptr);
+                                                     area.p, rowcnt.p, colcnt.p, ovf.p, nullptr, nullptr, nullptr,
+                                                     nullptr);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[2], st));

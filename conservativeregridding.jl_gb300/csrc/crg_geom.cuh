@@ -322,13 +322,29 @@ __device__ __forceinline__ void edge_plane(d3 ca, d3 cb, double sig, d3& nrm, do
   eb = kU32 * (fabs(ca.x) + fabs(ca.y) + fabs(ca.z)) * (fabs(d1.x) + fabs(d1.y) + fabs(d1.z));
 }
 
+// FP32 inputs of the side screening, rounded once instead of per test: the
+// clip edges' normals (w = |n32|_1) and start vertices, and the subject
+// polygon beside its FP64 copy (a and b ping-pong with bufA and bufB; a holds
+// the subject's vertices on entry).  Every value equals the rounding of the
+// FP64 value it stands for, so the decisions are those of converting in place.
+struct Screen32 {
+  const float4* planes;
+  const float4* clip;
+  float4* a;
+  float4* b;
+};
+
 // `planes`, when given (spherical only), holds edge_plane of every clip edge
-// (x, y, z = n, w = eb), computed once per clip polygon.
+// (x, y, z = n, w = eb), computed once per clip polygon; `s32`, when given
+// (spherical only), the FP32 screening inputs.
 template <bool kSpherical>
 __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, double sig,
-                                                     d3** res, const double4_32a* planes = nullptr) {
+                                                     d3** res, const double4_32a* planes = nullptr,
+                                                     const Screen32* s32 = nullptr) {
   d3* in = bufA;
   d3* out = bufB;
+  float4* in32 = s32 ? s32->a : nullptr;
+  float4* out32 = s32 ? s32->b : nullptr;
   int n = ns;
   for (int k = 0; k < nc && n > 0; ++k) {
     d3 ca = clip[k], cb = clip[k + 1 == nc ? 0 : k + 1];
@@ -364,11 +380,25 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
     double sv[CRG_MAXC];
     uint32_t inside = 0u, known = 0u;  // bit i: vertex i inside; sv[i] computed
     if (kSpherical) {
-      const float nx = (float)nrm.x, ny = (float)nrm.y, nz = (float)nrm.z;
-      const float ax = (float)ca.x, ay = (float)ca.y, az = (float)ca.z;
-      const float n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+      float nx, ny, nz, n1, ax, ay, az;
+      if (s32) {
+        const float4 p = s32->planes[k], c = s32->clip[k];
+        nx = p.x; ny = p.y; nz = p.z; n1 = p.w;
+        ax = c.x; ay = c.y; az = c.z;
+      } else {
+        nx = (float)nrm.x; ny = (float)nrm.y; nz = (float)nrm.z;
+        ax = (float)ca.x; ay = (float)ca.y; az = (float)ca.z;
+        n1 = fabsf(nx) + fabsf(ny) + fabsf(nz);
+      }
       for (int i = 0; i < n; ++i) {
-        const float wx = (float)in[i].x - ax, wy = (float)in[i].y - ay, wz = (float)in[i].z - az;
+        float vx, vy, vz;
+        if (s32) {
+          const float4 u = in32[i];
+          vx = u.x; vy = u.y; vz = u.z;
+        } else {
+          vx = (float)in[i].x; vy = (float)in[i].y; vz = (float)in[i].z;
+        }
+        const float wx = vx - ax, wy = vy - ay, wz = vz - az;
         const float s32 = fmaf(nx, wx, fmaf(ny, wy, nz * wz));
         const float B = 3.814697265625e-06f * n1 * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
         if (s32 > B) {
@@ -427,6 +457,7 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
       if (ci == pi) {
         if (ci) {
           if (m >= CRG_MAXC) return -1;
+          if (s32) out32[m] = in32[i];
           out[m++] = in[i];
         }
         continue;
@@ -440,13 +471,16 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
         x = kSpherical ? isect_sph(in[p], sp, in[i], sc) : isect_pl(in[p], sp, in[i], sc);
       }
       if (m >= CRG_MAXC) return -1;
+      if (s32) out32[m] = make_float4((float)x.x, (float)x.y, (float)x.z, 0.f);
       out[m++] = x;
       if (ci) {
         if (m >= CRG_MAXC) return -1;
+        if (s32) out32[m] = in32[i];
         out[m++] = in[i];
       }
     }
     d3* t = in; in = out; out = t;
+    float4* t32 = in32; in32 = out32; out32 = t32;
     n = m;
   }
   *res = in;

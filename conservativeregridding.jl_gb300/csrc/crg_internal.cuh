@@ -71,6 +71,7 @@ struct CellTable {
   int64_t n = 0;
   int maxv = 0;
   double* v = nullptr;   // [n * maxv * 3]
+  float4* v4 = nullptr;  // [n * maxv] the same vertices rounded to FP32 (w = 0)
   int8_t* nv = nullptr;  // [n]
   int8_t* ori = nullptr;  // [n] +1 counter-clockwise seen from outside (or from +z), -1 clockwise
 };
@@ -183,6 +184,7 @@ struct PairSearch {
   CellTable dtab, stab;
   const int2* cand = nullptr;              // [nc] pairs that may overlap
   const double4_32a* dplanes = nullptr;    // spherical: [nd * dtab.maxv]
+  const float4* dplanes32 = nullptr;       // spherical: the normals rounded to FP32, w = |n32|_1
   PairSearch();
   ~PairSearch();
   PairSearch(const PairSearch&) = delete;

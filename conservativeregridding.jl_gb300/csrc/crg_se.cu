@@ -342,7 +342,8 @@ __global__ void __launch_bounds__(128)
     k_se_overlap(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
                  const int8_t* __restrict__ dnv, const int8_t* __restrict__ dori, int dmaxv,
                  const double* __restrict__ sv, const int8_t* __restrict__ snv, const int8_t* __restrict__ sori,
-                 int smaxv, const double4_32a* __restrict__ dplanes, double r2, double* __restrict__ poly,
+                 int smaxv, const double4_32a* __restrict__ dplanes, const float4* __restrict__ dplanes32,
+                 const float4* __restrict__ dv4, const float4* __restrict__ sv4, double r2, double* __restrict__ poly,
                  double* __restrict__ cen_out, double* __restrict__ tarea, int32_t* __restrict__ nvert,
                  int32_t* __restrict__ tcount, unsigned long long* __restrict__ overflow) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -359,8 +360,12 @@ __global__ void __launch_bounds__(128)
   int m = 0;
   d3* res = bufA;
   if (nd >= 3 && ns >= 3) {
+    float4 fa[CRG_MAXC], fb[CRG_MAXC];
+    const float4* q4 = sv4 + (int64_t)pr.y * smaxv;
+    for (int k = 0; k < ns; ++k) fa[k] = q4[k];
+    const Screen32 s32{dplanes32 + (int64_t)pr.x * dmaxv, dv4 + (int64_t)pr.x * dmaxv, fa, fb};
     m = clip_polygon_oriented<true>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res,
-                                    dplanes + (int64_t)pr.x * dmaxv);
+                                    dplanes + (int64_t)pr.x * dmaxv, &s32);
     if (m < 0) {
       atomicAdd(overflow, 1ull);
       m = 0;
@@ -908,7 +913,8 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
       // per pair: the clipped polygon (CRG_MAXC vertex slots), its centroid and fan-triangle areas
       DBuf<double> poly((size_t)nc * 3 * CRG_MAXC, st), cen((size_t)nc * 3, st), tarea((size_t)nc * CRG_MAXC, st);
       k_se_overlap<<<nblk(nc, 128), 128, 0, st>>>(ps.cand, nc, D.v, D.nv, D.ori, D.maxv, S.v, S.nv, S.ori, S.maxv,
-                                                  ps.dplanes, r2, poly.p, cen.p, tarea.p, nvert.p, tcount.p, ovf.p);
+                                                  ps.dplanes, ps.dplanes32, D.v4, S.v4, r2, poly.p, cen.p, tarea.p,
+                                                  nvert.p, tcount.p, ovf.p);
       CRG_CHECK_CUDA(cudaGetLastError());
       exclusive_scan_i32(tcount.p, toff.p, nc, st);
       unsigned long long hovf = 0;
