@@ -101,6 +101,7 @@ void export_esmf(const crg_regridder* r, int32_t base, int64_t* row, int64_t* co
   double* dS = reinterpret_cast<double*>(dcol + nnz);
   double* dfa = dS + nnz;
   double* dfb = dfa + na;
+  ensure_row_col_sums(r);
   if (na) k_esmf_entries<<<(unsigned)((na + 255) / 256), 256>>>(r->rev.ptr, r->rev.idx, r->rev.val, na, r->dst_area,
                                                                 base, drow, dcol, dS);
   if (na) k_ratio<<<(unsigned)((na + 255) / 256), 256>>>(r->col_sum, r->src_area, na, dfa);
@@ -232,6 +233,7 @@ crg_status crg_get_areas(const crg_regridder* r, double* dst_areas, double* src_
 crg_status crg_get_row_col_sums(const crg_regridder* r, double* row_sums, double* col_sums) {
   return guarded([&] {
     CRG_REQUIRE(r != nullptr, CRG_ERR_INVALID_ARGUMENT, "regridder is NULL");
+    ensure_row_col_sums(r);
     if (row_sums && r->nd) CRG_CHECK_CUDA(cudaMemcpy(row_sums, r->row_sum, sizeof(double) * r->nd, cudaMemcpyDefault));
     if (col_sums && r->ns) CRG_CHECK_CUDA(cudaMemcpy(col_sums, r->col_sum, sizeof(double) * r->ns, cudaMemcpyDefault));
   });

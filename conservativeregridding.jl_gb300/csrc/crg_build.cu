@@ -873,20 +873,28 @@ __global__ void k_div_by(double* __restrict__ v, int64_t n, const unsigned long 
   if (i < n) v[i] = v[i] / __longlong_as_double((long long)*mx);
 }
 
-// FP32 weights: val32 = A, wn32 = A / area_row, adj32 = A / area_col, plus the
-// Kahan row sums of A.
 // FP32 copies of the entries and of the normalised / adjoint weights, one
-// thread per entry (erow: the row of each entry).
+// thread per entry (erow: the row of each entry): val32 = A, wn32 = A / area_row,
+// adj32 = A / area_col, each formed in FP64 as A times the FP64 reciprocal of the
+// area (one reciprocal per cell, k_recip: FP64 division is a long sequence on
+// GB300's FP64 pipe) and rounded to FP32.  The product is within 2^-52 of the
+// quotient, relative, so the weight is the rounded quotient except when that lies
+// within 2^-52 of an FP32 rounding midpoint, and then one FP32 ulp from it.
+__global__ void k_recip(const double* __restrict__ v, int64_t n, double* __restrict__ r) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = 1.0 / v[i];
+}
+
 __global__ void k_derive(const int32_t* __restrict__ erow, const int32_t* __restrict__ idx,
-                         const double* __restrict__ val, int64_t nnz, const double* __restrict__ area_row,
-                         const double* __restrict__ area_col, float* __restrict__ val32, float* __restrict__ wn32,
+                         const double* __restrict__ val, int64_t nnz, const double* __restrict__ inv_row,
+                         const double* __restrict__ inv_col, float* __restrict__ val32, float* __restrict__ wn32,
                          float* __restrict__ adj32) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= nnz) return;
   const double a = val[k];
   val32[k] = (float)a;
-  wn32[k] = (float)(a / area_row[erow[k]]);
-  adj32[k] = (float)(a / area_col[idx[k]]);
+  wn32[k] = (float)(a * inv_row[erow[k]]);
+  adj32[k] = (float)(a * inv_col[idx[k]]);
 }
 
 // Kahan-summed rows of A, entries in column order.
@@ -1371,6 +1379,31 @@ void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
   }
 }
 
+void ensure_row_col_sums(const crg_regridder* Rc) {
+  crg_regridder* R = const_cast<crg_regridder*>(Rc);  // the sums are a cache: R stays logically read-only
+  std::lock_guard<std::mutex> lock(R->sums_mu);
+  if (R->sums_ready) return;
+  int dev = 0;
+  CRG_CHECK_CUDA(cudaGetDevice(&dev));
+  struct Restore {
+    int d;
+    ~Restore() { cudaSetDevice(d); }
+  } restore{dev};
+  CRG_CHECK_CUDA(cudaSetDevice(R->device));
+  cudaStream_t st = nullptr;
+  CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaError_t e = cudaSuccess;
+  if (!R->row_sum) e = cudaMalloc((void**)&R->row_sum, sizeof(double) * (R->nd + 4));
+  if (e == cudaSuccess && !R->col_sum) e = cudaMalloc((void**)&R->col_sum, sizeof(double) * (R->ns + 4));
+  if (e == cudaSuccess && R->nd) k_row_sums<<<nblk(R->nd, 256), 256, 0, st>>>(R->fwd.ptr, R->fwd.val, R->nd, R->row_sum);
+  if (e == cudaSuccess && R->ns) k_row_sums<<<nblk(R->ns, 256), 256, 0, st>>>(R->rev.ptr, R->rev.val, R->ns, R->col_sum);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  CRG_CHECK_CUDA(e);
+  R->sums_ready = true;
+}
+
 void finish_build(crg_regridder* R, cudaStream_t st) {
   const int64_t nd = R->nd, ns = R->ns, nnz = R->nnz;
   for (DevCsr* c : {&R->fwd, &R->rev}) {
@@ -1378,19 +1411,18 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
     c->wn32 = keep_alloc<float>((size_t)nnz, st);
     c->adj32 = keep_alloc<float>((size_t)nnz, st);
   }
-  R->row_sum = keep_alloc<double>((size_t)nd, st);
-  R->col_sum = keep_alloc<double>((size_t)ns, st);
   build_merge_path(R->fwd, st);  // also the row of every entry
   build_merge_path(R->rev, st);
   if (nnz) {
-    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.erow, R->fwd.idx, R->fwd.val, nnz, R->dst_area, R->src_area,
+    DBuf<double> inv_d((size_t)nd, st), inv_s((size_t)ns, st);
+    k_recip<<<nblk(nd, 256), 256, 0, st>>>(R->dst_area, nd, inv_d.p);
+    k_recip<<<nblk(ns, 256), 256, 0, st>>>(R->src_area, ns, inv_s.p);
+    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.erow, R->fwd.idx, R->fwd.val, nnz, inv_d.p, inv_s.p,
                                              R->fwd.val32, R->fwd.wn32, R->fwd.adj32);
-    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.erow, R->rev.idx, R->rev.val, nnz, R->src_area, R->dst_area,
+    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.erow, R->rev.idx, R->rev.val, nnz, inv_s.p, inv_d.p,
                                              R->rev.val32, R->rev.wn32, R->rev.adj32);
+    CRG_CHECK_CUDA(cudaGetLastError());
   }
-  if (nd) k_row_sums<<<nblk(nd, 256), 256, 0, st>>>(R->fwd.ptr, R->fwd.val, nd, R->row_sum);
-  if (ns) k_row_sums<<<nblk(ns, 256), 256, 0, st>>>(R->rev.ptr, R->rev.val, ns, R->col_sum);
-  CRG_CHECK_CUDA(cudaGetLastError());
   crg_info& I = R->info;
   const DevCsr* cs[2] = {&R->fwd, &R->rev};
   for (int d = 0; d < 2; ++d) {

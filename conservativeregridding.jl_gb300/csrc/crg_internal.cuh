@@ -127,8 +127,12 @@ struct crg_regridder {
   crg::DevCsr rev;  // CSR of A^T (rows = src)
   double* dst_area = nullptr;   // [nd]
   double* src_area = nullptr;   // [ns]
-  double* row_sum = nullptr;    // [nd] Kahan row sums of A
-  double* col_sum = nullptr;    // [ns] Kahan column sums of A
+  // [nd] / [ns] Kahan row / column sums of A, computed on first request
+  // (ensure_row_col_sums) under sums_mu
+  double* row_sum = nullptr;
+  double* col_sum = nullptr;
+  std::mutex sums_mu;
+  bool sums_ready = false;
   crg_info info{};
   // staging for host-memory fields in crg_apply
   // per matrix copy ([0] A, [1] A^T), so that an apply of R and one of
@@ -194,9 +198,12 @@ struct PairSearch {
   void search(double* dst_area, double* src_area, cudaStream_t st);
 };
 
-// FP32 weights, Kahan row / column sums and the merge-path layouts of both
-// directions of R (after its matrix and areas are final).
+// FP32 weights and the merge-path layouts of both directions of R (after its
+// matrix and areas are final).
 void finish_build(crg_regridder* R, cudaStream_t st);
+// The Kahan row and column sums of A (row_sum, col_sum), computed the first
+// time they are asked for; safe to call from several threads.
+void ensure_row_col_sums(const crg_regridder* R);
 // crg_build_se_to_fv / crg_build_fv_to_se (crg_se.cu)
 crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, const crg_se_opts* opts,
                              bool se_is_dst);

@@ -278,7 +278,9 @@ crg_status crg_get_areas(const crg_regridder* r, double* dst_areas, double* src_
 
 /* Kahan-summed row sums (length n_dst) and column sums (length n_src) of A:
  * the quantities the reference's area-agreement test compares with the cell
- * areas (lib/ConservativeRegriddingTestHelpers/src/ConservativeRegriddingTestHelpers.jl:70-73). */
+ * areas (lib/ConservativeRegriddingTestHelpers/src/ConservativeRegriddingTestHelpers.jl:70-73).
+ * Computed on the first call (or the first crg_get_esmf_weights), not by the
+ * build; thread-safe. */
 crg_status crg_get_row_col_sums(const crg_regridder* r, double* row_sums, double* col_sums);
 
 /* ------------------------------------------------------------------------
