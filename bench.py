@@ -408,17 +408,23 @@ def run_ours(a, rank, world):
         regrid_(ho_r, T, hd, dims=dims)
 
     def timed(step):
-        step()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ne = max(3, min(a.steps, 20))
-        for _ in range(ne):
+        """Median over 5 windows of ne steps (3 warm-up steps first), and the
+        windows' range."""
+        for _ in range(3):
             step()
         torch.cuda.synchronize()
-        return (time.perf_counter() - t0) * 1e3 / ne
+        ne = max(3, min(a.steps, 6))
+        ws = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            for _ in range(ne):
+                step()
+            torch.cuda.synchronize()
+            ws.append((time.perf_counter() - t0) * 1e3 / ne)
+        return statistics.median(ws), (min(ws), max(ws))
 
-    e2e_seq_ms = timed(step_host_sequential)
-    e2e_ms = timed(step_host)
+    e2e_seq_ms, _ = timed(step_host_sequential)
+    e2e_ms, e2e_range = timed(step_host)
     h2d = 4 * K * (ns + nd)
     d2h = 4 * K * (nd + ns)
     assert torch.equal(ho_f, out_f.cpu()), "host-buffer apply differs from the device apply"
@@ -474,6 +480,8 @@ def run_ours(a, rank, world):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"},
         "e2e": {"value": round(world * (bf + br) / (e2e_ms * 1e-3) / 1e9, 2), "unit": "GB/s",
                 "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "ms_per_step_range": [round(e2e_range[0], 3), round(e2e_range[1], 3)],
+                "timing": "median of 5 windows of 6 steps after 3 warm-up steps (wall clock, synchronised)",
                 "call": "regrid_batch_ (crg_apply_batch) of the step's two applies, pinned host fields",
                 "sequential": {"ms_per_step": round(e2e_seq_ms, 3),
                                "GB/s": round(world * (bf + br) / (e2e_seq_ms * 1e-3) / 1e9, 2),
