@@ -353,18 +353,55 @@ __global__ void k_leaves(const float4* __restrict__ bound, const int32_t* __rest
   hi[l] = b;
 }
 
-__global__ void k_level_up(const float4* __restrict__ clo, const float4* __restrict__ chi, int64_t nchild,
-                           float4* __restrict__ plo, float4* __restrict__ phi, int64_t nparent) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nparent) return;
-  float4 a = clo[2 * i], b = chi[2 * i];
-  if (2 * i + 1 < nchild) {
-    float4 c = clo[2 * i + 1], d = chi[2 * i + 1];
-    a.x = fminf(a.x, c.x); a.y = fminf(a.y, c.y); a.z = fminf(a.z, c.z);
-    b.x = fmaxf(b.x, d.x); b.y = fmaxf(b.y, d.y); b.z = fmaxf(b.z, d.z);
+// Levels l0 + 1 .. l0 + nup (nup <= kUp) of the box hierarchy in one launch:
+// node i of level l + 1 bounds nodes 2i and 2i + 1 of level l, so each block
+// reduces its 2^kUp nodes of level l0 through shared memory, one level per
+// step, and writes every level it forms (min / max are exact: the boxes are
+// those of a launch per level).
+constexpr int kUp = 9;  // 512 nodes of level l0 per block of 256 threads
+struct LevelTable {
+  int64_t off[kMaxLevels];
+  int64_t cnt[kMaxLevels];
+};
+
+__global__ void __launch_bounds__(256)
+    k_levels_up(float4* __restrict__ lo, float4* __restrict__ hi, LevelTable lt, int l0, int nup) {
+  __shared__ float4 slo[1 << kUp], shi[1 << kUp];
+  int64_t cb = (int64_t)blockIdx.x << kUp;  // this block's first node of the current level
+  for (int k = threadIdx.x; k < (1 << kUp); k += blockDim.x)
+    if (cb + k < lt.cnt[l0]) {
+      slo[k] = lo[lt.off[l0] + cb + k];
+      shi[k] = hi[lt.off[l0] + cb + k];
+    }
+  __syncthreads();
+  int64_t nc = lt.cnt[l0];
+  for (int u = 1; u <= nup; ++u) {
+    const int l = l0 + u;
+    const int pw = (1 << kUp) >> u;  // this block's parents at level l
+    const int64_t pb = cb >> 1;
+    const int k = threadIdx.x;
+    const bool have = k < pw && pb + k < lt.cnt[l];  // then child 2k exists
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (have) {
+      a = slo[2 * k];
+      b = shi[2 * k];
+      if (cb + 2 * k + 1 < nc) {
+        const float4 c = slo[2 * k + 1], d = shi[2 * k + 1];
+        a.x = fminf(a.x, c.x); a.y = fminf(a.y, c.y); a.z = fminf(a.z, c.z);
+        b.x = fmaxf(b.x, d.x); b.y = fmaxf(b.y, d.y); b.z = fmaxf(b.z, d.z);
+      }
+    }
+    __syncthreads();
+    if (have) {
+      slo[k] = a;
+      shi[k] = b;
+      lo[lt.off[l] + pb + k] = a;
+      hi[lt.off[l] + pb + k] = b;
+    }
+    __syncthreads();
+    nc = lt.cnt[l];
+    cb = pb;
   }
-  plo[i] = a;
-  phi[i] = b;
 }
 
 struct Tree {
@@ -868,9 +905,24 @@ __global__ void k_max_val(const double* __restrict__ v, int64_t n, unsigned long
   if ((threadIdx.x & 31) == 0) atomicMax(mx, (unsigned long long)__double_as_longlong(m));
 }
 
-__global__ void k_div_by(double* __restrict__ v, int64_t n, const unsigned long long* __restrict__ mx) {
+// normalize!: both CSR copies of A and both area vectors divided by max(A),
+// one launch over the four arrays back to back.
+__global__ void k_div_by(double* __restrict__ a, double* __restrict__ b, int64_t nnz, double* __restrict__ c,
+                         int64_t nc, double* __restrict__ d, int64_t nd, const unsigned long long* __restrict__ mx) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) v[i] = v[i] / __longlong_as_double((long long)*mx);
+  double* v;
+  if (i < nnz) {
+    v = a;
+  } else if ((i -= nnz) < nnz) {
+    v = b;
+  } else if ((i -= nnz) < nc) {
+    v = c;
+  } else if ((i -= nc) < nd) {
+    v = d;
+  } else {
+    return;
+  }
+  v[i] = v[i] / __longlong_as_double((long long)*mx);
 }
 
 // FP32 copies of the entries and of the normalised / adjoint weights, one
@@ -1105,10 +1157,17 @@ void build_tree(const DevGrid& g, bool sph, double* area_out, HostTree& h, cudaS
   else
     k_leaves<false><<<nblk(nleaves, 128), 128, 0, st>>>(h.bound.p, h.perm.p, n, nleaves, h.lo.p, h.hi.p, h.sbound.p);
   CRG_CHECK_CUDA(cudaGetLastError());
-  for (int l = 1; l < nlev; ++l) {
-    k_level_up<<<nblk(h.t.cnt[l], 256), 256, 0, st>>>(h.lo.p + h.t.off[l - 1], h.hi.p + h.t.off[l - 1], h.t.cnt[l - 1],
-                                                    h.lo.p + h.t.off[l], h.hi.p + h.t.off[l], h.t.cnt[l]);
+  LevelTable lt{};
+  for (int l = 0; l < nlev; ++l) {
+    lt.off[l] = h.t.off[l];
+    lt.cnt[l] = h.t.cnt[l];
+  }
+  for (int l0 = 0; l0 + 1 < nlev;) {
+    const int nup = std::min(kUp, nlev - 1 - l0);
+    const int64_t blocks = (h.t.cnt[l0] + (1 << kUp) - 1) >> kUp;
+    k_levels_up<<<(unsigned)blocks, 256, 0, st>>>(h.lo.p, h.hi.p, lt, l0, nup);
     CRG_CHECK_CUDA(cudaGetLastError());
+    l0 += nup;
   }
   h.t.lo = h.lo.p;
   h.t.hi = h.hi.p;
@@ -1250,39 +1309,54 @@ bool is_device_pointer(const void* p) {
 }
 
 // Sorts the columns (and values) of every row of a CSR ascending.
+void sort_rows(const RowSet* sets, int nsets, cudaStream_t st) {
+  // per set: [nrows] mid rows | [nrows] long rows | [nrows] 9..32-entry rows; then [3] counts per set
+  std::vector<int64_t> base((size_t)nsets + 1, 0);
+  for (int k = 0; k < nsets; ++k) base[k + 1] = base[k] + 3 * sets[k].nrows;
+  DBuf<int32_t> lists((size_t)base[nsets] + 3 * nsets, st);
+  int32_t* counts = lists.p + base[nsets];
+  CRG_CHECK_CUDA(cudaMemsetAsync(counts, 0, 3 * nsets * sizeof(int32_t), st));
+  for (int k = 0; k < nsets; ++k) {
+    const RowSet& r = sets[k];
+    if (r.nrows == 0) continue;
+    int32_t* l = lists.p + base[k];
+    k_row_sort_small<<<nblk(r.nrows, 256), 256, 0, st>>>(r.ptr, r.nrows, r.idx, r.val);
+    k_row_classes<<<nblk(r.nrows, 256), 256, 0, st>>>(r.ptr, r.nrows, l + 2 * r.nrows, l, l + r.nrows, counts + 3 * k);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  std::vector<int32_t> h((size_t)3 * nsets);
+  CRG_CHECK_CUDA(cudaMemcpyAsync(h.data(), counts, sizeof(int32_t) * 3 * nsets, cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));  // one wait for all sets
+  for (int k = 0; k < nsets; ++k) {
+    const RowSet& r = sets[k];
+    const int32_t* hk = h.data() + 3 * k;
+    int32_t* l = lists.p + base[k];
+    if (hk[2]) {
+      k_row_sort_warp<<<nblk((int64_t)hk[2] * 32, 256), 256, 0, st>>>(r.ptr, l + 2 * r.nrows, hk[2], r.idx, r.val);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (hk[0]) {
+      k_row_sort_block<<<(unsigned)hk[0], kRowSortThreads, 0, st>>>(r.ptr, l, r.idx, r.val);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (hk[1]) {
+      DBuf<int64_t> off(hk[1] + 1, st);
+      k_long_windows<<<1, 1, 0, st>>>(r.ptr, l + r.nrows, hk[1], off.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+      int64_t total = 0;
+      CRG_CHECK_CUDA(cudaMemcpyAsync(&total, off.p + hk[1], sizeof(total), cudaMemcpyDeviceToHost, st));
+      CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+      DBuf<int32_t> gk(total, st);
+      DBuf<double> gv(total, st);
+      k_row_sort_long<<<(unsigned)hk[1], 1024, 0, st>>>(r.ptr, l + r.nrows, off.p, r.idx, r.val, gk.p, gv.p);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+  }
+}
+
 void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cudaStream_t st) {
-  if (nrows == 0) return;
-  k_row_sort_small<<<nblk(nrows, 256), 256, 0, st>>>(ptr, nrows, idx, val);
-  CRG_CHECK_CUDA(cudaGetLastError());
-  // [nrows] mid rows | [nrows] long rows | [nrows] 9..32-entry rows | [3] counts
-  DBuf<int32_t> lists(3 * nrows + 3, st);
-  int32_t* counts = lists.p + 3 * nrows;
-  CRG_CHECK_CUDA(cudaMemsetAsync(counts, 0, 3 * sizeof(int32_t), st));
-  k_row_classes<<<nblk(nrows, 256), 256, 0, st>>>(ptr, nrows, lists.p + 2 * nrows, lists.p, lists.p + nrows, counts);
-  CRG_CHECK_CUDA(cudaGetLastError());
-  int32_t h[3] = {0, 0, 0};
-  CRG_CHECK_CUDA(cudaMemcpyAsync(h, counts, sizeof(h), cudaMemcpyDeviceToHost, st));
-  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-  if (h[2]) {
-    k_row_sort_warp<<<nblk((int64_t)h[2] * 32, 256), 256, 0, st>>>(ptr, lists.p + 2 * nrows, h[2], idx, val);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-  if (h[0]) {
-    k_row_sort_block<<<(unsigned)h[0], kRowSortThreads, 0, st>>>(ptr, lists.p, idx, val);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-  if (h[1]) {
-    DBuf<int64_t> off(h[1] + 1, st);
-    k_long_windows<<<1, 1, 0, st>>>(ptr, lists.p + nrows, h[1], off.p);
-    CRG_CHECK_CUDA(cudaGetLastError());
-    int64_t total = 0;
-    CRG_CHECK_CUDA(cudaMemcpyAsync(&total, off.p + h[1], sizeof(total), cudaMemcpyDeviceToHost, st));
-    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-    DBuf<int32_t> gk(total, st);
-    DBuf<double> gv(total, st);
-    k_row_sort_long<<<(unsigned)h[1], 1024, 0, st>>>(ptr, lists.p + nrows, off.p, idx, val, gk.p, gv.p);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
+  const RowSet one{ptr, nrows, idx, val};
+  sort_rows(&one, 1, st);
 }
 
 void free_csr(DevCsr& c) {
@@ -1411,8 +1485,9 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
     c->wn32 = keep_alloc<float>((size_t)nnz, st);
     c->adj32 = keep_alloc<float>((size_t)nnz, st);
   }
-  build_merge_path(R->fwd, st);  // also the row of every entry
-  build_merge_path(R->rev, st);
+  DBuf<int32_t> dcounts(6, st);
+  build_merge_path(R->fwd, dcounts.p, st);  // also the row of every entry
+  build_merge_path(R->rev, dcounts.p + 3, st);
   if (nnz) {
     DBuf<double> inv_d((size_t)nd, st), inv_s((size_t)ns, st);
     k_recip<<<nblk(nd, 256), 256, 0, st>>>(R->dst_area, nd, inv_d.p);
@@ -1423,6 +1498,11 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
                                              R->rev.val32, R->rev.wn32, R->rev.adj32);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
+  int32_t hc[6];
+  CRG_CHECK_CUDA(cudaMemcpyAsync(hc, dcounts.p, sizeof(hc), cudaMemcpyDeviceToHost, st));
+  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+  finish_merge_path(R->fwd, hc, st);
+  finish_merge_path(R->rev, hc + 3, st);
   crg_info& I = R->info;
   const DevCsr* cs[2] = {&R->fwd, &R->rev};
   for (int d = 0; d < 2; ++d) {
@@ -1512,8 +1592,8 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
                                                      R->fwd.idx, R->fwd.val, R->rev.idx, R->rev.val);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
-    sort_rows(R->fwd.ptr, nd, R->fwd.idx, R->fwd.val, st);
-    sort_rows(R->rev.ptr, ns, R->rev.idx, R->rev.val, st);
+    const RowSet both[2] = {{R->fwd.ptr, nd, R->fwd.idx, R->fwd.val}, {R->rev.ptr, ns, R->rev.idx, R->rev.val}};
+    sort_rows(both, 2, st);
 
     // normalize! (regridder.jl:54-62)
     DBuf<unsigned long long> mx(1, st);
@@ -1522,25 +1602,21 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
       k_max_val<<<(unsigned)std::min<int64_t>(nblk(nnz, 256), 152 * 8), 256, 0, st>>>(R->fwd.val, nnz, mx.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
+    // max(A) is read back with the build's last synchronisation (the divisions read it on the device)
     unsigned long long hmx = 0;
     CRG_CHECK_CUDA(cudaMemcpyAsync(&hmx, mx.p, sizeof(hmx), cudaMemcpyDeviceToHost, st));
-    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-    double maxA;
-    memcpy(&maxA, &hmx, sizeof(double));
-    R->normalizer = normalize ? maxA : 1.0;
     R->normalized = normalize;
-    if (normalize) {
-      if (nnz) {
-        k_div_by<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.val, nnz, mx.p);
-        k_div_by<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.val, nnz, mx.p);
-      }
-      if (nd) k_div_by<<<nblk(nd, 256), 256, 0, st>>>(R->dst_area, nd, mx.p);
-      if (ns) k_div_by<<<nblk(ns, 256), 256, 0, st>>>(R->src_area, ns, mx.p);
+    if (normalize && 2 * nnz + nd + ns) {
+      k_div_by<<<nblk(2 * nnz + nd + ns, 256), 256, 0, st>>>(R->fwd.val, R->rev.val, nnz, R->dst_area, nd,
+                                                             R->src_area, ns, mx.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     finish_build(R, st);
     CRG_CHECK_CUDA(cudaEventRecord(ev.e[3], st));
     CRG_CHECK_CUDA(cudaEventSynchronize(ev.e[3]));
+    double maxA;
+    memcpy(&maxA, &hmx, sizeof(double));
+    R->normalizer = normalize ? maxA : 1.0;
     float t01 = 0, t12 = 0, t23 = 0, t03 = 0;
     cudaEventElapsedTime(&t01, ev.e[0], ev.e[1]);
     cudaEventElapsedTime(&t12, ev.e[1], ev.e[2]);

@@ -172,7 +172,20 @@ void host_pipeline_ends(const crg_apply_item& it, size_t& fill, size_t& drain);
 bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
-void build_merge_path(DevCsr& c, cudaStream_t st);
+// The merge-path layout of one direction, enqueued without host waits; its
+// counts land in dcounts[0..2] (device) and finish_merge_path takes them from
+// a host copy once the stream has reached them.
+void build_merge_path(DevCsr& c, int32_t* dcounts, cudaStream_t st);
+void finish_merge_path(DevCsr& c, const int32_t* hcounts, cudaStream_t st);
+// Each row segment of a CSR sorted by column (values follow), for several
+// CSRs with one host wait between classifying the rows and sorting them.
+struct RowSet {
+  const int32_t* ptr;
+  int64_t nrows;
+  int32_t* idx;
+  double* val;
+};
+void sort_rows(const RowSet* sets, int nsets, cudaStream_t st);
 void sort_rows(const int32_t* ptr, int64_t nrows, int32_t* idx, double* val, cudaStream_t st);
 
 // The search stage every build shares: both grids' cell tables on the device,

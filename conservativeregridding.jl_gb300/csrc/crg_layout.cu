@@ -102,10 +102,10 @@ __global__ void k_split_fill(const int32_t* __restrict__ ptr, const int32_t* __r
 
 // Slots of cut row s are base[s] .. base[s] + pieces - 1 in task order: the
 // row's first task writes its last-row slot, the later tasks their first-row slot.
-__global__ void k_slot_fill(int32_t* __restrict__ split, int64_t nsplit, const int32_t* __restrict__ base,
-                            int2* __restrict__ tslot) {
+__global__ void k_slot_fill(int32_t* __restrict__ split, const int32_t* __restrict__ nsplit,
+                            const int32_t* __restrict__ base, int2* __restrict__ tslot) {
   const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nsplit) return;
+  if (s >= *nsplit) return;
   const int32_t t0 = split[3 * s + 1], pieces = split[3 * s + 2], b = base[s];
   tslot[t0].y = b;
   for (int32_t k = 1; k < pieces; ++k) tslot[t0 + k].x = b + k;
@@ -114,12 +114,18 @@ __global__ void k_slot_fill(int32_t* __restrict__ split, int64_t nsplit, const i
 
 }  // namespace
 
-void build_merge_path(DevCsr& c, cudaStream_t st) {
+// Enqueued without waiting on the host: the buffers whose length depends on
+// the cut rows are sized by the task count (no more rows than tasks can be
+// cut), and the counts (cut rows, empty rows, carry slots) go to dcounts[0..2]
+// for finish_merge_path, after the caller's one synchronisation for both
+// directions.
+void build_merge_path(DevCsr& c, int32_t* dcounts, cudaStream_t st) {
   const int64_t n = c.nrows, nnz = c.nnz;
   c.erow = keep_alloc<int32_t>((size_t)nnz, st);
   const size_t nwords = (size_t)(nnz >> 5) + 2;
   c.rbits = keep_alloc<uint32_t>(nwords, st);
   CRG_CHECK_CUDA(cudaMemsetAsync(c.rbits, 0, sizeof(uint32_t) * nwords, st));
+  CRG_CHECK_CUDA(cudaMemsetAsync(dcounts, 0, 3 * sizeof(int32_t), st));
   // CRG_TASK_NNZ (32..1024) sets the nominal task length for tuning; CRG_TASK_CUT=fixed
   // cuts every task at exactly that length (rows spanning tasks everywhere)
   static const int task_nnz = [] {
@@ -138,47 +144,45 @@ void build_merge_path(DevCsr& c, cudaStream_t st) {
   c.nslots = 0;
   c.nempty = n;
   if (n == 0 || nnz == 0) return;
-  int32_t* work = nullptr;  // [1] empty rows | [ntasks + 1] bounds | [ntasks + 1] split positions
-  CRG_CHECK_CUDA(cudaMallocAsync((void**)&work, sizeof(int32_t) * (2 * c.ntasks + 3), st));
-  int32_t* nempty = work;
-  int32_t* bound = work + 1;
-  int32_t* pos = bound + c.ntasks + 1;
-  CRG_CHECK_CUDA(cudaMemsetAsync(nempty, 0, sizeof(int32_t), st));
-  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow, c.rbits, nempty);
+  const int64_t nt = c.ntasks;
+  int32_t* work = nullptr;  // [ntasks + 1] bounds | [ntasks + 1] split positions | [ntasks + 1] pieces
+  CRG_CHECK_CUDA(cudaMallocAsync((void**)&work, sizeof(int32_t) * (3 * nt + 3), st));
+  int32_t* bound = work;
+  int32_t* pos = bound + nt + 1;
+  int32_t* span = pos + nt + 1;
+  k_expand_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, n, c.erow, c.rbits, dcounts + 1);
   CRG_CHECK_CUDA(cudaGetLastError());
-  k_task_bounds<<<nblk(c.ntasks + 1, 256), 256, 0, st>>>(c.ptr, c.erow, nnz, c.ntasks, task_nnz, long_row, bound);
+  k_task_bounds<<<nblk(nt + 1, 256), 256, 0, st>>>(c.ptr, c.erow, nnz, nt, task_nnz, long_row, bound);
   CRG_CHECK_CUDA(cudaGetLastError());
-  k_task_records<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, c.erow, bound, c.ntasks, c.tasks, pos);
+  k_task_records<<<nblk(nt, 256), 256, 0, st>>>(c.ptr, c.erow, bound, nt, c.tasks, pos);
   CRG_CHECK_CUDA(cudaGetLastError());
-  exclusive_scan_i32(pos, pos, c.ntasks, st);
-  int32_t counts[2] = {0, 0};
-  CRG_CHECK_CUDA(cudaMemcpyAsync(&counts[0], pos + c.ntasks, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  CRG_CHECK_CUDA(cudaMemcpyAsync(&counts[1], nempty, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-  c.nsplit = counts[0];
-  c.nempty = counts[1];
-  if (c.nempty) {
-    c.nextrow = keep_alloc<int32_t>((size_t)n, st);
-    k_next_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.erow, n, nnz, c.nextrow);
-    CRG_CHECK_CUDA(cudaGetLastError());
-  }
-  CRG_CHECK_CUDA(cudaMemsetAsync(c.tslot, 0xff, sizeof(int2) * c.ntasks, st));  // -1: row not cut
-  c.split = keep_alloc<int32_t>((size_t)3 * c.nsplit, st);
-  if (c.nsplit) {
-    int32_t* span = nullptr;  // [nsplit + 1] pieces per cut row, scanned to first slots
-    CRG_CHECK_CUDA(cudaMallocAsync((void**)&span, sizeof(int32_t) * (c.nsplit + 1), st));
-    k_split_fill<<<nblk(c.ntasks, 256), 256, 0, st>>>(c.ptr, bound, c.ntasks, c.tasks, pos, c.split, span);
-    CRG_CHECK_CUDA(cudaGetLastError());
-    exclusive_scan_i32(span, span, c.nsplit, st);
-    k_slot_fill<<<nblk(c.nsplit, 256), 256, 0, st>>>(c.split, c.nsplit, span, c.tslot);
-    CRG_CHECK_CUDA(cudaGetLastError());
-    int32_t nslots = 0;
-    CRG_CHECK_CUDA(cudaMemcpyAsync(&nslots, span + c.nsplit, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    CRG_CHECK_CUDA(cudaFreeAsync(span, st));
-    CRG_CHECK_CUDA(cudaStreamSynchronize(st));
-    c.nslots = nslots;
-  }
+  exclusive_scan_i32(pos, pos, nt, st);  // pos[nt] = cut rows
+  CRG_CHECK_CUDA(cudaMemcpyAsync(dcounts, pos + nt, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
+  // the next non-empty row of each row (kept only when some row is empty)
+  c.nextrow = keep_alloc<int32_t>((size_t)n, st);
+  k_next_rows<<<nblk(n, 256), 256, 0, st>>>(c.ptr, c.erow, n, nnz, c.nextrow);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  CRG_CHECK_CUDA(cudaMemsetAsync(c.tslot, 0xff, sizeof(int2) * nt, st));  // -1: row not cut
+  c.split = keep_alloc<int32_t>((size_t)3 * nt, st);
+  CRG_CHECK_CUDA(cudaMemsetAsync(span, 0, sizeof(int32_t) * (nt + 1), st));
+  k_split_fill<<<nblk(nt, 256), 256, 0, st>>>(c.ptr, bound, nt, c.tasks, pos, c.split, span);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  exclusive_scan_i32(span, span, nt, st);  // first slots; span[nt] = carry slots
+  k_slot_fill<<<nblk(nt, 256), 256, 0, st>>>(c.split, pos + nt, span, c.tslot);
+  CRG_CHECK_CUDA(cudaGetLastError());
+  CRG_CHECK_CUDA(cudaMemcpyAsync(dcounts + 2, span + nt, sizeof(int32_t), cudaMemcpyDeviceToDevice, st));
   CRG_CHECK_CUDA(cudaFreeAsync(work, st));
+}
+
+void finish_merge_path(DevCsr& c, const int32_t* hcounts, cudaStream_t st) {
+  if (c.nrows == 0 || c.nnz == 0) return;
+  c.nsplit = hcounts[0];
+  c.nempty = hcounts[1];
+  c.nslots = hcounts[2];
+  if (c.nempty == 0) {
+    CRG_CHECK_CUDA(cudaFreeAsync(c.nextrow, st));
+    c.nextrow = nullptr;
+  }
 }
 
 }  // namespace crg
