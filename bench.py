@@ -699,12 +699,14 @@ def run_se(a):
     for name, make in (("se_to_fv", lambda: Regridder(fv, space)), ("fv_to_se", lambda: Regridder(space, fv))):
         make()
         times = []
-        for _ in range(5):
+        for i in range(5):
             torch.cuda.synchronize()
+            torch.cuda.nvtx.range_push(f"{name}{i}")  # NVTX ranges select launches for ncu's launch list
             t0 = time.perf_counter()
             R = make()
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
+            torch.cuda.nvtx.range_pop()
         tb = statistics.median(times)
         nd, ns = R.shape
         s = torch.rand(ns, dtype=torch.float64, device=dev, generator=torch.Generator(device=dev).manual_seed(1))

@@ -447,3 +447,49 @@ def test_concurrent_applies_on_two_streams(cuda):
     assert not errors, errors
     for y, ref in zip(outs, refs):
         assert torch.equal(y, ref)
+
+
+def _kahan_segments(indptr, data):
+    """Kahan sums of each CSR segment in stored order (the operation order of
+    the library's row sums)."""
+    out = np.empty(len(indptr) - 1)
+    for r in range(len(indptr) - 1):
+        s = c = 0.0
+        for v in data[indptr[r]:indptr[r + 1]]:
+            y = v - c
+            t = s + y
+            c = (t - s) - y
+            s = t
+        out[r] = s
+    return out
+
+
+def test_row_col_sums_on_request_from_threads(cuda):
+    """Row / column sums are computed on the first request, once, even when
+    several threads ask at the same time; they are the Kahan sums of A in
+    column (row) order and agree with the cell areas as the reference's area
+    test asks (lib/ConservativeRegriddingTestHelpers/src/ConservativeRegriddingTestHelpers.jl:70-73)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    dst, src = c1_grids()
+    R = Regridder(dst, src, normalize=True)
+    A = R.intersections
+    csr = A.tocsr()
+    csr.sort_indices()
+    csc = A.tocsc()
+    csc.sort_indices()
+    want_r, want_c = _kahan_segments(csr.indptr, csr.data), _kahan_segments(csc.indptr, csc.data)
+    with ThreadPoolExecutor(4) as ex:
+        got = list(ex.map(lambda _: R.row_col_sums(), range(4)))
+    for rs, cs in got:
+        assert np.array_equal(rs, want_r) and np.array_equal(cs, want_c)
+    tol = np.sqrt(np.finfo(np.float64).eps)
+    assert np.allclose(want_r, R.dst_areas, rtol=tol, atol=0)
+    # the destination grid starts at -89.6 degrees: source cells reaching below it are not covered
+    t, _ = src.cell_table()
+    covered = t[:, :4, 2].min(axis=1) > np.sin(np.radians(-89.6)) + 1e-12
+    assert 0 < (~covered).sum() < 400
+    assert np.allclose(want_c[covered], R.src_areas[covered], rtol=tol, atol=0)
+    assert np.all(want_c[~covered] < R.src_areas[~covered])
+    rs2, cs2 = R.transpose().row_col_sums()  # the transpose view shares the handle's sums
+    assert np.array_equal(rs2, want_r) and np.array_equal(cs2, want_c)
