@@ -336,7 +336,7 @@ __global__ void k_se_nodes(const double* __restrict__ coef, int64_t nelem, const
 //                  the polygon kept in the pair's slot
 //   k_se_items     per pair: its triangles of positive area as (pair, triangle) items
 //   k_se_tri_b<nq> per item: the sum over its rule points
-//   k_se_pair_sum  per pair: its items in fan order
+//   k_se_pair_sum  per pair and node: its items in fan order
 
 __global__ void __launch_bounds__(128)
     k_se_overlap(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
@@ -458,20 +458,27 @@ __global__ void __launch_bounds__(128)
     if (k < nq2) o[k] = T[k];
 }
 
+// One thread per (pair, node): the pair's items summed in fan order (the
+// nq2 threads of a pair read consecutive sums of each item).
 __global__ void k_se_pair_sum(const int32_t* __restrict__ toff, const int32_t* __restrict__ tcount, int64_t nc,
-                              const double* __restrict__ tb, int nq2, double* __restrict__ bv,
-                              int32_t* __restrict__ cnt) {
+                              const double* __restrict__ tb, int nq2, double* __restrict__ bv) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nc * nq2) return;
+  const int64_t pair = t / nq2;
+  const int k = (int)(t - pair * nq2);
+  const int64_t a = toff[pair];
+  const int n = tcount[pair];
+  double s = 0.0;
+  for (int j = 0; j < n; ++j) s = s + tb[(a + j) * nq2 + k];
+  bv[t] = s;
+}
+
+// Nonzero sums of each pair.
+__global__ void k_se_pair_nz(const double* __restrict__ bv, int64_t nc, int nq2, int32_t* __restrict__ cnt) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
-  const int64_t a = toff[t];
-  const int n = tcount[t];
   int nz = 0;
-  for (int k = 0; k < nq2; ++k) {
-    double s = 0.0;
-    for (int j = 0; j < n; ++j) s = s + tb[(a + j) * nq2 + k];
-    bv[t * nq2 + k] = s;
-    nz += s != 0.0;
-  }
+  for (int k = 0; k < nq2; ++k) nz += bv[t * nq2 + k] != 0.0;
   cnt[t] = nz;
 }
 
@@ -939,7 +946,8 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
           default: launch_tri_b<0>(o, ps, coef.p, se_is_dst, rule, tb.p, st); break;
         }
       }
-      k_se_pair_sum<<<nblk(nc, 128), 128, 0, st>>>(toff.p, tcount.p, nc, tb.p, nq2, bv.p, cnt.p);
+      k_se_pair_sum<<<nblk(nc * nq2, 256), 256, 0, st>>>(toff.p, tcount.p, nc, tb.p, nq2, bv.p);
+      k_se_pair_nz<<<nblk(nc, 256), 256, 0, st>>>(bv.p, nc, nq2, cnt.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
 
