@@ -17,7 +17,7 @@ from .grids import (
     unit_sphere_from_geographic,
 )
 from .regridder import Regridder, regrid, regrid_, regrid_adjoint_
-from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points
+from .grad import area_grad, lonlat_tangents, regrid_pullback, split_points, src_area_grad
 from .batch import ApplyPlan, build_batch, regrid_batch_
 from .esmf import esmf_weights, load_esmf_weights, save_esmf_weights
 from .fold import mirror_fold_
@@ -56,5 +56,6 @@ __all__ = [
     "reorder_cells",
     "save_esmf_weights",
     "split_points",
+    "src_area_grad",
     "unit_sphere_from_geographic",
 ]

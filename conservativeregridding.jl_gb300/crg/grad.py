@@ -1,5 +1,5 @@
 """Derivatives of regridding: the pullback of ``regrid!`` with respect to the
-source field and to the destination grid's vertices.
+source field and to the vertices of the destination and source grids.
 
 The reference has no derivatives (no ChainRulesCore dependency,
 Project.toml:10-23); this is the host side of ``crg_apply_adjoint`` and
@@ -59,6 +59,26 @@ def area_grad(R: Regridder, dst, src, row_weight=None, src_field=None, area_weig
     return out
 
 
+def src_area_grad(dst, src, row_weight, src_field, swapped: Regridder = None, stream=None) -> np.ndarray:
+    """sum_ij row_weight[i] src_field[j] dA_ij/dW with respect to the SOURCE
+    vertices W, laid out like the source vertices (as :func:`area_grad` lays
+    out the destination ones).
+
+    A_ij is the area of (destination cell i) ∩ (source cell j), a symmetric
+    function of the two cells, so this is :func:`area_grad` of the regridder
+    built the other way round -- ``Regridder(src, dst)``, whose destination
+    grid is this source grid -- with the two weight vectors exchanged.  Pass
+    that regridder as ``swapped`` to reuse it; otherwise one is built (an
+    unnormalised one: the derivative is of the unnormalised areas).  The
+    source cell areas never enter ``regrid!``'s forward result, so there is
+    no area term."""
+    dst_g, src_g = promote(as_grid(dst), as_grid(src))
+    Rs = Regridder(src_g, dst_g, stream=stream) if swapped is None else swapped
+    if Rs._transposed or Rs.shape != (src_g.ncells, dst_g.ncells):
+        raise DimensionMismatch(f"the swapped regridder has size {Rs.shape}, expected {(src_g.ncells, dst_g.ncells)}")
+    return area_grad(Rs, src_g, dst_g, row_weight=src_field, src_field=row_weight, stream=stream)
+
+
 def split_points(g: Grid, flat: np.ndarray) -> list:
     """Per-block (ny+1, nx+1, dim) views of a (npoints, dim) vertex array."""
     out, o = [], 0
@@ -69,11 +89,17 @@ def split_points(g: Grid, flat: np.ndarray) -> list:
     return out
 
 
-def regrid_pullback(R: Regridder, dst, src, src_field, dst_bar):
+def regrid_pullback(R: Regridder, dst, src, src_field, dst_bar, wrt_src: bool = False, swapped: Regridder = None):
     """Pullback of d = regrid(R, s) = (A s) ./ a at s = src_field for the output
     cotangent dst_bar: returns (s_bar, V_bar), s_bar = A' (dst_bar ./ a) (the
     adjoint apply) and V_bar the cotangent of the destination vertices laid
-    out as in :func:`area_grad`.  FP64, one field."""
+    out as in :func:`area_grad`.  With ``wrt_src=True`` it returns
+    (s_bar, V_bar, W_bar), W_bar the cotangent of the source vertices
+    (:func:`src_area_grad`; ``swapped`` = ``Regridder(src, dst)`` if one is
+    at hand).  Normalisation cancels in d, so the derivatives are those of
+    the unnormalised areas whether R is normalised or not.  FP64, one field."""
+    if R._transposed:
+        raise ArgumentError("regrid_pullback takes the forward regridder (dst <- src), not a transposed view")
     nd, ns = R.info["n_dst"], R.info["n_src"]
     s = _vec(src_field, ns, "src_field")
     g = _vec(dst_bar, nd, "dst_bar")
@@ -82,8 +108,11 @@ def regrid_pullback(R: Regridder, dst, src, src_field, dst_bar):
     s_bar = np.zeros(ns)
     regrid_adjoint_(s_bar, R, g)
     a = R.dst_areas * (R.info["normalizer"] if R.info["normalized"] else 1.0)
-    v_bar = area_grad(R, dst, src, g / a, s, -g * d / a)
-    return s_bar, v_bar
+    u = g / a
+    v_bar = area_grad(R, dst, src, u, s, -g * d / a)
+    if not wrt_src:
+        return s_bar, v_bar
+    return s_bar, v_bar, src_area_grad(dst, src, u, s, swapped=swapped)
 
 
 def lonlat_tangents(points: np.ndarray):
