@@ -8,7 +8,17 @@ arrays may be `CuArray`s (device pointers) or host `Array`s (staged by the
 library).
 
 This file is the `ccall` layer a maintainer adds next to ConservativeRegridding.jl;
-it depends only on `Libdl` and `SparseArrays`.
+it depends only on `Libdl`, `LinearAlgebra` and `SparseArrays`.  Two package
+extensions load with their trigger packages:
+
+- `ConservativeRegriddingGB300RegridderExt` (ConservativeRegridding):
+  `Regridder(GB300(), dst, src; normalize)` returns the reference's own
+  `Regridder` type with a `GB300Sparse` matrix, so `regrid!`, `transpose(R)`
+  and the extensions' field types run through the reference's pipeline (its
+  `mul!` is `crg_apply`); N-D arrays go to the library in one call.
+- `ConservativeRegriddingGB300ChainRulesCoreExt` (ChainRulesCore): `rrule`s
+  for `regrid(A, s)` (the adjoint apply) and `regrid_on(V, W, s)` (also the
+  destination and source vertex cotangents).
 """
 module ConservativeRegriddingGB300
 
@@ -88,17 +98,36 @@ end
 
 Base.size(A::GB300Sparse) = (Int(A.info.n_dst), Int(A.info.n_src))
 Base.size(A::GB300SparseT) = reverse(size(A.parent))
+Base.size(A::Union{GB300Sparse,GB300SparseT}, d::Integer) = d <= 2 ? size(A)[d] : 1
+SparseArrays.nnz(A::Union{GB300Sparse,GB300SparseT}) = Int(_direction(A)[1].info.nnz)
 LinearAlgebra.transpose(A::GB300Sparse) = GB300SparseT(A)
 LinearAlgebra.transpose(A::GB300SparseT) = A.parent
+
+Base.show(io::IO, A::GB300Sparse) = print(io, "$(size(A, 1))×$(size(A, 2)) GB300Sparse with $(nnz(A)) stored entries")
+Base.show(io::IO, A::GB300SparseT) = print(io, "transpose(", A.parent, ")")
+# `show(::Regridder)` prints its matrix with Base.print_array (src/regridder/regridder.jl:38-44)
+Base.print_array(io::IO, A::Union{GB300Sparse,GB300SparseT}) = show(io, A)
+
+"""
+    GB300()
+
+Backend tag of `ConservativeRegridding.Regridder(GB300(), dst, src; normalize)`
+(defined by the package extension for ConservativeRegridding): the build runs
+in `libcrg_gb300.so` and the result is an ordinary `Regridder` whose
+`intersections` is a `GB300Sparse`.
+"""
+struct GB300 end
 
 """
     curvilinear(points::Array{Float64,3})
 
 Describe a grid of `(nx+1) x (ny+1)` vertices given as a `3 x (nx+1) x (ny+1)`
-array of unit vectors (the reference's `CellBasedGrid` vertex matrix).
+array of unit vectors (the reference's `CellBasedGrid` vertex matrix), or a
+`2 x (nx+1) x (ny+1)` array of planar points.
 """
 function curvilinear(points::Array{Float64,3})
     dim, nxp, nyp = size(points)
+    dim in (2, 3) || throw(ArgumentError("points must be 2 or 3 coordinates per vertex, got $dim"))
     nx = Ref(Int64(nxp - 1)); ny = Ref(Int64(nyp - 1))
     desc = CrgGridDesc(0, dim == 3 ? 1 : 0, 1, 0, nx[] * ny[],
                        Base.unsafe_convert(Ptr{Int64}, nx), Base.unsafe_convert(Ptr{Int64}, ny),
@@ -107,14 +136,56 @@ function curvilinear(points::Array{Float64,3})
 end
 
 """
-    Regridder(dst_points, src_points; normalize = false) -> ConservativeRegridding.Regridder
+    cells(verts::Array{Float64,3}, nverts = nothing)
 
-GPU build of `Regridder(dst, src; normalize)` for vertex-matrix grids.  The
-returned struct has `intersections::GB300Sparse` and host copies of the areas.
+Describe a grid of per-cell convex polygons (HEALPix pixels, `FlatNoTree`
+polygon lists): `verts` is `dim x max_verts x ncells` (ring order, not
+closed; `dim` 3 on the sphere, 2 on the plane; `max_verts` 3 to 8) and
+`nverts` the vertex count of each cell (`nothing`: all `max_verts`).
+"""
+function cells(verts::Array{Float64,3}, nverts::Union{Nothing,Vector{Int32}} = nothing)
+    dim, maxv, n = size(verts)
+    dim in (2, 3) || throw(ArgumentError("vertices must have 2 or 3 coordinates, got $dim"))
+    nverts === nothing || length(nverts) == n ||
+        throw(DimensionMismatch("nverts has $(length(nverts)) entries for $n cells"))
+    desc = CrgGridDesc(1, dim == 3 ? 1 : 0, 0, maxv, n, C_NULL, C_NULL, C_NULL, pointer(verts),
+                       nverts === nothing ? Ptr{Int32}(C_NULL) : pointer(nverts))
+    return desc, (verts, nverts)
+end
+
+"""
+    grid(x)
+
+A grid descriptor (as returned by `curvilinear` / `cells`) for `x`: a
+descriptor itself, a `dim x (nx+1) x (ny+1)` vertex array, or an
+`(nx+1) x (ny+1)` matrix of points with 3 (unit sphere) or 2 (plane)
+coordinates each, such as the reference's `CellBasedGrid` point matrices of
+`UnitSphericalPoint`s.
+"""
+grid(x::Tuple{CrgGridDesc,Any}) = x
+grid(points::Array{Float64,3}) = curvilinear(points)
+function grid(points::AbstractMatrix)
+    dim = length(first(points))
+    p = Array{Float64,3}(undef, dim, size(points)...)
+    for I in CartesianIndices(points)
+        q = points[I]
+        length(q) == dim || throw(ArgumentError("every point needs $dim coordinates"))
+        for c in 1:dim
+            p[c, I] = q[c]
+        end
+    end
+    return curvilinear(p)
+end
+
+"""
+    build(dst, src; normalize = false) -> (A::GB300Sparse, dst_areas, src_areas)
+
+GPU build of `Regridder(dst, src; normalize)` (`crg_build`) for grid
+descriptors (see `grid`); the areas are host copies.
 """
 function build(dst, src; normalize::Bool = false)
-    d, keep_d = dst
-    s, keep_s = src
+    d, keep_d = grid(dst)
+    s, keep_s = grid(src)
     out = Ref{Ptr{Cvoid}}(C_NULL)
     opts = Ref(CrgBuildOpts(normalize, 0, C_NULL))
     GC.@preserve keep_d keep_s begin
@@ -129,25 +200,79 @@ function build(dst, src; normalize::Bool = false)
     return A, dst_areas, src_areas
 end
 
-"""
-    apply!(y, A, x; transpose = false, normalize = true, dims = 1)
+"Raw address of an array's first element plus `off` bytes: `Ptr` for host arrays, `CuPtr` for `CuArray`s."
+_raw(p, off::Integer = 0) = reinterpret(Ptr{Cvoid}, reinterpret(UInt, p) + UInt(off))
 
-`perform_regridding!` + `finalize_regridding!` for dense arrays: one call for
-all slices along the non-spatial axes (the reference loops `mul!` per slice).
+"The handle behind `A` and the C `transpose` flag of the direction `A` applies in."
+_direction(A::GB300Sparse) = (A, Int32(0))
+_direction(A::GB300SparseT) = (A.parent, Int32(1))
+
 """
-function apply!(y::AbstractArray{T}, A::Union{GB300Sparse,GB300SparseT}, x::AbstractArray{T};
-                normalize::Bool = true, dims::Int = 1) where {T<:Union{Float64,Float32}}
-    ndims(x) == ndims(y) || throw(DimensionMismatch("source and destination ranks must match"))
+    _slice_groups(f, x, y, dims)
+
+Cover every 1-D slice of `x` and `y` along `dims` with calls
+`f(xptr, x_stride_cell, x_stride_field, yptr, y_stride_cell, y_stride_field, nfields)`.
+The leading non-spatial axes whose strides chain (a dense array's axes before
+and after `dims` do, separately) go into one call as `nfields` fields; the
+remaining axes are looped over.  Dense arrays with `dims = 1` or
+`dims = ndims` therefore take one call.
+"""
+function _slice_groups(f, x::StridedArray{T}, y::StridedArray{T}, dims::Int) where {T}
+    other = Tuple(k for k in 1:ndims(x) if k != dims)
+    nf, fx, fy, run = 1, 1, 1, 0
+    for (r, k) in enumerate(other)
+        if r == 1
+            nf, fx, fy, run = size(x, k), stride(x, k), stride(y, k), 1
+        elseif stride(x, k) == fx * nf && stride(y, k) == fy * nf
+            nf *= size(x, k)
+            run = r
+        else
+            break
+        end
+    end
+    rest = other[run+1:end]
+    GC.@preserve x y for I in CartesianIndices(map(k -> size(x, k), rest))
+        ox = sum(ntuple(i -> (I[i] - 1) * stride(x, rest[i]), length(rest)); init = 0)
+        oy = sum(ntuple(i -> (I[i] - 1) * stride(y, rest[i]), length(rest)); init = 0)
+        f(_raw(pointer(x), ox * sizeof(T)), stride(x, dims), fx, _raw(pointer(y), oy * sizeof(T)), stride(y, dims), fy, nf)
+    end
+    return nothing
+end
+
+function _check_fields(y, x, dims, n_out, n_in)
+    ndims(x) == ndims(y) ||
+        throw(DimensionMismatch("source and destination ranks must match; got source rank $(ndims(x)) and destination rank $(ndims(y))"))
     1 <= dims <= ndims(x) || throw(ArgumentError("dims=$dims is out of range for a $(ndims(x))-dimensional array"))
-    h, t = A isa GB300SparseT ? (A.parent, Int32(1)) : (A, Int32(0))
-    sx, sy = strides(x), strides(y)
-    nf = length(x) ÷ size(x, dims)
-    fx = nf == 1 ? 1 : sx[dims == 1 ? 2 : 1]   # slices must be uniformly strided (dense arrays)
-    fy = nf == 1 ? 1 : sy[dims == 1 ? 2 : 1]
-    dtype = T === Float64 ? CRG_F64 : CRG_F32
-    check(ccall((:crg_apply, libcrg[]), Cint,
-                (Ptr{Cvoid}, Int32, Int32, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Int64, Int32, Ptr{Cvoid}),
-                h.ptr, t, dtype, pointer(x), sx[dims], fx, pointer(y), sy[dims], fy, nf, normalize, C_NULL))
+    (size(x, dims) == n_in && size(y, dims) == n_out) ||
+        throw(DimensionMismatch("regridder has size ($n_out, $n_in) but the source spatial axis has $(size(x, dims)) cells and the destination spatial axis has $(size(y, dims))"))
+    ox = Tuple(size(x, k) for k in 1:ndims(x) if k != dims)
+    oy = Tuple(size(y, k) for k in 1:ndims(y) if k != dims)
+    ox == oy ||
+        throw(DimensionMismatch("source and destination non-spatial axes must match; got source axes $ox and destination axes $oy"))
+    return nothing
+end
+
+_dtype(::Type{Float64}) = CRG_F64
+_dtype(::Type{Float32}) = CRG_F32
+
+"""
+    apply!(y, A, x; normalize = true, dims = 1)
+
+`perform_regridding!` + `finalize_regridding!` for strided arrays (host
+`Array`s or `CuArray`s): `y = (A x) ./ a_d` along the spatial axis `dims`
+for every slice along the other axes, in one library call for a dense array
+whose spatial axis is the first or the last (the reference loops `mul!` per
+slice, src/regridder/regrid.jl:303-318).  `A` may be a transposed view.
+"""
+function apply!(y::StridedArray{T}, A::Union{GB300Sparse,GB300SparseT}, x::StridedArray{T};
+                normalize::Bool = true, dims::Int = 1) where {T<:Union{Float64,Float32}}
+    _check_fields(y, x, dims, size(A)...)
+    h, t = _direction(A)
+    _slice_groups(x, y, dims) do xp, xsc, xsf, yp, ysc, ysf, nf
+        check(ccall((:crg_apply, libcrg[]), Cint,
+                    (Ptr{Cvoid}, Int32, Int32, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Int64, Int32, Ptr{Cvoid}),
+                    h.ptr, t, _dtype(T), xp, xsc, xsf, yp, ysc, ysf, nf, normalize, C_NULL))
+    end
     return y
 end
 
@@ -155,20 +280,42 @@ end
     adjoint!(gs, A, gd; normalize = true, dims = 1)
 
 Pullback of `apply!` with respect to the source field: `gs = A' (gd ./ a_d)`
-(or `A gd ./ ...` for a transposed view), through the other stored copy of A.
+(or `A (gd ./ a_s)` for a transposed view), through the other stored copy of
+A (`crg_apply_adjoint`, no atomics).
 """
-function adjoint!(gs::AbstractArray{T}, A::Union{GB300Sparse,GB300SparseT}, gd::AbstractArray{T};
+function adjoint!(gs::StridedArray{T}, A::Union{GB300Sparse,GB300SparseT}, gd::StridedArray{T};
                   normalize::Bool = true, dims::Int = 1) where {T<:Union{Float64,Float32}}
-    h, t = A isa GB300SparseT ? (A.parent, Int32(1)) : (A, Int32(0))
-    sx, sy = strides(gd), strides(gs)
-    nf = length(gd) ÷ size(gd, dims)
-    fx = nf == 1 ? 1 : sx[dims == 1 ? 2 : 1]
-    fy = nf == 1 ? 1 : sy[dims == 1 ? 2 : 1]
-    dtype = T === Float64 ? CRG_F64 : CRG_F32
-    check(ccall((:crg_apply_adjoint, libcrg[]), Cint,
-                (Ptr{Cvoid}, Int32, Int32, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Int64, Int32, Ptr{Cvoid}),
-                h.ptr, t, dtype, pointer(gd), sx[dims], fx, pointer(gs), sy[dims], fy, nf, normalize, C_NULL))
+    n_out, n_in = size(A)
+    _check_fields(gs, gd, dims, n_in, n_out)
+    h, t = _direction(A)
+    _slice_groups(gd, gs, dims) do xp, xsc, xsf, yp, ysc, ysf, nf
+        check(ccall((:crg_apply_adjoint, libcrg[]), Cint,
+                    (Ptr{Cvoid}, Int32, Int32, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Int64, Int32, Ptr{Cvoid}),
+                    h.ptr, t, _dtype(T), xp, xsc, xsf, yp, ysc, ysf, nf, normalize, C_NULL))
+    end
     return gs
+end
+
+# `mul!(y, R.intersections, x)` is the reference's perform_regridding!
+# (src/regridder/regrid.jl:95-98): A x without the division, which
+# finalize_regridding! then applies.  Vectors and matrices (columns = fields).
+LinearAlgebra.mul!(y::StridedVecOrMat{T}, A::Union{GB300Sparse,GB300SparseT}, x::StridedVecOrMat{T}) where {T<:Union{Float64,Float32}} =
+    apply!(y, A, x; normalize = false, dims = 1)
+
+function Base.:*(A::Union{GB300Sparse,GB300SparseT}, x::StridedVecOrMat{T}) where {T<:Union{Float64,Float32}}
+    y = similar(x, size(A, 1), size(x)[2:end]...)
+    return mul!(y, A, x)
+end
+
+"""
+    regrid(A, s; normalize = true, dims = 1) -> d
+
+Allocating `regrid!`: `d = (A s) ./ a_d` into a new array like `s`.  Its
+`ChainRulesCore.rrule` (package extension) pulls back through `adjoint!`.
+"""
+function regrid(A::Union{GB300Sparse,GB300SparseT}, s::StridedArray{T}; normalize::Bool = true, dims::Int = 1) where {T<:Union{Float64,Float32}}
+    d = similar(s, ntuple(k -> k == dims ? size(A, 1) : size(s, k), ndims(s)))
+    return apply!(d, A, s; normalize, dims)
 end
 
 """
@@ -180,9 +327,9 @@ Cotangent of the destination vertices for `sum_ij u_i s_j dA_ij/dV + sum_i c_i d
 (unnormalised areas `a`).
 """
 function area_grad(A::GB300Sparse, dst, src; row_weight = nothing, src_field = nothing, area_weight = nothing)
-    d, keep_d = dst
-    s, keep_s = src
-    g = zeros(Float64, d.kind == 0 ? size(keep_d[1]) : (Int(d.ncells) * Int(d.max_verts) * 3,))
+    d, keep_d = grid(dst)
+    s, keep_s = grid(src)
+    g = zeros(Float64, size(keep_d[1]))   # the vertex array's own layout
     ptr(v) = v === nothing ? Ptr{Float64}(C_NULL) : pointer(v)
     GC.@preserve keep_d keep_s row_weight src_field area_weight begin
         check(ccall((:crg_area_grad, libcrg[]), Cint,
@@ -191,6 +338,35 @@ function area_grad(A::GB300Sparse, dst, src; row_weight = nothing, src_field = n
                     A.ptr, Ref(d), Ref(s), ptr(row_weight), ptr(src_field), ptr(area_weight), g, C_NULL))
     end
     return g
+end
+
+"""
+    src_area_grad(dst, src, row_weight, src_field; swapped = nothing) -> Array{Float64}
+
+Cotangent of the SOURCE vertices for `sum_ij u_i s_j dA_ij/dW`, laid out like
+`src`'s vertex array.  `A_ij` is the area of (destination cell i) ∩ (source
+cell j), symmetric in the two cells, so this is `area_grad` of the regridder
+built the other way round, `build(src, dst)` (pass its `GB300Sparse` as
+`swapped` to reuse one), with the two weight vectors exchanged.
+"""
+function src_area_grad(dst, src, row_weight::Vector{Float64}, src_field::Vector{Float64}; swapped = nothing)
+    At = swapped === nothing ? build(src, dst)[1] : swapped
+    return area_grad(At, src, dst; row_weight = src_field, src_field = row_weight)
+end
+
+"""
+    regrid_on(V, W, s; normalize = false) -> d
+
+`d = regrid(R, s) = (A s) ./ a_d` with `R` built from the vertex arrays `V`
+(destination) and `W` (source), each `dim x (nx+1) x (ny+1)` (see
+`curvilinear`); FP64, one field.  It is a function of the coordinates as well
+as of `s`: its `ChainRulesCore.rrule` (package extension) returns the
+cotangents of `V` (`area_grad`), of `W` (`src_area_grad`) and of `s`
+(`adjoint!`).  Normalisation cancels in `d`.
+"""
+function regrid_on(V::Array{Float64,3}, W::Array{Float64,3}, s::Vector{Float64}; normalize::Bool = false)
+    A, _, _ = build(V, W; normalize)
+    return regrid(A, s)
 end
 
 """
