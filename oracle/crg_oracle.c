@@ -1155,6 +1155,289 @@ double og_cell_area_hook(int spherical, const double* v, int n) {
     return og_cell_area(spherical, p, n);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Forward-mode derivatives of the clip and area (dual numbers).            */
+/*                                                                          */
+/* The reference has no derivatives: its build writes Float64 buffers      */
+/* (src/regridder/intersection_areas.jl:14), so ForwardDiff cannot be       */
+/* pushed through it.  This is that experiment done on the oracle instead:  */
+/* every og_*_dn function runs exactly the value sequence of the FP64       */
+/* function of the same name above (same operations, fma placement and     */
+/* branch decisions, so the clipped polygon has the same structure) and     */
+/* carries the partial derivatives with respect to the three coordinates of */
+/* one vertex of the clip polygon (the destination cell).  It is the        */
+/* checker of the GPU area gradient.                                        */
+/* ------------------------------------------------------------------------ */
+
+typedef struct { double v, d[3]; } og_dn;
+typedef struct { og_dn x, y, z; } og_dv;
+
+static inline og_dn dn_k(double v) { og_dn r = {v, {0.0, 0.0, 0.0}}; return r; }
+static inline og_dn dn_add(og_dn a, og_dn b) {
+    og_dn r; r.v = a.v + b.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+static inline og_dn dn_sub(og_dn a, og_dn b) {
+    og_dn r; r.v = a.v - b.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+static inline og_dn dn_neg(og_dn a) {
+    og_dn r; r.v = -a.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+static inline og_dn dn_mul(og_dn a, og_dn b) {
+    og_dn r; r.v = a.v * b.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+/* a*b + c, the value rounded once as fma() */
+static inline og_dn dn_fma(og_dn a, og_dn b, og_dn c) {
+    og_dn r; r.v = fma(a.v, b.v, c.v);
+    for (int i = 0; i < 3; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i] + c.d[i];
+    return r;
+}
+static inline og_dn dn_div(og_dn a, og_dn b) {
+    og_dn r; r.v = a.v / b.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) / b.v;
+    return r;
+}
+static inline og_dn dn_sqrt(og_dn a) {
+    og_dn r; r.v = sqrt(a.v);
+    double h = r.v > 0.0 ? 0.5 / r.v : 0.0;
+    for (int i = 0; i < 3; ++i) r.d[i] = h * a.d[i];
+    return r;
+}
+static inline og_dn dn_abs(og_dn a) { return a.v < 0.0 ? dn_neg(a) : a; }
+
+static inline v3 dv_val(og_dv a) { v3 r = {a.x.v, a.y.v, a.z.v}; return r; }
+static inline og_dv dv_k(v3 a) { og_dv r = {dn_k(a.x), dn_k(a.y), dn_k(a.z)}; return r; }
+static inline og_dv dv_sub(og_dv a, og_dv b) { og_dv r = {dn_sub(a.x, b.x), dn_sub(a.y, b.y), dn_sub(a.z, b.z)}; return r; }
+/* og_dot */
+static inline og_dn dv_dot(og_dv a, og_dv b) { return dn_fma(a.x, b.x, dn_fma(a.y, b.y, dn_mul(a.z, b.z))); }
+/* og_cross (plain products) */
+static inline og_dv dv_cross(og_dv a, og_dv b) {
+    og_dv r;
+    r.x = dn_sub(dn_mul(a.y, b.z), dn_mul(a.z, b.y));
+    r.y = dn_sub(dn_mul(a.z, b.x), dn_mul(a.x, b.z));
+    r.z = dn_sub(dn_mul(a.x, b.y), dn_mul(a.y, b.x));
+    return r;
+}
+/* og_triple */
+static inline og_dn dv_triple(og_dv a, og_dv b, og_dv c) { return dv_dot(a, dv_cross(dv_sub(b, a), dv_sub(c, a))); }
+
+static og_dn og_side_sph_dn(og_dv nrm, og_dv ca, og_dv cb, double eb, int isig, og_dv v) {
+    og_dv w = dv_sub(v, ca);
+    og_dn s = dv_dot(nrm, w);
+    double bound = eb * (fabs(w.x.v) + fabs(w.y.v) + fabs(w.z.v)) + OG_TINY;
+    if (fabs(s.v) > bound) return s;
+    /* settled to its exact sign; the partials stay those of the FP64 value */
+    s.v = og_settle(s.v, bound, isig * og_det3_sign(dv_val(ca), dv_val(cb), dv_val(v)));
+    return s;
+}
+
+static og_dv og_isect_sph_dn(og_dv a, og_dn sa, og_dv b, og_dn sb) {
+    if (sa.v == 0.0) return a;
+    if (sb.v == 0.0) return b;
+    og_dn wa = dn_abs(sb), wb = dn_abs(sa);
+    og_dv x;
+    x.x = dn_fma(wb, b.x, dn_mul(wa, a.x));
+    x.y = dn_fma(wb, b.y, dn_mul(wa, a.y));
+    x.z = dn_fma(wb, b.z, dn_mul(wa, a.z));
+    og_dn ir = dn_div(dn_k(1.0), dn_sqrt(dv_dot(x, x)));
+    x.x = dn_mul(x.x, ir); x.y = dn_mul(x.y, ir); x.z = dn_mul(x.z, ir);
+    return x;
+}
+
+/* 2 arg(prod (D + iN)); d atan2(y, x) = (x dy - y dx) / (x^2 + y^2) */
+static og_dn og_area_sph_signed_dn(const og_dv* v, int m) {
+    if (m < 3) return dn_k(0.0);
+    og_dn re = dn_k(1.0), im = dn_k(0.0);
+    og_dv a = v[0];
+    for (int k = 1; k + 1 < m; ++k) {
+        og_dv b = v[k], c = v[k + 1];
+        og_dn N = dv_triple(a, b, c);
+        og_dn D = dn_add(dn_add(dn_add(dn_k(1.0), dv_dot(a, b)), dv_dot(b, c)), dv_dot(c, a));
+        og_dn re2 = dn_fma(re, D, dn_neg(dn_mul(im, N)));
+        og_dn im2 = dn_fma(re, N, dn_mul(im, D));
+        re = re2; im = im2;
+    }
+    og_dn r;
+    r.v = 2.0 * og_atan2(im.v, re.v);
+    double q = re.v * re.v + im.v * im.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = q > 0.0 ? 2.0 * (re.v * im.d[i] - im.v * re.d[i]) / q : 0.0;
+    return r;
+}
+
+static inline og_dn dn_cross2(og_dn ax, og_dn ay, og_dn bx, og_dn by) { return dn_sub(dn_mul(ax, by), dn_mul(ay, bx)); }
+
+static og_dn og_side_pl_dn(og_dv a, og_dv b, og_dn ex, og_dn ey, int isig, og_dv v) {
+    og_dn wx = dn_sub(v.x, a.x), wy = dn_sub(v.y, a.y);
+    og_dn s = dn_cross2(ex, ey, wx, wy);
+    if (isig < 0) s = dn_neg(s);
+    double bound = OG_U8 * (fabs(ex.v) * fabs(wy.v) + fabs(ey.v) * fabs(wx.v)) + OG_TINY;
+    if (fabs(s.v) > bound) return s;
+    s.v = og_settle(s.v, bound, isig * og_orient2_sign(a.x.v, a.y.v, b.x.v, b.y.v, v.x.v, v.y.v));
+    return s;
+}
+
+static og_dv og_isect_pl_dn(og_dv a, og_dn sa, og_dv b, og_dn sb) {
+    if (sa.v == 0.0) return a;
+    if (sb.v == 0.0) return b;
+    og_dn wa = dn_abs(sb), wb = dn_abs(sa);
+    og_dn w = dn_add(wa, wb);
+    og_dv x;
+    x.x = dn_div(dn_fma(wb, b.x, dn_mul(wa, a.x)), w);
+    x.y = dn_div(dn_fma(wb, b.y, dn_mul(wa, a.y)), w);
+    x.z = dn_k(0.0);
+    return x;
+}
+
+static og_dn og_area_pl_signed_dn(const og_dv* v, int m) {
+    if (m < 3) return dn_k(0.0);
+    og_dn s = dn_k(0.0);
+    for (int k = 1; k + 1 < m; ++k)
+        s = dn_add(s, dn_cross2(dn_sub(v[k].x, v[0].x), dn_sub(v[k].y, v[0].y),
+                                dn_sub(v[k + 1].x, v[0].x), dn_sub(v[k + 1].y, v[0].y)));
+    og_dn r; r.v = 0.5 * s.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = 0.5 * s.d[i];
+    return r;
+}
+
+/* og_clip_sph / og_clip_pl on dual vertices; the orientation of the clip
+ * polygon (a sign) is taken from the values. */
+static int og_clip_dn(int spherical, const og_dv* subj, int ns, const og_dv* clip, int nc, og_dv* res) {
+    og_dv ba[OG_MAXC], bb[OG_MAXC];
+    og_dv* in = ba; og_dv* out = bb;
+    v3 cv[OG_MAXV];
+    for (int i = 0; i < ns; ++i) in[i] = subj[i];
+    for (int k = 0; k < nc; ++k) cv[k] = dv_val(clip[k]);
+    int n = ns;
+    double sig = spherical ? og_orient_sph(cv, nc) : og_orient_pl(cv, nc);
+    int isig = sig < 0.0 ? -1 : 1;
+    for (int k = 0; k < nc && n > 0; ++k) {
+        og_dv ca = clip[k], cb = clip[(k + 1) % nc];
+        og_dv nrm = dv_k(cv[k]);
+        og_dn ex = dn_k(0.0), ey = dn_k(0.0);
+        double eb = 0.0;
+        if (spherical) {
+            og_dv d1 = dv_sub(cb, ca);
+            nrm = dv_cross(ca, d1);
+            if (sig < 0.0) { nrm.x = dn_neg(nrm.x); nrm.y = dn_neg(nrm.y); nrm.z = dn_neg(nrm.z); }
+            eb = OG_U32 * (fabs(ca.x.v) + fabs(ca.y.v) + fabs(ca.z.v)) * (fabs(d1.x.v) + fabs(d1.y.v) + fabs(d1.z.v));
+        } else {
+            ex = dn_sub(cb.x, ca.x);
+            ey = dn_sub(cb.y, ca.y);
+        }
+        int m = 0;
+        og_dv prev = in[n - 1];
+        og_dn sp = spherical ? og_side_sph_dn(nrm, ca, cb, eb, isig, prev) : og_side_pl_dn(ca, cb, ex, ey, isig, prev);
+        for (int i = 0; i < n; ++i) {
+            og_dv cur = in[i];
+            og_dn sc = spherical ? og_side_sph_dn(nrm, ca, cb, eb, isig, cur) : og_side_pl_dn(ca, cb, ex, ey, isig, cur);
+            if (sc.v >= 0.0) {
+                if (sp.v < 0.0) {
+                    if (m >= OG_MAXC) return -1;
+                    out[m++] = spherical ? og_isect_sph_dn(prev, sp, cur, sc) : og_isect_pl_dn(prev, sp, cur, sc);
+                }
+                if (m >= OG_MAXC) return -1;
+                out[m++] = cur;
+            } else if (sp.v >= 0.0) {
+                if (m >= OG_MAXC) return -1;
+                out[m++] = spherical ? og_isect_sph_dn(prev, sp, cur, sc) : og_isect_pl_dn(prev, sp, cur, sc);
+            }
+            prev = cur; sp = sc;
+        }
+        og_dv* t = in; in = out; out = t;
+        n = m;
+    }
+    for (int i = 0; i < n; ++i) res[i] = in[i];
+    return n;
+}
+
+/* Slot of vertex k of cell idx in the grid's vertex array: the point index
+ * ([points][dim], shared corners share a slot) of a curvilinear grid, or
+ * idx*maxv + k ([cells][maxv][dim]) of a polygon grid. */
+static int64_t og_vertex_slot(const og_grid* g, int64_t idx, int k) {
+    if (g->kind != OG_CURVI) return idx * g->maxv + k;
+    int b = 0;
+    while (b + 1 < g->nblocks && idx >= g->block_cell_off[b + 1]) b++;
+    int64_t loc = idx - g->block_cell_off[b];
+    int64_t nx = g->block_nx[b];
+    int64_t i = loc % nx + (k == 1 || k == 2), j = loc / nx + (k >= 2);
+    return g->block_point_off[b] + i + j * (nx + 1);
+}
+
+/* Cell idx of g as dual vertices with vertex `seed` carrying the unit partials
+ * (seed < 0: all constant). */
+static int og_cell_dn(const og_grid* g, int64_t idx, int seed, og_dv* out) {
+    v3 p[OG_MAXV];
+    int n = og_cell_verts(g, idx, p);
+    for (int k = 0; k < n; ++k) {
+        out[k] = dv_k(p[k]);
+        if (k == seed) { out[k].x.d[0] = 1.0; out[k].y.d[1] = 1.0; out[k].z.d[2] = 1.0; }
+    }
+    return n;
+}
+
+/* grad (zeroed first) = sum over the nonzeros of R of u_i s_j dA_ij/dV
+ *                     + sum_i c_i da_i/dV,
+ * with A_ij the unnormalised area of (destination cell i) ∩ (source cell j)
+ * -- the clip of subject = source cell j by clip = destination cell i, signed
+ * by the subject's orientation, as og_pair_area -- a_i the unnormalised area
+ * of destination cell i, and V the destination vertices laid out as
+ * og_vertex_slot numbers them (dim coordinates each: x, y, z on the sphere,
+ * x, y on the plane).  u and s may both be NULL (area term only); c may be
+ * NULL.  dst and src must be the grids R was built from.  Returns the number
+ * of pairs whose clip overflowed (left out). */
+int64_t og_area_grad(const og_regridder* R, const og_grid* dst, const og_grid* src, const double* u, const double* s,
+                     const double* c, double* grad) {
+    int spherical = dst->manifold == 1;
+    int dim = dst->dim;
+    int64_t nslots = dst->kind == OG_CURVI ? dst->block_point_off[dst->nblocks - 1] +
+                                                 (dst->block_nx[dst->nblocks - 1] + 1) * (dst->block_ny[dst->nblocks - 1] + 1)
+                                           : dst->ncells * dst->maxv;
+    memset(grad, 0, (size_t)(nslots * dim) * sizeof(double));
+    int64_t overflows = 0;
+    og_dv sv[OG_MAXV], dv[OG_MAXV], res[OG_MAXC];
+    v3 sp[OG_MAXV];
+    for (int64_t j = 0; u && s && j < R->ns; ++j) {
+        int nsv = og_cell_verts(src, j, sp);
+        for (int k = 0; k < nsv; ++k) sv[k] = dv_k(sp[k]);
+        double so = spherical ? og_orient_sph(sp, nsv) : og_orient_pl(sp, nsv);
+        for (int64_t q = R->colptr[j]; q < R->colptr[j + 1]; ++q) {
+            int64_t i = R->rowval[q];
+            double w = u[i] * s[j];
+            if (w == 0.0) continue;
+            int ndv = og_cell_dn(dst, i, -1, dv);
+            for (int k = 0; k < ndv; ++k) {
+                int nd = og_cell_dn(dst, i, k, dv);
+                int m = og_clip_dn(spherical, sv, nsv, dv, nd, res);
+                if (m < 0) { overflows++; break; }
+                og_dn a = spherical ? og_area_sph_signed_dn(res, m) : og_area_pl_signed_dn(res, m);
+                int64_t slot = og_vertex_slot(dst, i, k);
+                for (int e = 0; e < dim; ++e) grad[slot * dim + e] += w * so * a.d[e];
+            }
+        }
+    }
+    for (int64_t i = 0; c && i < R->nd; ++i) {
+        if (c[i] == 0.0) continue;
+        int nd = og_cell_dn(dst, i, -1, dv);
+        v3 p[OG_MAXV];
+        for (int k = 0; k < nd; ++k) p[k] = dv_val(dv[k]);
+        double o = spherical ? og_orient_sph(p, nd) : og_orient_pl(p, nd);
+        for (int k = 0; k < nd; ++k) {
+            og_cell_dn(dst, i, k, dv);
+            og_dn a = spherical ? og_area_sph_signed_dn(dv, nd) : og_area_pl_signed_dn(dv, nd);
+            int64_t slot = og_vertex_slot(dst, i, k);
+            for (int e = 0; e < dim; ++e) grad[slot * dim + e] += c[i] * o * a.d[e];
+        }
+    }
+    return overflows;
+}
+
 int og_num_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

@@ -89,6 +89,7 @@ def load() -> C.CDLL:
                 "og_se_inverse_hook": (None, [vp, vp, vp]),
                 "og_se_nodes_hook": (None, [vp, C.c_int, dbl, vp, vp]),
                 "og_se_poly_b_hook": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, vp]),
+                "og_area_grad": (i64, [vp, C.POINTER(og_grid), C.POINTER(og_grid), vp, vp, vp, vp]),
             }
             for n, (r, a) in sig.items():
                 f = getattr(lib, n)
@@ -181,6 +182,32 @@ class OracleRegridder:
         load().og_apply(self._h, int(transpose), s2.ctypes.data, 1, s2.shape[1], out.ctypes.data, 1, nout,
                         s2.shape[0], int(bool(normalize)), int(nthreads))
         return out[0] if one else out
+
+
+def area_grad(R: OracleRegridder, dst, src, row_weight=None, src_field=None, area_weight=None) -> np.ndarray:
+    """Forward-mode (dual-number) derivatives through the oracle's own clip
+    and area: sum_ij row_weight[i] src_field[j] dA_ij/dV + sum_i area_weight[i]
+    da_i/dV over the destination vertices V of the grids R was built from
+    (unnormalised areas), laid out like the library's crg_area_grad: (npoints,
+    dim) in block order for curvilinear grids, (ncells, max_verts, dim) for
+    polygon grids."""
+    lib = load()
+    dd, k1 = _desc(dst)
+    ds, k2 = _desc(src)
+    vec = lambda x, n: None if x is None else np.ascontiguousarray(x, np.float64).reshape(n)
+    u, s, c = vec(row_weight, R.nd), vec(src_field, R.ns), vec(area_weight, R.nd)
+    if (u is None) != (s is None):
+        raise ValueError("row_weight and src_field are given together")
+    if dst.kind == "curvilinear":
+        out = np.empty((sum(b.shape[0] * b.shape[1] for b in dst.blocks), dd.dim))
+    else:
+        out = np.empty(np.asarray(dst.cells).shape)
+    ptr = lambda a: None if a is None else a.ctypes.data
+    ovf = lib.og_area_grad(R._h, C.byref(dd), C.byref(ds), ptr(u), ptr(s), ptr(c), out.ctypes.data)
+    del k1, k2
+    if ovf:
+        raise RuntimeError(f"{ovf} clips overflowed")
+    return out
 
 
 def candidates(dst, src, use_tree=True, nthreads=0) -> np.ndarray:
