@@ -11,6 +11,7 @@
 // from several host threads: with host fields, the copies of one item
 // overlap those of the others on both directions of the host link.
 #include <algorithm>
+#include <cstdio>
 #include <atomic>
 #include <string>
 #include <thread>
@@ -32,6 +33,13 @@ void build_batch_impl(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* 
   CRG_REQUIRE(n == 0 || (dst && src && out), CRG_ERR_INVALID_ARGUMENT, "dst, src and out must not be NULL");
   for (int64_t k = 0; k < n; ++k) out[k] = nullptr;
   if (n == 0) return;
+  for (int64_t k = 0; k < n; ++k) {
+    char which[48];
+    snprintf(which, sizeof which, "item %lld destination", (long long)k);
+    check_grid_desc(&dst[k], which);
+    snprintf(which, sizeof which, "item %lld source", (long long)k);
+    check_grid_desc(&src[k], which);
+  }
   int dev = 0;
   CRG_CHECK_CUDA(cudaGetDevice(&dev));
   const int workers = (int)std::min<int64_t>(n, nthreads > 0 ? nthreads : 8);

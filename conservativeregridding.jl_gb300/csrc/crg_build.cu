@@ -1513,12 +1513,45 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
   }
 }
 
+void check_grid_desc(const crg_grid_desc* g, const char* which) {
+  CRG_REQUIRE(g != nullptr, CRG_ERR_INVALID_ARGUMENT, "%s grid descriptor is NULL", which);
+  CRG_REQUIRE(g->manifold == CRG_PLANAR || g->manifold == CRG_SPHERICAL, CRG_ERR_INVALID_ARGUMENT,
+              "%s grid: unknown manifold %d", which, g->manifold);
+  CRG_REQUIRE(g->ncells >= 0 && g->ncells < (int64_t)1 << 31, CRG_ERR_NOT_SUPPORTED,
+              "%s grid: ncells = %lld is outside [0, 2^31)", which, (long long)g->ncells);
+  if (g->kind == CRG_GRID_CURVILINEAR) {
+    CRG_REQUIRE(g->nblocks >= 1 && g->nblocks <= kMaxBlocks, CRG_ERR_INVALID_ARGUMENT,
+                "%s grid: nblocks = %d must be in 1..%d", which, g->nblocks, kMaxBlocks);
+    CRG_REQUIRE(g->block_nx && g->block_ny && g->points, CRG_ERR_INVALID_ARGUMENT,
+                "%s grid: curvilinear grid arrays are NULL", which);
+    int64_t cells = 0;
+    for (int b = 0; b < g->nblocks; ++b) {
+      const int64_t nx = g->block_nx[b], ny = g->block_ny[b];
+      CRG_REQUIRE(nx >= 1 && ny >= 1 && nx < (int64_t)1 << 31 && ny < (int64_t)1 << 31, CRG_ERR_INVALID_ARGUMENT,
+                  "%s grid: block %d has %lld x %lld cells", which, b, (long long)nx, (long long)ny);
+      cells += nx * ny;  // < 2^62 + 2^31: no overflow
+      CRG_REQUIRE(cells <= g->ncells, CRG_ERR_DIMENSION_MISMATCH,
+                  "%s grid: ncells = %lld but the blocks hold more cells", which, (long long)g->ncells);
+    }
+    CRG_REQUIRE(cells == g->ncells, CRG_ERR_DIMENSION_MISMATCH, "%s grid: ncells = %lld but the blocks hold %lld cells",
+                which, (long long)g->ncells, (long long)cells);
+  } else if (g->kind == CRG_GRID_CELLS) {
+    CRG_REQUIRE(g->max_verts >= 3 && g->max_verts <= CRG_MAXV, CRG_ERR_INVALID_ARGUMENT,
+                "%s grid: max_verts = %d must be in 3..%d", which, g->max_verts, CRG_MAXV);
+    CRG_REQUIRE(g->cell_verts || g->ncells == 0, CRG_ERR_INVALID_ARGUMENT, "%s grid: cell_verts is NULL", which);
+  } else {
+    CRG_REQUIRE(false, CRG_ERR_INVALID_ARGUMENT, "%s grid: unknown grid kind %d", which, g->kind);
+  }
+}
+
 crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts) {
   CRG_REQUIRE(dst && src, CRG_ERR_INVALID_ARGUMENT, "dst and src grids must not be NULL");
   CRG_REQUIRE(dst->manifold == src->manifold, CRG_ERR_INVALID_ARGUMENT,
               "Destination and source manifolds must be the same (got %d and %d); promote planar lon/lat to the sphere first",
               dst->manifold, src->manifold);
   CRG_REQUIRE(!opts || opts->flags == 0, CRG_ERR_INVALID_ARGUMENT, "crg_build_opts.flags must be 0");
+  check_grid_desc(dst, "destination");
+  check_grid_desc(src, "source");
   const bool sph = dst->manifold == CRG_SPHERICAL;
   cudaStream_t st = opts ? (cudaStream_t)opts->stream : nullptr;
   const int normalize = opts ? opts->normalize : 0;

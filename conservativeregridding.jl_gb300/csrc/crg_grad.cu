@@ -188,6 +188,8 @@ void area_grad_impl(const crg_regridder* r, const crg_grid_desc* dst, const crg_
   CRG_REQUIRE(grad != nullptr, CRG_ERR_INVALID_ARGUMENT, "gradient array is NULL");
   CRG_REQUIRE((u == nullptr) == (s == nullptr), CRG_ERR_INVALID_ARGUMENT,
               "row_weight and src_field are given together (or both NULL)");
+  check_grid_desc(dst, "destination");
+  check_grid_desc(src, "source");
   int dev = 0;
   CRG_CHECK_CUDA(cudaGetDevice(&dev));
   CRG_REQUIRE(dev == r->device, CRG_ERR_INVALID_ARGUMENT, "regridder lives on device %d but device %d is current",

@@ -150,6 +150,10 @@ struct crg_regridder {
 namespace crg {
 // crg_build_impl lives in crg_build.cu; apply entry points in crg_apply.cu.
 crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts);
+// Host-only checks of a grid descriptor (kind, manifold, sizes, NULL arrays),
+// run by the entry points before any device work; `which` names the grid in
+// the message.
+void check_grid_desc(const crg_grid_desc* g, const char* which);
 void free_regridder(crg_regridder* r);
 // Streams and events shared by the applies of a batch with host fields: the
 // chunks of all items form one pipeline (copies in on cin, applies on cst,

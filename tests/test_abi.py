@@ -67,3 +67,76 @@ def test_build_is_sm103a_and_in_tree():
     assert any("sm_103a" in f for f in _build.ARCH_FLAGS)
     assert "--fmad=false" in _build.NVCC_FLAGS
     assert _build.LIB_PATH.is_relative_to(ROOT)
+
+
+def _curvi(nx, ny, pts, manifold=None):
+    d = _lib.crg_grid_desc()
+    d.kind = _lib.CRG_GRID_CURVILINEAR
+    d.manifold = _lib.CRG_SPHERICAL if manifold is None else manifold
+    d.nblocks = 1
+    d.ncells = nx * ny
+    bx = (C.c_int64 * 1)(nx)
+    by = (C.c_int64 * 1)(ny)
+    d.block_nx = C.cast(bx, C.POINTER(C.c_int64))
+    d.block_ny = C.cast(by, C.POINTER(C.c_int64))
+    d.points = pts.ctypes.data
+    return d, (bx, by, pts)
+
+
+def test_build_checks_grid_descriptors_before_device_work():
+    """crg_build and crg_build_batch refuse malformed grids with the reference's
+    error classes (ArgumentError / DimensionMismatch, src/regridder/regrid.jl:242-245,
+    :289-296) before any CUDA call, so they answer the same without a GPU."""
+    import numpy as np
+
+    lib = _lib.load()
+    pts = np.zeros((3, 3, 3))
+    good, keep = _curvi(2, 2, pts)
+    out = C.c_void_p()
+
+    def build(dst, src=good):
+        st = lib.crg_build(C.byref(dst), C.byref(src), None, C.byref(out))
+        assert out.value is None
+        return st, lib.crg_last_error().decode()
+
+    bad, k1 = _curvi(2, 2, pts)
+    bad.manifold = 7
+    st, msg = build(good, bad)
+    assert st == _lib.CRG_ERR_INVALID_ARGUMENT and "manifold" in msg
+    bad, k1 = _curvi(2, 2, pts)
+    bad.nblocks = 0
+    assert build(bad) == (_lib.CRG_ERR_INVALID_ARGUMENT, "destination grid: nblocks = 0 must be in 1..12")
+    bad, k1 = _curvi(2, 2, pts)
+    bad.ncells = 5
+    st, msg = build(bad)
+    assert st == _lib.CRG_ERR_DIMENSION_MISMATCH and "ncells = 5" in msg
+    bad, k1 = _curvi(0, 2, pts)
+    st, msg = build(good, bad)
+    assert st == _lib.CRG_ERR_INVALID_ARGUMENT and msg.startswith("source grid: block 0 has 0 x 2 cells")
+    bad, k1 = _curvi(2, 2, pts)
+    bad.points = None
+    assert build(bad)[0] == _lib.CRG_ERR_INVALID_ARGUMENT
+    bad, k1 = _curvi(2, 2, pts)
+    bad.ncells = -1
+    assert build(bad)[0] == _lib.CRG_ERR_NOT_SUPPORTED
+    cells = _lib.crg_grid_desc()
+    cells.kind = _lib.CRG_GRID_CELLS
+    cells.manifold = _lib.CRG_SPHERICAL
+    cells.ncells = 4
+    cells.max_verts = 9
+    st, msg = build(cells)
+    assert st == _lib.CRG_ERR_INVALID_ARGUMENT and "max_verts = 9" in msg
+    cells.max_verts = 4
+    st, msg = build(cells)
+    assert st == _lib.CRG_ERR_INVALID_ARGUMENT and "cell_verts is NULL" in msg
+    cells.kind = 5
+    assert build(cells)[0] == _lib.CRG_ERR_INVALID_ARGUMENT
+    # a batch names the failing item and leaves every output NULL
+    dsts = (_lib.crg_grid_desc * 2)(good, good)
+    bad, k1 = _curvi(2, 2, pts)
+    bad.nblocks = 13
+    srcs = (_lib.crg_grid_desc * 2)(good, bad)
+    outs = (C.c_void_p * 2)(1, 1)
+    assert lib.crg_build_batch(2, dsts, srcs, None, 1, outs) == _lib.CRG_ERR_INVALID_ARGUMENT
+    assert lib.crg_last_error().decode().startswith("item 1 source grid: nblocks = 13")
+    assert list(outs) == [None, None]
