@@ -35,9 +35,9 @@ void build_batch_impl(int64_t n, const crg_grid_desc* dst, const crg_grid_desc* 
   if (n == 0) return;
   for (int64_t k = 0; k < n; ++k) {
     char which[48];
-    snprintf(which, sizeof which, "item %lld destination", (long long)k);
+    snprintf(which, sizeof which, "pair %lld: destination", (long long)k);
     check_grid_desc(&dst[k], which);
-    snprintf(which, sizeof which, "item %lld source", (long long)k);
+    snprintf(which, sizeof which, "pair %lld: source", (long long)k);
     check_grid_desc(&src[k], which);
   }
   int dev = 0;

@@ -138,5 +138,5 @@ def test_build_checks_grid_descriptors_before_device_work():
     srcs = (_lib.crg_grid_desc * 2)(good, bad)
     outs = (C.c_void_p * 2)(1, 1)
     assert lib.crg_build_batch(2, dsts, srcs, None, 1, outs) == _lib.CRG_ERR_INVALID_ARGUMENT
-    assert lib.crg_last_error().decode().startswith("item 1 source grid: nblocks = 13")
+    assert lib.crg_last_error().decode().startswith("pair 1: source grid: nblocks = 13")
     assert list(outs) == [None, None]
