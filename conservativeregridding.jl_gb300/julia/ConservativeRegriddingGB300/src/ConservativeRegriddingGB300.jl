@@ -26,6 +26,8 @@ using Libdl
 using SparseArrays
 using LinearAlgebra
 
+export GB300, GB300Sparse, GB300SparseT
+
 const libcrg = Ref{String}("")
 
 function __init__()
