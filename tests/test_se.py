@@ -128,3 +128,32 @@ def test_se_to_se_is_rejected():
     s = SpectralElementSpace.cubed_sphere(2, 3)
     with pytest.raises(ArgumentError, match="SE → SE"):
         Regridder(s, s)
+
+
+@pytest.mark.parametrize("ne,nq", [(2, 3), (3, 4), (4, 5)])
+def test_dss_groups_match_the_cubed_sphere_topology(ne, nq):
+    """The host's grouping of coincident nodes (the DSS of ClimaCore's
+    weighted_dss!, ext/ConservativeRegriddingClimaCoreExt.jl:709-715), fed the
+    oracle's node positions: a cubed sphere with ne x ne elements per face and
+    nq x nq nodes per element has 6 ne^2 (nq-1)^2 + 2 distinct points; shared
+    edge nodes come in pairs, element corners in fours, and the 8 cube corners
+    in threes."""
+    from crg import SpectralElementSpace
+
+    space = SpectralElementSpace.cubed_sphere(ne, nq)
+    cells, _ = space.elements.cell_table()
+    space._points = np.concatenate([oracle.se_nodes(c, nq)[0] for c in cells])
+    ptr, nodes = space.dss_groups()
+    sizes = np.diff(ptr)
+    assert space.nnodes - int(np.sum(sizes - 1)) == 6 * ne * ne * (nq - 1) ** 2 + 2
+    assert set(sizes.tolist()) <= {2, 3, 4}
+    # Euler: the element mesh has 6 ne^2 + 2 vertices (8 of valence 3) and 12 ne^2 edges
+    assert int(np.sum(sizes == 3)) == 8
+    assert int(np.sum(sizes == 4)) == 6 * ne * ne - 6
+    assert int(np.sum(sizes == 2)) == 12 * ne * ne * (nq - 2)
+    assert len(np.unique(nodes)) == len(nodes)
+    for g in range(len(sizes)):
+        members = nodes[ptr[g]:ptr[g + 1]]
+        assert np.all(np.diff(members) > 0)
+        p = space._points[members]
+        assert np.max(np.abs(p - p[0])) < 1e-9
