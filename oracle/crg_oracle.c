@@ -1,7 +1,7 @@
 /*
  * crg_oracle.c -- CPU oracle for the conservative-regridding hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: tests/, the smoke
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: tests/, the smoke
  * check in __graft_entry__.py and the cpu_baseline / reference legs of
  * bench.py load it; the product library never links, includes or calls it.
  *
@@ -1166,7 +1166,7 @@ double og_cell_area_hook(int spherical, const double* v, int n) {
 /* branch decisions, so the clipped polygon has the same structure) and     */
 /* carries the partial derivatives with respect to the three coordinates of */
 /* one vertex of the clip polygon (the destination cell).  It is the        */
-/* checker of the GPU area gradient.                                        */
+/* oracle of the GPU area gradient's tests.                                 */
 /* ------------------------------------------------------------------------ */
 
 typedef struct { double v, d[3]; } og_dn;

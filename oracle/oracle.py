@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (crg_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: the checker for tests/, the smoke check and the
-CPU-baseline / reference legs of bench.py.  The product library never uses it.
+TEST INFRASTRUCTURE ONLY: the oracle that tests/, the smoke check and the
+CPU-baseline / reference legs of bench.py compare against.  The product library never uses it.
 
 The oracle restates ConservativeRegridding.jl's build (treeify + threaded
 dual DFS + per-pair clip/area + sparse()) and apply (stdlib CSC mul! then

@@ -1,6 +1,6 @@
 """The oracle against the reference's known answers and independent
-high-precision values (CPU only).  This pins the checker before it is used to
-judge the CUDA kernels."""
+high-precision values (CPU only).  This pins the oracle before the CUDA kernels
+are compared with it."""
 from __future__ import annotations
 
 import json

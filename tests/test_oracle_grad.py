@@ -1,7 +1,7 @@
 """The oracle's forward-mode (dual-number) area derivatives, pinned on the
 CPU: exact shoelace gradients on the plane, and central finite differences
 of the oracle's own build on the sphere (curvilinear and polygon grids).
-These derivatives are the checker of the GPU's crg_area_grad
+These derivatives are the reference values of the GPU's crg_area_grad
 (tests/test_gpu_vertex_grad_oracle.py).  The reference has no derivatives,
 and its build does not accept dual numbers (it writes Float64 buffers), so
 the oracle stands in for "ForwardDiff through the CPU path"."""
