@@ -374,12 +374,14 @@ end
 """
     build_batch(pairs; normalize = false, nthreads = 0) -> Vector{GB300Sparse}
 
-`crg_build_batch`: many `(dst, src)` descriptor pairs built concurrently.
+`crg_build_batch`: many `(dst, src)` pairs built concurrently (each grid
+anything `grid` accepts).
 """
 function build_batch(pairs; normalize::Bool = false, nthreads::Integer = 0)
     n = length(pairs)
-    dd = [p[1][1] for p in pairs]; ds = [p[2][1] for p in pairs]
-    keep = [(p[1][2], p[2][2]) for p in pairs]
+    gp = [(grid(p[1]), grid(p[2])) for p in pairs]
+    dd = [g[1][1] for g in gp]; ds = [g[2][1] for g in gp]
+    keep = [(g[1][2], g[2][2]) for g in gp]
     out = Vector{Ptr{Cvoid}}(undef, n)
     opts = Ref(CrgBuildOpts(normalize, 0, C_NULL))
     GC.@preserve keep begin
