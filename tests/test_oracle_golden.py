@@ -158,3 +158,63 @@ def test_disjoint_grids_have_empty_matrix():
     R = oracle.OracleRegridder(a, b)
     assert R.nnz == 0
     assert np.array_equal(R.colptr, [0, 0, 0])
+
+
+def _ring_centres(nside):
+    """Pixel centres in ring order from the ring-scheme closed forms of
+    Gorski et al. (2005), ApJ 622:759, section 4: polar caps z = +-(1 - i^2 /
+    (3 N^2)), phi = (j - 1/2) pi / (2 i); equatorial belt z = 4/3 - 2 i / (3 N),
+    phi = (j - f) pi / (2 N) with f = 1 for odd i + N, else 1/2."""
+    N = nside
+    npix, ncap = 12 * N * N, 2 * N * (N - 1)
+    z, phi = np.empty(npix), np.empty(npix)
+    for r in range(npix):
+        if r < ncap:
+            i = (1 + int(np.sqrt(1 + 2 * r))) // 2
+            j = r + 1 - 2 * i * (i - 1)
+            z[r], phi[r] = 1 - i * i / (3.0 * N * N), (j - 0.5) * np.pi / (2 * i)
+        elif r < npix - ncap:
+            i = (r - ncap) // (4 * N) + N
+            j = (r - ncap) % (4 * N) + 1
+            f = 1.0 if (i + N) % 2 else 0.5
+            z[r], phi[r] = 4.0 / 3.0 - 2.0 * i / (3.0 * N), (j - f) * np.pi / (2 * N)
+        else:
+            q = npix - r
+            i = (1 + int(np.sqrt(2 * q - 1))) // 2
+            j = 4 * i + 1 - (q - 2 * i * (i - 1))
+            z[r], phi[r] = -1 + i * i / (3.0 * N * N), (j - 0.5) * np.pi / (2 * i)
+    s = np.sqrt((1 - z) * (1 + z))
+    return np.stack([s * np.cos(phi), s * np.sin(phi), z], axis=1)
+
+
+@pytest.mark.parametrize("nside", [1, 2, 4, 8, 16])
+def test_healpix_face_map_and_ring_order_match_the_published_centres(nside):
+    """The face map that places the corners, evaluated at the middle of each
+    nested pixel (face coordinates (ix + 1/2, iy + 1/2) / N), and the
+    nested -> ring permutation, reproduce the published ring-order pixel
+    centres: the corner geometry is pinned independently of its two codings."""
+    pix = np.arange(12 * nside * nside)
+    ix, iy, face = grids.healpix_nest2xyf(nside, pix)
+    mid = grids._hp_loc2vec((ix + 0.5) / nside, (iy + 0.5) / nside, face)
+    ring = grids.healpix_nest2ring(nside, pix)
+    want = _ring_centres(nside)[ring]
+    assert np.max(np.abs(mid - want)) < 1e-13
+
+
+def test_healpix_base_pixel_corners():
+    """nside 1: the 12 base pixels have 14 distinct corners -- the poles,
+    z = +-2/3 at longitudes 0, 90, 180, 270 and z = 0 at 45 + 90 k -- and each
+    pixel lists them north, west, south, east (z of N >= W, E >= S)."""
+    c = grids.healpix_corners_nested(1, np.arange(12))
+    pts = np.unique(np.round(c.reshape(-1, 3), 12), axis=0)
+    want = [(0.0, 0.0, 1.0), (0.0, 0.0, -1.0)]
+    s = np.sqrt(1 - 4.0 / 9.0)
+    for k in range(4):
+        a = np.pi / 2 * k
+        want += [(s * np.cos(a), s * np.sin(a), 2.0 / 3.0), (s * np.cos(a), s * np.sin(a), -2.0 / 3.0),
+                 (np.cos(a + np.pi / 4), np.sin(a + np.pi / 4), 0.0)]
+    want = np.unique(np.round(np.array(want), 12), axis=0)
+    assert pts.shape == (14, 3) and np.allclose(pts, want, atol=1e-12)
+    z = c[:, :, 2]
+    assert np.all(z[:, 0] >= z[:, 1] - 1e-15) and np.all(z[:, 0] >= z[:, 3] - 1e-15)
+    assert np.all(z[:, 2] <= z[:, 1] + 1e-15) and np.all(z[:, 2] <= z[:, 3] + 1e-15)
