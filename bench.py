@@ -56,10 +56,11 @@ def parse():
     p.add_argument("--pair", default="c5", choices=["c5", "identity"],
                    help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
                         "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
-    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1", "se"],
+    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1", "c4", "se"],
                    help="c5: the headline (HEALPix 256 <-> 0.25 degree, 128 fields); c3: 32 jittered lon-lat "
                         "pairs of uneven resolution built as one batch and applied as one CUDA graph; c1: the "
-                        "small FP64 case (2 degree -> shifted 3 degree lon-lat), build and plain FP64 apply; se: "
+                        "small FP64 case (2 degree -> shifted 3 degree lon-lat), build and plain FP64 apply; c4: the "
+                        "differentiation case (jittered C96 <- 1 degree): adjoint apply and vertex gradients; se: "
                         "spectral-element C48 (nq 4) <-> 0.5 degree lon-lat, both builds, the oracle's beside them")
     return p.parse_args()
 
@@ -681,6 +682,78 @@ def run_c1(a):
                            "note": "one launch of ~16 K rows: launch-latency bound"}}
 
 
+def run_c4(a):
+    """Differentiation: jittered C96 cubed sphere (vertices moved by U(-0.15,
+    0.15) cell widths, seed 11) <- 1-degree lon-lat, FP64, one field.  The
+    adjoint apply A^T (g ./ a) in GB/s (bytes 12 nnz + 4 (rows + 1) +
+    8 (cols + rows) + 8 rows, CUDA events over 200 launches), and the median
+    wall time of the destination-vertex area gradient (crg_area_grad), the
+    source-vertex one (crg_area_grad of the swapped regridder, built once)
+    and the whole pullback of L = sum w d^2 (host arrays in and out)."""
+    import torch
+
+    from crg import Regridder, area_grad, grids, regrid_, regrid_adjoint_, regrid_pullback, src_area_grad
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    dst, src = grids.cubed_sphere(96, jitter=0.15, seed=11), grids.lonlat_regular(1.0, 1.0)
+    R = Regridder(dst, src, normalize=True)
+    times = []
+    for _ in range(5):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        R = Regridder(dst, src, normalize=True)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    tb = statistics.median(times)
+    nd, ns = R.shape
+    rng = np.random.default_rng(2024)
+    s, w = rng.standard_normal(ns), rng.standard_normal(nd)
+    d = np.zeros(nd)
+    regrid_(d, R, s)
+    g = 2.0 * w * d
+    gd = torch.from_numpy(g).to(dev)
+    sb = torch.empty(ns, dtype=torch.float64, device=dev)
+    for _ in range(max(a.warmup, 3)):
+        regrid_adjoint_(sb, R, gd)
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 200
+    e0.record(stream)
+    for _ in range(reps):
+        regrid_adjoint_(sb, R, gd)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = 12 * R.nnz + 4 * (ns + 1) + 8 * (nd + ns) + 8 * nd
+    a_un = R.dst_areas * (R.info["normalizer"] if R.info["normalized"] else 1.0)
+    u, c = g / a_un, -g * d / a_un
+    Rs = Regridder(src, dst)
+
+    def median_s(fn, n=5):
+        fn()
+        out = []
+        for _ in range(n):
+            t0 = time.perf_counter()
+            fn()
+            out.append(time.perf_counter() - t0)
+        return statistics.median(out)
+
+    t_v = median_s(lambda: area_grad(R, dst, src, u, s, c))
+    t_w = median_s(lambda: src_area_grad(dst, src, u, s, swapped=Rs))
+    t_p = median_s(lambda: regrid_pullback(R, dst, src, s, g, wrt_src=True, swapped=Rs), n=3)
+    return {"metric": "differentiation: adjoint apply GB/s and vertex-gradient times",
+            "workload": "jittered C96 cubed sphere <- lonlat 1deg, fp64, 1 field",
+            "n_dst": nd, "n_src": ns, "nnz": R.nnz,
+            "build": {"ms_median": round(tb * 1e3, 3), "pairs_per_s": round(R.nnz / tb, 1)},
+            "adjoint_fp64": {"ms": round(ms, 4), "GB/s": round(nbytes / (ms * 1e-3) / 1e9, 2)},
+            "area_grad_dst": {"ms_median": round(t_v * 1e3, 3), "nonzeros_per_s": round(R.nnz / t_v, 1),
+                              "note": "host arrays in and out; 4 destination vertices per nonzero, one dual pass each"},
+            "area_grad_src": {"ms_median": round(t_w * 1e3, 3), "nonzeros_per_s": round(Rs.nnz / t_w, 1)},
+            "pullback_all": {"ms_median": round(t_p * 1e3, 3),
+                             "note": "apply + adjoint + both vertex gradients (swapped regridder reused)"}}
+
+
 def run_se(a):
     """Spectral-element C48 space with 4 x 4 GLL nodes per element (ClimaCore
     CubedSphereSpace(h_elem = 48, n_quad_points = 4)) and the 0.5-degree
@@ -814,9 +887,9 @@ def main():
     if a.profile:
         run_profile(a)
         return
-    if a.workload in ("c3", "c1", "se"):
+    if a.workload in ("c3", "c1", "c4", "se"):
         if rank == 0:
-            print(json.dumps({"c3": run_c3, "c1": run_c1, "se": run_se}[a.workload](a)))
+            print(json.dumps({"c3": run_c3, "c1": run_c1, "c4": run_c4, "se": run_se}[a.workload](a)))
         return
     if a.impl == "reference":
         if rank == 0:
