@@ -1148,6 +1148,15 @@ double og_pair_area_hook(int spherical, const double* s, int ns, const double* d
     return og_pair_area(spherical, sv, ns, dv, nd, ovf);
 }
 
+int og_det3_sign_hook(const double* a, const double* b, const double* c) {
+    v3 va = {a[0], a[1], a[2]}, vb = {b[0], b[1], b[2]}, vc = {c[0], c[1], c[2]};
+    return og_det3_sign(va, vb, vc);
+}
+
+int og_orient2_sign_hook(double ax, double ay, double bx, double by, double vx, double vy) {
+    return og_orient2_sign(ax, ay, bx, by, vx, vy);
+}
+
 double og_cell_area_hook(int spherical, const double* v, int n) {
     v3 p[OG_MAXV];
     int dim = spherical ? 3 : 2;

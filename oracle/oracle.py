@@ -90,6 +90,8 @@ def load() -> C.CDLL:
                 "og_se_nodes_hook": (None, [vp, C.c_int, dbl, vp, vp]),
                 "og_se_poly_b_hook": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, vp]),
                 "og_area_grad": (i64, [vp, C.POINTER(og_grid), C.POINTER(og_grid), vp, vp, vp, vp]),
+                "og_det3_sign_hook": (C.c_int, [vp, vp, vp]),
+                "og_orient2_sign_hook": (C.c_int, [dbl, dbl, dbl, dbl, dbl, dbl]),
             }
             for n, (r, a) in sig.items():
                 f = getattr(lib, n)
@@ -236,6 +238,18 @@ def pair_area(s, d, spherical=True) -> float:
 def cell_area(v, spherical=True) -> float:
     v = np.ascontiguousarray(v, np.float64)
     return load().og_cell_area_hook(int(spherical), v.ctypes.data, len(v))
+
+
+def det3_sign(a, b, c) -> int:
+    """Exact sign of det[a; b; c] (the clip's side test of c against the
+    great circle through a and b, decided by error-free expansions)."""
+    a, b, c = (np.ascontiguousarray(v, np.float64) for v in (a, b, c))
+    return load().og_det3_sign_hook(a.ctypes.data, b.ctypes.data, c.ctypes.data)
+
+
+def orient2_sign(a, b, v) -> int:
+    """Exact sign of (b - a) x (v - a) on the plane."""
+    return load().og_orient2_sign_hook(float(a[0]), float(a[1]), float(b[0]), float(b[1]), float(v[0]), float(v[1]))
 
 
 def atan2(y, x) -> float:
