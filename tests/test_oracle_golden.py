@@ -4,6 +4,7 @@ are compared with it."""
 from __future__ import annotations
 
 import json
+import sys
 
 import numpy as np
 import pytest
@@ -240,3 +241,41 @@ def test_cubed_sphere_cell_areas_match_the_gnomonic_closed_form(ne):
                      for j in range(ne) for i in range(ne)])
     want = np.tile(face, 6)
     assert np.max(np.abs(R.dst_areas - want) / want) < 5e-16 * max(ne, 2)
+
+
+def _sph_polygon(rng, centre, radius, n, ccw=True):
+    """Convex spherical polygon: n points at angular distance ~radius around
+    `centre`, in increasing angle (counter-clockwise seen from outside)."""
+    c = centre / np.linalg.norm(centre)
+    u = np.cross(c, [0.0, 0.0, 1.0] if abs(c[2]) < 0.9 else [1.0, 0.0, 0.0])
+    u /= np.linalg.norm(u)
+    v = np.cross(c, u)
+    th = np.sort(rng.uniform(0.0, 2.0 * np.pi, n))
+    p = np.cos(radius) * c[None] + np.sin(radius) * (np.cos(th)[:, None] * u + np.sin(th)[:, None] * v)
+    p /= np.linalg.norm(p, axis=1, keepdims=True)
+    return p if ccw else p[::-1].copy()
+
+
+def test_random_spherical_pairs_vs_mpmath():
+    """The oracle's spherical clip + area against the 60-digit clip and
+    Girard area of tests/golden/make_golden.py on 120 random convex pairs
+    (3 to 8 vertices, 0.01 to 0.5 rad across, either orientation)."""
+    pytest.importorskip("mpmath")
+    sys.path.insert(0, str(GOLDEN))
+    import make_golden as mg
+
+    rng = np.random.default_rng(21)
+    overlapping = 0
+    for trial in range(120):
+        c1 = rng.standard_normal(3)
+        r1, r2 = rng.uniform(0.01, 0.5), rng.uniform(0.01, 0.5)
+        c2 = c1 / np.linalg.norm(c1) + rng.uniform(-1, 1, 3) * (r1 + r2)
+        s = _sph_polygon(rng, c1, r1, int(rng.integers(3, 9)), bool(rng.integers(2)))
+        d = _sph_polygon(rng, c2, r2, int(rng.integers(3, 9)), bool(rng.integers(2)))
+        got = oracle.pair_area(s, d)
+        res = mg.mp_clip(s.tolist(), d.tolist())
+        want = float(mg.girard_area_mp(res)) if len(res) >= 3 else 0.0
+        overlapping += want > 0
+        scale = oracle.cell_area(s)
+        assert abs(got - want) <= 1e-14 * scale, (trial, got, want)
+    assert overlapping >= 40
