@@ -220,7 +220,7 @@ remaining axes are looped over.  Dense arrays with `dims = 1` or
 `dims = ndims` therefore take one call.
 """
 function _slice_groups(f, x::StridedArray{T}, y::StridedArray{T}, dims::Int) where {T}
-    other = Tuple(k for k in 1:ndims(x) if k != dims)
+    other = Tuple(k for k in 1:ndims(x) if k != dims && size(x, k) != 1)   # size-1 axes add no slices
     nf, fx, fy, run = 1, 1, 1, 0
     for (r, k) in enumerate(other)
         if r == 1
