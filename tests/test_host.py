@@ -108,3 +108,21 @@ def test_esmf_file_round_trip(tmp_path):
         assert set(ds.dimensions) == {"n_s", "n_a", "n_b"}
         assert ds.normalization == b"destarea" and ds.source_grid == b"src"
         assert list(ds.destination_grid_shape) == [1, 2]
+
+
+def test_convex_cells():
+    """The convexity check the jittered workloads rely on (the spherical clip
+    needs convex destination cells): regular, HEALPix and the C4 jittered
+    C96 grid are convex; pole cells with a repeated corner count as convex; a
+    dart (a concave quadrilateral) does not, in either orientation."""
+    assert grids.convex_cells(grids.lonlat_regular(5.0, 5.0)).all()
+    assert grids.convex_cells(grids.healpix_grid(8)).all()
+    assert grids.convex_cells(grids.cubed_sphere(96, jitter=0.15, seed=11)).all()
+    assert grids.convex_cells(grids.lonlat_jittered(90, 45, 0.2, seed=4)).all()
+    dart = [(0.0, 0.0), (2.0, 1.0), (0.0, 2.0), (0.7, 1.0)]
+    g = grids.polygon_grid([dart, dart[::-1], [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0)]])
+    assert grids.convex_cells(g).tolist() == [False, False, True]
+    sph = grids.polygon_grid([grids.unit_sphere_from_geographic(np.array([x for x, _ in dart]),
+                                                                np.array([y for _, y in dart]))],
+                             grids.SPHERICAL)
+    assert not grids.convex_cells(sph)[0]
