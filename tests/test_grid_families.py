@@ -6,6 +6,7 @@ fills them -- and RingGrids full grids and reordered cell numberings."""
 from __future__ import annotations
 
 import numpy as np
+import pytest
 import oracle
 
 from crg import grids, mirror_fold_
@@ -69,3 +70,48 @@ def test_reorder_cells_permutes_the_matrix():
     O = oracle.OracleRegridder(b, a)
     P = oracle.OracleRegridder(b, grids.reorder_cells(a, order))
     assert np.array_equal(P.intersections.toarray(), O.intersections.toarray()[:, order])
+
+
+@pytest.mark.parametrize("nx,ny", [(8, 5), (12, 2), (16, 4)])
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_mirror_fold_host_path(nx, ny, dtype):
+    """crg_mirror_fold on host fields (a host copy, no device needed) against
+    the reference's rule (ext/ConservativeRegriddingOceananigansExt.jl:221-240):
+    on the fold row, the primaries r = 1..Nx/4 and Nx/2+1..Nx/2+Nx/4 (1-based)
+    are copied into their partners Nx+1-r; every other cell is untouched.
+    1-D fields, and 2-D fields with the cells along either axis."""
+    from crg import mirror_fold_
+
+    rng = np.random.default_rng(nx * ny)
+    nq, nh, off = nx // 4, nx // 2, (ny - 1) * nx
+    prim = [r for r in range(1, nx + 1) if r <= nq or nh < r <= nh + nq]
+
+    def expect(col):
+        out = col.copy()
+        for r in prim:
+            out[off + nx - r] = col[off + r - 1]
+        return out
+
+    f = rng.standard_normal(nx * ny).astype(dtype)
+    want = expect(f)
+    mirror_fold_(f, nx, ny)
+    assert np.array_equal(f, want)
+    cm = rng.standard_normal((nx * ny, 3)).astype(dtype)  # cells along dims 1
+    want = np.stack([expect(cm[:, k]) for k in range(3)], axis=1)
+    mirror_fold_(cm, nx, ny, dims=1)
+    assert np.array_equal(cm, want)
+    fm = rng.standard_normal((3, nx * ny)).astype(dtype)  # cells along dims 2
+    want = np.stack([expect(fm[k]) for k in range(3)])
+    mirror_fold_(fm, nx, ny, dims=2)
+    assert np.array_equal(fm, want)
+
+
+def test_mirror_fold_refuses_unpaired_fold_rows():
+    """With nx not a multiple of 4 the rule above leaves fold-row cells without
+    a partner (nx = 10: cells 3 and 8), so such a fold is refused."""
+    from crg import ArgumentError, mirror_fold_
+
+    with pytest.raises(ArgumentError, match="multiple of 4"):
+        mirror_fold_(np.zeros(30), 10, 3)
+    with pytest.raises(ArgumentError, match="cells along dims"):
+        mirror_fold_(np.zeros(31), 8, 4)
