@@ -201,7 +201,11 @@ crg_status crg_apply_plan_destroy(crg_apply_plan* plan);
  * row_weight and src_field may both be NULL (area term only); area_weight
  * may be NULL.  For d = (A s) ./ a and an output cotangent g:
  * row_weight = g ./ a, area_weight = -g .* d ./ a.  Host or device pointers;
- * returns after the result is in grad. */
+ * returns after the result is in grad.  Derivatives with respect to the
+ * SOURCE vertices are this same call on the regridder built the other way
+ * round (crg_build(src, dst)), with dst and src swapped and row_weight and
+ * src_field exchanged: A_ij is the area of the intersection of two cells,
+ * symmetric in them (the source cell areas do not enter regrid!). */
 crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src,
                          const double* row_weight, const double* src_field, const double* area_weight, double* grad,
                          void* stream);
