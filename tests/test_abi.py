@@ -140,3 +140,26 @@ def test_build_checks_grid_descriptors_before_device_work():
     assert lib.crg_build_batch(2, dsts, srcs, None, 1, outs) == _lib.CRG_ERR_INVALID_ARGUMENT
     assert lib.crg_last_error().decode().startswith("pair 1: source grid: nblocks = 13")
     assert list(outs) == [None, None]
+
+
+def test_plain_c_caller(tmp_path):
+    """include/crg.h is C99 (no C++ needed by a caller), the library links
+    from C, and its GPU-free answers come back through the C ABI."""
+    import shutil
+    import subprocess
+
+    if shutil.which("gcc") is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    lib = _lib.load()
+    assert lib is not None
+    exe = tmp_path / "c_abi_caller"
+    build = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                            "-I", str(ROOT / "include"), str(ROOT / "tests" / "c_abi_caller.c"),
+                            str(_build.LIB_PATH), f"-Wl,-rpath,{_build.LIB_PATH.parent}", "-o", str(exe)],
+                           capture_output=True, text=True)
+    assert build.returncode == 0, build.stderr
+    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, run.stderr
+    assert "c abi ok" in run.stdout
