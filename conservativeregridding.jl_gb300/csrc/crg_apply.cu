@@ -1019,24 +1019,56 @@ namespace {
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
+// per device: the context the address was looked up in, and the address
+void* g_noalloc_ctx[kMaxDevices] = {};
 float* g_noalloc_ptr[kMaxDevices] = {};
 
-// Device address of g_noalloc_carry on the current device, looked up once per
-// device (the host-side name is only a stand-in, not a device address).
+// cuCtxGetCurrent through the runtime's driver entry point (no link against
+// the driver library): the identity of the current context, so that an address
+// looked up before a cudaDeviceReset (which makes a new primary context, where
+// the array may lie elsewhere) is never reused.
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(f);
+  }();
+  return fn;
+}
+
+// Device address of g_noalloc_carry in the current context of device `dev`
+// (the host-side name is only a stand-in, not a device address).  Looked up
+// once per context: the lookup also loads this file's module, which reserves
+// the array.
 float* noalloc_scratch(int dev) {
   CRG_REQUIRE(dev >= 0 && dev < kMaxDevices, CRG_ERR_NOT_SUPPORTED, "device %d is beyond the supported %d", dev,
               kMaxDevices);
+  const CtxGetCurrentFn get = ctx_get_current();
+  CRG_REQUIRE(get != nullptr, CRG_ERR_CUDA, "cuCtxGetCurrent is not available from the driver");
+  void* ctx = nullptr;
+  CRG_REQUIRE(get(&ctx) == 0 && ctx != nullptr, CRG_ERR_CUDA, "no current CUDA context on device %d", dev);
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  if (!g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != ctx) {
     void* p = nullptr;
     CRG_CHECK_CUDA(cudaGetSymbolAddress(&p, g_noalloc_carry));
     CRG_REQUIRE(p != nullptr, CRG_ERR_CUDA, "cudaGetSymbolAddress returned a null scratch address");
     g_noalloc_ptr[dev] = static_cast<float*>(p);
+    g_noalloc_ctx[dev] = ctx;
   }
   return g_noalloc_ptr[dev];
 }
 
 }  // namespace
+
+// Called by every build on the regridder's device: loads this file's module
+// (reserving the static scratch of crg_apply_noalloc) while the caller is
+// still setting up, rather than at its first allocation-free apply, when its
+// own pool may already hold the whole GPU.
+void noalloc_prepare(int dev) { (void)noalloc_scratch(dev); }
 
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st) {

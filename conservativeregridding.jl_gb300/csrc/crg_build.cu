@@ -1503,6 +1503,7 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
   CRG_CHECK_CUDA(cudaStreamSynchronize(st));
   finish_merge_path(R->fwd, hc, st);
   finish_merge_path(R->rev, hc + 3, st);
+  noalloc_prepare(R->device);
   crg_info& I = R->info;
   const DevCsr* cs[2] = {&R->fwd, &R->rev};
   for (int d = 0; d < 2; ++d) {

@@ -176,6 +176,9 @@ void host_pipeline_ends(const crg_apply_item& it, size_t& fill, size_t& drain);
 bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
+// Loads the module that holds crg_apply_noalloc's static scratch on device
+// `dev` (current) and caches its address; every build calls it.
+void noalloc_prepare(int dev);
 // The merge-path layout of one direction, enqueued without host waits; its
 // counts land in dcounts[0..2] (device) and finish_merge_path takes them from
 // a host copy once the stream has reached them.

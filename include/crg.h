@@ -224,15 +224,21 @@ crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const
  * 8-byte aligned (BF16) base pointers.  The partial sums of rows cut between
  * work blocks (crg_info.carry_slots, 512 bytes each) go to a scratch array the
  * library declares statically (CRG_NOALLOC_SCRATCH_BYTES per GPU, kept until
- * the process exits): at most 32,768 pieces.  Every regridder with at most
- * 1,048,576 nonzeros fits; a larger one fits unless many of its rows are
- * longer than 16 entries, and one that does not fit is refused with
- * CRG_ERR_NOT_SUPPORTED.  The first call on a device looks up that
- * array's device address (cudaGetSymbolAddress), so make that first call
- * before any stream capture.  The scratch is shared by every call on the
- * device and keeps the previous call's contents (each call writes every slot
- * it reads before reading it), so calls that may overlap on the GPU -- on
- * different streams without ordering -- race on it. */
+ * the process exits): at most 32,768 pieces.  With the default task length
+ * of 64 entries every regridder with at most 1,048,576 nonzeros fits (at most
+ * 2 pieces per 64 entries; the tuning variable CRG_TASK_NNZ = 32 halves that
+ * bound); a larger one fits unless many of its rows are longer than 16
+ * entries, and one that does not fit is refused with CRG_ERR_NOT_SUPPORTED.
+ * The array is reserved on a GPU when the part of the library holding it is
+ * loaded there: by the first crg_build (or crg_build_* / crg_build_batch) on
+ * that GPU, which also looks up its device address (cudaGetSymbolAddress) --
+ * so build before the application's pool takes the whole device.  A call in
+ * a CUDA context other than the one of the last lookup (after a
+ * cudaDeviceReset, say) looks the address up again; make that call before any
+ * stream capture.  The scratch is shared by every call on the device and
+ * keeps the previous call's contents (each call writes every slot it reads
+ * before reading it), so calls that may overlap on the GPU -- on different
+ * streams without ordering -- race on it. */
 crg_status crg_apply_noalloc(const crg_regridder* r, int32_t transpose, int32_t dtype,
                              const void* src, int64_t src_stride_cell, int64_t src_stride_field,
                              void* dst, int64_t dst_stride_cell, int64_t dst_stride_field,

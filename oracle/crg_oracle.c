@@ -1125,13 +1125,48 @@ static void og_apply_rev1(const og_regridder* R, const double* x, int64_t sx, do
  * spread over threads. */
 void og_apply(const og_regridder* R, int transpose, const double* src, int64_t src_stride_cell, int64_t src_stride_field,
               double* dst, int64_t dst_stride_cell, int64_t dst_stride_field, int64_t nfields, int normalize, int nthreads) {
-#ifdef _OPENMP
-    if (nthreads > 0) omp_set_num_threads(nthreads);
-#endif
-#pragma omp parallel for schedule(dynamic, 1)
+    /* nthreads applies to this call only (0: all threads) */
+    const int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
     for (int64_t f = 0; f < nfields; ++f) {
         if (!transpose) og_apply_fwd1(R, src + f * src_stride_field, src_stride_cell, dst + f * dst_stride_field, dst_stride_cell, normalize);
         else og_apply_rev1(R, src + f * src_stride_field, src_stride_cell, dst + f * dst_stride_field, dst_stride_cell, normalize);
+    }
+}
+
+/* The same on Float32 fields, as the reference runs regrid! on Float32 arrays
+ * with its SparseMatrixCSC{Float64}: SparseArrays' column scatter
+ * (C[rv[j]] += nzv[j] * x[col], regrid.jl:95-98) promotes every product to
+ * Float64 and rounds each updated entry back to Float32; the transpose's
+ * column gather accumulates in Float64 and rounds once; the division by the
+ * areas (regrid.jl:104-118) is Float64, rounded to Float32. */
+static void og_apply_fwd1_f32(const og_regridder* R, const float* x, int64_t sx, float* y, int64_t sy, int normalize) {
+    for (int64_t i = 0; i < R->nd; ++i) y[i * sy] = 0.0f;
+    for (int64_t j = 0; j < R->ns; ++j) {
+        double xj = (double)x[j * sx];
+        for (int64_t k = R->colptr[j]; k < R->colptr[j + 1]; ++k) {
+            float* yp = y + R->rowval[k] * sy;
+            *yp = (float)((double)*yp + R->nzval[k] * xj);
+        }
+    }
+    if (normalize) for (int64_t i = 0; i < R->nd; ++i) y[i * sy] = (float)((double)y[i * sy] / R->dst_areas[i]);
+}
+
+static void og_apply_rev1_f32(const og_regridder* R, const float* x, int64_t sx, float* y, int64_t sy, int normalize) {
+    for (int64_t j = 0; j < R->ns; ++j) {
+        double acc = 0.0;
+        for (int64_t k = R->colptr[j]; k < R->colptr[j + 1]; ++k) acc += R->nzval[k] * (double)x[R->rowval[k] * sx];
+        y[j * sy] = (float)(normalize ? acc / R->src_areas[j] : acc);
+    }
+}
+
+void og_apply_f32(const og_regridder* R, int transpose, const float* src, int64_t src_stride_cell, int64_t src_stride_field,
+                  float* dst, int64_t dst_stride_cell, int64_t dst_stride_field, int64_t nfields, int normalize, int nthreads) {
+    const int nt = nthreads > 0 ? nthreads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+    for (int64_t f = 0; f < nfields; ++f) {
+        if (!transpose) og_apply_fwd1_f32(R, src + f * src_stride_field, src_stride_cell, dst + f * dst_stride_field, dst_stride_cell, normalize);
+        else og_apply_rev1_f32(R, src + f * src_stride_field, src_stride_cell, dst + f * dst_stride_field, dst_stride_cell, normalize);
     }
 }
 

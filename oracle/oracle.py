@@ -73,6 +73,7 @@ def load() -> C.CDLL:
                 "og_get_areas": (None, [vp, vp, vp]),
                 "og_free": (None, [vp]),
                 "og_apply": (None, [vp, C.c_int, vp, i64, i64, vp, i64, i64, i64, C.c_int, C.c_int]),
+                "og_apply_f32": (None, [vp, C.c_int, vp, i64, i64, vp, i64, i64, i64, C.c_int, C.c_int]),
                 "og_candidates": (i64, [C.POINTER(og_grid), C.POINTER(og_grid), C.c_int, C.c_int, C.POINTER(vp)]),
                 "og_free_buffer": (None, [vp]),
                 "og_pair_area_hook": (dbl, [C.c_int, vp, C.c_int, vp, C.c_int, C.POINTER(C.c_int)]),
@@ -183,6 +184,21 @@ class OracleRegridder:
         out = np.empty((s2.shape[0], nout))
         load().og_apply(self._h, int(transpose), s2.ctypes.data, 1, s2.shape[1], out.ctypes.data, 1, nout,
                         s2.shape[0], int(bool(normalize)), int(nthreads))
+        return out[0] if one else out
+
+    def apply_f32(self, src, transpose=False, normalize=True, nthreads=0, out=None):
+        """The same on float32 fields (nfields, n), as the reference's regrid!
+        runs on Float32 arrays: products and sums in float64, every stored
+        value rounded to float32."""
+        src = np.ascontiguousarray(src, np.float32)
+        one = src.ndim == 1
+        s2 = src.reshape(1, -1) if one else src
+        nout = self.ns if transpose else self.nd
+        if out is None:
+            out = np.empty((s2.shape[0], nout), np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.shape == (s2.shape[0], nout)
+        load().og_apply_f32(self._h, int(transpose), s2.ctypes.data, 1, s2.shape[1], out.ctypes.data, 1, nout,
+                            s2.shape[0], int(bool(normalize)), int(nthreads))
         return out[0] if one else out
 
 

@@ -14,7 +14,8 @@ import oracle
 import pytest
 from conftest import cell_centres, sh_fields
 
-from crg import Regridder, grids, regrid_
+from crg import Regridder, regrid_, workloads
+from test_gpu_parity import assert_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -23,12 +24,18 @@ K = 64
 
 @pytest.fixture(scope="module")
 def c2(cuda):
-    dst, src = grids.lonlat_regular(1.0, 1.0), grids.cubed_sphere(48)
+    dst, src = workloads.precision()
     R = Regridder(dst, src, normalize=True)
     O = oracle.OracleRegridder(dst, src, normalize=True)
     S = sh_fields(cell_centres(src), K, 32, seed=48, noise=0.1)   # (K, n_src)
     D = sh_fields(cell_centres(dst), K, 32, seed=49, noise=0.1)   # (K, n_dst): input of transpose(R)
     return R, O, S, D
+
+
+def test_matrix_parity(c2):
+    """The matrix whose FP32 copy is measured here equals the oracle's."""
+    R, O, _, _ = c2
+    assert_parity(R, O)
 
 
 def _gpu(RR, X, dtype, layout):

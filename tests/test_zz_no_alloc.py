@@ -23,8 +23,8 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-6  # the FP32 tolerance of the apply tests (identical kernels: expected bit-equal)
 
 
-def _call(fn, R, transpose, x, K, y, stream=None):
-    return fn(C.c_void_p(R._h.ptr), transpose, _lib.CRG_F32, C.c_void_p(x.data_ptr()), K, 1, C.c_void_p(y.data_ptr()),
+def _call(fn, R, transpose, x, K, y, stream=None, dtype=_lib.CRG_F32):
+    return fn(C.c_void_p(R._h.ptr), transpose, dtype, C.c_void_p(x.data_ptr()), K, 1, C.c_void_p(y.data_ptr()),
               K, 1, K, 1, C.c_void_p(stream) if stream else None)
 
 
@@ -73,3 +73,31 @@ def test_noalloc_refusals(cuda):
     y = torch.zeros((big.shape[0], K), device="cuda")
     assert _call(lib.crg_apply_noalloc, big, 0, x, K, y) == _lib.CRG_ERR_NOT_SUPPORTED
     assert b"static scratch" in lib.crg_last_error()
+
+
+def test_noalloc_bf16_and_no_device_allocation(cuda):
+    """BF16 fields through the allocation-free path equal crg_apply's, and a
+    call changes the device's free memory by nothing (after a first call on
+    the same regridder, and with the stream drained on both sides)."""
+    import torch
+
+    lib = _lib.load()
+    R = Regridder(grids.lonlat_regular(10.0, 10.0), grids.healpix_grid(32), normalize=True)
+    nd, ns = R.shape
+    K = 32
+    gen = torch.Generator(device="cuda").manual_seed(9)
+    for dtype, code in ((torch.bfloat16, _lib.CRG_BF16), (torch.float32, _lib.CRG_F32)):
+        for transpose, nin, nout in ((0, ns, nd), (1, nd, ns)):
+            x = torch.randn((nin, K), generator=gen, device="cuda").to(dtype)
+            ref = torch.empty((nout, K), dtype=dtype, device="cuda")
+            got = torch.full((nout, K), float("nan"), dtype=dtype, device="cuda")
+            assert _call(lib.crg_apply, R, transpose, x, K, ref, dtype=code) == _lib.CRG_OK
+            assert _call(lib.crg_apply_noalloc, R, transpose, x, K, got, dtype=code) == _lib.CRG_OK
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            got.fill_(float("nan"))
+            torch.cuda.synchronize()
+            assert _call(lib.crg_apply_noalloc, R, transpose, x, K, got, dtype=code) == _lib.CRG_OK
+            torch.cuda.synchronize()
+            assert torch.cuda.mem_get_info()[0] == free0, "crg_apply_noalloc changed the free device memory"
+            assert torch.equal(got, ref), (dtype, transpose)
