@@ -617,6 +617,12 @@ def run_c3(a):
         items.append((y, R, x, 1))
         nbytes += step_bytes(R.nnz, nd, ns, K)[0]
     plan = ApplyPlan(items)
+    # the same applies captured as one graph branch per item (for comparison)
+    os.environ["CRG_PLAN_BATCH"] = "0"
+    try:
+        plan_branches = ApplyPlan(items)
+    finally:
+        del os.environ["CRG_PLAN_BATCH"]
 
     def loop():
         for y, R, x, dims in items:
@@ -627,6 +633,7 @@ def run_c3(a):
     for _ in range(max(a.warmup, 3)):
         loop()
         plan.launch()
+        plan_branches.launch()
     reps = max(5, min(a.steps, 50))
     torch.cuda.synchronize()
     ev[0].record(stream)
@@ -639,6 +646,12 @@ def run_c3(a):
     ev[2].synchronize()
     ms_loop = ev[0].elapsed_time(ev[1]) / reps
     ms_plan = ev[1].elapsed_time(ev[2]) / reps
+    ev[0].record(stream)
+    for _ in range(reps):
+        plan_branches.launch()
+    ev[1].record(stream)
+    ev[1].synchronize()
+    ms_branches = ev[0].elapsed_time(ev[1]) / reps
     cells = [(R.shape[0], R.shape[1]) for R in Rs]
     return {
         "metric": "batched build pairs/s (summed) and batched apply GB/s",
@@ -650,7 +663,11 @@ def run_c3(a):
                   "pairs_per_s_batch": round(nnz / t_batch, 1), "pairs_per_s_single": round(nnz / t_single, 1)},
         "apply": {"loop_ms": round(ms_loop, 4), "graph_ms": round(ms_plan, 4),
                   "GB/s_graph": round(nbytes / (ms_plan * 1e-3) / 1e9, 1),
-                  "GB/s_loop": round(nbytes / (ms_loop * 1e-3) / 1e9, 1), "bytes_per_batch": nbytes},
+                  "GB/s_loop": round(nbytes / (ms_loop * 1e-3) / 1e9, 1), "bytes_per_batch": nbytes,
+                  "graph_kernels": plan.info["kernels"], "graph_batched_items": plan.info["batched_items"],
+                  "graph": "one persistent launch over all pairs' work units + one for cut rows",
+                  "branches_ms": round(ms_branches, 4), "branches_kernels": plan_branches.info["kernels"],
+                  "GB/s_branches": round(nbytes / (ms_branches * 1e-3) / 1e9, 1)},
     }
 
 

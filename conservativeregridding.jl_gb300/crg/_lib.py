@@ -117,6 +117,7 @@ SIGNATURES = {
     "crg_apply_plan_create": (C.c_int, [C.c_int64, C.POINTER(crg_apply_item), C.POINTER(C.c_void_p)]),
     "crg_apply_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "crg_apply_plan_destroy": (C.c_int, [C.c_void_p]),
+    "crg_apply_plan_info": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_get_csc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "crg_mirror_fold": (C.c_int, [C.c_int32, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                   C.c_void_p]),

@@ -100,6 +100,14 @@ class ApplyPlan:
         self._p = p.value
         self._fin = weakref.finalize(self, _destroy, p.value)
 
+    @property
+    def info(self) -> dict:
+        """``kernels``: kernel launches of one replay; ``batched_items``: the
+        items run by the one persistent launch (the rest are their own applies)."""
+        k, b = C.c_int64(), C.c_int64()
+        check(_lib.load().crg_apply_plan_info(C.c_void_p(self._p), C.byref(k), C.byref(b)))
+        return {"kernels": k.value, "batched_items": b.value}
+
     def launch(self, stream=None):
         import torch
 

@@ -192,6 +192,10 @@ crg_status crg_apply_plan_destroy(crg_apply_plan* plan) {
   return guarded([&] { apply_plan_destroy_impl(plan); });
 }
 
+crg_status crg_apply_plan_info(const crg_apply_plan* plan, int64_t* kernels, int64_t* batched_items) {
+  return guarded([&] { apply_plan_info_impl(plan, kernels, batched_items); });
+}
+
 crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const crg_grid_desc* src,
                          const double* row_weight, const double* src_field, const double* area_weight, double* grad,
                          void* stream) {

@@ -320,103 +320,143 @@ int num_sms() {
 // entries); a row that began in an earlier task or continues into a later one
 // is written to the task's carry slot (0 = first row, 1 = last row) for
 // k_cm_fixup.
-template <class T> __device__ __forceinline__ float4 ldoff4(const char* base, uint32_t off);
-template <> __device__ __forceinline__ float4 ldoff4<float>(const char* base, uint32_t off) {
-  return __ldg(reinterpret_cast<const float4*>(base + off));
-}
-template <> __device__ __forceinline__ float4 ldoff4<__nv_bfloat16>(const char* base, uint32_t off) {
-  return ld4<__nv_bfloat16>(reinterpret_cast<const __nv_bfloat16*>(base + off));
+//
+// The gathers in flight hold the raw loads (16 bytes of 4 FP32 fields, 8 bytes
+// of 4 BF16 fields), converted to FP32 when consumed; BF16 keeps 16 of them in
+// flight instead of 8, so that a warp has as many bytes under way as with FP32
+// in about the same registers.
+template <class T> struct CmGather;
+template <> struct CmGather<float> {
+  using Raw = float4;
+  static constexpr int kInFlight = 8;
+  static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
+    return __ldg(reinterpret_cast<const float4*>(base + off));
+  }
+  static __device__ __forceinline__ float4 widen(Raw r) { return r; }
+};
+template <> struct CmGather<__nv_bfloat16> {
+  using Raw = uint2;
+  static constexpr int kInFlight = 16;
+  static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
+    return __ldg(reinterpret_cast<const uint2*>(base + off));
+  }
+  static __device__ __forceinline__ float4 widen(Raw u) {
+    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
+    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
+    return make_float4(a.x, a.y, b.x, b.y);
+  }
+};
+
+// One merge-path task of one 128-field pass, by one warp.  `xb` is the lane's
+// base (its 4 fields of cell 0), `fo` its first field, `on` whether it has
+// fields in this pass; B gathers are in flight.
+template <class T, bool kGaps, int B>
+__device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ tasks, const int2* __restrict__ tslot,
+                                        const int32_t* __restrict__ idx, const uint32_t* __restrict__ rbits,
+                                        const int32_t* __restrict__ nextrow, const float* __restrict__ w,
+                                        const char* xb, uint32_t cstride, T* __restrict__ y, int64_t ys, int64_t fo,
+                                        bool on, float* __restrict__ carry, int lane) {
+  using G = CmGather<T>;
+  const int4 tr = __ldg(tasks + task);
+  const int32_t e0 = tr.x, e1 = tr.y;
+  if (e0 >= e1) return;  // warp-uniform
+  const int32_t first = tr.z & 0x7fffffff;
+  // rows written to the carry slots: the first row if it began in an earlier
+  // task, the last row if it continues into a later one (-1: no such row)
+  const int32_t carry_first = tr.z < 0 ? first : -1;
+  const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
+  const int2 slot = (tr.z | tr.w) < 0 ? __ldg(tslot + task) : make_int2(-1, -1);
+  int32_t cur = first;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  auto flush = [&](int32_t row) {
+    if (!on) return;
+    if (row == carry_first) {
+      *reinterpret_cast<float4*>(carry + (int64_t)slot.x * 128 + lane * 4) = acc;
+    } else if (row == carry_last) {
+      *reinterpret_cast<float4*>(carry + (int64_t)slot.y * 128 + lane * 4) = acc;
+    } else {
+      st4<T>(y + (int64_t)row * ys + fo, acc);
+    }
+  };
+  // the chunk at c0: lane's byte offset of its source cell and weight, and
+  // the row starts among the chunk's entries (bit k: entry c0 + k)
+  auto load = [&](int32_t c0, uint32_t& starts, uint32_t& o, float& wt) {
+    const int32_t e = c0 + lane;
+    const bool valid = e < e1;
+    o = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
+    wt = valid ? __ldg(w + e) : 0.f;
+    starts = __funnelshift_r(__ldg(rbits + (c0 >> 5)), __ldg(rbits + (c0 >> 5) + 1), (uint32_t)c0 & 31u);
+    if (e1 - c0 < 32) starts &= (1u << (e1 - c0)) - 1u;
+  };
+  uint32_t starts;
+  uint32_t myo;
+  float myw;
+  load(e0, starts, myo, myw);
+  starts &= ~1u;  // entry e0 belongs to row `first` (already current)
+  for (int32_t c0 = e0; c0 < e1; c0 += 32) {
+    // the next chunk's entries load while this one is gathered
+    uint32_t nstarts = 0u, no = 0u;
+    float nwt = 0.f;
+    if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
+    const unsigned newrow = starts;
+    const int n = e1 - c0 < 32 ? e1 - c0 : 32;
+    for (int k = 0; k < n; k += B) {
+      typename G::Raw v[B];
+      float ww[B];
+#pragma unroll
+      for (int h = 0; h < B; ++h) {
+        const uint32_t o = __shfl_sync(0xffffffffu, myo, (k + h) & 31);
+        ww[h] = __shfl_sync(0xffffffffu, myw, (k + h) & 31);
+        v[h] = G::load(xb, o);  // past-the-end entries load cell 0 with weight 0
+      }
+#pragma unroll
+      for (int h = 0; h < B; ++h) {
+        if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
+        if ((newrow >> (k + h)) & 1u) {
+          flush(cur);
+          cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
+          acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        const float4 xv = G::widen(v[h]);
+        acc.x = fmaf(ww[h], xv.x, acc.x);
+        acc.y = fmaf(ww[h], xv.y, acc.y);
+        acc.z = fmaf(ww[h], xv.z, acc.z);
+        acc.w = fmaf(ww[h], xv.w, acc.w);
+      }
+    }
+    starts = nstarts;
+    myo = no;
+    myw = nwt;
+  }
+  flush(cur);
 }
 
-template <class T, bool kGaps>
+// The lane's field base of one 128-field pass starting at f0.
+template <class T>
+__device__ __forceinline__ const char* cm_lane_base(const T* x, int64_t f0, int64_t nf, int lane, int64_t& fo,
+                                                    bool& on) {
+  const int64_t f = f0 + (int64_t)lane * 4;
+  on = f < nf;
+  fo = on ? f : f0;
+  return reinterpret_cast<const char*>(x + fo);
+}
+
+template <class T, bool kGaps, int B = CmGather<T>::kInFlight>
 __global__ void __launch_bounds__(256, 3)
     k_cm_nnz(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
              const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow, const float* __restrict__ w,
              int64_t ntasks, const T* __restrict__ x,
              int64_t xs, T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
-  constexpr int B = 8;  // gathers in flight per warp
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int64_t f = f0 + (int64_t)lane * 4;
-  const bool on = f < nf;
-  const int64_t fo = on ? f : f0;
+  int64_t fo;
+  bool on;
   // per-lane base of this lane's 4 fields; cell j adds j * xs elements (32-bit byte offset)
-  const char* xb = reinterpret_cast<const char*>(x + fo);
+  const char* xb = cm_lane_base<T>(x, f0, nf, lane, fo, on);
   const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(T));
-  for (int64_t task = gw; task < ntasks; task += nw) {
-    const int4 tr = __ldg(tasks + task);
-    const int32_t e0 = tr.x, e1 = tr.y;
-    if (e0 >= e1) continue;  // warp-uniform
-    const int32_t first = tr.z & 0x7fffffff;
-    // rows written to the carry slots: the first row if it began in an earlier
-    // task, the last row if it continues into a later one (-1: no such row)
-    const int32_t carry_first = tr.z < 0 ? first : -1;
-    const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
-    const int2 slot = (tr.z | tr.w) < 0 ? __ldg(tslot + task) : make_int2(-1, -1);
-    int32_t cur = first;
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    auto flush = [&](int32_t row) {
-      if (!on) return;
-      if (row == carry_first) {
-        *reinterpret_cast<float4*>(carry + (int64_t)slot.x * 128 + lane * 4) = acc;
-      } else if (row == carry_last) {
-        *reinterpret_cast<float4*>(carry + (int64_t)slot.y * 128 + lane * 4) = acc;
-      } else {
-        st4<T>(y + (int64_t)row * ys + fo, acc);
-      }
-    };
-    // the chunk at c0: lane's byte offset of its source cell and weight, and
-    // the row starts among the chunk's entries (bit k: entry c0 + k)
-    auto load = [&](int32_t c0, uint32_t& starts, uint32_t& o, float& wt) {
-      const int32_t e = c0 + lane;
-      const bool valid = e < e1;
-      o = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
-      wt = valid ? __ldg(w + e) : 0.f;
-      starts = __funnelshift_r(__ldg(rbits + (c0 >> 5)), __ldg(rbits + (c0 >> 5) + 1), (uint32_t)c0 & 31u);
-      if (e1 - c0 < 32) starts &= (1u << (e1 - c0)) - 1u;
-    };
-    uint32_t starts;
-    uint32_t myo;
-    float myw;
-    load(e0, starts, myo, myw);
-    starts &= ~1u;  // entry e0 belongs to row `first` (already current)
-    for (int32_t c0 = e0; c0 < e1; c0 += 32) {
-      // the next chunk's entries load while this one is gathered
-      uint32_t nstarts = 0u, no = 0u;
-      float nwt = 0.f;
-      if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
-      const unsigned newrow = starts;
-      const int n = e1 - c0 < 32 ? e1 - c0 : 32;
-      for (int k = 0; k < n; k += B) {
-        float4 v[B];
-        float ww[B];
-#pragma unroll
-        for (int h = 0; h < B; ++h) {
-          const uint32_t o = __shfl_sync(0xffffffffu, myo, (k + h) & 31);
-          ww[h] = __shfl_sync(0xffffffffu, myw, (k + h) & 31);
-          v[h] = ldoff4<T>(xb, o);  // past-the-end entries load cell 0 with weight 0
-        }
-#pragma unroll
-        for (int h = 0; h < B; ++h) {
-          if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
-          if ((newrow >> (k + h)) & 1u) {
-            flush(cur);
-            cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
-            acc = make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-          acc.x = fmaf(ww[h], v[h].x, acc.x);
-          acc.y = fmaf(ww[h], v[h].y, acc.y);
-          acc.z = fmaf(ww[h], v[h].z, acc.z);
-          acc.w = fmaf(ww[h], v[h].w, acc.w);
-        }
-      }
-      starts = nstarts;
-      myo = no;
-      myw = nwt;
-    }
-    flush(cur);
-  }
+  for (int64_t task = gw; task < ntasks; task += nw)
+    cm_task<T, kGaps, B>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, on, carry, lane);
 }
 
 // Rows cut between tasks: sum their pieces in task order (deterministic).
@@ -725,6 +765,382 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
 }
 
 size_t elem_size(int dtype) { return dtype == CRG_F64 ? 8 : (dtype == CRG_F32 ? 4 : 2); }
+
+// ------------------------------------------------------------------ one launch for a batch
+//
+// The applies of many regridders (cell-major FP32 or BF16 fields, device
+// memory) as one grid of work units: merge-path items contribute one unit per
+// task and 128-field pass (the body of k_cm_nnz), row items one unit per
+// group of 32 / G rows (the body of k_spmm_rows, G lanes per row).  Every
+// warp takes units u = warp, warp + warps, ... and finds the unit's item by a
+// binary search in the items' first units.  A second launch sums the cut rows
+// of every merge-path item (k_cm_fixup's body) and zeroes their empty rows.
+// Each item's result has the bits of its own crg_apply: the same tasks, cut
+// rows and fixup order, or the same sequential row sums.
+
+struct BatchItem {
+  int64_t unit0;   // first unit of the item
+  int32_t kind;    // 0 merge-path, 1 rows
+  int32_t gaps;    // merge-path: some rows have no entries (nextrow)
+  int32_t lg;      // rows: log2 of the lanes per row
+  int32_t vec;     // rows: 4-field vector access
+  int64_t ntasks;  // merge-path: tasks per 128-field pass
+  int64_t nrows, nf, xs, ys, nslots;
+  const int4* tasks;
+  const int2* tslot;
+  const uint32_t* rbits;
+  const int32_t* nextrow;
+  const int32_t* ptr;
+  const int32_t* idx;
+  const float* w;
+  const void* x;
+  void* y;
+  float* carry;  // merge-path: [passes][nslots][128]
+};
+
+struct FinishItem {
+  int64_t unit0;
+  int32_t kind;  // 0 fixup of cut rows (nsplit units per pass), 1 zero rows without entries (32 rows per unit)
+  int32_t pad;
+  int64_t nsplit, nslots, nrows, nf, ys;
+  const int32_t* split;
+  const float* carry;
+  const int32_t* ptr;
+  void* y;
+};
+
+// index of the item holding unit u: the last i with unit0[i] <= u
+__device__ __forceinline__ int batch_find(const int64_t* __restrict__ unit0, int n, int64_t u) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(unit0 + mid) <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// k_spmm_rows for one group of rows: lane -> (row, g), fields f = 4 g, 4 g + 4 G, ...
+template <class T>
+__device__ __forceinline__ void rows_unit(const BatchItem& it, int64_t k, int lane) {
+  const int G = 1 << it.lg;
+  const int g = lane & (G - 1);
+  const int64_t r = k * (32 >> it.lg) + (lane >> it.lg);
+  if (r >= it.nrows) return;
+  const T* __restrict__ x = static_cast<const T*>(it.x);
+  T* __restrict__ y = static_cast<T*>(it.y);
+  const int32_t k0 = __ldg(it.ptr + r), k1 = __ldg(it.ptr + r + 1);
+  const int64_t nf = it.nf;
+  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool full = it.vec && f + 4 <= nf;
+    for (int32_t q = k0; q < k1; ++q) {
+      const int64_t j = __ldg(it.idx + q);
+      const float ww = __ldg(it.w + q);
+      const T* xp = x + j * it.xs + f;
+      float4 v;
+      if (full) {
+        v = ld4<T>(xp);
+      } else {
+        v.x = ld1<T>(xp);
+        v.y = f + 1 < nf ? ld1<T>(xp + 1) : 0.f;
+        v.z = f + 2 < nf ? ld1<T>(xp + 2) : 0.f;
+        v.w = f + 3 < nf ? ld1<T>(xp + 3) : 0.f;
+      }
+      acc.x = fmaf(ww, v.x, acc.x);
+      acc.y = fmaf(ww, v.y, acc.y);
+      acc.z = fmaf(ww, v.z, acc.z);
+      acc.w = fmaf(ww, v.w, acc.w);
+    }
+    T* yp = y + r * it.ys + f;
+    if (full) {
+      st4<T>(yp, acc);
+    } else {
+      st1<T>(yp, acc.x);
+      if (f + 1 < nf) st1<T>(yp + 1, acc.y);
+      if (f + 2 < nf) st1<T>(yp + 2, acc.z);
+      if (f + 3 < nf) st1<T>(yp + 3, acc.w);
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256, 3) k_batch_apply(const BatchItem* __restrict__ items,
+                                                        const int64_t* __restrict__ unit0, int nitems,
+                                                        int64_t nunits) {
+  constexpr int B = CmGather<T>::kInFlight;
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = gw; u < nunits; u += nw) {
+    const BatchItem& it = items[batch_find(unit0, nitems, u)];
+    const int64_t k = u - it.unit0;
+    if (it.kind == 0) {
+      const int64_t pass = k / it.ntasks, task = k - pass * it.ntasks;
+      int64_t fo;
+      bool on;
+      const char* xb = cm_lane_base<T>(static_cast<const T*>(it.x), pass * 128, it.nf, lane, fo, on);
+      const uint32_t cstride = (uint32_t)(it.xs * (int64_t)sizeof(T));
+      float* carry = it.carry ? it.carry + pass * it.nslots * 128 : nullptr;
+      if (it.gaps)
+        cm_task<T, true, B>(task, it.tasks, it.tslot, it.idx, it.rbits, it.nextrow, it.w, xb, cstride,
+                            static_cast<T*>(it.y), it.ys, fo, on, carry, lane);
+      else
+        cm_task<T, false, B>(task, it.tasks, it.tslot, it.idx, it.rbits, nullptr, it.w, xb, cstride,
+                             static_cast<T*>(it.y), it.ys, fo, on, carry, lane);
+    } else {
+      rows_unit<T>(it, k, lane);
+    }
+  }
+}
+
+template <class T>
+__global__ void k_batch_finish(const FinishItem* __restrict__ items, const int64_t* __restrict__ unit0, int nitems,
+                               int64_t nunits) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = gw; u < nunits; u += nw) {
+    const FinishItem& it = items[batch_find(unit0, nitems, u)];
+    const int64_t k = u - it.unit0;
+    T* __restrict__ y = static_cast<T*>(it.y);
+    if (it.kind == 0) {
+      // k_cm_fixup: the pieces of cut row s in task order
+      const int64_t pass = k / it.nsplit, sp = k - pass * it.nsplit;
+      const int64_t f = pass * 128 + (int64_t)lane * 4;
+      if (f >= it.nf) continue;
+      const int32_t row = __ldg(it.split + 3 * sp), s0 = __ldg(it.split + 3 * sp + 1),
+                    pieces = __ldg(it.split + 3 * sp + 2);
+      const float* c = it.carry + pass * it.nslots * 128;
+      float4 acc = *reinterpret_cast<const float4*>(c + (int64_t)s0 * 128 + lane * 4);
+      for (int32_t q = 1; q < pieces; ++q) {
+        const float4 d = *reinterpret_cast<const float4*>(c + (int64_t)(s0 + q) * 128 + lane * 4);
+        acc.x += d.x; acc.y += d.y; acc.z += d.z; acc.w += d.w;
+      }
+      st4<T>(y + (int64_t)row * it.ys + f, acc);
+    } else {
+      // k_zero_empty_cm: rows without entries
+      const int64_t r = k * 32 + lane;
+      if (r >= it.nrows || __ldg(it.ptr + r + 1) > __ldg(it.ptr + r)) continue;
+      for (int64_t f = 0; f < it.nf; ++f) st1<T>(y + r * it.ys + f, 0.f);
+    }
+  }
+}
+
+}  // namespace
+
+// The device tables of a batch (one allocation) and its launches.
+struct BatchLaunch {
+  void* mem = nullptr;
+  int device = 0;
+  struct Part {
+    int dtype = CRG_F32;
+    const BatchItem* items = nullptr;
+    const int64_t* unit0 = nullptr;
+    int nitems = 0;
+    int64_t nunits = 0;
+    const FinishItem* fitems = nullptr;
+    const int64_t* funit0 = nullptr;
+    int nfitems = 0;
+    int64_t nfunits = 0;
+  };
+  std::vector<Part> parts;  // one per field type present
+};
+
+BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled) {
+  handled.assign((size_t)n, 0);
+  std::vector<BatchItem> bi[2];
+  std::vector<FinishItem> fi[2];
+  std::vector<int64_t> carry_off[2];  // per merge-path item: float offset of its carry, -1 none
+  int64_t units[2] = {0, 0}, funits[2] = {0, 0}, carry_floats = 0;
+  int dev = 0;
+  CRG_CHECK_CUDA(cudaGetDevice(&dev));
+  for (int64_t k = 0; k < n; ++k) {
+    const crg_apply_item& it = items[k];
+    const crg_regridder* r = it.regridder;
+    if (!r || !(it.dtype == CRG_F32 || it.dtype == CRG_BF16) || r->device != dev || it.nfields < 1) continue;
+    const bool t = it.transpose != 0;
+    const DevCsr& c = it.adjoint ? (t ? r->fwd : r->rev) : (t ? r->rev : r->fwd);
+    const int64_t nf = it.nfields;
+    if (c.nrows == 0) {
+      handled[k] = 1;  // nothing to write
+      continue;
+    }
+    const int64_t ssc = it.src_stride_cell, ssf = it.src_stride_field, dsc = it.dst_stride_cell,
+                  dsf = it.dst_stride_field;
+    // fields side by side (or one field), device memory, positive strides
+    if (!(nf == 1 || (ssf == 1 && dsf == 1))) continue;
+    if (!it.dst || (c.ncols > 0 && !it.src) || dsc <= 0 || (c.ncols > 0 && ssc <= 0)) continue;
+    if (!is_device_pointer(it.dst) || (c.ncols > 0 && !is_device_pointer(it.src))) continue;
+    const int d = it.dtype == CRG_BF16 ? 1 : 0;
+    const int es = d ? 2 : 4;
+    const float* w = it.normalize ? (it.adjoint ? c.adj32 : c.wn32) : c.val32;
+    const bool cell_major = ssf == 1 && dsf == 1 && nf > 1;
+    const bool vec4 = nf % 4 == 0 && ssc % 4 == 0 && dsc % 4 == 0 && (uintptr_t)it.src % (4 * es) == 0 &&
+                      (uintptr_t)it.dst % (4 * es) == 0;
+    const bool span32 = (double)c.ncols * (double)ssc * es < 4.0e9;
+    BatchItem b{};
+    b.nrows = c.nrows;
+    b.nf = nf;
+    b.xs = ssc;
+    b.ys = dsc;
+    b.ptr = c.ptr;
+    b.idx = c.idx;
+    b.w = w;
+    b.x = it.src;
+    b.y = it.dst;
+    const int64_t passes = (nf + 127) / 128;
+    if (spmm_path() == SpmmPath::kAuto && cell_major && vec4 && nf >= 32 && span32) {
+      // the merge path, as launch_cm_nnz runs it
+      b.kind = 0;
+      b.gaps = c.nextrow != nullptr;
+      b.ntasks = c.ntasks;
+      b.nslots = c.nslots;
+      b.tasks = c.tasks;
+      b.tslot = c.tslot;
+      b.rbits = c.rbits;
+      b.nextrow = c.nextrow;
+      const int64_t nu = c.ntasks * passes;
+      if (nu > 0) {
+        b.unit0 = units[d];
+        units[d] += nu;
+        carry_off[d].push_back(c.nslots ? carry_floats : -1);
+        carry_floats += c.nslots * 128 * passes;
+        bi[d].push_back(b);
+      }
+      FinishItem f{};
+      f.nsplit = c.nsplit;
+      f.nslots = c.nslots;
+      f.nrows = c.nrows;
+      f.nf = nf;
+      f.ys = dsc;
+      f.split = c.split;
+      f.ptr = c.ptr;
+      f.y = it.dst;
+      if (c.nsplit && nu > 0) {
+        f.kind = 0;
+        f.unit0 = funits[d];
+        f.carry = reinterpret_cast<const float*>((intptr_t)carry_off[d].back());  // offset until allocation
+        funits[d] += c.nsplit * passes;
+        fi[d].push_back(f);
+      }
+      if (c.nempty) {
+        f.kind = 1;
+        f.carry = nullptr;
+        f.unit0 = funits[d];
+        funits[d] += (c.nrows + 31) / 32;
+        fi[d].push_back(f);
+      }
+    } else {
+      // the row kernels: G lanes per row, as launch_f32 picks them
+      b.kind = 1;
+      b.vec = vec4;
+      const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
+      int lg = 0;
+      while ((1 << lg) < lanes) ++lg;
+      b.lg = lg;
+      b.unit0 = units[d];
+      units[d] += (c.nrows + (32 >> lg) - 1) / (32 >> lg);
+      bi[d].push_back(b);
+    }
+    handled[k] = 1;
+  }
+  // one allocation: [items][unit0] per part, carry
+  size_t bytes = 0;
+  auto take = [&](size_t b) {
+    const size_t at = bytes;
+    bytes += (b + 255) / 256 * 256;
+    return at;
+  };
+  size_t off_items[2], off_u0[2], off_f[2], off_fu0[2];
+  for (int d = 0; d < 2; ++d) {
+    off_items[d] = take(bi[d].size() * sizeof(BatchItem));
+    off_u0[d] = take(bi[d].size() * sizeof(int64_t));
+    off_f[d] = take(fi[d].size() * sizeof(FinishItem));
+    off_fu0[d] = take(fi[d].size() * sizeof(int64_t));
+  }
+  const size_t off_carry = take((size_t)carry_floats * sizeof(float));
+  BatchLaunch* L = new BatchLaunch;
+  L->device = dev;
+  try {
+    if (bytes) CRG_CHECK_CUDA(cudaMalloc(&L->mem, bytes));
+    char* base = static_cast<char*>(L->mem);
+    float* carry = reinterpret_cast<float*>(base + off_carry);
+    for (int d = 0; d < 2; ++d) {
+      if (bi[d].empty() && fi[d].empty()) continue;
+      size_t mp = 0;
+      for (auto& b : bi[d])
+        if (b.kind == 0) {
+          const int64_t o = carry_off[d][mp++];
+          b.carry = o >= 0 ? carry + o : nullptr;
+        }
+      for (auto& f : fi[d])
+        if (f.kind == 0) f.carry = carry + (intptr_t)f.carry;
+      std::vector<int64_t> u0(bi[d].size()), fu0(fi[d].size());
+      for (size_t q = 0; q < bi[d].size(); ++q) u0[q] = bi[d][q].unit0;
+      for (size_t q = 0; q < fi[d].size(); ++q) fu0[q] = fi[d][q].unit0;
+      auto up = [&](size_t off, const void* src, size_t nb) {
+        if (nb) CRG_CHECK_CUDA(cudaMemcpy(base + off, src, nb, cudaMemcpyHostToDevice));
+      };
+      up(off_items[d], bi[d].data(), bi[d].size() * sizeof(BatchItem));
+      up(off_u0[d], u0.data(), u0.size() * sizeof(int64_t));
+      up(off_f[d], fi[d].data(), fi[d].size() * sizeof(FinishItem));
+      up(off_fu0[d], fu0.data(), fu0.size() * sizeof(int64_t));
+      BatchLaunch::Part p;
+      p.dtype = d ? CRG_BF16 : CRG_F32;
+      p.items = reinterpret_cast<const BatchItem*>(base + off_items[d]);
+      p.unit0 = reinterpret_cast<const int64_t*>(base + off_u0[d]);
+      p.nitems = (int)bi[d].size();
+      p.nunits = units[d];
+      p.fitems = reinterpret_cast<const FinishItem*>(base + off_f[d]);
+      p.funit0 = reinterpret_cast<const int64_t*>(base + off_fu0[d]);
+      p.nfitems = (int)fi[d].size();
+      p.nfunits = funits[d];
+      L->parts.push_back(p);
+    }
+  } catch (...) {
+    batch_free(L);
+    throw;
+  }
+  return L;
+}
+
+void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
+  const int64_t max_warps = (int64_t)num_sms() * 24;  // three blocks of 8 warps per SM
+  for (const auto& p : L->parts) {
+    if (p.nunits) {
+      const int64_t warps = std::min<int64_t>(p.nunits, max_warps);
+      if (p.dtype == CRG_F32)
+        k_batch_apply<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits);
+      else
+        k_batch_apply<__nv_bfloat16><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    if (p.nfunits) {
+      const int64_t warps = std::min<int64_t>(p.nfunits, max_warps);
+      if (p.dtype == CRG_F32)
+        k_batch_finish<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.fitems, p.funit0, p.nfitems, p.nfunits);
+      else
+        k_batch_finish<__nv_bfloat16><<<nblk(warps * 32, 256), 256, 0, st>>>(p.fitems, p.funit0, p.nfitems,
+                                                                              p.nfunits);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+  }
+}
+
+int batch_launches(const BatchLaunch* L) {
+  int n = 0;
+  for (const auto& p : L->parts) n += (p.nunits > 0) + (p.nfunits > 0);
+  return n;
+}
+
+void batch_free(BatchLaunch* L) {
+  if (!L) return;
+  if (L->mem) cudaFree(L->mem);
+  delete L;
+}
+
+namespace {
 
 }  // namespace
 

@@ -12,6 +12,8 @@
 // overlap those of the others on both directions of the host link.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <atomic>
 #include <string>
 #include <thread>
@@ -23,6 +25,9 @@ struct crg_apply_plan {
   cudaGraphExec_t exec = nullptr;
   std::vector<crg_regridder*> held;  // retained for the plan's lifetime
   int device = 0;
+  crg::BatchLaunch* batch = nullptr;  // the items one persistent launch runs (tables, carry)
+  int64_t kernels = 0;                 // kernel launches per replay
+  int64_t batched = 0;                 // items run by the persistent launch
 };
 
 namespace crg {
@@ -236,8 +241,16 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
     CRG_REQUIRE(it.dst && is_device_pointer(it.dst) && (!it.src || is_device_pointer(it.src)), CRG_ERR_NOT_SUPPORTED,
                 "item %lld: a plan replays on the GPU alone, so fields must be device pointers", (long long)k);
   }
-  // Capture: the origin stream forks one branch per item (their outputs are
-  // distinct), so the graph runs small items side by side.
+  // The items of cell-major FP32 / BF16 fields (or single fields) run as one
+  // persistent launch over all their work units (plus one launch for the rows
+  // cut between tasks and the empty rows); the others keep their own applies.
+  // CRG_PLAN_BATCH=0 captures every item as its own apply (for comparison).
+  std::vector<char> handled((size_t)n, 0);
+  BatchLaunch* batch = nullptr;
+  const char* pb = getenv("CRG_PLAN_BATCH");
+  if (!(pb && strcmp(pb, "0") == 0)) batch = batch_prepare(n, items, handled);
+  // Capture: the origin stream forks one branch per remaining item (their
+  // outputs are distinct), so the graph runs small items side by side.
   std::vector<cudaStream_t> sts(n + 1, nullptr);
   std::vector<cudaEvent_t> evs(n + 1, nullptr);
   auto cleanup = [&]() {
@@ -249,6 +262,7 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
   cudaGraph_t graph = nullptr;
   try {
     for (int64_t k = 0; k <= n; ++k) {
+      if (k < n && handled[k]) continue;
       CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&sts[k], cudaStreamNonBlocking));
       CRG_CHECK_CUDA(cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming));
     }
@@ -257,6 +271,7 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
     try {
       CRG_CHECK_CUDA(cudaEventRecord(evs[n], origin));
       for (int64_t k = 0; k < n; ++k) {
+        if (handled[k]) continue;
         const crg_apply_item& it = items[k];
         CRG_CHECK_CUDA(cudaStreamWaitEvent(sts[k], evs[n], 0));
         apply_impl(it.regridder, it.transpose, it.dtype, it.adjoint != 0, it.src, it.src_stride_cell,
@@ -265,6 +280,7 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
         CRG_CHECK_CUDA(cudaEventRecord(evs[k], sts[k]));
         CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[k], 0));
       }
+      if (batch) batch_enqueue(batch, origin);
     } catch (...) {
       cudaStreamEndCapture(origin, &graph);
       if (graph) cudaGraphDestroy(graph);
@@ -273,14 +289,29 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
     CRG_CHECK_CUDA(cudaStreamEndCapture(origin, &graph));
   } catch (...) {
     cleanup();
+    batch_free(batch);
     throw;
   }
   cleanup();
+  size_t nnodes = 0;
+  int64_t kernels = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nnodes) == cudaSuccess && nnodes) {
+    std::vector<cudaGraphNode_t> nodes(nnodes);
+    if (cudaGraphGetNodes(graph, nodes.data(), &nnodes) == cudaSuccess)
+      for (size_t q = 0; q < nnodes; ++q) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nodes[q], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) ++kernels;
+      }
+  }
   crg_apply_plan* p = new crg_apply_plan;
   p->device = dev;
+  p->batch = batch;
+  p->kernels = kernels;
+  for (int64_t k = 0; k < n; ++k) p->batched += batch && handled[k] ? 1 : 0;
   const cudaError_t e = cudaGraphInstantiate(&p->exec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) {
+    batch_free(batch);
     delete p;
     CRG_CHECK_CUDA(e);
   }
@@ -301,9 +332,16 @@ void apply_plan_launch_impl(crg_apply_plan* p, cudaStream_t st) {
   CRG_CHECK_CUDA(cudaGraphLaunch(p->exec, st));
 }
 
+void apply_plan_info_impl(const crg_apply_plan* p, int64_t* kernels, int64_t* batched_items) {
+  CRG_REQUIRE(p != nullptr, CRG_ERR_INVALID_ARGUMENT, "plan is NULL");
+  if (kernels) *kernels = p->kernels;
+  if (batched_items) *batched_items = p->batched;
+}
+
 void apply_plan_destroy_impl(crg_apply_plan* p) {
   if (!p) return;
   if (p->exec) cudaGraphExecDestroy(p->exec);
+  batch_free(p->batch);
   for (crg_regridder* r : p->held)
     if (r->refs.fetch_sub(1) == 1) free_regridder(r);
   delete p;

@@ -16,6 +16,7 @@
 //      inside rows -- the pattern of SparseArrays.sparse(i_dst, i_src, area)
 //      (intersection_areas.jl:115-121) -- plus normalize! and the derived
 //      FP32 weights used by the apply kernels.
+#include <stdlib.h>
 #include <stdarg.h>
 #include <stdio.h>
 
@@ -459,7 +460,16 @@ __global__ void k_traverse(const uint2* __restrict__ in, int64_t nin, const unsi
                            TreeView td, TreeView ts, uint2* __restrict__ next, unsigned long long* __restrict__ nnext,
                            int64_t cap_next, uint2* __restrict__ leaves, unsigned long long* __restrict__ nleaves,
                            int64_t cap_leaves, int* __restrict__ overflow) {
-  if (nin < 0) nin = (int64_t)*nin_dev;
+  if (nin < 0) {
+    // levels launched back to back (input count on the device): after a level
+    // overflowed, its output is incomplete, so the later levels do nothing
+    // (the host then restarts with the per-level loop); otherwise the count is
+    // within the input buffer, which has the capacity of the output one
+    // (one value per warp: the flag may be set while this level runs)
+    if (__shfl_sync(0xffffffffu, *(volatile int*)overflow, 0)) return;
+    nin = (int64_t)*nin_dev;
+    if (nin > cap_next) nin = cap_next;
+  }
   const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   const int64_t nloop = (nin + 31) / 32 * 32;
@@ -1183,6 +1193,19 @@ TreeView view_of(const Tree& t) {
   return v;
 }
 
+// Capacity of the frontier and leaf-pair buffers of the traversal's levels
+// launched back to back.  CRG_TRAVERSE_CAPACITY (>= 1, read at every build)
+// lowers it, to exercise the per-level fallback a frontier too large for the
+// buffers takes.
+int64_t traverse_capacity(int64_t dflt) {
+  const char* e = getenv("CRG_TRAVERSE_CAPACITY");
+  if (e) {
+    const long long v = atoll(e);
+    if (v >= 1 && v < dflt) return (int64_t)v;
+  }
+  return dflt;
+}
+
 // K3 host loop.  Returns the candidate list (dst cell, src cell).
 void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& cand, int64_t& ncand, cudaStream_t st) {
   ncand = 0;
@@ -1211,7 +1234,7 @@ void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& c
   // kept on the device: one host round trip instead of one per level.
   if (nfront > 0) {
     const int steps = std::max(D.t.nlev, S.t.nlev) - 1;
-    const int64_t cap = std::max<int64_t>(1 << 16, 2 * (D.t.ncells + S.t.ncells));
+    const int64_t cap = traverse_capacity(std::max<int64_t>(1 << 16, 2 * (D.t.ncells + S.t.ncells)));
     DBuf<uint2> fa((size_t)cap, st), fb((size_t)cap, st), fl((size_t)cap, st);
     DBuf<unsigned long long> cnt((size_t)steps + 2, st);
     DBuf<int> ovf(1, st);
@@ -1254,8 +1277,12 @@ void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& c
                                                  (int64_t)next.n, leafp.p, counters.p + 1, (int64_t)leafp.n,
                                                  counters_ovf.p);
     CRG_CHECK_CUDA(cudaGetLastError());
+    int hov = 0;
     CRG_CHECK_CUDA(cudaMemcpyAsync(hc, counters.p, sizeof(hc), cudaMemcpyDeviceToHost, st));
+    CRG_CHECK_CUDA(cudaMemcpyAsync(&hov, counters_ovf.p, sizeof(int), cudaMemcpyDeviceToHost, st));
     CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    // the buffers hold 4 pairs per input pair, the most one pair can make
+    CRG_REQUIRE(hov == 0, CRG_ERR_INTERNAL, "dual traversal overflowed its per-level buffers");
     nfront = (int64_t)hc[0];
     nleaf = (int64_t)hc[1];
     std::swap(front.p, next.p);

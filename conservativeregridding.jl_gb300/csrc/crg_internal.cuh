@@ -176,6 +176,15 @@ void host_pipeline_ends(const crg_apply_item& it, size_t& fill, size_t& drain);
 bool is_device_pointer(const void* p);
 void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const void* src, int64_t ssc, int64_t ssf,
                         void* dst, int64_t dsc, int64_t dsf, int64_t nf, int normalize, cudaStream_t st);
+// The applies of a batch that one persistent launch can run (cell-major FP32 /
+// BF16 fields or single fields, device memory): their device tables, built
+// once; handled[k] = 1 for the items it covers (the others need their own
+// crg_apply).  batch_enqueue queues its launches (at most two per field type).
+struct BatchLaunch;
+BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled);
+void batch_enqueue(const BatchLaunch* L, cudaStream_t st);
+int batch_launches(const BatchLaunch* L);
+void batch_free(BatchLaunch* L);
 // Loads the module that holds crg_apply_noalloc's static scratch on device
 // `dev` (current) and caches its address; every build calls it.
 void noalloc_prepare(int dev);
@@ -240,4 +249,5 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items);
 void apply_batch_impl(int64_t n, const crg_apply_item* items, int nthreads, cudaStream_t st);
 void apply_plan_launch_impl(crg_apply_plan* p, cudaStream_t st);
 void apply_plan_destroy_impl(crg_apply_plan* p);
+void apply_plan_info_impl(const crg_apply_plan* p, int64_t* kernels, int64_t* batched_items);
 }  // namespace crg

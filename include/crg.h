@@ -185,6 +185,15 @@ typedef struct crg_apply_plan crg_apply_plan;
 crg_status crg_apply_plan_create(int64_t n, const crg_apply_item* items, crg_apply_plan** out);
 crg_status crg_apply_plan_launch(crg_apply_plan* plan, void* stream);
 crg_status crg_apply_plan_destroy(crg_apply_plan* plan);
+/* How a plan runs (no reference counterpart): the kernel launches of one
+ * replay, and how many of its items the persistent batch launch covers.  The
+ * items of cell-major FP32 / BF16 fields (or single fields) run as one launch
+ * over all their work units -- merge-path tasks of the items with 32 fields
+ * or more in 16-byte aligned rows, groups of rows of the others -- plus one
+ * launch that sums the rows cut between tasks and zeroes empty rows; each
+ * item's result has the bits of its own crg_apply.  The other items (FP64,
+ * field-major) are captured as their own applies.  Either pointer may be NULL. */
+crg_status crg_apply_plan_info(const crg_apply_plan* plan, int64_t* kernels, int64_t* batched_items);
 
 /* Derivatives of the areas with respect to the destination grid's vertices.
  * No counterpart in the reference (it has no derivatives, Project.toml:10-23);

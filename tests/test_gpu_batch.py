@@ -160,3 +160,47 @@ def test_regrid_batch_host_pipeline(pairs, same_copy):
         expect = np.empty(dst.shape, np.float32)
         regrid_(expect, RR, x, dims=dims)
         assert np.array_equal(dst.numpy(), expect)
+
+
+@pytest.mark.parametrize("normalize", [True, False])
+def test_apply_plan_persistent_launch(pairs, normalize):
+    """One persistent launch (plus one for cut and empty rows per field type)
+    runs every cell-major FP32 / BF16 item and every single-field item: field
+    counts on both sides of the merge-path threshold (32), aligned or not
+    (K % 4), R and transpose(R), a regridder with empty rows; FP64 and
+    field-major items stay their own applies.  Bit for bit the single applies."""
+    import torch
+
+    Rs = build_batch(pairs, normalize=True)
+    # a destination partly outside the source (rows without entries in R)
+    part = Regridder(grids.lonlat_grid(np.arange(0.0, 361.0, 10.0), np.arange(-90.0, 91.0, 10.0)),
+                     grids.lonlat_grid(np.arange(0.0, 181.0, 6.0), np.arange(-30.0, 31.0, 6.0)), normalize=True)
+    gen = torch.Generator(device="cuda").manual_seed(12)
+    specs = [(1, torch.float32, 1), (3, torch.float32, 1), (7, torch.bfloat16, 1), (12, torch.float32, 1),
+             (32, torch.float32, 1), (33, torch.float32, 1), (100, torch.float32, 1), (128, torch.bfloat16, 1),
+             (200, torch.float32, 1), (512, torch.float32, 1), (64, torch.float64, 1), (20, torch.float32, 2)]
+    regs = [R if k % 2 == 0 else R.transpose() for k, R in enumerate(Rs)] + [part, part.transpose()]
+    items, expect_batched = [], 0
+    for k, (K, dt, dims) in enumerate(specs + specs[:2]):
+        RR = regs[k % len(regs)] if k < len(specs) else regs[len(Rs) + k - len(specs)]
+        n_out, n_in = RR.shape
+        shape_in, shape_out = ((n_in, K), (n_out, K)) if dims == 1 else ((K, n_in), (K, n_out))
+        if K == 1:
+            shape_in, shape_out = (n_in,), (n_out,)
+        x = torch.randn(shape_in, generator=gen, device="cuda").to(dt)
+        y = torch.full(shape_out, float("nan"), device="cuda").to(dt)
+        items.append((y, RR, x, dims))
+        expect_batched += dt != torch.float64 and (dims == 1 or K == 1)
+    plan = ApplyPlan(items, normalize=normalize)
+    info = plan.info
+    assert info["batched_items"] == expect_batched
+    for _ in range(2):
+        for y, _, _, _ in items:
+            y.fill_(float("nan"))
+        plan.launch()
+        torch.cuda.synchronize()
+        for y, RR, x, dims in items:
+            ref = torch.empty_like(y)
+            regrid_(ref, RR, x, dims=dims, normalize=normalize)
+            torch.cuda.synchronize()
+            assert torch.equal(y, ref), (tuple(y.shape), y.dtype)

@@ -99,6 +99,8 @@ def test_batch_pairs_parity_and_plan(cuda):
         items.append((y, R, x, 1))
         xs.append(x)
     plan = ApplyPlan(items)
+    # every pair in the one persistent launch: at most 3 kernels per replay
+    assert plan.info["batched_items"] == len(items) and plan.info["kernels"] <= 3, plan.info
     plan.launch()
     torch.cuda.synchronize()
     for (dst, src), R, K, (y, _, x, _) in zip(pairs, Rs, ks, items):
