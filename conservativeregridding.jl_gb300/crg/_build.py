@@ -24,7 +24,7 @@ LIB_PATH = BUILD_DIR / "libcrg_gb300.so"
 # the FP64 peak probe of the build's roofline: its own library, not part of the ABI
 PEAKS_SOURCE = "crg_peaks.cu"
 PEAKS_LIB_PATH = BUILD_DIR / "libcrg_peaks.so"
-SOURCES = ["crg_scan.cu", "crg_build.cu", "crg_layout.cu", "crg_apply.cu", "crg_grad.cu", "crg_batch.cu", "crg_se.cu", "crg_api.cu"]
+SOURCES = ["crg_scan.cu", "crg_build.cu", "crg_layout.cu", "crg_apply.cu", "crg_grad.cu", "crg_batch.cu", "crg_se.cu", "crg_tune.cu", "crg_api.cu"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: only explicit fma() fuses, so the FP64 geometry follows the
 # exact operation order that the CPU oracle restates.

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <atomic>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "crg_internal.cuh"
@@ -91,6 +92,76 @@ __global__ void k_spmv_f64(const int32_t* __restrict__ ptr, const int32_t* __res
   }
   if (row_div) acc = acc / row_div[r];
   y[r * ysc + f * ysf] = acc;
+}
+
+// FP64 fields side by side (cell-major), many of them: G lanes per row, 4
+// fields per lane (two 16-byte loads when aligned), the row's (column,
+// weight) entries loaded G at a time and broadcast by shuffles.  Each field
+// is summed exactly as k_spmv_f64 sums it -- acc = 0, then acc + (w x) per
+// entry in ascending column order, each operation rounded once -- and divided
+// by the row area, so every field has the bits of the one-field apply (and of
+// the reference's mul! then ./ areas).  The division by column areas of the
+// adjoint is applied to the input beforehand (k_div_cols_f64), the same
+// quotient k_spmv_f64 forms per entry.
+template <int G, bool kVec>
+__global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                     const double* __restrict__ val, int64_t nrows,
+                                                     const double* __restrict__ x, int64_t xs, double* __restrict__ y,
+                                                     int64_t ys, int64_t nf, const double* __restrict__ row_div) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane % G;
+  const int gbase = lane - g;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  if (r >= nrows) return;  // the whole lane group shares r
+  const int32_t k0 = __ldg(ptr + r), n = __ldg(ptr + r + 1) - k0;
+  const double div = row_div ? __ldg(row_div + r) : 1.0;
+  for (int64_t f0 = 0; f0 < nf; f0 += (int64_t)G * 4) {
+    const int64_t f = f0 + (int64_t)g * 4;
+    const bool on = f < nf;
+    const bool full = kVec && f + 4 <= nf;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int kb = 0; kb < n; kb += G) {
+      const bool in = kb + g < n;
+      const int32_t myj = in ? __ldg(idx + k0 + kb + g) : 0;
+      const double myv = in ? __ldg(val + k0 + kb + g) : 0.0;
+      const int ne = min(G, n - kb);
+#pragma unroll 4
+      for (int e = 0; e < ne; ++e) {
+        const int64_t j = __shfl_sync(gmask, myj, gbase + e);
+        const double wv = __shfl_sync(gmask, myv, gbase + e);
+        if (!on) continue;
+        const double* xp = x + j * xs + f;
+        double xv[4];
+        if (full) {
+          const double2 a = __ldg(reinterpret_cast<const double2*>(xp));
+          const double2 b = __ldg(reinterpret_cast<const double2*>(xp) + 1);
+          xv[0] = a.x; xv[1] = a.y; xv[2] = b.x; xv[3] = b.y;
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) xv[q] = f + q < nf ? __ldg(xp + q) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = __dadd_rn(acc[q], __dmul_rn(wv, xv[q]));
+      }
+    }
+    if (!on) continue;
+    double* yp = y + r * ys + f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double o = row_div ? __ddiv_rn(acc[q], div) : acc[q];
+      if (full || f + q < nf) yp[q] = o;
+    }
+  }
+}
+
+// x'[c, f] = x[c, f] / col_div[c] for the adjoint's input (cell-major).
+__global__ void k_div_cols_f64(const double* __restrict__ x, int64_t xs, int64_t ncells, int64_t nf,
+                               const double* __restrict__ col_div, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncells * nf) return;
+  const int64_t c = i / nf, f = i - c * nf;
+  out[i] = __ddiv_rn(x[c * xs + f], __ldg(col_div + c));
 }
 
 // ------------------------------------------------------------------ cell-major fields
@@ -441,8 +512,8 @@ __device__ __forceinline__ const char* cm_lane_base(const T* x, int64_t f0, int6
   return reinterpret_cast<const char*>(x + fo);
 }
 
-template <class T, bool kGaps, int B = CmGather<T>::kInFlight>
-__global__ void __launch_bounds__(256, 3)
+template <class T, bool kGaps, int B = CmGather<T>::kInFlight, int MINB = 3>
+__global__ void __launch_bounds__(256, MINB)
     k_cm_nnz(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
              const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow, const float* __restrict__ w,
              int64_t ntasks, const T* __restrict__ x,
@@ -480,16 +551,108 @@ __global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, co
 // The merge-path kernel over all 128-field passes, the fixup of rows cut
 // between tasks, and zeros for rows without entries.  `carry` holds
 // nslots * 128 floats when the layout has rows cut between tasks.
+//
+// The autotuner's candidates for this kernel (index 0 is the default): the
+// gathers in flight per warp and the blocks of 8 warps per SM (the register
+// cap follows: 80 registers at 3, 64 at 4, 128 at 2).  Every candidate sums
+// the same entries in the same order, so the choice never changes a result.
+constexpr int kCmVariants = 4;
+template <class T> struct CmVariant;
+template <> struct CmVariant<float> {
+  static constexpr int B[kCmVariants] = {8, 4, 16, 12};
+  static constexpr int MINB[kCmVariants] = {3, 4, 2, 2};
+};
+template <> struct CmVariant<__nv_bfloat16> {
+  static constexpr int B[kCmVariants] = {16, 8, 32, 24};
+  static constexpr int MINB[kCmVariants] = {3, 3, 2, 2};
+};
+
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                   float* carry, cudaStream_t st);
+                   float* carry, cudaStream_t st, int variant = 0);
+
+// The device part of an autotuner key: name and SM count of the current device.
+std::string device_key() {
+  static std::mutex mu;
+  static std::vector<std::string> names;
+  int dev = 0;
+  CRG_CHECK_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)names.size() <= dev) names.resize(dev + 1);
+  if (names[dev].empty()) {
+    cudaDeviceProp prop;
+    CRG_CHECK_CUDA(cudaGetDeviceProperties(&prop, dev));
+    char b[320];
+    snprintf(b, sizeof b, "%s/%dsm", prop.name, prop.multiProcessorCount);
+    for (char* q = b; *q; ++q)
+      if (*q == ' ' || *q == '\t') *q = '_';
+    names[dev] = b;
+  }
+  return names[dev];
+}
+
+std::string matrix_key(const char* family, const DevCsr& c, const char* dtype, int64_t nf) {
+  char b[256];
+  snprintf(b, sizeof b, "%s %s rows=%lld cols=%lld nnz=%lld %s K=%lld", family, device_key().c_str(),
+           (long long)c.nrows, (long long)c.ncols, (long long)c.nnz, dtype, (long long)nf);
+  return b;
+}
+
+// The fastest of n candidates for `key`: the cached choice, else (outside
+// stream capture) each candidate run once to warm up and twice timed with
+// CUDA events on `st`, in turn, and the choice stored.  Candidate 0 when the
+// tuner is off or the stream is capturing.  run(i) must leave the same result
+// for every i.
+template <class F>
+int tune_choose(const std::string& key, int n, cudaStream_t st, F run) {
+  int choice = 0;
+  if (n <= 1 || !tune_enabled()) return 0;
+  if (tune_lookup(key, choice)) return choice < n ? choice : 0;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  CRG_CHECK_CUDA(cudaStreamIsCapturing(st, &cs));
+  if (cs != cudaStreamCaptureStatusNone) return 0;
+  std::vector<cudaEvent_t> ev(2 * n, nullptr);
+  struct Guard {
+    std::vector<cudaEvent_t>& v;
+    ~Guard() {
+      for (auto e : v)
+        if (e) cudaEventDestroy(e);
+    }
+  } guard{ev};
+  for (auto& e : ev) CRG_CHECK_CUDA(cudaEventCreate(&e));
+  std::vector<float> ms(n, 0.f);
+  for (int i = 0; i < n; ++i) run(i);
+  for (int rep = 0; rep < 2; ++rep) {
+    for (int i = 0; i < n; ++i) {
+      CRG_CHECK_CUDA(cudaEventRecord(ev[2 * i], st));
+      run(i);
+      CRG_CHECK_CUDA(cudaEventRecord(ev[2 * i + 1], st));
+    }
+    CRG_CHECK_CUDA(cudaEventSynchronize(ev[2 * n - 1]));
+    for (int i = 0; i < n; ++i) {
+      float t = 0.f;
+      CRG_CHECK_CUDA(cudaEventElapsedTime(&t, ev[2 * i], ev[2 * i + 1]));
+      ms[i] += t;
+    }
+  }
+  for (int i = 1; i < n; ++i)
+    if (ms[i] < ms[choice]) choice = i;
+  tune_store(key, choice, ms.data(), n);
+  return choice;
+}
+
+template <class T> const char* dtype_name();
+template <> const char* dtype_name<float>() { return "f32"; }
+template <> const char* dtype_name<__nv_bfloat16>() { return "bf16"; }
 
 template <class T>
 void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
                    cudaStream_t st) {
   float* carry = nullptr;
   if (c.nslots) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * c.nslots * 128, st));
-  cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st);
+  const int v = tune_choose(matrix_key("cm_nnz", c, dtype_name<T>(), nf), kCmVariants, st,
+                            [&](int i) { cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st, i); });
+  cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st, v);
   if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
 }
 
@@ -501,19 +664,30 @@ __global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* _
   for (int64_t f = 0; f < nf; ++f) st1<T>(y + r * ys + f, 0.f);
 }
 
+template <class T, int V>
+void cm_nnz_launch(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t f0, int64_t nf,
+                   float* carry, cudaStream_t st) {
+  constexpr int B = CmVariant<T>::B[V], MINB = CmVariant<T>::MINB[V];
+  const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 8 * MINB);  // MINB blocks of 8 warps per SM
+  if (c.nextrow)
+    k_cm_nnz<T, true, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, c.nextrow, w,
+                                                                      c.ntasks, x, xs, y, ys, f0, nf, carry);
+  else
+    k_cm_nnz<T, false, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, nullptr, w,
+                                                                       c.ntasks, x, xs, y, ys, f0, nf, carry);
+}
+
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                   float* carry, cudaStream_t st) {
-  // three blocks of 8 warps per SM
-  const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 24);
+                   float* carry, cudaStream_t st, int variant) {
   for (int64_t f0 = 0; f0 < nf; f0 += 128) {
     if (c.ntasks) {
-      if (c.nextrow)
-        k_cm_nnz<T, true><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, c.nextrow, w,
-                                                                 c.ntasks, x, xs, y, ys, f0, nf, carry);
-      else
-        k_cm_nnz<T, false><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, nullptr, w,
-                                                                  c.ntasks, x, xs, y, ys, f0, nf, carry);
+      switch (variant) {
+        case 1: cm_nnz_launch<T, 1>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+        case 2: cm_nnz_launch<T, 2>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+        case 3: cm_nnz_launch<T, 3>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+        default: cm_nnz_launch<T, 0>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+      }
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (c.nsplit) {
@@ -540,18 +714,28 @@ inline SpmmPath spmm_path() {
   return p;
 }
 
+// k_cm_rows with RB rows per lane group; the autotuner picks RB (the
+// candidates 2, 1, 4; every row is summed in entry order whatever RB).
+template <class T>
+void cm_rows_rb(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf, int RB,
+                cudaStream_t st);
+
 template <class T>
 void launch_cm_rows(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
                     cudaStream_t st) {
+  static const int kRB[3] = {2, 1, 4};
+  const int v = tune_choose(matrix_key("cm_rows", c, dtype_name<T>(), nf), 3, st,
+                            [&](int i) { cm_rows_rb<T>(c, w, x, xs, y, ys, nf, kRB[i], st); });
+  cm_rows_rb<T>(c, w, x, xs, y, ys, nf, kRB[v], st);
+}
+
+template <class T>
+void cm_rows_rb(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf, int RB,
+                cudaStream_t st) {
   const int64_t n = c.nrows;
   const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
   int G = 1;
   while (G < lanes) G <<= 1;
-  static const int RB = [] {
-    const char* e = getenv("CRG_SPMM_RB");
-    int v = e ? atoi(e) : 2;
-    return (v == 1 || v == 2 || v == 4) ? v : 2;
-  }();
   const unsigned blocks = nblk((n + RB - 1) / RB * G, 256);
 #define CRG_CM(GG, RR) k_cm_rows<T, GG, RR><<<blocks, 256, 0, st>>>(c.ptr, c.idx, w, n, nullptr, x, xs, y, ys, nf)
 #define CRG_CM_RB(GG) \
@@ -566,6 +750,7 @@ void launch_cm_rows(const DevCsr& c, const float* w, const T* x, int64_t xs, T* 
   }
 #undef CRG_CM_RB
 #undef CRG_CM
+  CRG_CHECK_CUDA(cudaGetLastError());
 }
 
 // out[j * ldo + i] = in[i * ldi + j] for i < rows, j < cols: 32 x 32 tiles
@@ -641,6 +826,49 @@ void launch_transpose(const T* in, int64_t ldi, T* out, int64_t ldo, int64_t row
     k_transpose<T><<<grid, dim3(32, 8), 0, st>>>(in + r0 * ldi, ldi, out + r0, ldo, rr, cols);
   }
   CRG_CHECK_CUDA(cudaGetLastError());
+}
+
+// Cell-major FP64 fields (more than one): k_cm_rows_f64, G lanes per row.
+// With the adjoint's column division, the input is divided once per element
+// into a temporary first.
+void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const double* x, int64_t xs, double* y,
+                   int64_t ys, int64_t nf, cudaStream_t st) {
+  const int64_t n = c.nrows;
+  if (n == 0 || nf == 0) return;
+  const double* xin = x;
+  int64_t xin_s = xs;
+  double* tmp = nullptr;
+  if (adjoint && div) {
+    CRG_CHECK_CUDA(cudaMallocAsync((void**)&tmp, sizeof(double) * ((size_t)c.ncols * nf + 4), st));
+    if (c.ncols) {
+      k_div_cols_f64<<<nblk(c.ncols * nf, 256), 256, 0, st>>>(x, xs, c.ncols, nf, div, tmp);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
+    xin = tmp;
+    xin_s = nf;
+  }
+  const double* rdiv = adjoint ? nullptr : div;
+  const bool vec = nf % 4 == 0 && xin_s % 2 == 0 && ys % 2 == 0 && (uintptr_t)xin % 16 == 0 && (uintptr_t)y % 16 == 0;
+  const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
+  int G = 1;
+  while (G < lanes) G <<= 1;
+  const unsigned blocks = nblk(n * G, 256);
+#define CRG_F64_CASE(GG)                                                                                        \
+  case GG:                                                                                                      \
+    if (vec) k_cm_rows_f64<GG, true><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv); \
+    else k_cm_rows_f64<GG, false><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv);   \
+    break;
+  switch (G) {
+    CRG_F64_CASE(1)
+    CRG_F64_CASE(2)
+    CRG_F64_CASE(4)
+    CRG_F64_CASE(8)
+    CRG_F64_CASE(16)
+    CRG_F64_CASE(32)
+  }
+#undef CRG_F64_CASE
+  CRG_CHECK_CUDA(cudaGetLastError());
+  if (tmp) CRG_CHECK_CUDA(cudaFreeAsync(tmp, st));
 }
 
 template <class T>
@@ -821,49 +1049,91 @@ __device__ __forceinline__ int batch_find(const int64_t* __restrict__ unit0, int
 }
 
 // k_spmm_rows for one group of rows: lane -> (row, g), fields f = 4 g, 4 g + 4 G, ...
+// A row of up to kRowRegs entries keeps them in registers and issues all its
+// gathers of a field group before the FMAs; longer rows loop.  Either way each
+// field is summed in entry order, as the row kernels do.
+constexpr int kRowRegs = 8;
+
 template <class T>
-__device__ __forceinline__ void rows_unit(const BatchItem& it, int64_t k, int lane) {
-  const int G = 1 << it.lg;
-  const int g = lane & (G - 1);
-  const int64_t r = k * (32 >> it.lg) + (lane >> it.lg);
-  if (r >= it.nrows) return;
-  const T* __restrict__ x = static_cast<const T*>(it.x);
-  T* __restrict__ y = static_cast<T*>(it.y);
-  const int32_t k0 = __ldg(it.ptr + r), k1 = __ldg(it.ptr + r + 1);
-  const int64_t nf = it.nf;
-  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    const bool full = it.vec && f + 4 <= nf;
-    for (int32_t q = k0; q < k1; ++q) {
-      const int64_t j = __ldg(it.idx + q);
-      const float ww = __ldg(it.w + q);
-      const T* xp = x + j * it.xs + f;
-      float4 v;
-      if (full) {
-        v = ld4<T>(xp);
-      } else {
-        v.x = ld1<T>(xp);
-        v.y = f + 1 < nf ? ld1<T>(xp + 1) : 0.f;
-        v.z = f + 2 < nf ? ld1<T>(xp + 2) : 0.f;
-        v.w = f + 3 < nf ? ld1<T>(xp + 3) : 0.f;
-      }
-      acc.x = fmaf(ww, v.x, acc.x);
-      acc.y = fmaf(ww, v.y, acc.y);
-      acc.z = fmaf(ww, v.z, acc.z);
-      acc.w = fmaf(ww, v.w, acc.w);
-    }
-    T* yp = y + r * it.ys + f;
-    if (full) {
-      st4<T>(yp, acc);
-    } else {
-      st1<T>(yp, acc.x);
-      if (f + 1 < nf) st1<T>(yp + 1, acc.y);
-      if (f + 2 < nf) st1<T>(yp + 2, acc.z);
-      if (f + 3 < nf) st1<T>(yp + 3, acc.w);
-    }
+__device__ __forceinline__ float4 ld4_tail(const T* xp, int64_t f, int64_t nf, bool full) {
+  if (full) return ld4<T>(xp);
+  float4 v;
+  v.x = ld1<T>(xp);
+  v.y = f + 1 < nf ? ld1<T>(xp + 1) : 0.f;
+  v.z = f + 2 < nf ? ld1<T>(xp + 2) : 0.f;
+  v.w = f + 3 < nf ? ld1<T>(xp + 3) : 0.f;
+  return v;
+}
+
+template <class T>
+__device__ __forceinline__ void st4_tail(T* yp, float4 acc, int64_t f, int64_t nf, bool full) {
+  if (full) {
+    st4<T>(yp, acc);
+  } else {
+    st1<T>(yp, acc.x);
+    if (f + 1 < nf) st1<T>(yp + 1, acc.y);
+    if (f + 2 < nf) st1<T>(yp + 2, acc.z);
+    if (f + 3 < nf) st1<T>(yp + 3, acc.w);
   }
 }
 
+__device__ __forceinline__ void fma4(float w, float4 v, float4& acc) {
+  acc.x = fmaf(w, v.x, acc.x);
+  acc.y = fmaf(w, v.y, acc.y);
+  acc.z = fmaf(w, v.z, acc.z);
+  acc.w = fmaf(w, v.w, acc.w);
+}
+
+template <class T>
+__device__ __forceinline__ void rows_unit(const BatchItem* __restrict__ itp, int64_t k, int lane) {
+  const int lg = itp->lg;
+  const int G = 1 << lg;
+  const int g = lane & (G - 1);
+  const int64_t r = k * (32 >> lg) + (lane >> lg);
+  const int64_t nrows = itp->nrows;
+  if (r >= nrows) return;
+  const int64_t nf = itp->nf, xs = itp->xs, ys = itp->ys;
+  const bool vec = itp->vec != 0;
+  const int32_t* __restrict__ idx = itp->idx;
+  const float* __restrict__ w = itp->w;
+  const T* __restrict__ x = static_cast<const T*>(itp->x);
+  T* __restrict__ y = static_cast<T*>(itp->y) + r * ys;
+  const int32_t k0 = __ldg(itp->ptr + r), k1 = __ldg(itp->ptr + r + 1);
+  const int n = k1 - k0;
+  if (n <= kRowRegs) {
+    int64_t jj[kRowRegs];
+    float ww[kRowRegs];
+#pragma unroll
+    for (int e = 0; e < kRowRegs; ++e) {
+      jj[e] = e < n ? (int64_t)__ldg(idx + k0 + e) * xs : 0;
+      ww[e] = e < n ? __ldg(w + k0 + e) : 0.f;
+    }
+    for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+      const bool full = vec && f + 4 <= nf;
+      float4 v[kRowRegs];
+#pragma unroll
+      for (int e = 0; e < kRowRegs; ++e)
+        if (e < n) v[e] = ld4_tail<T>(x + jj[e] + f, f, nf, full);
+      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int e = 0; e < kRowRegs; ++e)
+        if (e < n) fma4(ww[e], v[e], acc);
+      st4_tail<T>(y + f, acc, f, nf, full);
+    }
+    return;
+  }
+  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+    const bool full = vec && f + 4 <= nf;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int32_t q = k0; q < k1; ++q) {
+      const int64_t j = __ldg(idx + q);
+      fma4(__ldg(w + q), ld4_tail<T>(x + j * xs + f, f, nf, full), acc);
+    }
+    st4_tail<T>(y + f, acc, f, nf, full);
+  }
+}
+
+// The merge-path items of a batch: one unit per task and 128-field pass.
 template <class T>
 __global__ void __launch_bounds__(256, 3) k_batch_apply(const BatchItem* __restrict__ items,
                                                         const int64_t* __restrict__ unit0, int nitems,
@@ -873,24 +1143,34 @@ __global__ void __launch_bounds__(256, 3) k_batch_apply(const BatchItem* __restr
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t u = gw; u < nunits; u += nw) {
-    const BatchItem& it = items[batch_find(unit0, nitems, u)];
-    const int64_t k = u - it.unit0;
-    if (it.kind == 0) {
-      const int64_t pass = k / it.ntasks, task = k - pass * it.ntasks;
-      int64_t fo;
-      bool on;
-      const char* xb = cm_lane_base<T>(static_cast<const T*>(it.x), pass * 128, it.nf, lane, fo, on);
-      const uint32_t cstride = (uint32_t)(it.xs * (int64_t)sizeof(T));
-      float* carry = it.carry ? it.carry + pass * it.nslots * 128 : nullptr;
-      if (it.gaps)
-        cm_task<T, true, B>(task, it.tasks, it.tslot, it.idx, it.rbits, it.nextrow, it.w, xb, cstride,
-                            static_cast<T*>(it.y), it.ys, fo, on, carry, lane);
-      else
-        cm_task<T, false, B>(task, it.tasks, it.tslot, it.idx, it.rbits, nullptr, it.w, xb, cstride,
-                             static_cast<T*>(it.y), it.ys, fo, on, carry, lane);
-    } else {
-      rows_unit<T>(it, k, lane);
-    }
+    const BatchItem* itp = items + batch_find(unit0, nitems, u);
+    const int64_t ntasks = itp->ntasks, k = u - itp->unit0;
+    const int64_t pass = k / ntasks, task = k - pass * ntasks;
+    int64_t fo;
+    bool on;
+    const char* xb = cm_lane_base<T>(static_cast<const T*>(itp->x), pass * 128, itp->nf, lane, fo, on);
+    const uint32_t cstride = (uint32_t)(itp->xs * (int64_t)sizeof(T));
+    float* carry = itp->carry ? itp->carry + pass * itp->nslots * 128 : nullptr;
+    if (itp->gaps)
+      cm_task<T, true, B>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb, cstride,
+                          static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
+    else
+      cm_task<T, false, B>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xb, cstride,
+                           static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
+  }
+}
+
+// The row items of a batch: one unit per group of 32 / G rows, three blocks
+// of 8 warps per SM; the gathers of a short row are all in flight at once.
+template <class T>
+__global__ void __launch_bounds__(256, 3) k_batch_rows(const BatchItem* __restrict__ items,
+                                                    const int64_t* __restrict__ unit0, int nitems, int64_t nunits) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t u = gw; u < nunits; u += nw) {
+    const BatchItem* itp = items + batch_find(unit0, nitems, u);
+    rows_unit<T>(itp, u - itp->unit0, lane);
   }
 }
 
@@ -935,10 +1215,14 @@ struct BatchLaunch {
   int device = 0;
   struct Part {
     int dtype = CRG_F32;
-    const BatchItem* items = nullptr;
+    const BatchItem* items = nullptr;  // merge-path items
     const int64_t* unit0 = nullptr;
     int nitems = 0;
     int64_t nunits = 0;
+    const BatchItem* ritems = nullptr;  // row items
+    const int64_t* runit0 = nullptr;
+    int nritems = 0;
+    int64_t nrunits = 0;
     const FinishItem* fitems = nullptr;
     const int64_t* funit0 = nullptr;
     int nfitems = 0;
@@ -949,10 +1233,10 @@ struct BatchLaunch {
 
 BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled) {
   handled.assign((size_t)n, 0);
-  std::vector<BatchItem> bi[2];
+  std::vector<BatchItem> bi[2], ri[2];  // merge-path items, row items
   std::vector<FinishItem> fi[2];
   std::vector<int64_t> carry_off[2];  // per merge-path item: float offset of its carry, -1 none
-  int64_t units[2] = {0, 0}, funits[2] = {0, 0}, carry_floats = 0;
+  int64_t units[2] = {0, 0}, runits[2] = {0, 0}, funits[2] = {0, 0}, carry_floats = 0;
   int dev = 0;
   CRG_CHECK_CUDA(cudaGetDevice(&dev));
   for (int64_t k = 0; k < n; ++k) {
@@ -1039,9 +1323,9 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
       int lg = 0;
       while ((1 << lg) < lanes) ++lg;
       b.lg = lg;
-      b.unit0 = units[d];
-      units[d] += (c.nrows + (32 >> lg) - 1) / (32 >> lg);
-      bi[d].push_back(b);
+      b.unit0 = runits[d];
+      runits[d] += (c.nrows + (32 >> lg) - 1) / (32 >> lg);
+      ri[d].push_back(b);
     }
     handled[k] = 1;
   }
@@ -1052,10 +1336,12 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
     bytes += (b + 255) / 256 * 256;
     return at;
   };
-  size_t off_items[2], off_u0[2], off_f[2], off_fu0[2];
+  size_t off_items[2], off_u0[2], off_r[2], off_ru0[2], off_f[2], off_fu0[2];
   for (int d = 0; d < 2; ++d) {
     off_items[d] = take(bi[d].size() * sizeof(BatchItem));
     off_u0[d] = take(bi[d].size() * sizeof(int64_t));
+    off_r[d] = take(ri[d].size() * sizeof(BatchItem));
+    off_ru0[d] = take(ri[d].size() * sizeof(int64_t));
     off_f[d] = take(fi[d].size() * sizeof(FinishItem));
     off_fu0[d] = take(fi[d].size() * sizeof(int64_t));
   }
@@ -1067,7 +1353,7 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
     char* base = static_cast<char*>(L->mem);
     float* carry = reinterpret_cast<float*>(base + off_carry);
     for (int d = 0; d < 2; ++d) {
-      if (bi[d].empty() && fi[d].empty()) continue;
+      if (bi[d].empty() && ri[d].empty() && fi[d].empty()) continue;
       size_t mp = 0;
       for (auto& b : bi[d])
         if (b.kind == 0) {
@@ -1076,14 +1362,17 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
         }
       for (auto& f : fi[d])
         if (f.kind == 0) f.carry = carry + (intptr_t)f.carry;
-      std::vector<int64_t> u0(bi[d].size()), fu0(fi[d].size());
+      std::vector<int64_t> u0(bi[d].size()), ru0(ri[d].size()), fu0(fi[d].size());
       for (size_t q = 0; q < bi[d].size(); ++q) u0[q] = bi[d][q].unit0;
+      for (size_t q = 0; q < ri[d].size(); ++q) ru0[q] = ri[d][q].unit0;
       for (size_t q = 0; q < fi[d].size(); ++q) fu0[q] = fi[d][q].unit0;
       auto up = [&](size_t off, const void* src, size_t nb) {
         if (nb) CRG_CHECK_CUDA(cudaMemcpy(base + off, src, nb, cudaMemcpyHostToDevice));
       };
       up(off_items[d], bi[d].data(), bi[d].size() * sizeof(BatchItem));
       up(off_u0[d], u0.data(), u0.size() * sizeof(int64_t));
+      up(off_r[d], ri[d].data(), ri[d].size() * sizeof(BatchItem));
+      up(off_ru0[d], ru0.data(), ru0.size() * sizeof(int64_t));
       up(off_f[d], fi[d].data(), fi[d].size() * sizeof(FinishItem));
       up(off_fu0[d], fu0.data(), fu0.size() * sizeof(int64_t));
       BatchLaunch::Part p;
@@ -1092,6 +1381,10 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
       p.unit0 = reinterpret_cast<const int64_t*>(base + off_u0[d]);
       p.nitems = (int)bi[d].size();
       p.nunits = units[d];
+      p.ritems = reinterpret_cast<const BatchItem*>(base + off_r[d]);
+      p.runit0 = reinterpret_cast<const int64_t*>(base + off_ru0[d]);
+      p.nritems = (int)ri[d].size();
+      p.nrunits = runits[d];
       p.fitems = reinterpret_cast<const FinishItem*>(base + off_f[d]);
       p.funit0 = reinterpret_cast<const int64_t*>(base + off_fu0[d]);
       p.nfitems = (int)fi[d].size();
@@ -1108,6 +1401,15 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
 void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
   const int64_t max_warps = (int64_t)num_sms() * 24;  // three blocks of 8 warps per SM
   for (const auto& p : L->parts) {
+    if (p.nrunits) {
+      const int64_t warps = std::min<int64_t>(p.nrunits, max_warps);
+      if (p.dtype == CRG_F32)
+        k_batch_rows<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems, p.nrunits);
+      else
+        k_batch_rows<__nv_bfloat16><<<nblk(warps * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems,
+                                                                            p.nrunits);
+      CRG_CHECK_CUDA(cudaGetLastError());
+    }
     if (p.nunits) {
       const int64_t warps = std::min<int64_t>(p.nunits, max_warps);
       if (p.dtype == CRG_F32)
@@ -1130,7 +1432,7 @@ void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
 
 int batch_launches(const BatchLaunch* L) {
   int n = 0;
-  for (const auto& p : L->parts) n += (p.nunits > 0) + (p.nfunits > 0);
+  for (const auto& p : L->parts) n += (p.nunits > 0) + (p.nrunits > 0) + (p.nfunits > 0);
   return n;
 }
 
@@ -1230,7 +1532,9 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   // the apply on device buffers
   auto compute = [&](const void* x, int64_t xsc, int64_t xsf, void* y, int64_t ysc, int64_t ysf, int64_t n,
                      cudaStream_t s) {
-    if (dtype == CRG_F64) {
+    if (dtype == CRG_F64 && xsf == 1 && ysf == 1 && n > 1 && spmm_path() == SpmmPath::kAuto) {
+      launch_cm_f64(c, adjoint, div, (const double*)x, xsc, (double*)y, ysc, n, s);
+    } else if (dtype == CRG_F64) {
       const double* cdiv = adjoint ? div : nullptr;
       const double* rdiv = adjoint ? nullptr : div;
       for (int64_t f0 = 0; f0 < n; f0 += 65535) {

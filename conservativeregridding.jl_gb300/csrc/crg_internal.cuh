@@ -185,6 +185,11 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
 void batch_enqueue(const BatchLaunch* L, cudaStream_t st);
 int batch_launches(const BatchLaunch* L);
 void batch_free(BatchLaunch* L);
+// The autotuner's table of choices (crg_tune.cu): the fastest candidate of a
+// kernel family per key, persisted to a small file.
+bool tune_enabled();
+bool tune_lookup(const std::string& key, int& choice);
+void tune_store(const std::string& key, int choice, const float* ms, int n);
 // Loads the module that holds crg_apply_noalloc's static scratch on device
 // `dev` (current) and caches its address; every build calls it.
 void noalloc_prepare(int dev);
