@@ -393,13 +393,13 @@ int num_sms() {
 // k_cm_fixup.
 //
 // The gathers in flight hold the raw loads (16 bytes of 4 FP32 fields, 8 bytes
-// of 4 BF16 fields), converted to FP32 when consumed; BF16 keeps 16 of them in
-// flight instead of 8, so that a warp has as many bytes under way as with FP32
-// in about the same registers.
+// of 4 BF16 fields), converted to FP32 when consumed.  kInFlight is the
+// default count; the autotuner's candidates (CmVariant) set others.
 template <class T> struct CmGather;
 template <> struct CmGather<float> {
   using Raw = float4;
-  static constexpr int kInFlight = 8;
+  static constexpr int kInFlight = 4;
+  static constexpr int kMinBlocks = 4;
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const float4*>(base + off));
   }
@@ -407,7 +407,8 @@ template <> struct CmGather<float> {
 };
 template <> struct CmGather<__nv_bfloat16> {
   using Raw = uint2;
-  static constexpr int kInFlight = 16;
+  static constexpr int kInFlight = 8;
+  static constexpr int kMinBlocks = 3;
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const uint2*>(base + off));
   }
@@ -559,12 +560,12 @@ __global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, co
 constexpr int kCmVariants = 4;
 template <class T> struct CmVariant;
 template <> struct CmVariant<float> {
-  static constexpr int B[kCmVariants] = {8, 4, 16, 12};
-  static constexpr int MINB[kCmVariants] = {3, 4, 2, 2};
+  static constexpr int B[kCmVariants] = {4, 8, 16, 12};
+  static constexpr int MINB[kCmVariants] = {4, 3, 2, 2};
 };
 template <> struct CmVariant<__nv_bfloat16> {
-  static constexpr int B[kCmVariants] = {16, 8, 32, 24};
-  static constexpr int MINB[kCmVariants] = {3, 3, 2, 2};
+  static constexpr int B[kCmVariants] = {8, 16, 4, 24};
+  static constexpr int MINB[kCmVariants] = {3, 3, 4, 2};
 };
 
 template <class T>
@@ -1133,9 +1134,10 @@ __device__ __forceinline__ void rows_unit(const BatchItem* __restrict__ itp, int
   }
 }
 
-// The merge-path items of a batch: one unit per task and 128-field pass.
+// The merge-path items of a batch: one unit per task and 128-field pass (the
+// default gathers in flight and blocks per SM of k_cm_nnz).
 template <class T>
-__global__ void __launch_bounds__(256, 3) k_batch_apply(const BatchItem* __restrict__ items,
+__global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(const BatchItem* __restrict__ items,
                                                         const int64_t* __restrict__ unit0, int nitems,
                                                         int64_t nunits) {
   constexpr int B = CmGather<T>::kInFlight;
@@ -1411,7 +1413,8 @@ void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (p.nunits) {
-      const int64_t warps = std::min<int64_t>(p.nunits, max_warps);
+      const int minb = p.dtype == CRG_F32 ? CmGather<float>::kMinBlocks : CmGather<__nv_bfloat16>::kMinBlocks;
+      const int64_t warps = std::min<int64_t>(p.nunits, (int64_t)num_sms() * 8 * minb);
       if (p.dtype == CRG_F32)
         k_batch_apply<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits);
       else
