@@ -166,6 +166,31 @@ __global__ void k_div_cols_f64(const double* __restrict__ x, int64_t xs, int64_t
 
 // ------------------------------------------------------------------ cell-major fields
 
+// One row (entries k0..k1) without 4-field vectors: lane g of a group of G
+// takes fields f0 + g + G t (t < 4) of each block of 4 G fields, so that each
+// scalar load of the group reads consecutive elements.  Every field is summed
+// in entry order from zero.
+template <class T>
+__device__ __forceinline__ void rows_strided(const int32_t* __restrict__ idx, const float* __restrict__ w, int32_t k0,
+                                             int32_t k1, const T* __restrict__ x, int64_t xs, T* __restrict__ y,
+                                             int64_t nf, int g, int G) {
+  for (int64_t f0 = 0; f0 < nf; f0 += (int64_t)G * 4) {
+    const int64_t f = f0 + g;
+    float a[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int32_t q = k0; q < k1; ++q) {
+      const int64_t j = __ldg(idx + q);
+      const float ww = __ldg(w + q);
+      const T* xp = x + j * xs + f;
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        if (f + (int64_t)t * G < nf) a[t] = fmaf(ww, ld1<T>(xp + (int64_t)t * G), a[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (f + (int64_t)t * G < nf) st1<T>(y + f + (int64_t)t * G, a[t]);
+  }
+}
+
 template <class T, int G, bool kVec>
 __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                                                    const float* __restrict__ w, int64_t nrows, const T* __restrict__ x,
@@ -174,6 +199,10 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
   if (r >= nrows) return;
   const int32_t k0 = ptr[r], k1 = ptr[r + 1];
+  if (!kVec) {
+    rows_strided<T>(idx, w, k0, k1, x, xsc, y + r * ysc, nf, g, G);
+    return;
+  }
   for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const bool full = kVec && f + 4 <= nf;
@@ -1049,12 +1078,8 @@ __device__ __forceinline__ int batch_find(const int64_t* __restrict__ unit0, int
   return lo;
 }
 
-// k_spmm_rows for one group of rows: lane -> (row, g), fields f = 4 g, 4 g + 4 G, ...
-// A row of up to kRowRegs entries keeps them in registers and issues all its
-// gathers of a field group before the FMAs; longer rows loop.  Either way each
-// field is summed in entry order, as the row kernels do.
-constexpr int kRowRegs = 8;
-
+// k_spmm_rows for one group of rows: lane -> (row, g), fields f = 4 g, 4 g + 4 G, ...;
+// each field summed in entry order, as the row kernels do.
 template <class T>
 __device__ __forceinline__ float4 ld4_tail(const T* xp, int64_t f, int64_t nf, bool full) {
   if (full) return ld4<T>(xp);
@@ -1078,57 +1103,35 @@ __device__ __forceinline__ void st4_tail(T* yp, float4 acc, int64_t f, int64_t n
   }
 }
 
-__device__ __forceinline__ void fma4(float w, float4 v, float4& acc) {
-  acc.x = fmaf(w, v.x, acc.x);
-  acc.y = fmaf(w, v.y, acc.y);
-  acc.z = fmaf(w, v.z, acc.z);
-  acc.w = fmaf(w, v.w, acc.w);
-}
-
 template <class T>
 __device__ __forceinline__ void rows_unit(const BatchItem* __restrict__ itp, int64_t k, int lane) {
   const int lg = itp->lg;
   const int G = 1 << lg;
   const int g = lane & (G - 1);
   const int64_t r = k * (32 >> lg) + (lane >> lg);
-  const int64_t nrows = itp->nrows;
-  if (r >= nrows) return;
-  const int64_t nf = itp->nf, xs = itp->xs, ys = itp->ys;
+  if (r >= itp->nrows) return;
+  const int64_t nf = itp->nf, xs = itp->xs;
   const bool vec = itp->vec != 0;
   const int32_t* __restrict__ idx = itp->idx;
   const float* __restrict__ w = itp->w;
   const T* __restrict__ x = static_cast<const T*>(itp->x);
-  T* __restrict__ y = static_cast<T*>(itp->y) + r * ys;
+  T* __restrict__ y = static_cast<T*>(itp->y) + r * itp->ys;
   const int32_t k0 = __ldg(itp->ptr + r), k1 = __ldg(itp->ptr + r + 1);
-  const int n = k1 - k0;
-  if (n <= kRowRegs) {
-    int64_t jj[kRowRegs];
-    float ww[kRowRegs];
-#pragma unroll
-    for (int e = 0; e < kRowRegs; ++e) {
-      jj[e] = e < n ? (int64_t)__ldg(idx + k0 + e) * xs : 0;
-      ww[e] = e < n ? __ldg(w + k0 + e) : 0.f;
-    }
-    for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
-      const bool full = vec && f + 4 <= nf;
-      float4 v[kRowRegs];
-#pragma unroll
-      for (int e = 0; e < kRowRegs; ++e)
-        if (e < n) v[e] = ld4_tail<T>(x + jj[e] + f, f, nf, full);
-      float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int e = 0; e < kRowRegs; ++e)
-        if (e < n) fma4(ww[e], v[e], acc);
-      st4_tail<T>(y + f, acc, f, nf, full);
-    }
+  if (!vec) {
+    rows_strided<T>(idx, w, k0, k1, x, xs, y, nf, g, G);
     return;
   }
   for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
-    const bool full = vec && f + 4 <= nf;
+    const bool full = f + 4 <= nf;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (int32_t q = k0; q < k1; ++q) {
       const int64_t j = __ldg(idx + q);
-      fma4(__ldg(w + q), ld4_tail<T>(x + j * xs + f, f, nf, full), acc);
+      const float ww = __ldg(w + q);
+      const float4 v = ld4_tail<T>(x + j * xs + f, f, nf, full);
+      acc.x = fmaf(ww, v.x, acc.x);
+      acc.y = fmaf(ww, v.y, acc.y);
+      acc.z = fmaf(ww, v.z, acc.z);
+      acc.w = fmaf(ww, v.w, acc.w);
     }
     st4_tail<T>(y + f, acc, f, nf, full);
   }
@@ -1162,18 +1165,17 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
   }
 }
 
-// The row items of a batch: one unit per group of 32 / G rows, three blocks
-// of 8 warps per SM; the gathers of a short row are all in flight at once.
+// The row items of a batch: one warp per unit (a group of 32 / G rows), the
+// grid covering every unit, so that as many warps are resident as the
+// per-item row kernels have.
 template <class T>
-__global__ void __launch_bounds__(256, 3) k_batch_rows(const BatchItem* __restrict__ items,
+__global__ void __launch_bounds__(256) k_batch_rows(const BatchItem* __restrict__ items,
                                                     const int64_t* __restrict__ unit0, int nitems, int64_t nunits) {
   const int lane = threadIdx.x & 31;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t u = gw; u < nunits; u += nw) {
-    const BatchItem* itp = items + batch_find(unit0, nitems, u);
-    rows_unit<T>(itp, u - itp->unit0, lane);
-  }
+  const int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (u >= nunits) return;
+  const BatchItem* itp = items + batch_find(unit0, nitems, u);
+  rows_unit<T>(itp, u - itp->unit0, lane);
 }
 
 template <class T>
@@ -1404,12 +1406,11 @@ void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
   const int64_t max_warps = (int64_t)num_sms() * 24;  // three blocks of 8 warps per SM
   for (const auto& p : L->parts) {
     if (p.nrunits) {
-      const int64_t warps = std::min<int64_t>(p.nrunits, max_warps);
       if (p.dtype == CRG_F32)
-        k_batch_rows<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems, p.nrunits);
+        k_batch_rows<float><<<nblk(p.nrunits * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems, p.nrunits);
       else
-        k_batch_rows<__nv_bfloat16><<<nblk(warps * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems,
-                                                                            p.nrunits);
+        k_batch_rows<__nv_bfloat16><<<nblk(p.nrunits * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems,
+                                                                                p.nrunits);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (p.nunits) {
