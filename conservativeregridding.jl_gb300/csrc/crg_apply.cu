@@ -32,6 +32,7 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "crg_internal.cuh"
@@ -532,6 +533,158 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
   flush(cur);
 }
 
+// BF16 fields in 16-byte aligned rows of a multiple of 8 fields: each lane
+// takes 8 fields (one 16-byte load), so 16 lanes cover a 128-field pass and
+// the two half-warps gather two entries at once -- half 0 the even entries of
+// the task, half 1 the odd ones -- with B loads in flight per lane.  A row's
+// sum is (its even entries) + (its odd entries), each accumulated in entry
+// order in FP32: the half-warps' sums are added when the row ends (the same
+// value in both halves, addition being commutative) and half 0 writes the
+// row.  Deterministic, and the same in every path that runs BF16 fields
+// (crg_apply, crg_apply_noalloc, plans); rows cut between tasks go through
+// the carry slots like the 4-field kernel's.
+template <bool kGaps, int B>
+__device__ __forceinline__ void cm_task_h8(int64_t task, const int4* __restrict__ tasks,
+                                           const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
+                                           const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow,
+                                           const float* __restrict__ w, const char* xb, uint32_t cstride,
+                                           __nv_bfloat16* __restrict__ y, int64_t ys, int64_t fo, bool on,
+                                           float* __restrict__ carry, int lane) {
+  const int half = lane >> 4, hl = lane & 15;
+  const int4 tr = __ldg(tasks + task);
+  const int32_t e0 = tr.x, e1 = tr.y;
+  if (e0 >= e1) return;  // warp-uniform
+  const int32_t first = tr.z & 0x7fffffff;
+  const int32_t carry_first = tr.z < 0 ? first : -1;
+  const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
+  const int2 slot = (tr.z | tr.w) < 0 ? __ldg(tslot + task) : make_int2(-1, -1);
+  int32_t cur = first;
+  float acc[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc[i] = 0.f;
+  // the row's total in both halves, written by half 0 (warp-uniform call)
+  auto flush = [&](int32_t row) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 16);
+    if (half != 0 || !on) return;
+    if (row == carry_first || row == carry_last) {
+      float* c = carry + (int64_t)(row == carry_first ? slot.x : slot.y) * 128 + hl * 8;
+      *reinterpret_cast<float4*>(c) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+      *reinterpret_cast<float4*>(c + 4) = make_float4(acc[4], acc[5], acc[6], acc[7]);
+    } else {
+      uint4 u;
+      __nv_bfloat162 b;
+      b = __floats2bfloat162_rn(acc[0], acc[1]); u.x = *reinterpret_cast<uint32_t*>(&b);
+      b = __floats2bfloat162_rn(acc[2], acc[3]); u.y = *reinterpret_cast<uint32_t*>(&b);
+      b = __floats2bfloat162_rn(acc[4], acc[5]); u.z = *reinterpret_cast<uint32_t*>(&b);
+      b = __floats2bfloat162_rn(acc[6], acc[7]); u.w = *reinterpret_cast<uint32_t*>(&b);
+      *reinterpret_cast<uint4*>(y + (int64_t)row * ys + fo) = u;
+    }
+  };
+  auto zero = [&]() {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = 0.f;
+  };
+  auto load = [&](int32_t c0, uint32_t& starts, uint32_t& o, float& wt) {
+    const int32_t e = c0 + lane;
+    const bool valid = e < e1;
+    o = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
+    wt = valid ? __ldg(w + e) : 0.f;
+    starts = __funnelshift_r(__ldg(rbits + (c0 >> 5)), __ldg(rbits + (c0 >> 5) + 1), (uint32_t)c0 & 31u);
+    if (e1 - c0 < 32) starts &= (1u << (e1 - c0)) - 1u;
+  };
+  uint32_t starts, myo;
+  float myw;
+  load(e0, starts, myo, myw);
+  starts &= ~1u;  // entry e0 belongs to row `first`
+  for (int32_t c0 = e0; c0 < e1; c0 += 32) {
+    uint32_t nstarts = 0u, no = 0u;
+    float nwt = 0.f;
+    if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
+    const unsigned newrow = starts;
+    const int n = e1 - c0 < 32 ? e1 - c0 : 32;
+    for (int k = 0; k < n; k += 2 * B) {
+      uint4 v[B];
+      float ww[B];
+#pragma unroll
+      for (int h = 0; h < B; ++h) {
+        const int src = (k + 2 * h + half) & 31;  // this half's entry of pair h
+        const uint32_t o = __shfl_sync(0xffffffffu, myo, src);
+        ww[h] = __shfl_sync(0xffffffffu, myw, src);
+        v[h] = __ldg(reinterpret_cast<const uint4*>(xb + o));  // past-the-end entries: cell 0, weight 0
+      }
+#pragma unroll
+      for (int h = 0; h < B; ++h) {
+        const int ke = k + 2 * h;  // half 0's entry; half 1 has ke + 1
+        if (ke >= n) break;
+        if ((newrow >> ke) & 1u) {
+          flush(cur);
+          cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
+          zero();
+        }
+        const bool odd_in = ke + 1 < n;
+        if (half == 0) {
+          const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].x));
+          const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].y));
+          const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].z));
+          const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].w));
+          acc[0] = fmaf(ww[h], a.x, acc[0]); acc[1] = fmaf(ww[h], a.y, acc[1]);
+          acc[2] = fmaf(ww[h], b.x, acc[2]); acc[3] = fmaf(ww[h], b.y, acc[3]);
+          acc[4] = fmaf(ww[h], c.x, acc[4]); acc[5] = fmaf(ww[h], c.y, acc[5]);
+          acc[6] = fmaf(ww[h], d.x, acc[6]); acc[7] = fmaf(ww[h], d.y, acc[7]);
+        }
+        if (!odd_in) break;
+        if ((newrow >> (ke + 1)) & 1u) {
+          flush(cur);
+          cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
+          zero();
+        }
+        if (half == 1) {
+          const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].x));
+          const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].y));
+          const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].z));
+          const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].w));
+          acc[0] = fmaf(ww[h], a.x, acc[0]); acc[1] = fmaf(ww[h], a.y, acc[1]);
+          acc[2] = fmaf(ww[h], b.x, acc[2]); acc[3] = fmaf(ww[h], b.y, acc[3]);
+          acc[4] = fmaf(ww[h], c.x, acc[4]); acc[5] = fmaf(ww[h], c.y, acc[5]);
+          acc[6] = fmaf(ww[h], d.x, acc[6]); acc[7] = fmaf(ww[h], d.y, acc[7]);
+        }
+      }
+    }
+    starts = nstarts;
+    myo = no;
+    myw = nwt;
+  }
+  flush(cur);
+}
+
+// The lane's field base of a 128-field pass starting at f0 for cm_task_h8:
+// 8 fields per lane, 16 lanes per entry.
+__device__ __forceinline__ const char* cm_lane_base_h8(const __nv_bfloat16* x, int64_t f0, int64_t nf, int lane,
+                                                       int64_t& fo, bool& on) {
+  const int64_t f = f0 + (int64_t)(lane & 15) * 8;
+  on = f < nf;
+  fo = on ? f : f0;
+  return reinterpret_cast<const char*>(x + fo);
+}
+
+template <bool kGaps, int B, int MINB>
+__global__ void __launch_bounds__(256, MINB)
+    k_cm_nnz_h8(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
+                const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow, const float* __restrict__ w,
+                int64_t ntasks, const __nv_bfloat16* __restrict__ x, int64_t xs, __nv_bfloat16* __restrict__ y,
+                int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int64_t fo;
+  bool on;
+  const char* xb = cm_lane_base_h8(x, f0, nf, lane, fo, on);
+  const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(__nv_bfloat16));
+  for (int64_t task = gw; task < ntasks; task += nw)
+    cm_task_h8<kGaps, B>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, on, carry, lane);
+}
+
 // The lane's field base of one 128-field pass starting at f0.
 template <class T>
 __device__ __forceinline__ const char* cm_lane_base(const T* x, int64_t f0, int64_t nf, int lane, int64_t& fo,
@@ -596,6 +749,18 @@ template <> struct CmVariant<__nv_bfloat16> {
   static constexpr int B[kCmVariants] = {8, 16, 4, 24};
   static constexpr int MINB[kCmVariants] = {3, 3, 4, 2};
 };
+
+// The half-warp BF16 kernel's candidates (pairs of entries in flight per lane).
+struct CmVariantH8 {
+  static constexpr int B[kCmVariants] = {4, 8, 2, 6};
+  static constexpr int MINB[kCmVariants] = {4, 3, 4, 3};
+};
+
+// Whether BF16 fields take the half-warp kernel: 16-byte loads and stores of
+// 8 fields need rows of a multiple of 8 fields in 16-byte aligned memory.
+inline bool bf16_h8(const void* x, int64_t xs, const void* y, int64_t ys, int64_t nf) {
+  return nf % 8 == 0 && xs % 8 == 0 && ys % 8 == 0 && (uintptr_t)x % 16 == 0 && (uintptr_t)y % 16 == 0;
+}
 
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
@@ -697,6 +862,19 @@ __global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* _
 template <class T, int V>
 void cm_nnz_launch(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t f0, int64_t nf,
                    float* carry, cudaStream_t st) {
+  if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+    if (bf16_h8(x, xs, y, ys, nf)) {
+      constexpr int B = CmVariantH8::B[V], MINB = CmVariantH8::MINB[V];
+      const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 8 * MINB);
+      if (c.nextrow)
+        k_cm_nnz_h8<true, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, c.nextrow,
+                                                                          w, c.ntasks, x, xs, y, ys, f0, nf, carry);
+      else
+        k_cm_nnz_h8<false, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, nullptr,
+                                                                           w, c.ntasks, x, xs, y, ys, f0, nf, carry);
+      return;
+    }
+  }
   constexpr int B = CmVariant<T>::B[V], MINB = CmVariant<T>::MINB[V];
   const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 8 * MINB);  // MINB blocks of 8 warps per SM
   if (c.nextrow)
@@ -1041,7 +1219,7 @@ struct BatchItem {
   int32_t kind;    // 0 merge-path, 1 rows
   int32_t gaps;    // merge-path: some rows have no entries (nextrow)
   int32_t lg;      // rows: log2 of the lanes per row
-  int32_t vec;     // rows: 4-field vector access
+  int32_t vec;     // rows: 4-field vector access; merge-path BF16: the half-warp kernel (cm_task_h8)
   int64_t ntasks;  // merge-path: tasks per 128-field pass
   int64_t nrows, nf, xs, ys, nslots;
   const int4* tasks;
@@ -1156,6 +1334,19 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
     const char* xb = cm_lane_base<T>(static_cast<const T*>(itp->x), pass * 128, itp->nf, lane, fo, on);
     const uint32_t cstride = (uint32_t)(itp->xs * (int64_t)sizeof(T));
     float* carry = itp->carry ? itp->carry + pass * itp->nslots * 128 : nullptr;
+    if constexpr (std::is_same<T, __nv_bfloat16>::value) {
+      if (itp->vec) {
+        constexpr int BH = CmVariantH8::B[0];
+        const char* xh = cm_lane_base_h8(static_cast<const T*>(itp->x), pass * 128, itp->nf, lane, fo, on);
+        if (itp->gaps)
+          cm_task_h8<true, BH>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xh,
+                               cstride, static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
+        else
+          cm_task_h8<false, BH>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xh, cstride,
+                                static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
+        continue;
+      }
+    }
     if (itp->gaps)
       cm_task<T, true, B>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb, cstride,
                           static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
@@ -1282,6 +1473,7 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
       // the merge path, as launch_cm_nnz runs it
       b.kind = 0;
       b.gaps = c.nextrow != nullptr;
+      b.vec = d == 1 && bf16_h8(it.src, ssc, it.dst, dsc, nf);
       b.ntasks = c.ntasks;
       b.nslots = c.nslots;
       b.tasks = c.tasks;

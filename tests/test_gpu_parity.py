@@ -493,3 +493,35 @@ def test_row_col_sums_on_request_from_threads(cuda):
     assert np.all(want_c[~covered] < R.src_areas[~covered])
     rs2, cs2 = R.transpose().row_col_sums()  # the transpose view shares the handle's sums
     assert np.array_equal(rs2, want_r) and np.array_equal(cs2, want_c)
+
+
+@pytest.mark.parametrize("K", [128, 64, 40, 200])
+@pytest.mark.parametrize("case", ["cut_rows", "empty_rows"])
+def test_bf16_apply_cut_and_empty_rows(cuda, K, case):
+    """BF16 cell-major fields (FP32 accumulation) against the FP64 apply of the
+    same rounded inputs, on matrices with rows cut between merge-path tasks
+    (10-degree cells over HEALPix 32: ~30 entries per row) and with rows that
+    have no entries (a destination partly outside the source), both
+    directions: within the BF16 output rounding."""
+    import torch
+
+    if case == "cut_rows":
+        R = Regridder(grids.lonlat_regular(10.0, 10.0), grids.healpix_grid(32), normalize=True)
+        assert R.info["cut_rows"][0] > 0
+    else:
+        R = Regridder(grids.lonlat_grid(np.arange(0.0, 361.0, 10.0), np.arange(-90.0, 91.0, 10.0)),
+                      grids.lonlat_grid(np.arange(0.0, 181.0, 6.0), np.arange(-30.0, 31.0, 6.0)), normalize=True)
+        assert R.info["empty_rows"][0] > 0
+    gen = torch.Generator(device="cuda").manual_seed(K)
+    A = R.intersections
+    for RR, counts in ((R, A.getnnz(axis=1)), (R.transpose(), A.getnnz(axis=0))):
+        n_out, n_in = RR.shape
+        x = torch.randn((n_in, K), generator=gen, device="cuda").bfloat16()
+        y = torch.full((n_out, K), float("nan"), device="cuda").bfloat16()
+        regrid_(y, RR, x, dims=1)
+        ref = torch.empty((n_out, K), dtype=torch.float64, device="cuda")
+        regrid_(ref, RR, x.double(), dims=1)
+        err = (y.double() - ref).abs().max().item()
+        assert np.isfinite(err) and err <= 8e-3 * ref.abs().max().item(), err
+        empty = torch.from_numpy(np.asarray(counts) == 0).cuda()
+        assert bool((y[empty] == 0).all())
