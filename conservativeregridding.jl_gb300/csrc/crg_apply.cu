@@ -1281,37 +1281,77 @@ __device__ __forceinline__ void st4_tail(T* yp, float4 acc, int64_t f, int64_t n
   }
 }
 
+// One group of rows of a row item: G lanes per row (lane group g = lane % G),
+// fields in blocks of 4 G -- 4 consecutive fields per lane when the rows are
+// 4-vectors, else 4 fields strided by G (contiguous scalar loads across the
+// group).  The group loads G of the row's (column, weight) entries at once and
+// broadcasts them by shuffles; 4 entries' gathers are issued before their
+// FMAs.  Every field is summed in entry order from zero, as the row kernels
+// of crg_apply do.
 template <class T>
 __device__ __forceinline__ void rows_unit(const BatchItem* __restrict__ itp, int64_t k, int lane) {
   const int lg = itp->lg;
   const int G = 1 << lg;
   const int g = lane & (G - 1);
+  const int gbase = lane - g;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << gbase);
   const int64_t r = k * (32 >> lg) + (lane >> lg);
-  if (r >= itp->nrows) return;
+  if (r >= itp->nrows) return;  // the whole lane group shares r
   const int64_t nf = itp->nf, xs = itp->xs;
   const bool vec = itp->vec != 0;
   const int32_t* __restrict__ idx = itp->idx;
   const float* __restrict__ w = itp->w;
   const T* __restrict__ x = static_cast<const T*>(itp->x);
   T* __restrict__ y = static_cast<T*>(itp->y) + r * itp->ys;
-  const int32_t k0 = __ldg(itp->ptr + r), k1 = __ldg(itp->ptr + r + 1);
-  if (!vec) {
-    rows_strided<T>(idx, w, k0, k1, x, xs, y, nf, g, G);
-    return;
-  }
-  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
-    const bool full = f + 4 <= nf;
+  const int32_t k0 = __ldg(itp->ptr + r), n = __ldg(itp->ptr + r + 1) - k0;
+  for (int64_t f0 = 0; f0 < nf; f0 += (int64_t)G * 4) {
+    // this lane's 4 fields: f + s * t, t < 4
+    const int64_t f = vec ? f0 + (int64_t)g * 4 : f0 + g;
+    const int64_t s = vec ? 1 : G;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int32_t q = k0; q < k1; ++q) {
-      const int64_t j = __ldg(idx + q);
-      const float ww = __ldg(w + q);
-      const float4 v = ld4_tail<T>(x + j * xs + f, f, nf, full);
-      acc.x = fmaf(ww, v.x, acc.x);
-      acc.y = fmaf(ww, v.y, acc.y);
-      acc.z = fmaf(ww, v.z, acc.z);
-      acc.w = fmaf(ww, v.w, acc.w);
+    for (int kb = 0; kb < n; kb += G) {
+      const bool in = kb + g < n;
+      const int32_t myj = in ? __ldg(idx + k0 + kb + g) : 0;
+      const float myw = in ? __ldg(w + k0 + kb + g) : 0.f;
+      const int ne = min(G, n - kb);
+      for (int e = 0; e < ne; e += 4) {
+        float4 v[4];
+        float ww[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          const int src = gbase + min(e + h, G - 1);
+          const int64_t j = __shfl_sync(gmask, myj, src);
+          ww[h] = __shfl_sync(gmask, myw, src);
+          const T* xp = x + j * xs + f;
+          if (e + h >= ne) {
+            v[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+          } else if (vec) {
+            v[h] = ld4<T>(xp);
+          } else {
+            v[h].x = f < nf ? ld1<T>(xp) : 0.f;
+            v[h].y = f + s < nf ? ld1<T>(xp + s) : 0.f;
+            v[h].z = f + 2 * s < nf ? ld1<T>(xp + 2 * s) : 0.f;
+            v[h].w = f + 3 * s < nf ? ld1<T>(xp + 3 * s) : 0.f;
+          }
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+          if (e + h >= ne) break;
+          acc.x = fmaf(ww[h], v[h].x, acc.x);
+          acc.y = fmaf(ww[h], v[h].y, acc.y);
+          acc.z = fmaf(ww[h], v[h].z, acc.z);
+          acc.w = fmaf(ww[h], v[h].w, acc.w);
+        }
+      }
     }
-    st4_tail<T>(y + f, acc, f, nf, full);
+    if (vec) {
+      if (f < nf) st4<T>(y + f, acc);
+    } else {
+      if (f < nf) st1<T>(y + f, acc.x);
+      if (f + s < nf) st1<T>(y + f + s, acc.y);
+      if (f + 2 * s < nf) st1<T>(y + f + 2 * s, acc.z);
+      if (f + 3 * s < nf) st1<T>(y + f + 3 * s, acc.w);
+    }
   }
 }
 
