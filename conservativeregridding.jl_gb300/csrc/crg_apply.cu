@@ -449,16 +449,33 @@ template <> struct CmGather<__nv_bfloat16> {
   }
 };
 
+// Rows that are not 16-byte 4-vectors (a field count or stride not a multiple
+// of 4): lane l takes fields f0 + l + 32 t (t < 4) of a 128-field pass, bit t
+// of `onm` set when that field exists, so that each of the four scalar loads
+// of a gather reads 32 consecutive elements across the warp.
+template <class T>
+__device__ __forceinline__ float4 cm_strided_load(const char* base, uint32_t off, int onm) {
+  const T* p = reinterpret_cast<const T*>(base + off);
+  float4 v;
+  v.x = (onm & 1) ? ld1<T>(p) : 0.f;
+  v.y = (onm & 2) ? ld1<T>(p + 32) : 0.f;
+  v.z = (onm & 4) ? ld1<T>(p + 64) : 0.f;
+  v.w = (onm & 8) ? ld1<T>(p + 96) : 0.f;
+  return v;
+}
+
 // One merge-path task of one 128-field pass, by one warp.  `xb` is the lane's
-// base (its 4 fields of cell 0), `fo` its first field, `on` whether it has
-// fields in this pass; B gathers are in flight.
-template <class T, bool kGaps, int B>
+// base (its first field of cell 0), `fo` that field, `onm` which of its 4
+// fields exist (bit t); B gathers are in flight.  kVec: the lane's fields are
+// fo .. fo + 3 (16-byte FP32 / 8-byte BF16 vectors); otherwise fo + 32 t.
+template <class T, bool kGaps, int B, bool kVec = true>
 __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ tasks, const int2* __restrict__ tslot,
                                         const int32_t* __restrict__ idx, const uint32_t* __restrict__ rbits,
                                         const int32_t* __restrict__ nextrow, const float* __restrict__ w,
                                         const char* xb, uint32_t cstride, T* __restrict__ y, int64_t ys, int64_t fo,
-                                        bool on, float* __restrict__ carry, int lane) {
+                                        int onm, float* __restrict__ carry, int lane) {
   using G = CmGather<T>;
+  using Raw = typename std::conditional<kVec, typename G::Raw, float4>::type;
   const int4 tr = __ldg(tasks + task);
   const int32_t e0 = tr.x, e1 = tr.y;
   if (e0 >= e1) return;  // warp-uniform
@@ -471,13 +488,26 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
   int32_t cur = first;
   float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
   auto flush = [&](int32_t row) {
-    if (!on) return;
-    if (row == carry_first) {
-      *reinterpret_cast<float4*>(carry + (int64_t)slot.x * 128 + lane * 4) = acc;
-    } else if (row == carry_last) {
-      *reinterpret_cast<float4*>(carry + (int64_t)slot.y * 128 + lane * 4) = acc;
-    } else {
+    if (!onm) return;
+    if (row == carry_first || row == carry_last) {
+      float* c = carry + (int64_t)(row == carry_first ? slot.x : slot.y) * 128;
+      if (kVec) {
+        *reinterpret_cast<float4*>(c + lane * 4) = acc;
+      } else {
+        c += lane;
+        if (onm & 1) c[0] = acc.x;
+        if (onm & 2) c[32] = acc.y;
+        if (onm & 4) c[64] = acc.z;
+        if (onm & 8) c[96] = acc.w;
+      }
+    } else if (kVec) {
       st4<T>(y + (int64_t)row * ys + fo, acc);
+    } else {
+      T* yp = y + (int64_t)row * ys + fo;
+      if (onm & 1) st1<T>(yp, acc.x);
+      if (onm & 2) st1<T>(yp + 32, acc.y);
+      if (onm & 4) st1<T>(yp + 64, acc.z);
+      if (onm & 8) st1<T>(yp + 96, acc.w);
     }
   };
   // the chunk at c0: lane's byte offset of its source cell and weight, and
@@ -503,13 +533,15 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
     const unsigned newrow = starts;
     const int n = e1 - c0 < 32 ? e1 - c0 : 32;
     for (int k = 0; k < n; k += B) {
-      typename G::Raw v[B];
+      Raw v[B];
       float ww[B];
 #pragma unroll
       for (int h = 0; h < B; ++h) {
         const uint32_t o = __shfl_sync(0xffffffffu, myo, (k + h) & 31);
         ww[h] = __shfl_sync(0xffffffffu, myw, (k + h) & 31);
-        v[h] = G::load(xb, o);  // past-the-end entries load cell 0 with weight 0
+        // past-the-end entries load cell 0 with weight 0
+        if constexpr (kVec) v[h] = G::load(xb, o);
+        else v[h] = cm_strided_load<T>(xb, o, onm);
       }
 #pragma unroll
       for (int h = 0; h < B; ++h) {
@@ -519,7 +551,9 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
           cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
           acc = make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        const float4 xv = G::widen(v[h]);
+        float4 xv;
+        if constexpr (kVec) xv = G::widen(v[h]);
+        else xv = v[h];
         acc.x = fmaf(ww[h], xv.x, acc.x);
         acc.y = fmaf(ww[h], xv.y, acc.y);
         acc.z = fmaf(ww[h], xv.z, acc.z);
@@ -533,169 +567,24 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
   flush(cur);
 }
 
-// BF16 fields in 16-byte aligned rows of a multiple of 8 fields: each lane
-// takes 8 fields (one 16-byte load), so 16 lanes cover a 128-field pass and
-// the two half-warps gather two entries at once -- half 0 the even entries of
-// the task, half 1 the odd ones -- with B loads in flight per lane.  A row's
-// sum is (its even entries) + (its odd entries), each accumulated in entry
-// order in FP32: the half-warps' sums are added when the row ends (the same
-// value in both halves, addition being commutative) and half 0 writes the
-// row.  Deterministic, and the same in every path that runs BF16 fields
-// (crg_apply, crg_apply_noalloc, plans); rows cut between tasks go through
-// the carry slots like the 4-field kernel's.
-template <bool kGaps, int B>
-__device__ __forceinline__ void cm_task_h8(int64_t task, const int4* __restrict__ tasks,
-                                           const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
-                                           const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow,
-                                           const float* __restrict__ w, const char* xb, uint32_t cstride,
-                                           __nv_bfloat16* __restrict__ y, int64_t ys, int64_t fo, bool on,
-                                           float* __restrict__ carry, int lane) {
-  const int half = lane >> 4, hl = lane & 15;
-  const int4 tr = __ldg(tasks + task);
-  const int32_t e0 = tr.x, e1 = tr.y;
-  if (e0 >= e1) return;  // warp-uniform
-  const int32_t first = tr.z & 0x7fffffff;
-  const int32_t carry_first = tr.z < 0 ? first : -1;
-  const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
-  const int2 slot = (tr.z | tr.w) < 0 ? __ldg(tslot + task) : make_int2(-1, -1);
-  int32_t cur = first;
-  float acc[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) acc[i] = 0.f;
-  // the row's total in both halves, written by half 0 (warp-uniform call)
-  auto flush = [&](int32_t row) {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], 16);
-    if (half != 0 || !on) return;
-    if (row == carry_first || row == carry_last) {
-      float* c = carry + (int64_t)(row == carry_first ? slot.x : slot.y) * 128 + hl * 8;
-      *reinterpret_cast<float4*>(c) = make_float4(acc[0], acc[1], acc[2], acc[3]);
-      *reinterpret_cast<float4*>(c + 4) = make_float4(acc[4], acc[5], acc[6], acc[7]);
-    } else {
-      uint4 u;
-      __nv_bfloat162 b;
-      b = __floats2bfloat162_rn(acc[0], acc[1]); u.x = *reinterpret_cast<uint32_t*>(&b);
-      b = __floats2bfloat162_rn(acc[2], acc[3]); u.y = *reinterpret_cast<uint32_t*>(&b);
-      b = __floats2bfloat162_rn(acc[4], acc[5]); u.z = *reinterpret_cast<uint32_t*>(&b);
-      b = __floats2bfloat162_rn(acc[6], acc[7]); u.w = *reinterpret_cast<uint32_t*>(&b);
-      *reinterpret_cast<uint4*>(y + (int64_t)row * ys + fo) = u;
-    }
-  };
-  auto zero = [&]() {
-#pragma unroll
-    for (int i = 0; i < 8; ++i) acc[i] = 0.f;
-  };
-  auto load = [&](int32_t c0, uint32_t& starts, uint32_t& o, float& wt) {
-    const int32_t e = c0 + lane;
-    const bool valid = e < e1;
-    o = valid ? (uint32_t)__ldg(idx + e) * cstride : 0u;
-    wt = valid ? __ldg(w + e) : 0.f;
-    starts = __funnelshift_r(__ldg(rbits + (c0 >> 5)), __ldg(rbits + (c0 >> 5) + 1), (uint32_t)c0 & 31u);
-    if (e1 - c0 < 32) starts &= (1u << (e1 - c0)) - 1u;
-  };
-  uint32_t starts, myo;
-  float myw;
-  load(e0, starts, myo, myw);
-  starts &= ~1u;  // entry e0 belongs to row `first`
-  for (int32_t c0 = e0; c0 < e1; c0 += 32) {
-    uint32_t nstarts = 0u, no = 0u;
-    float nwt = 0.f;
-    if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
-    const unsigned newrow = starts;
-    const int n = e1 - c0 < 32 ? e1 - c0 : 32;
-    for (int k = 0; k < n; k += 2 * B) {
-      uint4 v[B];
-      float ww[B];
-#pragma unroll
-      for (int h = 0; h < B; ++h) {
-        const int src = (k + 2 * h + half) & 31;  // this half's entry of pair h
-        const uint32_t o = __shfl_sync(0xffffffffu, myo, src);
-        ww[h] = __shfl_sync(0xffffffffu, myw, src);
-        v[h] = __ldg(reinterpret_cast<const uint4*>(xb + o));  // past-the-end entries: cell 0, weight 0
-      }
-#pragma unroll
-      for (int h = 0; h < B; ++h) {
-        const int ke = k + 2 * h;  // half 0's entry; half 1 has ke + 1
-        if (ke >= n) break;
-        if ((newrow >> ke) & 1u) {
-          flush(cur);
-          cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
-          zero();
-        }
-        const bool odd_in = ke + 1 < n;
-        if (half == 0) {
-          const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].x));
-          const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].y));
-          const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].z));
-          const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].w));
-          acc[0] = fmaf(ww[h], a.x, acc[0]); acc[1] = fmaf(ww[h], a.y, acc[1]);
-          acc[2] = fmaf(ww[h], b.x, acc[2]); acc[3] = fmaf(ww[h], b.y, acc[3]);
-          acc[4] = fmaf(ww[h], c.x, acc[4]); acc[5] = fmaf(ww[h], c.y, acc[5]);
-          acc[6] = fmaf(ww[h], d.x, acc[6]); acc[7] = fmaf(ww[h], d.y, acc[7]);
-        }
-        if (!odd_in) break;
-        if ((newrow >> (ke + 1)) & 1u) {
-          flush(cur);
-          cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
-          zero();
-        }
-        if (half == 1) {
-          const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].x));
-          const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].y));
-          const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].z));
-          const float2 d = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&v[h].w));
-          acc[0] = fmaf(ww[h], a.x, acc[0]); acc[1] = fmaf(ww[h], a.y, acc[1]);
-          acc[2] = fmaf(ww[h], b.x, acc[2]); acc[3] = fmaf(ww[h], b.y, acc[3]);
-          acc[4] = fmaf(ww[h], c.x, acc[4]); acc[5] = fmaf(ww[h], c.y, acc[5]);
-          acc[6] = fmaf(ww[h], d.x, acc[6]); acc[7] = fmaf(ww[h], d.y, acc[7]);
-        }
-      }
-    }
-    starts = nstarts;
-    myo = no;
-    myw = nwt;
-  }
-  flush(cur);
-}
-
-// The lane's field base of a 128-field pass starting at f0 for cm_task_h8:
-// 8 fields per lane, 16 lanes per entry.
-__device__ __forceinline__ const char* cm_lane_base_h8(const __nv_bfloat16* x, int64_t f0, int64_t nf, int lane,
-                                                       int64_t& fo, bool& on) {
-  const int64_t f = f0 + (int64_t)(lane & 15) * 8;
-  on = f < nf;
-  fo = on ? f : f0;
-  return reinterpret_cast<const char*>(x + fo);
-}
-
-template <bool kGaps, int B, int MINB>
-__global__ void __launch_bounds__(256, MINB)
-    k_cm_nnz_h8(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
-                const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow, const float* __restrict__ w,
-                int64_t ntasks, const __nv_bfloat16* __restrict__ x, int64_t xs, __nv_bfloat16* __restrict__ y,
-                int64_t ys, int64_t f0, int64_t nf, float* __restrict__ carry) {
-  const int lane = threadIdx.x & 31;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  int64_t fo;
-  bool on;
-  const char* xb = cm_lane_base_h8(x, f0, nf, lane, fo, on);
-  const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(__nv_bfloat16));
-  for (int64_t task = gw; task < ntasks; task += nw)
-    cm_task_h8<kGaps, B>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, on, carry, lane);
-}
-
-// The lane's field base of one 128-field pass starting at f0.
-template <class T>
+// The lane's field base of one 128-field pass starting at f0, its first
+// field and which of its 4 fields exist.
+template <class T, bool kVec>
 __device__ __forceinline__ const char* cm_lane_base(const T* x, int64_t f0, int64_t nf, int lane, int64_t& fo,
-                                                    bool& on) {
-  const int64_t f = f0 + (int64_t)lane * 4;
-  on = f < nf;
-  fo = on ? f : f0;
+                                                    int& onm) {
+  if (kVec) {
+    const int64_t f = f0 + (int64_t)lane * 4;
+    onm = f < nf ? 0xf : 0;  // nf is a multiple of 4
+    fo = f < nf ? f : f0;
+  } else {
+    const int64_t rem = nf - f0 - lane;
+    onm = (rem > 0 ? 1 : 0) | (rem > 32 ? 2 : 0) | (rem > 64 ? 4 : 0) | (rem > 96 ? 8 : 0);
+    fo = rem > 0 ? f0 + lane : f0;
+  }
   return reinterpret_cast<const char*>(x + fo);
 }
 
-template <class T, bool kGaps, int B = CmGather<T>::kInFlight, int MINB = 3>
+template <class T, bool kGaps, int B = CmGather<T>::kInFlight, int MINB = 3, bool kVec = true>
 __global__ void __launch_bounds__(256, MINB)
     k_cm_nnz(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
              const uint32_t* __restrict__ rbits, const int32_t* __restrict__ nextrow, const float* __restrict__ w,
@@ -705,12 +594,12 @@ __global__ void __launch_bounds__(256, MINB)
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   int64_t fo;
-  bool on;
-  // per-lane base of this lane's 4 fields; cell j adds j * xs elements (32-bit byte offset)
-  const char* xb = cm_lane_base<T>(x, f0, nf, lane, fo, on);
+  int onm;
+  // per-lane base of this lane's fields; cell j adds j * xs elements (32-bit byte offset)
+  const char* xb = cm_lane_base<T, kVec>(x, f0, nf, lane, fo, onm);
   const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(T));
   for (int64_t task = gw; task < ntasks; task += nw)
-    cm_task<T, kGaps, B>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, on, carry, lane);
+    cm_task<T, kGaps, B, kVec>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, onm, carry, lane);
 }
 
 // Rows cut between tasks: sum their pieces in task order (deterministic).
@@ -729,6 +618,25 @@ __global__ void k_cm_fixup(const int32_t* __restrict__ split, int64_t nsplit, co
     s.x += c.x; s.y += c.y; s.z += c.z; s.w += c.w;
   }
   st4<T>(y + (int64_t)row * ys + f, s);
+}
+
+// The same for rows that are not 4-vectors: lane l sums fields l + 32 t of the
+// pass, as cm_task's strided layout wrote them.
+template <class T>
+__global__ void k_cm_fixup_s(const int32_t* __restrict__ split, int64_t nsplit, const float* __restrict__ carry,
+                             T* __restrict__ y, int64_t ys, int64_t f0, int64_t nf) {
+  const int64_t wi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wi >= nsplit) return;
+  const int32_t row = split[3 * wi], s0 = split[3 * wi + 1], pieces = split[3 * wi + 2];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int p = lane + 32 * t;
+    if (f0 + p >= nf) break;
+    float acc = carry[(int64_t)s0 * 128 + p];
+    for (int32_t k = 1; k < pieces; ++k) acc += carry[(int64_t)(s0 + k) * 128 + p];
+    st1<T>(y + (int64_t)row * ys + f0 + p, acc);
+  }
 }
 
 // The merge-path kernel over all 128-field passes, the fixup of rows cut
@@ -750,21 +658,9 @@ template <> struct CmVariant<__nv_bfloat16> {
   static constexpr int MINB[kCmVariants] = {3, 3, 4, 2};
 };
 
-// The half-warp BF16 kernel's candidates (pairs of entries in flight per lane).
-struct CmVariantH8 {
-  static constexpr int B[kCmVariants] = {4, 8, 2, 6};
-  static constexpr int MINB[kCmVariants] = {4, 3, 4, 3};
-};
-
-// Whether BF16 fields take the half-warp kernel: 16-byte loads and stores of
-// 8 fields need rows of a multiple of 8 fields in 16-byte aligned memory.
-inline bool bf16_h8(const void* x, int64_t xs, const void* y, int64_t ys, int64_t nf) {
-  return nf % 8 == 0 && xs % 8 == 0 && ys % 8 == 0 && (uintptr_t)x % 16 == 0 && (uintptr_t)y % 16 == 0;
-}
-
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                   float* carry, cudaStream_t st, int variant = 0);
+                   float* carry, cudaStream_t st, int variant = 0, bool vec = true);
 
 // The device part of an autotuner key: name and SM count of the current device.
 std::string device_key() {
@@ -842,12 +738,12 @@ template <> const char* dtype_name<__nv_bfloat16>() { return "bf16"; }
 
 template <class T>
 void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                   cudaStream_t st) {
+                   cudaStream_t st, bool vec) {
   float* carry = nullptr;
   if (c.nslots) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * c.nslots * 128, st));
-  const int v = tune_choose(matrix_key("cm_nnz", c, dtype_name<T>(), nf), kCmVariants, st,
-                            [&](int i) { cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st, i); });
-  cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st, v);
+  const int v = tune_choose(matrix_key(vec ? "cm_nnz" : "cm_nnz_strided", c, dtype_name<T>(), nf), kCmVariants, st,
+                            [&](int i) { cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st, i, vec); });
+  cm_nnz_passes<T>(c, w, x, xs, y, ys, nf, carry, st, v, vec);
   if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
 }
 
@@ -859,47 +755,42 @@ __global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* _
   for (int64_t f = 0; f < nf; ++f) st1<T>(y + r * ys + f, 0.f);
 }
 
-template <class T, int V>
+template <class T, int V, bool kVec>
 void cm_nnz_launch(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t f0, int64_t nf,
                    float* carry, cudaStream_t st) {
-  if constexpr (std::is_same<T, __nv_bfloat16>::value) {
-    if (bf16_h8(x, xs, y, ys, nf)) {
-      constexpr int B = CmVariantH8::B[V], MINB = CmVariantH8::MINB[V];
-      const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 8 * MINB);
-      if (c.nextrow)
-        k_cm_nnz_h8<true, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, c.nextrow,
-                                                                          w, c.ntasks, x, xs, y, ys, f0, nf, carry);
-      else
-        k_cm_nnz_h8<false, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, nullptr,
-                                                                           w, c.ntasks, x, xs, y, ys, f0, nf, carry);
-      return;
-    }
-  }
   constexpr int B = CmVariant<T>::B[V], MINB = CmVariant<T>::MINB[V];
   const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 8 * MINB);  // MINB blocks of 8 warps per SM
   if (c.nextrow)
-    k_cm_nnz<T, true, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, c.nextrow, w,
-                                                                      c.ntasks, x, xs, y, ys, f0, nf, carry);
+    k_cm_nnz<T, true, B, MINB, kVec><<<nblk(warps * 32, 256), 256, 0, st>>>(
+        c.tasks, c.tslot, c.idx, c.rbits, c.nextrow, w, c.ntasks, x, xs, y, ys, f0, nf, carry);
   else
-    k_cm_nnz<T, false, B, MINB><<<nblk(warps * 32, 256), 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.rbits, nullptr, w,
-                                                                       c.ntasks, x, xs, y, ys, f0, nf, carry);
+    k_cm_nnz<T, false, B, MINB, kVec><<<nblk(warps * 32, 256), 256, 0, st>>>(
+        c.tasks, c.tslot, c.idx, c.rbits, nullptr, w, c.ntasks, x, xs, y, ys, f0, nf, carry);
+}
+
+template <class T, bool kVec>
+void cm_nnz_variant(int variant, const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys,
+                    int64_t f0, int64_t nf, float* carry, cudaStream_t st) {
+  switch (variant) {
+    case 1: cm_nnz_launch<T, 1, kVec>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+    case 2: cm_nnz_launch<T, 2, kVec>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+    case 3: cm_nnz_launch<T, 3, kVec>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+    default: cm_nnz_launch<T, 0, kVec>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
+  }
 }
 
 template <class T>
 void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
-                   float* carry, cudaStream_t st, int variant) {
+                   float* carry, cudaStream_t st, int variant, bool vec) {
   for (int64_t f0 = 0; f0 < nf; f0 += 128) {
     if (c.ntasks) {
-      switch (variant) {
-        case 1: cm_nnz_launch<T, 1>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
-        case 2: cm_nnz_launch<T, 2>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
-        case 3: cm_nnz_launch<T, 3>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
-        default: cm_nnz_launch<T, 0>(c, w, x, xs, y, ys, f0, nf, carry, st); break;
-      }
+      if (vec) cm_nnz_variant<T, true>(variant, c, w, x, xs, y, ys, f0, nf, carry, st);
+      else cm_nnz_variant<T, false>(variant, c, w, x, xs, y, ys, f0, nf, carry, st);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (c.nsplit) {
-      k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
+      if (vec) k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
+      else k_cm_fixup_s<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, f0, nf);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
   }
@@ -1117,9 +1008,10 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
   const SpmmPath path = spmm_path();
   // the merge-path kernel addresses source cells with 32-bit byte offsets
   const bool span32 = (double)c.ncols * (double)xsc * es < 4.0e9;
-  if (path == SpmmPath::kAuto && cell_major && vec4 && nf >= 32 && span32) {
-    // merge-path over entries; rows with no entries are zeroed separately
-    launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st);
+  if (path == SpmmPath::kAuto && cell_major && nf >= 32 && span32) {
+    // merge-path over entries (4-field vectors when the rows allow, else each
+    // lane's fields strided by 32); rows with no entries are zeroed separately
+    launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st, vec4);
     return;
   }
   {
@@ -1219,7 +1111,7 @@ struct BatchItem {
   int32_t kind;    // 0 merge-path, 1 rows
   int32_t gaps;    // merge-path: some rows have no entries (nextrow)
   int32_t lg;      // rows: log2 of the lanes per row
-  int32_t vec;     // rows: 4-field vector access; merge-path BF16: the half-warp kernel (cm_task_h8)
+  int32_t vec;     // 4-field vector access (merge-path items: else the strided lane layout)
   int64_t ntasks;  // merge-path: tasks per 128-field pass
   int64_t nrows, nf, xs, ys, nslots;
   const int4* tasks;
@@ -1237,7 +1129,7 @@ struct BatchItem {
 struct FinishItem {
   int64_t unit0;
   int32_t kind;  // 0 fixup of cut rows (nsplit units per pass), 1 zero rows without entries (32 rows per unit)
-  int32_t pad;
+  int32_t vec;   // fixup: the carry slots hold the 4-vector lane layout (else the strided one)
   int64_t nsplit, nslots, nrows, nf, ys;
   const int32_t* split;
   const float* carry;
@@ -1370,29 +1262,28 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
     const int64_t ntasks = itp->ntasks, k = u - itp->unit0;
     const int64_t pass = k / ntasks, task = k - pass * ntasks;
     int64_t fo;
-    bool on;
-    const char* xb = cm_lane_base<T>(static_cast<const T*>(itp->x), pass * 128, itp->nf, lane, fo, on);
+    int onm;
+    const T* x = static_cast<const T*>(itp->x);
     const uint32_t cstride = (uint32_t)(itp->xs * (int64_t)sizeof(T));
     float* carry = itp->carry ? itp->carry + pass * itp->nslots * 128 : nullptr;
-    if constexpr (std::is_same<T, __nv_bfloat16>::value) {
-      if (itp->vec) {
-        constexpr int BH = CmVariantH8::B[0];
-        const char* xh = cm_lane_base_h8(static_cast<const T*>(itp->x), pass * 128, itp->nf, lane, fo, on);
-        if (itp->gaps)
-          cm_task_h8<true, BH>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xh,
-                               cstride, static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
-        else
-          cm_task_h8<false, BH>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xh, cstride,
-                                static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
-        continue;
-      }
+    T* y = static_cast<T*>(itp->y);
+    if (itp->vec) {
+      const char* xb = cm_lane_base<T, true>(x, pass * 128, itp->nf, lane, fo, onm);
+      if (itp->gaps)
+        cm_task<T, true, B, true>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb,
+                                  cstride, y, itp->ys, fo, onm, carry, lane);
+      else
+        cm_task<T, false, B, true>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xb, cstride,
+                                   y, itp->ys, fo, onm, carry, lane);
+    } else {
+      const char* xb = cm_lane_base<T, false>(x, pass * 128, itp->nf, lane, fo, onm);
+      if (itp->gaps)
+        cm_task<T, true, B, false>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb,
+                                   cstride, y, itp->ys, fo, onm, carry, lane);
+      else
+        cm_task<T, false, B, false>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xb,
+                                    cstride, y, itp->ys, fo, onm, carry, lane);
     }
-    if (itp->gaps)
-      cm_task<T, true, B>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb, cstride,
-                          static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
-    else
-      cm_task<T, false, B>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xb, cstride,
-                           static_cast<T*>(itp->y), itp->ys, fo, on, carry, lane);
   }
 }
 
@@ -1420,19 +1311,29 @@ __global__ void k_batch_finish(const FinishItem* __restrict__ items, const int64
     const int64_t k = u - it.unit0;
     T* __restrict__ y = static_cast<T*>(it.y);
     if (it.kind == 0) {
-      // k_cm_fixup: the pieces of cut row s in task order
+      // k_cm_fixup / k_cm_fixup_s: the pieces of cut row s in task order
       const int64_t pass = k / it.nsplit, sp = k - pass * it.nsplit;
-      const int64_t f = pass * 128 + (int64_t)lane * 4;
-      if (f >= it.nf) continue;
       const int32_t row = __ldg(it.split + 3 * sp), s0 = __ldg(it.split + 3 * sp + 1),
                     pieces = __ldg(it.split + 3 * sp + 2);
       const float* c = it.carry + pass * it.nslots * 128;
-      float4 acc = *reinterpret_cast<const float4*>(c + (int64_t)s0 * 128 + lane * 4);
-      for (int32_t q = 1; q < pieces; ++q) {
-        const float4 d = *reinterpret_cast<const float4*>(c + (int64_t)(s0 + q) * 128 + lane * 4);
-        acc.x += d.x; acc.y += d.y; acc.z += d.z; acc.w += d.w;
+      if (it.vec) {
+        const int64_t f = pass * 128 + (int64_t)lane * 4;
+        if (f >= it.nf) continue;
+        float4 acc = *reinterpret_cast<const float4*>(c + (int64_t)s0 * 128 + lane * 4);
+        for (int32_t q = 1; q < pieces; ++q) {
+          const float4 d = *reinterpret_cast<const float4*>(c + (int64_t)(s0 + q) * 128 + lane * 4);
+          acc.x += d.x; acc.y += d.y; acc.z += d.z; acc.w += d.w;
+        }
+        st4<T>(y + (int64_t)row * it.ys + f, acc);
+      } else {
+        for (int t = 0; t < 4; ++t) {
+          const int p = lane + 32 * t;
+          if (pass * 128 + p >= it.nf) break;
+          float acc = c[(int64_t)s0 * 128 + p];
+          for (int32_t q = 1; q < pieces; ++q) acc += c[(int64_t)(s0 + q) * 128 + p];
+          st1<T>(y + (int64_t)row * it.ys + pass * 128 + p, acc);
+        }
       }
-      st4<T>(y + (int64_t)row * it.ys + f, acc);
     } else {
       // k_zero_empty_cm: rows without entries
       const int64_t r = k * 32 + lane;
@@ -1509,11 +1410,11 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
     b.x = it.src;
     b.y = it.dst;
     const int64_t passes = (nf + 127) / 128;
-    if (spmm_path() == SpmmPath::kAuto && cell_major && vec4 && nf >= 32 && span32) {
+    if (spmm_path() == SpmmPath::kAuto && cell_major && nf >= 32 && span32) {
       // the merge path, as launch_cm_nnz runs it
       b.kind = 0;
       b.gaps = c.nextrow != nullptr;
-      b.vec = d == 1 && bf16_h8(it.src, ssc, it.dst, dsc, nf);
+      b.vec = vec4;
       b.ntasks = c.ntasks;
       b.nslots = c.nslots;
       b.tasks = c.tasks;
@@ -1539,6 +1440,7 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
       f.y = it.dst;
       if (c.nsplit && nu > 0) {
         f.kind = 0;
+        f.vec = vec4;
         f.unit0 = funits[d];
         f.carry = reinterpret_cast<const float*>((intptr_t)carry_off[d].back());  // offset until allocation
         funits[d] += c.nsplit * passes;

@@ -495,15 +495,19 @@ def test_row_col_sums_on_request_from_threads(cuda):
     assert np.array_equal(rs2, want_r) and np.array_equal(cs2, want_c)
 
 
-@pytest.mark.parametrize("K", [128, 64, 40, 200])
+@pytest.mark.parametrize("dtype,K", [("bfloat16", 128), ("bfloat16", 64), ("bfloat16", 40), ("bfloat16", 200),
+                                     ("bfloat16", 45), ("float32", 33), ("float32", 130), ("float32", 128)])
 @pytest.mark.parametrize("case", ["cut_rows", "empty_rows"])
-def test_bf16_apply_cut_and_empty_rows(cuda, K, case):
-    """BF16 cell-major fields (FP32 accumulation) against the FP64 apply of the
-    same rounded inputs, on matrices with rows cut between merge-path tasks
-    (10-degree cells over HEALPix 32: ~30 entries per row) and with rows that
-    have no entries (a destination partly outside the source), both
-    directions: within the BF16 output rounding."""
+def test_low_precision_apply_cut_and_empty_rows(cuda, dtype, K, case):
+    """FP32 / BF16 cell-major fields (FP32 accumulation) against the FP64 apply
+    of the same rounded inputs, on matrices with rows cut between merge-path
+    tasks (10-degree cells over HEALPix 32: ~30 entries per row) and with rows
+    that have no entries (a destination partly outside the source), both
+    directions: within the output rounding.  Field counts that are not a
+    multiple of 4 take the merge path's strided lane layout."""
     import torch
+
+    tol = 8e-3 if dtype == "bfloat16" else 2e-6
 
     if case == "cut_rows":
         R = Regridder(grids.lonlat_regular(10.0, 10.0), grids.healpix_grid(32), normalize=True)
@@ -516,12 +520,12 @@ def test_bf16_apply_cut_and_empty_rows(cuda, K, case):
     A = R.intersections
     for RR, counts in ((R, A.getnnz(axis=1)), (R.transpose(), A.getnnz(axis=0))):
         n_out, n_in = RR.shape
-        x = torch.randn((n_in, K), generator=gen, device="cuda").bfloat16()
-        y = torch.full((n_out, K), float("nan"), device="cuda").bfloat16()
+        x = torch.randn((n_in, K), generator=gen, device="cuda").to(getattr(torch, dtype))
+        y = torch.full((n_out, K), float("nan"), device="cuda").to(getattr(torch, dtype))
         regrid_(y, RR, x, dims=1)
         ref = torch.empty((n_out, K), dtype=torch.float64, device="cuda")
         regrid_(ref, RR, x.double(), dims=1)
         err = (y.double() - ref).abs().max().item()
-        assert np.isfinite(err) and err <= 8e-3 * ref.abs().max().item(), err
+        assert np.isfinite(err) and err <= tol * ref.abs().max().item(), err
         empty = torch.from_numpy(np.asarray(counts) == 0).cuda()
         assert bool((y[empty] == 0).all())
