@@ -589,9 +589,15 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 //
 // The same tests give each kept pair its class: the mask of destination edges
 // that may cut the source cell (neither all vertices clearly inside nor all
-// outside).  Clipping the pairs grouped by class lets the lanes of a warp
-// meet their crossing points at the same stages.
-constexpr int kClasses = 256;  // cut masks of up to 8 edges; class kClasses = dropped
+// outside), and the vertex count of the clipped polygon as a clip in FP32
+// predicts it (only a grouping key: the FP64 clip decides).  Clipping the
+// pairs grouped by class lets the lanes of a warp meet their crossing points
+// at the same stages and run the area's fan over the same number of
+// triangles.
+constexpr int kMaskClasses = 256;  // cut masks of up to 8 edges
+constexpr int kSizeClasses = 16;   // predicted vertex counts 0 .. 15 (15: 15 or more)
+constexpr int kClasses = kMaskClasses * kSizeClasses;  // class kClasses = dropped
+constexpr int kPredCap = 12;       // vertices the FP32 prediction follows (more: counted as 15)
 
 __global__ void __launch_bounds__(256)
     k_separated(const int2* __restrict__ cand, int64_t nc, const float4* __restrict__ dv4,
@@ -625,7 +631,49 @@ __global__ void __launch_bounds__(256)
     sep = out;
     if (!in) mask |= 1 << k;
   }
-  cls[t] = sep ? kClasses : (uint16_t)(mask & (kClasses - 1));
+  if (sep) {
+    cls[t] = kClasses;
+    return;
+  }
+  // Sutherland-Hodgman in FP32 by the edges that may cut: the side of a point
+  // is n . x (n is orthogonal to the edge's start), so the crossing points need
+  // no normalisation for their signs
+  float3 pa[kPredCap], pb[kPredCap];
+  int m = ns;
+  for (int i = 0; i < ns; ++i) pa[i] = make_float3(v[i].x, v[i].y, v[i].z);
+  float3* in_ = pa;
+  float3* out_ = pb;
+  for (int k = 0; k < nd && m > 0 && m <= kPredCap; ++k) {
+    if (!((mask >> k) & 1)) continue;
+    const float4 p = pl[k];
+    int o = 0;
+    float sp = 0.f;
+    {
+      const float3 q = in_[m - 1];
+      sp = fmaf(p.x, q.x, fmaf(p.y, q.y, p.z * q.z));
+    }
+    for (int i = 0; i < m && o <= kPredCap; ++i) {
+      const float3 q = in_[i], r = in_[i == 0 ? m - 1 : i - 1];
+      const float sq = fmaf(p.x, q.x, fmaf(p.y, q.y, p.z * q.z));
+      if ((sq >= 0.f) != (sp >= 0.f)) {
+        const float wa = fabsf(sq), wb = fabsf(sp);
+        if (o < kPredCap)
+          out_[o] = make_float3(fmaf(wa, r.x, wb * q.x), fmaf(wa, r.y, wb * q.y), fmaf(wa, r.z, wb * q.z));
+        ++o;
+      }
+      if (sq >= 0.f) {
+        if (o < kPredCap) out_[o] = q;
+        ++o;
+      }
+      sp = sq;
+    }
+    m = o;
+    float3* tmp = in_;
+    in_ = out_;
+    out_ = tmp;
+  }
+  const int size = m < 0 ? 0 : (m > kPredCap ? kSizeClasses - 1 : min(m, kSizeClasses - 1));
+  cls[t] = (uint16_t)((mask & (kMaskClasses - 1)) | (size << 8));
 }
 
 __global__ void __launch_bounds__(256)
