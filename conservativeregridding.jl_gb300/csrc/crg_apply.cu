@@ -548,7 +548,8 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
         if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
         if ((newrow >> (k + h)) & 1u) {
           flush(cur);
-          cur = kGaps ? __ldg(nextrow + cur) : cur + 1;
+          // kGaps: the next row with entries (nextrow), when the layout has one
+          cur = kGaps ? (nextrow ? __ldg(nextrow + cur) : cur + 1) : cur + 1;
           acc = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         float4 xv;
@@ -1267,22 +1268,16 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
     const uint32_t cstride = (uint32_t)(itp->xs * (int64_t)sizeof(T));
     float* carry = itp->carry ? itp->carry + pass * itp->nslots * 128 : nullptr;
     T* y = static_cast<T*>(itp->y);
+    // nextrow is NULL unless the item has rows without entries (checked per row change)
+    const int32_t* nextrow = itp->gaps ? itp->nextrow : nullptr;
     if (itp->vec) {
       const char* xb = cm_lane_base<T, true>(x, pass * 128, itp->nf, lane, fo, onm);
-      if (itp->gaps)
-        cm_task<T, true, B, true>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb,
-                                  cstride, y, itp->ys, fo, onm, carry, lane);
-      else
-        cm_task<T, false, B, true>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xb, cstride,
-                                   y, itp->ys, fo, onm, carry, lane);
+      cm_task<T, true, B, true>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nextrow, itp->w, xb, cstride, y,
+                                itp->ys, fo, onm, carry, lane);
     } else {
       const char* xb = cm_lane_base<T, false>(x, pass * 128, itp->nf, lane, fo, onm);
-      if (itp->gaps)
-        cm_task<T, true, B, false>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, itp->nextrow, itp->w, xb,
-                                   cstride, y, itp->ys, fo, onm, carry, lane);
-      else
-        cm_task<T, false, B, false>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nullptr, itp->w, xb,
-                                    cstride, y, itp->ys, fo, onm, carry, lane);
+      cm_task<T, true, B, false>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nextrow, itp->w, xb, cstride,
+                                 y, itp->ys, fo, onm, carry, lane);
     }
   }
 }
@@ -1536,15 +1531,16 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
   return L;
 }
 
-void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
+void batch_enqueue(const BatchLaunch* L, cudaStream_t st, cudaStream_t rows_st) {
   const int64_t max_warps = (int64_t)num_sms() * 24;  // three blocks of 8 warps per SM
   for (const auto& p : L->parts) {
     if (p.nrunits) {
       if (p.dtype == CRG_F32)
-        k_batch_rows<float><<<nblk(p.nrunits * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems, p.nrunits);
+        k_batch_rows<float><<<nblk(p.nrunits * 32, 256), 256, 0, rows_st>>>(p.ritems, p.runit0, p.nritems,
+                                                                             p.nrunits);
       else
-        k_batch_rows<__nv_bfloat16><<<nblk(p.nrunits * 32, 256), 256, 0, st>>>(p.ritems, p.runit0, p.nritems,
-                                                                                p.nrunits);
+        k_batch_rows<__nv_bfloat16><<<nblk(p.nrunits * 32, 256), 256, 0, rows_st>>>(p.ritems, p.runit0, p.nritems,
+                                                                                     p.nrunits);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (p.nunits) {

@@ -251,8 +251,8 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
   if (!(pb && strcmp(pb, "0") == 0)) batch = batch_prepare(n, items, handled);
   // Capture: the origin stream forks one branch per remaining item (their
   // outputs are distinct), so the graph runs small items side by side.
-  std::vector<cudaStream_t> sts(n + 1, nullptr);
-  std::vector<cudaEvent_t> evs(n + 1, nullptr);
+  std::vector<cudaStream_t> sts(n + 2, nullptr);  // [n + 1]: the batch's row items
+  std::vector<cudaEvent_t> evs(n + 2, nullptr);
   auto cleanup = [&]() {
     for (auto e : evs)
       if (e) cudaEventDestroy(e);
@@ -261,7 +261,7 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
   };
   cudaGraph_t graph = nullptr;
   try {
-    for (int64_t k = 0; k <= n; ++k) {
+    for (int64_t k = 0; k <= n + 1; ++k) {
       if (k < n && handled[k]) continue;
       CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&sts[k], cudaStreamNonBlocking));
       CRG_CHECK_CUDA(cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming));
@@ -278,9 +278,17 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
                    it.src_stride_field, it.dst, it.dst_stride_cell, it.dst_stride_field, it.nfields, it.normalize,
                    sts[k]);
         CRG_CHECK_CUDA(cudaEventRecord(evs[k], sts[k]));
-        CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[k], 0));
       }
-      if (batch) batch_enqueue(batch, origin);
+      if (batch) {
+        // the merge-path items on the origin, the row items on their own
+        // branch, both beside the items of their own applies
+        CRG_CHECK_CUDA(cudaStreamWaitEvent(sts[n + 1], evs[n], 0));
+        batch_enqueue(batch, origin, sts[n + 1]);
+        CRG_CHECK_CUDA(cudaEventRecord(evs[n + 1], sts[n + 1]));
+        CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[n + 1], 0));
+      }
+      for (int64_t k = 0; k < n; ++k)  // join the branches
+        if (!handled[k]) CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[k], 0));
     } catch (...) {
       cudaStreamEndCapture(origin, &graph);
       if (graph) cudaGraphDestroy(graph);

@@ -179,10 +179,12 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
 // The applies of a batch that one persistent launch can run (cell-major FP32 /
 // BF16 fields or single fields, device memory): their device tables, built
 // once; handled[k] = 1 for the items it covers (the others need their own
-// crg_apply).  batch_enqueue queues its launches (at most two per field type).
+// crg_apply).  batch_enqueue queues its launches: the row items' on rows_st,
+// the merge-path items' and their fixup on st (the two sets write different
+// items, so the streams may run side by side).
 struct BatchLaunch;
 BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled);
-void batch_enqueue(const BatchLaunch* L, cudaStream_t st);
+void batch_enqueue(const BatchLaunch* L, cudaStream_t st, cudaStream_t rows_st);
 int batch_launches(const BatchLaunch* L);
 void batch_free(BatchLaunch* L);
 // The autotuner's table of choices (crg_tune.cu): the fastest candidate of a
