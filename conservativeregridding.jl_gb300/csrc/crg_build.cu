@@ -617,22 +617,33 @@ __global__ void __launch_bounds__(256)
   for (int i = 0; i < ns; ++i) v[i] = q[i];
   const float4* c = dv4 + (int64_t)pr.x * dmaxv;
   const float4* pl = planes32 + (int64_t)pr.x * dmaxv;
-  int sep = 0, mask = 0;
+  int sep = 0, mask = 0, nout = 0;  // nout: subject vertices on the outer side of the last edge that may cut
   for (int k = 0; k < nd && !sep; ++k) {
     const float4 p = pl[k], a = c[k];  // n32 (w = |n32|_1) and ca32
-    int out = 1, in = 1;
+    int out = 1, in = 1, no = 0;
     for (int i = 0; i < ns; ++i) {
       const float wx = v[i].x - a.x, wy = v[i].y - a.y, wz = v[i].z - a.z;
       const float s = fmaf(p.x, wx, fmaf(p.y, wy, p.z * wz));
       const float B = 3.814697265625e-06f * p.w * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
       out &= s < -B;
       in &= s > B;
+      no += s < 0.f;
     }
     sep = out;
-    if (!in) mask |= 1 << k;
+    if (!in) {
+      mask |= 1 << k;
+      nout = no;
+    }
   }
   if (sep) {
     cls[t] = kClasses;
+    return;
+  }
+  // no edge may cut: the subject is the result; one edge: a convex polygon
+  // cut by one half-space keeps its inner vertices and gains two crossings
+  if (__popc(mask) <= 1) {
+    const int m = mask == 0 || nout == 0 ? ns : (nout >= ns ? 0 : ns - nout + 2);
+    cls[t] = (uint16_t)((mask & (kMaskClasses - 1)) | (min(m, kSizeClasses - 1) << 8));
     return;
   }
   // Sutherland-Hodgman in FP32 by the edges that may cut: the side of a point
