@@ -589,21 +589,20 @@ __global__ void k_leaf_emit(const uint2* __restrict__ lp, int64_t nlp, const flo
 //
 // The same tests give each kept pair its class: the mask of destination edges
 // that may cut the source cell (neither all vertices clearly inside nor all
-// outside), and the vertex count of the clipped polygon as a clip in FP32
-// predicts it (only a grouping key: the FP64 clip decides).  Clipping the
+// outside), and the vertex count of the clipped polygon as FP32 side tests
+// predict it (only a grouping key: the FP64 clip decides).  Clipping the
 // pairs grouped by class lets the lanes of a warp meet their crossing points
 // at the same stages and run the area's fan over the same number of
 // triangles.
 constexpr int kMaskClasses = 256;  // cut masks of up to 8 edges
 constexpr int kSizeClasses = 16;   // predicted vertex counts 0 .. 15 (15: 15 or more)
 constexpr int kClasses = kMaskClasses * kSizeClasses;  // class kClasses = dropped
-constexpr int kPredCap = 12;       // vertices the FP32 prediction follows (more: counted as 15)
 
 __global__ void __launch_bounds__(256)
     k_separated(const int2* __restrict__ cand, int64_t nc, const float4* __restrict__ dv4,
                 const int8_t* __restrict__ dnv, int dmaxv, const float4* __restrict__ sv4,
-                const int8_t* __restrict__ snv, int smaxv, const float4* __restrict__ planes32,
-                uint16_t* __restrict__ cls) {
+                const int8_t* __restrict__ snv, const int8_t* __restrict__ sori, int smaxv,
+                const float4* __restrict__ planes32, uint16_t* __restrict__ cls) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nc) return;
   const int2 pr = cand[t];
@@ -617,74 +616,56 @@ __global__ void __launch_bounds__(256)
   for (int i = 0; i < ns; ++i) v[i] = q[i];
   const float4* c = dv4 + (int64_t)pr.x * dmaxv;
   const float4* pl = planes32 + (int64_t)pr.x * dmaxv;
-  int sep = 0, mask = 0, nout = 0;  // nout: subject vertices on the outer side of the last edge that may cut
+  int sep = 0, mask = 0;
+  uint64_t sp = 0;  // bit 8 k + i: subject vertex i on the inner side of destination edge k (plain FP32 sign)
   for (int k = 0; k < nd && !sep; ++k) {
     const float4 p = pl[k], a = c[k];  // n32 (w = |n32|_1) and ca32
-    int out = 1, in = 1, no = 0;
+    int out = 1, in = 1;
     for (int i = 0; i < ns; ++i) {
       const float wx = v[i].x - a.x, wy = v[i].y - a.y, wz = v[i].z - a.z;
       const float s = fmaf(p.x, wx, fmaf(p.y, wy, p.z * wz));
       const float B = 3.814697265625e-06f * p.w * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
       out &= s < -B;
       in &= s > B;
-      no += s < 0.f;
+      if (s >= 0.f) sp |= 1ull << (8 * k + i);
     }
     sep = out;
-    if (!in) {
-      mask |= 1 << k;
-      nout = no;
-    }
+    if (!in) mask |= 1 << k;
   }
   if (sep) {
     cls[t] = kClasses;
     return;
   }
-  // no edge may cut: the subject is the result; one edge: a convex polygon
-  // cut by one half-space keeps its inner vertices and gains two crossings
-  if (__popc(mask) <= 1) {
-    const int m = mask == 0 || nout == 0 ? ns : (nout >= ns ? 0 : ns - nout + 2);
-    cls[t] = (uint16_t)((mask & (kMaskClasses - 1)) | (min(m, kSizeClasses - 1) << 8));
-    return;
-  }
-  // Sutherland-Hodgman in FP32 by the edges that may cut: the side of a point
-  // is n . x (n is orthogonal to the edge's start), so the crossing points need
-  // no normalisation for their signs
-  float3 pa[kPredCap], pb[kPredCap];
-  int m = ns;
-  for (int i = 0; i < ns; ++i) pa[i] = make_float3(v[i].x, v[i].y, v[i].z);
-  float3* in_ = pa;
-  float3* out_ = pb;
-  for (int k = 0; k < nd && m > 0 && m <= kPredCap; ++k) {
-    if (!((mask >> k) & 1)) continue;
-    const float4 p = pl[k];
-    int o = 0;
-    float sp = 0.f;
-    {
-      const float3 q = in_[m - 1];
-      sp = fmaf(p.x, q.x, fmaf(p.y, q.y, p.z * q.z));
+  // The vertex count of the intersection of two convex polygons (general
+  // position): the subject's vertices inside the destination cell, the
+  // destination's vertices inside the subject, and one per pair of edges that
+  // cross (each edge's endpoints on either side of the other's great circle).
+  uint64_t sq = 0;  // bit 8 j + k: destination vertex k on the inner side of subject edge j
+  const float sg = (float)sori[pr.y];
+  for (int j = 0; j < ns; ++j) {
+    const float4 a = v[j], b = v[j + 1 == ns ? 0 : j + 1];
+    const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
+    const float nx = sg * (a.y * ez - a.z * ey), ny = sg * (a.z * ex - a.x * ez), nz = sg * (a.x * ey - a.y * ex);
+    for (int k = 0; k < nd; ++k) {
+      const float4 d = c[k];
+      const float s = fmaf(nx, d.x - a.x, fmaf(ny, d.y - a.y, nz * (d.z - a.z)));
+      if (s >= 0.f) sq |= 1ull << (8 * j + k);
     }
-    for (int i = 0; i < m && o <= kPredCap; ++i) {
-      const float3 q = in_[i], r = in_[i == 0 ? m - 1 : i - 1];
-      const float sq = fmaf(p.x, q.x, fmaf(p.y, q.y, p.z * q.z));
-      if ((sq >= 0.f) != (sp >= 0.f)) {
-        const float wa = fabsf(sq), wb = fabsf(sp);
-        if (o < kPredCap)
-          out_[o] = make_float3(fmaf(wa, r.x, wb * q.x), fmaf(wa, r.y, wb * q.y), fmaf(wa, r.z, wb * q.z));
-        ++o;
-      }
-      if (sq >= 0.f) {
-        if (o < kPredCap) out_[o] = q;
-        ++o;
-      }
-      sp = sq;
-    }
-    m = o;
-    float3* tmp = in_;
-    in_ = out_;
-    out_ = tmp;
   }
-  const int size = m < 0 ? 0 : (m > kPredCap ? kSizeClasses - 1 : min(m, kSizeClasses - 1));
-  cls[t] = (uint16_t)((mask & (kMaskClasses - 1)) | (size << 8));
+  uint32_t allp = (1u << ns) - 1u, allq = (1u << nd) - 1u;
+  for (int k = 0; k < nd; ++k) allp &= (uint32_t)(sp >> (8 * k)) & 0xffu;
+  for (int j = 0; j < ns; ++j) allq &= (uint32_t)(sq >> (8 * j)) & 0xffu;
+  int m = __popc(allp) + __popc(allq);
+  for (int j = 0; j < ns; ++j) {
+    const int j1 = j + 1 == ns ? 0 : j + 1;
+    const uint32_t rq = (uint32_t)(sq >> (8 * j)) & 0xffu;  // destination vertices vs subject edge j
+    for (int k = 0; k < nd; ++k) {
+      const int k1 = k + 1 == nd ? 0 : k + 1;
+      const uint32_t rp = (uint32_t)(sp >> (8 * k)) & 0xffu;  // subject vertices vs destination edge k
+      m += (((rp >> j) ^ (rp >> j1)) & ((rq >> k) ^ (rq >> k1)) & 1u) ? 1 : 0;
+    }
+  }
+  cls[t] = (uint16_t)((mask & (kMaskClasses - 1)) | (min(m, kSizeClasses - 1) << 8));
 }
 
 __global__ void __launch_bounds__(256)
@@ -1522,8 +1503,8 @@ void PairSearch::search(double* dst_area, double* src_area, cudaStream_t st) {
     DBuf<uint16_t> cls((size_t)nc + 1, st);
     cnt.zero();
     fill.zero();
-    k_separated<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, dtab.v4, dtab.nv, dtab.maxv, stab.v4, stab.nv, stab.maxv,
-                                               dplanes32, cls.p);
+    k_separated<<<nblk(nc, 256), 256, 0, st>>>(cand, nc, dtab.v4, dtab.nv, dtab.maxv, stab.v4, stab.nv, stab.ori,
+                                               stab.maxv, dplanes32, cls.p);
     CRG_CHECK_CUDA(cudaGetLastError());
     k_class_count<<<nblk(nc, 256), 256, 0, st>>>(cls.p, nc, cnt.p);
     CRG_CHECK_CUDA(cudaGetLastError());

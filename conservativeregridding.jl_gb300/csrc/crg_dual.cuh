@@ -127,13 +127,7 @@ __device__ __forceinline__ D3n<N> isect_sph_n(const D3n<N>& a, const Dn<N>& sa, 
   if (sb.v == 0.0) return b;
   const Dn<N> wa = dn_abs(sb), wb = dn_abs(sa);
   D3n<N> x{dn_fma(wb, b.x, dn_mul(wa, a.x)), dn_fma(wb, b.y, dn_mul(wa, a.y)), dn_fma(wb, b.z, dn_mul(wa, a.z))};
-  // the value of isect_sph's rsqrt_nr; d(d^-1/2) = -(1/2) d^-3/2 dd
-  const Dn<N> dd = d3n_dot(x, x);
-  Dn<N> ir;
-  ir.v = rsqrt_nr(dd.v);
-  const double c = ((-0.5 * ir.v) * ir.v) * ir.v;
-#pragma unroll
-  for (int i = 0; i < N; ++i) ir.d[i] = c * dd.d[i];
+  const Dn<N> ir = dn_div(dn_const<N>(1.0), dn_sqrt(d3n_dot(x, x)));
   return D3n<N>{dn_mul(x.x, ir), dn_mul(x.y, ir), dn_mul(x.z, ir)};
 }
 

@@ -14,9 +14,7 @@
 //    precision.
 //  * crossing of segment a->b with the clip plane: x = |s_a| b + |s_b| a
 //    (both weights non-negative, so x lies on the minor arc), then normalised
-//    by one reciprocal square root and three products; the reciprocal square
-//    root is Newton-Raphson's iteration y <- y (3/2 - (d/2) y^2), two steps
-//    from a binary32 seed (rsqrt_nr).
+//    by one reciprocal square root taken as 1 / sqrt and three products.
 //  * polygon solid angle: fan from vertex 0; each triangle contributes the
 //    complex factor D + iN of Van Oosterom & Strackee (1983),
 //    N = a.((b-a) x (c-a)) = a.(b x c), D = 1 + a.b + b.c + c.a; the area is
@@ -25,10 +23,8 @@
 //    (Abramowitz & Stegun 4.4.42), with a table-chosen number of terms.
 //
 // Every operation is an IEEE-754 binary64 +,-,*,/,sqrt or an explicit fma in a
-// fixed order (plus the correctly rounded binary32 sqrt and division of
-// rsqrt_nr's seed), and the library is compiled with --fmad=false, so any CPU
-// coding of the same sequence compiled without contraction gives identical
-// bits.
+// fixed order, and the library is compiled with --fmad=false, so any CPU coding
+// of the same sequence compiled without contraction gives identical bits.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -211,25 +207,6 @@ __device__ __forceinline__ double side_sph(d3 nrm, d3 ca, d3 cb, double eb, int 
   return settle(s, bound, isig * det3_sign(ca, cb, v));
 }
 
-// 1 / sqrt(d), d > 0, for the crossing points: d scaled exactly by 4^-k into
-// [0.25, 2), a binary32 seed 1 / sqrt (both operations correctly rounded),
-// two Newton-Raphson steps for the inverse square root in FP64,
-// y <- y (3/2 - (d/2) y^2), and the exact scaling by 2^-k.  About half the
-// FP64 instructions of an IEEE square root and division, within a few ulps of
-// 1 / sqrt(d).  Outside 2^-1000 .. 2^1000 it is 1 / sqrt(d).
-__device__ __forceinline__ double rsqrt_nr(double d) {
-  if (!(d >= 0x1p-1000 && d <= 0x1p1000)) return 1.0 / sqrt(d);
-  const long long bits = __double_as_longlong(d);
-  const int e = (int)((bits >> 52) & 0x7ff) - 1022;  // d = m 2^e, m in [0.5, 1)
-  const int k = e / 2;                                // truncated: e - 2k in {-1, 0, 1}
-  const double ds = d * __longlong_as_double((long long)(1023 - 2 * k) << 52);
-  double y = (double)__fdiv_rn(1.0f, __fsqrt_rn((float)ds));
-  const double h = 0.5 * ds;
-  y = y * fma(-h, y * y, 1.5);
-  y = y * fma(-h, y * y, 1.5);
-  return y * __longlong_as_double((long long)(1023 - k) << 52);
-}
-
 // A vertex exactly on the clip line is passed through unchanged.
 __device__ __forceinline__ d3 isect_sph(d3 a, double sa, d3 b, double sb) {
   if (sa == 0.0) return a;
@@ -239,9 +216,8 @@ __device__ __forceinline__ d3 isect_sph(d3 a, double sa, d3 b, double sb) {
   x.x = fma(wb, b.x, wa * a.x);
   x.y = fma(wb, b.y, wa * a.y);
   x.z = fma(wb, b.z, wa * a.z);
-  // one reciprocal square root and three products (FP64 division and square
-  // root are long instruction sequences on a part with little FP64 throughput)
-  const double ir = rsqrt_nr(ddot(x, x));
+  // one reciprocal and three products: FP64 division is a long instruction sequence
+  const double ir = 1.0 / sqrt(ddot(x, x));
   x.x = x.x * ir; x.y = x.y * ir; x.z = x.z * ir;
   return x;
 }
@@ -371,6 +347,25 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
   float4* out32 = s32 ? s32->b : nullptr;
   int n = ns;
   for (int k = 0; k < nc && n > 0; ++k) {
+    if (kSpherical && s32) {
+      // Skip the stages whose plane leaves every vertex clearly inside (by the
+      // FP32 test below): they return the polygon unchanged.  A lane thus
+      // reaches its next cutting stage at once, and the FP64 work of the
+      // stage body is shared by the lanes that cut at any stage, not only at
+      // this one.
+      for (; k < nc; ++k) {
+        const float4 p = s32->planes[k], c = s32->clip[k];
+        bool all_in = true;
+        for (int i = 0; i < n && all_in; ++i) {
+          const float4 u = in32[i];
+          const float wx = u.x - c.x, wy = u.y - c.y, wz = u.z - c.z;
+          const float sv32 = fmaf(p.x, wx, fmaf(p.y, wy, p.z * wz));
+          all_in = sv32 > 3.814697265625e-06f * p.w * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
+        }
+        if (!all_in) break;
+      }
+      if (k >= nc) break;
+    }
     d3 ca = clip[k], cb = clip[k + 1 == nc ? 0 : k + 1];
     const int isig = sig < 0.0 ? -1 : 1;
     d3 nrm{0.0, 0.0, 0.0};

@@ -220,32 +220,6 @@ static double og_orient_sph(const v3* c, int n) {
     return s >= 0.0 ? 1.0 : -1.0;
 }
 
-/* 1 / sqrt(d), d > 0, as the GPU coding computes it (crg_geom.cuh rsqrt_nr):
- * d scaled exactly by 4^-k into [0.25, 2), a binary32 seed 1 / sqrt (IEEE
- * sqrtf and division, correctly rounded), two Newton-Raphson steps for the
- * inverse square root y <- y (3/2 - (d/2) y^2) in binary64, the exact scaling
- * by 2^-k.  Outside 2^-1000 .. 2^1000: 1 / sqrt(d). */
-static inline double og_pow2(int e) {
-    uint64_t b = (uint64_t)(1023 + e) << 52;
-    double r;
-    memcpy(&r, &b, sizeof r);
-    return r;
-}
-static inline double og_rsqrt_nr(double d) {
-    if (!(d >= 0x1p-1000 && d <= 0x1p1000)) return 1.0 / sqrt(d);
-    uint64_t bits;
-    memcpy(&bits, &d, sizeof bits);
-    const int e = (int)((bits >> 52) & 0x7ff) - 1022;
-    const int k = e / 2;
-    const double ds = d * og_pow2(-2 * k);
-    const float sf = sqrtf((float)ds);
-    double y = (double)(1.0f / sf);
-    const double h = 0.5 * ds;
-    y = y * fma(-h, y * y, 1.5);
-    y = y * fma(-h, y * y, 1.5);
-    return y * og_pow2(-k);
-}
-
 static inline v3 og_isect_sph(v3 a, double sa, v3 b, double sb) {
     if (sa == 0.0) return a;
     if (sb == 0.0) return b;
@@ -254,9 +228,9 @@ static inline v3 og_isect_sph(v3 a, double sa, v3 b, double sb) {
     x.x = fma(wb, b.x, wa * a.x);
     x.y = fma(wb, b.y, wa * a.y);
     x.z = fma(wb, b.z, wa * a.z);
-    /* normalised with one reciprocal square root and three products (the
-       same sequence as the GPU coding) */
-    double ir = og_rsqrt_nr(og_dot(x, x));
+    /* normalised with one reciprocal and three products (one rounding more
+       than three quotients, and the same sequence as the GPU coding) */
+    double ir = 1.0 / sqrt(og_dot(x, x));
     x.x = x.x * ir; x.y = x.y * ir; x.z = x.z * ir;
     return x;
 }
@@ -1316,11 +1290,7 @@ static og_dv og_isect_sph_dn(og_dv a, og_dn sa, og_dv b, og_dn sb) {
     x.x = dn_fma(wb, b.x, dn_mul(wa, a.x));
     x.y = dn_fma(wb, b.y, dn_mul(wa, a.y));
     x.z = dn_fma(wb, b.z, dn_mul(wa, a.z));
-    /* the value of og_isect_sph's og_rsqrt_nr; d(d^-1/2) = -(1/2) d^-3/2 dd */
-    og_dn dd = dv_dot(x, x), ir;
-    ir.v = og_rsqrt_nr(dd.v);
-    const double c = ((-0.5 * ir.v) * ir.v) * ir.v;
-    for (int i = 0; i < 3; ++i) ir.d[i] = c * dd.d[i];
+    og_dn ir = dn_div(dn_k(1.0), dn_sqrt(dv_dot(x, x)));
     x.x = dn_mul(x.x, ir); x.y = dn_mul(x.y, ir); x.z = dn_mul(x.z, ir);
     return x;
 }
