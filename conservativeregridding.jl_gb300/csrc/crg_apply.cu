@@ -200,11 +200,11 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
   const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
   if (r >= nrows) return;
   const int32_t k0 = ptr[r], k1 = ptr[r + 1];
-  if (!kVec) {
+  if constexpr (!kVec) {
     rows_strided<T>(idx, w, k0, k1, x, xsc, y + r * ysc, nf, g, G);
     return;
   }
-  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
+  for (int64_t f = (int64_t)g * 4; kVec && f < nf; f += (int64_t)G * 4) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const bool full = kVec && f + 4 <= nf;
     for (int32_t k = k0; k < k1; ++k) {
