@@ -192,21 +192,14 @@ __device__ __forceinline__ void rows_strided(const int32_t* __restrict__ idx, co
   }
 }
 
-template <class T, int G, bool kVec>
-__global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                                                   const float* __restrict__ w, int64_t nrows, const T* __restrict__ x,
-                                                   int64_t xsc, T* __restrict__ y, int64_t ysc, int64_t nf) {
-  const int g = threadIdx.x % G;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-  if (r >= nrows) return;
-  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
-  if constexpr (!kVec) {
-    rows_strided<T>(idx, w, k0, k1, x, xsc, y + r * ysc, nf, g, G);
-    return;
-  }
-  for (int64_t f = (int64_t)g * 4; kVec && f < nf; f += (int64_t)G * 4) {
+// k_spmm_rows with rows of 4-field vectors: lane g takes fields 4 g, 4 g + 4 G, ...
+template <class T, int G>
+__device__ __forceinline__ void spmm_rows_vec(const int32_t* __restrict__ idx, const float* __restrict__ w, int32_t k0,
+                                              int32_t k1, const T* __restrict__ x, int64_t xsc, T* __restrict__ yr,
+                                              int64_t nf, int g) {
+  for (int64_t f = (int64_t)g * 4; f < nf; f += (int64_t)G * 4) {
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    const bool full = kVec && f + 4 <= nf;
+    const bool full = f + 4 <= nf;
     for (int32_t k = k0; k < k1; ++k) {
       const int64_t j = idx[k];
       const float ww = __ldg(w + k);
@@ -225,7 +218,7 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
       acc.z = fmaf(ww, v.z, acc.z);
       acc.w = fmaf(ww, v.w, acc.w);
     }
-    T* yp = y + r * ysc + f;
+    T* yp = yr + f;
     if (full) {
       st4<T>(yp, acc);
     } else {
@@ -234,6 +227,21 @@ __global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ p
       if (f + 2 < nf) st1<T>(yp + 2, acc.z);
       if (f + 3 < nf) st1<T>(yp + 3, acc.w);
     }
+  }
+}
+
+template <class T, int G, bool kVec>
+__global__ void __launch_bounds__(256) k_spmm_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                   const float* __restrict__ w, int64_t nrows, const T* __restrict__ x,
+                                                   int64_t xsc, T* __restrict__ y, int64_t ysc, int64_t nf) {
+  const int g = threadIdx.x % G;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  if (r >= nrows) return;
+  const int32_t k0 = ptr[r], k1 = ptr[r + 1];
+  if constexpr (!kVec) {
+    rows_strided<T>(idx, w, k0, k1, x, xsc, y + r * ysc, nf, g, G);
+  } else {
+    spmm_rows_vec<T, G>(idx, w, k0, k1, x, xsc, y + r * ysc, nf, g);
   }
 }
 
