@@ -347,25 +347,6 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
   float4* out32 = s32 ? s32->b : nullptr;
   int n = ns;
   for (int k = 0; k < nc && n > 0; ++k) {
-    if (kSpherical && s32) {
-      // Skip the stages whose plane leaves every vertex clearly inside (by the
-      // FP32 test below): they return the polygon unchanged.  A lane thus
-      // reaches its next cutting stage at once, and the FP64 work of the
-      // stage body is shared by the lanes that cut at any stage, not only at
-      // this one.
-      for (; k < nc; ++k) {
-        const float4 p = s32->planes[k], c = s32->clip[k];
-        bool all_in = true;
-        for (int i = 0; i < n && all_in; ++i) {
-          const float4 u = in32[i];
-          const float wx = u.x - c.x, wy = u.y - c.y, wz = u.z - c.z;
-          const float sv32 = fmaf(p.x, wx, fmaf(p.y, wy, p.z * wz));
-          all_in = sv32 > 3.814697265625e-06f * p.w * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
-        }
-        if (!all_in) break;
-      }
-      if (k >= nc) break;
-    }
     d3 ca = clip[k], cb = clip[k + 1 == nc ? 0 : k + 1];
     const int isig = sig < 0.0 ? -1 : 1;
     d3 nrm{0.0, 0.0, 0.0};
