@@ -717,7 +717,7 @@ __global__ void k_edge_planes(const double* __restrict__ v, const int8_t* __rest
 }
 
 template <bool kSph>
-__global__ void __launch_bounds__(128, 5) k_clip(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
+__global__ void __launch_bounds__(128) k_clip(const int2* __restrict__ cand, int64_t nc, const double* __restrict__ dv,
                                               const int8_t* __restrict__ dnv, const int8_t* __restrict__ dori,
                                               int dmaxv, const double* __restrict__ sv,
                                               const int8_t* __restrict__ snv, const int8_t* __restrict__ sori,
@@ -728,44 +728,35 @@ __global__ void __launch_bounds__(128, 5) k_clip(const int2* __restrict__ cand, 
                                               const float4* __restrict__ dplanes32, const float4* __restrict__ dv4,
                                               const float4* __restrict__ sv4) {
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  // spherical: every lane of a warp takes part in the clip (its crossing points are shared)
-  if (!kSph && t >= nc) return;
-  const bool valid = t < nc;
-  const int2 pr = valid ? cand[t] : make_int2(0, 0);
+  if (t >= nc) return;
+  int2 pr = cand[t];
   d3 clip[CRG_MAXV];
   d3 bufA[CRG_MAXC], bufB[CRG_MAXC];
-  const int nd = valid ? dnv[pr.x] : 0, ns = valid ? snv[pr.y] : 0;
+  int nd = dnv[pr.x], ns = snv[pr.y];
   const double* q = dv + (int64_t)pr.x * dmaxv * 3;
   for (int k = 0; k < nd; ++k) { clip[k].x = q[3 * k]; clip[k].y = q[3 * k + 1]; clip[k].z = q[3 * k + 2]; }
   q = sv + (int64_t)pr.y * smaxv * 3;
   for (int k = 0; k < ns; ++k) { bufA[k].x = q[3 * k]; bufA[k].y = q[3 * k + 1]; bufA[k].z = q[3 * k + 2]; }
-  const double sig = valid ? (double)sori[pr.y] : 1.0;  // the subject's orientation (k_cell_geom)
-  const bool poly = nd >= 3 && ns >= 3;
+  const double sig = sori[pr.y];  // the subject's orientation (k_cell_geom)
   double a = 0.0;
-  if (kSph) {
-    __shared__ CrossTask s_tasks[4][kCrossTasks];  // per warp of the 128-thread block
-    __shared__ CrossOut s_outs[4][kCrossTasks];
-    const int w = threadIdx.x >> 5;
+  if (nd >= 3 && ns >= 3) {
     d3* res;
-    float4 fa[CRG_MAXC], fb[CRG_MAXC];
-    Screen32 s32{dplanes32 + (int64_t)pr.x * dmaxv, dv4 + (int64_t)pr.x * dmaxv, fa, fb};
-    if (poly) {
+    float4 fa[kSph ? CRG_MAXC : 1], fb[kSph ? CRG_MAXC : 1];
+    Screen32 s32{nullptr, nullptr, fa, fb};
+    if (kSph) {
+      s32.planes = dplanes32 + (int64_t)pr.x * dmaxv;
+      s32.clip = dv4 + (int64_t)pr.x * dmaxv;
       const float4* q4 = sv4 + (int64_t)pr.y * smaxv;
       for (int k = 0; k < ns; ++k) fa[k] = q4[k];
     }
-    const int m = clip_sph_warp(bufA, bufB, ns, clip, nd, (double)(valid ? dori[pr.x] : 1), &res,
-                                dplanes + (int64_t)pr.x * dmaxv, &s32, poly, s_tasks[w], s_outs[w]);
-    if (poly) {
-      if (m < 0) atomicAdd(overflow, 1ull);
-      else a = area_sph_signed(res, m) * sig;
+    int m = clip_polygon_oriented<kSph>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res,
+                                        kSph ? dplanes + (int64_t)pr.x * dmaxv : nullptr, kSph ? &s32 : nullptr);
+    if (m < 0) {
+      atomicAdd(overflow, 1ull);
+    } else {
+      a = (kSph ? area_sph_signed(res, m) : area_pl_signed(res, m)) * sig;
     }
-  } else if (poly) {
-    d3* res;
-    const int m = clip_polygon_oriented<false>(bufA, bufB, ns, clip, nd, (double)dori[pr.x], &res);
-    if (m < 0) atomicAdd(overflow, 1ull);
-    else a = area_pl_signed(res, m) * sig;
   }
-  if (!valid) return;
   area[t] = a;
   if (a > 0.0) {
     atomicAdd(&rowcnt[pr.x], 1);

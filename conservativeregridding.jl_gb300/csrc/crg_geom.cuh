@@ -487,177 +487,6 @@ __device__ __forceinline__ int clip_polygon_oriented(d3* bufA, d3* bufB, int ns,
   return n;
 }
 
-// ---------------------------------------------------------------- warp-shared crossing points
-//
-// The spherical clip of clip_polygon_oriented with the FP64 work of its
-// stages shared across a warp.  In a warp the lanes clip different pairs; at
-// each stage only some of them are cut (the others keep their polygon), and
-// a cut lane's FP64 work is mostly its two crossing points (the side values
-// of the crossing edges' endpoints and the normalised crossing, ~37 FP64
-// operations each).  Here every lane cut at this stage by exactly two edges
-// posts its two crossing points as tasks in shared memory; all 32 lanes then
-// compute the tasks, 32 at a time, and the owners read the results.  A task
-// runs the operations clip_polygon_oriented runs for that crossing, so the
-// polygons -- and the areas -- are bit-identical.  All 32 lanes of the warp
-// must call it (inactive lanes with active = false).
-struct CrossTask {
-  d3 a, b, nrm, ca;  // the crossing edge a -> b and the stage's half-space
-  double sa, sb;     // side values of a and b when already computed (bits of `known`)
-  uint32_t known;
-};
-struct CrossOut {
-  d3 x;
-  float4 x32;
-};
-constexpr int kCrossTasks = 64;  // two per lane
-
-__device__ __forceinline__ int clip_sph_warp(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, double sig,
-                                             d3** res, const double4_32a* planes, const Screen32* s32,
-                                             bool active, CrossTask* __restrict__ tasks,
-                                             CrossOut* __restrict__ outs) {
-  const int lane = threadIdx.x & 31;
-  d3* in = bufA;
-  d3* out = bufB;
-  float4* in32 = s32->a;
-  float4* out32 = s32->b;
-  int n = active ? ns : 0;
-  bool ovf = false;
-  const int kmax = (int)__reduce_max_sync(0xffffffffu, active ? (unsigned)nc : 0u);
-  const int isig = sig < 0.0 ? -1 : 1;
-  for (int k = 0; k < kmax; ++k) {
-    const bool live = n > 0 && k < nc;
-    d3 ca{0.0, 0.0, 0.0}, cb{0.0, 0.0, 0.0}, nrm{0.0, 0.0, 0.0};
-    double eb = 0.0;
-    double sv[CRG_MAXC];
-    uint32_t inside = 0u, known = 0u;
-    int e0 = -1, e1 = -1, ncross = 0;
-    bool work = false;
-    if (live) {
-      ca = clip[k];
-      cb = clip[k + 1 == nc ? 0 : k + 1];
-      const double4_32a p = planes[k];
-      nrm = d3{p.x, p.y, p.z};
-      eb = p.w;
-      const float4 p32 = s32->planes[k], c32 = s32->clip[k];
-      for (int i = 0; i < n; ++i) {
-        const float4 u = in32[i];
-        const float wx = u.x - c32.x, wy = u.y - c32.y, wz = u.z - c32.z;
-        const float v32 = fmaf(p32.x, wx, fmaf(p32.y, wy, p32.z * wz));
-        const float B = 3.814697265625e-06f * p32.w * (1.0f + fabsf(wx) + fabsf(wy) + fabsf(wz));  // 2^-18
-        if (v32 > B) {
-          inside |= 1u << i;
-        } else if (!(v32 < -B)) {
-          sv[i] = side_sph(nrm, ca, cb, eb, isig, in[i]);
-          known |= 1u << i;
-          if (sv[i] >= 0.0) inside |= 1u << i;
-        }
-      }
-      const int nin = __popc(inside);
-      if (nin == 0) {
-        n = 0;
-      } else if (nin < n) {
-        work = true;
-        for (int i = 0; i < n; ++i) {
-          const int q = i == 0 ? n - 1 : i - 1;
-          if (((inside >> i) & 1u) != ((inside >> q) & 1u)) {
-            if (ncross == 0) e0 = i;
-            else e1 = i;
-            ++ncross;
-          }
-        }
-      }
-    }
-    // the two crossing points of every lane cut by two edges, computed by the whole warp
-    const bool two = work && ncross == 2;
-    const unsigned bal = __ballot_sync(0xffffffffu, two);
-    const int rank = __popc(bal & ((1u << lane) - 1u));
-    const int ntask = 2 * __popc(bal);
-    if (two) {
-      const int p0 = e0 == 0 ? n - 1 : e0 - 1, p1 = e1 == 0 ? n - 1 : e1 - 1;
-      const int ends[4] = {p0, e0, p1, e1};
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        CrossTask& t = tasks[2 * rank + h];
-        const int ia = ends[2 * h], ib = ends[2 * h + 1];
-        t.a = in[ia];
-        t.b = in[ib];
-        t.nrm = nrm;
-        t.ca = ca;
-        t.known = ((known >> ia) & 1u) | (((known >> ib) & 1u) << 1);
-        t.sa = ((known >> ia) & 1u) ? sv[ia] : 0.0;
-        t.sb = ((known >> ib) & 1u) ? sv[ib] : 0.0;
-      }
-    }
-    __syncwarp();
-    for (int q = lane; q < ntask; q += 32) {
-      const CrossTask& t = tasks[q];
-      // a vertex the FP32 test decided takes the plain FP64 side, as in clip_polygon_oriented
-      const double sa = (t.known & 1u) ? t.sa : ddot(t.nrm, dsub(t.a, t.ca));
-      const double sb = (t.known & 2u) ? t.sb : ddot(t.nrm, dsub(t.b, t.ca));
-      const d3 x = isect_sph(t.a, sa, t.b, sb);
-      outs[q].x = x;
-      outs[q].x32 = make_float4((float)x.x, (float)x.y, (float)x.z, 0.f);
-    }
-    __syncwarp();
-    if (work) {
-      auto side = [&](int i) -> double {
-        if (!((known >> i) & 1u)) {
-          sv[i] = ddot(nrm, dsub(in[i], ca));
-          known |= 1u << i;
-        }
-        return sv[i];
-      };
-      CrossOut o0, o1;
-      if (two) {
-        o0 = outs[2 * rank];
-        o1 = outs[2 * rank + 1];
-      }
-      int m = 0;
-      for (int i = 0; i < n && !ovf; ++i) {
-        const int q = i == 0 ? n - 1 : i - 1;
-        const bool ci = ((inside >> i) & 1u) != 0u, pi = ((inside >> q) & 1u) != 0u;
-        if (ci == pi) {
-          if (ci) {
-            if (m >= CRG_MAXC) { ovf = true; break; }
-            out32[m] = in32[i];
-            out[m++] = in[i];
-          }
-          continue;
-        }
-        // a crossing edge (more than two only for non-convex input: computed here)
-        d3 x;
-        float4 x32;
-        if (two) {
-          x = i == e0 ? o0.x : o1.x;
-          x32 = i == e0 ? o0.x32 : o1.x32;
-        } else {
-          const double sp = side(q), sc = side(i);
-          x = isect_sph(in[q], sp, in[i], sc);
-          x32 = make_float4((float)x.x, (float)x.y, (float)x.z, 0.f);
-        }
-        if (m >= CRG_MAXC) { ovf = true; break; }
-        out32[m] = x32;
-        out[m++] = x;
-        if (ci) {
-          if (m >= CRG_MAXC) { ovf = true; break; }
-          out32[m] = in32[i];
-          out[m++] = in[i];
-        }
-      }
-      if (ovf) {
-        n = 0;
-      } else {
-        d3* t = in; in = out; out = t;
-        float4* t32 = in32; in32 = out32; out32 = t32;
-        n = m;
-      }
-    }
-    __syncwarp();  // the task buffers are reused by the next stage
-  }
-  *res = in;
-  return ovf ? -1 : n;
-}
-
 // clip_polygon_oriented with the clip polygon's orientation computed here
 template <bool kSpherical>
 __device__ __forceinline__ int clip_polygon(d3* bufA, d3* bufB, int ns, const d3* clip, int nc, d3** res) {
