@@ -117,7 +117,7 @@ __device__ __forceinline__ Dn<N> side_sph_n(const D3n<N>& nrm, const D3n<N>& ca,
   Dn<N> s = d3n_dot(nrm, w);
   const double bound = eb * (fabs(w.x.v) + fabs(w.y.v) + fabs(w.z.v)) + kTiny;
   if (fabs(s.v) > bound) return s;
-  s.v = settle(s.v, bound, isig * det3_sign(dval(ca), dval(cb), dval(v)));
+  s.v = settle(s.v, bound, isig * det3_sign_adapt(dval(ca), dval(cb), dval(v)));
   return s;
 }
 
@@ -125,7 +125,11 @@ template <int N>
 __device__ __forceinline__ D3n<N> isect_sph_n(const D3n<N>& a, const Dn<N>& sa, const D3n<N>& b, const Dn<N>& sb) {
   if (sa.v == 0.0) return a;
   if (sb.v == 0.0) return b;
-  const Dn<N> wa = dn_abs(sb), wb = dn_abs(sa);
+  Dn<N> wa = dn_abs(sb), wb = dn_abs(sa);
+  if (fmax(wa.v, wb.v) < kIsectTiny) {  // isect_sph's rescaling of tiny weights
+    wa = dn_scale(kIsectScale, wa);
+    wb = dn_scale(kIsectScale, wb);
+  }
   D3n<N> x{dn_fma(wb, b.x, dn_mul(wa, a.x)), dn_fma(wb, b.y, dn_mul(wa, a.y)), dn_fma(wb, b.z, dn_mul(wa, a.z))};
   const Dn<N> ir = dn_div(dn_const<N>(1.0), dn_sqrt(d3n_dot(x, x)));
   return D3n<N>{dn_mul(x.x, ir), dn_mul(x.y, ir), dn_mul(x.z, ir)};
@@ -185,7 +189,11 @@ template <int N>
 __device__ __forceinline__ D3n<N> isect_pl_n(const D3n<N>& a, const Dn<N>& sa, const D3n<N>& b, const Dn<N>& sb) {
   if (sa.v == 0.0) return a;
   if (sb.v == 0.0) return b;
-  const Dn<N> wa = dn_abs(sb), wb = dn_abs(sa);
+  Dn<N> wa = dn_abs(sb), wb = dn_abs(sa);
+  if (fmax(wa.v, wb.v) < kIsectTiny) {
+    wa = dn_scale(kIsectScale, wa);
+    wb = dn_scale(kIsectScale, wb);
+  }
   const Dn<N> w = dn_add(wa, wb);
   return D3n<N>{dn_div(dn_fma(wb, b.x, dn_mul(wa, a.x)), w), dn_div(dn_fma(wb, b.y, dn_mul(wa, a.y)), w),
                 dn_const<N>(0.0)};

@@ -100,8 +100,71 @@ static __device__ __noinline__ int det3_sign(d3 a, d3 b, d3 c) {
   return exact_sign(t, 24);
 }
 
-// sign of (bx-ax)(vy-ay) - (by-ay)(vx-ax), exactly
+// p*q - r*w as the double-double s + lo (TwoProduct for both products, TwoSum
+// of the heads, the tails added in FP64), and |p*q| + |r*w| for the bound.
+// |s + lo - (p*q - r*w)| <= 4 u^2 (|p*q| + |r*w|), u = 2^-53.
+__device__ __forceinline__ void minor_dd(double p, double q, double r, double w, double& s, double& lo,
+                                         double& perm) {
+  double p1, e1, p2, e2, t;
+  two_prod(p, q, p1, e1);
+  two_prod(r, w, p2, e2);
+  two_sum(p1, -p2, s, t);
+  lo = t + (e1 - e2);
+  perm = fabs(p1) + fabs(p2);
+}
+
+// 2^-99 = 128 u^2: four times the worst-case error of det3_sign_adapt's
+// double-double value relative to the permanent (< 32 u^2).
+constexpr double kDetDD = 1.5777218104420236e-30;
+// an absolute floor for bounds: covers rounding of products in the subnormal range
+constexpr double kTiny = 1e-290;
+
+// Sign of det[a; b; c] from a double-double evaluation (Dekker 1971 products,
+// Shewchuk 1997 adaptive filtering), or 0 when that value cannot decide it.  The
+// 2x2 minors of b, c are formed as double-doubles, multiplied by a's components
+// with TwoProduct heads and FP64 tails, the three heads summed exactly and the
+// eight tail terms (below 5 u perm in all) in FP64, four roundings deep.  The
+// value differs from the determinant by at most 3 u^2 perm (minors) + 2 u^2 perm
+// (tail products) + 20 u^2 perm (tail sum) + O(u^3), perm = sum_k |a_k|
+// (|b_i c_j| + |b_j c_i|): outside 128 u^2 perm (+1e-290 for products in the
+// subnormal range) its sign is the determinant's.
+__device__ __forceinline__ int det3_sign_dd(d3 a, d3 b, d3 c) {
+  double sx, lx, px, sy, ly, py, sz, lz, pz;
+  minor_dd(b.y, c.z, b.z, c.y, sx, lx, px);
+  minor_dd(b.z, c.x, b.x, c.z, sy, ly, py);
+  minor_dd(b.x, c.y, b.y, c.x, sz, lz, pz);
+  double hx, ex, hy, ey, hz, ez, s1, r1, s, r2;
+  two_prod(a.x, sx, hx, ex);
+  two_prod(a.y, sy, hy, ey);
+  two_prod(a.z, sz, hz, ez);
+  two_sum(hx, hy, s1, r1);
+  two_sum(s1, hz, s, r2);
+  const double tail = ((r1 + r2) + ((ex + ey) + ez)) + ((a.x * lx + a.y * ly) + a.z * lz);
+  const double d = s + tail;
+  const double perm = (fabs(a.x) * px + fabs(a.y) * py) + fabs(a.z) * pz;
+  if (fabs(d) > kDetDD * perm + kTiny) return d > 0.0 ? 1 : -1;
+  return 0;
+}
+
+__device__ __forceinline__ bool same_point(d3 p, d3 q) { return p.x == q.x && p.y == q.y && p.z == q.z; }
+
+// The exact sign of det[a; b; c], the same as det3_sign's.  Two equal points
+// give 0 at once (a vertex of one grid that is a vertex of the other: most of
+// the exact-sign calls between grids that share vertices).  Otherwise the
+// double-double filter decides unless the determinant is below 1e-30 of its
+// terms (exactly zero, as for three points with one coordinate zero); then the
+// error-free expansion does.  The filter costs about a tenth of the expansion
+// where points lie on a great circle only up to the rounding of their
+// coordinates (meridians of a lon-lat grid through another grid's vertices).
+static __device__ __noinline__ int det3_sign_adapt(d3 a, d3 b, d3 c) {
+  if (same_point(c, a) || same_point(c, b) || same_point(a, b)) return 0;
+  const int s = det3_sign_dd(a, b, c);
+  return s != 0 ? s : det3_sign(a, b, c);
+}
+
+// sign of (bx-ax)(vy-ay) - (by-ay)(vx-ax), exactly (0 at once for two equal points)
 static __device__ __noinline__ int orient2_sign(double ax, double ay, double bx, double by, double vx, double vy) {
+  if ((vx == ax && vy == ay) || (vx == bx && vy == by) || (ax == bx && ay == by)) return 0;
   double d[4][2];
   two_sum(bx, -ax, d[0][0], d[0][1]);
   two_sum(vy, -ay, d[1][0], d[1][1]);
@@ -126,7 +189,6 @@ static __device__ __noinline__ int orient2_sign(double ax, double ay, double bx,
 
 constexpr double kU32 = 3.552713678800501e-15;  // 32 * 2^-53
 constexpr double kU8 = 8.881784197001252e-16;   // 8 * 2^-53
-constexpr double kTiny = 1e-290;
 
 __device__ __forceinline__ double settle(double s, double bound, int sg) {
   if (fabs(s) > bound) return s;
@@ -204,14 +266,25 @@ __device__ __forceinline__ double side_sph(d3 nrm, d3 ca, d3 cb, double eb, int 
   double s = ddot(nrm, w);
   double bound = eb * (fabs(w.x) + fabs(w.y) + fabs(w.z)) + kTiny;
   if (fabs(s) > bound) return s;
-  return settle(s, bound, isig * det3_sign(ca, cb, v));
+  return settle(s, bound, isig * det3_sign_adapt(ca, cb, v));
 }
+
+// Crossing weights below 2^-400 are scaled by 2^600 (exactly) before they are
+// combined.  They come from side values the exact sign settled to about
+// DBL_MIN at both ends of an edge; unscaled, the squared norm of the combination
+// underflows to 0 and the crossing point becomes infinite.  The normalisation
+// removes the factor, and weights from 2^-400 up take the unscaled sequence.
+constexpr double kIsectTiny = 0x1p-400, kIsectScale = 0x1p600;
 
 // A vertex exactly on the clip line is passed through unchanged.
 __device__ __forceinline__ d3 isect_sph(d3 a, double sa, d3 b, double sb) {
   if (sa == 0.0) return a;
   if (sb == 0.0) return b;
   double wa = fabs(sb), wb = fabs(sa);
+  if (fmax(wa, wb) < kIsectTiny) {
+    wa *= kIsectScale;
+    wb *= kIsectScale;
+  }
   d3 x;
   x.x = fma(wb, b.x, wa * a.x);
   x.y = fma(wb, b.y, wa * a.y);
@@ -298,6 +371,10 @@ __device__ __forceinline__ d3 isect_pl(d3 a, double sa, d3 b, double sb) {
   if (sa == 0.0) return a;
   if (sb == 0.0) return b;
   double wa = fabs(sb), wb = fabs(sa);
+  if (fmax(wa, wb) < kIsectTiny) {  // as in isect_sph: the products would lose their bits
+    wa *= kIsectScale;
+    wb *= kIsectScale;
+  }
   double w = wa + wb;
   d3 x;
   x.x = fma(wb, b.x, wa * a.x) / w;

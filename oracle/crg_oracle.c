@@ -220,10 +220,18 @@ static double og_orient_sph(const v3* c, int n) {
     return s >= 0.0 ? 1.0 : -1.0;
 }
 
+/* Crossing weights below 2^-400 (side values settled to about DBL_MIN at both
+ * ends of an edge) are scaled by 2^600, exactly, before they are combined:
+ * unscaled, the squared norm underflows to 0 and the point becomes infinite.
+ * The normalisation removes the factor; larger weights are left as they are. */
+#define OG_ISECT_TINY 0x1p-400
+#define OG_ISECT_SCALE 0x1p600
+
 static inline v3 og_isect_sph(v3 a, double sa, v3 b, double sb) {
     if (sa == 0.0) return a;
     if (sb == 0.0) return b;
     double wa = fabs(sb), wb = fabs(sa);
+    if (fmax(wa, wb) < OG_ISECT_TINY) { wa *= OG_ISECT_SCALE; wb *= OG_ISECT_SCALE; }
     v3 x;
     x.x = fma(wb, b.x, wa * a.x);
     x.y = fma(wb, b.y, wa * a.y);
@@ -312,6 +320,7 @@ static inline v3 og_isect_pl(v3 a, double sa, v3 b, double sb) {
     if (sa == 0.0) return a;
     if (sb == 0.0) return b;
     double wa = fabs(sb), wb = fabs(sa);
+    if (fmax(wa, wb) < OG_ISECT_TINY) { wa *= OG_ISECT_SCALE; wb *= OG_ISECT_SCALE; }
     double w = wa + wb;
     v3 x;
     x.x = fma(wb, b.x, wa * a.x) / w;
@@ -1255,6 +1264,11 @@ static inline og_dn dn_sqrt(og_dn a) {
     return r;
 }
 static inline og_dn dn_abs(og_dn a) { return a.v < 0.0 ? dn_neg(a) : a; }
+static inline og_dn dn_scale(double k, og_dn a) {
+    og_dn r; r.v = k * a.v;
+    for (int i = 0; i < 3; ++i) r.d[i] = k * a.d[i];
+    return r;
+}
 
 static inline v3 dv_val(og_dv a) { v3 r = {a.x.v, a.y.v, a.z.v}; return r; }
 static inline og_dv dv_k(v3 a) { og_dv r = {dn_k(a.x), dn_k(a.y), dn_k(a.z)}; return r; }
@@ -1286,6 +1300,7 @@ static og_dv og_isect_sph_dn(og_dv a, og_dn sa, og_dv b, og_dn sb) {
     if (sa.v == 0.0) return a;
     if (sb.v == 0.0) return b;
     og_dn wa = dn_abs(sb), wb = dn_abs(sa);
+    if (fmax(wa.v, wb.v) < OG_ISECT_TINY) { wa = dn_scale(OG_ISECT_SCALE, wa); wb = dn_scale(OG_ISECT_SCALE, wb); }
     og_dv x;
     x.x = dn_fma(wb, b.x, dn_mul(wa, a.x));
     x.y = dn_fma(wb, b.y, dn_mul(wa, a.y));
@@ -1331,6 +1346,7 @@ static og_dv og_isect_pl_dn(og_dv a, og_dn sa, og_dv b, og_dn sb) {
     if (sa.v == 0.0) return a;
     if (sb.v == 0.0) return b;
     og_dn wa = dn_abs(sb), wb = dn_abs(sa);
+    if (fmax(wa.v, wb.v) < OG_ISECT_TINY) { wa = dn_scale(OG_ISECT_SCALE, wa); wb = dn_scale(OG_ISECT_SCALE, wb); }
     og_dn w = dn_add(wa, wb);
     og_dv x;
     x.x = dn_div(dn_fma(wb, b.x, dn_mul(wa, a.x)), w);

@@ -279,3 +279,22 @@ def test_random_spherical_pairs_vs_mpmath():
         scale = oracle.cell_area(s)
         assert abs(got - want) <= 1e-14 * scale, (trial, got, want)
     assert overlapping >= 40
+
+
+def test_pole_rows_conserve_area():
+    """45-degree cells against 0.5-degree cells: both grids have a pole row whose
+    cells carry the pole twice (sind(90) = 1 exactly, cosd(90) = 0).  Side values
+    that the exact sign settles to about DBL_MIN at both ends of an edge make
+    crossing weights whose combination underflows; the crossing is rescaled
+    first, so every cell's intersections still add up to its area (before the
+    rescaling one 0.5-degree pole cell lost all of it, and 22 entries)."""
+    dst, src = grids.lonlat_regular(45.0, 45.0), grids.lonlat_regular(0.5, 0.5)
+    R = oracle.OracleRegridder(dst, src, normalize=False)
+    assert R.nnz == 261768 and np.isfinite(R.nzval).all()
+    rows = np.zeros(R.nd)
+    cols = np.zeros(R.ns)
+    np.add.at(rows, R.rowval, R.nzval)
+    np.add.at(cols, np.repeat(np.arange(R.ns), np.diff(R.colptr)), R.nzval)
+    assert np.max(np.abs(rows - R.dst_areas) / R.dst_areas) < 1e-12
+    assert np.max(np.abs(cols - R.src_areas) / R.src_areas) < 1e-12
+    assert abs(R.nzval.sum() - 4 * np.pi) < 1e-11
