@@ -74,6 +74,8 @@ def parse():
                    help="skip the summaries of the smaller configurations in the default line")
     p.add_argument("--profile", action="store_true",
                    help="only build and run `steps` forward+transpose SpMM rounds (for an ncu capture)")
+    p.add_argument("--dtype", default="float32", choices=["float32", "bfloat16"],
+                   help="field type of the --profile rounds")
     p.add_argument("--pair", default="c5", choices=["c5", "identity"],
                    help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
                         "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
@@ -114,8 +116,13 @@ def run_profile(a):
         out_f = torch.empty((K, nd), device=dev)
         out_r = torch.empty((K, ns), device=dev)
         dims = 2
+    elem = 4
+    if a.dtype == "bfloat16":
+        src, dsrc = src.bfloat16(), dsrc.bfloat16()
+        out_f, out_r = out_f.bfloat16(), out_r.bfloat16()
+        elem = 2
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    bf, br = step_bytes(R.nnz, nd, ns, K)
+    bf, br = step_bytes(R.nnz, nd, ns, K, elem=elem)
     reps = 8  # back-to-back launches per direction keep the GPU busy past the host call overhead
     for i in range(a.steps):
         regrid_(out_f, R, src, dims=dims)

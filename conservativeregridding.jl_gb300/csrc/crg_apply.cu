@@ -540,7 +540,8 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
     if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
     const unsigned newrow = starts;
     const int n = e1 - c0 < 32 ? e1 - c0 : 32;
-    for (int k = 0; k < n; k += B) {
+    // B entries of the chunk from entry k: their gathers first, then their FMAs
+    auto group = [&](int k, int nn) {
       Raw v[B];
       float ww[B];
 #pragma unroll
@@ -553,7 +554,7 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
       }
 #pragma unroll
       for (int h = 0; h < B; ++h) {
-        if (k + h >= n) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
+        if (k + h >= nn) break;  // no FMA with past-the-end data (0 * Inf would poison the row)
         if ((newrow >> (k + h)) & 1u) {
           flush(cur);
           // kGaps: the next row with entries (nextrow), when the layout has one
@@ -568,6 +569,13 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
         acc.z = fmaf(ww[h], xv.z, acc.z);
         acc.w = fmaf(ww[h], xv.w, acc.w);
       }
+    };
+    if (n == 32) {
+      // a full chunk, unrolled: shuffle lanes and row-start bits are constants
+#pragma unroll
+      for (int k = 0; k < 32; k += B) group(k, 32);
+    } else {
+      for (int k = 0; k < n; k += B) group(k, n);
     }
     starts = nstarts;
     myo = no;
