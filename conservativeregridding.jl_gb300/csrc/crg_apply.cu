@@ -438,6 +438,9 @@ template <> struct CmGather<float> {
   using Raw = float4;
   static constexpr int kInFlight = 4;
   static constexpr int kMinBlocks = 4;
+  // (offset, weight) pairs by two shuffles per entry (latency-bound: the
+  // shared-memory staging measured 0.402 against 0.396 ms per step)
+  static constexpr bool kStage = false;
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const float4*>(base + off));
   }
@@ -447,6 +450,9 @@ template <> struct CmGather<__nv_bfloat16> {
   using Raw = uint2;
   static constexpr int kInFlight = 8;
   static constexpr int kMinBlocks = 3;
+  // (offset, weight) pairs by one broadcast shared load per entry: the BF16
+  // kernel is closer to its issue limit (0.320 against 0.333 ms per step)
+  static constexpr bool kStage = true;
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const uint2*>(base + off));
   }
@@ -476,12 +482,15 @@ __device__ __forceinline__ float4 cm_strided_load(const char* base, uint32_t off
 // base (its first field of cell 0), `fo` that field, `onm` which of its 4
 // fields exist (bit t); B gathers are in flight.  kVec: the lane's fields are
 // fo .. fo + 3 (16-byte FP32 / 8-byte BF16 vectors); otherwise fo + 32 t.
+// `stg`: the warp's 64-slot staging in shared memory; with CmGather<T>::kStage
+// each 32-entry chunk's (source offset, weight) pairs go there, so that an
+// entry costs one broadcast 8-byte shared load instead of two shuffles.
 template <class T, bool kGaps, int B, bool kVec = true>
 __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ tasks, const int2* __restrict__ tslot,
                                         const int32_t* __restrict__ idx, const uint32_t* __restrict__ rbits,
                                         const int32_t* __restrict__ nextrow, const float* __restrict__ w,
                                         const char* xb, uint32_t cstride, T* __restrict__ y, int64_t ys, int64_t fo,
-                                        int onm, float* __restrict__ carry, int lane) {
+                                        int onm, float* __restrict__ carry, int lane, uint2* __restrict__ stg) {
   using G = CmGather<T>;
   using Raw = typename std::conditional<kVec, typename G::Raw, float4>::type;
   const int4 tr = __ldg(tasks + task);
@@ -533,6 +542,14 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
   float myw;
   load(e0, starts, myo, myw);
   starts &= ~1u;  // entry e0 belongs to row `first` (already current)
+  // slots 0..31 and 32..63 alternate between chunks; the warp barrier after a
+  // chunk's pairs are written also ends every read of the other half
+  int half = 0;
+  if constexpr (G::kStage) {
+    __syncwarp();
+    stg[lane] = make_uint2(myo, __float_as_uint(myw));
+    __syncwarp();
+  }
   for (int32_t c0 = e0; c0 < e1; c0 += 32) {
     // the next chunk's entries load while this one is gathered
     uint32_t nstarts = 0u, no = 0u;
@@ -540,14 +557,22 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
     if (c0 + 32 < e1) load(c0 + 32, nstarts, no, nwt);
     const unsigned newrow = starts;
     const int n = e1 - c0 < 32 ? e1 - c0 : 32;
+    const uint2* sp = stg + half;
     // B entries of the chunk from entry k: their gathers first, then their FMAs
     auto group = [&](int k, int nn) {
       Raw v[B];
       float ww[B];
 #pragma unroll
       for (int h = 0; h < B; ++h) {
-        const uint32_t o = __shfl_sync(0xffffffffu, myo, (k + h) & 31);
-        ww[h] = __shfl_sync(0xffffffffu, myw, (k + h) & 31);
+        uint32_t o;
+        if constexpr (G::kStage) {
+          const uint2 ow = sp[(k + h) & 31];
+          o = ow.x;
+          ww[h] = __uint_as_float(ow.y);
+        } else {
+          o = __shfl_sync(0xffffffffu, myo, (k + h) & 31);
+          ww[h] = __shfl_sync(0xffffffffu, myw, (k + h) & 31);
+        }
         // past-the-end entries load cell 0 with weight 0
         if constexpr (kVec) v[h] = G::load(xb, o);
         else v[h] = cm_strided_load<T>(xb, o, onm);
@@ -578,8 +603,14 @@ __device__ __forceinline__ void cm_task(int64_t task, const int4* __restrict__ t
       for (int k = 0; k < n; k += B) group(k, n);
     }
     starts = nstarts;
-    myo = no;
-    myw = nwt;
+    if constexpr (G::kStage) {
+      half ^= 32;
+      stg[half + lane] = make_uint2(no, __float_as_uint(nwt));
+      __syncwarp();
+    } else {
+      myo = no;
+      myw = nwt;
+    }
   }
   flush(cur);
 }
@@ -615,8 +646,11 @@ __global__ void __launch_bounds__(256, MINB)
   // per-lane base of this lane's fields; cell j adds j * xs elements (32-bit byte offset)
   const char* xb = cm_lane_base<T, kVec>(x, f0, nf, lane, fo, onm);
   const uint32_t cstride = (uint32_t)(xs * (int64_t)sizeof(T));
+  __shared__ uint2 s_stage[CmGather<T>::kStage ? 8 : 1][64];
+  uint2* stg = CmGather<T>::kStage ? s_stage[threadIdx.x >> 5] : nullptr;
   for (int64_t task = gw; task < ntasks; task += nw)
-    cm_task<T, kGaps, B, kVec>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, onm, carry, lane);
+    cm_task<T, kGaps, B, kVec>(task, tasks, tslot, idx, rbits, nextrow, w, xb, cstride, y, ys, fo, onm, carry, lane,
+                               stg);
 }
 
 // Rows cut between tasks: sum their pieces in task order (deterministic).
@@ -1274,6 +1308,8 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  __shared__ uint2 s_stage[CmGather<T>::kStage ? 8 : 1][64];
+  uint2* stg = CmGather<T>::kStage ? s_stage[threadIdx.x >> 5] : nullptr;
   for (int64_t u = gw; u < nunits; u += nw) {
     const BatchItem* itp = items + batch_find(unit0, nitems, u);
     const int64_t ntasks = itp->ntasks, k = u - itp->unit0;
@@ -1289,11 +1325,11 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
     if (itp->vec) {
       const char* xb = cm_lane_base<T, true>(x, pass * 128, itp->nf, lane, fo, onm);
       cm_task<T, true, B, true>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nextrow, itp->w, xb, cstride, y,
-                                itp->ys, fo, onm, carry, lane);
+                                itp->ys, fo, onm, carry, lane, stg);
     } else {
       const char* xb = cm_lane_base<T, false>(x, pass * 128, itp->nf, lane, fo, onm);
       cm_task<T, true, B, false>(task, itp->tasks, itp->tslot, itp->idx, itp->rbits, nextrow, itp->w, xb, cstride,
-                                 y, itp->ys, fo, onm, carry, lane);
+                                 y, itp->ys, fo, onm, carry, lane, stg);
     }
   }
 }
