@@ -682,12 +682,16 @@ def run_c3(a):
         items.append((y, R, x, 1))
         nbytes += step_bytes(R.nnz, nd, ns, K)[0]
     plan = ApplyPlan(items)
-    # the same applies captured as one graph branch per item (for comparison)
-    os.environ["CRG_PLAN_BATCH"] = "0"
-    try:
-        plan_branches = ApplyPlan(items)
-    finally:
-        del os.environ["CRG_PLAN_BATCH"]
+    # for comparison: every item as its own graph branch, and every item in the
+    # persistent launch
+    forms = {}
+    for form, env in (("branches", "0"), ("all", "all")):
+        os.environ["CRG_PLAN_BATCH"] = env
+        try:
+            forms[form] = ApplyPlan(items)
+        finally:
+            del os.environ["CRG_PLAN_BATCH"]
+    plan_branches, plan_all = forms["branches"], forms["all"]
 
     def loop():
         for y, R, x, dims in items:
@@ -699,6 +703,7 @@ def run_c3(a):
         loop()
         plan.launch()
         plan_branches.launch()
+        plan_all.launch()
     reps = max(5, min(a.steps, 50))
     torch.cuda.synchronize()
     ev[0].record(stream)
@@ -717,6 +722,12 @@ def run_c3(a):
     ev[1].record(stream)
     ev[1].synchronize()
     ms_branches = ev[0].elapsed_time(ev[1]) / reps
+    ev[0].record(stream)
+    for _ in range(reps):
+        plan_all.launch()
+    ev[1].record(stream)
+    ev[1].synchronize()
+    ms_all = ev[0].elapsed_time(ev[1]) / reps
     # one replay of each plan inside an NVTX range (selects their launches for ncu's launch list)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("c3_plan")
@@ -740,9 +751,12 @@ def run_c3(a):
                   "GB/s_graph": round(nbytes / (ms_plan * 1e-3) / 1e9, 1),
                   "GB/s_loop": round(nbytes / (ms_loop * 1e-3) / 1e9, 1), "bytes_per_batch": nbytes,
                   "graph_kernels": plan.info["kernels"], "graph_batched_items": plan.info["batched_items"],
-                  "graph": "one persistent launch over all pairs' work units + one for cut rows",
+                  "graph": "one CUDA graph: the small multi-pass pairs in one persistent launch, every other "
+                           "pair its own tuned apply on a branch",
                   "branches_ms": round(ms_branches, 4), "branches_kernels": plan_branches.info["kernels"],
-                  "GB/s_branches": round(nbytes / (ms_branches * 1e-3) / 1e9, 1)},
+                  "GB/s_branches": round(nbytes / (ms_branches * 1e-3) / 1e9, 1),
+                  "all_persistent_ms": round(ms_all, 4), "all_persistent_kernels": plan_all.info["kernels"],
+                  "GB/s_all_persistent": round(nbytes / (ms_all * 1e-3) / 1e9, 1)},
     }
 
 

@@ -441,6 +441,10 @@ template <> struct CmGather<float> {
   // (offset, weight) pairs by two shuffles per entry (latency-bound: the
   // shared-memory staging measured 0.402 against 0.396 ms per step)
   static constexpr bool kStage = false;
+  // k_batch_apply holds the vector, strided and row paths at once; at 4 blocks
+  // per SM (64 registers) it spills a little, and still beats 3 blocks (0.58
+  // against 0.73 ms for a batch of 32 uneven pairs)
+  static constexpr int kBatchMinBlocks = 4;
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const float4*>(base + off));
   }
@@ -453,6 +457,7 @@ template <> struct CmGather<__nv_bfloat16> {
   // (offset, weight) pairs by one broadcast shared load per entry: the BF16
   // kernel is closer to its issue limit (0.320 against 0.333 ms per step)
   static constexpr bool kStage = true;
+  static constexpr int kBatchMinBlocks = 3;
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const uint2*>(base + off));
   }
@@ -1298,19 +1303,31 @@ __device__ __forceinline__ void rows_unit(const BatchItem* __restrict__ itp, int
   }
 }
 
-// The merge-path items of a batch: one unit per task and 128-field pass (the
-// default gathers in flight and blocks per SM of k_cm_nnz).
+// The items of a batch: units 0 .. nunits-1 are merge-path units, one per
+// task and 128-field pass (the default gathers in flight and blocks per SM of
+// k_cm_nnz); units nunits .. nunits+nrunits-1 are row units of the other items
+// (a warp per group of 32 / G rows, rows_unit).  One grid-stride loop over
+// both: the warps stay resident, and the row units fill the end of the launch
+// instead of waiting for SM slots the persistent warps hold.
 template <class T>
-__global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(const BatchItem* __restrict__ items,
+__global__ void __launch_bounds__(256, CmGather<T>::kBatchMinBlocks) k_batch_apply(const BatchItem* __restrict__ items,
                                                         const int64_t* __restrict__ unit0, int nitems,
-                                                        int64_t nunits) {
+                                                        int64_t nunits, const BatchItem* __restrict__ ritems,
+                                                        const int64_t* __restrict__ runit0, int nritems,
+                                                        int64_t nrunits) {
   constexpr int B = CmGather<T>::kInFlight;
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
   __shared__ uint2 s_stage[CmGather<T>::kStage ? 8 : 1][64];
   uint2* stg = CmGather<T>::kStage ? s_stage[threadIdx.x >> 5] : nullptr;
-  for (int64_t u = gw; u < nunits; u += nw) {
+  for (int64_t u = gw; u < nunits + nrunits; u += nw) {
+    if (u >= nunits) {
+      const int64_t v = u - nunits;
+      const BatchItem* rtp = ritems + batch_find(runit0, nritems, v);
+      rows_unit<T>(rtp, v - rtp->unit0, lane);
+      continue;
+    }
     const BatchItem* itp = items + batch_find(unit0, nitems, u);
     const int64_t ntasks = itp->ntasks, k = u - itp->unit0;
     const int64_t pass = k / ntasks, task = k - pass * ntasks;
@@ -1332,19 +1349,6 @@ __global__ void __launch_bounds__(256, CmGather<T>::kMinBlocks) k_batch_apply(co
                                  y, itp->ys, fo, onm, carry, lane, stg);
     }
   }
-}
-
-// The row items of a batch: one warp per unit (a group of 32 / G rows), the
-// grid covering every unit, so that as many warps are resident as the
-// per-item row kernels have.
-template <class T>
-__global__ void __launch_bounds__(256) k_batch_rows(const BatchItem* __restrict__ items,
-                                                    const int64_t* __restrict__ unit0, int nitems, int64_t nunits) {
-  const int lane = threadIdx.x & 31;
-  const int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (u >= nunits) return;
-  const BatchItem* itp = items + batch_find(unit0, nitems, u);
-  rows_unit<T>(itp, u - itp->unit0, lane);
 }
 
 template <class T>
@@ -1414,7 +1418,7 @@ struct BatchLaunch {
   std::vector<Part> parts;  // one per field type present
 };
 
-BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled) {
+BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled, bool all) {
   handled.assign((size_t)n, 0);
   std::vector<BatchItem> bi[2], ri[2];  // merge-path items, row items
   std::vector<FinishItem> fi[2];
@@ -1457,7 +1461,15 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
     b.x = it.src;
     b.y = it.dst;
     const int64_t passes = (nf + 127) / 128;
-    if (spmm_path() == SpmmPath::kAuto && cell_major && nf >= 32 && span32) {
+    const bool merge_path = spmm_path() == SpmmPath::kAuto && cell_major && nf >= 32 && span32;
+    // Measured on 32 uneven pairs: the persistent launch runs a small matrix's
+    // many 128-field passes side by side (3x its own launch), but a large
+    // matrix or a row-kernel item runs 10-25% (2-3x) faster in its own tuned
+    // launch on a graph branch.
+    const int64_t resident = (int64_t)num_sms() * 8 *
+                             (d ? CmGather<__nv_bfloat16>::kBatchMinBlocks : CmGather<float>::kBatchMinBlocks);
+    if (!all && !(merge_path && passes >= 2 && c.ntasks < resident)) continue;
+    if (merge_path) {
       // the merge path, as launch_cm_nnz runs it
       b.kind = 0;
       b.gaps = c.nextrow != nullptr;
@@ -1583,25 +1595,19 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
   return L;
 }
 
-void batch_enqueue(const BatchLaunch* L, cudaStream_t st, cudaStream_t rows_st) {
+void batch_enqueue(const BatchLaunch* L, cudaStream_t st) {
   const int64_t max_warps = (int64_t)num_sms() * 24;  // three blocks of 8 warps per SM
   for (const auto& p : L->parts) {
-    if (p.nrunits) {
+    if (p.nunits + p.nrunits) {
+      const int minb =
+          p.dtype == CRG_F32 ? CmGather<float>::kBatchMinBlocks : CmGather<__nv_bfloat16>::kBatchMinBlocks;
+      const int64_t warps = std::min<int64_t>(p.nunits + p.nrunits, (int64_t)num_sms() * 8 * minb);
       if (p.dtype == CRG_F32)
-        k_batch_rows<float><<<nblk(p.nrunits * 32, 256), 256, 0, rows_st>>>(p.ritems, p.runit0, p.nritems,
-                                                                             p.nrunits);
+        k_batch_apply<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits, p.ritems,
+                                                                    p.runit0, p.nritems, p.nrunits);
       else
-        k_batch_rows<__nv_bfloat16><<<nblk(p.nrunits * 32, 256), 256, 0, rows_st>>>(p.ritems, p.runit0, p.nritems,
-                                                                                     p.nrunits);
-      CRG_CHECK_CUDA(cudaGetLastError());
-    }
-    if (p.nunits) {
-      const int minb = p.dtype == CRG_F32 ? CmGather<float>::kMinBlocks : CmGather<__nv_bfloat16>::kMinBlocks;
-      const int64_t warps = std::min<int64_t>(p.nunits, (int64_t)num_sms() * 8 * minb);
-      if (p.dtype == CRG_F32)
-        k_batch_apply<float><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits);
-      else
-        k_batch_apply<__nv_bfloat16><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits);
+        k_batch_apply<__nv_bfloat16><<<nblk(warps * 32, 256), 256, 0, st>>>(p.items, p.unit0, p.nitems, p.nunits,
+                                                                            p.ritems, p.runit0, p.nritems, p.nrunits);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     if (p.nfunits) {
@@ -1618,7 +1624,7 @@ void batch_enqueue(const BatchLaunch* L, cudaStream_t st, cudaStream_t rows_st) 
 
 int batch_launches(const BatchLaunch* L) {
   int n = 0;
-  for (const auto& p : L->parts) n += (p.nunits > 0) + (p.nrunits > 0) + (p.nfunits > 0);
+  for (const auto& p : L->parts) n += (p.nunits + p.nrunits > 0) + (p.nfunits > 0);
   return n;
 }
 

@@ -241,18 +241,19 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
     CRG_REQUIRE(it.dst && is_device_pointer(it.dst) && (!it.src || is_device_pointer(it.src)), CRG_ERR_NOT_SUPPORTED,
                 "item %lld: a plan replays on the GPU alone, so fields must be device pointers", (long long)k);
   }
-  // The items of cell-major FP32 / BF16 fields (or single fields) run as one
-  // persistent launch over all their work units (plus one launch for the rows
-  // cut between tasks and the empty rows); the others keep their own applies.
-  // CRG_PLAN_BATCH=0 captures every item as its own apply (for comparison).
+  // Items whose own apply cannot fill the GPU run as one persistent launch over
+  // all their work units (plus one launch for the rows cut between tasks and
+  // the empty rows); the others keep their own, autotuned applies as graph
+  // branches beside it.  CRG_PLAN_BATCH=0 captures every item as its own apply,
+  // CRG_PLAN_BATCH=all puts every item the persistent launch can run into it.
   std::vector<char> handled((size_t)n, 0);
   BatchLaunch* batch = nullptr;
   const char* pb = getenv("CRG_PLAN_BATCH");
-  if (!(pb && strcmp(pb, "0") == 0)) batch = batch_prepare(n, items, handled);
+  if (!(pb && strcmp(pb, "0") == 0)) batch = batch_prepare(n, items, handled, pb && strcmp(pb, "all") == 0);
   // Capture: the origin stream forks one branch per remaining item (their
   // outputs are distinct), so the graph runs small items side by side.
-  std::vector<cudaStream_t> sts(n + 2, nullptr);  // [n + 1]: the batch's row items
-  std::vector<cudaEvent_t> evs(n + 2, nullptr);
+  std::vector<cudaStream_t> sts(n + 1, nullptr);  // [n]: the origin (and the batch's launches)
+  std::vector<cudaEvent_t> evs(n + 1, nullptr);
   auto cleanup = [&]() {
     for (auto e : evs)
       if (e) cudaEventDestroy(e);
@@ -261,7 +262,7 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
   };
   cudaGraph_t graph = nullptr;
   try {
-    for (int64_t k = 0; k <= n + 1; ++k) {
+    for (int64_t k = 0; k <= n; ++k) {
       if (k < n && handled[k]) continue;
       CRG_CHECK_CUDA(cudaStreamCreateWithFlags(&sts[k], cudaStreamNonBlocking));
       CRG_CHECK_CUDA(cudaEventCreateWithFlags(&evs[k], cudaEventDisableTiming));
@@ -279,14 +280,7 @@ crg_apply_plan* apply_plan_impl(int64_t n, const crg_apply_item* items) {
                    sts[k]);
         CRG_CHECK_CUDA(cudaEventRecord(evs[k], sts[k]));
       }
-      if (batch) {
-        // the merge-path items on the origin, the row items on their own
-        // branch, both beside the items of their own applies
-        CRG_CHECK_CUDA(cudaStreamWaitEvent(sts[n + 1], evs[n], 0));
-        batch_enqueue(batch, origin, sts[n + 1]);
-        CRG_CHECK_CUDA(cudaEventRecord(evs[n + 1], sts[n + 1]));
-        CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[n + 1], 0));
-      }
+      if (batch) batch_enqueue(batch, origin);  // beside the items of their own applies
       for (int64_t k = 0; k < n; ++k)  // join the branches
         if (!handled[k]) CRG_CHECK_CUDA(cudaStreamWaitEvent(origin, evs[k], 0));
     } catch (...) {

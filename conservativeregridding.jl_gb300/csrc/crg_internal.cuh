@@ -179,12 +179,15 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
 // The applies of a batch that one persistent launch can run (cell-major FP32 /
 // BF16 fields or single fields, device memory): their device tables, built
 // once; handled[k] = 1 for the items it covers (the others need their own
-// crg_apply).  batch_enqueue queues its launches: the row items' on rows_st,
-// the merge-path items' and their fixup on st (the two sets write different
-// items, so the streams may run side by side).
+// crg_apply).  batch_enqueue queues its launches on st: one persistent launch
+// over the merge-path and row units of every item, then one for cut rows and
+// empty rows.
 struct BatchLaunch;
-BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled);
-void batch_enqueue(const BatchLaunch* L, cudaStream_t st, cudaStream_t rows_st);
+// all = false: only the merge-path items of several 128-field passes and fewer
+// tasks than the GPU holds warps (whose own launches run the passes one after
+// another, latency-bound); all = true: every item the launch can run.
+BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<char>& handled, bool all);
+void batch_enqueue(const BatchLaunch* L, cudaStream_t st);
 int batch_launches(const BatchLaunch* L);
 void batch_free(BatchLaunch* L);
 // The autotuner's table of choices (crg_tune.cu): the fastest candidate of a

@@ -187,12 +187,16 @@ crg_status crg_apply_plan_launch(crg_apply_plan* plan, void* stream);
 crg_status crg_apply_plan_destroy(crg_apply_plan* plan);
 /* How a plan runs (no reference counterpart): the kernel launches of one
  * replay, and how many of its items the persistent batch launch covers.  The
- * items of cell-major FP32 / BF16 fields (or single fields) run as one launch
- * over all their work units -- merge-path tasks of the items with 32 fields
- * or more in 16-byte aligned rows, groups of rows of the others -- plus one
- * launch that sums the rows cut between tasks and zeroes empty rows; each
- * item's result has the bits of its own crg_apply.  The other items (FP64,
- * field-major) are captured as their own applies.  Either pointer may be NULL. */
+ * items whose own apply cannot fill the GPU -- cell-major FP32 / BF16 fields
+ * of more than 128 fields on a matrix with fewer merge-path tasks than the GPU
+ * holds resident warps -- run as one launch over all their (task, 128-field
+ * pass) units, plus one launch that sums the rows cut between tasks and zeroes
+ * empty rows; the others are captured as their own, autotuned applies on graph
+ * branches beside it.  With the environment variable CRG_PLAN_BATCH=all every
+ * cell-major FP32 / BF16 or single-field item joins the persistent launch
+ * (groups of rows for the items below 32 fields), with CRG_PLAN_BATCH=0 none
+ * does.  Each item's result has the bits of its own crg_apply either way.
+ * Either pointer may be NULL. */
 crg_status crg_apply_plan_info(const crg_apply_plan* plan, int64_t* kernels, int64_t* batched_items);
 
 /* Derivatives of the areas with respect to the destination grid's vertices.

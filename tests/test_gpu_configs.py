@@ -84,7 +84,7 @@ def test_derivatives_build_parity(cuda):
     assert_parity(Regridder(dst, src, normalize=True), oracle.OracleRegridder(dst, src, normalize=True))
 
 
-def test_batch_pairs_parity_and_plan(cuda):
+def test_batch_pairs_parity_and_plan(cuda, monkeypatch):
     import torch
 
     pairs, ks = workloads.batch_pairs()
@@ -98,12 +98,24 @@ def test_batch_pairs_parity_and_plan(cuda):
         y = torch.full((nd, K), float("nan"), device=dev)
         items.append((y, R, x, 1))
         xs.append(x)
+    # default: the small matrices with more than 128 fields in the persistent
+    # launch, every other pair its own tuned apply on a graph branch
     plan = ApplyPlan(items)
+    assert plan.info["batched_items"] == sum(K > 128 for K in ks), plan.info
     # every pair in the one persistent launch: at most 3 kernels per replay
-    assert plan.info["batched_items"] == len(items) and plan.info["kernels"] <= 3, plan.info
+    monkeypatch.setenv("CRG_PLAN_BATCH", "all")
+    plan_all = ApplyPlan(items)
+    monkeypatch.delenv("CRG_PLAN_BATCH")
+    assert plan_all.info["batched_items"] == len(items) and plan_all.info["kernels"] <= 3, plan_all.info
     plan.launch()
     torch.cuda.synchronize()
-    for (dst, src), R, K, (y, _, x, _) in zip(pairs, Rs, ks, items):
+    got = [y.clone() for y, _, _, _ in items]
+    for y, _, _, _ in items:
+        y.fill_(float("nan"))
+    plan_all.launch()
+    torch.cuda.synchronize()
+    for (dst, src), R, K, g, (y, _, x, _) in zip(pairs, Rs, ks, got, items):
+        assert torch.equal(g, y), f"pair {R.shape} K={K}: the two plans differ"
         O = oracle.OracleRegridder(dst, src, normalize=True)
         assert_parity(R, O)
         ref = O.apply(x.T.double().cpu().numpy())
