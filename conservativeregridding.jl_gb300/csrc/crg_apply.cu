@@ -431,13 +431,13 @@ int num_sms() {
 // k_cm_fixup.
 //
 // The gathers in flight hold the raw loads (16 bytes of 4 FP32 fields, 8 bytes
-// of 4 BF16 fields), converted to FP32 when consumed.  kInFlight is the
-// default count; the autotuner's candidates (CmVariant) set others.
+// of 4 BF16 fields), converted to FP32 when consumed.  kInFlight is the count
+// of the persistent batch launch (k_batch_apply, at kBatchMinBlocks blocks per
+// SM); the autotuner's candidates (CmVariant) set those of k_cm_nnz.
 template <class T> struct CmGather;
 template <> struct CmGather<float> {
   using Raw = float4;
   static constexpr int kInFlight = 4;
-  static constexpr int kMinBlocks = 4;
   // (offset, weight) pairs by two shuffles per entry (latency-bound: the
   // shared-memory staging measured 0.402 against 0.396 ms per step)
   static constexpr bool kStage = false;
@@ -453,7 +453,6 @@ template <> struct CmGather<float> {
 template <> struct CmGather<__nv_bfloat16> {
   using Raw = uint2;
   static constexpr int kInFlight = 8;
-  static constexpr int kMinBlocks = 3;
   // (offset, weight) pairs by one broadcast shared load per entry: the BF16
   // kernel is closer to its issue limit (0.320 against 0.333 ms per step)
   static constexpr bool kStage = true;
