@@ -85,11 +85,32 @@ __global__ void k_spmv_f64(const int32_t* __restrict__ ptr, const int32_t* __res
   const int64_t f = f0 + blockIdx.y;
   const double* xf = x + f * xsf;
   double acc = 0.0;
-  for (int32_t k = ptr[r]; k < ptr[r + 1]; ++k) {
-    int32_t j = idx[k];
-    double xv = xf[(int64_t)j * xsc];
-    if (col_div) xv = xv / col_div[j];
-    acc = acc + val[k] * xv;
+  int32_t k = __ldg(ptr + r);
+  const int32_t k1 = __ldg(ptr + r + 1);
+  // four entries' loads issued before their (ordered) sums: the row's gathers
+  // overlap instead of waiting one after another
+  for (; k + 4 <= k1; k += 4) {
+    int32_t j[4];
+    double v[4], xv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      j[q] = __ldg(idx + k + q);
+      v[q] = __ldg(val + k + q);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) xv[q] = xf[(int64_t)j[q] * xsc];
+    if (col_div) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) xv[q] = xv[q] / __ldg(col_div + j[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc = acc + v[q] * xv[q];
+  }
+  for (; k < k1; ++k) {
+    const int32_t jj = __ldg(idx + k);
+    double xx = xf[(int64_t)jj * xsc];
+    if (col_div) xx = xx / __ldg(col_div + jj);
+    acc = acc + __ldg(val + k) * xx;
   }
   if (row_div) acc = acc / row_div[r];
   y[r * ysc + f * ysf] = acc;
