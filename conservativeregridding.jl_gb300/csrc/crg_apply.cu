@@ -35,6 +35,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "crg_div.cuh"
 #include "crg_internal.cuh"
 
 namespace crg {
@@ -129,7 +130,8 @@ template <int G, bool kVec>
 __global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                                                      const double* __restrict__ val, int64_t nrows,
                                                      const double* __restrict__ x, int64_t xs, double* __restrict__ y,
-                                                     int64_t ys, int64_t nf, const double* __restrict__ row_div) {
+                                                     int64_t ys, int64_t nf, const double* __restrict__ row_div,
+                                                     const double* __restrict__ row_rcp) {
   const int lane = threadIdx.x & 31;
   const int g = lane % G;
   const int gbase = lane - g;
@@ -138,6 +140,7 @@ __global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__
   if (r >= nrows) return;  // the whole lane group shares r
   const int32_t k0 = __ldg(ptr + r), n = __ldg(ptr + r + 1) - k0;
   const double div = row_div ? __ldg(row_div + r) : 1.0;
+  const double rcp = row_div ? __ldg(row_rcp + r) : 1.0;  // RN(1 / div): the quotients correct from it
   for (int64_t f0 = 0; f0 < nf; f0 += (int64_t)G * 4) {
     const int64_t f = f0 + (int64_t)g * 4;
     const bool on = f < nf;
@@ -171,7 +174,7 @@ __global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__
     double* yp = y + r * ys + f;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      const double o = row_div ? __ddiv_rn(acc[q], div) : acc[q];
+      const double o = row_div ? div_rn_by(acc[q], div, rcp) : acc[q];
       if (full || f + q < nf) yp[q] = o;
     }
   }
@@ -1006,8 +1009,8 @@ void launch_transpose(const T* in, int64_t ldi, T* out, int64_t ldo, int64_t row
 // Cell-major FP64 fields (more than one): k_cm_rows_f64, G lanes per row.
 // With the adjoint's column division, the input is divided once per element
 // into a temporary first.
-void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const double* x, int64_t xs, double* y,
-                   int64_t ys, int64_t nf, cudaStream_t st) {
+void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const double* div_inv, const double* x,
+                   int64_t xs, double* y, int64_t ys, int64_t nf, cudaStream_t st) {
   const int64_t n = c.nrows;
   if (n == 0 || nf == 0) return;
   const double* xin = x;
@@ -1023,6 +1026,7 @@ void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const doubl
     xin_s = nf;
   }
   const double* rdiv = adjoint ? nullptr : div;
+  const double* rinv = adjoint ? nullptr : div_inv;
   const bool vec = nf % 4 == 0 && xin_s % 2 == 0 && ys % 2 == 0 && (uintptr_t)xin % 16 == 0 && (uintptr_t)y % 16 == 0;
   const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
   int G = 1;
@@ -1030,8 +1034,10 @@ void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const doubl
   const unsigned blocks = nblk(n * G, 256);
 #define CRG_F64_CASE(GG)                                                                                        \
   case GG:                                                                                                      \
-    if (vec) k_cm_rows_f64<GG, true><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv); \
-    else k_cm_rows_f64<GG, false><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv);   \
+    if (vec)                                                                                                    \
+      k_cm_rows_f64<GG, true><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv, rinv); \
+    else                                                                                                        \
+      k_cm_rows_f64<GG, false><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv, rinv); \
     break;
   switch (G) {
     CRG_F64_CASE(1)
@@ -1722,6 +1728,7 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   // direction: which copy of A is read, and which area vector divides
   const DevCsr& c = adjoint ? (t ? r->fwd : r->rev) : (t ? r->rev : r->fwd);
   const double* div = normalize ? (t ? r->src_area : r->dst_area) : nullptr;
+  const double* div_inv = normalize ? (t ? r->src_area_inv : r->dst_area_inv) : nullptr;
   const int64_t nin = c.ncols, nout = c.nrows;
   if (nf == 0 || nout == 0) return;
   CRG_REQUIRE(dst != nullptr && (src != nullptr || nin == 0), CRG_ERR_INVALID_ARGUMENT, "field pointer is NULL");
@@ -1745,7 +1752,7 @@ void apply_impl(const crg_regridder* rc, int transpose, int dtype, bool adjoint,
   auto compute = [&](const void* x, int64_t xsc, int64_t xsf, void* y, int64_t ysc, int64_t ysf, int64_t n,
                      cudaStream_t s) {
     if (dtype == CRG_F64 && xsf == 1 && ysf == 1 && n > 1 && spmm_path() == SpmmPath::kAuto) {
-      launch_cm_f64(c, adjoint, div, (const double*)x, xsc, (double*)y, ysc, n, s);
+      launch_cm_f64(c, adjoint, div, div_inv, (const double*)x, xsc, (double*)y, ysc, n, s);
     } else if (dtype == CRG_F64) {
       const double* cdiv = adjoint ? div : nullptr;
       const double* rdiv = adjoint ? nullptr : div;

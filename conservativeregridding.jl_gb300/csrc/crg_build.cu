@@ -1448,6 +1448,8 @@ void free_regridder(crg_regridder* r) {
   free_csr(r->rev);
   cudaFree(r->dst_area);
   cudaFree(r->src_area);
+  cudaFree(r->dst_area_inv);
+  cudaFree(r->src_area_inv);
   cudaFree(r->row_sum);
   cudaFree(r->col_sum);
   for (int d = 0; d < 2; ++d) {
@@ -1557,14 +1559,17 @@ void finish_build(crg_regridder* R, cudaStream_t st) {
   DBuf<int32_t> dcounts(6, st);
   build_merge_path(R->fwd, dcounts.p, st);  // also the row of every entry
   build_merge_path(R->rev, dcounts.p + 3, st);
+  // the reciprocals of the final areas, kept for the FP64 apply's quotients
+  R->dst_area_inv = keep_alloc<double>((size_t)nd, st);
+  R->src_area_inv = keep_alloc<double>((size_t)ns, st);
+  if (nd) k_recip<<<nblk(nd, 256), 256, 0, st>>>(R->dst_area, nd, R->dst_area_inv);
+  if (ns) k_recip<<<nblk(ns, 256), 256, 0, st>>>(R->src_area, ns, R->src_area_inv);
+  CRG_CHECK_CUDA(cudaGetLastError());
   if (nnz) {
-    DBuf<double> inv_d((size_t)nd, st), inv_s((size_t)ns, st);
-    k_recip<<<nblk(nd, 256), 256, 0, st>>>(R->dst_area, nd, inv_d.p);
-    k_recip<<<nblk(ns, 256), 256, 0, st>>>(R->src_area, ns, inv_s.p);
-    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.erow, R->fwd.idx, R->fwd.val, nnz, inv_d.p, inv_s.p,
-                                             R->fwd.val32, R->fwd.wn32, R->fwd.adj32);
-    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.erow, R->rev.idx, R->rev.val, nnz, inv_s.p, inv_d.p,
-                                             R->rev.val32, R->rev.wn32, R->rev.adj32);
+    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->fwd.erow, R->fwd.idx, R->fwd.val, nnz, R->dst_area_inv,
+                                             R->src_area_inv, R->fwd.val32, R->fwd.wn32, R->fwd.adj32);
+    k_derive<<<nblk(nnz, 256), 256, 0, st>>>(R->rev.erow, R->rev.idx, R->rev.val, nnz, R->src_area_inv,
+                                             R->dst_area_inv, R->rev.val32, R->rev.wn32, R->rev.adj32);
     CRG_CHECK_CUDA(cudaGetLastError());
   }
   int32_t hc[6];

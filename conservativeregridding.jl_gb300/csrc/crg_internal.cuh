@@ -127,6 +127,10 @@ struct crg_regridder {
   crg::DevCsr rev;  // CSR of A^T (rows = src)
   double* dst_area = nullptr;   // [nd]
   double* src_area = nullptr;   // [ns]
+  // RN(1 / area) per cell, of the final (normalised) areas: the FP64 apply of
+  // several fields corrects its quotients from these
+  double* dst_area_inv = nullptr;  // [nd]
+  double* src_area_inv = nullptr;  // [ns]
   // [nd] / [ns] Kahan row / column sums of A, computed on first request
   // (ensure_row_col_sums) under sums_mu
   double* row_sum = nullptr;

@@ -1,6 +1,8 @@
-// Test helper: the clip's exact-sign predicates evaluated on the GPU for a
-// batch of point triples, so that tests can compare them with rational
-// arithmetic.  Built by tests/test_gpu_predicates.py into a temporary folder.
+// Test helper: the clip's exact-sign predicates and the FP64 apply's
+// corrected quotients evaluated on the GPU for batches of inputs, so that
+// tests can compare them with rational arithmetic and with IEEE division.
+// Built by tests/test_gpu_predicates.py into a temporary folder.
+#include "crg_div.cuh"
 #include "crg_geom.cuh"
 
 namespace {
@@ -12,6 +14,13 @@ __global__ void k_det3(const double* p, int n, int* out) {
   out[3 * i] = crg::det3_sign_adapt(a, b, c);
   out[3 * i + 1] = crg::det3_sign_dd(a, b, c);
   out[3 * i + 2] = crg::det3_sign(a, b, c);
+}
+
+__global__ void k_div(const double* a, const double* d, int n, double* fast, double* ieee) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  fast[i] = crg::div_rn_by(a[i], d[i], __drcp_rn(d[i]));
+  ieee[i] = __ddiv_rn(a[i], d[i]);
 }
 }  // namespace
 
@@ -31,5 +40,23 @@ extern "C" int crg_test_det3(const double* abc, int n, int* out) {
   if (e == cudaSuccess) e = cudaMemcpy(out, o, sizeof(int) * 3 * (size_t)n, cudaMemcpyDeviceToHost);
   cudaFree(d);
   cudaFree(o);
+  return (int)e;
+}
+
+// a, d: n dividends and divisors in host memory.  fast: div_rn_by(a, d, RN(1/d));
+// ieee: the IEEE quotient.  Returns a cudaError_t.
+extern "C" int crg_test_div(const double* a, const double* d, int n, double* fast, double* ieee) {
+  double* buf = nullptr;
+  const size_t b = sizeof(double) * (size_t)n;
+  cudaError_t e = cudaMalloc(&buf, 4 * b + 16);
+  if (e == cudaSuccess) e = cudaMemcpy(buf, a, b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(buf + n, d, b, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n > 0) {
+    k_div<<<(n + 127) / 128, 128>>>(buf, buf + n, n, buf + 2 * (size_t)n, buf + 3 * (size_t)n);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(fast, buf + 2 * (size_t)n, b, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(ieee, buf + 3 * (size_t)n, b, cudaMemcpyDeviceToHost);
+  cudaFree(buf);
   return (int)e;
 }

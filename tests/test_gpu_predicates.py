@@ -10,7 +10,14 @@ Cases: points on a great circle up to the rounding of their coordinates
 (meridians and parallels built from cos/sin, near-coplanar combinations one ulp
 off), exactly coplanar points, and lattice vectors whose determinant is +-1 ulp^2
 of terms near 1 (continued-fraction convergents), where only the expansion can
-decide.  The helper library is compiled from tests/gpu_predicates.cu."""
+decide.
+
+The FP64 apply of several fields divides each output element by its row's area
+with a reciprocal taken once per row and Markstein's correction, checked and
+otherwise replaced by the IEEE division: every quotient must have the IEEE
+bits, on random operands, near-midpoint quotients, divisors whose significand
+is all ones, powers of two, zeros, subnormal and overflowing quotients.
+The helper library is compiled from tests/gpu_predicates.cu."""
 from __future__ import annotations
 
 import ctypes
@@ -28,13 +35,21 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
-def det3(cuda, tmp_path_factory):
+def helpers(cuda, tmp_path_factory):
     out = tmp_path_factory.mktemp("pred") / "libcrg_test_pred.so"
     subprocess.run([_build._nvcc(), *_build.NVCC_FLAGS, *_build.ARCH_FLAGS, f"-I{_build.CSRC}", "-shared",
                     "-o", str(out), str(ROOT / "tests" / "gpu_predicates.cu")], check=True, capture_output=True)
     lib = ctypes.CDLL(str(out))
     lib.crg_test_det3.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     lib.crg_test_det3.restype = ctypes.c_int
+    lib.crg_test_div.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.crg_test_div.restype = ctypes.c_int
+    return lib
+
+
+@pytest.fixture(scope="module")
+def det3(helpers):
+    lib = helpers
 
     def run(triples):
         t = np.ascontiguousarray(np.asarray(triples, dtype=np.float64).reshape(-1, 9))
@@ -116,3 +131,37 @@ def test_det3_sign_exact_on_gpu(det3):
     eq = np.array([np.array_equal(q[0:3], q[6:9]) or np.array_equal(q[3:6], q[6:9]) or np.array_equal(q[0:3], q[3:6])
                    for q in cases])
     assert eq.sum() >= 400 and not want[eq].any()
+
+
+def _div_cases():
+    rng = np.random.default_rng(21)
+    a = list(rng.standard_normal(20000) * 10.0 ** rng.integers(-30, 30, 20000))
+    d = list(np.abs(rng.standard_normal(20000)) * 10.0 ** rng.integers(-12, 3, 20000))
+    # quotients within two ulps either side of k / d for small integers k
+    for _ in range(20000):
+        dd = float(rng.uniform(0.5, 2.0)) * 2.0 ** int(rng.integers(-40, 5))
+        aa = float(rng.integers(1, 1 << 20)) * dd
+        for step in (-2, -1, 0, 1, 2):
+            x = aa
+            for _ in range(abs(step)):
+                x = np.nextafter(x, np.inf if step > 0 else -np.inf)
+            a.append(float(x))
+            d.append(dd)
+    ones = np.nextafter(2.0, 0.0)  # significand all ones
+    for e in range(-60, 60, 7):
+        for x in rng.standard_normal(200):
+            a += [float(x), float(x) * 2.0 ** e, 2.0 ** e, -(2.0 ** e)]
+            d += [float(ones * 2.0 ** (e // 2))] * 2 + [3.0, float(ones)]
+    a += [0.0, -0.0, 1e-310, -1e-320, 1e300, 1e-300, 1.0, np.nextafter(1.0, 2.0)]
+    d += [3.0, 3.0, 7.0, 3.0, 1e-10, 1e10, 1.0, 1.0]
+    return np.array(a), np.array(d)
+
+
+def test_corrected_quotient_is_ieee(helpers):
+    a, d = _div_cases()
+    fast, ieee = np.empty_like(a), np.empty_like(a)
+    assert helpers.crg_test_div(a.ctypes.data, d.ctypes.data, len(a), fast.ctypes.data, ieee.ctypes.data) == 0
+    with np.errstate(all="ignore"):
+        host = a / d
+    assert np.array_equal(ieee.view(np.uint64), host.view(np.uint64))
+    assert np.array_equal(fast.view(np.uint64), ieee.view(np.uint64))
