@@ -138,11 +138,9 @@ class Regridder:
         check(lib.crg_regridder_info(C.c_void_p(ptr), C.byref(info)))
         self.info = {k: (list(getattr(info, k)) if k in _PAIR_FIELDS else getattr(info, k))
                      for k, _ in _lib.crg_info._fields_ if k != "pad"}
-        nd, ns = info.n_dst, info.n_src
-        self.dst_temp = np.zeros(nd)
-        self.src_temp = np.zeros(ns)
         self._csc = [None]  # shared caches with transposed views
         self._areas = [None]
+        self._temps = [None]
 
     # -- R.dst_areas / R.src_areas (copied from the device on first use) --
     def _area_pair(self):
@@ -153,6 +151,22 @@ class Regridder:
             check(lib.crg_get_areas(C.c_void_p(self._h.ptr), d.ctypes.data, s.ctypes.data))
             self._areas[0] = (d, s)
         return self._areas[0]
+
+    # -- R.dst_temp / R.src_temp: the reference struct's work vectors, made on
+    # first use (two host vectors of the grids' sizes; zeroing them on every
+    # build cost more than a millisecond for a million cells) --
+    def _temp_pair(self):
+        if self._temps[0] is None:
+            self._temps[0] = (np.zeros(self.info["n_dst"]), np.zeros(self.info["n_src"]))
+        return self._temps[0]
+
+    @property
+    def dst_temp(self) -> np.ndarray:
+        return self._temp_pair()[1 if self._transposed else 0]
+
+    @property
+    def src_temp(self) -> np.ndarray:
+        return self._temp_pair()[0 if self._transposed else 1]
 
     @property
     def dst_areas(self) -> np.ndarray:
@@ -184,7 +198,6 @@ class Regridder:
         view = dict(self.__dict__)
         view["_h"] = _Handle(self._h.ptr)
         view["_transposed"] = not self._transposed
-        view["dst_temp"], view["src_temp"] = self.src_temp, self.dst_temp
         view["dst_space"], view["src_space"] = self.src_space, self.dst_space
         return Regridder(None, None, _view=view)
 

@@ -59,8 +59,8 @@ def test_flat_field_stride():
 
 def _fake_regridder(nd, ns):
     return Regridder(None, None, _view=dict(_h=None, _transposed=False, info={"n_dst": nd, "n_src": ns, "nnz": 0},
-                                            _areas=[(np.ones(nd), np.ones(ns))], dst_temp=np.zeros(nd),
-                                            src_temp=np.zeros(ns), _csc=[None], dst_space=None, src_space=None))
+                                            _areas=[(np.ones(nd), np.ones(ns))], _temps=[None], _csc=[None],
+                                            dst_space=None, src_space=None))
 
 
 def test_regrid_argument_errors():
@@ -82,8 +82,7 @@ def test_transpose_view_swaps_areas_and_temps():
     R._h = type("H", (), {"ptr": 0})()
     # transpose() retains through the library; emulate the view bookkeeping only
     view = dict(R.__dict__)
-    view["_transposed"] = True  # the area properties swap with the flag
-    view["dst_temp"], view["src_temp"] = R.src_temp, R.dst_temp
+    view["_transposed"] = True  # the area and work-vector properties swap with the flag
     T = Regridder(None, None, _view=view)
     assert T.shape == (4, 9)
     assert T.src_areas is R.dst_areas and T.dst_areas is R.src_areas
