@@ -79,12 +79,13 @@ def parse():
     p.add_argument("--pair", default="c5", choices=["c5", "identity"],
                    help="profile grids: the workload, or the 0.25-degree lon-lat grid onto itself (a diagonal "
                         "matrix, i.e. a permuted copy, to calibrate the SpMM against plain bandwidth)")
-    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1", "c4", "se"],
+    p.add_argument("--workload", default="c5", choices=["c5", "c3", "c1", "c4", "se", "fields"],
                    help="c5: the headline (HEALPix 256 <-> 0.25 degree, 128 fields); c3: 32 jittered lon-lat "
                         "pairs of uneven resolution built as one batch and applied as one CUDA graph; c1: the "
                         "small FP64 case (2 degree -> shifted 3 degree lon-lat), build and plain FP64 apply; c4: the "
                         "differentiation case (jittered C96 <- 1 degree): adjoint apply and vertex gradients; se: "
-                        "spectral-element C48 (nq 4) <-> 0.5 degree lon-lat, both builds, the oracle's beside them")
+                        "spectral-element C48 (nq 4) <-> 0.5 degree lon-lat, both builds, the oracle's beside them; "
+                        "fields: the headline matrix applied to 1 .. 512 cell-major fields of FP32, BF16 and FP64")
     return p.parse_args()
 
 
@@ -760,6 +761,55 @@ def run_c3(a):
     }
 
 
+def run_fields(a):
+    """The headline matrix (HEALPix 256 <-> 0.25 degree) applied forward and
+    transposed to K cell-major fields, K = 1 .. 512, FP32, BF16 and FP64: CUDA-
+    event time per step (both directions, inputs resident, larger than L2 from
+    K = 64 FP32) and the algorithmic bytes per second."""
+    import torch
+
+    from crg import Regridder, regrid_
+
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    hp, ll = grids_c5(a.nside, a.dlon)
+    R = Regridder(hp, ll, normalize=True)
+    T = R.transpose()
+    nnz, nd, ns = R.nnz, R.shape[0], R.shape[1]
+    peak, peak_source = hbm_peak()
+    gen = torch.Generator(device=dev).manual_seed(9)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    out = []
+    for dt, elem, wb in ((torch.float32, 4, 4), (torch.bfloat16, 2, 4), (torch.float64, 8, 8)):
+        for K in (1, 2, 4, 8, 16, 32, 64, 128, 256, 512):
+            if dt == torch.float64 and K > 128:
+                continue
+            shp = (lambda n: (n,)) if K == 1 else (lambda n: (n, K))
+            x = torch.randn(shp(ns), generator=gen, device=dev).to(dt)
+            z = torch.randn(shp(nd), generator=gen, device=dev).to(dt)
+            y, w = torch.empty(shp(nd), dtype=dt, device=dev), torch.empty(shp(ns), dtype=dt, device=dev)
+            for _ in range(3):
+                regrid_(y, R, x)
+                regrid_(w, T, z)
+            reps = 10
+            ev[0].record()
+            for _ in range(reps):
+                regrid_(y, R, x)
+                regrid_(w, T, z)
+            ev[1].record()
+            ev[1].synchronize()
+            ms = ev[0].elapsed_time(ev[1]) / reps
+            bf, br = step_bytes(nnz, nd, ns, K, elem=elem, wbytes=wb)
+            gbs = (bf + br) / (ms * 1e-3) / 1e9
+            out.append({"dtype": str(dt).replace("torch.", ""), "fields": K, "ms_per_step": round(ms, 4),
+                        "GB/s": round(gbs, 1), "frac_of_hbm": round(gbs / peak, 3)})
+            del x, z, y, w
+    return {"metric": "apply GB/s over field counts (forward + transpose, cell-major)",
+            "workload": WORKLOAD.split(",")[0] + ", K fields", "peak_GBs": peak, "peak_source": peak_source,
+            "bytes": "8 B per nonzero (FP32 weight and column; FP64: 12 B) + row pointers + K x elem x (rows + "
+                     "columns) per direction", "results": out}
+
+
 # ----------------------------------------------------------------- small FP64 workload
 
 def run_c1(a):
@@ -1028,9 +1078,10 @@ def main():
     if a.profile:
         run_profile(a)
         return
-    if a.workload in ("c3", "c1", "c4", "se"):
+    if a.workload in ("c3", "c1", "c4", "se", "fields"):
         if rank == 0:
-            print(json.dumps({"c3": run_c3, "c1": run_c1, "c4": run_c4, "se": run_se}[a.workload](a)))
+            print(json.dumps({"c3": run_c3, "c1": run_c1, "c4": run_c4, "se": run_se,
+                              "fields": run_fields}[a.workload](a)))
         return
     if a.impl == "reference":
         if rank == 0:

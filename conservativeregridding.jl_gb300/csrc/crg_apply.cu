@@ -826,6 +826,146 @@ void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y
   if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
 }
 
+// Merge-path tasks for cell-major fields, 2 to 31 per cell: G lanes
+// (4 fields each) per entry, 32 / G entries of the task at a time, so that a
+// warp gathers 32 / G source rows per load and a polar row of hundreds of
+// entries is spread over its tasks like any other.  Each lane group forms its
+// entry's products; a segmented inclusive scan over the groups (Kogge-Stone,
+// rows from erow) sums every row's run of entries inside the chunk; the group
+// holding a row's last entry of the chunk adds what earlier chunks carried and
+// writes the row -- to its carry slot when the row is cut between tasks
+// (k_cm_fixup sums those).  The chunk's last row stays open until the next
+// chunk shows whether it continues.  Order of the FP32 sums: a fixed scan tree
+// per chunk, the chunks in entry order: the same bits for a given matrix and
+// field count (the scan's width follows the lanes per entry), every time.
+template <class T, int G, bool kVec>
+__global__ void __launch_bounds__(256, 4)
+    k_cm_narrow(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
+                const int32_t* __restrict__ erow, const float* __restrict__ w, int64_t ntasks,
+                const T* __restrict__ x, int64_t xs, T* __restrict__ y, int64_t ys, int64_t nf,
+                float* __restrict__ carry) {
+  constexpr int E = 32 / G;
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31, i = lane / G, g = lane % G;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int f = 4 * g;  // the lane's first field
+  const int onm = (f < nf ? 1 : 0) | (f + 1 < nf ? 2 : 0) | (f + 2 < nf ? 4 : 0) | (f + 3 < nf ? 8 : 0);
+  for (int64_t task = gw; task < ntasks; task += nw) {
+    const int4 tr = __ldg(tasks + task);
+    const int32_t e0 = tr.x, e1 = tr.y;
+    if (e0 >= e1) continue;  // warp-uniform
+    const int32_t carry_first = tr.z < 0 ? (tr.z & 0x7fffffff) : -1;
+    const int32_t carry_last = tr.w < 0 ? (tr.w & 0x7fffffff) : -1;
+    const int2 slot = (tr.z | tr.w) < 0 ? __ldg(tslot + task) : make_int2(-1, -1);
+    auto write = [&](int32_t row, float4 v) {
+      if (!onm) return;
+      if (row == carry_first || row == carry_last) {
+        float* c = carry + (int64_t)(row == carry_first ? slot.x : slot.y) * 128 + f;
+        if (onm & 1) c[0] = v.x;
+        if (onm & 2) c[1] = v.y;
+        if (onm & 4) c[2] = v.z;
+        if (onm & 8) c[3] = v.w;
+      } else if (kVec) {
+        st4<T>(y + (int64_t)row * ys + f, v);
+      } else {
+        T* yp = y + (int64_t)row * ys + f;
+        if (onm & 1) st1<T>(yp, v.x);
+        if (onm & 2) st1<T>(yp + 1, v.y);
+        if (onm & 4) st1<T>(yp + 2, v.z);
+        if (onm & 8) st1<T>(yp + 3, v.w);
+      }
+    };
+    int32_t open_row = -1;  // the row the previous chunk ended in, not written yet
+    float4 open = make_float4(0.f, 0.f, 0.f, 0.f);
+    // a chunk's entry of this lane group: its row, source cell and weight
+    // (row -1 past the task's end), and the gathered fields
+    auto meta = [&](int32_t c, int32_t& row, int32_t& col, float& wt) {
+      const int32_t e = c + i;
+      const bool valid = e < e1;
+      row = valid ? __ldg(erow + e) : -1;
+      col = valid ? __ldg(idx + e) : 0;
+      wt = valid ? __ldg(w + e) : 0.f;
+    };
+    auto gather = [&](int32_t row, int32_t col) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row >= 0 && onm) {
+        const T* xp = x + (int64_t)col * xs + f;
+        if (kVec) {
+          v = ld4<T>(xp);
+        } else {
+          v.x = (onm & 1) ? ld1<T>(xp) : 0.f;
+          v.y = (onm & 2) ? ld1<T>(xp + 1) : 0.f;
+          v.z = (onm & 4) ? ld1<T>(xp + 2) : 0.f;
+          v.w = (onm & 8) ? ld1<T>(xp + 3) : 0.f;
+        }
+      }
+      return v;
+    };
+    // two chunks ahead: the next chunk's gather and the one after's indices
+    // are in flight while a chunk is summed
+    int32_t row_a, col_a, row_b, col_b;
+    float wt_a, wt_b;
+    meta(e0, row_a, col_a, wt_a);
+    float4 v_a = gather(row_a, col_a);
+    meta(e0 + E, row_b, col_b, wt_b);
+    for (int32_t c0 = e0; c0 < e1; c0 += E) {
+      const float4 v_b = gather(row_b, col_b);
+      int32_t row_c, col_c;
+      float wt_c;
+      meta(c0 + 2 * E, row_c, col_c, wt_c);
+      const int32_t row = row_a;
+      const bool valid = row >= 0;
+      float4 p = make_float4(wt_a * v_a.x, wt_a * v_a.y, wt_a * v_a.z, wt_a * v_a.w);
+      row_a = row_b;
+      col_a = col_b;
+      wt_a = wt_b;
+      v_a = v_b;
+      row_b = row_c;
+      col_b = col_c;
+      wt_b = wt_c;
+      const int32_t row0 = __shfl_sync(kFull, row, 0);
+      // the open row ended where this chunk begins: write it (group 0)
+      if (open_row >= 0 && row0 != open_row) {
+        if (i == 0) write(open_row, open);
+        open_row = -1;
+      }
+      const int32_t prow = __shfl_up_sync(kFull, row, G);
+      bool head = i == 0 || row != prow;
+#pragma unroll
+      for (int d = 1; d < E; d <<= 1) {
+        const float qx = __shfl_up_sync(kFull, p.x, d * G), qy = __shfl_up_sync(kFull, p.y, d * G);
+        const float qz = __shfl_up_sync(kFull, p.z, d * G), qw = __shfl_up_sync(kFull, p.w, d * G);
+        const bool qh = __shfl_up_sync(kFull, head ? 1 : 0, d * G) != 0;
+        if (i >= d && !head) {
+          p.x = qx + p.x;
+          p.y = qy + p.y;
+          p.z = qz + p.z;
+          p.w = qw + p.w;
+          head = qh;
+        }
+      }
+      // the run of entry i now holds its row's sum from the chunk start (or the row's first entry in it)
+      if (row == open_row) {  // continues the open row (implies row == row0)
+        p.x = open.x + p.x;
+        p.y = open.y + p.y;
+        p.z = open.z + p.z;
+        p.w = open.w + p.w;
+      }
+      const int32_t nrow = __shfl_down_sync(kFull, row, G);
+      const bool chunk_end = i == E - 1;
+      if (valid && !chunk_end && nrow != row) write(row, p);
+      // the chunk's last group: its row stays open (E entries were valid) or the task ends here
+      const int32_t lrow = __shfl_sync(kFull, row, (E - 1) * G + g);
+      const float4 lp = make_float4(__shfl_sync(kFull, p.x, (E - 1) * G + g), __shfl_sync(kFull, p.y, (E - 1) * G + g),
+                                    __shfl_sync(kFull, p.z, (E - 1) * G + g), __shfl_sync(kFull, p.w, (E - 1) * G + g));
+      open_row = lrow;  // -1 when the chunk was not full: its rows are all written
+      open = lp;
+    }
+    if (open_row >= 0 && i == 0) write(open_row, open);
+  }
+}
+
 // Rows without entries produce zero output (the row gather writes nothing for them).
 template <class T>
 __global__ void k_zero_empty_cm(const int32_t* __restrict__ ptr, int64_t n, T* __restrict__ y, int64_t ys, int64_t nf) {
@@ -879,6 +1019,48 @@ void cm_nnz_passes(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y
   }
 }
 
+// 2 to 31 cell-major fields: k_cm_narrow over
+// the merge-path tasks, then the cut rows' sums and the empty rows.  `carry`:
+// scratch of c.nslots * 128 floats, or NULL to take it from the stream's pool.
+template <class T>
+void launch_cm_narrow(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y, int64_t ys, int64_t nf,
+                      cudaStream_t st, bool vec, float* carry_given = nullptr) {
+  float* carry = carry_given;
+  if (!carry && c.nslots) CRG_CHECK_CUDA(cudaMallocAsync((void**)&carry, sizeof(float) * c.nslots * 128, st));
+  if (c.ntasks) {
+    const int64_t lanes = (nf + 3) / 4;
+    int G = 1;
+    while (G < lanes) G <<= 1;
+    const int64_t warps = std::min<int64_t>(c.ntasks, (int64_t)num_sms() * 8 * 4);
+    const unsigned blocks = nblk(warps * 32, 256);
+#define CRG_NARROW(GG)                                                                                          \
+  if (vec)                                                                                                      \
+    k_cm_narrow<T, GG, true><<<blocks, 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.erow, w, c.ntasks, x, xs, y, ys, nf, \
+                                                     carry);                                                    \
+  else                                                                                                          \
+    k_cm_narrow<T, GG, false><<<blocks, 256, 0, st>>>(c.tasks, c.tslot, c.idx, c.erow, w, c.ntasks, x, xs, y, ys,   \
+                                                      nf, carry);
+    switch (G) {
+      case 1: CRG_NARROW(1) break;
+      case 2: CRG_NARROW(2) break;
+      case 4: CRG_NARROW(4) break;
+      default: CRG_NARROW(8) break;
+    }
+#undef CRG_NARROW
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  if (c.nsplit) {
+    if (vec) k_cm_fixup<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, 0, nf);
+    else k_cm_fixup_s<T><<<nblk(c.nsplit * 32, 256), 256, 0, st>>>(c.split, c.nsplit, carry, y, ys, 0, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  if (c.nempty) {
+    k_zero_empty_cm<T><<<nblk(c.nrows, 256), 256, 0, st>>>(c.ptr, c.nrows, y, ys, nf);
+    CRG_CHECK_CUDA(cudaGetLastError());
+  }
+  if (!carry_given && carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
+}
+
 // Kernel choice for FP32/BF16 fields.  CRG_SPMM_PATH selects an alternative
 // for tuning and profiling: "rows" (the row kernels for every layout, no
 // merge-path, no transposes); unset = automatic.
@@ -890,6 +1072,15 @@ inline SpmmPath spmm_path() {
     return (e && strcmp(e, "rows") == 0) ? SpmmPath::kRows : SpmmPath::kAuto;
   }();
   return p;
+}
+
+// Whether launch_f32 applies these fields with k_cm_narrow: 2 to 31 fields
+// side by side (at 32 it measured the same as the merge path: 0.303 ms for the
+// HEALPix 256 <-> 0.25-degree step).  A single field keeps the row kernel's sequential row sums,
+// the same as each field of a field-major apply (whose host pipeline applies
+// its fields in chunks, down to one field at a time).
+bool narrow_path(SpmmPath path, bool cell_major, int64_t nf) {
+  return path == SpmmPath::kAuto && cell_major && nf < 32;
 }
 
 // k_cm_rows with RB rows per lane group; the autotuner picks RB (the
@@ -1094,6 +1285,11 @@ void launch_f32(const DevCsr& c, bool normalize, bool adjoint, const T* x, int64
     // merge-path over entries (4-field vectors when the rows allow, else each
     // lane's fields strided by 32); rows with no entries are zeroed separately
     launch_cm_nnz<T>(c, w, x, xsc, y, ysc, nf, st, vec4);
+    return;
+  }
+  if (narrow_path(path, cell_major, nf)) {
+    // fewer fields: the same tasks, several entries per warp load
+    launch_cm_narrow<T>(c, w, x, xsc, y, ysc, nf, st, vec4);
     return;
   }
   {
@@ -1487,6 +1683,9 @@ BatchLaunch* batch_prepare(int64_t n, const crg_apply_item* items, std::vector<c
     b.x = it.src;
     b.y = it.dst;
     const int64_t passes = (nf + 127) / 128;
+    // crg_apply runs fewer than 32 fields with k_cm_narrow, whose sums the row
+    // units would not reproduce: those items keep their own applies
+    if (narrow_path(spmm_path(), cell_major, nf)) continue;
     const bool merge_path = spmm_path() == SpmmPath::kAuto && cell_major && nf >= 32 && span32;
     // Measured on 32 uneven pairs: the persistent launch runs a small matrix's
     // many 128-field passes side by side (3x its own launch), but a large
@@ -2041,6 +2240,15 @@ void apply_noalloc_impl(const crg_regridder* r, int transpose, int dtype, const 
               "source fields span 4 GB or more");
   float* carry = noalloc_scratch(dev);
   const float* w = normalize ? c.wn32 : c.val32;
+  // the kernels crg_apply takes for these fields, with the static scratch
+  if (nf < 32) {
+    if (dtype == CRG_F32)
+      launch_cm_narrow<float>(c, w, (const float*)src, ssc, (float*)dst, dsc, nf, st, true, carry);
+    else
+      launch_cm_narrow<__nv_bfloat16>(c, w, (const __nv_bfloat16*)src, ssc, (__nv_bfloat16*)dst, dsc, nf, st, true,
+                                      carry);
+    return;
+  }
   if (dtype == CRG_F32)
     cm_nnz_passes<float>(c, w, (const float*)src, ssc, (float*)dst, dsc, nf, carry, st);
   else

@@ -165,8 +165,9 @@ def test_regrid_batch_host_pipeline(pairs, same_copy):
 @pytest.mark.parametrize("normalize", [True, False])
 def test_apply_plan_persistent_launch(pairs, normalize, monkeypatch):
     """With CRG_PLAN_BATCH=all, one persistent launch (plus one for cut and
-    empty rows per field type) runs every cell-major FP32 / BF16 item and every
-    single-field item: field
+    empty rows per field type) runs every single-field FP32 / BF16 item and
+    every cell-major one of 32 fields or more (2 to 31 fields keep their own
+    applies on the narrow merge-path kernel): field
     counts on both sides of the merge-path threshold (32), aligned or not
     (K % 4), R and transpose(R), a regridder with empty rows; FP64 and
     field-major items stay their own applies.  Bit for bit the single applies."""
@@ -191,7 +192,8 @@ def test_apply_plan_persistent_launch(pairs, normalize, monkeypatch):
         x = torch.randn(shape_in, generator=gen, device="cuda").to(dt)
         y = torch.full(shape_out, float("nan"), device="cuda").to(dt)
         items.append((y, RR, x, dims))
-        expect_batched += dt != torch.float64 and (dims == 1 or K == 1)
+        # 2 to 31 fields run k_cm_narrow in their own apply
+        expect_batched += dt != torch.float64 and (K == 1 or (dims == 1 and K >= 32))
     monkeypatch.setenv("CRG_PLAN_BATCH", "all")  # every item the persistent launch can run
     plan = ApplyPlan(items, normalize=normalize)
     monkeypatch.delenv("CRG_PLAN_BATCH")

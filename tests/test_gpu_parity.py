@@ -529,3 +529,48 @@ def test_low_precision_apply_cut_and_empty_rows(cuda, dtype, K, case):
         assert np.isfinite(err) and err <= tol * ref.abs().max().item(), err
         empty = torch.from_numpy(np.asarray(counts) == 0).cuda()
         assert bool((y[empty] == 0).all())
+
+
+@pytest.mark.parametrize("dtype", ["float32", "bfloat16"])
+@pytest.mark.parametrize("case", ["cut_rows", "empty_rows", "polar_rows"])
+def test_narrow_fields(cuda, dtype, case):
+    """2 to 31 cell-major fields run the narrow merge-path kernel (several
+    entries per warp load, a segmented scan per chunk of a task, rows continued
+    across chunks and cut across tasks), one field the row kernel: against the
+    FP64 apply of the same rounded inputs within the output rounding, both
+    directions, K = 1 (a vector) .. 31, aligned rows or not; rows without
+    entries are zero; applying again gives the same bits.  Matrices: rows cut
+    between tasks (10-degree cells over HEALPix 32), rows without entries, and
+    HEALPix 64 over 0.5-degree cells, whose polar rows hold hundreds of entries."""
+    import torch
+
+    tol = 8e-3 if dtype == "bfloat16" else 2e-6
+    if case == "cut_rows":
+        R = Regridder(grids.lonlat_regular(10.0, 10.0), grids.healpix_grid(32), normalize=True)
+        assert R.info["cut_rows"][0] > 0
+    elif case == "empty_rows":
+        R = Regridder(grids.lonlat_grid(np.arange(0.0, 361.0, 10.0), np.arange(-90.0, 91.0, 10.0)),
+                      grids.lonlat_grid(np.arange(0.0, 181.0, 6.0), np.arange(-30.0, 31.0, 6.0)), normalize=True)
+        assert R.info["empty_rows"][0] > 0
+    else:
+        R = Regridder(grids.healpix_grid(64), grids.lonlat_regular(0.5, 0.5), normalize=True)
+        assert R.intersections.getnnz(axis=1).max() > 200
+    A = R.intersections
+    dt = getattr(torch, dtype)
+    for K in (1, 2, 3, 4, 5, 7, 8, 12, 16, 17, 24, 31):
+        gen = torch.Generator(device="cuda").manual_seed(100 + K)
+        for RR, counts in ((R, A.getnnz(axis=1)), (R.transpose(), A.getnnz(axis=0))):
+            n_out, n_in = RR.shape
+            shp_in, shp_out = ((n_in,), (n_out,)) if K == 1 else ((n_in, K), (n_out, K))
+            x = torch.randn(shp_in, generator=gen, device="cuda").to(dt)
+            y = torch.full(shp_out, float("nan"), device="cuda").to(dt)
+            regrid_(y, RR, x, dims=1)
+            ref = torch.empty(shp_out, dtype=torch.float64, device="cuda")
+            regrid_(ref, RR, x.double(), dims=1)
+            err = (y.double() - ref).abs().max().item()
+            assert np.isfinite(err) and err <= tol * ref.abs().max().item(), (K, err)
+            empty = torch.from_numpy(np.asarray(counts) == 0).cuda()
+            assert bool((y[empty] == 0).all())
+            y2 = torch.empty_like(y)
+            regrid_(y2, RR, x, dims=1)
+            assert torch.equal(y, y2), K
