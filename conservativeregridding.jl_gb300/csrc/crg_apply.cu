@@ -180,6 +180,58 @@ __global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__
   }
 }
 
+// Two to four cell-major FP64 fields (nf <= NF): one thread per row, all its fields,
+// the row's entries U at a time (their loads issued before the ordered sums),
+// each field summed in entry order from 0.0 and its quotient by the row area
+// formed as k_cm_rows_f64 forms it.  With a lane per row the FP64 warp
+// instructions carry 32 rows' operations; k_cm_rows_f64 at one lane per row
+// walked a row's entries one load after another.
+template <int NF, int U>
+__global__ void __launch_bounds__(128) k_spmv_f64_k(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                                    const double* __restrict__ val, int64_t nrows,
+                                                    const double* __restrict__ x, int64_t xs, double* __restrict__ y,
+                                                    int64_t ys, int nf, const double* __restrict__ row_div,
+                                                    const double* __restrict__ row_rcp) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  double acc[NF];
+#pragma unroll
+  for (int q = 0; q < NF; ++q) acc[q] = 0.0;
+  int32_t k = __ldg(ptr + r);
+  const int32_t k1 = __ldg(ptr + r + 1);
+  for (; k + U <= k1; k += U) {
+    double v[U], xv[U][NF];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      v[u] = __ldg(val + k + u);
+      const double* xp = x + (int64_t)__ldg(idx + k + u) * xs;
+#pragma unroll
+      for (int q = 0; q < NF; ++q) xv[u][q] = q < nf ? __ldg(xp + q) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int q = 0; q < NF; ++q) acc[q] = acc[q] + v[u] * xv[u][q];
+  }
+  for (; k < k1; ++k) {
+    const double vk = __ldg(val + k);
+    const double* xp = x + (int64_t)__ldg(idx + k) * xs;
+#pragma unroll
+    for (int q = 0; q < NF; ++q) acc[q] = acc[q] + vk * (q < nf ? __ldg(xp + q) : 0.0);
+  }
+  double* yp = y + r * ys;
+  if (row_div) {
+    const double div = __ldg(row_div + r), rcp = __ldg(row_rcp + r);
+#pragma unroll
+    for (int q = 0; q < NF; ++q)
+      if (q < nf) yp[q] = div_rn_by(acc[q], div, rcp);
+  } else {
+#pragma unroll
+    for (int q = 0; q < NF; ++q)
+      if (q < nf) yp[q] = acc[q];
+  }
+}
+
 // x'[c, f] = x[c, f] / col_div[c] for the adjoint's input (cell-major).
 __global__ void k_div_cols_f64(const double* __restrict__ x, int64_t xs, int64_t ncells, int64_t nf,
                                const double* __restrict__ col_div, double* __restrict__ out) {
@@ -1218,6 +1270,15 @@ void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const doubl
   }
   const double* rdiv = adjoint ? nullptr : div;
   const double* rinv = adjoint ? nullptr : div_inv;
+  if (nf <= 4) {
+    // (at 8 fields this measured 0.91 against 0.79 ms per step for k_cm_rows_f64)
+    const unsigned b = nblk(n, 128);
+    if (nf <= 2) k_spmv_f64_k<2, 4><<<b, 128, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, (int)nf, rdiv, rinv);
+    else k_spmv_f64_k<4, 4><<<b, 128, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, (int)nf, rdiv, rinv);
+    CRG_CHECK_CUDA(cudaGetLastError());
+    if (tmp) CRG_CHECK_CUDA(cudaFreeAsync(tmp, st));
+    return;
+  }
   const bool vec = nf % 4 == 0 && xin_s % 2 == 0 && ys % 2 == 0 && (uintptr_t)xin % 16 == 0 && (uintptr_t)y % 16 == 0;
   const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
   int G = 1;
