@@ -12,13 +12,20 @@
 //                   column order from 0.0 -- the same sequence as the
 //                   reference's column-scatter mul! for each row -- then the
 //                   optional division by the row area.
+//   k_spmv_f64_k    FP64, 2-4 cell-major fields: the same per field, a thread
+//                   per row with all its fields.
+//   k_cm_rows_f64   FP64, more cell-major fields: G lanes per row, 4 fields
+//                   per lane, the same per field.
 //   k_cm_nnz        FP32/BF16 fields stored cell-major (the fields of one cell
 //                   side by side), >= 32 of them: merge-path over ~64-entry
-//                   tasks, a warp per task, 4 fields per lane, 8 gathers of a
+//                   tasks, a warp per task, 4 fields per lane, B gathers of a
 //                   source cell's field vector in flight (+ k_cm_fixup for
 //                   rows cut between tasks, k_zero_empty_cm for empty rows).
-//   k_cm_rows       cell-major, fewer fields: G lanes per row, RB rows per
-//                   lane group, 4 fields per lane.
+//   k_cm_narrow     cell-major, 2-31 fields: the same tasks, 32 / G entries
+//                   per warp load (G lanes of 4 fields each per entry), a
+//                   segmented scan per chunk of entries.
+//   k_cm_rows       cell-major, fewer fields with CRG_SPMM_PATH=rows: G lanes
+//                   per row, RB rows per lane group, 4 fields per lane.
 //   k_fm_rows       field-major (spatial index contiguous per field): a row
 //                   per lane; with >= 32 fields the first apply of a direction
 //                   may choose k_transpose + the cell-major path instead.
