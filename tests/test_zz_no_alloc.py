@@ -37,9 +37,9 @@ def test_noalloc_matches_apply_on_consecutive_calls(cuda):
     R = Regridder(grids.lonlat_regular(10.0, 10.0), grids.healpix_grid(32), normalize=True)
     assert R.info["carry_slots"][0] > 0
     nd, ns = R.shape
-    K = 64
     gen = torch.Generator(device="cuda").manual_seed(5)
-    for transpose, nin, nout in ((0, ns, nd), (1, nd, ns)):
+    # 64 fields: the merge-path kernel; 8: the narrow one (both through the scratch)
+    for K, transpose, nin, nout in ((64, 0, ns, nd), (64, 1, nd, ns), (8, 0, ns, nd), (8, 1, nd, ns)):
         for _ in range(2):  # two calls in a row share the static scratch
             x = torch.randn((nin, K), generator=gen, device="cuda")
             ref = torch.empty((nout, K), device="cuda")
