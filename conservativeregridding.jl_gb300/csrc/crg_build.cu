@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "crg_div.cuh"
 #include "crg_geom.cuh"
 #include "crg_internal.cuh"
 #include "crg_scan.cuh"
@@ -959,22 +960,31 @@ __global__ void k_max_val(const double* __restrict__ v, int64_t n, unsigned long
 
 // normalize!: both CSR copies of A and both area vectors divided by max(A),
 // one launch over the four arrays back to back.
+// Each thread takes kDivPer elements (grid-stride) and the IEEE reciprocal of
+// max(A) once: the quotients come from Markstein's correction, checked, with
+// the IEEE division where the check fails (crg_div.cuh) -- the bits of v / m.
+constexpr int kDivPer = 8;
 __global__ void k_div_by(double* __restrict__ a, double* __restrict__ b, int64_t nnz, double* __restrict__ c,
                          int64_t nc, double* __restrict__ d, int64_t nd, const unsigned long long* __restrict__ mx) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double* v;
-  if (i < nnz) {
-    v = a;
-  } else if ((i -= nnz) < nnz) {
-    v = b;
-  } else if ((i -= nnz) < nc) {
-    v = c;
-  } else if ((i -= nc) < nd) {
-    v = d;
-  } else {
-    return;
+  const double m = __longlong_as_double((long long)*mx);
+  const double rcp = 1.0 / m;
+  const int64_t total = 2 * nnz + nc + nd;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < total; j += stride) {
+    int64_t i = j;
+    double* v;
+    if (i < nnz) {
+      v = a;
+    } else if ((i -= nnz) < nnz) {
+      v = b;
+    } else if ((i -= nnz) < nc) {
+      v = c;
+    } else {
+      i -= nc;
+      v = d;
+    }
+    v[i] = div_rn_by(v[i], m, rcp);
   }
-  v[i] = v[i] / __longlong_as_double((long long)*mx);
 }
 
 // FP32 copies of the entries and of the normalised / adjoint weights, one
@@ -1715,8 +1725,8 @@ crg_regridder* build_impl(const crg_grid_desc* dst, const crg_grid_desc* src, co
     CRG_CHECK_CUDA(cudaMemcpyAsync(&hmx, mx.p, sizeof(hmx), cudaMemcpyDeviceToHost, st));
     R->normalized = normalize;
     if (normalize && 2 * nnz + nd + ns) {
-      k_div_by<<<nblk(2 * nnz + nd + ns, 256), 256, 0, st>>>(R->fwd.val, R->rev.val, nnz, R->dst_area, nd,
-                                                             R->src_area, ns, mx.p);
+      k_div_by<<<nblk((2 * nnz + nd + ns + kDivPer - 1) / kDivPer, 256), 256, 0, st>>>(
+          R->fwd.val, R->rev.val, nnz, R->dst_area, nd, R->src_area, ns, mx.p);
       CRG_CHECK_CUDA(cudaGetLastError());
     }
     finish_build(R, st);
