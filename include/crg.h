@@ -231,7 +231,8 @@ crg_status crg_area_grad(const crg_regridder* r, const crg_grid_desc* dst, const
  * application whose memory pool owns the whole device (a Julia CUDA.jl or
  * PyTorch caching allocator sized to the GPU, a model that pre-allocates
  * everything at start-up and forbids allocation while it runs).  Same
- * arguments as crg_apply, restricted to the batched cell-major path: device
+ * arguments as crg_apply, restricted to the cell-major merge-path kernels (the
+ * narrow one below 32 fields), whose results it has bit for bit: device
  * pointers only, dtype CRG_F32 or CRG_BF16, src_stride_field = dst_stride_field
  * = 1, nfields and both cell strides multiples of 4, 16-byte aligned (FP32) /
  * 8-byte aligned (BF16) base pointers.  The partial sums of rows cut between
