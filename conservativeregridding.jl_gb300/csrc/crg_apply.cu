@@ -543,10 +543,11 @@ template <> struct CmGather<__nv_bfloat16> {
   static __device__ __forceinline__ Raw load(const char* base, uint32_t off) {
     return __ldg(reinterpret_cast<const uint2*>(base + off));
   }
+  // a BF16 value is the upper half of its FP32 value: one shift (the element
+  // in the low half) and one mask (the element in the high half) per pair
   static __device__ __forceinline__ float4 widen(Raw u) {
-    const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.x));
-    const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&u.y));
-    return make_float4(a.x, a.y, b.x, b.y);
+    return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u),
+                       __uint_as_float(u.y << 16), __uint_as_float(u.y & 0xffff0000u));
   }
 };
 
