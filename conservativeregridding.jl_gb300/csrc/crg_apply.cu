@@ -885,18 +885,19 @@ void launch_cm_nnz(const DevCsr& c, const float* w, const T* x, int64_t xs, T* y
   if (carry) CRG_CHECK_CUDA(cudaFreeAsync(carry, st));
 }
 
-// Merge-path tasks for cell-major fields, 2 to 31 per cell: G lanes
-// (4 fields each) per entry, 32 / G entries of the task at a time, so that a
-// warp gathers 32 / G source rows per load and a polar row of hundreds of
-// entries is spread over its tasks like any other.  Each lane group forms its
-// entry's products; a segmented inclusive scan over the groups (Kogge-Stone,
-// rows from erow) sums every row's run of entries inside the chunk; the group
-// holding a row's last entry of the chunk adds what earlier chunks carried and
-// writes the row -- to its carry slot when the row is cut between tasks
-// (k_cm_fixup sums those).  The chunk's last row stays open until the next
-// chunk shows whether it continues.  Order of the FP32 sums: a fixed scan tree
-// per chunk, the chunks in entry order: the same bits for a given matrix and
-// field count (the scan's width follows the lanes per entry), every time.
+// Merge-path tasks for cell-major fields, 2 to 31 per cell: G lanes (4 fields
+// each) per lane group, every lane group taking two consecutive entries of a
+// chunk of 64 / G, so that a warp gathers 64 / G source rows per two loads and
+// a polar row of hundreds of entries is spread over its tasks like any other.
+// A lane group adds its two entries' products when they share a row; a
+// segmented inclusive scan over the groups (Kogge-Stone, rows from erow) then
+// sums every row's run of entries inside the chunk; the group holding a row's
+// last entry of the chunk adds what earlier chunks carried and writes the row
+// -- to its carry slot when the row is cut between tasks (k_cm_fixup sums
+// those).  The chunk's last row stays open until the next chunk shows whether
+// it continues.  Order of the FP32 sums: pairs, then a fixed scan tree per
+// chunk, the chunks in entry order: the same bits for a given matrix and field
+// count (the chunk's width follows the lanes per entry), every time.
 template <class T, int G, bool kVec>
 __global__ void __launch_bounds__(256, 4)
     k_cm_narrow(const int4* __restrict__ tasks, const int2* __restrict__ tslot, const int32_t* __restrict__ idx,
@@ -937,10 +938,9 @@ __global__ void __launch_bounds__(256, 4)
     };
     int32_t open_row = -1;  // the row the previous chunk ended in, not written yet
     float4 open = make_float4(0.f, 0.f, 0.f, 0.f);
-    // a chunk's entry of this lane group: its row, source cell and weight
-    // (row -1 past the task's end), and the gathered fields
-    auto meta = [&](int32_t c, int32_t& row, int32_t& col, float& wt) {
-      const int32_t e = c + i;
+    // entry e of the task for this lane group: its row (-1 past the task's
+    // end), source cell and weight, and its gathered fields
+    auto meta = [&](int32_t e, int32_t& row, int32_t& col, float& wt) {
       const bool valid = e < e1;
       row = valid ? __ldg(erow + e) : -1;
       col = valid ? __ldg(idx + e) : 0;
@@ -961,88 +961,70 @@ __global__ void __launch_bounds__(256, 4)
       }
       return v;
     };
-    // two chunks ahead: the next chunk's gather and the one after's indices
-    // are in flight while a chunk is summed
-    int32_t row_a, col_a, row_b, col_b;
-    float wt_a, wt_b;
-    meta(e0, row_a, col_a, wt_a);
-    float4 v_a = gather(row_a, col_a);
-    meta(e0 + E, row_b, col_b, wt_b);
-    for (int32_t c0 = e0; c0 < e1; c0 += E) {
-      const float4 v_b = gather(row_b, col_b);
-      int32_t row_c, col_c;
-      float wt_c;
-      meta(c0 + 2 * E, row_c, col_c, wt_c);
-      const int32_t row = row_a;
-      const bool valid = row >= 0;
-      float4 p = make_float4(wt_a * v_a.x, wt_a * v_a.y, wt_a * v_a.z, wt_a * v_a.w);
-      row_a = row_b;
-      col_a = col_b;
-      wt_a = wt_b;
-      v_a = v_b;
-      row_b = row_c;
-      col_b = col_c;
-      wt_b = wt_c;
-      const int32_t row0 = __shfl_sync(kFull, row, 0);
+    auto add = [](float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); };
+    auto mul = [](float wt, float4 v) { return make_float4(wt * v.x, wt * v.y, wt * v.z, wt * v.w); };
+    // Chunks of 2 E entries: lane group i takes entries 2i (a) and 2i + 1 (b).
+    // The next chunk's indices and gathers are in flight while a chunk is summed.
+    int32_t ra, ca, rb, cb;
+    float wa, wb;
+    meta(e0 + 2 * i, ra, ca, wa);
+    meta(e0 + 2 * i + 1, rb, cb, wb);
+    float4 va = gather(ra, ca), vb = gather(rb, cb);
+    for (int32_t c0 = e0; c0 < e1; c0 += 2 * E) {
+      int32_t na, nca, nb, ncb;
+      float nwa, nwb;
+      meta(c0 + 2 * E + 2 * i, na, nca, nwa);
+      meta(c0 + 2 * E + 2 * i + 1, nb, ncb, nwb);
+      const float4 nva = gather(na, nca), nvb = gather(nb, ncb);
+      const float4 pa = mul(wa, va), pb = mul(wb, vb);
+      const int32_t row0 = __shfl_sync(kFull, ra, 0);
       // the open row ended where this chunk begins: write it (group 0)
       if (open_row >= 0 && row0 != open_row) {
         if (i == 0) write(open_row, open);
         open_row = -1;
       }
-      const int32_t prow = __shfl_up_sync(kFull, row, G);
-      // bit i G: entry i starts a run (a row's first entry in the chunk; past
-      // the task's end every entry does)
-      const bool head = i == 0 || row != prow;
-      const unsigned heads = __ballot_sync(kFull, g == 0 && head);
-      if constexpr (G <= 2) {
-        // s: the first entry of entry i's run; a round adds the partial sum of
-        // entry i - d when that entry is in the same run
-        const unsigned upto = lane == 31 ? 0xffffffffu : (2u << lane) - 1u;
-        const int s = (31 - __clz(heads & upto)) / G;
+      // a starts a run: the chunk's first entry, or a row change from the
+      // previous entry (b of group i - 1); the group's last run (the one b is
+      // in) starts inside it when b's row differs from a's, or at a
+      const int32_t prev = __shfl_up_sync(kFull, rb, G);
+      const bool head_a = i == 0 || ra != prev;
+      const bool same = ra == rb;
+      bool h = !same || head_a;
+      float4 t = same ? add(pa, pb) : pb;
+      // segmented inclusive scan of the groups' last runs
 #pragma unroll
-        for (int d = 1; d < E; d <<= 1) {
-          const float qx = __shfl_up_sync(kFull, p.x, d * G), qy = __shfl_up_sync(kFull, p.y, d * G);
-          const float qz = __shfl_up_sync(kFull, p.z, d * G), qw = __shfl_up_sync(kFull, p.w, d * G);
-          if (i - d >= s) {
-            p.x = qx + p.x;
-            p.y = qy + p.y;
-            p.z = qz + p.z;
-            p.w = qw + p.w;
-          }
-        }
-      } else {
-        // the same sums with the run flags shuffled along (fewer rounds: this
-        // measured faster at 4 and 8 lanes per entry)
-        bool h = head;
-#pragma unroll
-        for (int d = 1; d < E; d <<= 1) {
-          const float qx = __shfl_up_sync(kFull, p.x, d * G), qy = __shfl_up_sync(kFull, p.y, d * G);
-          const float qz = __shfl_up_sync(kFull, p.z, d * G), qw = __shfl_up_sync(kFull, p.w, d * G);
-          const bool qh = __shfl_up_sync(kFull, h ? 1 : 0, d * G) != 0;
-          if (i >= d && !h) {
-            p.x = qx + p.x;
-            p.y = qy + p.y;
-            p.z = qz + p.z;
-            p.w = qw + p.w;
-            h = qh;
-          }
+      for (int d = 1; d < E; d <<= 1) {
+        const float qx = __shfl_up_sync(kFull, t.x, d * G), qy = __shfl_up_sync(kFull, t.y, d * G);
+        const float qz = __shfl_up_sync(kFull, t.z, d * G), qw = __shfl_up_sync(kFull, t.w, d * G);
+        const bool qh = __shfl_up_sync(kFull, h ? 1 : 0, d * G) != 0;
+        if (i >= d && !h) {
+          t = make_float4(qx + t.x, qy + t.y, qz + t.z, qw + t.w);
+          h = qh;
         }
       }
-      // the run of entry i now holds its row's sum from the chunk start (or the row's first entry in it)
-      if (row == open_row) {  // continues the open row (implies row == row0)
-        p.x = open.x + p.x;
-        p.y = open.y + p.y;
-        p.z = open.z + p.z;
-        p.w = open.w + p.w;
+      // a's run, when it ends at a: the previous group's scan (same run) + pa
+      const float4 sp = make_float4(__shfl_up_sync(kFull, t.x, G), __shfl_up_sync(kFull, t.y, G),
+                                    __shfl_up_sync(kFull, t.z, G), __shfl_up_sync(kFull, t.w, G));
+      if (ra >= 0 && !same) {
+        float4 ta = head_a ? pa : add(sp, pa);
+        if (ra == open_row) ta = add(open, ta);
+        write(ra, ta);
       }
-      const bool chunk_end = i == E - 1;
-      if (valid && !chunk_end && ((heads >> ((i + 1) * G)) & 1u)) write(row, p);
-      // the chunk's last group: its row stays open (E entries were valid) or the task ends here
-      const int32_t lrow = __shfl_sync(kFull, row, (E - 1) * G + g);
-      const float4 lp = make_float4(__shfl_sync(kFull, p.x, (E - 1) * G + g), __shfl_sync(kFull, p.y, (E - 1) * G + g),
-                                    __shfl_sync(kFull, p.z, (E - 1) * G + g), __shfl_sync(kFull, p.w, (E - 1) * G + g));
-      open_row = lrow;  // -1 when the chunk was not full: its rows are all written
-      open = lp;
+      // b's run so far (with what earlier chunks carried); written when the
+      // next entry starts another row, kept open at the chunk's end
+      if (rb == open_row) t = add(open, t);
+      const int32_t next = __shfl_down_sync(kFull, ra, G);
+      if (rb >= 0 && i < E - 1 && next != rb) write(rb, t);
+      const int last = (E - 1) * G + g;
+      open_row = __shfl_sync(kFull, rb, last);  // -1 when the chunk was not full: all its rows are written
+      open = make_float4(__shfl_sync(kFull, t.x, last), __shfl_sync(kFull, t.y, last),
+                         __shfl_sync(kFull, t.z, last), __shfl_sync(kFull, t.w, last));
+      ra = na;
+      rb = nb;
+      wa = nwa;
+      wb = nwb;
+      va = nva;
+      vb = nvb;
     }
     if (open_row >= 0 && i == 0) write(open_row, open);
   }
