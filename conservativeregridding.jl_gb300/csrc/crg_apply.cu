@@ -21,9 +21,9 @@
 //                   tasks, a warp per task, 4 fields per lane, B gathers of a
 //                   source cell's field vector in flight (+ k_cm_fixup for
 //                   rows cut between tasks, k_zero_empty_cm for empty rows).
-//   k_cm_narrow     cell-major, 2-31 fields: the same tasks, 32 / G entries
-//                   per warp load (G lanes of 4 fields each per entry), a
-//                   segmented scan per chunk of entries.
+//   k_cm_narrow     cell-major, 2-31 fields: the same tasks in chunks of
+//                   64 / G entries (G lanes of 4 fields each per lane group,
+//                   two entries per group), a segmented scan per chunk.
 //   k_cm_rows       cell-major, fewer fields with CRG_SPMM_PATH=rows: G lanes
 //                   per row, RB rows per lane group, 4 fields per lane.
 //   k_fm_rows       field-major (spatial index contiguous per field): a row
