@@ -15,7 +15,8 @@
 //   k_spmv_f64_k    FP64, 2-4 cell-major fields: the same per field, a thread
 //                   per row with all its fields.
 //   k_cm_rows_f64   FP64, more cell-major fields: G lanes per row, 4 fields
-//                   per lane, the same per field.
+//                   per lane, the same per field; up to 32 fields the
+//                   autotuner also times batches of 4 or 8 entries per group.
 //   k_cm_nnz        FP32/BF16 fields stored cell-major (the fields of one cell
 //                   side by side), >= 32 of them: merge-path over ~64-entry
 //                   tasks, a warp per task, 4 fields per lane, B gathers of a
@@ -125,14 +126,15 @@ __global__ void k_spmv_f64(const int32_t* __restrict__ ptr, const int32_t* __res
 
 // FP64 fields side by side (cell-major), many of them: G lanes per row, 4
 // fields per lane (two 16-byte loads when aligned), the row's (column,
-// weight) entries loaded G at a time and broadcast by shuffles.  Each field
+// weight) entries loaded G at a time (KB = 0) or in batches of KB and
+// broadcast by shuffles.  Each field
 // is summed exactly as k_spmv_f64 sums it -- acc = 0, then acc + (w x) per
 // entry in ascending column order, each operation rounded once -- and divided
 // by the row area, so every field has the bits of the one-field apply (and of
 // the reference's mul! then ./ areas).  The division by column areas of the
 // adjoint is applied to the input beforehand (k_div_cols_f64), the same
 // quotient k_spmv_f64 forms per entry.
-template <int G, bool kVec>
+template <int G, bool kVec, int KB>
 __global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
                                                      const double* __restrict__ val, int64_t nrows,
                                                      const double* __restrict__ x, int64_t xs, double* __restrict__ y,
@@ -152,28 +154,88 @@ __global__ void __launch_bounds__(256) k_cm_rows_f64(const int32_t* __restrict__
     const bool on = f < nf;
     const bool full = kVec && f + 4 <= nf;
     double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (int kb = 0; kb < n; kb += G) {
-      const bool in = kb + g < n;
-      const int32_t myj = in ? __ldg(idx + k0 + kb + g) : 0;
-      const double myv = in ? __ldg(val + k0 + kb + g) : 0.0;
-      const int ne = min(G, n - kb);
-#pragma unroll 4
-      for (int e = 0; e < ne; ++e) {
-        const int64_t j = __shfl_sync(gmask, myj, gbase + e);
-        const double wv = __shfl_sync(gmask, myv, gbase + e);
-        if (!on) continue;
-        const double* xp = x + j * xs + f;
-        double xv[4];
-        if (full) {
-          const double2 a = __ldg(reinterpret_cast<const double2*>(xp));
-          const double2 b = __ldg(reinterpret_cast<const double2*>(xp) + 1);
-          xv[0] = a.x; xv[1] = a.y; xv[2] = b.x; xv[3] = b.y;
-        } else {
+    if constexpr (KB > 0) {
+      // Batches of KB entries (the autotuner's candidates up to 32 fields),
+      // entry kb + u G + e held by lane e of the group.  The next batch's
+      // (column, weight) pairs load while this batch's gathers are in flight,
+      // and the sums follow in entry order: a polar row of hundreds of entries
+      // costs one gather latency per KB entries instead of an index and a
+      // gather latency per G.
+      static_assert(KB % G == 0, "a batch is a whole number of entries per lane");
+      constexpr int kB = KB, U = kB / G;
+      int32_t bj[U];
+      double bw[U];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) xv[q] = f + q < nf ? __ldg(xp + q) : 0.0;
+      for (int u = 0; u < U; ++u) {
+        const int e = u * G + g;
+        bj[u] = e < n ? __ldg(idx + k0 + e) : 0;
+        bw[u] = e < n ? __ldg(val + k0 + e) : 0.0;
+      }
+      for (int kb = 0; kb < n; kb += kB) {
+        int32_t nj[U];
+        double nw[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int e = kb + kB + u * G + g;
+          nj[u] = e < n ? __ldg(idx + k0 + e) : 0;
+          nw[u] = e < n ? __ldg(val + k0 + e) : 0.0;
         }
+        double xv[kB][4], wv[kB];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[q] = __dadd_rn(acc[q], __dmul_rn(wv, xv[q]));
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int e = 0; e < G; ++e) {
+            const int m = u * G + e;
+            const int64_t j = __shfl_sync(gmask, bj[u], gbase + e);
+            wv[m] = __shfl_sync(gmask, bw[u], gbase + e);
+            const bool ok = on && kb + m < n;
+            const double* xp = x + j * xs + f;
+            if (ok && full) {
+              const double2 a = __ldg(reinterpret_cast<const double2*>(xp));
+              const double2 b = __ldg(reinterpret_cast<const double2*>(xp) + 1);
+              xv[m][0] = a.x; xv[m][1] = a.y; xv[m][2] = b.x; xv[m][3] = b.y;
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) xv[m][q] = (ok && f + q < nf) ? __ldg(xp + q) : 0.0;
+            }
+          }
+#pragma unroll
+        for (int m = 0; m < kB; ++m)
+          if (kb + m < n) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[q] = __dadd_rn(acc[q], __dmul_rn(wv[m], xv[m][q]));
+          }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          bj[u] = nj[u];
+          bw[u] = nw[u];
+        }
+      }
+    } else {
+      // the group's lanes load G entries at a time
+      for (int kb = 0; kb < n; kb += G) {
+        const bool in = kb + g < n;
+        const int32_t myj = in ? __ldg(idx + k0 + kb + g) : 0;
+        const double myv = in ? __ldg(val + k0 + kb + g) : 0.0;
+        const int ne = min(G, n - kb);
+#pragma unroll 4
+        for (int e = 0; e < ne; ++e) {
+          const int64_t j = __shfl_sync(gmask, myj, gbase + e);
+          const double wv = __shfl_sync(gmask, myv, gbase + e);
+          if (!on) continue;
+          const double* xp = x + j * xs + f;
+          double xv[4];
+          if (full) {
+            const double2 a = __ldg(reinterpret_cast<const double2*>(xp));
+            const double2 b = __ldg(reinterpret_cast<const double2*>(xp) + 1);
+            xv[0] = a.x; xv[1] = a.y; xv[2] = b.x; xv[3] = b.y;
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) xv[q] = f + q < nf ? __ldg(xp + q) : 0.0;
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[q] = __dadd_rn(acc[q], __dmul_rn(wv, xv[q]));
+        }
       }
     }
     if (!on) continue;
@@ -1261,6 +1323,37 @@ void launch_transpose(const T* in, int64_t ldi, T* out, int64_t ldo, int64_t row
   CRG_CHECK_CUDA(cudaGetLastError());
 }
 
+// One launch of k_cm_rows_f64: G lanes per row, batches of KB entries (0: G
+// at a time).
+template <int G, int KB>
+void cm_f64_rows(const DevCsr& c, bool vec, const double* x, int64_t xs, double* y, int64_t ys, int64_t nf,
+                 const double* rdiv, const double* rinv, cudaStream_t st) {
+  const unsigned blocks = nblk(c.nrows * G, 256);
+  if (vec)
+    k_cm_rows_f64<G, true, KB><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, c.nrows, x, xs, y, ys, nf, rdiv, rinv);
+  else
+    k_cm_rows_f64<G, false, KB><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, c.nrows, x, xs, y, ys, nf, rdiv, rinv);
+  CRG_CHECK_CUDA(cudaGetLastError());
+}
+
+// The autotuner's candidates for k_cm_rows_f64 with G lanes per row (index 0
+// is the default): 0 loads G entries at a time; 1 batches of 8 entries (2 to
+// 8 lanes per row); 2 batches of 4 (2 or 4 lanes per row).  Every candidate
+// sums each field in entry order, so the choice never changes a result.
+int cm_f64_variants(int G) { return G >= 2 && G <= 4 ? 3 : (G == 8 ? 2 : 1); }
+
+template <int G>
+void cm_f64_variant(int v, const DevCsr& c, bool vec, const double* x, int64_t xs, double* y, int64_t ys,
+                    int64_t nf, const double* rdiv, const double* rinv, cudaStream_t st) {
+  if constexpr (G >= 2 && G <= 8) {
+    if (v == 1) return cm_f64_rows<G, 8>(c, vec, x, xs, y, ys, nf, rdiv, rinv, st);
+  }
+  if constexpr (G >= 2 && G <= 4) {
+    if (v == 2) return cm_f64_rows<G, 4>(c, vec, x, xs, y, ys, nf, rdiv, rinv, st);
+  }
+  cm_f64_rows<G, 0>(c, vec, x, xs, y, ys, nf, rdiv, rinv, st);
+}
+
 // Cell-major FP64 fields (more than one): k_cm_rows_f64, G lanes per row.
 // With the adjoint's column division, the input is divided once per element
 // into a temporary first.
@@ -1295,24 +1388,17 @@ void launch_cm_f64(const DevCsr& c, bool adjoint, const double* div, const doubl
   const int64_t lanes = (std::min<int64_t>(nf, 128) + 3) / 4;
   int G = 1;
   while (G < lanes) G <<= 1;
-  const unsigned blocks = nblk(n * G, 256);
-#define CRG_F64_CASE(GG)                                                                                        \
-  case GG:                                                                                                      \
-    if (vec)                                                                                                    \
-      k_cm_rows_f64<GG, true><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv, rinv); \
-    else                                                                                                        \
-      k_cm_rows_f64<GG, false><<<blocks, 256, 0, st>>>(c.ptr, c.idx, c.val, n, xin, xin_s, y, ys, nf, rdiv, rinv); \
-    break;
-  switch (G) {
-    CRG_F64_CASE(1)
-    CRG_F64_CASE(2)
-    CRG_F64_CASE(4)
-    CRG_F64_CASE(8)
-    CRG_F64_CASE(16)
-    CRG_F64_CASE(32)
-  }
-#undef CRG_F64_CASE
-  CRG_CHECK_CUDA(cudaGetLastError());
+  auto run = [&](int v) {
+    switch (G) {
+      case 1: cm_f64_variant<1>(v, c, vec, xin, xin_s, y, ys, nf, rdiv, rinv, st); break;
+      case 2: cm_f64_variant<2>(v, c, vec, xin, xin_s, y, ys, nf, rdiv, rinv, st); break;
+      case 4: cm_f64_variant<4>(v, c, vec, xin, xin_s, y, ys, nf, rdiv, rinv, st); break;
+      case 8: cm_f64_variant<8>(v, c, vec, xin, xin_s, y, ys, nf, rdiv, rinv, st); break;
+      case 16: cm_f64_variant<16>(v, c, vec, xin, xin_s, y, ys, nf, rdiv, rinv, st); break;
+      default: cm_f64_variant<32>(v, c, vec, xin, xin_s, y, ys, nf, rdiv, rinv, st); break;
+    }
+  };
+  run(tune_choose(matrix_key(vec ? "cm_f64" : "cm_f64_strided", c, "f64", nf), cm_f64_variants(G), st, run));
   if (tmp) CRG_CHECK_CUDA(cudaFreeAsync(tmp, st));
 }
 

@@ -1,8 +1,9 @@
 """The autotuner: on the first apply of a (device, matrix copy, field type,
 field count) it times its candidates -- gathers in flight and blocks per SM of
-the merge-path kernel, rows per lane group of the row kernel -- keeps the
-fastest, and appends the choice to its cache file; a later process reads the
-file and makes the same choice without timing.  Every candidate sums the same
+the merge-path kernel, rows per lane group of the row kernel, entries per
+batch of the FP64 row kernel -- keeps the fastest, and appends the choice to
+its cache file; a later process reads the file and makes the same choice
+without timing.  Every candidate sums the same
 entries in the same order, so results do not depend on the choice, nor on the
 tuner being on.  Each case runs in a fresh process with its own cache file
 (CRG_AUTOTUNE_CACHE) and the choices logged to stderr (CRG_AUTOTUNE_LOG)."""
@@ -91,3 +92,48 @@ def test_autotune_row_kernel_family(cuda, tmp_path):
     assert sum(" cm_rows " in l for l in measured) == 4 and len(cache.read_text().splitlines()) == 4, log1
     off, _ = _run(tmp_path, "rows0", CRG_AUTOTUNE="0", CRG_SPMM_PATH="rows")
     assert np.array_equal(first, off)
+
+
+SCRIPT_F64 = r"""
+import sys
+import numpy as np
+import torch
+sys.path.insert(0, sys.argv[1])
+from crg import Regridder, grids, regrid_
+R = Regridder(grids.healpix_grid(32), grids.lonlat_regular(2.0, 2.0), normalize=True)
+out = []
+g = torch.Generator(device="cuda").manual_seed(3)
+for K in (8, 16, 24, 6):  # 2, 4 and 8 lanes per row; 6 fields: no 16-byte vectors
+    for RR in (R, R.transpose()):
+        x = torch.randn((RR.shape[1], K), generator=g, device="cuda", dtype=torch.float64)
+        y = torch.empty((RR.shape[0], K), device="cuda", dtype=torch.float64)
+        regrid_(y, RR, x, dims=1)
+        out.append(y.cpu().numpy().ravel())
+np.save(sys.argv[2], np.concatenate(out))
+"""
+
+
+def test_autotune_fp64_row_candidates_same_bits(cuda, tmp_path):
+    """The FP64 row kernel's candidates (entries loaded G at a time, or in
+    batches of 8 or 4 with the next batch's indices in flight), each forced
+    through the cache file, give the bits of the tuned run."""
+    e = {k: v for k, v in os.environ.items() if k != "CRG_SPMM_PATH"}
+    e.update(CRG_AUTOTUNE_LOG="1")
+
+    def run(name, cache):
+        out = tmp_path / f"{name}.npy"
+        r = subprocess.run([sys.executable, "-c", SCRIPT_F64, str(ROOT / "conservativeregridding.jl_gb300"), str(out)],
+                           env=dict(e, CRG_AUTOTUNE_CACHE=str(cache)), capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+        return np.load(out), [l for l in r.stderr.splitlines() if l.startswith("crg autotune:")]
+
+    tuned, log = run("tuned", tmp_path / "tuned.tsv")
+    keys = [l[len("crg autotune: "):].rsplit(" -> ", 1)[0] for l in log if " cm_f64" in l and "measured" in l]
+    # 8, 16, 24 fields (vectors) and 6 (strided), each direction
+    assert sum(k.startswith("cm_f64 ") for k in keys) == 6 and sum(k.startswith("cm_f64_strided ") for k in keys) == 2, log
+    for v in range(3):
+        cache = tmp_path / f"forced{v}.tsv"
+        cache.write_text("".join(f"{k}\t{v}\t0\n" for k in keys))
+        forced, flog = run(f"forced{v}", cache)
+        assert sum(l.endswith(f"-> {v} (cached)") for l in flog) >= 2, flog
+        assert np.array_equal(forced, tuned), v

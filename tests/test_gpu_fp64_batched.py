@@ -6,8 +6,9 @@ reference's regrid! -- one stdlib CSC mul! per slice, then ./ a_d
 (src/regridder/regrid.jl:95-118, the N-D loop :303-318) -- as the oracle
 computes it, and of the one-field GPU apply.  Field counts below, at and above
 the 128 a lane group covers, aligned and not; R and transpose(R); with and
-without normalisation; the adjoint against one-field adjoints; and the 128
-fields of the large configuration (HEALPix 256 <-> 0.25 degree).
+without normalisation; the adjoint against one-field adjoints; and 8, 24 and
+128 fields of the large configuration (HEALPix 256 <-> 0.25 degree), whose
+polar rows hold hundreds of entries.
 """
 from __future__ import annotations
 
@@ -38,7 +39,7 @@ def _cm(R, X, transpose, normalize):
     return y.T.cpu().numpy()
 
 
-@pytest.mark.parametrize("K", [2, 7, 64, 128, 130, 300])
+@pytest.mark.parametrize("K", [2, 7, 8, 16, 24, 32, 64, 128, 130, 300])
 @pytest.mark.parametrize("transpose", [False, True])
 @pytest.mark.parametrize("normalize", [True, False])
 def test_cell_major_fp64_bit_exact(c1, K, transpose, normalize):
@@ -65,18 +66,25 @@ def test_cell_major_fp64_adjoint_matches_one_field(c1, K):
         assert torch.equal(out[:, k], one), k
 
 
-def test_large_128_fields_fp64(cuda):
+@pytest.fixture(scope="module")
+def large(cuda):
+    hp, ll = workloads.large()
+    return hp, ll, Regridder(hp, ll, normalize=True), oracle.OracleRegridder(hp, ll, normalize=True)
+
+
+@pytest.mark.parametrize("K", [8, 24, 128])
+def test_large_fields_fp64(large, K):
+    """The large configuration's polar rows (hundreds of entries) at 8 and 24
+    fields, which run the batched-entry candidates of the row kernel, and at
+    128."""
     import torch
 
-    hp, ll = workloads.large()
-    R = Regridder(hp, ll, normalize=True)
-    O = oracle.OracleRegridder(hp, ll, normalize=True)
-    K = 128
+    hp, ll, R, O = large
     dev = torch.device("cuda", 0)
     for transpose, g in ((False, ll), (True, hp)):
         x = workloads.harmonic_fields(workloads.cell_centres(g), K, 16, 3 + transpose, 0.1, dev).double()
         y = torch.empty((R.shape[1] if transpose else R.shape[0], K), dtype=torch.float64, device=dev)
         regrid_(y, R.transpose() if transpose else R, x.T.contiguous(), dims=1)
-        pick = np.arange(0, K, 16)
+        pick = np.arange(0, K, max(1, K // 8))
         ref = O.apply(x[pick].cpu().numpy(), transpose=transpose)
         assert np.array_equal(y[:, pick].T.cpu().numpy(), ref)
