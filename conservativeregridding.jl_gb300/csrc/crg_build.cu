@@ -1341,6 +1341,11 @@ void dual_traverse(const HostTree& D, const HostTree& S, bool sph, DBuf<int2>& c
     std::swap(front.n, next.n);
   }
   if (nleaf == 0) return;
+  // A leaf pair yields at most kLeaf^2 candidates, so below 2^32 / kLeaf^2 leaf
+  // pairs the int32 scan of their counts cannot pass 2^32, and a total of 2^31
+  // or more shows as negative (checked after the scan).
+  CRG_REQUIRE(nleaf < ((int64_t)1 << 32) / (kLeaf * kLeaf), CRG_ERR_NOT_SUPPORTED,
+              "%lld leaf pairs: the candidate count could overflow int32", (long long)nleaf);
   DBuf<int32_t> cnt((size_t)nleaf + 1, st);
   if (sph)
     k_leaf_count<true><<<nblk(nleaf, 128), 128, 0, st>>>(leafp.p, nleaf, D.t.sbound, D.t.ncells, S.t.sbound, S.t.ncells, cnt.p);

@@ -904,6 +904,12 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
       ps.search(fv_area, elem_area.p, st);
     const int64_t nc = ps.nc;
     R->ncand = ps.nc_search;
+    // A pair yields at most CRG_MAXC fan triangles and nq^2 <= 64 nonzeros, so
+    // below 2^26 pairs the int32 scans of those counts cannot pass 2^32, and a
+    // total of 2^31 or more shows as negative (checked after each scan).
+    static_assert(CRG_MAXC <= kSeMaxNq * kSeMaxNq, "the pair bound covers the triangle count");
+    CRG_REQUIRE(nc < ((int64_t)1 << 26), CRG_ERR_NOT_SUPPORTED,
+                "%lld overlapping pairs: the per-pair counts could overflow int32", (long long)nc);
     DBuf<double> coef;
     element_coeffs(se_is_dst ? ps.dtab : ps.stab, coef, st);
     DBuf<double> wj((size_t)nn + 1, st);
@@ -932,6 +938,7 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
       CRG_REQUIRE(hovf == 0, CRG_ERR_GEOMETRY,
                   "%llu candidate pairs exceeded the clipped-polygon capacity of %d vertices (non-convex cells?)",
                   (unsigned long long)hovf, CRG_MAXC);
+      CRG_REQUIRE(nitems >= 0, CRG_ERR_NOT_SUPPORTED, "the triangle count overflows int32");
       DBuf<int2> items((size_t)nitems + 1, st);
       DBuf<double> tb((size_t)nitems * nq2 + 1, st);
       k_se_items<<<nblk(nc, 128), 128, 0, st>>>(nvert.p, tarea.p, toff.p, nc, items.p);
@@ -995,6 +1002,7 @@ crg_regridder* build_se_impl(const crg_grid_desc* fv, const crg_se_space* se, co
     int32_t m = 0;
     CRG_CHECK_CUDA(cudaMemcpyAsync(&m, poff.p + cg.n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     CRG_CHECK_CUDA(cudaStreamSynchronize(st));
+    CRG_REQUIRE(m >= 0, CRG_ERR_NOT_SUPPORTED, "the nonzero count overflows int32");
     DevCsr& crows = se_is_dst ? R->rev : R->fwd;  // rows = FV cells
     DevCsr& nrows = se_is_dst ? R->fwd : R->rev;  // rows = nodes
     crows.nrows = nfv; crows.ncols = nn;

@@ -102,7 +102,10 @@ typedef struct crg_info {
  * SparseArrays.sparse assembly (src/regridder/intersection_areas.jl:115-121),
  * per-cell areas (src/regridder/regridder.jl:165-178) and normalize!.
  * Mixed planar/spherical inputs are rejected: promote on the host, as the
- * reference's Regridder(dst, src) does (src/regridder/regridder.jl:109-117). */
+ * reference's Regridder(dst, src) does (src/regridder/regridder.jl:109-117).
+ * Indices are 32-bit: a grid of 2^31 cells or more, a search of 2^31 candidate
+ * pairs or more (or of 2^26 leaf pairs of 8-cell blocks, whose count could
+ * pass 2^32) is refused with CRG_ERR_NOT_SUPPORTED. */
 crg_status crg_build(const crg_grid_desc* dst, const crg_grid_desc* src, const crg_build_opts* opts,
                      crg_regridder** out);
 
@@ -344,7 +347,9 @@ typedef struct crg_se_opts {
  * dst_areas = the FV cell areas, src_areas = the node weights; not normalised.
  * regrid! then gives d = (A s) ./ a_d; constants are preserved exactly up to
  * rounding.  Errors: CRG_ERR_INVALID_ARGUMENT for a non-spherical grid, an
- * element without 4 vertices, nq outside 2..8 or a rule degree above 8. */
+ * element without 4 vertices, nq outside 2..8 or a rule degree above 8;
+ * CRG_ERR_NOT_SUPPORTED for 2^31 nodes or more and for 2^26 overlapping
+ * (element, cell) pairs or more (32-bit counts). */
 crg_status crg_build_se_to_fv(const crg_grid_desc* dst, const crg_se_space* src, const crg_se_opts* opts,
                               crg_regridder** out);
 
