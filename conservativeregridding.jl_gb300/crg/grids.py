@@ -163,6 +163,29 @@ def lonlat_regular(dlon: float, dlat: float, lon0: float = 0.0, lat0: float = -9
     return lonlat_grid(lon, lat, full_sphere=True, name=name or f"lonlat_{nx}x{ny}")
 
 
+def rotated_lonlat(dlon: float, dlat: float, north_pole: Sequence[float] = (0.0, 90.0), name: str = "") -> Grid:
+    """Global lon-lat grid with spacing (dlon, dlat) in a frame whose north pole
+    lies at the geographic point ``north_pole`` = (lon, lat) in degrees, like
+    an Oceananigans ``RotatedLatitudeLongitudeGrid`` that covers the sphere.
+    The reference treats it as any Oceananigans grid: its vertex matrix becomes
+    a CellBasedGrid under KnownFullSphereExtentWrapper
+    (ext/ConservativeRegriddingOceananigansExt.jl:242-264).
+
+    The regular grid's unit vectors are turned by R = Rz(lon) Ry(90 - lat),
+    which carries the z axis to the pole.  A rotation maps great circles to
+    great circles, so every cell is a regular cell moved rigidly; the pole rows
+    still meet in one point each and the 360-degree column equals column 0."""
+    g = lonlat_regular(dlon, dlat)
+    sp, cp = sincosd(north_pole[1])
+    sl, cl = sincosd(north_pole[0])
+    ry = np.array([[sp, 0.0, cp], [0.0, 1.0, 0.0], [-cp, 0.0, sp]])  # z -> (cos lat, 0, sin lat)
+    rz = np.array([[cl, -sl, 0.0], [sl, cl, 0.0], [0.0, 0.0, 1.0]])
+    pts = g.blocks[0] @ (rz @ ry).T
+    nx, ny = g.block_shapes[0]
+    return Grid("curvilinear", SPHERICAL, blocks=[pts], full_sphere=True,
+                name=name or f"rotated_lonlat_{nx}x{ny}_pole_{north_pole[0]:g}_{north_pole[1]:g}")
+
+
 def lonlat_jittered(nx: int, ny: int, jitter: float, seed: int, name: str = "") -> Grid:
     """Global nx x ny lon-lat grid whose interior vertices move by
     U(-jitter, jitter) cell widths in lon and lat.  Pole rows stay on the

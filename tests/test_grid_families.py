@@ -115,3 +115,22 @@ def test_mirror_fold_refuses_unpaired_fold_rows():
         mirror_fold_(np.zeros(30), 10, 3)
     with pytest.raises(ArgumentError, match="cells along dims"):
         mirror_fold_(np.zeros(31), 8, 4)
+
+
+def test_rotated_lonlat_is_a_rigid_rotation():
+    """grids.rotated_lonlat (an Oceananigans RotatedLatitudeLongitudeGrid
+    covering the sphere): the pole rows meet exactly at the requested pole and
+    its antipode, the seam column repeats column 0, the cells have the regular
+    grid's areas (rotation keeps great-circle cells congruent), they tile the
+    sphere, and the default pole gives the regular grid bit for bit."""
+    g = grids.rotated_lonlat(10.0, 10.0, (70.0, 55.0))
+    pole = grids.unit_sphere_from_geographic(70.0, 55.0)
+    b = g.blocks[0]
+    assert np.all(b[-1] == pole) and np.all(b[0] == -pole)
+    assert np.array_equal(b[:, 0], b[:, -1])
+    assert g.full_sphere and grids.convex_cells(g).all()
+    assert np.array_equal(grids.rotated_lonlat(10.0, 10.0).blocks[0], grids.lonlat_regular(10.0, 10.0).blocks[0])
+    O = oracle.OracleRegridder(grids.healpix_grid(8), g)
+    O0 = oracle.OracleRegridder(grids.healpix_grid(8), grids.lonlat_regular(10.0, 10.0))
+    assert np.allclose(O.src_areas, O0.src_areas, rtol=1e-14, atol=0)
+    assert abs(O.src_areas.sum() - 4 * np.pi) < 1e-12

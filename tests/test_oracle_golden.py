@@ -91,6 +91,8 @@ CASES = {
     "lonlat4_to_cs12": lambda: (grids.cubed_sphere(12), grids.lonlat_regular(4.0, 4.0)),
     "cs8_to_lonlat5": lambda: (grids.lonlat_regular(5.0, 5.0), grids.cubed_sphere(8)),
     "jittered": lambda: (grids.lonlat_jittered(60, 30, 0.2, 3), grids.lonlat_jittered(90, 45, 0.2, 4)),
+    "rotated_lonlat10_pole70_55_to_healpix8": lambda: (grids.healpix_grid(8),
+                                                       grids.rotated_lonlat(10.0, 10.0, (70.0, 55.0))),
 }
 
 
