@@ -6,6 +6,7 @@ the functions below raises, there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import re
 import threading
 
 from . import _build
@@ -142,6 +143,14 @@ _lock = threading.Lock()
 _lib = None
 
 
+def abi_version() -> int:
+    """CRG_ABI_VERSION as include/crg.h defines it."""
+    m = re.search(r"^#define CRG_ABI_VERSION (\d+)", (_build.INCLUDE / "crg.h").read_text(), re.M)
+    if not m:
+        raise RuntimeError("include/crg.h does not define CRG_ABI_VERSION")
+    return int(m.group(1))
+
+
 def load(build_if_missing: bool = True) -> C.CDLL:
     """Load (building first if stale) the CUDA library."""
     global _lib
@@ -156,6 +165,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
                 fn = getattr(lib, name)
                 fn.restype = res
                 fn.argtypes = args
+            want, got = abi_version(), int(lib.crg_abi_version())
+            if got != want:
+                raise RuntimeError(f"{_build.LIB_PATH} implements C ABI version {got}, include/crg.h declares {want}: "
+                                   "rebuild the library")
             _lib = lib
         return _lib
 

@@ -28,6 +28,23 @@ def test_binding_covers_only_declared_symbols():
     assert set(_lib.SIGNATURES) == set(declared_symbols())
 
 
+def test_loader_checks_the_abi_version(monkeypatch):
+    """load() compares the library's crg_abi_version() with CRG_ABI_VERSION of
+    include/crg.h and refuses a library built for another version."""
+    lib = _lib.load()
+    assert _lib.abi_version() == lib.crg_abi_version() == 2
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "abi_version", lambda: 3)
+    try:
+        _lib.load(build_if_missing=False)
+    except RuntimeError as e:
+        assert "ABI version 2" in str(e) and "declares 3" in str(e)
+    else:
+        raise AssertionError("a library of another ABI version was accepted")
+    monkeypatch.undo()
+    assert _lib.load() is lib
+
+
 def test_cpu_safe_entry_points():
     lib = _lib.load()
     assert lib.crg_abi_version() == 2
